@@ -1,0 +1,203 @@
+"""Generate golden fixtures by running scikit-fem itself (run in a container
+where the scikit-fem source tree is importable; the fixtures travel, the
+reference does not).
+
+    PYTHONPATH=<scikit-fem checkout> python tests/golden/make_golden.py
+
+Each case stores the mesh (p, t), the reference's element_dofs, its
+quadrature (X, W), the coefficient arrays it was given, the assembled CSR
+(indptr, indices, data) and, where the case has one, the load vector b or
+the adjoint oracles.  Sizes are small so the fixtures stay a few hundred KB.
+"""
+
+import os
+import sys
+
+import numpy as np
+
+import skfem
+from skfem import (Basis, BilinearForm, ElementHex1, ElementTetP1,
+                   ElementTetP2, ElementTriP1, ElementTriP2, ElementVector,
+                   Functional, LinearForm, MeshHex, MeshTet, MeshTri)
+from skfem.helpers import dot, grad
+from skfem.models.elasticity import linear_elasticity
+from skfem.models.poisson import laplace, mass, unit_load
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def save(name, **arrs):
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **arrs)
+    print(name, {k: getattr(v, "shape", v) for k, v in arrs.items()})
+
+
+def csr_arrays(K):
+    K = K.tocsr()
+    return dict(indptr=K.indptr, indices=K.indices, data=K.data,
+                shape=np.array(K.shape))
+
+
+@BilinearForm
+def k_laplace_mass(u, v, w):
+    return w.k * dot(grad(u), grad(v)) + u * v
+
+
+@BilinearForm
+def k_laplace(u, v, w):
+    return w.k * dot(grad(u), grad(v))
+
+
+@BilinearForm
+def theta_laplace(u, v, w):
+    return w.theta * dot(grad(u), grad(v))
+
+
+@LinearForm
+def f_load(v, w):
+    return w.f * v
+
+
+def jitter(m, rng, amp):
+    p = m.p.copy()
+    lo, hi = p.min(axis=1, keepdims=True), p.max(axis=1, keepdims=True)
+    inner = np.all((p > lo + 1e-12) & (p < hi - 1e-12), axis=0)
+    return inner
+
+
+def main():
+    rng = np.random.default_rng(20261203)
+
+    # 1. doctest case: MeshTri() default, mass matrix (bilinear_form.py:26-30)
+    m = MeshTri()
+    ib = Basis(m, ElementTriP1())
+    save("tri_default_mass", p=m.p, t=m.t, element_dofs=ib.element_dofs,
+         X=ib.X, W=ib.W, **csr_arrays(mass.assemble(ib)))
+
+    # 2. TriP1 Laplace + unit load on a 16x16 tensor mesh (configs[0] shape)
+    m = MeshTri.init_tensor(np.linspace(0, 1, 17), np.linspace(0, 1, 17))
+    ib = Basis(m, ElementTriP1())
+    save("tri_p1_laplace", p=m.p, t=m.t, element_dofs=ib.element_dofs,
+         X=ib.X, W=ib.W, b=unit_load.assemble(ib), **csr_arrays(laplace.assemble(ib)))
+
+    # 3. TetP1 k*Laplace + mass, 6x6x6 cells, k ~ lognormal(0,1) per element
+    m = MeshTet.init_tensor(*(np.linspace(0, 1, 7),) * 3)
+    ib = Basis(m, ElementTetP1())
+    k = rng.lognormal(0.0, 1.0, m.t.shape[1])
+    K = k_laplace_mass.assemble(ib, k=ib.zero_w() + k[:, None])
+    b = f_load.assemble(ib, f=ib.zero_w() + k[:, None])
+    save("tet_p1_k_laplace_mass", p=m.p, t=m.t, element_dofs=ib.element_dofs,
+         X=ib.X, W=ib.W, k=k, b=b, **csr_arrays(K))
+
+    # 4. vector TetP2 elasticity, 3x3x3 cells jittered +-0.2h, lambda=1, mu=0.5
+    n = 3
+    m = MeshTet.init_tensor(*(np.linspace(0, 1, n + 1),) * 3)
+    p = m.p.copy()
+    inner = jitter(m, rng, 0.2)
+    p[:, inner] += rng.uniform(-0.2 / n, 0.2 / n, size=(3, int(inner.sum())))
+    m = MeshTet(p, m.t)
+    ib = Basis(m, ElementVector(ElementTetP2()), intorder=4)
+    K = linear_elasticity(1.0, 0.5).assemble(ib)
+    save("tet_p2_vec_elasticity", p=m.p, t=m.t, element_dofs=ib.element_dofs,
+         X=ib.X, W=ib.W, **csr_arrays(K))
+
+    # 5. scalar TetP2 Laplace on an unjittered 3x3x3 mesh (exact-zero entries)
+    m = MeshTet.init_tensor(*(np.linspace(0, 1, 4),) * 3)
+    ib = Basis(m, ElementTetP2())
+    save("tet_p2_laplace", p=m.p, t=m.t, element_dofs=ib.element_dofs,
+         X=ib.X, W=ib.W, b=unit_load.assemble(ib), **csr_arrays(laplace.assemble(ib)))
+
+    # 6. TriP2 k*Laplace on a jittered 8x8 unit square, k ~ lognormal(0,0.5)
+    n = 8
+    m = MeshTri.init_tensor(np.linspace(0, 1, n + 1), np.linspace(0, 1, n + 1))
+    p = m.p.copy()
+    inner = jitter(m, rng, 0.2)
+    p[:, inner] += rng.uniform(-0.2 / n, 0.2 / n, size=(2, int(inner.sum())))
+    m = MeshTri(p, m.t)
+    ib = Basis(m, ElementTriP2())
+    k = rng.lognormal(0.0, 0.5, m.t.shape[1])
+    K = k_laplace.assemble(ib, k=ib.zero_w() + k[:, None])
+    save("tri_p2_k_laplace", p=m.p, t=m.t, element_dofs=ib.element_dofs,
+         X=ib.X, W=ib.W, k=k, b=unit_load.assemble(ib), **csr_arrays(K))
+
+    # 7. Hex1 theta*Laplace on the 4^3 cube (configs[3] submesh) + adjoint oracles
+    m = MeshHex.init_tensor(*(np.linspace(0, 1, 5),) * 3)
+    ib = Basis(m, ElementHex1())
+    theta = rng.uniform(0.01, 1.0, m.t.shape[1])
+    wv = rng.standard_normal(ib.N)
+    uv = rng.standard_normal(ib.N)
+    K = theta_laplace.assemble(ib, theta=ib.zero_w() + theta[:, None])
+
+    @Functional
+    def a_wu(w):
+        return dot(grad(w['wh']), grad(w['uh']))
+    dtheta = a_wu.elemental(ib, wh=ib.interpolate(wv), uh=ib.interpolate(uv))
+
+    def J_of(pp):
+        mm = MeshHex(pp, m.t)
+        bb = Basis(mm, ElementHex1())
+        KK = theta_laplace.assemble(bb, theta=bb.zero_w() + theta[:, None])
+        return wv @ (KK @ uv)
+
+    h = 1e-6
+    dX = np.zeros_like(m.p)
+    for a in range(3):
+        for q in range(m.p.shape[1]):
+            pp = m.p.copy()
+            pp[a, q] += h
+            fp = J_of(pp)
+            pp[a, q] -= 2 * h
+            dX[a, q] = (fp - J_of(pp)) / (2 * h)
+    # load-vector VJP: d(w^T b(f, X))/d f_e and /dX for b = f*v
+    bvec = f_load.assemble(ib, f=ib.zero_w() + theta[:, None])
+
+    def L_of(pp):
+        mm = MeshHex(pp, m.t)
+        bb = Basis(mm, ElementHex1())
+        return wv @ f_load.assemble(bb, f=bb.zero_w() + theta[:, None])
+
+    dXb = np.zeros_like(m.p)
+    for a in range(3):
+        for q in range(m.p.shape[1]):
+            pp = m.p.copy()
+            pp[a, q] += h
+            fp = L_of(pp)
+            pp[a, q] -= 2 * h
+            dXb[a, q] = (fp - L_of(pp)) / (2 * h)
+    save("hex1_theta_laplace", p=m.p, t=m.t, element_dofs=ib.element_dofs,
+         X=ib.X, W=ib.W, theta=theta, wv=wv, uv=uv, dtheta=dtheta, dX=dX,
+         b=bvec, dXb=dXb, **csr_arrays(K))
+
+    # 8. Hex1 Laplace on an unjittered 8^3 cube: rounding-noise entries
+    m = MeshHex.init_tensor(*(np.linspace(0, 1, 9),) * 3)
+    ib = Basis(m, ElementHex1())
+    save("hex1_laplace_8", p=m.p, t=m.t, element_dofs=ib.element_dofs,
+         X=ib.X, W=ib.W, b=unit_load.assemble(ib), **csr_arrays(laplace.assemble(ib)))
+
+    # 9. TetP1 Laplace on a jittered 5^3 mesh, two different bases of one mesh
+    n = 5
+    m = MeshTet.init_tensor(*(np.linspace(0, 1, n + 1),) * 3)
+    p = m.p.copy()
+    inner = jitter(m, rng, 0.2)
+    p[:, inner] += rng.uniform(-0.2 / n, 0.2 / n, size=(3, int(inner.sum())))
+    m = MeshTet(p, m.t)
+    ib = Basis(m, ElementTetP1())
+    save("tet_p1_jitter_laplace", p=m.p, t=m.t, element_dofs=ib.element_dofs,
+         X=ib.X, W=ib.W, b=unit_load.assemble(ib), **csr_arrays(laplace.assemble(ib)))
+
+    # quadrature rules the configs use, exactly as the reference tabulates them
+    from skfem.quadrature import get_quadrature_tet, get_quadrature_tri
+    rules = {}
+    for o in (1, 2, 3, 4):
+        X, W = get_quadrature_tri(o)
+        rules["tri%d_X" % o], rules["tri%d_W" % o] = X, W
+        X, W = get_quadrature_tet(o)
+        rules["tet%d_X" % o], rules["tet%d_W" % o] = X, W
+    save("quadrature_rules", **rules)
+
+    with open(os.path.join(OUT, "VERSION"), "w") as f:
+        f.write("scikit-fem %s, numpy %s, python %s\n"
+                % (skfem.__version__, np.__version__, sys.version.split()[0]))
+
+
+if __name__ == "__main__":
+    main()
