@@ -1,0 +1,325 @@
+"""Benchmark: GPU cell assembly (scikit-fem's BilinearForm.assemble) on GB300.
+
+Default workload: TetP1 k*dot(grad u, grad v) + u*v on the unit-cube tensor
+mesh with 101 nodes per axis (6,000,000 tets, 1,030,301 nodes), per-element
+k ~ lognormal(0, 1) (seeded), float64, plain forward assembly to CSR.
+
+One step = one assembly of the whole mesh into the CSR pattern (local
+matrices + fixed-order segmented sum), inputs resident in HBM.  The working
+set (staging 768 MB, CSR 122 MB) is far larger than L2, so no flush is
+needed between steps.  ``e2e`` times the public API call a user makes --
+``form.assemble(basis, k=<(nelems, nqp) host array>)`` returning a
+scipy.sparse.csr_matrix -- including the host->device copy of k and the
+device->host copy of the CSR.
+
+``--impl reference`` times the CPU oracle (a numpy restatement of
+scikit-fem's assembly, single process, its local loop split over all host
+threads as BilinearForm(nthreads=...) does) on a bounded sample of the same
+workload.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (ROOT, os.path.join(ROOT, "scikit-fem_gb300")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "elements/s & %HBM roofline: plain vs adjoint/batched assemble, rel err <=1e-12"
+UNIT = "elements/s"
+
+# algorithmic bytes per element of a steady-state TetP1 assembly
+# (element ids 16 B + coefficient 8 B) + coordinates + CSR values, see the design doc
+def algorithmic_bytes(nelems, nverts, nnz, dim=3, nloc=4):
+    return nelems * (nloc * 4 + 8) + nverts * dim * 8 + nnz * 8
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# measured DFMA throughput of this GB300 pool (fp64_probe: 0.598e12 FMA/s)
+FP64_PEAK_GFLOPS = 1195.0
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(n_nodes, seed):
+    import skfem_gb300 as F
+    m = F.MeshTet.init_tensor(*(np.linspace(0, 1, n_nodes),) * 3)
+    rng = np.random.default_rng(seed)
+    k = rng.lognormal(0.0, 1.0, m.nelements)
+    return m, k
+
+
+def gpu_arm(args):
+    import torch
+
+    import skfem_gb300 as F
+    from skfem_gb300 import _native as N
+    from skfem_gb300 import helpers as H
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    m, k = build_workload(args.nodes, args.seed + rank)
+    b = F.Basis(m, F.ElementTetP1())
+
+    @F.BilinearForm
+    def form(u, v, w):
+        return w.k * H.dot(H.grad(u), H.grad(v)) + u * v
+
+    kd = torch.from_numpy(k).cuda()
+    # first call builds the pattern (one-time, reported separately)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    K0 = form.assemble_torch(b, k=kd)
+    torch.cuda.synchronize()
+    pattern_s = time.perf_counter() - t0
+    entry = next(iter(b._patterns.values()))
+    nnz = entry.nnz
+
+    # a bare C-ABI step: inputs in HBM, results in HBM
+    coeffs, ch, c_form = form._setup(b, None, {"k": kd})
+    vals = torch.empty(nnz, dtype=torch.float64, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    lib = N.lib()
+    stream = torch.cuda.current_stream()
+    sp = N.stream_ptr(stream)
+
+    def step():
+        N.check(lib.fem_assemble(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
+                                 entry.pat.handle, N.ptr(entry.staging), N.ptr(vals),
+                                 N.ptr(status), sp))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        time.sleep(0.3)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        time.sleep(0.2)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = t.item()
+    assert int(status.item()) == 0, "assembly status %d" % int(status.item())
+    assert torch.equal(vals, K0.values()), "repeated assembly not bitwise identical"
+
+    # per-kernel split (same stream, CUDA events): local kernel vs segmented sum
+    local_buf = entry.staging
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    t_local, t_sum = 0.0, 0.0
+    reps = max(3, args.steps)
+    for _ in range(reps):
+        e0.record(stream)
+        N.check(lib.fem_local_matrices(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
+                                       N.ptr(local_buf), sp))
+        e1.record(stream)
+        N.check(lib.fem_csr_sum(entry.pat.handle, N.ptr(local_buf), N.ptr(vals), None, sp))
+        e2.record(stream)
+        torch.cuda.synchronize()
+        t_local += e0.elapsed_time(e1)
+        t_sum += e1.elapsed_time(e2)
+    t_local /= reps
+    t_sum /= reps
+
+    # e2e: public API with host buffers (k as the reference takes it)
+    kw_host = b.zero_w() + k[:, None]
+    for _ in range(2):
+        form.assemble(b, k=kw_host)
+    torch.cuda.synchronize()
+    e2e_steps = max(2, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        Kh = form.assemble(b, k=kw_host)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    h2d = kw_host.nbytes
+    d2h = Kh.data.nbytes + Kh.indices.nbytes + Kh.indptr.nbytes
+
+    hbm, peak_kind = peaks()
+    nel = m.nelements
+    B = algorithmic_bytes(nel, m.p.shape[1], nnz)
+    achieved = B / (ms * 1e-3) / 1e9
+    flops_per_el = 102.0  # FP64 ops of the TetP1 local kernel, counted in the design doc
+    fp64_achieved = nel * flops_per_el / (t_local * 1e-3) / 1e9
+    res = {
+        "metric": METRIC, "value": nel * world / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak" if world > 1 else "replicas only",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded tensor mesh, lognormal k)",
+        "config": {"workload": "TetP1 k*laplace+mass, 101^3-node unit cube tensor mesh, 6 tets/cell",
+                   "nelems": nel, "nverts": int(m.p.shape[1]), "nnz": nnz,
+                   "l2": "inputs+staging larger than L2 (no flush)", "parallelism": "replicas",
+                   "pattern_build_s": pattern_s},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                     "peak_kind": peak_kind, "algorithmic_bytes_per_step": B,
+                     "kernel": "whole assembly step (local + segmented sum)"},
+        "fp64": {"kernel": "local matrices (simplex_scalar_kernel<3,1>)",
+                 "ms": t_local, "gflops": fp64_achieved, "peak_gflops": FP64_PEAK_GFLOPS,
+                 "frac": fp64_achieved / FP64_PEAK_GFLOPS},
+        "kernels_ms": {"local": t_local, "csr_sum": t_sum},
+        "clocks": clk.summary(),
+        "e2e": {"value": nel / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s},
+        "gpu_launches": 3 * args.steps,
+    }
+    if rank == 0 and not args.no_cpu:
+        res["cpu_baseline"] = cpu_baseline(args)
+    if dist:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(res))
+
+
+def cpu_baseline(args, threads=1):
+    """The oracle (numpy restatement of the reference) on a bounded sample:
+    the same form on a smaller mesh of the same family, timed like the
+    reference's performance.py (Basis construction + assemble)."""
+    import oracle as O
+    n = args.cpu_nodes
+    m = O.mesh_tet_tensor(*(np.linspace(0, 1, n),) * 3)
+    k = np.random.default_rng(args.seed).lognormal(0.0, 1.0, m.nelements)
+    times = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        bo = O.OBasis(m, O.TetP1())
+        O.bilinear_assemble(O.k_laplace_mass, bo, k=bo.zero_w() + k[:, None], nthreads=threads)
+        times.append(time.perf_counter() - t0)
+    t = min(times)
+    return {"value": m.nelements / t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "TetP1 k*laplace+mass on a %d^3-node cube (%d tets), Basis + assemble, "
+                      "best of 2" % (n, m.nelements)}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    import oracle as O
+    n = args.cpu_nodes
+    m = O.mesh_tet_tensor(*(np.linspace(0, 1, n),) * 3)
+    k = np.random.default_rng(args.seed).lognormal(0.0, 1.0, m.nelements)
+    for _ in range(args.warmup):
+        bo = O.OBasis(m, O.TetP1())
+        O.bilinear_assemble(O.k_laplace_mass, bo, k=bo.zero_w() + k[:, None], nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        bo = O.OBasis(m, O.TetP1())
+        O.bilinear_assemble(O.k_laplace_mass, bo, k=bo.zero_w() + k[:, None], nthreads=threads)
+    dt = (time.perf_counter() - t0) / args.steps
+    v = m.nelements / dt
+    res = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+           "higher_is_better": True, "scaling": "replicas only", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic (seeded tensor mesh, lognormal k)",
+           "config": {"workload": "TetP1 k*laplace+mass, tensor cube mesh (bounded sample of the "
+                                  "101^3-node workload)", "nodes_per_axis": n,
+                      "nelems": m.nelements},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": "%d^3-node cube, %d tets per step" % (n, m.nelements)},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(res))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nodes", type=int, default=101, help="nodes per axis of the cube")
+    ap.add_argument("--cpu-nodes", type=int, default=41, help="nodes per axis of the CPU sample")
+    ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

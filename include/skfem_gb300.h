@@ -1,0 +1,205 @@
+/*
+ * skfem_gb300 -- C ABI of the GB300 (sm_103a) cell-assembly library.
+ *
+ * The library replaces the numerical core of scikit-fem's cell assembly:
+ *
+ *   CellBasis.__init__ / MappingAffine / MappingIsoparametric /
+ *   ElementH1.gbasis / ElementVector.gbasis      (skfem/assembly/basis/cell_basis.py:42-106,
+ *                                                 skfem/mapping/mapping_affine.py:55-232,
+ *                                                 skfem/mapping/mapping_isoparametric.py:112-226,
+ *                                                 skfem/element/element_h1.py:10-24,
+ *                                                 skfem/element/element_vector.py:36-48)
+ *   BilinearForm._assemble / LinearForm._assemble (skfem/assembly/form/bilinear_form.py:58-128,
+ *                                                 skfem/assembly/form/linear_form.py:18-49)
+ *   COOData._assemble_scipy_csr / COOData.toarray (skfem/assembly/form/coo_data.py:27-36, 102-108)
+ *
+ * Conventions
+ *   - Every array argument is a DEVICE pointer owned by the caller (torch
+ *     tensors on the Python side).  The library never frees caller memory.
+ *   - FemPattern objects are allocated by fem_pattern_build and released
+ *     with fem_pattern_destroy.
+ *   - Every entry point is stream-ordered on the given stream and returns 0
+ *     on success or a FemStatus code; fem_last_error() gives a thread-local
+ *     message describing the last failure on the calling thread.
+ *   - Values are float64, indices int32, exactly as the reference
+ *     (skfem/assembly/dofs.py:270, skfem/mesh/mesh.py:558-559).
+ *   - Layouts follow the reference: p is (dim, nverts) C-contiguous
+ *     (Mesh.p), element_dofs is (nbfun, nelems) C-contiguous
+ *     (Dofs.element_dofs).
+ */
+#ifndef SKFEM_GB300_H
+#define SKFEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* fem_stream_t; /* == cudaStream_t */
+
+/* Status codes. */
+enum FemStatus {
+  FEM_OK = 0,
+  FEM_ERR_ARGUMENT = 1,      /* invalid argument (raised as ValueError by the Python layer) */
+  FEM_ERR_UNSUPPORTED = 2,   /* family / form combination not implemented (NotImplementedError) */
+  FEM_ERR_CUDA = 3,          /* CUDA runtime error */
+  FEM_ERR_ZERO_JACOBIAN = 4, /* isoparametric detDF == 0 (mapping_isoparametric.py:195-196) */
+  FEM_ERR_STALE_PATTERN = 5, /* exact-zero structure of the local matrices changed: rebuild */
+  FEM_ERR_CAPACITY = 6       /* a CSR row exceeds the per-row working-set limit */
+};
+
+/* Element families (the reference classes they stand for). */
+enum FemFamily {
+  FEM_TRI_P1 = 1, /* ElementTriP1  (element_tri_p1.py:18-33)  */
+  FEM_TRI_P2 = 2, /* ElementTriP2  (element_tri_p2.py:22-48)  */
+  FEM_TET_P1 = 3, /* ElementTetP1  (element_tet_p1.py:19-45)  */
+  FEM_TET_P2 = 4, /* ElementTetP2  (element_tet_p2.py:26-103) */
+  FEM_HEX_1 = 5   /* ElementHex1   (element_hex1.py:23-69), isoparametric */
+};
+
+/* Mesh geometry (Mesh.p / Mesh.t, skfem/mesh/mesh.py:42-44, 544-591). */
+typedef struct FemMesh {
+  int32_t dim;      /* 2 or 3 */
+  int32_t nloc;     /* vertices per element: 3, 4 or 8 */
+  int64_t nverts;   /* columns of p */
+  int64_t nelems;   /* columns of t */
+  const double* p;  /* (dim, nverts) */
+  const int32_t* t; /* (nloc, nelems) */
+} FemMesh;
+
+/* Global numbering of one basis (Dofs, skfem/assembly/dofs.py:264-334). */
+typedef struct FemBasis {
+  int32_t family;              /* FemFamily */
+  int32_t vector;              /* 1 for ElementVector(family), 0 for scalar */
+  int32_t nbfun;               /* local functions (vector: dim * scalar) */
+  int32_t pad_;
+  int64_t ndofs;               /* N */
+  const int32_t* element_dofs; /* (nbfun, nelems) */
+} FemBasis;
+
+/* A per-element coefficient: scale * field[e], or scale when field == NULL. */
+typedef struct FemCoef {
+  double scale;
+  const double* field;
+} FemCoef;
+
+/*
+ * Bilinear forms the kernels evaluate (integrand, summed over terms whose
+ * coefficient scale is nonzero):
+ *   scalar bases:  diff * dot(grad u, grad v) + mass * u * v
+ *   vector bases:  lam  * div u * div v                       (a_{bk,al} = d_bk d_al)
+ *                + lap  * ddot(grad u, grad v)                (d_ab d_kl)
+ *                + tr   * ddot(grad u, transpose(grad v))     (d_bl d_ka)
+ *                + mass * dot(u, v)
+ * linear_elasticity(L, M) (skfem/models/elasticity.py:44-53) is
+ * lam = L, lap = M, tr = M.
+ */
+typedef struct FemBilinear {
+  FemCoef diff, mass;
+  FemCoef lam, lap, tr;
+} FemBilinear;
+
+/* Linear form: load * v (scalar) or dot(load_vec, v) with load_vec = (load, load, ...) off. */
+typedef struct FemLinear {
+  FemCoef load;
+} FemLinear;
+
+/* Opaque one-time structure: row incidence, CSR pattern, local-to-slot map. */
+typedef struct FemPattern FemPattern;
+
+/* Last error message of the calling thread ("" if none). */
+const char* fem_last_error(void);
+
+/* Library version string. */
+const char* fem_version(void);
+
+/*
+ * Local (element) matrices: local[(e * nbfun + i) * nbfun + j] = K_e[i][j],
+ * i = test function (row), j = trial function (column), the same entry as
+ * the reference's data[j, i, e] (bilinear_form.py:90-98).
+ */
+int fem_local_matrices(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
+                       double* local, fem_stream_t stream);
+
+/* Local load vectors: local[e * nbfun + i] (linear_form.py:40-44). */
+int fem_local_vectors(const FemMesh* mesh, const FemBasis* basis, const FemLinear* form,
+                      double* local, fem_stream_t stream);
+
+/*
+ * One-time pattern build (replaces coo_matrix(...).eliminate_zeros().tocsr(),
+ * coo_data.py:34-36).  The local matrices of `form` are evaluated once with
+ * separately rounded products and sums (no fused multiply-add, as numpy
+ * evaluates the reference's forms); local entries that come out exactly
+ * +-0.0 create no CSR entry, as eliminate_zeros drops them before the
+ * duplicates are summed.  The pattern also records which per-element
+ * coefficients were exactly zero, so that fem_assemble can report when the
+ * zero structure changes.  form == NULL builds only the row incidence
+ * (enough for load vectors).  Synchronises `stream`.
+ */
+int fem_pattern_build(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
+                      FemPattern** out, fem_stream_t stream);
+
+/* Sizes: nnz of the CSR pattern, number of rows (N), and the bytes of the
+ * local-matrix staging buffer fem_assemble needs. */
+int fem_pattern_info(const FemPattern* pat, int64_t* nnz, int64_t* nrows, int64_t* staging_bytes);
+
+/* Copy the CSR structure out: indptr (nrows+1), indices (nnz), both int32. */
+int fem_pattern_export(const FemPattern* pat, int32_t* indptr, int32_t* indices, fem_stream_t stream);
+
+void fem_pattern_destroy(FemPattern* pat);
+
+/*
+ * Steady-state assembly into an existing pattern: local matrices into
+ * `staging` (fem_pattern_info bytes), then a fixed-order, atomic-free
+ * segmented sum into csr_values (nnz).  status (device int32, may be NULL)
+ * receives FEM_ERR_STALE_PATTERN when the exact-zero structure of the local
+ * matrices may have changed: some per-element coefficient became exactly
+ * zero or stopped being zero since the pattern was built.  The caller then
+ * rebuilds the pattern and assembles again.
+ */
+int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
+                 const FemPattern* pat, double* staging, double* csr_values, int32_t* status,
+                 fem_stream_t stream);
+
+/* Segmented sum only (local matrices already in `local`). */
+int fem_csr_sum(const FemPattern* pat, const double* local, double* csr_values, int32_t* status,
+                fem_stream_t stream);
+
+/* Load vector b (nrows) from local vectors (incidence order, no atomics). */
+int fem_vector_sum(const FemPattern* pat, const double* local, double* b, fem_stream_t stream);
+
+/* Load vector end to end: local vectors into staging (nelems*nbfun doubles) then b. */
+int fem_assemble_vector(const FemMesh* mesh, const FemBasis* basis, const FemLinear* form,
+                        const FemPattern* pat, double* staging, double* b, fem_stream_t stream);
+
+/*
+ * Adjoint (no counterpart in the reference, which differentiates only with
+ * respect to the solution field, skfem/autodiff/__init__.py:124-213).
+ * For J = w^T K(coef, X) u with K from a bilinear form whose terms are
+ * linear in per-element fields:
+ *   dcoef_diff[e] = d J / d field_diff[e]  (may be NULL), likewise dcoef_mass,
+ *   dX (dim, nverts) = d J / d p            (may be NULL), accumulated per
+ *   vertex in a fixed order (no atomics).
+ * Geometry is recomputed in the adjoint; nothing per quadrature point is stored.
+ * elem_scratch: nelems * nloc * dim doubles (per-element vertex gradients).
+ */
+int fem_bilinear_vjp(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
+                     const FemPattern* vertex_incidence, const double* w, const double* u,
+                     double* dcoef_diff, double* dcoef_mass, double* dX, double* elem_scratch,
+                     fem_stream_t stream);
+
+/* J = w^T b(coef, X): dload[e] and dX (same conventions). */
+int fem_linear_vjp(const FemMesh* mesh, const FemBasis* basis, const FemLinear* form,
+                   const FemPattern* vertex_incidence, const double* w, double* dload, double* dX,
+                   double* elem_scratch, fem_stream_t stream);
+
+/* Vertex incidence of the mesh (rows = vertices), used by the adjoint's
+ * fixed-order gather of per-element coordinate gradients. */
+int fem_vertex_incidence_build(const FemMesh* mesh, FemPattern** out, fem_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SKFEM_GB300_H */

@@ -732,10 +732,12 @@ def _normalize_w(basis: OBasis, w: Dict) -> Dict:
 
 
 def bilinear_local(form: Callable, ubasis: OBasis, vbasis: Optional[OBasis] = None,
-                   **w):
+                   nthreads: int = 0, **w):
     """BilinearForm._assemble (bilinear_form.py:58-128): returns
     ``data`` of shape (Nu, Nv, nelems), ``rows``/``cols`` in the reference's
-    COO order (index nt*(Nv*j + i) + e), and the shape (Nv_dofs, Nu_dofs)."""
+    COO order (index nt*(Nv*j + i) + e), and the shape (Nv_dofs, Nu_dofs).
+    nthreads > 0 splits the (j, i) loop over Python threads as the
+    reference does (bilinear_form.py:100-119)."""
     vbasis = ubasis if vbasis is None else vbasis
     nt = ubasis.nelems
     dx = ubasis.dx
@@ -749,14 +751,28 @@ def bilinear_local(form: Callable, ubasis: OBasis, vbasis: Optional[OBasis] = No
             ixs = slice(nt * (Nv * j + i), nt * (Nv * j + i + 1))
             rows[ixs] = vbasis.element_dofs[i]
             cols[ixs] = ubasis.element_dofs[j]
-            data[j, i, :] = np.sum(form(*ubasis.basis[j], *vbasis.basis[i], wd) * dx, axis=1)
+            if nthreads <= 0:
+                data[j, i, :] = np.sum(form(*ubasis.basis[j], *vbasis.basis[i], wd) * dx, axis=1)
+    if nthreads > 0:
+        from threading import Thread
+        pairs = np.array([[i, j] for j in range(Nu) for i in range(Nv)])
+
+        def work(ix):
+            for i, j in ix:
+                data[j, i] = np.sum(form(*ubasis.basis[j], *vbasis.basis[i], wd) * dx, axis=1)
+
+        ths = [Thread(target=work, args=(ix,)) for ix in np.array_split(pairs, nthreads, axis=0)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
     return data, rows, cols, (vbasis.N, ubasis.N)
 
 
 def bilinear_assemble(form: Callable, ubasis: OBasis, vbasis: Optional[OBasis] = None,
-                      **w):
+                      nthreads: int = 0, **w):
     """Form -> COO -> eliminate_zeros -> CSR (coo_data.py:27-36)."""
-    data, rows, cols, shape = bilinear_local(form, ubasis, vbasis, **w)
+    data, rows, cols, shape = bilinear_local(form, ubasis, vbasis, nthreads=nthreads, **w)
     K = coo_matrix((data.flatten("C"), (rows, cols)), shape=shape)
     K.eliminate_zeros()
     return K.tocsr()

@@ -1,0 +1,330 @@
+// extern "C" entry points of libskfem_gb300 (declared in include/skfem_gb300.h).
+
+#include <mutex>
+#include <string>
+
+#include "fem_common.cuh"
+
+namespace fem_fast {
+int local_matrices(const FemMesh&, const FemBasis&, const FemBilinear&, double*, int32_t*,
+                   cudaStream_t);
+int local_vectors(const FemMesh&, const FemBasis&, const FemLinear&, double*, int32_t*,
+                  cudaStream_t);
+}  // namespace fem_fast
+namespace fem_exact {
+int local_matrices(const FemMesh&, const FemBasis&, const FemBilinear&, double*, int32_t*,
+                   cudaStream_t);
+}  // namespace fem_exact
+
+namespace fem {
+int build_incidence(const int32_t* dofs, int64_t nelems, int nb, int64_t nrows, Pattern* P,
+                    cudaStream_t st);
+int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, Pattern* P,
+              cudaStream_t st);
+int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st);
+int vector_sum(const Pattern& P, const double* local, double* b, cudaStream_t st);
+void free_pattern(Pattern* P);
+
+namespace {
+thread_local std::string g_err;
+}
+
+void set_error(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = std::string("[") + std::to_string(code) + "] " + buf;
+}
+
+int check_cuda(cudaError_t err, const char* what) {
+  set_error(FEM_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorString(err), cudaGetErrorName(err));
+  return FEM_ERR_CUDA;
+}
+
+int basis_nb_scalar(int family) {
+  switch (family) {
+    case FEM_TRI_P1: return 3;
+    case FEM_TRI_P2: return 6;
+    case FEM_TET_P1: return 4;
+    case FEM_TET_P2: return 10;
+    case FEM_HEX_1: return 8;
+    default: return 0;
+  }
+}
+
+int basis_dim(int family) {
+  switch (family) {
+    case FEM_TRI_P1:
+    case FEM_TRI_P2: return 2;
+    case FEM_TET_P1:
+    case FEM_TET_P2:
+    case FEM_HEX_1: return 3;
+    default: return 0;
+  }
+}
+
+// Per-element zero bits of the form's coefficients (bit k: channel k is 0).
+__global__ void coef_zero_bits_kernel(FemBilinear f, int64_t n, const uint8_t* __restrict__ ref,
+                                      uint8_t* __restrict__ out, int32_t* __restrict__ status) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const FemCoef* c[5] = {&f.diff, &f.mass, &f.lam, &f.lap, &f.tr};
+  uint8_t bits = 0;
+#pragma unroll
+  for (int k = 0; k < 5; ++k)
+    if (coef_at(*c[k], e) == 0.0) bits |= (uint8_t)(1u << k);
+  if (out) out[e] = bits;
+  if (ref && ref[e] != bits) atomicOr(status, 1 << FEM_ERR_STALE_PATTERN);
+}
+
+}  // namespace fem
+
+struct FemPattern {
+  fem::Pattern P;
+  uint8_t* coef_bits = nullptr;  // nelems, or null when built without a form
+  int family = 0, vector = 0;
+};
+
+using fem::set_error;
+
+namespace fem {
+const Pattern* pattern_of(const FemPattern* h) { return h ? &h->P : nullptr; }
+int new_pattern_handle(Pattern* P, FemPattern** out) {
+  FemPattern* H = new FemPattern();
+  H->P = *P;
+  delete P;
+  *out = H;
+  return 0;
+}
+}  // namespace fem
+
+static int validate(const FemMesh* m, const FemBasis* b) {
+  if (!m || !b) {
+    set_error(FEM_ERR_ARGUMENT, "null mesh or basis");
+    return FEM_ERR_ARGUMENT;
+  }
+  const int nbs = fem::basis_nb_scalar(b->family);
+  if (nbs == 0) {
+    set_error(FEM_ERR_UNSUPPORTED, "unknown element family %d", b->family);
+    return FEM_ERR_UNSUPPORTED;
+  }
+  const int dim = fem::basis_dim(b->family);
+  if (m->dim != dim) {
+    set_error(FEM_ERR_ARGUMENT, "Incompatible Mesh and Element: mesh dim %d, element dim %d",
+              m->dim, dim);
+    return FEM_ERR_ARGUMENT;
+  }
+  const int nloc = b->family == FEM_HEX_1 ? 8 : dim + 1;
+  if (m->nloc != nloc) {
+    set_error(FEM_ERR_ARGUMENT, "Incompatible Mesh and Element: %d vertices per cell, expected %d",
+              m->nloc, nloc);
+    return FEM_ERR_ARGUMENT;
+  }
+  const int nb = b->vector ? nbs * dim : nbs;
+  if (b->nbfun != nb) {
+    set_error(FEM_ERR_ARGUMENT, "nbfun %d does not match the family (%d)", b->nbfun, nb);
+    return FEM_ERR_ARGUMENT;
+  }
+  if (m->nelems < 0 || m->nverts < 0 || (m->nelems > 0 && (!m->p || !m->t || !b->element_dofs))) {
+    set_error(FEM_ERR_ARGUMENT, "invalid mesh arrays");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (b->vector && b->family == FEM_HEX_1) {
+    set_error(FEM_ERR_UNSUPPORTED, "ElementVector(ElementHex1) is not implemented");
+    return FEM_ERR_UNSUPPORTED;
+  }
+  return 0;
+}
+
+static int read_status(int32_t* dstatus, cudaStream_t st) {
+  int32_t h = 0;
+  FEM_TRY_CUDA(cudaMemcpyAsync(&h, dstatus, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  FEM_TRY_CUDA(cudaStreamSynchronize(st));
+  if (h & (1 << FEM_ERR_ZERO_JACOBIAN)) {
+    set_error(FEM_ERR_ZERO_JACOBIAN, "Zero Jacobian determinant");
+    return FEM_ERR_ZERO_JACOBIAN;
+  }
+  return 0;
+}
+
+extern "C" {
+
+const char* fem_last_error(void) { return fem::g_err.c_str(); }
+
+const char* fem_version(void) { return "skfem_gb300 0.1 (sm_103a)"; }
+
+int fem_local_matrices(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
+                       double* local, fem_stream_t stream) {
+  int rc = validate(mesh, basis);
+  if (rc) return rc;
+  if (!form || !local) {
+    set_error(FEM_ERR_ARGUMENT, "null form or output");
+    return FEM_ERR_ARGUMENT;
+  }
+  return fem_fast::local_matrices(*mesh, *basis, *form, local, nullptr, (cudaStream_t)stream);
+}
+
+int fem_local_vectors(const FemMesh* mesh, const FemBasis* basis, const FemLinear* form,
+                      double* local, fem_stream_t stream) {
+  int rc = validate(mesh, basis);
+  if (rc) return rc;
+  if (!form || !local) {
+    set_error(FEM_ERR_ARGUMENT, "null form or output");
+    return FEM_ERR_ARGUMENT;
+  }
+  return fem_fast::local_vectors(*mesh, *basis, *form, local, nullptr, (cudaStream_t)stream);
+}
+
+int fem_pattern_build(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
+                      FemPattern** out, fem_stream_t stream) {
+  int rc = validate(mesh, basis);
+  if (rc) return rc;
+  if (!out) {
+    set_error(FEM_ERR_ARGUMENT, "null output handle");
+    return FEM_ERR_ARGUMENT;
+  }
+  *out = nullptr;
+  cudaStream_t st = (cudaStream_t)stream;
+  FemPattern* H = new FemPattern();
+  H->family = basis->family;
+  H->vector = basis->vector;
+  auto fail = [&](int code) {
+    fem::free_pattern(new fem::Pattern(H->P));  // releases device arrays
+    cudaFree(H->coef_bits);
+    delete H;
+    return code;
+  };
+  rc = fem::build_incidence(basis->element_dofs, mesh->nelems, basis->nbfun, basis->ndofs, &H->P, st);
+  if (rc) return fail(rc);
+  if (form) {
+    const int nb = basis->nbfun;
+    const int64_t L = (int64_t)nb * nb;
+    double* local = nullptr;
+    int32_t* dstatus = nullptr;
+    cudaError_t e1 = cudaMallocAsync(&local, std::max<int64_t>(1, mesh->nelems * L) * sizeof(double), st);
+    if (e1 != cudaSuccess) return fail(fem::check_cuda(e1, "cudaMallocAsync(local)"));
+    e1 = cudaMallocAsync(&dstatus, sizeof(int32_t), st);
+    if (e1 != cudaSuccess) return fail(fem::check_cuda(e1, "cudaMallocAsync(status)"));
+    cudaMemsetAsync(dstatus, 0, sizeof(int32_t), st);
+    rc = fem_exact::local_matrices(*mesh, *basis, *form, local, dstatus, st);
+    if (!rc) rc = read_status(dstatus, st);
+    if (!rc) rc = fem::build_csr(basis->element_dofs, nb, basis->ndofs, local, &H->P, st);
+    if (!rc && mesh->nelems > 0) {
+      cudaError_t e2 = cudaMallocAsync(&H->coef_bits, mesh->nelems, st);
+      if (e2 != cudaSuccess) rc = fem::check_cuda(e2, "cudaMallocAsync(coef_bits)");
+      else {
+        fem::coef_zero_bits_kernel<<<(unsigned)fem::ceil_div(mesh->nelems, 256), 256, 0, st>>>(
+            *form, mesh->nelems, nullptr, H->coef_bits, nullptr);
+        cudaError_t e3 = cudaGetLastError();
+        if (e3 != cudaSuccess) rc = fem::check_cuda(e3, "coef_zero_bits_kernel");
+      }
+    }
+    cudaFreeAsync(local, st);
+    cudaFreeAsync(dstatus, st);
+    cudaError_t e4 = cudaStreamSynchronize(st);
+    if (!rc && e4 != cudaSuccess) rc = fem::check_cuda(e4, "pattern build");
+    if (rc) return fail(rc);
+  }
+  *out = H;
+  return 0;
+}
+
+int fem_pattern_info(const FemPattern* pat, int64_t* nnz, int64_t* nrows, int64_t* staging_bytes) {
+  if (!pat) {
+    set_error(FEM_ERR_ARGUMENT, "null pattern");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (nnz) *nnz = pat->P.nnz;
+  if (nrows) *nrows = pat->P.nrows;
+  if (staging_bytes)
+    *staging_bytes = pat->P.nelems * (int64_t)pat->P.nbfun_v * std::max(1, pat->P.nbfun_u) *
+                     (int64_t)sizeof(double);
+  return 0;
+}
+
+int fem_pattern_export(const FemPattern* pat, int32_t* indptr, int32_t* indices,
+                       fem_stream_t stream) {
+  if (!pat || !pat->P.has_matrix) {
+    set_error(FEM_ERR_ARGUMENT, "pattern has no CSR structure");
+    return FEM_ERR_ARGUMENT;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (indptr)
+    FEM_TRY_CUDA(cudaMemcpyAsync(indptr, pat->P.indptr, (pat->P.nrows + 1) * sizeof(int32_t),
+                                 cudaMemcpyDeviceToDevice, st));
+  if (indices && pat->P.nnz > 0)
+    FEM_TRY_CUDA(cudaMemcpyAsync(indices, pat->P.indices, pat->P.nnz * sizeof(int32_t),
+                                 cudaMemcpyDeviceToDevice, st));
+  return 0;
+}
+
+void fem_pattern_destroy(FemPattern* pat) {
+  if (!pat) return;
+  fem::free_pattern(new fem::Pattern(pat->P));
+  cudaFree(pat->coef_bits);
+  delete pat;
+}
+
+int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
+                 const FemPattern* pat, double* staging, double* csr_values, int32_t* status,
+                 fem_stream_t stream) {
+  int rc = validate(mesh, basis);
+  if (rc) return rc;
+  if (!form || !pat || !staging || !csr_values) {
+    set_error(FEM_ERR_ARGUMENT, "null form, pattern or buffer");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (pat->P.nelems != mesh->nelems || pat->P.nbfun_v != basis->nbfun || !pat->P.has_matrix) {
+    set_error(FEM_ERR_ARGUMENT, "pattern does not belong to this mesh / basis");
+    return FEM_ERR_ARGUMENT;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (status && pat->coef_bits && mesh->nelems > 0) {
+    fem::coef_zero_bits_kernel<<<(unsigned)fem::ceil_div(mesh->nelems, 256), 256, 0, st>>>(
+        *form, mesh->nelems, pat->coef_bits, nullptr, status);
+    FEM_LAUNCH_CHECK("coef_zero_bits_kernel");
+  }
+  rc = fem_fast::local_matrices(*mesh, *basis, *form, staging, status, st);
+  if (rc) return rc;
+  return fem::csr_sum(pat->P, staging, csr_values, st);
+}
+
+int fem_csr_sum(const FemPattern* pat, const double* local, double* csr_values, int32_t* status,
+                fem_stream_t stream) {
+  (void)status;
+  if (!pat || !local || !csr_values) {
+    set_error(FEM_ERR_ARGUMENT, "null pattern or buffer");
+    return FEM_ERR_ARGUMENT;
+  }
+  return fem::csr_sum(pat->P, local, csr_values, (cudaStream_t)stream);
+}
+
+int fem_vector_sum(const FemPattern* pat, const double* local, double* b, fem_stream_t stream) {
+  if (!pat || !local || !b) {
+    set_error(FEM_ERR_ARGUMENT, "null pattern or buffer");
+    return FEM_ERR_ARGUMENT;
+  }
+  return fem::vector_sum(pat->P, local, b, (cudaStream_t)stream);
+}
+
+int fem_assemble_vector(const FemMesh* mesh, const FemBasis* basis, const FemLinear* form,
+                        const FemPattern* pat, double* staging, double* b, fem_stream_t stream) {
+  int rc = validate(mesh, basis);
+  if (rc) return rc;
+  if (!form || !pat || !staging || !b) {
+    set_error(FEM_ERR_ARGUMENT, "null form, pattern or buffer");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (pat->P.nelems != mesh->nelems || pat->P.nbfun_v != basis->nbfun) {
+    set_error(FEM_ERR_ARGUMENT, "pattern does not belong to this mesh / basis");
+    return FEM_ERR_ARGUMENT;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  rc = fem_fast::local_vectors(*mesh, *basis, *form, staging, nullptr, st);
+  if (rc) return rc;
+  return fem::vector_sum(pat->P, staging, b, st);
+}
+
+}  // extern "C"

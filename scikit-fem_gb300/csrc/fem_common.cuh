@@ -1,0 +1,81 @@
+// Shared definitions of the skfem_gb300 CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "../../include/skfem_gb300.h"
+
+namespace fem {
+
+// ---------------------------------------------------------------- errors
+void set_error(int code, const char* fmt, ...);
+int check_cuda(cudaError_t err, const char* what);
+
+#define FEM_TRY_CUDA(expr)                                   \
+  do {                                                       \
+    cudaError_t _e = (expr);                                 \
+    if (_e != cudaSuccess) return ::fem::check_cuda(_e, #expr); \
+  } while (0)
+
+#define FEM_LAUNCH_CHECK(what)                                      \
+  do {                                                              \
+    cudaError_t _e = cudaGetLastError();                            \
+    if (_e != cudaSuccess) return ::fem::check_cuda(_e, what);      \
+  } while (0)
+
+// ---------------------------------------------------------------- pattern
+// Row incidence: for row r, inc[inc_ptr[r] .. inc_ptr[r+1]) lists the
+// (element, local index) pairs whose DOF is r, encoded e * nbfun + i and
+// sorted ascending -- the fixed summation order of every later call.
+// CSR: indptr/indices as scipy returns them.  slot[(q) * nbfun_u + j] is
+// the offset of local column j of incidence entry q inside its row
+// (0xFFFF: exact-zero local entry, no CSR slot).
+struct Pattern {
+  int64_t nrows = 0;
+  int64_t nelems = 0;
+  int32_t nbfun_v = 0;   // local rows per element
+  int32_t nbfun_u = 0;   // local columns per element
+  int64_t ninc = 0;      // incidence entries = nelems * nbfun_v
+  int64_t nnz = 0;
+  int32_t max_row_nnz = 0;
+  int32_t max_row_inc = 0;
+  int32_t* inc_ptr = nullptr;   // nrows + 1
+  int32_t* inc = nullptr;       // ninc
+  int32_t* indptr = nullptr;    // nrows + 1 (matrix patterns only)
+  int32_t* indices = nullptr;   // nnz
+  uint16_t* slot = nullptr;     // ninc * nbfun_u
+  bool has_matrix = false;
+};
+
+// ---------------------------------------------------------------- helpers
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+inline int num_sms() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 152;
+  }
+  return n;
+}
+
+__device__ __forceinline__ double coef_at(const FemCoef& c, int64_t e) {
+  return c.field ? c.scale * c.field[e] : c.scale;
+}
+
+// Exclusive scan of n int32 counts into out (n+1 entries); device scratch
+// from the caller's allocation helper.  Returns the total via *total (host).
+int exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, int64_t* total,
+                       cudaStream_t stream);
+
+int basis_nb_scalar(int family);
+int basis_dim(int family);
+
+}  // namespace fem

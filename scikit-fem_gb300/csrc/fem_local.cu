@@ -1,0 +1,656 @@
+// Fused local-matrix kernels: geometry + basis + form + quadrature in one
+// FP64 pass per element, writing element matrices K_e[i][j] (i = test row,
+// j = trial column) to an element-major staging array.
+//
+// Replaces, per element family, the chain
+//   MappingAffine._init_Ab/_init_invA (skfem/mapping/mapping_affine.py:55-131)
+//   MappingIsoparametric._J/detDF/invDF (skfem/mapping/mapping_isoparametric.py:112-226)
+//   ElementH1.gbasis / ElementVector.gbasis (skfem/element/element_h1.py:10-24,
+//                                            skfem/element/element_vector.py:36-48)
+//   CellBasis dx = |detDF| * W (skfem/assembly/basis/cell_basis.py:104-105)
+//   BilinearForm._kernel / LinearForm._kernel (bilinear_form.py:150-151, linear_form.py:48-49)
+//
+// Affine simplices use the tensor representation (exact reference
+// integrals from fem_tables.cuh contracted with the barycentric-gradient
+// Gram matrix of each cell), which integrates the same polynomials the
+// reference's quadrature integrates exactly, in far fewer FP64 operations.
+// The trilinear hexahedron takes a closed form on parallelepipeds (where
+// the Jacobian is constant and the 4x4x4 rule is exact) and the full
+// 64-point isoparametric quadrature otherwise.
+//
+// This file is compiled twice: the default build lets the compiler fuse
+// multiply-adds (the values path), the FEM_EXACT build disables
+// contraction (-fmad=false) so that products that cancel exactly in
+// separately rounded arithmetic -- as numpy evaluates them -- come out as
+// exact zeros; that build feeds the eliminate_zeros mask of the pattern.
+
+#include "fem_common.cuh"
+#include "fem_tables.cuh"
+
+#ifdef FEM_EXACT
+#define FEM_NS fem_exact
+#else
+#define FEM_NS fem_fast
+#endif
+
+namespace FEM_NS {
+
+using fem::coef_at;
+
+constexpr int kBlock = 128;
+
+// --------------------------------------------------------------- geometry
+// c[a] = det(A) * grad(lambda_a) for the barycentric coordinates of the
+// cell, with A[i][j] = p_i(t_{j+1}) - p_i(t_0) (mapping_affine.py:64-70)
+// and the cofactor expressions of mapping_affine.py:92-129.
+template <int D>
+struct Simplex {
+  double c[D + 1][D];
+  double det;
+};
+
+template <int D>
+__device__ __forceinline__ void simplex_geometry(const FemMesh& m, int64_t e, Simplex<D>& s) {
+  double x[D + 1][D];
+#pragma unroll
+  for (int a = 0; a <= D; ++a) {
+    const int64_t v = m.t[a * m.nelems + e];
+#pragma unroll
+    for (int k = 0; k < D; ++k) x[a][k] = m.p[k * m.nverts + v];
+  }
+  double A[D][D];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) A[i][j] = x[j + 1][i] - x[0][i];
+  if constexpr (D == 2) {
+    s.det = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+    s.c[1][0] = A[1][1];
+    s.c[1][1] = -A[0][1];
+    s.c[2][0] = -A[1][0];
+    s.c[2][1] = A[0][0];
+  } else {
+    s.c[1][0] = -A[1][2] * A[2][1] + A[1][1] * A[2][2];
+    s.c[2][0] = A[1][2] * A[2][0] - A[1][0] * A[2][2];
+    s.c[3][0] = -A[1][1] * A[2][0] + A[1][0] * A[2][1];
+    s.c[1][1] = A[0][2] * A[2][1] - A[0][1] * A[2][2];
+    s.c[2][1] = -A[0][2] * A[2][0] + A[0][0] * A[2][2];
+    s.c[3][1] = A[0][1] * A[2][0] - A[0][0] * A[2][1];
+    s.c[1][2] = -A[0][2] * A[1][1] + A[0][1] * A[1][2];
+    s.c[2][2] = A[0][2] * A[1][0] - A[0][0] * A[1][2];
+    s.c[3][2] = -A[0][1] * A[1][0] + A[0][0] * A[1][1];
+    s.det = A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) -
+            A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
+            A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
+  }
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    double acc = s.c[1][k];
+#pragma unroll
+    for (int a = 2; a <= D; ++a) acc = acc + s.c[a][k];
+    s.c[0][k] = -acc;
+  }
+}
+
+template <int D>
+__device__ __forceinline__ double dotc(const double* a, const double* b) {
+  double r = a[0] * b[0];
+#pragma unroll
+  for (int k = 1; k < D; ++k) r = r + a[k] * b[k];
+  return r;
+}
+
+// ----------------------------------------------------------- smem epilogue
+// Each thread writes its element's matrix into a padded row of shared
+// memory; the block then streams the rows out contiguously.
+template <int L>
+__device__ __forceinline__ void flush_rows(double* smem, double* __restrict__ out, int64_t e0,
+                                           int64_t nelems) {
+  __syncthreads();
+  const int64_t nb = ((nelems - e0) < (int64_t)kBlock ? (nelems - e0) : (int64_t)kBlock);
+  const int64_t total = nb * L;
+  double* dst = out + e0 * L;
+  for (int64_t g = threadIdx.x; g < total; g += blockDim.x) {
+    const int el = (int)(g / L);
+    const int k = (int)(g - (int64_t)el * L);
+    dst[g] = smem[el * (L + 1) + k];
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------ simplex, scalar P1 / P2
+template <int D, int ORDER>
+struct SimplexTraits;
+template <> struct SimplexTraits<2, 1> { static constexpr int NB = 3; static constexpr double FACT = 2.0; };
+template <> struct SimplexTraits<2, 2> { static constexpr int NB = 6; static constexpr double FACT = 2.0; };
+template <> struct SimplexTraits<3, 1> { static constexpr int NB = 4; static constexpr double FACT = 6.0; };
+template <> struct SimplexTraits<3, 2> { static constexpr int NB = 10; static constexpr double FACT = 6.0; };
+
+template <int D, int ORDER>
+__global__ void __launch_bounds__(kBlock) simplex_scalar_kernel(FemMesh m, FemBilinear f,
+                                                                double* __restrict__ out) {
+  constexpr int NB = SimplexTraits<D, ORDER>::NB;
+  constexpr int L = NB * NB;
+  constexpr double FACT = SimplexTraits<D, ORDER>::FACT;
+  extern __shared__ double smem[];
+  const int64_t e0 = (int64_t)blockIdx.x * kBlock;
+  const int64_t e = e0 + threadIdx.x;
+  if (e < m.nelems) {
+    Simplex<D> s;
+    simplex_geometry<D>(m, e, s);
+    const double adet = fabs(s.det);
+    // stiffness scale kd / (d! |det|); mass scale km |det| / d!
+    const double sd = coef_at(f.diff, e) / (FACT * adet);
+    const double sm = coef_at(f.mass, e) * (adet / FACT);
+    double gram[D + 1][D + 1];
+#pragma unroll
+    for (int a = 0; a <= D; ++a)
+#pragma unroll
+      for (int b = a; b <= D; ++b) gram[a][b] = dotc<D>(s.c[a], s.c[b]);
+    double* row = smem + threadIdx.x * (L + 1);
+#define G(a, b) ((a) <= (b) ? gram[a][b] : gram[b][a])
+#define KS(i, j, v) { const double _v = sd * (v); row[(i) * NB + (j)] = _v; row[(j) * NB + (i)] = _v; }
+#define KM(i, j, v) { const double _v = sm * (v); row[(i) * NB + (j)] += _v; if ((i) != (j)) row[(j) * NB + (i)] += _v; }
+    if constexpr (D == 2 && ORDER == 1) { TRI1_STIFF(G, KS); TRI1_MASS(KM); }
+    if constexpr (D == 2 && ORDER == 2) { TRI2_STIFF(G, KS); TRI2_MASS(KM); }
+    if constexpr (D == 3 && ORDER == 1) { TET1_STIFF(G, KS); TET1_MASS(KM); }
+    if constexpr (D == 3 && ORDER == 2) { TET2_STIFF(G, KS); TET2_MASS(KM); }
+#undef G
+#undef KS
+#undef KM
+  }
+  flush_rows<L>(smem, out, e0, m.nelems);
+}
+
+// -------------------------------------------- simplex, vector P2 (and P1)
+// K[(i a)(j b)] = sum_{p,q} BB[i][j][p][q] * E_pq[a][b]
+// E_pq[a][b] = s0 (lam c_p[a] c_q[b] + tr c_p[b] c_q[a] + lap delta_ab c_p.c_q),
+// s0 = 1/(d! |det|), E_qp = E_pq^T; plus mass delta_ab sm MM[i][j].
+// The element's 3 (or 2) rows of one scalar node are produced at a time
+// and streamed out through shared memory.
+template <int D, int ORDER>
+__global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBilinear f,
+                                                            double* __restrict__ out) {
+  constexpr int BS = 64;
+  constexpr int NS = SimplexTraits<D, ORDER>::NB;  // scalar functions
+  constexpr int NB = NS * D;                        // vector functions
+  constexpr int NV = D + 1;
+  constexpr int NPAIR = NV * (NV + 1) / 2;
+  constexpr int RB = D * NB;                        // values per node row block
+  constexpr double FACT = SimplexTraits<D, ORDER>::FACT;
+  extern __shared__ double smem[];
+  double* Es = smem;                                 // [NPAIR*D*D][BS]
+  double* rows = smem + NPAIR * D * D * BS;          // [BS][RB+1]
+  const int64_t e0 = (int64_t)blockIdx.x * BS;
+  const int64_t e = e0 + threadIdx.x;
+  const int tid = threadIdx.x;
+  const bool live = e < m.nelems;
+  double sm = 0.0;
+  if (live) {
+    Simplex<D> s;
+    simplex_geometry<D>(m, e, s);
+    const double adet = fabs(s.det);
+    const double s0 = 1.0 / (FACT * adet);
+    const double lam = coef_at(f.lam, e) * s0;
+    const double lap = coef_at(f.lap, e) * s0;
+    const double tr = coef_at(f.tr, e) * s0;
+    sm = coef_at(f.mass, e) * (adet / FACT);
+    int pq = 0;
+#pragma unroll
+    for (int p = 0; p < NV; ++p) {
+#pragma unroll
+      for (int q = p; q < NV; ++q) {
+        const double g = lap * dotc<D>(s.c[p], s.c[q]);
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+          for (int b = 0; b < D; ++b) {
+            double v = lam * (s.c[p][a] * s.c[q][b]) + tr * (s.c[p][b] * s.c[q][a]);
+            if (a == b) v = v + g;
+            Es[((pq * D + a) * D + b) * BS + tid] = v;
+          }
+        ++pq;
+      }
+    }
+  }
+  // pair index of (p, q), p <= q
+  auto pidx = [](int p, int q) { return p * NV - (p * (p - 1)) / 2 + (q - p); };
+#pragma unroll 1
+  for (int i = 0; i < NS; ++i) {
+    if (live) {
+      double* row = rows + tid * (RB + 1);
+#pragma unroll
+      for (int j = 0; j < NS; ++j) {
+        double blk[D][D];
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+          for (int b = 0; b < D; ++b) blk[a][b] = 0.0;
+#define T(p, q, c)                                                                   \
+  {                                                                                  \
+    const int _pp = (p) <= (q) ? (p) : (q), _qq = (p) <= (q) ? (q) : (p);            \
+    const int _k = pidx(_pp, _qq);                                                   \
+    _Pragma("unroll") for (int a = 0; a < D; ++a) _Pragma("unroll") for (int b = 0; b < D; ++b) { \
+      const double ev = (p) <= (q) ? Es[((_k * D + a) * D + b) * BS + tid]           \
+                                   : Es[((_k * D + b) * D + a) * BS + tid];          \
+      blk[a][b] = blk[a][b] + (c) * ev;                                              \
+    }                                                                                \
+  }
+        if constexpr (D == 3 && ORDER == 2) {
+          switch (i) {
+            case 0: TET2BB_ROW0(j, T); break;
+            case 1: TET2BB_ROW1(j, T); break;
+            case 2: TET2BB_ROW2(j, T); break;
+            case 3: TET2BB_ROW3(j, T); break;
+            case 4: TET2BB_ROW4(j, T); break;
+            case 5: TET2BB_ROW5(j, T); break;
+            case 6: TET2BB_ROW6(j, T); break;
+            case 7: TET2BB_ROW7(j, T); break;
+            case 8: TET2BB_ROW8(j, T); break;
+            case 9: TET2BB_ROW9(j, T); break;
+            default: break;
+          }
+        } else if constexpr (D == 2 && ORDER == 2) {
+          switch (i) {
+            case 0: TRI2BB_ROW0(j, T); break;
+            case 1: TRI2BB_ROW1(j, T); break;
+            case 2: TRI2BB_ROW2(j, T); break;
+            case 3: TRI2BB_ROW3(j, T); break;
+            case 4: TRI2BB_ROW4(j, T); break;
+            case 5: TRI2BB_ROW5(j, T); break;
+            default: break;
+          }
+        } else {
+          // P1: grad phi_i = grad lambda_i, BB[i][j][p][q] = delta_ip delta_jq
+          T(i, j, 1.0);
+        }
+#undef T
+        double mij = 0.0;
+        if constexpr (D == 3 && ORDER == 2) {
+#define KM(ii, jj, v) if (((ii) == i && (jj) == j) || ((ii) == j && (jj) == i)) mij = (v);
+          TET2_MASS(KM);
+#undef KM
+        } else if constexpr (D == 2 && ORDER == 2) {
+#define KM(ii, jj, v) if (((ii) == i && (jj) == j) || ((ii) == j && (jj) == i)) mij = (v);
+          TRI2_MASS(KM);
+#undef KM
+        } else if constexpr (D == 3) {
+#define KM(ii, jj, v) if (((ii) == i && (jj) == j) || ((ii) == j && (jj) == i)) mij = (v);
+          TET1_MASS(KM);
+#undef KM
+        } else {
+#define KM(ii, jj, v) if (((ii) == i && (jj) == j) || ((ii) == j && (jj) == i)) mij = (v);
+          TRI1_MASS(KM);
+#undef KM
+        }
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+          for (int b = 0; b < D; ++b) {
+            double v = blk[a][b];
+            if (a == b) v = v + sm * mij;
+            row[a * NB + j * D + b] = v;
+          }
+      }
+    }
+    // stream rows (i*D .. i*D+D-1) of every element of the block
+    __syncthreads();
+    const int64_t nb = ((m.nelems - e0) < (int64_t)BS ? (m.nelems - e0) : (int64_t)BS);
+    for (int64_t g = threadIdx.x; g < nb * RB; g += blockDim.x) {
+      const int el = (int)(g / RB);
+      const int k = (int)(g - (int64_t)el * RB);
+      out[(e0 + el) * (int64_t)(NB * NB) + (int64_t)i * RB + k] = rows[el * (RB + 1) + k];
+    }
+    __syncthreads();
+  }
+}
+
+// ----------------------------------------------------------- hexahedron Q1
+// Reference node k sits at corner c_hex_corner[k] (refdom.py:173-180);
+// phi_k = prod_ax f(c, x_ax) with f(1,t) = t, f(0,t) = 1 - t.
+struct Hex {
+  double x[8][3];
+};
+
+__device__ __forceinline__ void hex_load(const FemMesh& m, int64_t e, Hex& h) {
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+    const int64_t v = m.t[n * m.nelems + e];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) h.x[n][k] = m.p[k * m.nverts + v];
+  }
+}
+
+// Parallelepiped test: every node equals x7 + J c_n with J's columns the
+// edges from node 7 (corner 000) to nodes 4 (100), 5 (010), 6 (001).
+__device__ __forceinline__ bool hex_affine(const Hex& h, double J[3][3]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    J[k][0] = h.x[4][k] - h.x[7][k];
+    J[k][1] = h.x[5][k] - h.x[7][k];
+    J[k][2] = h.x[6][k] - h.x[7][k];
+  }
+  bool ok = true;
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double v = h.x[7][k];
+      if (c_hex_corner[n][0]) v = v + J[k][0];
+      if (c_hex_corner[n][1]) v = v + J[k][1];
+      if (c_hex_corner[n][2]) v = v + J[k][2];
+      ok = ok && (v == h.x[n][k]);
+    }
+  }
+  return ok;
+}
+
+// adj(J) (so that J^{-1} = adj / det), as mapping_isoparametric.py:216-224
+__device__ __forceinline__ double adj3(const double J[3][3], double ad[3][3]) {
+  ad[0][0] = -J[1][2] * J[2][1] + J[1][1] * J[2][2];
+  ad[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+  ad[2][0] = -J[1][1] * J[2][0] + J[1][0] * J[2][1];
+  ad[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+  ad[1][1] = -J[0][2] * J[2][0] + J[0][0] * J[2][2];
+  ad[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+  ad[0][2] = -J[0][2] * J[1][1] + J[0][1] * J[1][2];
+  ad[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+  ad[2][2] = -J[0][1] * J[1][0] + J[0][0] * J[1][1];
+  return J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+         J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+         J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+}
+
+// M = |det| J^{-1} J^{-T} = adj adj^T / |det|  (symmetric)
+__device__ __forceinline__ void hex_metric(const double ad[3][3], double det, double w,
+                                           double M[3][3]) {
+  const double s = w / fabs(det);
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int l = k; l < 3; ++l) {
+      const double v = s * (ad[k][0] * ad[l][0] + ad[k][1] * ad[l][1] + ad[k][2] * ad[l][2]);
+      M[k][l] = v;
+      M[l][k] = v;
+    }
+}
+
+__device__ __forceinline__ void hex_shape(double x, double y, double z, double phi[8],
+                                          double dphi[8][3]) {
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+    const int cx = c_hex_corner[n][0], cy = c_hex_corner[n][1], cz = c_hex_corner[n][2];
+    const double fx = cx ? x : 1.0 - x, fy = cy ? y : 1.0 - y, fz = cz ? z : 1.0 - z;
+    const double sx = cx ? 1.0 : -1.0, sy = cy ? 1.0 : -1.0, sz = cz ? 1.0 : -1.0;
+    phi[n] = fx * fy * fz;
+    dphi[n][0] = sx * (fy * fz);
+    dphi[n][1] = sy * (fx * fz);
+    dphi[n][2] = sz * (fx * fy);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) hex_scalar_kernel(FemMesh m, FemBilinear f,
+                                                            double* __restrict__ out,
+                                                            int32_t* __restrict__ status) {
+  constexpr int L = 64;
+  extern __shared__ double smem[];
+  const int64_t e0 = (int64_t)blockIdx.x * kBlock;
+  const int64_t e = e0 + threadIdx.x;
+  if (e < m.nelems) {
+    Hex h;
+    hex_load(m, e, h);
+    const double kd = coef_at(f.diff, e);
+    const double km = coef_at(f.mass, e);
+    double* row = smem + threadIdx.x * (L + 1);
+    double J[3][3];
+    if (hex_affine(h, J)) {
+      double ad[3][3];
+      const double det = adj3(J, ad);
+      if (det == 0.0) if (status) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
+      double M[3][3];
+      hex_metric(ad, det, kd, M);
+      const double sm = km * fabs(det);
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = i; j < 8; ++j) {
+          double v = 0.0;
+#pragma unroll
+          for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int l = 0; l < 3; ++l) v = v + M[k][l] * c_hex_S[k][l][i][j];
+          v = v + sm * c_hex_M[i][j];
+          row[i * 8 + j] = v;
+          row[j * 8 + i] = v;
+        }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 64; ++k) row[k] = 0.0;
+#pragma unroll 1
+      for (int qz = 0; qz < 4; ++qz)
+#pragma unroll 1
+        for (int qy = 0; qy < 4; ++qy)
+#pragma unroll 1
+          for (int qx = 0; qx < 4; ++qx) {
+            double phi[8], dphi[8][3];
+            hex_shape(c_gl4_x[qx], c_gl4_x[qy], c_gl4_x[qz], phi, dphi);
+            const double w = c_gl4_w[qx] * c_gl4_w[qy] * c_gl4_w[qz];
+            double Jq[3][3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+              for (int b = 0; b < 3; ++b) {
+                double acc = 0.0;
+#pragma unroll
+                for (int n = 0; n < 8; ++n) acc = acc + h.x[n][a] * dphi[n][b];
+                Jq[a][b] = acc;
+              }
+            double ad[3][3];
+            const double det = adj3(Jq, ad);
+            if (det == 0.0) {
+              if (status) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
+              continue;
+            }
+            double M[3][3];
+            hex_metric(ad, det, w * kd, M);
+            const double sm = w * km * fabs(det);
+            double hv[8][3];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+              for (int k = 0; k < 3; ++k)
+                hv[i][k] = M[k][0] * dphi[i][0] + M[k][1] * dphi[i][1] + M[k][2] * dphi[i][2];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+              for (int j = i; j < 8; ++j) {
+                const double v = hv[i][0] * dphi[j][0] + hv[i][1] * dphi[j][1] +
+                                 hv[i][2] * dphi[j][2] + sm * (phi[i] * phi[j]);
+                row[i * 8 + j] += v;
+              }
+          }
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < i; ++j) row[i * 8 + j] = row[j * 8 + i];
+    }
+  }
+  flush_rows<L>(smem, out, e0, m.nelems);
+}
+
+// ------------------------------------------------------------ load vectors
+template <int D, int ORDER>
+__global__ void simplex_load_kernel(FemMesh m, FemLinear f, int ncomp, double* __restrict__ out) {
+  constexpr int NS = SimplexTraits<D, ORDER>::NB;
+  constexpr double FACT = SimplexTraits<D, ORDER>::FACT;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.nelems) return;
+  double x[D + 1][D];
+#pragma unroll
+  for (int a = 0; a <= D; ++a) {
+    const int64_t v = m.t[a * m.nelems + e];
+#pragma unroll
+    for (int k = 0; k < D; ++k) x[a][k] = m.p[k * m.nverts + v];
+  }
+  double det;
+  if constexpr (D == 2) {
+    det = (x[1][0] - x[0][0]) * (x[2][1] - x[0][1]) - (x[2][0] - x[0][0]) * (x[1][1] - x[0][1]);
+  } else {
+    double A[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) A[i][j] = x[j + 1][i] - x[0][i];
+    det = A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) -
+          A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
+          A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
+  }
+  const double s = coef_at(f.load, e) * (fabs(det) / FACT);
+#pragma unroll
+  for (int i = 0; i < NS; ++i) {
+    double lv;
+    if constexpr (D == 2 && ORDER == 1) lv = tri1_load(i);
+    else if constexpr (D == 2) lv = tri2_load(i);
+    else if constexpr (ORDER == 1) lv = tet1_load(i);
+    else lv = tet2_load(i);
+    const double v = s * lv;
+    for (int c = 0; c < ncomp; ++c) out[e * (int64_t)(NS * ncomp) + i * ncomp + c] = v;
+  }
+}
+
+__global__ void hex_load_kernel(FemMesh m, FemLinear f, int ncomp, double* __restrict__ out,
+                                int32_t* __restrict__ status) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.nelems) return;
+  Hex h;
+  hex_load(m, e, h);
+  const double fe = coef_at(f.load, e);
+  double b[8];
+  double J[3][3];
+  if (hex_affine(h, J)) {
+    double ad[3][3];
+    const double det = adj3(J, ad);
+    if (det == 0.0) if (status) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
+    const double v = fe * fabs(det) * 0.125;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) b[i] = v;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) b[i] = 0.0;
+    for (int q = 0; q < 64; ++q) {
+      const int qx = q & 3, qy = (q >> 2) & 3, qz = q >> 4;
+      double phi[8], dphi[8][3];
+      hex_shape(c_gl4_x[qx], c_gl4_x[qy], c_gl4_x[qz], phi, dphi);
+      const double w = c_gl4_w[qx] * c_gl4_w[qy] * c_gl4_w[qz];
+      double Jq[3][3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb) {
+          double acc = 0.0;
+#pragma unroll
+          for (int n = 0; n < 8; ++n) acc = acc + h.x[n][a] * dphi[n][bb];
+          Jq[a][bb] = acc;
+        }
+      double ad[3][3];
+      const double det = adj3(Jq, ad);
+      if (det == 0.0) if (status) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
+      const double s = fe * w * fabs(det);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) b[i] = b[i] + s * phi[i];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    for (int c = 0; c < ncomp; ++c) out[e * (int64_t)(8 * ncomp) + i * ncomp + c] = b[i];
+}
+
+// ------------------------------------------------------------------ launch
+template <typename K>
+static int set_smem(K kernel, size_t bytes) {
+  if (bytes > 48 * 1024) {
+    cudaError_t err =
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (err != cudaSuccess) return fem::check_cuda(err, "cudaFuncSetAttribute");
+  }
+  return 0;
+}
+
+int local_matrices(const FemMesh& m, const FemBasis& b, const FemBilinear& f, double* out,
+                   int32_t* status, cudaStream_t st) {
+  if (m.nelems == 0) return 0;
+  const int fam = b.family;
+  const int64_t grid = fem::ceil_div(m.nelems, kBlock);
+  int rc = 0;
+  if (!b.vector) {
+    switch (fam) {
+#define LAUNCH_S(D, O)                                                                 \
+  {                                                                                    \
+    constexpr int NB = SimplexTraits<D, O>::NB;                                        \
+    const size_t sm = (size_t)kBlock * (NB * NB + 1) * sizeof(double);                 \
+    if ((rc = set_smem(simplex_scalar_kernel<D, O>, sm))) return rc;                   \
+    simplex_scalar_kernel<D, O><<<(unsigned)grid, kBlock, sm, st>>>(m, f, out);        \
+    break;                                                                             \
+  }
+      case FEM_TRI_P1: LAUNCH_S(2, 1)
+      case FEM_TRI_P2: LAUNCH_S(2, 2)
+      case FEM_TET_P1: LAUNCH_S(3, 1)
+      case FEM_TET_P2: LAUNCH_S(3, 2)
+#undef LAUNCH_S
+      case FEM_HEX_1: {
+        const size_t sm = (size_t)kBlock * 65 * sizeof(double);
+        if ((rc = set_smem(hex_scalar_kernel, sm))) return rc;
+        hex_scalar_kernel<<<(unsigned)grid, kBlock, sm, st>>>(m, f, out, status);
+        break;
+      }
+      default:
+        fem::set_error(FEM_ERR_UNSUPPORTED, "unsupported element family %d", fam);
+        return FEM_ERR_UNSUPPORTED;
+    }
+  } else {
+    const int64_t vgrid = fem::ceil_div(m.nelems, 64);
+    switch (fam) {
+#define LAUNCH_V(D, O)                                                                 \
+  {                                                                                    \
+    constexpr int NS = SimplexTraits<D, O>::NB, NB = NS * D, NV = D + 1;               \
+    constexpr int NPAIR = NV * (NV + 1) / 2, RB = D * NB;                              \
+    const size_t sm = ((size_t)NPAIR * D * D * 64 + (size_t)64 * (RB + 1)) * sizeof(double); \
+    if ((rc = set_smem(simplex_vector_kernel<D, O>, sm))) return rc;                   \
+    simplex_vector_kernel<D, O><<<(unsigned)vgrid, 64, sm, st>>>(m, f, out);           \
+    break;                                                                             \
+  }
+      case FEM_TRI_P1: LAUNCH_V(2, 1)
+      case FEM_TRI_P2: LAUNCH_V(2, 2)
+      case FEM_TET_P1: LAUNCH_V(3, 1)
+      case FEM_TET_P2: LAUNCH_V(3, 2)
+#undef LAUNCH_V
+      default:
+        fem::set_error(FEM_ERR_UNSUPPORTED,
+                       "vector bases are implemented for simplex P1/P2 families (got family %d)", fam);
+        return FEM_ERR_UNSUPPORTED;
+    }
+  }
+  FEM_LAUNCH_CHECK("local matrix kernel");
+  return 0;
+}
+
+int local_vectors(const FemMesh& m, const FemBasis& b, const FemLinear& f, double* out,
+                  int32_t* status, cudaStream_t st) {
+  if (m.nelems == 0) return 0;
+  const int ncomp = b.vector ? m.dim : 1;
+  const unsigned grid = (unsigned)fem::ceil_div(m.nelems, 128);
+  switch (b.family) {
+    case FEM_TRI_P1: simplex_load_kernel<2, 1><<<grid, 128, 0, st>>>(m, f, ncomp, out); break;
+    case FEM_TRI_P2: simplex_load_kernel<2, 2><<<grid, 128, 0, st>>>(m, f, ncomp, out); break;
+    case FEM_TET_P1: simplex_load_kernel<3, 1><<<grid, 128, 0, st>>>(m, f, ncomp, out); break;
+    case FEM_TET_P2: simplex_load_kernel<3, 2><<<grid, 128, 0, st>>>(m, f, ncomp, out); break;
+    case FEM_HEX_1: hex_load_kernel<<<grid, 128, 0, st>>>(m, f, ncomp, out, status); break;
+    default:
+      fem::set_error(FEM_ERR_UNSUPPORTED, "unsupported element family %d", b.family);
+      return FEM_ERR_UNSUPPORTED;
+  }
+  FEM_LAUNCH_CHECK("local vector kernel");
+  return 0;
+}
+
+}  // namespace FEM_NS

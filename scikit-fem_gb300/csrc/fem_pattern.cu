@@ -1,0 +1,544 @@
+// One-time CSR pattern build and the per-call fixed-order segmented sum.
+//
+// Replaces COOData._assemble_scipy_csr (skfem/assembly/form/coo_data.py:27-36):
+//   coo_matrix((data, (rows, cols))).eliminate_zeros().tocsr()
+// whose result is a canonical CSR (sorted column indices, duplicates summed)
+// in which a (row, col) pair exists iff at least one of its local entries is
+// nonzero -- eliminate_zeros drops exact +-0.0 local entries before the
+// duplicates are summed.  And COOData.toarray for load vectors
+// (coo_data.py:102-108).
+//
+// Build (once per mesh / basis / zero structure):
+//   1. row incidence: for every global row r the (element, local row) pairs
+//      that map to r, counted, scanned, filled and sorted so that every later
+//      summation runs in ascending (element, local row) order;
+//   2. per row, one warp gathers the candidate columns of its incidence
+//      entries whose local value is nonzero, sorts them in shared memory
+//      (bitonic), counts the unique ones (row length), and after a scan
+//      writes the column indices and, for each local entry, the offset of
+//      its column inside the row (the slot map).
+// Every call afterwards: one row group per CSR row walks the row's
+// incidence list in order and adds each local row into shared-memory
+// accumulators at the precomputed slots -- deterministic, no atomics.
+
+#include "fem_common.cuh"
+
+namespace fem {
+
+namespace {
+
+constexpr int kWarpsPerBlock = 4;
+
+__global__ void count_rows_kernel(const int32_t* __restrict__ dofs, int64_t nelems, int nb,
+                                  int64_t nrows, int32_t* __restrict__ cnt,
+                                  int32_t* __restrict__ err) {
+  const int64_t n = nelems * nb;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t r = dofs[idx];
+    if (r < 0 || r >= nrows) {
+      atomicOr(err, 1);
+      continue;
+    }
+    atomicAdd(&cnt[r], 1);
+  }
+}
+
+__global__ void fill_rows_kernel(const int32_t* __restrict__ dofs, int64_t nelems, int nb,
+                                 int64_t nrows, const int32_t* __restrict__ ptr,
+                                 int32_t* __restrict__ cursor, int32_t* __restrict__ inc) {
+  const int64_t n = nelems * nb;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t r = dofs[idx];
+    if (r < 0 || r >= nrows) continue;
+    const int64_t i = idx / nelems;
+    const int64_t e = idx - i * nelems;
+    const int32_t pos = ptr[r] + atomicAdd(&cursor[r], 1);
+    inc[pos] = (int32_t)(e * nb + i);
+  }
+}
+
+// Sort each row's incidence segment ascending (segments are short: the
+// number of cells sharing a DOF).
+__global__ void sort_segments_kernel(const int32_t* __restrict__ ptr, int64_t nrows,
+                                     int32_t* __restrict__ inc, int32_t* __restrict__ maxlen) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int32_t b = ptr[r], n = ptr[r + 1] - b;
+  int32_t* s = inc + b;
+  for (int k = 1; k < n; ++k) {
+    const int32_t v = s[k];
+    int m = k - 1;
+    while (m >= 0 && s[m] > v) {
+      s[m + 1] = s[m];
+      --m;
+    }
+    s[m + 1] = v;
+  }
+  atomicMax(maxlen, n);
+}
+
+// Bitonic sort of `n2` (power of two) int32 keys in shared memory by one warp.
+__device__ void warp_bitonic_sort(int32_t* a, int n2) {
+  const int lane = threadIdx.x & 31;
+  for (int k = 2; k <= n2; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < n2; i += 32) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const int32_t x = a[i], y = a[ixj];
+          const bool up = (i & k) == 0;
+          if ((x > y) == up) {
+            a[i] = y;
+            a[ixj] = x;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// Candidate columns of row r at fixed positions q*nu + j (masked: INT_MAX),
+// sorted copy in `srt`, original order in `cand`.  Returns unique count.
+__device__ int row_columns(int64_t r, const int32_t* __restrict__ inc_ptr,
+                           const int32_t* __restrict__ inc, const int32_t* __restrict__ udofs,
+                           const double* __restrict__ local, int64_t nelems, int nv, int nu,
+                           int cap, int32_t* cand, int32_t* srt) {
+  const int lane = threadIdx.x & 31;
+  const int32_t b = inc_ptr[r], len = inc_ptr[r + 1] - b;
+  const int n = len * nu;
+  int n2 = 1;
+  while (n2 < n) n2 <<= 1;
+  for (int k = lane; k < n2; k += 32) {
+    int32_t c = INT32_MAX;
+    if (k < n) {
+      const int q = k / nu, j = k - q * nu;
+      const int32_t code = inc[b + q];
+      const int64_t e = code / nv;
+      const int64_t i = code - e * nv;
+      const double v = local[(e * nv + i) * nu + j];
+      if (v != 0.0) c = udofs[(int64_t)j * nelems + e];
+    }
+    if (k < n) cand[k] = c;
+    srt[k] = c;
+  }
+  __syncwarp();
+  warp_bitonic_sort(srt, n2);
+  // unique count of the non-sentinel prefix
+  int cnt = 0;
+  for (int base = 0; base < n; base += 32) {
+    const int k = base + lane;
+    bool first = false;
+    if (k < n) {
+      const int32_t c = srt[k];
+      first = (c != INT32_MAX) && (k == 0 || srt[k - 1] != c);
+    }
+    cnt += __popc(__ballot_sync(0xffffffffu, first));
+  }
+  return cnt;
+}
+
+__global__ void row_nnz_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                               const int32_t* __restrict__ udofs, const double* __restrict__ local,
+                               int64_t nrows, int64_t nelems, int nv, int nu, int cap,
+                               int32_t* __restrict__ row_nnz, int32_t* __restrict__ maxnnz) {
+  extern __shared__ int32_t ismem[];
+  const int w = threadIdx.x >> 5;
+  int32_t* cand = ismem + (size_t)w * 2 * cap;
+  int32_t* srt = cand + cap;
+  for (int64_t r = (int64_t)blockIdx.x * kWarpsPerBlock + w; r < nrows;
+       r += (int64_t)gridDim.x * kWarpsPerBlock) {
+    const int cnt = row_columns(r, inc_ptr, inc, udofs, local, nelems, nv, nu, cap, cand, srt);
+    if ((threadIdx.x & 31) == 0) {
+      row_nnz[r] = cnt;
+      atomicMax(maxnnz, cnt);
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void row_fill_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                                const int32_t* __restrict__ udofs, const double* __restrict__ local,
+                                int64_t nrows, int64_t nelems, int nv, int nu, int cap,
+                                const int32_t* __restrict__ indptr, int32_t* __restrict__ indices,
+                                uint16_t* __restrict__ slot) {
+  extern __shared__ int32_t ismem[];
+  const int w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  int32_t* cand = ismem + (size_t)w * 2 * cap;
+  int32_t* srt = cand + cap;
+  for (int64_t r = (int64_t)blockIdx.x * kWarpsPerBlock + w; r < nrows;
+       r += (int64_t)gridDim.x * kWarpsPerBlock) {
+    row_columns(r, inc_ptr, inc, udofs, local, nelems, nv, nu, cap, cand, srt);
+    const int32_t b = inc_ptr[r], len = inc_ptr[r + 1] - b;
+    const int n = len * nu;
+    // compact unique columns to the front of srt (ballot-based stream compaction)
+    int out = 0;
+    for (int base = 0; base < n; base += 32) {
+      const int k = base + lane;
+      int32_t c = INT32_MAX;
+      bool first = false;
+      if (k < n) {
+        c = srt[k];
+        first = (c != INT32_MAX) && (k == 0 || srt[k - 1] != c);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, first);
+      __syncwarp();
+      if (first) {
+        const int pos = out + __popc(m & ((1u << lane) - 1u));
+        srt[pos] = c;  // pos <= k: never overwrites an unread element of this chunk
+      }
+      out += __popc(m);
+      __syncwarp();
+    }
+    const int32_t row0 = indptr[r];
+    for (int k = lane; k < out; k += 32) indices[row0 + k] = srt[k];
+    __syncwarp();
+    for (int k = lane; k < n; k += 32) {
+      const int32_t c = cand[k];
+      uint16_t s = 0xFFFF;
+      if (c != INT32_MAX) {
+        int lo = 0, hi = out - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (srt[mid] < c) lo = mid + 1;
+          else hi = mid;
+        }
+        s = (uint16_t)lo;
+      }
+      slot[(int64_t)b * nu + k] = s;
+    }
+    __syncwarp();
+  }
+}
+
+// Fixed-order segmented sum.  G lanes per row (G = power of two >= nu);
+// shared accumulators of `stride` doubles per row.
+template <int G>
+__global__ void csr_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                               const uint16_t* __restrict__ slot, const int32_t* __restrict__ indptr,
+                               const double* __restrict__ local, int64_t nrows, int nu, int stride,
+                               double* __restrict__ vals) {
+  extern __shared__ double acc_smem[];
+  constexpr int RPW = 32 / G;  // rows per warp
+  const int lane = threadIdx.x & 31;
+  const int sub = lane / G;      // row within warp
+  const int j = lane - sub * G;  // local column
+  const int wib = threadIdx.x >> 5;
+  double* acc = acc_smem + ((size_t)wib * RPW + sub) * stride;
+  const int64_t rows_per_block = (int64_t)(blockDim.x >> 5) * RPW;
+  for (int64_t rb = (int64_t)blockIdx.x * rows_per_block; rb < nrows;
+       rb += (int64_t)gridDim.x * rows_per_block) {
+    const int64_t r = rb + (int64_t)wib * RPW + sub;
+    const bool live = r < nrows;
+    int32_t b = 0, len = 0, p0 = 0, nnz = 0;
+    if (live) {
+      b = inc_ptr[r];
+      len = inc_ptr[r + 1] - b;
+      p0 = indptr[r];
+      nnz = indptr[r + 1] - p0;
+    }
+    for (int k = j; k < nnz; k += G) acc[k] = 0.0;
+    // longest incidence list in the warp
+    int maxlen = len;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
+    __syncwarp();
+    for (int q = 0; q < maxlen; ++q) {
+      if (q < len && j < nu) {
+        const int64_t code = inc[b + q];
+        const uint16_t s = slot[((int64_t)b + q) * nu + j];
+        if (s != 0xFFFF) acc[s] += local[code * nu + j];
+      }
+      __syncwarp();
+    }
+    for (int k = j; k < nnz; k += G) vals[p0 + k] = acc[k];
+    __syncwarp();
+  }
+}
+
+__global__ void vector_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                                  const double* __restrict__ local, int64_t nrows,
+                                  double* __restrict__ b) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int32_t p0 = inc_ptr[r], p1 = inc_ptr[r + 1];
+  double s = 0.0;
+  for (int32_t q = p0; q < p1; ++q) s += local[inc[q]];
+  b[r] = s;
+}
+
+__global__ void max_reduce_kernel(const int32_t* __restrict__ x, int64_t n, int32_t* out) {
+  int32_t m = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    m = max(m, x[i]);
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+int grid_for(int64_t n, int block) {
+  const int64_t g = ceil_div(n, block);
+  const int64_t cap = (int64_t)num_sms() * 32;
+  return (int)std::max<int64_t>(1, std::min(g, cap));
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------- scan
+// Exclusive scan, 1024 int32 per block (warp shuffles + one shared pass),
+// block totals scanned recursively, then added back.
+namespace {
+constexpr int kScanBlock = 1024;
+
+__global__ void scan_blocks_kernel(const int32_t* __restrict__ in, int32_t* __restrict__ out,
+                                   int64_t n, int32_t* __restrict__ sums) {
+  __shared__ int32_t wsum[32];
+  const int64_t i = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int32_t v = i < n ? in[i] : 0;
+  int32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int32_t s = wsum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    wsum[lane] = s;
+  }
+  __syncthreads();
+  const int32_t incl = x + (w > 0 ? wsum[w - 1] : 0);
+  if (i < n) out[i] = incl - v;
+  if (threadIdx.x == kScanBlock - 1) sums[blockIdx.x] = incl;
+}
+
+__global__ void scan_add_kernel(int32_t* __restrict__ out, int64_t n, const int32_t* __restrict__ offs) {
+  const int64_t i = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
+  if (i < n) out[i] += offs[blockIdx.x];
+}
+
+int scan_rec(const int32_t* in, int32_t* out, int64_t n, cudaStream_t st) {
+  const int64_t nb = ceil_div(n, kScanBlock);
+  int32_t *sums = nullptr, *offs = nullptr;
+  FEM_TRY_CUDA(cudaMallocAsync(&sums, nb * sizeof(int32_t), st));
+  FEM_TRY_CUDA(cudaMallocAsync(&offs, nb * sizeof(int32_t), st));
+  scan_blocks_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(in, out, n, sums);
+  FEM_LAUNCH_CHECK("scan_blocks_kernel");
+  if (nb > 1) {
+    int rc = scan_rec(sums, offs, nb, st);
+    if (rc) return rc;
+    scan_add_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(out, n, offs);
+    FEM_LAUNCH_CHECK("scan_add_kernel");
+  }
+  cudaFreeAsync(sums, st);
+  cudaFreeAsync(offs, st);
+  return 0;
+}
+}  // namespace
+
+int exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, int64_t* total,
+                       cudaStream_t stream) {
+  // out[0..n]: out[k] = sum(in[0..k)); out[n] = total.  `in` must hold n+1
+  // entries with in[n] == 0 (callers allocate counts with one spare slot).
+  if (n + 1 > INT32_MAX) {
+    set_error(FEM_ERR_CAPACITY, "scan of %lld entries exceeds int32", (long long)n);
+    return FEM_ERR_CAPACITY;
+  }
+  int rc = scan_rec(in, out, n + 1, stream);
+  if (rc) return rc;
+  if (total) {
+    int32_t t = 0;
+    FEM_TRY_CUDA(cudaMemcpyAsync(&t, out + n, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+    FEM_TRY_CUDA(cudaStreamSynchronize(stream));
+    *total = t;
+  }
+  return 0;
+}
+
+// Build row incidence of `dofs` (nb, nelems) over nrows rows.
+int build_incidence(const int32_t* dofs, int64_t nelems, int nb, int64_t nrows, Pattern* P,
+                    cudaStream_t st) {
+  P->nrows = nrows;
+  P->nelems = nelems;
+  P->nbfun_v = nb;
+  P->ninc = nelems * nb;
+  if (P->ninc >= INT32_MAX) {
+    set_error(FEM_ERR_CAPACITY, "nelems * nbfun = %lld exceeds int32 incidence codes",
+              (long long)P->ninc);
+    return FEM_ERR_CAPACITY;
+  }
+  int32_t *cnt = nullptr, *cursor = nullptr, *flags = nullptr;
+  FEM_TRY_CUDA(cudaMallocAsync(&P->inc_ptr, (nrows + 1) * sizeof(int32_t), st));
+  FEM_TRY_CUDA(cudaMallocAsync(&P->inc, std::max<int64_t>(1, P->ninc) * sizeof(int32_t), st));
+  FEM_TRY_CUDA(cudaMallocAsync(&cnt, (nrows + 1) * sizeof(int32_t), st));
+  FEM_TRY_CUDA(cudaMallocAsync(&cursor, (nrows + 1) * sizeof(int32_t), st));
+  FEM_TRY_CUDA(cudaMallocAsync(&flags, 2 * sizeof(int32_t), st));
+  FEM_TRY_CUDA(cudaMemsetAsync(cnt, 0, (nrows + 1) * sizeof(int32_t), st));
+  FEM_TRY_CUDA(cudaMemsetAsync(cursor, 0, (nrows + 1) * sizeof(int32_t), st));
+  FEM_TRY_CUDA(cudaMemsetAsync(flags, 0, 2 * sizeof(int32_t), st));
+  if (P->ninc > 0) {
+    count_rows_kernel<<<grid_for(P->ninc, 256), 256, 0, st>>>(dofs, nelems, nb, nrows, cnt, flags);
+    FEM_LAUNCH_CHECK("count_rows_kernel");
+  }
+  int64_t total = 0;
+  int rc = exclusive_scan_i32(cnt, P->inc_ptr, nrows, &total, st);
+  if (rc) return rc;
+  if (P->ninc > 0) {
+    fill_rows_kernel<<<grid_for(P->ninc, 256), 256, 0, st>>>(dofs, nelems, nb, nrows, P->inc_ptr,
+                                                             cursor, P->inc);
+    FEM_LAUNCH_CHECK("fill_rows_kernel");
+  }
+  if (nrows > 0) {
+    sort_segments_kernel<<<(unsigned)ceil_div(nrows, 128), 128, 0, st>>>(P->inc_ptr, nrows, P->inc,
+                                                                        flags + 1);
+    FEM_LAUNCH_CHECK("sort_segments_kernel");
+  }
+  int32_t h[2] = {0, 0};
+  FEM_TRY_CUDA(cudaMemcpyAsync(h, flags, sizeof(h), cudaMemcpyDeviceToHost, st));
+  FEM_TRY_CUDA(cudaStreamSynchronize(st));
+  cudaFreeAsync(cnt, st);
+  cudaFreeAsync(cursor, st);
+  cudaFreeAsync(flags, st);
+  if (h[0]) {
+    set_error(FEM_ERR_ARGUMENT, "element_dofs holds an index outside [0, %lld)", (long long)nrows);
+    return FEM_ERR_ARGUMENT;
+  }
+  if (total != P->ninc) {
+    set_error(FEM_ERR_ARGUMENT, "incidence count mismatch (%lld vs %lld)", (long long)total,
+              (long long)P->ninc);
+    return FEM_ERR_ARGUMENT;
+  }
+  P->max_row_inc = h[1];
+  return 0;
+}
+
+int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, Pattern* P,
+              cudaStream_t st) {
+  P->nbfun_u = nu;
+  const int nv = P->nbfun_v;
+  int cap = 1;
+  while (cap < P->max_row_inc * nu) cap <<= 1;
+  cap = std::max(cap, 32);
+  if (cap > 8192) {
+    set_error(FEM_ERR_CAPACITY,
+              "a row gathers %d candidate columns (limit 8192): the mesh has a DOF shared by "
+              "%d cells", P->max_row_inc * nu, P->max_row_inc);
+    return FEM_ERR_CAPACITY;
+  }
+  const size_t smem = (size_t)kWarpsPerBlock * 2 * cap * sizeof(int32_t);
+  if (smem > 48 * 1024) {
+    FEM_TRY_CUDA(cudaFuncSetAttribute(row_nnz_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    FEM_TRY_CUDA(cudaFuncSetAttribute(row_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  }
+  int32_t *row_nnz = nullptr, *flags = nullptr;
+  FEM_TRY_CUDA(cudaMallocAsync(&row_nnz, (P->nrows + 1) * sizeof(int32_t), st));
+  FEM_TRY_CUDA(cudaMallocAsync(&flags, sizeof(int32_t), st));
+  FEM_TRY_CUDA(cudaMemsetAsync(flags, 0, sizeof(int32_t), st));
+  FEM_TRY_CUDA(cudaMemsetAsync(row_nnz, 0, (P->nrows + 1) * sizeof(int32_t), st));
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(P->nrows, kWarpsPerBlock),
+                                                              (int64_t)num_sms() * 16));
+  if (P->nrows > 0) {
+    row_nnz_kernel<<<grid, 32 * kWarpsPerBlock, smem, st>>>(P->inc_ptr, P->inc, udofs, local,
+                                                           P->nrows, P->nelems, nv, nu, cap,
+                                                           row_nnz, flags);
+    FEM_LAUNCH_CHECK("row_nnz_kernel");
+  }
+  FEM_TRY_CUDA(cudaMallocAsync(&P->indptr, (P->nrows + 1) * sizeof(int32_t), st));
+  int64_t nnz = 0;
+  int rc = exclusive_scan_i32(row_nnz, P->indptr, P->nrows, &nnz, st);
+  if (rc) return rc;
+  int32_t maxnnz = 0;
+  FEM_TRY_CUDA(cudaMemcpyAsync(&maxnnz, flags, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  FEM_TRY_CUDA(cudaStreamSynchronize(st));
+  if (maxnnz > 0xFFFE) {
+    set_error(FEM_ERR_CAPACITY, "a CSR row has %d entries (limit 65534)", maxnnz);
+    return FEM_ERR_CAPACITY;
+  }
+  P->nnz = nnz;
+  P->max_row_nnz = maxnnz;
+  FEM_TRY_CUDA(cudaMallocAsync(&P->indices, std::max<int64_t>(1, nnz) * sizeof(int32_t), st));
+  FEM_TRY_CUDA(cudaMallocAsync(&P->slot, std::max<int64_t>(1, P->ninc * nu) * sizeof(uint16_t), st));
+  if (P->nrows > 0) {
+    row_fill_kernel<<<grid, 32 * kWarpsPerBlock, smem, st>>>(P->inc_ptr, P->inc, udofs, local,
+                                                            P->nrows, P->nelems, nv, nu, cap,
+                                                            P->indptr, P->indices, P->slot);
+    FEM_LAUNCH_CHECK("row_fill_kernel");
+  }
+  cudaFreeAsync(row_nnz, st);
+  cudaFreeAsync(flags, st);
+  FEM_TRY_CUDA(cudaStreamSynchronize(st));
+  (void)ncols;
+  P->has_matrix = true;
+  return 0;
+}
+
+int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st) {
+  if (!P.has_matrix) {
+    set_error(FEM_ERR_ARGUMENT, "pattern has no CSR structure (built without local matrices)");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (P.nrows == 0 || P.nnz == 0) return 0;
+  const int nu = P.nbfun_u;
+  const int stride = std::max(1, P.max_row_nnz);
+  const int threads = 128;
+  const int warps = threads / 32;
+  int rc = 0;
+  auto launch = [&](auto kern, int G) -> int {
+    const int rpw = 32 / G;
+    const size_t smem = (size_t)warps * rpw * stride * sizeof(double);
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return check_cuda(e, "csr_sum smem");
+    }
+    const int64_t rows_per_block = (int64_t)warps * rpw;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(P.nrows, rows_per_block),
+                                                                (int64_t)num_sms() * 64));
+    kern<<<grid, threads, smem, st>>>(P.inc_ptr, P.inc, P.slot, P.indptr, local, P.nrows, nu,
+                                      stride, vals);
+    return 0;
+  };
+  if (nu <= 2) rc = launch(csr_sum_kernel<2>, 2);
+  else if (nu <= 4) rc = launch(csr_sum_kernel<4>, 4);
+  else if (nu <= 8) rc = launch(csr_sum_kernel<8>, 8);
+  else if (nu <= 16) rc = launch(csr_sum_kernel<16>, 16);
+  else if (nu <= 32) rc = launch(csr_sum_kernel<32>, 32);
+  else {
+    set_error(FEM_ERR_UNSUPPORTED, "more than 32 local functions per cell (%d)", nu);
+    return FEM_ERR_UNSUPPORTED;
+  }
+  if (rc) return rc;
+  FEM_LAUNCH_CHECK("csr_sum_kernel");
+  return 0;
+}
+
+int vector_sum(const Pattern& P, const double* local, double* b, cudaStream_t st) {
+  if (P.nrows == 0) return 0;
+  vector_sum_kernel<<<(unsigned)ceil_div(P.nrows, 256), 256, 0, st>>>(P.inc_ptr, P.inc, local,
+                                                                     P.nrows, b);
+  FEM_LAUNCH_CHECK("vector_sum_kernel");
+  return 0;
+}
+
+void free_pattern(Pattern* P) {
+  if (!P) return;
+  cudaFree(P->inc_ptr);
+  cudaFree(P->inc);
+  cudaFree(P->indptr);
+  cudaFree(P->indices);
+  cudaFree(P->slot);
+  delete P;
+}
+
+}  // namespace fem

@@ -1,0 +1,87 @@
+"""In-tree build of libskfem_gb300.so for sm_103a (GB300).
+
+Four translation units compiled in parallel with one -gencode each; the
+local-matrix kernels are compiled twice: with FMA contraction (values) and
+with ``-fmad=false`` (the exact-zero mask of the pattern build).
+"""
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(ROOT, "csrc")
+OUT_DIR = os.path.join(PKG, "_lib")
+LIB = os.path.join(OUT_DIR, "libskfem_gb300.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+         "-Xptxas", "-warn-spills"]
+
+UNITS = [
+    ("fem_local.cu", "fem_local_fast.o", []),
+    ("fem_local.cu", "fem_local_exact.o", ["-DFEM_EXACT", "-fmad=false"]),
+    ("fem_pattern.cu", "fem_pattern.o", []),
+    ("fem_vjp.cu", "fem_vjp.o", []),
+    ("fem_batched.cu", "fem_batched.o", []),
+    ("fem_abi.cu", "fem_abi.o", []),
+]
+
+
+def nvcc():
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the skfem_gb300 CUDA library cannot be built")
+
+
+def _sources_newer_than(path):
+    if not os.path.exists(path):
+        return True
+    t = os.path.getmtime(path)
+    for f in os.listdir(CSRC):
+        if f.endswith((".cu", ".cuh", ".h")) and os.path.getmtime(os.path.join(CSRC, f)) > t:
+            return True
+    hdr = os.path.join(os.path.dirname(ROOT), "include", "skfem_gb300.h")
+    return os.path.exists(hdr) and os.path.getmtime(hdr) > t
+
+
+def build(force=False, verbose=False):
+    """Compile the CUDA library if any source changed; returns the .so path."""
+    if not force and not _sources_newer_than(LIB):
+        return LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    # regenerate the exact reference tensors (pure Python, fractions)
+    subprocess.run(["python3", os.path.join(CSRC, "gen_tables.py")], check=True,
+                   stdout=subprocess.DEVNULL)
+    cc = nvcc()
+    units = [u for u in UNITS if os.path.exists(os.path.join(CSRC, u[0]))]
+
+    def compile_unit(u):
+        src, obj, extra = u
+        cmd = [cc] + ARCH + FLAGS + extra + ["-c", os.path.join(CSRC, src), "-o",
+                                             os.path.join(OUT_DIR, obj)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr))
+        return r.stderr
+
+    with ThreadPoolExecutor(max_workers=len(units)) as ex:
+        logs = list(ex.map(compile_unit, units))
+    if verbose:
+        for l in logs:
+            if l.strip():
+                print(l)
+    tmp = LIB + ".tmp"
+    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + [os.path.join(OUT_DIR, u[1]) for u in units]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose=True))

@@ -1,0 +1,107 @@
+"""CellBasis: a mesh and an element resident on the GPU.
+
+Mirrors skfem/assembly/basis/cell_basis.py:42-106 and abstract_basis.py:45-88
+for the API a form needs (``N``, ``Nbfun``, ``nelems``, ``element_dofs``,
+``X``, ``W``, ``zero_w``, ``mesh``, ``elem``).  Unlike the reference it does
+not precompute basis values and gradients at every quadrature point: the
+kernels evaluate geometry and bases per element from the mesh arrays kept
+in HBM (``p``, ``t``, ``element_dofs``), uploaded once here.
+"""
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .dofs import Dofs
+from .mesh import as_mesh
+from .quadrature import get_quadrature
+
+__all__ = ["CellBasis", "Basis"]
+
+
+class CellBasis:
+    def __init__(self, mesh, elem, mapping=None, intorder=None, elements=None,
+                 quadrature=None, dofs=None, disable_doflocs=False, device=None):
+        mesh = as_mesh(mesh)
+        if mesh.refdom != elem.refdom:
+            raise ValueError("Incompatible Mesh and Element.")      # abstract_basis.py:55-56
+        if mapping is not None:
+            raise NotImplementedError("custom mappings are not supported; the kernels use the "
+                                      "mesh's own affine / isoparametric mapping")
+        if elements is not None:
+            raise NotImplementedError("element subsets are not implemented yet")
+        self.mesh = mesh
+        self.elem = elem
+        self.dofs = Dofs(mesh, elem) if dofs is None else dofs
+        self.Nbfun = self.dofs.element_dofs.shape[0]
+        self.nelems = mesh.nelements
+        self.tind = None
+        self.intorder = intorder if intorder is not None else 2 * elem.maxdeg
+        if quadrature is not None:
+            raise NotImplementedError("custom quadrature rules are not supported by the kernels")
+        self.X, self.W = get_quadrature(elem.refdom, self.intorder)
+        if elem.refdom == "hex" and self.X.shape[1] != 64:
+            # the isoparametric kernel integrates with the default 4x4x4 rule
+            raise NotImplementedError("ElementHex1 is assembled with the default 4x4x4 rule "
+                                      "(intorder 6 or 7)")
+        min_order = {1: 2, 2: 4}.get(elem.maxdeg, 0) if elem.refdom != "hex" else 0
+        if self.intorder < min_order:
+            raise NotImplementedError(
+                "intorder %d integrates the mass term of %s inexactly; the kernels integrate "
+                "exactly (intorder >= %d)" % (self.intorder, type(elem).__name__, min_order))
+        self.device = N.require_cuda(device)
+        self._patterns = {}
+        self._upload()
+
+    # -------------------------------------------------------------- device
+    def _upload(self):
+        dev = self.device
+        self.p_dev = torch.from_numpy(np.ascontiguousarray(self.mesh.p)).to(dev)
+        self.t_dev = torch.from_numpy(np.ascontiguousarray(self.mesh.t)).to(dev)
+        ed = self.dofs.element_dofs
+        if ed.shape == self.mesh.t.shape and np.array_equal(ed, self.mesh.t):
+            self.ed_dev = self.t_dev
+        else:
+            self.ed_dev = torch.from_numpy(np.ascontiguousarray(ed)).to(dev)
+        dim = self.mesh.p.shape[0]
+        self.c_mesh = N.FemMesh(dim, self.mesh.t.shape[0], self.mesh.p.shape[1],
+                                self.nelems, self.p_dev.data_ptr(), self.t_dev.data_ptr())
+        self.c_basis = N.FemBasis(N.FAMILY[self.elem.family], int(self.elem.vector),
+                                  self.Nbfun, 0, self.N, self.ed_dev.data_ptr())
+
+    def update_coordinates(self, p):
+        """Replace the node coordinates (same topology) -- used by shape
+        optimisation loops; patterns stay valid if the zero structure does."""
+        p = torch.as_tensor(p, dtype=torch.float64, device=self.device).contiguous()
+        if tuple(p.shape) != tuple(self.p_dev.shape):
+            raise ValueError("coordinate array has the wrong shape")
+        self.p_dev = p
+        self.c_mesh.p = p.data_ptr()
+
+    # ----------------------------------------------------------------- API
+    @property
+    def N(self):
+        return self.dofs.N
+
+    @property
+    def element_dofs(self):
+        return self.dofs.element_dofs
+
+    def zero_w(self, dtype=None):
+        """abstract_basis.py:378-382."""
+        return np.zeros((self.nelems, 0 if self.W is None else len(self.W)), dtype=dtype)
+
+    def zeros(self, dtype=None):
+        return np.zeros(self.N, dtype=dtype)
+
+    def quadrature(self):
+        return self.X, self.W
+
+    def default_parameters(self):
+        return {}
+
+    def __repr__(self):
+        return "CellBasis(%r, %r) on %s: %d DOFs" % (self.mesh, self.elem, self.device, self.N)
+
+
+Basis = CellBasis

@@ -1,0 +1,216 @@
+"""Meshes: the reference's data layout (p (dim, nverts) float64, t (nloc,
+nelems) int32) and the tensor-mesh constructors the workloads use.
+
+Node and cell numbering must match scikit-fem's for the CSR pattern to be
+bit-identical, so the constructors follow (in our own code):
+  MeshTri1.init_tensor   skfem/mesh/mesh_tri_1.py:31-80 (+ sort_t, :28)
+  MeshTet1.init_tensor   skfem/mesh/mesh_tet_1.py:327-393
+  MeshHex1.init_tensor   skfem/mesh/mesh_hex_1.py:98-155
+  Mesh.__post_init__     skfem/mesh/mesh.py:544-591 (sort_t, dtypes)
+  Mesh.build_entities    skfem/mesh/mesh.py:1065-1082 (edges / facets)
+"""
+
+import numpy as np
+
+__all__ = ["Mesh", "MeshTri", "MeshTri1", "MeshTet", "MeshTet1", "MeshHex", "MeshHex1",
+           "as_mesh"]
+
+# local vertex pairs of the entities, in the reference's order
+TRI_FACETS = np.array([[0, 1], [1, 2], [0, 2]])                           # refdom.py:60-62
+TET_EDGES = np.array([[0, 1], [1, 2], [0, 2], [0, 3], [1, 3], [2, 3]])    # refdom.py:101-106
+
+
+class Mesh:
+    """Base class: ``p`` (dim, nverts) float64 and ``t`` (nloc, nelems) int32."""
+
+    kind = ""
+    refdom = ""
+    affine = False
+    sort_t = False
+    nloc = 0
+
+    def __init__(self, doflocs, t, **kwargs):
+        p = np.ascontiguousarray(np.asarray(doflocs, dtype=np.float64))
+        t = np.asarray(t)
+        if self.sort_t:
+            t = np.sort(t, axis=0)
+        t = np.ascontiguousarray(t, dtype=np.int32)
+        if p.ndim != 2 or t.ndim != 2 or t.shape[0] != self.nloc:
+            raise ValueError("Mesh expects p (dim, nverts) and t (%d, nelems)" % self.nloc)
+        self.doflocs = p
+        self.t = t
+        self._entities = {}
+
+    @property
+    def p(self):
+        return self.doflocs
+
+    @property
+    def nelements(self):
+        return self.t.shape[1]
+
+    @property
+    def nvertices(self):
+        return int(self.t.max()) + 1 if self.t.size else 0
+
+    def dim(self):
+        return self.p.shape[0]
+
+    # ------------------------------------------------------------ entities
+    def _build(self, name, local_pairs):
+        if name not in self._entities:
+            t = self.t
+            a = t[local_pairs[:, 0]]
+            b = t[local_pairs[:, 1]]
+            lo = np.minimum(a, b).astype(np.int64).ravel()
+            hi = np.maximum(a, b).astype(np.int64).ravel()
+            # lexicographic (lo, hi) order == order of the scalar key lo*n + hi
+            n = max(self.nvertices, 1)
+            key = lo * n + hi
+            uk, inv = np.unique(key, return_inverse=True)
+            ent = np.vstack((uk // n, uk % n)).astype(np.int32)
+            self._entities[name] = (ent, inv.reshape(len(local_pairs), t.shape[1]).astype(np.int32))
+        return self._entities[name]
+
+    def __repr__(self):
+        return "%s(%d vertices, %d elements)" % (type(self).__name__, self.p.shape[1],
+                                                 self.nelements)
+
+
+class MeshTri1(Mesh):
+    """Triangular mesh (MeshTri1, mesh_tri_1.py:13-28): affine, sort_t."""
+
+    kind = refdom = "tri"
+    affine = True
+    sort_t = True
+    nloc = 3
+
+    def __init__(self, doflocs=None, t=None, **kwargs):
+        if doflocs is None:
+            doflocs = np.array([[0., 0.], [1., 0.], [0., 1.], [1., 1.]]).T
+            t = np.array([[0, 1, 2], [1, 3, 2]]).T
+        super().__init__(doflocs, t, **kwargs)
+
+    @property
+    def facets(self):
+        return self._build("facets", TRI_FACETS)[0]
+
+    @property
+    def t2f(self):
+        return self._build("facets", TRI_FACETS)[1]
+
+    @classmethod
+    def init_tensor(cls, x, y):
+        x = np.sort(np.asarray(x, dtype=np.float64))
+        y = np.sort(np.asarray(y, dtype=np.float64))
+        nx, ny = len(x), len(y)
+        # vertex (ix, iy) -> iy + ny*ix
+        p = np.vstack((np.repeat(x, ny), np.tile(y, nx)))
+        cx = np.repeat(np.arange(nx - 1), ny - 1)
+        cy = np.tile(np.arange(ny - 1), nx - 1)
+        v00 = cy + ny * cx
+        v01 = v00 + 1
+        v10 = v00 + ny
+        v11 = v10 + 1
+        t = np.hstack((np.vstack((v00, v01, v11)), np.vstack((v00, v10, v11))))
+        return cls(p, t)
+
+
+class MeshTet1(Mesh):
+    """Tetrahedral mesh (MeshTet1, mesh_tet_1.py:13-44): affine."""
+
+    kind = refdom = "tet"
+    affine = True
+    nloc = 4
+
+    def __init__(self, doflocs=None, t=None, **kwargs):
+        if doflocs is None:
+            doflocs = np.array([[0., 0., 0.], [0., 0., 1.], [0., 1., 0.], [1., 0., 0.],
+                                [0., 1., 1.], [1., 0., 1.], [1., 1., 0.], [1., 1., 1.]]).T
+            t = np.array([[0, 1, 2, 3], [3, 5, 1, 7], [2, 3, 6, 7], [2, 3, 1, 7],
+                          [1, 2, 4, 7]]).T
+        super().__init__(doflocs, t, **kwargs)
+
+    @property
+    def edges(self):
+        return self._build("edges", TET_EDGES)[0]
+
+    @property
+    def t2e(self):
+        return self._build("edges", TET_EDGES)[1]
+
+    @classmethod
+    def init_tensor(cls, x, y, z):
+        p, c = _box_cells(x, y, z)
+        t = np.hstack([c[[0, 1, 5, 7]], c[[0, 1, 4, 7]], c[[0, 2, 4, 7]],
+                       c[[0, 3, 5, 7]], c[[0, 2, 6, 7]], c[[0, 3, 6, 7]]])
+        return cls(p, t)
+
+
+class MeshHex1(Mesh):
+    """Trilinear hexahedral mesh (MeshHex1, mesh_hex_1.py:13-47): isoparametric."""
+
+    kind = refdom = "hex"
+    affine = False
+    nloc = 8
+
+    def __init__(self, doflocs=None, t=None, **kwargs):
+        if doflocs is None:
+            doflocs = np.array([[0., 0., 0.], [0., 0., 1.], [0., 1., 0.], [1., 0., 0.],
+                                [0., 1., 1.], [1., 0., 1.], [1., 1., 0.], [1., 1., 1.]]).T
+            t = np.array([[0, 1, 2, 3, 4, 5, 6, 7]]).T
+        super().__init__(doflocs, t, **kwargs)
+
+    @classmethod
+    def init_tensor(cls, x, y, z):
+        p, c = _box_cells(x, y, z)
+        return cls(p, c)
+
+
+def _box_cells(x, y, z):
+    """Vertices of a tensor grid and the 8 corners of every cell in the
+    reference's numbering: vertex (ix, iy, iz) -> iy + ny*ix + ny*nx*iz,
+    cell (cx, cy, cz) -> cy + (ny-1)*cx + (ny-1)*(nx-1)*cz."""
+    x = np.sort(np.asarray(x, dtype=np.float64))
+    y = np.sort(np.asarray(y, dtype=np.float64))
+    z = np.sort(np.asarray(z, dtype=np.float64))
+    nx, ny, nz = len(x), len(y), len(z)
+    iz, ix, iy = np.meshgrid(np.arange(nz), np.arange(nx), np.arange(ny), indexing="ij")
+    p = np.vstack((x[ix.ravel()], y[iy.ravel()], z[iz.ravel()]))
+    cz, cx, cy = np.meshgrid(np.arange(nz - 1), np.arange(nx - 1), np.arange(ny - 1),
+                             indexing="ij")
+    cx, cy, cz = cx.ravel(), cy.ravel(), cz.ravel()
+
+    def n(a, b, c):
+        return b + ny * a + ny * nx * c
+
+    corners = np.array([
+        n(cx, cy, cz), n(cx, cy + 1, cz), n(cx + 1, cy, cz), n(cx, cy, cz + 1),
+        n(cx + 1, cy + 1, cz), n(cx, cy + 1, cz + 1), n(cx + 1, cy, cz + 1),
+        n(cx + 1, cy + 1, cz + 1),
+    ])
+    return p, corners
+
+
+MeshTri = MeshTri1
+MeshTet = MeshTet1
+MeshHex = MeshHex1
+
+
+def as_mesh(m):
+    """Accept our meshes or any object with ``p``/``t`` arrays (e.g. a
+    scikit-fem mesh); the cell type is read from ``t``'s rows and the
+    dimension."""
+    if isinstance(m, Mesh):
+        return m
+    p, t = np.asarray(m.p), np.asarray(m.t)
+    kinds = {(2, 3): MeshTri1, (3, 4): MeshTet1, (3, 8): MeshHex1}
+    cls = kinds.get((p.shape[0], t.shape[0]))
+    if cls is None:
+        raise NotImplementedError("mesh with dim %d and %d vertices per cell is not supported"
+                                  % (p.shape[0], t.shape[0]))
+    out = cls.__new__(cls)
+    out.doflocs = np.ascontiguousarray(p, dtype=np.float64)
+    out.t = np.ascontiguousarray(t, dtype=np.int32)  # already sorted by its own class
+    out._entities = {}
+    return out

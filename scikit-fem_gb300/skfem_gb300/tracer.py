@@ -1,0 +1,308 @@
+"""Symbolic tracing of form callables.
+
+The reference evaluates a form callable on numpy ``DiscreteField`` arrays
+at every quadrature point (bilinear_form.py:150-151).  Here the callable is
+run once on symbolic stand-ins: ``u``/``v`` carry symbols for their values
+and derivatives and ``w.name`` yields a coefficient symbol.  Every symbol is
+a ``Sym`` -- a polynomial that is at most linear in the trial quantities and
+at most linear in the test quantities, whose coefficients are monomials in
+the named coefficient fields.  Helpers written with numpy (einsum on object
+arrays, as ``skfem.helpers`` does) trace unchanged.
+
+The traced polynomial is then matched to the kernel's coefficient channels
+(``FemBilinear`` / ``FemLinear`` in include/skfem_gb300.h); forms outside
+those families raise NotImplementedError rather than falling back.
+"""
+
+import numbers
+
+import numpy as np
+
+__all__ = ["Sym", "SymField", "trace_bilinear", "trace_linear", "bilinear_channels",
+           "linear_channels", "Poly"]
+
+REL = 1e-13
+
+
+class Poly(dict):
+    """{fields tuple (sorted names, with multiplicity): float coefficient}."""
+
+    def add(self, other, s=1.0):
+        out = Poly(self)
+        for k, v in other.items():
+            out[k] = out.get(k, 0.0) + s * v
+        return Poly({k: v for k, v in out.items() if v != 0.0})
+
+    def scaled(self, s):
+        return Poly({k: v * s for k, v in self.items() if v * s != 0.0})
+
+    def close(self, other):
+        keys = set(self) | set(other)
+        scale = max([abs(v) for v in self.values()] + [abs(v) for v in other.values()] + [0.0])
+        return all(abs(self.get(k, 0.0) - other.get(k, 0.0)) <= REL * scale for k in keys)
+
+    def is_zero(self):
+        return all(v == 0.0 for v in self.values())
+
+
+class Sym:
+    """Bilinear polynomial: {(uq, vq, fields): coef}; uq/vq are None, ('v', c)
+    (value of component c) or ('d', c, k) (derivative k of component c)."""
+
+    __slots__ = ("terms", "grad")
+    __array_ufunc__ = None
+
+    def __init__(self, terms=None):
+        self.terms = {} if terms is None else {k: v for k, v in terms.items() if v != 0.0}
+        self.grad = None
+
+    @staticmethod
+    def const(c):
+        return Sym({(None, None, ()): float(c)})
+
+    @staticmethod
+    def lift(o):
+        if isinstance(o, Sym):
+            return o
+        if isinstance(o, numbers.Number) or (isinstance(o, np.ndarray) and o.ndim == 0
+                                             and o.dtype != object):
+            return Sym.const(float(o))
+        if isinstance(o, np.ndarray) and o.ndim == 0:
+            return Sym.lift(o.item())
+        raise TypeError("cannot combine %r with a traced form quantity" % type(o))
+
+    # arithmetic --------------------------------------------------------
+    def _bcast(self, o, op):
+        return np.frompyfunc(lambda x: op(self, x), 1, 1)(o)
+
+    def __add__(self, o):
+        if isinstance(o, np.ndarray) and o.ndim > 0:
+            return self._bcast(o, Sym.__add__)
+        o = Sym.lift(o)
+        t = dict(self.terms)
+        for k, v in o.terms.items():
+            t[k] = t.get(k, 0.0) + v
+        return Sym(t)
+
+    __radd__ = __add__
+
+    def __neg__(self):
+        return Sym({k: -v for k, v in self.terms.items()})
+
+    def __pos__(self):
+        return self
+
+    def __sub__(self, o):
+        if isinstance(o, np.ndarray) and o.ndim > 0:
+            return self._bcast(o, Sym.__sub__)
+        return self + (-Sym.lift(o))
+
+    def __rsub__(self, o):
+        if isinstance(o, np.ndarray) and o.ndim > 0:
+            return self._bcast(o, Sym.__rsub__)
+        return Sym.lift(o) + (-self)
+
+    def __mul__(self, o):
+        if isinstance(o, np.ndarray) and o.ndim > 0:
+            return self._bcast(o, Sym.__mul__)
+        o = Sym.lift(o)
+        t = {}
+        for (u1, v1, f1), c1 in self.terms.items():
+            for (u2, v2, f2), c2 in o.terms.items():
+                if u1 is not None and u2 is not None:
+                    raise NotImplementedError("form is not linear in the trial function")
+                if v1 is not None and v2 is not None:
+                    raise NotImplementedError("form is not linear in the test function")
+                k = (u1 if u1 is not None else u2, v1 if v1 is not None else v2,
+                     tuple(sorted(f1 + f2)))
+                t[k] = t.get(k, 0.0) + c1 * c2
+        return Sym(t)
+
+    __rmul__ = __mul__
+
+    def __truediv__(self, o):
+        if isinstance(o, numbers.Number):
+            return self * (1.0 / o)
+        o = Sym.lift(o)
+        if set(o.terms) == {(None, None, ())}:
+            return self * (1.0 / o.terms[(None, None, ())])
+        raise NotImplementedError("division by a coefficient field is not supported")
+
+    def __pow__(self, n):
+        if not isinstance(n, numbers.Integral) or n < 0:
+            raise NotImplementedError("only non-negative integer powers are supported")
+        out = Sym.const(1.0)
+        for _ in range(n):
+            out = out * self
+        return out
+
+    def __repr__(self):
+        return "Sym(%r)" % self.terms
+
+    # numpy-compatible bits some helpers touch
+    @property
+    def shape(self):
+        return ()
+
+
+class SymField(np.ndarray):
+    """Object array of Syms with a ``grad`` attribute (vector fields)."""
+
+    def __new__(cls, value, grad=None):
+        obj = np.asarray(value, dtype=object).view(cls)
+        obj.grad = grad
+        return obj
+
+    def __array_finalize__(self, obj):
+        if obj is None:
+            return
+        self.grad = getattr(obj, "grad", None)
+
+
+def _field(which, elem, dim):
+    """Symbolic trial (which='u') or test (which='v') function."""
+    def q(*key):
+        if which == "u":
+            return Sym({(key, None, ()): 1.0})
+        return Sym({(None, key, ()): 1.0})
+
+    if not elem.vector:
+        s = q("v", 0)
+        s.grad = np.array([q("d", 0, k) for k in range(dim)], dtype=object)
+        return s
+    val = np.array([q("v", c) for c in range(dim)], dtype=object)
+    grad = np.array([[q("d", c, k) for k in range(dim)] for c in range(dim)], dtype=object)
+    return SymField(val, grad)
+
+
+class SymParams(dict):
+    """The ``w`` argument: coefficient fields become symbols, numbers pass."""
+
+    def __init__(self, fields, numbers_):
+        super().__init__()
+        for k in fields:
+            self[k] = Sym({(None, None, (k,)): 1.0})
+        for k, v in numbers_.items():
+            self[k] = v
+
+    def __getattr__(self, name):
+        if name in self:
+            return self[name]
+        self._missing(name)
+
+    def __getitem__(self, name):
+        if name in self.keys():
+            return dict.__getitem__(self, name)
+        self._missing(name)
+
+    @staticmethod
+    def _missing(name):
+        if name in ("x", "h"):
+            raise NotImplementedError(
+                "w.%s (quadrature-point %s) is not supported by the GPU kernels; pass "
+                "per-element coefficient arrays instead" % (name, "coordinates" if name == "x"
+                                                            else "mesh parameter"))
+        raise AttributeError("Attribute '{}' not found in 'w'.".format(name))
+
+
+def _scalarize(r):
+    if isinstance(r, np.ndarray):
+        if r.ndim != 0:
+            raise ValueError("form must return a scalar field (got shape %s)" % (r.shape,))
+        r = r.item()
+    return Sym.lift(r)
+
+
+def trace_bilinear(form, elem, dim, fields, numbers_):
+    u = _field("u", elem, dim)
+    v = _field("v", elem, dim)
+    return _scalarize(form(u, v, SymParams(fields, numbers_)))
+
+
+def trace_linear(form, elem, dim, fields, numbers_):
+    v = _field("v", elem, dim)
+    return _scalarize(form(v, SymParams(fields, numbers_)))
+
+
+def _poly_table(sym):
+    tab = {}
+    for (uq, vq, f), c in sym.terms.items():
+        tab.setdefault((uq, vq), Poly())
+        tab[(uq, vq)] = tab[(uq, vq)].add(Poly({f: c}))
+    return tab
+
+
+def bilinear_channels(sym, elem, dim):
+    """Map a traced bilinear form onto {diff, mass} (scalar) or
+    {lam, lap, tr, mass} (vector) coefficient polynomials."""
+    tab = _poly_table(sym)
+    for (uq, vq) in tab:
+        if uq is None or vq is None:
+            raise NotImplementedError("form has terms that are not bilinear in (u, v)")
+    zero = Poly()
+    get = lambda uq, vq: tab.get((uq, vq), zero)  # noqa: E731
+    used = set()
+    if not elem.vector:
+        diff = get(("d", 0, 0), ("d", 0, 0))
+        for k in range(dim):
+            for l in range(dim):
+                p = get(("d", 0, k), ("d", 0, l))
+                used.add((("d", 0, k), ("d", 0, l)))
+                ref = diff if k == l else zero
+                if not p.close(ref):
+                    raise NotImplementedError(
+                        "only isotropic diffusion k*dot(grad u, grad v) is implemented")
+        mass = get(("v", 0), ("v", 0))
+        used.add((("v", 0), ("v", 0)))
+        rest = set(tab) - used
+        if any(not tab[k].is_zero() for k in rest):
+            raise NotImplementedError("form has value-derivative (advection-type) terms")
+        return {"diff": diff, "mass": mass}
+    # vector: T[(b,k),(a,l)] for d_k u_b d_l v_a
+    if dim < 2:
+        raise NotImplementedError("vector forms need dim >= 2")
+    lam = get(("d", 0, 0), ("d", 1, 1))
+    lap = get(("d", 0, 1), ("d", 0, 1))
+    tr = get(("d", 0, 1), ("d", 1, 0))
+    for b in range(dim):
+        for k in range(dim):
+            for a in range(dim):
+                for l in range(dim):
+                    key = (("d", b, k), ("d", a, l))
+                    used.add(key)
+                    ref = zero
+                    if b == k and a == l:
+                        ref = ref.add(lam)
+                    if a == b and k == l:
+                        ref = ref.add(lap)
+                    if b == l and k == a:
+                        ref = ref.add(tr)
+                    if not get(*key).close(ref):
+                        raise NotImplementedError(
+                            "vector form is not of the isotropic form lam*div(u)div(v) + "
+                            "lap*ddot(grad u, grad v) + tr*ddot(grad u, grad v^T)")
+    mass = get(("v", 0), ("v", 0))
+    for a in range(dim):
+        for b in range(dim):
+            key = (("v", b), ("v", a))
+            used.add(key)
+            if not get(*key).close(mass if a == b else zero):
+                raise NotImplementedError("vector mass term must be c * dot(u, v)")
+    rest = set(tab) - used
+    if any(not tab[k].is_zero() for k in rest):
+        raise NotImplementedError("form has value-derivative (advection-type) terms")
+    return {"lam": lam, "lap": lap, "tr": tr, "mass": mass}
+
+
+def linear_channels(sym, elem, dim):
+    tab = _poly_table(sym)
+    for (uq, vq) in tab:
+        if uq is not None or vq is None:
+            raise NotImplementedError("linear form must be linear in v only")
+    if elem.vector:
+        raise NotImplementedError("linear forms on vector bases are not implemented")
+    load = tab.get((None, ("v", 0)), Poly())
+    rest = set(tab) - {(None, ("v", 0))}
+    if any(not tab[k].is_zero() for k in rest):
+        raise NotImplementedError("only f * v load forms are implemented")
+    return {"load": load}

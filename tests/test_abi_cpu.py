@@ -1,0 +1,39 @@
+"""CPU checks of the C ABI: the library builds for sm_103a, loads, and
+exports every function include/skfem_gb300.h declares (no compute calls)."""
+import ctypes
+
+from _util import header_functions
+
+
+def test_header_declares_entry_points():
+    fns = header_functions()
+    for f in ("fem_pattern_build", "fem_assemble", "fem_bilinear_vjp", "fem_last_error"):
+        assert f in fns
+
+
+def test_library_exports_every_declared_symbol():
+    from skfem_gb300 import _build
+    path = _build.build()
+    lib = ctypes.CDLL(path)
+    missing = [f for f in header_functions() if not hasattr(lib, f)]
+    assert not missing, missing
+    lib.fem_version.restype = ctypes.c_char_p
+    assert b"sm_103a" in lib.fem_version()
+    lib.fem_last_error.restype = ctypes.c_char_p
+    assert lib.fem_last_error() == b""
+
+
+def test_argument_errors_without_gpu():
+    """Validation happens on the host before any CUDA call."""
+    from skfem_gb300 import _build, _native as N
+    lib = ctypes.CDLL(_build.build())
+    lib.fem_last_error.restype = ctypes.c_char_p
+    m = N.FemMesh(2, 3, 4, 2, None, None)
+    b = N.FemBasis(N.FAMILY["TetP1"], 0, 4, 0, 4, None)  # 3-D element on a 2-D mesh
+    f = N.FemBilinear()
+    rc = lib.fem_local_matrices(ctypes.byref(m), ctypes.byref(b), ctypes.byref(f), None, None)
+    assert rc == N.FEM_ERR_ARGUMENT
+    assert b"Incompatible Mesh and Element" in lib.fem_last_error()
+    b = N.FemBasis(99, 0, 4, 0, 4, None)
+    rc = lib.fem_local_matrices(ctypes.byref(m), ctypes.byref(b), ctypes.byref(f), None, None)
+    assert rc == N.FEM_ERR_UNSUPPORTED

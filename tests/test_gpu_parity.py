@@ -1,0 +1,292 @@
+"""GPU parity: the CUDA path against scikit-fem's own results (golden
+fixtures made by tests/golden/make_golden.py) and against the CPU oracle on
+seeded inputs.  Bounds: CSR indptr/indices bit-exact, values within 1e-12
+relative Frobenius and 1e-13 * max|K| entrywise, load vectors the same,
+repeated runs bitwise identical."""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+import skfem_gb300 as F
+from skfem_gb300 import helpers as H
+from skfem_gb300.models.elasticity import linear_elasticity
+from skfem_gb300.models.poisson import laplace, mass, unit_load
+from _util import REL_FRO, REL_MAX, csr_diff, golden
+
+pytestmark = pytest.mark.gpu
+
+
+@F.BilinearForm
+def k_laplace_mass(u, v, w):
+    return w.k * H.dot(H.grad(u), H.grad(v)) + u * v
+
+
+@F.BilinearForm
+def k_laplace(u, v, w):
+    return w.k * H.dot(H.grad(u), H.grad(v))
+
+
+@F.BilinearForm
+def theta_laplace(u, v, w):
+    return w.theta * H.dot(H.grad(u), H.grad(v))
+
+
+@F.LinearForm
+def f_load(v, w):
+    return w.f * v
+
+
+MESH = {3: F.MeshTri, 4: F.MeshTet, 8: F.MeshHex}
+
+
+def basis_of(g, elem, intorder=None):
+    m = MESH[g["t"].shape[0]](g["p"], g["t"])
+    return F.Basis(m, elem, intorder=intorder)
+
+
+def check_matrix(K, g, pattern_exact=True):
+    same, extra, missing, noise, rf, rm = csr_diff(
+        K.indptr, K.indices, K.data, g["indptr"], g["indices"], g["data"], K.shape)
+    assert rf <= REL_FRO, rf
+    assert rm <= REL_MAX, rm
+    if pattern_exact:
+        assert same, "pattern differs: %d extra, %d missing, max |value| %.3g of max|K|" % (
+            extra, missing, noise)
+    else:
+        # entries present on one side only must be rounding noise of
+        # mathematically-zero local entries
+        assert noise <= REL_MAX, noise
+
+
+CASES = [
+    # name, element factory, form, kwargs builder, exact pattern expected
+    ("tri_default_mass", F.ElementTriP1, mass, lambda b, g: {}, True),
+    ("tri_p1_laplace", F.ElementTriP1, laplace, lambda b, g: {}, True),
+    ("tet_p1_k_laplace_mass", F.ElementTetP1, k_laplace_mass,
+     lambda b, g: {"k": b.zero_w() + g["k"][:, None]}, True),
+    ("tet_p1_jitter_laplace", F.ElementTetP1, laplace, lambda b, g: {}, True),
+    ("tri_p2_k_laplace", F.ElementTriP2, k_laplace,
+     lambda b, g: {"k": b.zero_w() + g["k"][:, None]}, True),
+    ("tet_p2_laplace", F.ElementTetP2, laplace, lambda b, g: {}, True),
+    ("tet_p2_vec_elasticity", lambda: F.ElementVector(F.ElementTetP2()),
+     linear_elasticity(1.0, 0.5), lambda b, g: {}, True),
+    ("hex1_theta_laplace", F.ElementHex1, theta_laplace,
+     lambda b, g: {"theta": b.zero_w() + g["theta"][:, None]}, True),
+    ("hex1_laplace_8", F.ElementHex1, laplace, lambda b, g: {}, True),
+]
+
+
+@pytest.mark.parametrize("name,elem,form,kw,exact", CASES, ids=[c[0] for c in CASES])
+def test_matrix_vs_reference_values(name, elem, form, kw, exact):
+    """Values within tolerance; entries present on one side only are noise."""
+    g = golden(name)
+    b = basis_of(g, elem(), intorder=4 if name == "tet_p2_vec_elasticity" else None)
+    K = form.assemble(b, **kw(b, g))
+    check_matrix(K, g, pattern_exact=False)
+
+
+@pytest.mark.parametrize("name,elem,form,kw,exact", CASES, ids=[c[0] for c in CASES])
+def test_matrix_vs_reference_pattern(name, elem, form, kw, exact):
+    """indptr / indices bit-exact against scikit-fem."""
+    g = golden(name)
+    b = basis_of(g, elem(), intorder=4 if name == "tet_p2_vec_elasticity" else None)
+    K = form.assemble(b, **kw(b, g))
+    check_matrix(K, g, pattern_exact=True)
+
+
+@pytest.mark.parametrize("name,elem,form,kw", [
+    ("tri_p1_laplace", F.ElementTriP1, unit_load, lambda b, g: {}),
+    ("tet_p1_k_laplace_mass", F.ElementTetP1, f_load, lambda b, g: {"f": b.zero_w() + g["k"][:, None]}),
+    ("tri_p2_k_laplace", F.ElementTriP2, unit_load, lambda b, g: {}),
+    ("tet_p2_laplace", F.ElementTetP2, unit_load, lambda b, g: {}),
+    ("hex1_theta_laplace", F.ElementHex1, f_load, lambda b, g: {"f": b.zero_w() + g["theta"][:, None]}),
+    ("hex1_laplace_8", F.ElementHex1, unit_load, lambda b, g: {}),
+])
+def test_load_vector_vs_reference(name, elem, form, kw):
+    g = golden(name)
+    b = basis_of(g, elem())
+    vec = form.assemble(b, **kw(b, g))
+    ref = g["b"]
+    assert np.linalg.norm(vec - ref) <= REL_FRO * np.linalg.norm(ref)
+    assert np.max(np.abs(vec - ref)) <= REL_MAX * np.max(np.abs(ref))
+
+
+def test_repeated_runs_bitwise_identical():
+    m = F.MeshTet.init_tensor(*(np.linspace(0, 1, 13),) * 3)
+    b = F.Basis(m, F.ElementTetP1())
+    k = np.random.default_rng(1).lognormal(0, 1, m.nelements)
+    kw = {"k": b.zero_w() + k[:, None]}
+    K1 = k_laplace_mass.assemble(b, **kw)
+    K2 = k_laplace_mass.assemble(b, **kw)
+    assert np.array_equal(K1.data, K2.data)
+    T = k_laplace_mass.assemble_torch(b, **kw)
+    assert torch.equal(T.values().cpu(), torch.from_numpy(K1.data))
+
+
+def _oracle_case(kind, n, elem_o, elem_p, seed, jitter=0.0):
+    rng = np.random.default_rng(seed)
+    if kind == "tri":
+        m = O.mesh_tri_tensor(np.linspace(0, 1, n + 1), np.linspace(0, 1, n + 1))
+    elif kind == "tet":
+        m = O.mesh_tet_tensor(*(np.linspace(0, 1, n + 1),) * 3)
+    else:
+        m = O.mesh_hex_tensor(*(np.linspace(0, 1, n + 1),) * 3)
+    if jitter:
+        p = m.p.copy()
+        inner = np.all((p > 1e-12) & (p < 1 - 1e-12), axis=0)
+        p[:, inner] += rng.uniform(-jitter / n, jitter / n, size=(p.shape[0], int(inner.sum())))
+        m = O.OMesh(p, m.t, m.kind)
+    bo = O.OBasis(m, elem_o)
+    bp = F.Basis(MESH[m.t.shape[0]](m.p, m.t), elem_p)
+    return m, bo, bp, rng
+
+
+@pytest.mark.parametrize("kind,n,eo,ep,jit", [
+    ("tri", 40, O.TriP1(), F.ElementTriP1(), 0.25),
+    ("tri", 24, O.TriP2(), F.ElementTriP2(), 0.25),
+    ("tet", 10, O.TetP1(), F.ElementTetP1(), 0.2),
+    ("tet", 5, O.TetP2(), F.ElementTetP2(), 0.2),
+    ("hex", 6, O.Hex1(), F.ElementHex1(), 0.2),
+])
+def test_k_laplace_mass_vs_oracle(kind, n, eo, ep, jit):
+    m, bo, bp, rng = _oracle_case(kind, n, eo, ep, 7, jit)
+    k = rng.lognormal(0, 1, m.nelements)
+    c = rng.uniform(0.5, 2.0, m.nelements)
+    Ko = O.bilinear_assemble(lambda u, v, w: w["k"] * O.dot(O.grad(u), O.grad(v))
+                             + w["c"] * (u * v), bo,
+                             k=bo.zero_w() + k[:, None], c=bo.zero_w() + c[:, None])
+
+    @F.BilinearForm
+    def form(u, v, w):
+        return w.k * H.dot(H.grad(u), H.grad(v)) + w.c * u * v
+
+    Kp = form.assemble(bp, k=bp.zero_w() + k[:, None], c=bp.zero_w() + c[:, None])
+    same, extra, missing, noise, rf, rm = csr_diff(Kp.indptr, Kp.indices, Kp.data, Ko.indptr,
+                                                   Ko.indices, Ko.data, Kp.shape)
+    assert same and rf <= REL_FRO and rm <= REL_MAX, (extra, missing, rf, rm)
+    bo_ = O.linear_assemble(O.f_load, bo, f=bo.zero_w() + k[:, None])
+    bp_ = f_load.assemble(bp, f=bp.zero_w() + k[:, None])
+    assert np.max(np.abs(bp_ - bo_)) <= REL_MAX * np.max(np.abs(bo_))
+
+
+def test_vector_elasticity_vs_oracle():
+    m, bo, bp, rng = _oracle_case("tet", 4, O.Vector(O.TetP2()),
+                                  F.ElementVector(F.ElementTetP2()), 3, 0.2)
+    Ko = O.bilinear_assemble(O.linear_elasticity(2.0, 0.7), bo)
+    Kp = linear_elasticity(2.0, 0.7).assemble(bp)
+    same, extra, missing, noise, rf, rm = csr_diff(Kp.indptr, Kp.indices, Kp.data, Ko.indptr,
+                                                   Ko.indices, Ko.data, Kp.shape)
+    assert rf <= REL_FRO and rm <= REL_MAX and noise <= REL_MAX, (rf, rm, noise)
+
+
+def test_hex1_adjoint_vs_reference_oracles():
+    """d(w^T K(theta, X) u)/d theta and /d X against Functional.elemental and
+    central differences (h = 1e-6) of the reference's assemble (4^3 cells)."""
+    from skfem_gb300.autodiff import assemble_vjp
+    g = golden("hex1_theta_laplace")
+    b = basis_of(g, F.ElementHex1())
+    theta = torch.tensor(g["theta"], device="cuda", requires_grad=True)
+    X = torch.tensor(g["p"], device="cuda", requires_grad=True)
+    w = torch.tensor(g["wv"], device="cuda")
+    u = torch.tensor(g["uv"], device="cuda")
+    J = assemble_vjp(theta_laplace, b, w, u, X=X, theta=theta)
+    J.backward()
+    np.testing.assert_allclose(theta.grad.cpu().numpy(), g["dtheta"], rtol=1e-12, atol=1e-14)
+    # FD reference has truncation + cancellation error ~1e-8 relative
+    dX = X.grad.cpu().numpy()
+    assert np.max(np.abs(dX - g["dX"])) <= 1e-6 * np.max(np.abs(g["dX"]))
+
+
+def test_hex1_load_adjoint_vs_fd():
+    from skfem_gb300.autodiff import assemble_linear_vjp
+    g = golden("hex1_theta_laplace")
+    b = basis_of(g, F.ElementHex1())
+    f = torch.tensor(g["theta"], device="cuda", requires_grad=True)
+    X = torch.tensor(g["p"], device="cuda", requires_grad=True)
+    w = torch.tensor(g["wv"], device="cuda")
+    J = assemble_linear_vjp(f_load, b, w, X=X, f=f)
+    J.backward()
+    dX = X.grad.cpu().numpy()
+    assert np.max(np.abs(dX - g["dXb"])) <= 1e-6 * np.max(np.abs(g["dXb"]))
+
+
+@pytest.mark.parametrize("kind,n,eo,ep", [
+    ("tri", 4, O.TriP1(), F.ElementTriP1()),
+    ("tri", 3, O.TriP2(), F.ElementTriP2()),
+    ("tet", 2, O.TetP1(), F.ElementTetP1()),
+    ("tet", 2, O.TetP2(), F.ElementTetP2()),
+    ("hex", 2, O.Hex1(), F.ElementHex1()),
+])
+def test_simplex_and_hex_adjoint_vs_fd(kind, n, eo, ep):
+    from skfem_gb300.autodiff import assemble_vjp
+    m, bo, bp, rng = _oracle_case(kind, n, eo, ep, 11, 0.2)
+    k = rng.uniform(0.5, 2.0, m.nelements)
+    c = rng.uniform(0.5, 2.0, m.nelements)
+    wv = rng.standard_normal(bo.N)
+    uv = rng.standard_normal(bo.N)
+
+    def form_o(u, v, w):
+        return w["k"] * O.dot(O.grad(u), O.grad(v)) + w["c"] * (u * v)
+
+    def J_of(p):
+        bb = O.OBasis(O.OMesh(p, m.t, m.kind), eo)
+        K = O.bilinear_assemble(form_o, bb, k=bb.zero_w() + k[:, None], c=bb.zero_w() + c[:, None])
+        return wv @ (K @ uv)
+
+    dX_fd = O.fd_x_gradient(J_of, m.p, 1e-6)
+
+    @F.BilinearForm
+    def form(u, v, w):
+        return w.k * H.dot(H.grad(u), H.grad(v)) + w.c * u * v
+
+    kt = torch.tensor(k, device="cuda", requires_grad=True)
+    ct = torch.tensor(c, device="cuda", requires_grad=True)
+    X = torch.tensor(m.p, device="cuda", requires_grad=True)
+    J = assemble_vjp(form, bp, torch.tensor(wv, device="cuda"), torch.tensor(uv, device="cuda"),
+                     X=X, k=kt, c=ct)
+    assert abs(J.item() - J_of(m.p)) <= 1e-12 * abs(J_of(m.p)) + 1e-14
+    J.backward()
+    assert np.max(np.abs(X.grad.cpu().numpy() - dX_fd)) <= 1e-6 * np.max(np.abs(dX_fd))
+    # coefficient gradients: exact (local quadratic forms)
+    dk = O.theta_gradient(O.laplace, bo, wv, uv)
+    dc = O.theta_gradient(O.mass, bo, wv, uv)
+    np.testing.assert_allclose(kt.grad.cpu().numpy(), dk, rtol=1e-11, atol=1e-13)
+    np.testing.assert_allclose(ct.grad.cpu().numpy(), dc, rtol=1e-11, atol=1e-13)
+
+
+def test_zero_jacobian_raises_like_reference():
+    """mapping_isoparametric.py:195-196: a degenerate hexahedron raises."""
+    p = np.array([[0., 0., 0.], [0., 0., 0.], [0., 1., 0.], [1., 0., 0.],
+                  [0., 1., 1.], [1., 0., 1.], [1., 1., 0.], [1., 1., 1.]]).T
+    p[:, 0] = p[:, 7]  # collapse a corner onto the opposite one
+    m = F.MeshHex(p, np.arange(8)[:, None])
+    b = F.Basis(m, F.ElementHex1())
+    with pytest.raises(Exception, match="Zero Jacobian determinant"):
+        laplace.assemble(b)
+
+
+def test_errors_match_reference_types():
+    b = F.Basis(F.MeshTri(), F.ElementTriP1())
+    with pytest.raises(ValueError):
+        k_laplace.assemble(b, k=np.zeros((b.nelems, 7)))     # quadrature mismatch
+    with pytest.raises(ValueError):
+        k_laplace.assemble(b, k=np.zeros(b.N + 1))            # wrong DOF-vector length
+    with pytest.raises(NotImplementedError):
+        F.BilinearForm(lambda u, v, w: u.grad[0] * v).assemble(b)
+
+
+def test_stale_pattern_is_rebuilt():
+    """A coefficient that becomes exactly zero removes entries, as
+    eliminate_zeros does in the reference."""
+    m = F.MeshTri.init_tensor(np.linspace(0, 1, 5), np.linspace(0, 1, 5))
+    b = F.Basis(m, F.ElementTriP1())
+    k = np.ones(m.nelements)
+    K1 = k_laplace.assemble(b, k=b.zero_w() + k[:, None])
+    k[:4] = 0.0
+    K2 = k_laplace.assemble(b, k=b.zero_w() + k[:, None])
+    bo = O.OBasis(O.OMesh(m.p, m.t, "tri"), O.TriP1())
+    Ko = O.bilinear_assemble(O.k_laplace, bo, k=bo.zero_w() + k[:, None])
+    assert K2.nnz < K1.nnz
+    np.testing.assert_array_equal(K2.indptr, Ko.indptr)
+    np.testing.assert_array_equal(K2.indices, Ko.indices)

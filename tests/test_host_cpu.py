@@ -1,0 +1,85 @@
+"""Host-side logic that needs no GPU: meshes, DOF numbering, quadrature and
+form tracing against the reference's fixtures and conventions."""
+import numpy as np
+import pytest
+
+import skfem_gb300 as F
+from skfem_gb300 import helpers as H
+from skfem_gb300.tracer import bilinear_channels, linear_channels, trace_bilinear, trace_linear
+from skfem_gb300.models.elasticity import linear_elasticity
+from _util import golden
+
+
+def test_tensor_meshes_and_dofs_match_reference():
+    g = golden("tri_p1_laplace")
+    m = F.MeshTri.init_tensor(np.linspace(0, 1, 17), np.linspace(0, 1, 17))
+    np.testing.assert_array_equal(m.p, g["p"])
+    np.testing.assert_array_equal(m.t, g["t"])
+    g = golden("tet_p1_k_laplace_mass")
+    m = F.MeshTet.init_tensor(*(np.linspace(0, 1, 7),) * 3)
+    np.testing.assert_array_equal(m.p, g["p"])
+    np.testing.assert_array_equal(m.t, g["t"])
+    g = golden("hex1_laplace_8")
+    m = F.MeshHex.init_tensor(*(np.linspace(0, 1, 9),) * 3)
+    np.testing.assert_array_equal(m.p, g["p"])
+    np.testing.assert_array_equal(m.t, g["t"])
+
+
+@pytest.mark.parametrize("name,elem", [
+    ("tet_p2_vec_elasticity", lambda: F.ElementVector(F.ElementTetP2())),
+    ("tet_p2_laplace", F.ElementTetP2),
+    ("tri_p2_k_laplace", F.ElementTriP2),
+    ("hex1_theta_laplace", F.ElementHex1),
+])
+def test_element_dofs_match_reference(name, elem):
+    g = golden(name)
+    kind = {3: F.MeshTri, 4: F.MeshTet, 8: F.MeshHex}[g["t"].shape[0]]
+    d = F.Dofs(kind(g["p"], g["t"]), elem())
+    np.testing.assert_array_equal(d.element_dofs, g["element_dofs"])
+
+
+@pytest.mark.parametrize("refdom,order,name", [
+    ("tri", 2, "tri_p1_laplace"), ("tri", 4, "tri_p2_k_laplace"),
+    ("tet", 2, "tet_p1_k_laplace_mass"), ("tet", 4, "tet_p2_vec_elasticity"),
+    ("hex", 6, "hex1_laplace_8")])
+def test_quadrature_matches_reference(refdom, order, name):
+    g = golden(name)
+    X, W = F.get_quadrature(refdom, order)
+    np.testing.assert_allclose(X, g["X"], rtol=0, atol=1e-15)
+    np.testing.assert_allclose(W, g["W"], rtol=0, atol=1e-15)
+
+
+def test_trace_scalar_forms():
+    e = F.ElementTetP1()
+    s = trace_bilinear(lambda u, v, w: w.k * H.dot(H.grad(u), H.grad(v)) + u * v, e, 3,
+                       {"k": None}, {})
+    assert bilinear_channels(s, e, 3) == {"diff": {("k",): 1.0}, "mass": {(): 1.0}}
+    s = trace_bilinear(lambda u, v, w: 2.0 * (u.grad[0] * v.grad[0] + u.grad[1] * v.grad[1]
+                                              + u.grad[2] * v.grad[2]), e, 3, {}, {})
+    assert bilinear_channels(s, e, 3)["diff"] == {(): 2.0}
+    s = trace_linear(lambda v, w: w.f * v, e, 3, {"f": None}, {})
+    assert linear_channels(s, e, 3) == {"load": {("f",): 1.0}}
+
+
+def test_trace_elasticity():
+    e = F.ElementVector(F.ElementTetP2())
+    ch = bilinear_channels(trace_bilinear(linear_elasticity(1.0, 0.5).form, e, 3, {}, {}), e, 3)
+    assert ch["lam"] == {(): 1.0} and ch["lap"] == {(): 0.5} and ch["tr"] == {(): 0.5}
+
+
+def test_trace_rejects_unsupported_forms():
+    e = F.ElementTetP1()
+    with pytest.raises(NotImplementedError):
+        bilinear_channels(trace_bilinear(lambda u, v, w: u.grad[0] * v, e, 3, {}, {}), e, 3)
+    with pytest.raises(NotImplementedError):
+        bilinear_channels(trace_bilinear(lambda u, v, w: u.grad[0] * v.grad[0], e, 3, {}, {}),
+                          e, 3)
+    with pytest.raises(NotImplementedError):
+        trace_bilinear(lambda u, v, w: u * u * v, e, 3, {}, {})
+    with pytest.raises(NotImplementedError):
+        trace_bilinear(lambda u, v, w: w.x[0] * u * v, e, 3, {}, {})
+
+
+def test_basis_rejects_mismatch_without_gpu():
+    with pytest.raises(ValueError):
+        F.Basis(F.MeshTri(), F.ElementTetP1())
