@@ -311,7 +311,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nodes", type=int, default=101, help="nodes per axis of the cube")
-    ap.add_argument("--cpu-nodes", type=int, default=41, help="nodes per axis of the CPU sample")
+    ap.add_argument("--cpu-nodes", type=int, default=61, help="nodes per axis of the CPU sample")
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
