@@ -162,6 +162,22 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
                  const FemPattern* pat, double* staging, double* csr_values, int32_t* status,
                  fem_stream_t stream);
 
+/*
+ * fem_assemble without any device allocation or scratch argument -- no
+ * counterpart in the reference.  For callers that can pass inputs and
+ * outputs but cannot allocate GPU memory (a framework that owns the
+ * device's memory behind its own allocator, or an application that forbids
+ * allocations after start-up).  The local-matrix staging lives in a 64 MiB
+ * file-scope device array that every GPU loading the library keeps until
+ * exit; meshes needing more (nelems * nbfun^2 * 8 bytes: TetP1 up to
+ * 524,288 cells) are rejected with FEM_ERR_CAPACITY.  The first call on a
+ * device looks up the array's device address (make it before any stream
+ * capture).  Calls share the array: calls that overlap on the GPU race.
+ */
+int fem_assemble_noalloc(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
+                         const FemPattern* pat, double* csr_values, int32_t* status,
+                         fem_stream_t stream);
+
 /* Segmented sum only (local matrices already in `local`). */
 int fem_csr_sum(const FemPattern* pat, const double* local, double* csr_values, int32_t* status,
                 fem_stream_t stream);

@@ -91,6 +91,13 @@ using fem::set_error;
 
 namespace fem {
 const Pattern* pattern_of(const FemPattern* h) { return h ? &h->P : nullptr; }
+const uint8_t* pattern_coef_bits(const FemPattern* h) { return h ? h->coef_bits : nullptr; }
+int coef_check(const FemBilinear& f, int64_t n, const uint8_t* ref, int32_t* status,
+               cudaStream_t st) {
+  coef_zero_bits_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(f, n, ref, nullptr, status);
+  FEM_LAUNCH_CHECK("coef_zero_bits_kernel");
+  return 0;
+}
 int new_pattern_handle(Pattern* P, FemPattern** out) {
   FemPattern* H = new FemPattern();
   H->P = *P;

@@ -27,6 +27,7 @@ UNITS = [
     ("fem_vjp.cu", "fem_vjp.o", []),
     ("fem_batched.cu", "fem_batched.o", []),
     ("fem_abi.cu", "fem_abi.o", []),
+    ("fem_noalloc.cu", "fem_noalloc.o", []),
 ]
 
 
