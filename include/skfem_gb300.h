@@ -105,6 +105,30 @@ typedef struct FemLinear {
   FemCoef load;
 } FemLinear;
 
+/*
+ * The form as a straight-line program in the reference's own operation
+ * order, for the exact-zero mask of the pattern build (see
+ * fem_pattern_build).  Instruction k computes register k:
+ *   op 0 CONST imm | 1 U a (trial quantity a) | 2 V a (test quantity a) |
+ *   3 COEF a (coefficient slot a) | 4 ADD a b | 5 SUB a b | 6 MUL a b |
+ *   7 DIV a b | 8 NEG a
+ * Quantity c is the value of component c, ncomp + c*dim + k the derivative
+ * k of component c (ncomp = dim for vector bases, 1 for scalar ones).
+ */
+typedef struct FemInstr {
+  int32_t op, a, b, pad_;
+  double imm;
+} FemInstr;
+
+typedef struct FemProgram {
+  int32_t ninstr;         /* <= 512 */
+  int32_t out;            /* register holding the integrand */
+  int32_t ncoef;          /* <= 8 */
+  int32_t nq;             /* quantity of quadrature points of the basis */
+  const FemInstr* ins;    /* device array of ninstr instructions */
+  const double* coef[8];  /* per-element coefficient fields (device) */
+} FemProgram;
+
 /* Opaque one-time structure: row incidence, CSR pattern, local-to-slot map. */
 typedef struct FemPattern FemPattern;
 
@@ -132,13 +156,19 @@ int fem_local_vectors(const FemMesh* mesh, const FemBasis* basis, const FemLinea
  * separately rounded products and sums (no fused multiply-add, as numpy
  * evaluates the reference's forms); local entries that come out exactly
  * +-0.0 create no CSR entry, as eliminate_zeros drops them before the
- * duplicates are summed.  The pattern also records which per-element
+ * duplicates are summed.  With `program` (may be NULL), the entries whose
+ * value is rounding noise of a mathematically-zero integral -- below 1e-9
+ * of their element's largest entry -- are re-evaluated with the reference's
+ * exact sequence of operations (its quadrature nodes, basis expressions,
+ * mapping formulas, the form's operation order, numpy's pairwise sum), so
+ * that the pattern keeps exactly the entries the reference keeps.  The
+ * pattern also records which per-element
  * coefficients were exactly zero, so that fem_assemble can report when the
  * zero structure changes.  form == NULL builds only the row incidence
  * (enough for load vectors).  Synchronises `stream`.
  */
 int fem_pattern_build(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
-                      FemPattern** out, fem_stream_t stream);
+                      const FemProgram* program, FemPattern** out, fem_stream_t stream);
 
 /* Sizes: nnz of the CSR pattern, number of rows (N), and the bytes of the
  * local-matrix staging buffer fem_assemble needs. */

@@ -24,6 +24,8 @@ int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, 
 int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st);
 int vector_sum(const Pattern& P, const double* local, double* b, cudaStream_t st);
 void free_pattern(Pattern* P);
+int faithful_mask(const FemMesh& m, const FemBasis& b, const FemProgram& prog, int nq, double* local,
+                  int32_t* status, cudaStream_t st);
 
 namespace {
 thread_local std::string g_err;
@@ -153,6 +155,11 @@ static int read_status(int32_t* dstatus, cudaStream_t st) {
     set_error(FEM_ERR_ZERO_JACOBIAN, "Zero Jacobian determinant");
     return FEM_ERR_ZERO_JACOBIAN;
   }
+  if (h & (1 << FEM_ERR_UNSUPPORTED)) {
+    set_error(FEM_ERR_UNSUPPORTED, "the exact-zero mask has no reference rule for this basis's "
+              "quadrature");
+    return FEM_ERR_UNSUPPORTED;
+  }
   return 0;
 }
 
@@ -185,7 +192,7 @@ int fem_local_vectors(const FemMesh* mesh, const FemBasis* basis, const FemLinea
 }
 
 int fem_pattern_build(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
-                      FemPattern** out, fem_stream_t stream) {
+                      const FemProgram* program, FemPattern** out, fem_stream_t stream) {
   int rc = validate(mesh, basis);
   if (rc) return rc;
   if (!out) {
@@ -216,6 +223,7 @@ int fem_pattern_build(const FemMesh* mesh, const FemBasis* basis, const FemBilin
     if (e1 != cudaSuccess) return fail(fem::check_cuda(e1, "cudaMallocAsync(status)"));
     cudaMemsetAsync(dstatus, 0, sizeof(int32_t), st);
     rc = fem_exact::local_matrices(*mesh, *basis, *form, local, dstatus, st);
+    if (!rc && program) rc = fem::faithful_mask(*mesh, *basis, *program, program->nq, local, dstatus, st);
     if (!rc) rc = read_status(dstatus, st);
     if (!rc) rc = fem::build_csr(basis->element_dofs, nb, basis->ndofs, local, &H->P, st);
     if (!rc && mesh->nelems > 0) {

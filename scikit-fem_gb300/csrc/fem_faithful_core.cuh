@@ -1,0 +1,272 @@
+// Host/device core of the exact-zero mask (see fem_faithful.cu): the
+// reference's basis expressions, mapping formulas, quadrature sum and the
+// form-program interpreter, in separately rounded IEEE double arithmetic.
+// Compile with -fmad=false (device) and without FMA contraction (host).
+#pragma once
+
+#include <cmath>
+#include <stdint.h>
+
+#include "../../include/skfem_gb300.h"
+
+#ifdef __CUDACC__
+#define FEM_HD __host__ __device__
+#else
+#define FEM_HD
+#endif
+
+namespace fem_faithful {
+
+constexpr int kMaxProgram = 512;
+
+using Instr = FemInstr;
+
+enum { OP_CONST = 0, OP_U, OP_V, OP_COEF, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG };
+
+// ----------------------------------------------------------- reference bases
+FEM_HD void lbasis(int family, int i, double x, double y, double z, double& phi,
+                       double d[3]) {
+  d[0] = d[1] = d[2] = 0.0;
+  switch (family) {
+    case FEM_TRI_P1:
+      if (i == 0) { phi = (1. - x) - y; d[0] = -1. + 0. * x; d[1] = -1. + 0. * x; }
+      else if (i == 1) { phi = x; d[0] = 1. + 0. * x; d[1] = 0. * x; }
+      else { phi = y; d[0] = 0. * x; d[1] = 1. + 0. * x; }
+      return;
+    case FEM_TET_P1:
+      if (i == 0) { phi = ((1 - x) - y) - z; d[0] = d[1] = d[2] = -1 + 0 * x; }
+      else if (i == 1) { phi = x; d[0] = 1 + 0 * x; d[1] = 0 * x; d[2] = 0 * x; }
+      else if (i == 2) { phi = y; d[0] = 0 * x; d[1] = 1 + 0 * x; d[2] = 0 * x; }
+      else { phi = z; d[0] = 0 * x; d[1] = 0 * x; d[2] = 1 + 0 * x; }
+      return;
+    case FEM_TRI_P2:
+      switch (i) {
+        case 0:
+          phi = ((((1. - 3. * x) - 3. * y) + 2. * (x * x)) + (4. * x) * y) + 2. * (y * y);
+          d[0] = (-3 + 4. * x) + 4. * y;
+          d[1] = (-3 + 4. * x) + 4. * y;
+          return;
+        case 1: phi = 2. * (x * x) - x; d[0] = 4. * x - 1; d[1] = 0. * x; return;
+        case 2: phi = 2. * (y * y) - y; d[0] = 0. * x; d[1] = 4. * y - 1; return;
+        case 3:
+          phi = (4. * x - 4. * (x * x)) - (4. * x) * y;
+          d[0] = (4 - 8. * x) - 4. * y;
+          d[1] = -4. * x;
+          return;
+        case 4: phi = (4. * x) * y; d[0] = 4. * y; d[1] = 4. * x; return;
+        default:
+          phi = (4. * y - (4. * x) * y) - 4. * (y * y);
+          d[0] = -4. * y;
+          d[1] = (4 - 4. * x) - 8. * y;
+          return;
+      }
+    case FEM_TET_P2:
+      switch (i) {
+        case 0: {
+          phi = ((((((((1. - 3. * x) + 2. * (x * x)) - 3. * y) + (4. * x) * y) + 2. * (y * y)) -
+                   3. * z) + (4. * x) * z) + (4. * y) * z) + 2. * (z * z);
+          const double g = ((-3. + 4. * x) + 4. * y) + 4. * z;
+          d[0] = d[1] = d[2] = g;
+          return;
+        }
+        case 1: phi = -1. * x + 2. * (x * x); d[0] = -1 + 4 * x; d[1] = 0 * x; d[2] = 0 * x; return;
+        case 2: phi = -1. * y + 2. * (y * y); d[0] = 0 * x; d[1] = -1. + 4. * y; d[2] = 0 * x; return;
+        case 3: phi = -1. * z + 2. * (z * z); d[0] = 0 * x; d[1] = 0 * x; d[2] = -1. + 4. * z; return;
+        case 4:
+          phi = ((4. * x - 4. * (x * x)) - (4. * x) * y) - (4 * x) * z;
+          d[0] = ((4. - 8. * x) - 4. * y) - 4. * z;
+          d[1] = -4. * x;
+          d[2] = -4. * x;
+          return;
+        case 5: phi = (4. * x) * y; d[0] = 4. * y; d[1] = 4. * x; d[2] = 0 * x; return;
+        case 6:
+          phi = (((0. + 4. * y) - (4. * x) * y) - 4. * (y * y)) - (4. * y) * z;
+          d[0] = -4. * y;
+          d[1] = ((4. - 4. * x) - 8. * y) - 4. * z;
+          d[2] = -4. * y;
+          return;
+        case 7:
+          phi = (((0. + 4. * z) - (4. * x) * z) - (4. * y) * z) - 4. * (z * z);
+          d[0] = -4. * z;
+          d[1] = -4. * z;
+          d[2] = ((4. - 4. * x) - 4. * y) - 8. * z;
+          return;
+        case 8: phi = 0. + (4. * x) * z; d[0] = 4. * z; d[1] = 0 * x; d[2] = 4 * x; return;
+        default: phi = 0. + (4. * y) * z; d[0] = 0 * x; d[1] = 4 * z; d[2] = 4 * y; return;
+      }
+    case FEM_HEX_1:
+      switch (i) {
+        case 0: phi = (x * y) * z; d[0] = y * z; d[1] = x * z; d[2] = x * y; return;
+        case 1: phi = (x * y) * (1 - z); d[0] = y * (1 - z); d[1] = x * (1 - z); d[2] = (-x) * y; return;
+        case 2: phi = (x * (1 - y)) * z; d[0] = (1 - y) * z; d[1] = (-x) * z; d[2] = x * (1 - y); return;
+        case 3: phi = ((1 - x) * y) * z; d[0] = (-y) * z; d[1] = (1 - x) * z; d[2] = (1 - x) * y; return;
+        case 4:
+          phi = (x * (1 - y)) * (1 - z);
+          d[0] = (1 - y) * (1 - z); d[1] = (-x) * (1 - z); d[2] = (-x) * (1 - y);
+          return;
+        case 5:
+          phi = ((1 - x) * y) * (1 - z);
+          d[0] = (-y) * (1 - z); d[1] = (1 - x) * (1 - z); d[2] = (-(1 - x)) * y;
+          return;
+        case 6:
+          phi = ((1 - x) * (1 - y)) * z;
+          d[0] = (-(1 - y)) * z; d[1] = (-(1 - x)) * z; d[2] = (1 - x) * (1 - y);
+          return;
+        default:
+          phi = ((1 - x) * (1 - y)) * (1 - z);
+          d[0] = (-(1 - y)) * (1 - z); d[1] = (-(1 - x)) * (1 - z); d[2] = (-(1 - x)) * (1 - y);
+          return;
+      }
+    default:
+      phi = 0.0;
+      return;
+  }
+}
+
+// ------------------------------------------------------ reference quadrature
+struct Rule {
+  const double* X;  // (dim, nq) row-major
+  const double* W;
+  int nq;
+};
+
+// numpy's pairwise summation for n <= 128 (as measured on the reference's
+// platform: sequential below 8 terms, else eight accumulators)
+FEM_HD double np_pairwise_sum(const double* a, int n) {
+  if (n < 8) {
+    double res = -0.0;
+    for (int i = 0; i < n; ++i) res = res + a[i];
+    return res;
+  }
+  double r[8];
+  for (int j = 0; j < 8; ++j) r[j] = a[j];
+  int i = 8;
+  for (; i < n - (n % 8); i += 8)
+    for (int j = 0; j < 8; ++j) r[j] = r[j] + a[i + j];
+  double res = ((r[0] + r[1]) + (r[2] + r[3])) + ((r[4] + r[5]) + (r[6] + r[7]));
+  for (; i < n; ++i) res = res + a[i];
+  return res;
+}
+
+// ---------------------------------------------------------------- mappings
+template <int D>
+FEM_HD void affine_inverse(const FemMesh& m, int64_t e, double inv[3][3], double& det) {
+  double A[3][3];
+  for (int i = 0; i < D; ++i)
+    for (int j = 0; j < D; ++j)
+      A[i][j] = m.p[i * m.nverts + m.t[(j + 1) * m.nelems + e]] - m.p[i * m.nverts + m.t[e]];
+  if (D == 2) {
+    det = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+    inv[0][0] = A[1][1] / det;
+    inv[0][1] = (-A[0][1]) / det;
+    inv[1][0] = (-A[1][0]) / det;
+    inv[1][1] = A[0][0] / det;
+  } else {
+    det = (A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) -
+           A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0])) +
+          A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
+    inv[0][0] = ((-A[1][2]) * A[2][1] + A[1][1] * A[2][2]) / det;
+    inv[1][0] = (A[1][2] * A[2][0] - A[1][0] * A[2][2]) / det;
+    inv[2][0] = ((-A[1][1]) * A[2][0] + A[1][0] * A[2][1]) / det;
+    inv[0][1] = (A[0][2] * A[2][1] - A[0][1] * A[2][2]) / det;
+    inv[1][1] = ((-A[0][2]) * A[2][0] + A[0][0] * A[2][2]) / det;
+    inv[2][1] = (A[0][1] * A[2][0] - A[0][0] * A[2][1]) / det;
+    inv[0][2] = ((-A[0][2]) * A[1][1] + A[0][1] * A[1][2]) / det;
+    inv[1][2] = (A[0][2] * A[1][0] - A[0][0] * A[1][2]) / det;
+    inv[2][2] = ((-A[0][1]) * A[1][0] + A[0][0] * A[1][1]) / det;
+  }
+}
+
+FEM_HD void hex_inverse(const FemMesh& m, int64_t e, double x, double y, double z,
+                            double inv[3][3], double& det) {
+  double J[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) J[i][j] = 0.0;
+  for (int itr = 0; itr < 8; ++itr) {
+    double phi, d[3];
+    lbasis(FEM_HEX_1, itr, x, y, z, phi, d);
+    const int64_t v = m.t[itr * m.nelems + e];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) J[i][j] = J[i][j] + m.p[i * m.nverts + v] * d[j];
+  }
+  det = (J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+         J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0])) +
+        J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+  inv[0][0] = ((-J[1][2]) * J[2][1] + J[1][1] * J[2][2]) / det;
+  inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+  inv[2][0] = ((-J[1][1]) * J[2][0] + J[1][0] * J[2][1]) / det;
+  inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+  inv[1][1] = ((-J[0][2]) * J[2][0] + J[0][0] * J[2][2]) / det;
+  inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+  inv[0][2] = ((-J[0][2]) * J[1][1] + J[0][1] * J[1][2]) / det;
+  inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+  inv[2][2] = ((-J[0][1]) * J[1][0] + J[0][0] * J[1][1]) / det;
+}
+
+// quantities of local function `fn` at a point: q[c] values, q[ncomp + c*D + k] derivatives
+template <int D>
+FEM_HD void quantities(int family, bool vec, int fn, double x, double y, double z,
+                           const double inv[3][3], double* q) {
+  const int sfn = vec ? fn / D : fn;
+  const int comp = vec ? fn % D : 0;
+  const int ncomp = vec ? D : 1;
+  double phi, d[3];
+  lbasis(family, sfn, x, y, z, phi, d);
+  double g[3];
+  for (int j = 0; j < D; ++j) {
+    double s = 0.0;
+    for (int i = 0; i < D; ++i) s = s + inv[i][j] * d[i];
+    g[j] = s;
+  }
+  for (int c = 0; c < ncomp; ++c) {
+    q[c] = (c == comp) ? phi : 0.0;
+    for (int k = 0; k < D; ++k) q[ncomp + c * D + k] = (c == comp) ? g[k] : 0.0;
+  }
+}
+
+FEM_HD double run(const Instr* ins, int n, int out, const double* qu, const double* qv,
+                      const double* coef, double* R) {
+  for (int k = 0; k < n; ++k) {
+    const Instr I = ins[k];
+    double r = 0.0;
+    switch (I.op) {
+      case OP_CONST: r = I.imm; break;
+      case OP_U: r = qu[I.a]; break;
+      case OP_V: r = qv[I.a]; break;
+      case OP_COEF: r = coef[I.a]; break;
+      case OP_ADD: r = R[I.a] + R[I.b]; break;
+      case OP_SUB: r = R[I.a] - R[I.b]; break;
+      case OP_MUL: r = R[I.a] * R[I.b]; break;
+      case OP_DIV: r = R[I.a] / R[I.b]; break;
+      case OP_NEG: r = -R[I.a]; break;
+      default: break;
+    }
+    R[k] = r;
+  }
+  return R[out];
+}
+
+// The replayed value of local entry (row i, column j) of element e.
+template <int D>
+FEM_HD double replay_entry(const FemMesh& m, const FemBasis& b, const FemProgram& prog,
+                           const Rule& rule, int64_t e, int i, int j, const double* coef,
+                           double* R, double* vals) {
+  const bool hex = b.family == FEM_HEX_1;
+  const bool vec = b.vector != 0;
+  double inv[3][3], det = 0.0;
+  if (!hex) affine_inverse<D>(m, e, inv, det);
+  double qu[D + D * D], qv[D + D * D];
+  for (int q = 0; q < rule.nq; ++q) {
+    const double x = rule.X[q];
+    const double y = rule.X[rule.nq + q];
+    const double z = D == 3 ? rule.X[2 * rule.nq + q] : 0.0;
+    if (hex) hex_inverse(m, e, x, y, z, inv, det);
+    quantities<D>(b.family, vec, j, x, y, z, inv, qu);
+    quantities<D>(b.family, vec, i, x, y, z, inv, qv);
+    const double f = run(prog.ins, prog.ninstr, prog.out, qu, qv, coef, R);
+    vals[q] = f * (fabs(det) * rule.W[q]);
+  }
+  return np_pairwise_sum(vals, rule.nq);
+}
+
+}  // namespace fem_faithful

@@ -28,6 +28,7 @@ UNITS = [
     ("fem_batched.cu", "fem_batched.o", []),
     ("fem_abi.cu", "fem_abi.o", []),
     ("fem_noalloc.cu", "fem_noalloc.o", []),
+    ("fem_faithful.cu", "fem_faithful.o", ["-fmad=false"]),
 ]
 
 
@@ -54,9 +55,9 @@ def build(force=False, verbose=False):
     if not force and not _sources_newer_than(LIB):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
-    # regenerate the exact reference tensors (pure Python, fractions)
-    subprocess.run(["python3", os.path.join(CSRC, "gen_tables.py")], check=True,
-                   stdout=subprocess.DEVNULL)
+    # fem_tables.cuh / fem_refquad.cuh are generated once by gen_tables.py /
+    # gen_refquad.py and committed: regenerating them on another platform
+    # could change the last bits of numpy-computed quadrature nodes.
     cc = nvcc()
     units = [u for u in UNITS if os.path.exists(os.path.join(CSRC, u[0]))]
 

@@ -48,6 +48,16 @@ class FemLinear(ctypes.Structure):
     _fields_ = [("load", FemCoef)]
 
 
+class FemInstr(ctypes.Structure):
+    _fields_ = [("op", ctypes.c_int32), ("a", ctypes.c_int32), ("b", ctypes.c_int32),
+                ("pad_", ctypes.c_int32), ("imm", ctypes.c_double)]
+
+
+class FemProgram(ctypes.Structure):
+    _fields_ = [("ninstr", ctypes.c_int32), ("out", ctypes.c_int32), ("ncoef", ctypes.c_int32),
+                ("nq", ctypes.c_int32), ("ins", ctypes.c_void_p), ("coef", ctypes.c_void_p * 8)]
+
+
 class FemError(RuntimeError):
     pass
 
@@ -67,7 +77,7 @@ _SIGS = {
     "fem_version": (ctypes.c_char_p, []),
     "fem_local_matrices": (ctypes.c_int, [_P, _P, _P, _P, _P]),
     "fem_local_vectors": (ctypes.c_int, [_P, _P, _P, _P, _P]),
-    "fem_pattern_build": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(ctypes.c_void_p), _P]),
+    "fem_pattern_build": (ctypes.c_int, [_P, _P, _P, _P, ctypes.POINTER(ctypes.c_void_p), _P]),
     "fem_pattern_info": (ctypes.c_int, [_P, _I64P, _I64P, _I64P]),
     "fem_pattern_export": (ctypes.c_int, [_P, _P, _P, _P]),
     "fem_pattern_destroy": (None, [_P]),

@@ -22,7 +22,8 @@ import scipy.sparse as sp
 import torch
 
 from . import _native as N
-from .tracer import (bilinear_channels, linear_channels, trace_bilinear, trace_linear)
+from .tracer import (bilinear_channels, linear_channels, trace_bilinear, trace_linear,
+                     trace_tape)
 
 __all__ = ["Form", "BilinearForm", "LinearForm", "asm", "ElementField"]
 
@@ -160,12 +161,32 @@ def _structure_key(ch):
                         for name, p in ch.items()))
 
 
+def _program(form, basis, coeffs):
+    """The form's exact-order program (tracer.trace_tape) on the device."""
+    try:
+        ins, out, names = trace_tape(form.form, basis.elem, basis.mesh.p.shape[0],
+                                     list(coeffs.fields), coeffs.numbers)
+    except NotImplementedError:
+        # an operation the replay cannot reproduce bit for bit: the mask then
+        # comes from the separately rounded tensor-form evaluation alone
+        return None, None
+    if len(ins) > 512 or len(names) > 8:
+        return None, None
+    arr = (N.FemInstr * len(ins))(*[N.FemInstr(op, a, b, 0, imm) for op, a, b, imm in ins])
+    dev = torch.frombuffer(bytearray(arr), dtype=torch.uint8).to(basis.device)
+    prog = N.FemProgram(len(ins), out, len(names), basis.X.shape[1], dev.data_ptr())
+    for k, n in enumerate(names):
+        prog.coef[k] = coeffs.fields[n].data_ptr()
+    return prog, dev
+
+
 class _PatternEntry:
-    def __init__(self, basis, c_form, stream):
+    def __init__(self, basis, c_form, stream, program=None):
         lib = N.lib()
         h = ctypes.c_void_p()
         N.check(lib.fem_pattern_build(N.byref(basis.c_mesh), N.byref(basis.c_basis),
                                       N.byref(c_form) if c_form is not None else None,
+                                      N.byref(program) if program is not None else None,
                                       ctypes.byref(h), stream))
         self.pat = N.Pattern(h.value)
         dev = basis.device
@@ -211,7 +232,9 @@ class BilinearForm(Form):
         key = ("bilinear", _structure_key(ch))
         entry = ubasis._patterns.get(key)
         if entry is None:
-            entry = _PatternEntry(ubasis, c_form, stream)
+            prog, keep = _program(self, ubasis, coeffs)
+            entry = _PatternEntry(ubasis, c_form, stream, prog)
+            del keep
             ubasis._patterns[key] = entry
         vals = torch.empty(max(entry.nnz, 1), dtype=torch.float64, device=ubasis.device)[:entry.nnz]
         entry.status.zero_()
@@ -283,7 +306,7 @@ class LinearForm(Form):
         key = ("incidence",)
         entry = basis._patterns.get(key)
         if entry is None:
-            entry = _PatternEntry(basis, None, stream)
+            entry = _PatternEntry(basis, None, stream, None)
             basis._patterns[key] = entry
         b = torch.empty(basis.N, dtype=torch.float64, device=basis.device)
         N.check(N.lib().fem_assemble_vector(N.byref(basis.c_mesh), N.byref(basis.c_basis),

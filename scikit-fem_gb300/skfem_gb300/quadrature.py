@@ -2,7 +2,13 @@
 
 The affine-simplex kernels integrate with exact reference tensors and need
 no points; the rules here give ``Basis.X`` / ``Basis.W`` (and so the shape
-of ``zero_w()``) and the hexahedral rule of the isoparametric kernel.
+of ``zero_w()``), the hexahedral rule of the isoparametric kernel and the
+nodes of the exact-zero mask.  Triangle / tetrahedron rules of orders 1-4
+are the reference's own tables, bit-exact (``_refquad.py``, generated from
+fixtures recorded by running the reference): which rounding-noise local
+entries the reference computes as exactly 0.0 depends on the last bits of
+its nodes.  The closed forms below derive the same rules (to a few ulps)
+and are used for orders the tables do not hold.
 
   tri order <= 2: 3-point rule at (1/6, 1/6), (2/3, 1/6), (1/6, 2/3)
   tri order 3, 4: the symmetric 6-point degree-4 rule (Dunavant 1985; two
@@ -63,7 +69,25 @@ def _tri_degree4():
     return v
 
 
+def _table(refdom, norder):
+    from ._refquad import RULES
+    key = "%s%d" % (refdom, max(norder, 1 if refdom == "tet" else 2))
+    if key not in RULES:
+        return None
+    X, W = RULES[key]
+    return (np.array([[float.fromhex(v) for v in row] for row in X]),
+            np.array([float.fromhex(v) for v in W]))
+
+
 def get_quadrature(refdom, norder):
+    if refdom in ("tri", "tet"):
+        t = _table(refdom, norder)
+        if t is not None:
+            return t
+    return closed_form_quadrature(refdom, norder)
+
+
+def closed_form_quadrature(refdom, norder):
     if refdom == "tri":
         if norder <= 2:
             a, b = 1.0 / 6.0, 2.0 / 3.0

@@ -306,3 +306,156 @@ def linear_channels(sym, elem, dim):
     if any(not tab[k].is_zero() for k in rest):
         raise NotImplementedError("only f * v load forms are implemented")
     return {"load": load}
+
+
+# ---------------------------------------------------------------------------
+# Exact-order tape (the pattern build's eliminate_zeros mask)
+# ---------------------------------------------------------------------------
+# The reference evaluates a form with numpy ufuncs and einsum on float64
+# arrays; on the reference's platform every einsum contraction is a plain
+# sequential sum in row-major index order without fused multiply-add, which
+# is also the order numpy's einsum uses on object arrays.  Running the form
+# on TapeNode objects therefore records, per quadrature point, the exact
+# sequence of separately rounded operations the reference performs.  The
+# CUDA mask kernel replays it for the local entries whose value is
+# rounding noise, so that the entries the reference computes as exactly
+# 0.0 -- and drops in eliminate_zeros -- are the entries dropped here.
+
+OP_CONST, OP_U, OP_V, OP_COEF, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG = range(9)
+
+
+class Tape:
+    def __init__(self):
+        self.ins = []
+        self.consts = {}
+        self.loads = {}
+
+    def emit(self, op, a=-1, b=-1, imm=0.0):
+        self.ins.append((op, a, b, float(imm)))
+        return len(self.ins) - 1
+
+    def const(self, c):
+        c = float(c)
+        key = (c, np.signbit(c))
+        if key not in self.consts:
+            self.consts[key] = self.emit(OP_CONST, imm=c)
+        return TapeNode(self, self.consts[key])
+
+    def load(self, op, k):
+        if (op, k) not in self.loads:
+            self.loads[(op, k)] = self.emit(op, a=k)
+        return TapeNode(self, self.loads[(op, k)])
+
+
+class TapeNode:
+    __slots__ = ("tape", "idx", "grad")
+    __array_ufunc__ = None
+
+    def __init__(self, tape, idx):
+        self.tape, self.idx, self.grad = tape, idx, None
+
+    def _lift(self, o):
+        if isinstance(o, TapeNode):
+            return o
+        if isinstance(o, numbers.Number):
+            return self.tape.const(o)
+        if isinstance(o, np.ndarray) and o.ndim == 0:
+            return self._lift(o.item())
+        raise TypeError("cannot combine %r with a traced form quantity" % type(o))
+
+    def _bin(self, op, o, rev=False):
+        if isinstance(o, np.ndarray) and o.ndim > 0:
+            return np.frompyfunc(lambda x: self._bin(op, x, rev), 1, 1)(o)
+        o = self._lift(o)
+        a, b = (o, self) if rev else (self, o)
+        return TapeNode(self.tape, self.tape.emit(op, a.idx, b.idx))
+
+    def __add__(self, o):
+        return self._bin(OP_ADD, o)
+
+    def __radd__(self, o):
+        return self._bin(OP_ADD, o, rev=True)
+
+    def __sub__(self, o):
+        return self._bin(OP_SUB, o)
+
+    def __rsub__(self, o):
+        return self._bin(OP_SUB, o, rev=True)
+
+    def __mul__(self, o):
+        return self._bin(OP_MUL, o)
+
+    def __rmul__(self, o):
+        return self._bin(OP_MUL, o, rev=True)
+
+    def __truediv__(self, o):
+        return self._bin(OP_DIV, o)
+
+    def __rtruediv__(self, o):
+        return self._bin(OP_DIV, o, rev=True)
+
+    def __neg__(self):
+        return TapeNode(self.tape, self.tape.emit(OP_NEG, self.idx))
+
+    def __pos__(self):
+        return self
+
+    def __pow__(self, n):
+        # numpy evaluates x**2 as x*x; other integer powers are not
+        # reproduced bit-exactly and are rejected
+        if n == 2:
+            return self * self
+        if n == 1:
+            return self
+        raise NotImplementedError("only **2 is supported in the exact-zero mask")
+
+    @property
+    def shape(self):
+        return ()
+
+
+class TapeParams(dict):
+    def __init__(self, tape, fields, numbers_):
+        super().__init__()
+        self.slots = {}
+        for k in fields:
+            self.slots[k] = len(self.slots)
+            self[k] = tape.load(OP_COEF, self.slots[k])
+        for k, v in numbers_.items():
+            self[k] = v
+
+    __getattr__ = SymParams.__getattr__
+    __getitem__ = SymParams.__getitem__
+    _missing = SymParams._missing
+
+
+def _tape_field(tape, which, elem, dim):
+    """Quantity k: value of component c -> c; derivative k of component c ->
+    ncomp + c*dim + k (ncomp = dim for vector bases, 1 for scalar)."""
+    op = OP_U if which == "u" else OP_V
+    if not elem.vector:
+        s = tape.load(op, 0)
+        s.grad = np.array([tape.load(op, 1 + k) for k in range(dim)], dtype=object)
+        return s
+    val = np.array([tape.load(op, c) for c in range(dim)], dtype=object)
+    grad = np.array([[tape.load(op, dim + c * dim + k) for k in range(dim)] for c in range(dim)],
+                    dtype=object)
+    return SymField(val, grad)
+
+
+def trace_tape(form, elem, dim, fields, numbers_):
+    """Record the exact-order program of a bilinear form; returns
+    (instructions, output index, coefficient slot names)."""
+    tape = Tape()
+    u = _tape_field(tape, "u", elem, dim)
+    v = _tape_field(tape, "v", elem, dim)
+    w = TapeParams(tape, fields, numbers_)
+    r = form(u, v, w)
+    if isinstance(r, np.ndarray):
+        if r.ndim != 0:
+            raise ValueError("form must return a scalar field")
+        r = r.item()
+    if not isinstance(r, TapeNode):
+        r = tape.const(r)
+    names = sorted(w.slots, key=w.slots.get)
+    return tape.ins, r.idx, names
