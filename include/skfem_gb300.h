@@ -139,6 +139,15 @@ const char* fem_last_error(void);
 const char* fem_version(void);
 
 /*
+ * Launch parameters of one element family, set by the autotuner
+ * (skfem_gb300.autotune): cells per CTA of the local kernel (64, 128, 256),
+ * persistent grid (0: one CTA per tile; k > 0: at most k CTAs per SM,
+ * grid-stride) and incidence entries loaded together by the segmented sum
+ * (4, 8, 16).  Process-wide; affects later launches.
+ */
+int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll);
+
+/*
  * Local (element) matrices: local[(e * nbfun + i) * nbfun + j] = K_e[i][j],
  * i = test function (row), j = trial function (column), the same entry as
  * the reference's data[j, i, e] (bilinear_form.py:90-98).

@@ -8,6 +8,8 @@
 namespace fem_fast {
 int local_matrices(const FemMesh&, const FemBasis&, const FemBilinear&, double*, int32_t*,
                    cudaStream_t);
+int local_matrices_checked(const FemMesh&, const FemBasis&, const FemBilinear&, double*,
+                           const uint8_t*, int32_t*, cudaStream_t);
 int local_vectors(const FemMesh&, const FemBasis&, const FemLinear&, double*, int32_t*,
                   cudaStream_t);
 }  // namespace fem_fast
@@ -79,6 +81,16 @@ __global__ void coef_zero_bits_kernel(FemBilinear f, int64_t n, const uint8_t* _
     if (coef_at(*c[k], e) == 0.0) bits |= (uint8_t)(1u << k);
   if (out) out[e] = bits;
   if (ref && ref[e] != bits) atomicOr(status, 1 << FEM_ERR_STALE_PATTERN);
+}
+
+namespace {
+std::mutex g_tuning_mu;
+Tuning g_tuning[8];
+}
+
+Tuning tuning_for(int family) {
+  std::lock_guard<std::mutex> lock(g_tuning_mu);
+  return (family >= 0 && family < 8) ? g_tuning[family] : Tuning();
 }
 
 }  // namespace fem
@@ -168,6 +180,20 @@ extern "C" {
 const char* fem_last_error(void) { return fem::g_err.c_str(); }
 
 const char* fem_version(void) { return "skfem_gb300 0.1 (sm_103a)"; }
+
+int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll) {
+  if (family < 1 || family > 5 || (local_block != 64 && local_block != 128 && local_block != 256) ||
+      persistent < 0 || (sum_unroll != 4 && sum_unroll != 8 && sum_unroll != 16)) {
+    set_error(FEM_ERR_ARGUMENT, "invalid tuning (family %d, block %d, persistent %d, unroll %d)",
+              family, local_block, persistent, sum_unroll);
+    return FEM_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> lock(fem::g_tuning_mu);
+  fem::g_tuning[family].local_block = local_block;
+  fem::g_tuning[family].persistent = persistent;
+  fem::g_tuning[family].sum_unroll = sum_unroll;
+  return 0;
+}
 
 int fem_local_matrices(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
                        double* local, fem_stream_t stream) {
@@ -296,14 +322,14 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
     return FEM_ERR_ARGUMENT;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  if (status && pat->coef_bits && mesh->nelems > 0) {
-    fem::coef_zero_bits_kernel<<<(unsigned)fem::ceil_div(mesh->nelems, 256), 256, 0, st>>>(
-        *form, mesh->nelems, pat->coef_bits, nullptr, status);
-    FEM_LAUNCH_CHECK("coef_zero_bits_kernel");
-  }
-  rc = fem_fast::local_matrices(*mesh, *basis, *form, staging, status, st);
+  // the local kernel also compares each element's coefficient zero bits
+  // with the pattern's (FEM_ERR_STALE_PATTERN)
+  rc = fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
+                                        status ? pat->coef_bits : nullptr, status, st);
   if (rc) return rc;
-  return fem::csr_sum(pat->P, staging, csr_values, st);
+  fem::Pattern P = pat->P;
+  P.sum_unroll = fem::tuning_for(basis->family).sum_unroll;
+  return fem::csr_sum(P, staging, csr_values, st);
 }
 
 int fem_csr_sum(const FemPattern* pat, const double* local, double* csr_values, int32_t* status,
@@ -313,7 +339,9 @@ int fem_csr_sum(const FemPattern* pat, const double* local, double* csr_values, 
     set_error(FEM_ERR_ARGUMENT, "null pattern or buffer");
     return FEM_ERR_ARGUMENT;
   }
-  return fem::csr_sum(pat->P, local, csr_values, (cudaStream_t)stream);
+  fem::Pattern P = pat->P;
+  P.sum_unroll = fem::tuning_for(pat->family).sum_unroll;
+  return fem::csr_sum(P, local, csr_values, (cudaStream_t)stream);
 }
 
 int fem_vector_sum(const FemPattern* pat, const double* local, double* b, fem_stream_t stream) {

@@ -6,6 +6,7 @@
 
 #include <cstdarg>
 #include <cstdio>
+#include <algorithm>
 #include <string>
 
 #include "../../include/skfem_gb300.h"
@@ -50,6 +51,7 @@ struct Pattern {
   int32_t* indices = nullptr;   // nnz
   uint16_t* slot = nullptr;     // ninc * nbfun_u
   bool has_matrix = false;
+  int sum_unroll = 8;    // set from the family's tuning when the pattern is built
 };
 
 // ---------------------------------------------------------------- helpers
@@ -74,6 +76,14 @@ __device__ __forceinline__ double coef_at(const FemCoef& c, int64_t e) {
 // from the caller's allocation helper.  Returns the total via *total (host).
 int exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, int64_t* total,
                        cudaStream_t stream);
+
+// Launch parameters chosen by the autotuner (fem_set_tuning), per family.
+struct Tuning {
+  int local_block = 128;  // threads (= cells) per CTA of the local kernel
+  int persistent = 0;     // >0: grid capped at persistent * SMs (grid-stride)
+  int sum_unroll = 8;     // incidence entries loaded together in the sum
+};
+Tuning tuning_for(int family);
 
 int basis_nb_scalar(int family);
 int basis_dim(int family);

@@ -64,11 +64,11 @@ __device__ __forceinline__ void simplex_geometry(const FemMesh& m, int64_t e, Si
 #pragma unroll
     for (int j = 0; j < D; ++j) A[i][j] = x[j + 1][i] - x[0][i];
   if constexpr (D == 2) {
-    s.det = A[0][0] * A[1][1] - A[0][1] * A[1][0];
     s.c[1][0] = A[1][1];
     s.c[1][1] = -A[0][1];
     s.c[2][0] = -A[1][0];
     s.c[2][1] = A[0][0];
+    s.det = A[0][0] * A[1][1] - A[0][1] * A[1][0];
   } else {
     s.c[1][0] = -A[1][2] * A[2][1] + A[1][1] * A[2][2];
     s.c[2][0] = A[1][2] * A[2][0] - A[1][0] * A[2][2];
@@ -79,10 +79,14 @@ __device__ __forceinline__ void simplex_geometry(const FemMesh& m, int64_t e, Si
     s.c[1][2] = -A[0][2] * A[1][1] + A[0][1] * A[1][2];
     s.c[2][2] = A[0][2] * A[1][0] - A[0][0] * A[1][2];
     s.c[3][2] = -A[0][1] * A[1][0] + A[0][0] * A[1][1];
-    s.det = A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) -
-            A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
-            A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
+    // first row of A times first column of adj(A)
+    s.det = A[0][0] * s.c[1][0] + A[0][1] * s.c[2][0] + A[0][2] * s.c[3][0];
   }
+}
+
+// c[0] = -(c[1] + ... + c[D]) (grad lambda_0 = -sum grad lambda_m)
+template <int D>
+__device__ __forceinline__ void simplex_c0(Simplex<D>& s) {
 #pragma unroll
   for (int k = 0; k < D; ++k) {
     double acc = s.c[1][k];
@@ -103,11 +107,11 @@ __device__ __forceinline__ double dotc(const double* a, const double* b) {
 // ----------------------------------------------------------- smem epilogue
 // Each thread writes its element's matrix into a padded row of shared
 // memory; the block then streams the rows out contiguously.
-template <int L>
+template <int L, int BS = kBlock>
 __device__ __forceinline__ void flush_rows(double* smem, double* __restrict__ out, int64_t e0,
                                            int64_t nelems) {
   __syncthreads();
-  const int64_t nb = ((nelems - e0) < (int64_t)kBlock ? (nelems - e0) : (int64_t)kBlock);
+  const int64_t nb = ((nelems - e0) < (int64_t)BS ? (nelems - e0) : (int64_t)BS);
   const int64_t total = nb * L;
   double* dst = out + e0 * L;
   for (int64_t g = threadIdx.x; g < total; g += blockDim.x) {
@@ -126,31 +130,67 @@ template <> struct SimplexTraits<2, 2> { static constexpr int NB = 6; static con
 template <> struct SimplexTraits<3, 1> { static constexpr int NB = 4; static constexpr double FACT = 6.0; };
 template <> struct SimplexTraits<3, 2> { static constexpr int NB = 10; static constexpr double FACT = 6.0; };
 
-template <int D, int ORDER>
-__global__ void __launch_bounds__(kBlock) simplex_scalar_kernel(FemMesh m, FemBilinear f,
-                                                                double* __restrict__ out) {
+// Per-element zero bits of the form's coefficients (bit k: channel k of
+// diff, mass, lam, lap, tr is exactly 0); compared with the bits recorded
+// at pattern build, a change means the zero structure may have changed.
+__device__ __forceinline__ void check_coef_bits(const FemBilinear& f, int64_t e,
+                                                const uint8_t* __restrict__ ref,
+                                                int32_t* __restrict__ status) {
+  if (!ref) return;
+  uint8_t bits = 0;
+  bits |= (coef_at(f.diff, e) == 0.0) ? 1u : 0u;
+  bits |= (coef_at(f.mass, e) == 0.0) ? 2u : 0u;
+  bits |= (coef_at(f.lam, e) == 0.0) ? 4u : 0u;
+  bits |= (coef_at(f.lap, e) == 0.0) ? 8u : 0u;
+  bits |= (coef_at(f.tr, e) == 0.0) ? 16u : 0u;
+  if (bits != ref[e] && status) atomicOr(status, 1 << FEM_ERR_STALE_PATTERN);
+}
+
+template <int D, int ORDER, int BS>
+__global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBilinear f,
+                                                                double* __restrict__ out,
+                                                                const uint8_t* __restrict__ ref_bits,
+                                                                int32_t* __restrict__ status) {
   constexpr int NB = SimplexTraits<D, ORDER>::NB;
   constexpr int L = NB * NB;
-  constexpr double FACT = SimplexTraits<D, ORDER>::FACT;
+  constexpr double INV_FACT = 1.0 / SimplexTraits<D, ORDER>::FACT;
   extern __shared__ double smem[];
-  const int64_t e0 = (int64_t)blockIdx.x * kBlock;
+  // grid-stride over element tiles of BS cells (persistent when the grid is
+  // smaller than the number of tiles)
+  for (int64_t e0 = (int64_t)blockIdx.x * BS; e0 < m.nelems; e0 += (int64_t)gridDim.x * BS) {
   const int64_t e = e0 + threadIdx.x;
   if (e < m.nelems) {
+    check_coef_bits(f, e, ref_bits, status);
     Simplex<D> s;
     simplex_geometry<D>(m, e, s);
     const double adet = fabs(s.det);
     // stiffness scale kd / (d! |det|); mass scale km |det| / d!
-    const double sd = coef_at(f.diff, e) / (FACT * adet);
-    const double sm = coef_at(f.mass, e) * (adet / FACT);
+    const double sd = coef_at(f.diff, e) * ((1.0 / adet) * INV_FACT);
+    const double sm = coef_at(f.mass, e) * (adet * INV_FACT);
+    // Gram of c_1..c_D, then row 0 from c_0 = -sum c_m
     double gram[D + 1][D + 1];
 #pragma unroll
-    for (int a = 0; a <= D; ++a)
+    for (int a = 1; a <= D; ++a)
 #pragma unroll
       for (int b = a; b <= D; ++b) gram[a][b] = dotc<D>(s.c[a], s.c[b]);
+#pragma unroll
+    for (int b = 1; b <= D; ++b) {
+      double acc = 0.0;
+#pragma unroll
+      for (int a = 1; a <= D; ++a) acc = acc + (a <= b ? gram[a][b] : gram[b][a]);
+      gram[0][b] = -acc;
+    }
+    {
+      double acc = 0.0;
+#pragma unroll
+      for (int b = 1; b <= D; ++b) acc = acc + gram[0][b];
+      gram[0][0] = -acc;
+    }
     double* row = smem + threadIdx.x * (L + 1);
+    double kst[NB][NB];
 #define G(a, b) ((a) <= (b) ? gram[a][b] : gram[b][a])
-#define KS(i, j, v) { const double _v = sd * (v); row[(i) * NB + (j)] = _v; row[(j) * NB + (i)] = _v; }
-#define KM(i, j, v) { const double _v = sm * (v); row[(i) * NB + (j)] += _v; if ((i) != (j)) row[(j) * NB + (i)] += _v; }
+#define KS(i, j, v) { kst[i][j] = (v); }
+#define KM(i, j, v) { const double _v = sd * kst[i][j] + sm * (v); row[(i) * NB + (j)] = _v; row[(j) * NB + (i)] = _v; }
     if constexpr (D == 2 && ORDER == 1) { TRI1_STIFF(G, KS); TRI1_MASS(KM); }
     if constexpr (D == 2 && ORDER == 2) { TRI2_STIFF(G, KS); TRI2_MASS(KM); }
     if constexpr (D == 3 && ORDER == 1) { TET1_STIFF(G, KS); TET1_MASS(KM); }
@@ -159,7 +199,8 @@ __global__ void __launch_bounds__(kBlock) simplex_scalar_kernel(FemMesh m, FemBi
 #undef KS
 #undef KM
   }
-  flush_rows<L>(smem, out, e0, m.nelems);
+  flush_rows<L, BS>(smem, out, e0, m.nelems);
+  }
 }
 
 // -------------------------------------------- simplex, vector P2 (and P1)
@@ -170,7 +211,9 @@ __global__ void __launch_bounds__(kBlock) simplex_scalar_kernel(FemMesh m, FemBi
 // and streamed out through shared memory.
 template <int D, int ORDER>
 __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBilinear f,
-                                                            double* __restrict__ out) {
+                                                            double* __restrict__ out,
+                                                            const uint8_t* __restrict__ ref_bits,
+                                                            int32_t* __restrict__ status) {
   constexpr int BS = 64;
   constexpr int NS = SimplexTraits<D, ORDER>::NB;  // scalar functions
   constexpr int NB = NS * D;                        // vector functions
@@ -187,8 +230,10 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
   const bool live = e < m.nelems;
   double sm = 0.0;
   if (live) {
+    check_coef_bits(f, e, ref_bits, status);
     Simplex<D> s;
     simplex_geometry<D>(m, e, s);
+    simplex_c0<D>(s);
     const double adet = fabs(s.det);
     const double s0 = 1.0 / (FACT * adet);
     const double lam = coef_at(f.lam, e) * s0;
@@ -391,12 +436,14 @@ __device__ __forceinline__ void hex_shape(double x, double y, double z, double p
 
 __global__ void __launch_bounds__(kBlock) hex_scalar_kernel(FemMesh m, FemBilinear f,
                                                             double* __restrict__ out,
+                                                            const uint8_t* __restrict__ ref_bits,
                                                             int32_t* __restrict__ status) {
   constexpr int L = 64;
   extern __shared__ double smem[];
   const int64_t e0 = (int64_t)blockIdx.x * kBlock;
   const int64_t e = e0 + threadIdx.x;
   if (e < m.nelems) {
+    check_coef_bits(f, e, ref_bits, status);
     Hex h;
     hex_load(m, e, h);
     const double kd = coef_at(f.diff, e);
@@ -576,37 +623,55 @@ static int set_smem(K kernel, size_t bytes) {
   return 0;
 }
 
-int local_matrices(const FemMesh& m, const FemBasis& b, const FemBilinear& f, double* out,
-                   int32_t* status, cudaStream_t st) {
+template <int D, int O, int BS>
+static int launch_scalar(const FemMesh& m, const FemBilinear& f, double* out,
+                         const uint8_t* ref_bits, int32_t* status, int persistent,
+                         cudaStream_t st) {
+  constexpr int NB = SimplexTraits<D, O>::NB;
+  const size_t sm = (size_t)BS * (NB * NB + 1) * sizeof(double);
+  int rc = set_smem(simplex_scalar_kernel<D, O, BS>, sm);
+  if (rc) return rc;
+  int64_t grid = fem::ceil_div(m.nelems, BS);
+  if (persistent > 0) grid = std::min<int64_t>(grid, (int64_t)persistent * fem::num_sms());
+  simplex_scalar_kernel<D, O, BS><<<(unsigned)grid, BS, sm, st>>>(m, f, out, ref_bits, status);
+  return 0;
+}
+
+template <int D, int O>
+static int launch_scalar_tuned(const FemMesh& m, const FemBilinear& f, double* out,
+                               const uint8_t* ref_bits, int32_t* status, cudaStream_t st) {
+  const fem::Tuning t = fem::tuning_for(D == 2 ? (O == 1 ? FEM_TRI_P1 : FEM_TRI_P2)
+                                               : (O == 1 ? FEM_TET_P1 : FEM_TET_P2));
+  switch (t.local_block) {
+    case 64: return launch_scalar<D, O, 64>(m, f, out, ref_bits, status, t.persistent, st);
+    case 256: return launch_scalar<D, O, 256>(m, f, out, ref_bits, status, t.persistent, st);
+    default: return launch_scalar<D, O, 128>(m, f, out, ref_bits, status, t.persistent, st);
+  }
+}
+
+int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinear& f, double* out,
+                           const uint8_t* ref_bits, int32_t* status, cudaStream_t st) {
   if (m.nelems == 0) return 0;
   const int fam = b.family;
   const int64_t grid = fem::ceil_div(m.nelems, kBlock);
   int rc = 0;
   if (!b.vector) {
     switch (fam) {
-#define LAUNCH_S(D, O)                                                                 \
-  {                                                                                    \
-    constexpr int NB = SimplexTraits<D, O>::NB;                                        \
-    const size_t sm = (size_t)kBlock * (NB * NB + 1) * sizeof(double);                 \
-    if ((rc = set_smem(simplex_scalar_kernel<D, O>, sm))) return rc;                   \
-    simplex_scalar_kernel<D, O><<<(unsigned)grid, kBlock, sm, st>>>(m, f, out);        \
-    break;                                                                             \
-  }
-      case FEM_TRI_P1: LAUNCH_S(2, 1)
-      case FEM_TRI_P2: LAUNCH_S(2, 2)
-      case FEM_TET_P1: LAUNCH_S(3, 1)
-      case FEM_TET_P2: LAUNCH_S(3, 2)
-#undef LAUNCH_S
+      case FEM_TRI_P1: rc = launch_scalar_tuned<2, 1>(m, f, out, ref_bits, status, st); break;
+      case FEM_TRI_P2: rc = launch_scalar_tuned<2, 2>(m, f, out, ref_bits, status, st); break;
+      case FEM_TET_P1: rc = launch_scalar_tuned<3, 1>(m, f, out, ref_bits, status, st); break;
+      case FEM_TET_P2: rc = launch_scalar_tuned<3, 2>(m, f, out, ref_bits, status, st); break;
       case FEM_HEX_1: {
         const size_t sm = (size_t)kBlock * 65 * sizeof(double);
         if ((rc = set_smem(hex_scalar_kernel, sm))) return rc;
-        hex_scalar_kernel<<<(unsigned)grid, kBlock, sm, st>>>(m, f, out, status);
+        hex_scalar_kernel<<<(unsigned)grid, kBlock, sm, st>>>(m, f, out, ref_bits, status);
         break;
       }
       default:
         fem::set_error(FEM_ERR_UNSUPPORTED, "unsupported element family %d", fam);
         return FEM_ERR_UNSUPPORTED;
     }
+    if (rc) return rc;
   } else {
     const int64_t vgrid = fem::ceil_div(m.nelems, 64);
     switch (fam) {
@@ -616,7 +681,7 @@ int local_matrices(const FemMesh& m, const FemBasis& b, const FemBilinear& f, do
     constexpr int NPAIR = NV * (NV + 1) / 2, RB = D * NB;                              \
     const size_t sm = ((size_t)NPAIR * D * D * 64 + (size_t)64 * (RB + 1)) * sizeof(double); \
     if ((rc = set_smem(simplex_vector_kernel<D, O>, sm))) return rc;                   \
-    simplex_vector_kernel<D, O><<<(unsigned)vgrid, 64, sm, st>>>(m, f, out);           \
+    simplex_vector_kernel<D, O><<<(unsigned)vgrid, 64, sm, st>>>(m, f, out, ref_bits, status);           \
     break;                                                                             \
   }
       case FEM_TRI_P1: LAUNCH_V(2, 1)
@@ -632,6 +697,11 @@ int local_matrices(const FemMesh& m, const FemBasis& b, const FemBilinear& f, do
   }
   FEM_LAUNCH_CHECK("local matrix kernel");
   return 0;
+}
+
+int local_matrices(const FemMesh& m, const FemBasis& b, const FemBilinear& f, double* out,
+                   int32_t* status, cudaStream_t st) {
+  return local_matrices_checked(m, b, f, out, nullptr, status, st);
 }
 
 int local_vectors(const FemMesh& m, const FemBasis& b, const FemLinear& f, double* out,

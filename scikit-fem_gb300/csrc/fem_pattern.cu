@@ -215,8 +215,12 @@ __global__ void row_fill_kernel(const int32_t* __restrict__ inc_ptr, const int32
 }
 
 // Fixed-order segmented sum.  G lanes per row (G = power of two >= nu);
-// shared accumulators of `stride` doubles per row.
-template <int G>
+// shared accumulators of `stride` doubles per row.  Incidence entries are
+// taken U at a time: their index, slot and value loads are issued together
+// (independent of each other), then added in order -- entry q's additions
+// complete (__syncwarp) before entry q+1's, so every slot sums its
+// contributions in ascending (element, local row) order.
+template <int G, int U>
 __global__ void csr_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                                const uint16_t* __restrict__ slot, const int32_t* __restrict__ indptr,
                                const double* __restrict__ local, int64_t nrows, int nu, int stride,
@@ -241,18 +245,29 @@ __global__ void csr_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_
       nnz = indptr[r + 1] - p0;
     }
     for (int k = j; k < nnz; k += G) acc[k] = 0.0;
-    // longest incidence list in the warp
     int maxlen = len;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
     __syncwarp();
-    for (int q = 0; q < maxlen; ++q) {
-      if (q < len && j < nu) {
-        const int64_t code = inc[b + q];
-        const uint16_t s = slot[((int64_t)b + q) * nu + j];
-        if (s != 0xFFFF) acc[s] += local[code * nu + j];
+    for (int q0 = 0; q0 < maxlen; q0 += U) {
+      double v[U];
+      int s[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int q = q0 + u;
+        s[u] = 0xFFFF;
+        v[u] = 0.0;
+        if (q < len && j < nu) {
+          const int64_t code = __ldg(inc + b + q);
+          s[u] = __ldg(slot + ((int64_t)b + q) * nu + j);
+          v[u] = __ldg(local + code * nu + j);
+        }
       }
-      __syncwarp();
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (s[u] != 0xFFFF) acc[s[u]] += v[u];
+        __syncwarp();
+      }
     }
     for (int k = j; k < nnz; k += G) vals[p0 + k] = acc[k];
     __syncwarp();
@@ -509,11 +524,12 @@ int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st
                                       stride, vals);
     return 0;
   };
-  if (nu <= 2) rc = launch(csr_sum_kernel<2>, 2);
-  else if (nu <= 4) rc = launch(csr_sum_kernel<4>, 4);
-  else if (nu <= 8) rc = launch(csr_sum_kernel<8>, 8);
-  else if (nu <= 16) rc = launch(csr_sum_kernel<16>, 16);
-  else if (nu <= 32) rc = launch(csr_sum_kernel<32>, 32);
+  const int U = P.sum_unroll;
+  if (nu <= 2) rc = U >= 16 ? launch(csr_sum_kernel<2, 16>, 2) : U >= 8 ? launch(csr_sum_kernel<2, 8>, 2) : launch(csr_sum_kernel<2, 4>, 2);
+  else if (nu <= 4) rc = U >= 16 ? launch(csr_sum_kernel<4, 16>, 4) : U >= 8 ? launch(csr_sum_kernel<4, 8>, 4) : launch(csr_sum_kernel<4, 4>, 4);
+  else if (nu <= 8) rc = U >= 16 ? launch(csr_sum_kernel<8, 16>, 8) : U >= 8 ? launch(csr_sum_kernel<8, 8>, 8) : launch(csr_sum_kernel<8, 4>, 8);
+  else if (nu <= 16) rc = U >= 8 ? launch(csr_sum_kernel<16, 8>, 16) : launch(csr_sum_kernel<16, 4>, 16);
+  else if (nu <= 32) rc = U >= 8 ? launch(csr_sum_kernel<32, 8>, 32) : launch(csr_sum_kernel<32, 4>, 32);
   else {
     set_error(FEM_ERR_UNSUPPORTED, "more than 32 local functions per cell (%d)", nu);
     return FEM_ERR_UNSUPPORTED;

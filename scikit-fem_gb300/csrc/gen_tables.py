@@ -199,6 +199,40 @@ def emit_simplex_contractions(tag, d, order):
     return "\n".join(out) + "\n"
 
 
+def reduced_terms(BB, i, j, d):
+    """sum_ab BB[i][j][a][b] G(a,b) rewritten over G(m,n), 1 <= m <= n <= d,
+    using grad l_0 = -sum_m grad l_m (so G(0,n) = -sum_m G(m,n))."""
+    n = d + 1
+    out = {}
+
+    def expand(a):
+        return [(a, F(1))] if a > 0 else [(m, F(-1)) for m in range(1, n)]
+
+    for a in range(n):
+        for b in range(n):
+            c = BB[i][j][a][b]
+            if c == 0:
+                continue
+            for (m, sm) in expand(a):
+                for (k, sk) in expand(b):
+                    key = (min(m, k), max(m, k))
+                    out[key] = out.get(key, F(0)) + c * sm * sk
+    return {k: v for k, v in out.items() if v != 0}
+
+
+def emit_reduced(tag, d, order):
+    """K(i, j, stiffness over reduced Gram GR(m,n), mass constant) for i <= j."""
+    BB, MM, LV = simplex_tables(d, order)
+    nb = len(BB)
+    body = []
+    for i in range(nb):
+        for j in range(i, nb):
+            t = reduced_terms(BB, i, j, d)
+            expr = " + ".join("(%s)*GR(%d,%d)" % (dlit(c), m, k) for (m, k), c in sorted(t.items()))
+            body.append("  K(%d,%d, %s, %s);" % (i, j, expr if expr else "0.0", dlit(MM[i][j])))
+    return "#define %s_KRED(GR, K) do { \\\n%s \\\n} while (0)\n" % (tag, " \\\n".join(body))
+
+
 def emit_bb_terms(tag, d):
     """For the vector P2 kernel: per (i,j) block, the list of (a, b, coef)."""
     BB, _, _ = simplex_tables(d, 2)
@@ -264,6 +298,7 @@ def main():
     out.append(emit_simplex_contractions("TET2", 3, 2))
     for tag, d, o in (("TRI1", 2, 1), ("TRI2", 2, 2), ("TET1", 3, 1), ("TET2", 3, 2)):
         out.append(emit_qacc(tag, d, o))
+        out.append(emit_reduced(tag, d, o))
     out.append(emit_bb_terms("TET2BB", 3))
     out.append(emit_bb_terms("TRI2BB", 2))
     HS, HM, HL = hex_tables()
