@@ -285,8 +285,11 @@ def _abi_step(F, N, form, b, coefs):
     return step, entry, c_form, vals
 
 
-def secondary_workloads(args):
-    """The other workloads of the assembly path, each timed on the device."""
+def secondary_workloads(args, only=None):
+    """The other workloads of the assembly path, each timed on the device.
+    ``only`` restricts the run to one of tri_p1 / tet_p2_vec / hex1_vjp /
+    batched (sizes from --vec-n, --hex-n, --batch)."""
+    want = (lambda name: only is None or only == name)
     import torch
 
     import skfem_gb300 as F
@@ -299,123 +302,152 @@ def secondary_workloads(args):
     out = {}
     rng = np.random.default_rng(args.seed)
     reps = 10
-
-    # cfg1: TriP1 Laplace + unit load, 256x256 squares (131,072 triangles)
-    m = F.MeshTri.init_tensor(np.linspace(0, 1, 257), np.linspace(0, 1, 257))
-    b = F.Basis(m, F.ElementTriP1())
-    step, entry, _, _ = _abi_step(F, N, laplace, b, {})
-    ms_k = _time(step, reps)
-    ms_b = _time(lambda: unit_load.assemble_torch(b), reps)
-    B = m.nelements * (3 * 4) + m.p.size * 8 + entry.nnz * 8
-    out["tri_p1_laplace_256"] = {
-        "nelems": m.nelements, "nnz": entry.nnz, "ms_matrix": ms_k, "ms_load": ms_b,
-        "elements_per_s": m.nelements / ((ms_k + ms_b) * 1e-3),
-        "hbm_frac_matrix": B / (ms_k * 1e-3) / 1e9 / hbm}
-
-    # cfg3: vector TetP2 elasticity, 41^3 nodes jittered +-0.2h, lambda=1, mu=0.5
-    n = 40
-    m = F.MeshTet.init_tensor(*(np.linspace(0, 1, n + 1),) * 3)
-    p = m.p.copy()
-    inner = np.all((p > 1e-12) & (p < 1 - 1e-12), axis=0)
-    p[:, inner] += rng.uniform(-0.2 / n, 0.2 / n, size=(3, int(inner.sum())))
-    m = F.MeshTet(p, m.t)
-    b = F.Basis(m, F.ElementVector(F.ElementTetP2()), intorder=4)
-    form = linear_elasticity(1.0, 0.5)
-    t0 = time.perf_counter()
-    step, entry, c_form, vals = _abi_step(F, N, form, b, {})
-    torch.cuda.synchronize()
-    build_s = time.perf_counter() - t0
-    ms = _time(step, 3)
     lib = N.lib()
-    ms_local = _time(lambda: N.check(lib.fem_local_matrices(
-        N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form), N.ptr(entry.staging),
-        N.stream_ptr())), 3)
-    B = m.nelements * (10 * 4) + m.p.size * 8 + entry.nnz * 8
-    out["tet_p2_vec_elasticity_41"] = {
-        "nelems": m.nelements, "ndofs": b.N, "nnz": entry.nnz, "ms": ms, "ms_local": ms_local,
-        "pattern_build_s": build_s, "elements_per_s": m.nelements / (ms * 1e-3),
-        "hbm_frac": B / (ms * 1e-3) / 1e9 / hbm, "algorithmic_bytes": B}
-    del step, entry, vals, b
-    torch.cuda.empty_cache()
 
-    # cfg4: Hex1 theta*Laplace 64^3 cells: plain assembly vs forward + adjoint
-    from skfem_gb300.autodiff import _vertex_incidence
-    m = F.MeshHex.init_tensor(*(np.linspace(0, 1, 65),) * 3)
-    b = F.Basis(m, F.ElementHex1())
+    if want('tri_p1'):
+        # cfg1: TriP1 Laplace + unit load, 256x256 squares (131,072 triangles)
+        m = F.MeshTri.init_tensor(np.linspace(0, 1, 257), np.linspace(0, 1, 257))
+        b = F.Basis(m, F.ElementTriP1())
+        step, entry, _, _ = _abi_step(F, N, laplace, b, {})
+        ms_k = _time(step, reps)
+        ms_b = _time(lambda: unit_load.assemble_torch(b), reps)
+        B = m.nelements * (3 * 4) + m.p.size * 8 + entry.nnz * 8
+        out["tri_p1_laplace_256"] = {
+            "nelems": m.nelements, "nnz": entry.nnz, "ms_matrix": ms_k, "ms_load": ms_b,
+            "elements_per_s": m.nelements / ((ms_k + ms_b) * 1e-3),
+            "hbm_frac_matrix": B / (ms_k * 1e-3) / 1e9 / hbm}
 
-    @F.BilinearForm
-    def theta_laplace(u, v, w):
-        return w.theta * H.dot(H.grad(u), H.grad(v))
+    if want('tet_p2_vec'):
+        # cfg3: vector TetP2 elasticity, 41^3 nodes jittered +-0.2h, lambda=1, mu=0.5
+        n = args.vec_n
+        m = F.MeshTet.init_tensor(*(np.linspace(0, 1, n + 1),) * 3)
+        p = m.p.copy()
+        inner = np.all((p > 1e-12) & (p < 1 - 1e-12), axis=0)
+        p[:, inner] += rng.uniform(-0.2 / n, 0.2 / n, size=(3, int(inner.sum())))
+        m = F.MeshTet(p, m.t)
+        b = F.Basis(m, F.ElementVector(F.ElementTetP2()), intorder=4)
+        form = linear_elasticity(1.0, 0.5)
+        t0 = time.perf_counter()
+        step, entry, c_form, vals = _abi_step(F, N, form, b, {})
+        torch.cuda.synchronize()
+        build_s = time.perf_counter() - t0
+        ms = _time(step, 3)
+        lib = N.lib()
+        ms_local = _time(lambda: N.check(lib.fem_local_matrices(
+            N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form), N.ptr(entry.staging),
+            N.stream_ptr())), 3)
+        B = m.nelements * (10 * 4) + m.p.size * 8 + entry.nnz * 8
+        out["tet_p2_vec_elasticity_%d" % (n + 1)] = {
+            "nelems": m.nelements, "ndofs": b.N, "nnz": entry.nnz, "ms": ms, "ms_local": ms_local,
+            "pattern_build_s": build_s, "elements_per_s": m.nelements / (ms * 1e-3),
+            "hbm_frac": B / (ms * 1e-3) / 1e9 / hbm, "algorithmic_bytes": B}
+        del step, entry, vals, b
+        torch.cuda.empty_cache()
 
-    theta = torch.tensor(rng.uniform(0.01, 1.0, m.nelements), device="cuda")
-    w = torch.tensor(rng.standard_normal(b.N), device="cuda")
-    u = torch.tensor(rng.standard_normal(b.N), device="cuda")
-    step, entry, c_form, vals = _abi_step(F, N, theta_laplace, b, {"theta": theta})
-    vinc = _vertex_incidence(b)
-    dth = torch.empty(m.nelements, dtype=torch.float64, device="cuda")
-    dX = torch.empty_like(b.p_dev)
-    scratch = torch.empty(m.nelements * 24, dtype=torch.float64, device="cuda")
+    if want('hex1_vjp'):
+        # cfg4: Hex1 theta*Laplace 64^3 cells: plain assembly vs forward + adjoint
+        from skfem_gb300.autodiff import _vertex_incidence
+        m = F.MeshHex.init_tensor(*(np.linspace(0, 1, args.hex_n + 1),) * 3)
+        b = F.Basis(m, F.ElementHex1())
 
-    def vjp():
-        N.check(lib.fem_bilinear_vjp(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
-                                     vinc.handle, N.ptr(w), N.ptr(u), N.ptr(dth), None,
-                                     N.ptr(dX), N.ptr(scratch), N.stream_ptr()))
+        @F.BilinearForm
+        def theta_laplace(u, v, w):
+            return w.theta * H.dot(H.grad(u), H.grad(v))
 
-    ms_f = _time(step, reps)
-    ms_fv = _time(lambda: (step(), vjp()), reps)
-    out["hex1_theta_laplace_64_vjp"] = {
-        "nelems": m.nelements, "nnz": entry.nnz, "ms_forward": ms_f, "ms_forward_plus_vjp": ms_fv,
-        "vjp_over_forward": ms_fv / ms_f, "elements_per_s_forward": m.nelements / (ms_f * 1e-3)}
-    del step, entry, vals, b, scratch
-    torch.cuda.empty_cache()
+        theta = torch.tensor(rng.uniform(0.01, 1.0, m.nelements), device="cuda")
+        w = torch.tensor(rng.standard_normal(b.N), device="cuda")
+        u = torch.tensor(rng.standard_normal(b.N), device="cuda")
+        step, entry, c_form, vals = _abi_step(F, N, theta_laplace, b, {"theta": theta})
+        vinc = _vertex_incidence(b)
+        dth = torch.empty(m.nelements, dtype=torch.float64, device="cuda")
+        dX = torch.empty_like(b.p_dev)
+        scratch = torch.empty(m.nelements * 24, dtype=torch.float64, device="cuda")
 
-    # cfg5: 512 jittered TriP2 squares, cells log-uniform in [2k, 200k], forward + adjoint
-    from skfem_gb300.batched import BatchedBasis, GraphedAssembly
-    brng = np.random.default_rng(args.seed + 5)
-    cells = np.exp(brng.uniform(np.log(2e3), np.log(2e5), args.batch))
-    meshes, ks = [], []
-    for c in cells:
-        nn = max(1, int(round(np.sqrt(c / 2))))
-        mm = F.MeshTri.init_tensor(np.linspace(0, 1, nn + 1), np.linspace(0, 1, nn + 1))
-        pp = mm.p.copy()
-        inner = np.all((pp > 1e-12) & (pp < 1 - 1e-12), axis=0)
-        pp[:, inner] += brng.uniform(-0.2 / nn, 0.2 / nn, size=(2, int(inner.sum())))
-        meshes.append(F.MeshTri(pp, mm.t))
-        ks.append(brng.lognormal(0.0, 0.5, mm.nelements))
+        def vjp():
+            N.check(lib.fem_bilinear_vjp(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
+                                         vinc.handle, N.ptr(w), N.ptr(u), N.ptr(dth), None,
+                                         N.ptr(dX), N.ptr(scratch), N.stream_ptr()))
 
-    @F.BilinearForm
-    def k_laplace(u, v, w):
-        return w.k * H.dot(H.grad(u), H.grad(v))
+        ms_f = _time(step, reps)
+        ms_fv = _time(lambda: (step(), vjp()), reps)
+        out["hex1_theta_laplace_%d_vjp" % args.hex_n] = {
+            "nelems": m.nelements, "nnz": entry.nnz, "ms_forward": ms_f, "ms_forward_plus_vjp": ms_fv,
+            "vjp_over_forward": ms_fv / ms_f, "elements_per_s_forward": m.nelements / (ms_f * 1e-3)}
+        del step, entry, vals, b, scratch
+        torch.cuda.empty_cache()
 
-    t0 = time.perf_counter()
-    bb = BatchedBasis(meshes, F.ElementTriP2())
-    kk = torch.tensor(np.concatenate(ks), device="cuda")
-    wb = torch.tensor(brng.standard_normal(bb.N), device="cuda")
-    ub = torch.tensor(brng.standard_normal(bb.N), device="cuda")
-    from skfem_gb300 import autotune
-    best, _ = autotune.tune(k_laplace, bb, {"k": kk}, reps=2, use_cache=False)
-    ga = GraphedAssembly(k_laplace, bb, {"k": kk}, w=wb, u=ub).capture()
-    torch.cuda.synchronize()
-    setup_s = time.perf_counter() - t0
-    ms_graph = _time(ga.replay, 5)
-    ga.check()
-    # per-mesh plain launches of the same kernels (patterns prebuilt, eager)
-    per = []
-    for mm, kv in zip(meshes, ks):
-        bm = F.Basis(mm, F.ElementTriP2())
-        kt = torch.tensor(kv, device="cuda")
-        g1 = GraphedAssembly(k_laplace, bm, {"k": kt},
-                             w=torch.zeros(bm.N, dtype=torch.float64, device="cuda"),
-                             u=torch.zeros(bm.N, dtype=torch.float64, device="cuda"))
-        per.append(g1)
-    ms_loop = _time(lambda: [g.run_eager() for g in per], 3, warm=1)
-    ncell = int(bb.nelems)
-    out["batched_512_trip2_forward_vjp"] = {
-        "meshes": len(meshes), "nelems": ncell, "nnz": int(ga.entry.nnz), "setup_s": setup_s,
-        "autotuned": best, "ms_graph_replay": ms_graph, "ms_per_mesh_launches": ms_loop,
-        "elements_per_s_batched": ncell / (ms_graph * 1e-3),
-        "elements_per_s_per_mesh": ncell / (ms_loop * 1e-3),
-        "speedup": ms_loop / ms_graph, "launches_per_step": ga.launches_per_step()}
+    if want('batched'):
+        # cfg5: 512 jittered TriP2 squares, cells log-uniform in [2k, 200k], forward + adjoint
+        from skfem_gb300.batched import BatchedBasis, GraphedAssembly
+        brng = np.random.default_rng(args.seed + 5)
+        cells = np.exp(brng.uniform(np.log(2e3), np.log(2e5), args.batch))
+        meshes, ks = [], []
+        for c in cells:
+            nn = max(1, int(round(np.sqrt(c / 2))))
+            mm = F.MeshTri.init_tensor(np.linspace(0, 1, nn + 1), np.linspace(0, 1, nn + 1))
+            pp = mm.p.copy()
+            inner = np.all((pp > 1e-12) & (pp < 1 - 1e-12), axis=0)
+            pp[:, inner] += brng.uniform(-0.2 / nn, 0.2 / nn, size=(2, int(inner.sum())))
+            meshes.append(F.MeshTri(pp, mm.t))
+            ks.append(brng.lognormal(0.0, 0.5, mm.nelements))
+
+        @F.BilinearForm
+        def k_laplace(u, v, w):
+            return w.k * H.dot(H.grad(u), H.grad(v))
+
+        t0 = time.perf_counter()
+        bb = BatchedBasis(meshes, F.ElementTriP2())
+        kk = torch.tensor(np.concatenate(ks), device="cuda")
+        wb = torch.tensor(brng.standard_normal(bb.N), device="cuda")
+        ub = torch.tensor(brng.standard_normal(bb.N), device="cuda")
+        from skfem_gb300 import autotune
+        best, _ = autotune.tune(k_laplace, bb, {"k": kk}, reps=2, use_cache=False)
+        ga = GraphedAssembly(k_laplace, bb, {"k": kk}, w=wb, u=ub).capture()
+        torch.cuda.synchronize()
+        setup_s = time.perf_counter() - t0
+        ms_graph = _time(ga.replay, 5)
+        ga.check()
+        # per-mesh plain launches of the same kernels (patterns prebuilt, eager)
+        per = []
+        for mm, kv in zip(meshes, ks):
+            bm = F.Basis(mm, F.ElementTriP2())
+            kt = torch.tensor(kv, device="cuda")
+            g1 = GraphedAssembly(k_laplace, bm, {"k": kt},
+                                 w=torch.zeros(bm.N, dtype=torch.float64, device="cuda"),
+                                 u=torch.zeros(bm.N, dtype=torch.float64, device="cuda"))
+            per.append(g1)
+        ms_loop = _time(lambda: [g.run_eager() for g in per], 3, warm=1)
+        # per-mesh calls through the public API (assemble + autograd adjoint), as a
+        # user without the batched path would write them
+        from skfem_gb300.autodiff import assemble_vjp
+        api = []
+        for mm, kv, g1 in zip(meshes, ks, per):
+            api.append((g1.basis, torch.tensor(kv, device="cuda"),
+                        torch.tensor(brng.standard_normal(g1.basis.N), device="cuda"),
+                        torch.tensor(brng.standard_normal(g1.basis.N), device="cuda")))
+
+        def api_loop():
+            for bm, kt, wv, uv in api:
+                kr = kt.clone().requires_grad_(True)
+                X = bm.p_dev.clone().requires_grad_(True)
+                J = assemble_vjp(k_laplace, bm, wv, uv, X=X, k=kr)
+                J.backward()
+        api_loop()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        api_loop()
+        torch.cuda.synchronize()
+        ms_api = (time.perf_counter() - t1) * 1e3
+        ncell = int(bb.nelems)
+        out["batched_512_trip2_forward_vjp"] = {
+            "meshes": len(meshes), "nelems": ncell, "nnz": int(ga.entry.nnz), "setup_s": setup_s,
+            "autotuned": best, "ms_graph_replay": ms_graph, "ms_per_mesh_launches": ms_loop,
+            "elements_per_s_batched": ncell / (ms_graph * 1e-3),
+            "elements_per_s_per_mesh": ncell / (ms_loop * 1e-3),
+            "speedup_vs_per_mesh_launches": ms_loop / ms_graph,
+            "ms_per_mesh_api_calls": ms_api, "speedup_vs_per_mesh_api": ms_api / ms_graph,
+            "launches_per_step": ga.launches_per_step()}
+
     return out
 
 
@@ -480,12 +512,21 @@ def main():
     ap.add_argument("--cpu-nodes", type=int, default=61, help="nodes per axis of the CPU sample")
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--batch", type=int, default=512, help="meshes of the batched workload")
+    ap.add_argument("--vec-n", type=int, default=40, help="cells per axis, vector TetP2 workload")
+    ap.add_argument("--hex-n", type=int, default=64, help="cells per axis, Hex1 adjoint workload")
+    ap.add_argument("--only", default=None,
+                    choices=["tri_p1", "tet_p2_vec", "hex1_vjp", "batched"],
+                    help="run one secondary workload alone and print its record")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the TriP1 / vector TetP2 / Hex1 adjoint / batched workloads")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(secondary_workloads(args, only=args.only)))
     else:
         gpu_arm(args)
 

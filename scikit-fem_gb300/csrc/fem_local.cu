@@ -310,23 +310,13 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
           T(i, j, 1.0);
         }
 #undef T
+        // mass: delta_ab sm MM[i][j] (elasticity has none: uniform branch)
         double mij = 0.0;
-        if constexpr (D == 3 && ORDER == 2) {
-#define KM(ii, jj, v) if (((ii) == i && (jj) == j) || ((ii) == j && (jj) == i)) mij = (v);
-          TET2_MASS(KM);
-#undef KM
-        } else if constexpr (D == 2 && ORDER == 2) {
-#define KM(ii, jj, v) if (((ii) == i && (jj) == j) || ((ii) == j && (jj) == i)) mij = (v);
-          TRI2_MASS(KM);
-#undef KM
-        } else if constexpr (D == 3) {
-#define KM(ii, jj, v) if (((ii) == i && (jj) == j) || ((ii) == j && (jj) == i)) mij = (v);
-          TET1_MASS(KM);
-#undef KM
-        } else {
-#define KM(ii, jj, v) if (((ii) == i && (jj) == j) || ((ii) == j && (jj) == i)) mij = (v);
-          TRI1_MASS(KM);
-#undef KM
+        if (sm != 0.0) {
+          if constexpr (D == 3 && ORDER == 2) mij = c_tet2_mm[i][j];
+          else if constexpr (D == 2 && ORDER == 2) mij = c_tri2_mm[i][j];
+          else if constexpr (D == 3) mij = c_tet1_mm[i][j];
+          else mij = c_tri1_mm[i][j];
         }
 #pragma unroll
         for (int a = 0; a < D; ++a)

@@ -92,6 +92,17 @@ __device__ __forceinline__ void simplex_grads(const FemMesh& m, int64_t e, doubl
   vol = fabs(det) / Traits<D, 1>::FACT;
 }
 
+// local DOF of the P2 edge function between vertices a != c (element_tri_p2.py:
+// edges 01, 12, 02; element_tet_p2.py: 01, 12, 02, 03, 13, 23)
+template <int D>
+__device__ __forceinline__ constexpr int edge_dof(int a, int c) {
+  const int lo = a < c ? a : c, hi = a < c ? c : a;
+  if (D == 2) return lo == 0 ? (hi == 1 ? 3 : 5) : 4;
+  if (lo == 0) return hi == 1 ? 4 : (hi == 2 ? 6 : 7);
+  if (lo == 1) return hi == 2 ? 5 : 8;
+  return 9;
+}
+
 template <int D, int ORDER>
 __global__ void simplex_bilinear_vjp_kernel(FemMesh m, FemBasis b, FemBilinear f,
                                             const double* __restrict__ w,
@@ -117,13 +128,57 @@ __global__ void simplex_bilinear_vjp_kernel(FemMesh m, FemBasis b, FemBilinear f
 #pragma unroll
     for (int c = 0; c < NV; ++c) Q[a][c] = 0.0;
   double mu = 0.0;
+  const bool need_mass = f.mass.scale != 0.0 || dcm != nullptr;
 #define W(i) wl[i]
 #define U(i) ul[i]
 #define QQ(a, c) Q[a][c]
-  if constexpr (D == 2 && ORDER == 1) { TRI1_QACC(W, U, QQ); TRI1_MACC(W, U, mu); }
-  if constexpr (D == 2 && ORDER == 2) { TRI2_QACC(W, U, QQ); TRI2_MACC(W, U, mu); }
-  if constexpr (D == 3 && ORDER == 1) { TET1_QACC(W, U, QQ); TET1_MACC(W, U, mu); }
-  if constexpr (D == 3 && ORDER == 2) { TET2_QACC(W, U, QQ); TET2_MACC(W, U, mu); }
+  if constexpr (ORDER == 1) {
+    // P1: grad phi_a = grad lambda_a, so Q_ab = w_a u_b
+#pragma unroll
+    for (int a = 0; a < NV; ++a)
+#pragma unroll
+      for (int c = 0; c < NV; ++c) Q[a][c] = wl[a] * ul[c];
+    if (need_mass) {
+      if constexpr (D == 2) { TRI1_MACC(W, U, mu); } else { TET1_MACC(W, U, mu); }
+    }
+  } else {
+    // P2 in barycentric form: sum_i w_i p_ia = sum_c alpha_ac lambda_c with
+    // alpha_aa = 3 w_a, alpha_ac = 4 w_(edge a-c) - w_a, and
+    // (1/|T|) int lambda_c lambda_d = (1 + delta_cd) kappa, kappa = 1/((d+1)(d+2)),
+    // so Q = kappa (alpha beta^T + (alpha 1)(beta 1)^T).
+    constexpr double kappa = 1.0 / ((D + 1) * (D + 2));
+    double al[NV][NV], be[NV][NV], ra[NV], rb[NV];
+#pragma unroll
+    for (int a = 0; a < NV; ++a) {
+      ra[a] = 0.0;
+      rb[a] = 0.0;
+#pragma unroll
+      for (int c = 0; c < NV; ++c) {
+        if (a == c) {
+          al[a][c] = 3.0 * wl[a];
+          be[a][c] = 3.0 * ul[a];
+        } else {
+          const int ed = edge_dof<D>(a, c);
+          al[a][c] = 4.0 * wl[ed] - wl[a];
+          be[a][c] = 4.0 * ul[ed] - ul[a];
+        }
+        ra[a] += al[a][c];
+        rb[a] += be[a][c];
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < NV; ++a)
+#pragma unroll
+      for (int c = 0; c < NV; ++c) {
+        double v = ra[a] * rb[c];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v += al[a][k] * be[c][k];
+        Q[a][c] = kappa * v;
+      }
+    if (need_mass) {
+      if constexpr (D == 2) { TRI2_MACC(W, U, mu); } else { TET2_MACC(W, U, mu); }
+    }
+  }
 #undef W
 #undef U
 #undef QQ
@@ -221,6 +276,229 @@ __device__ __forceinline__ double adj3(const double J[3][3], double ad[3][3]) {
   return J[0][0] * ad[0][0] + J[0][1] * ad[1][0] + J[0][2] * ad[2][0];
 }
 
+// Parallelepiped cells (constant J): the 2x2x2 Gauss rule is exact for
+// every adjoint integrand, and the trilinear tensor structure makes all
+// quadrature-point values sum-factorisable.  Corner (cx,cy,cz) of the
+// reference cube carries nodal value V[cx][cy][cz]; B[c][q] = f_c(g_q) with
+// f_0(t) = 1 - t, f_1(t) = t at the two Gauss points.
+//   grad_ref v at (qx,qy,qz):  d_x v = sum_{cy,cz} (V[1][cy][cz] - V[0][cy][cz]) B[cy][qy] B[cz][qz], ...
+// With G = J^-1, M' = G G^T, c = w_q |det J| and a, b the reference
+// gradients of w_h, u_h, the per-point stress-like matrix is
+//   Z_q = c [ (kd a.M'b + km w_h u_h) I - kd (a (M'b)^T + b (M'a)^T) ]
+// and dE/dx_n = G^T R_n,  R_n[r] = sum_q sum_m Z_q[r][m] d_m phi_n(q), which
+// is again a tensor-product contraction.
+template <int MODE>
+__device__ __forceinline__ void hex_vjp_affine(const double x[8][3], const double wl[8],
+                                               const double ul[8], double kd, double km,
+                                               double& Ed, double& Em, double gx[8][3],
+                                               int32_t* status) {
+  double J[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    J[k][0] = x[4][k] - x[7][k];
+    J[k][1] = x[5][k] - x[7][k];
+    J[k][2] = x[6][k] - x[7][k];
+  }
+  double ad[3][3];
+  const double det = adj3(J, ad);
+  if (det == 0.0) {
+    if (status) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
+    return;
+  }
+  const double inv = 1.0 / det, adet = fabs(det);
+  double Gm[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Gm[a][c] = ad[a][c] * inv;
+  double Mp[3][3];  // G G^T
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = a; c < 3; ++c) {
+      const double v = Gm[a][0] * Gm[c][0] + Gm[a][1] * Gm[c][1] + Gm[a][2] * Gm[c][2];
+      Mp[a][c] = v;
+      Mp[c][a] = v;
+    }
+  // nodal values on the corner grid V[cx][cy][cz]
+  double W[2][2][2], U[2][2][2];
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+    W[c_hex_corner[n][0]][c_hex_corner[n][1]][c_hex_corner[n][2]] = wl[n];
+    U[c_hex_corner[n][0]][c_hex_corner[n][1]][c_hex_corner[n][2]] = ul[n];
+  }
+  const double g0 = c_gl2_x[0], g1 = c_gl2_x[1];
+  const double B[2][2] = {{1.0 - g0, 1.0 - g1}, {g0, g1}};
+  // reference gradients at the 8 points: A[k][qx][qy][qz]
+  double A[3][2][2][2], Bg[3][2][2][2];
+  auto grad8 = [&](const double V[2][2][2], double out[3][2][2][2]) {
+    // d_x: differences along x, interpolate in y, z (independent of qx)
+    double Dx[2][2], Dy[2][2], Dz[2][2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        Dx[i][j] = V[1][i][j] - V[0][i][j];  // (cy, cz)
+        Dy[i][j] = V[i][1][j] - V[i][0][j];  // (cx, cz)
+        Dz[i][j] = V[i][j][1] - V[i][j][0];  // (cx, cy)
+      }
+    double Tx[2][2], Ty[2][2], Tz[2][2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        Tx[q][j] = Dx[0][j] * B[0][q] + Dx[1][j] * B[1][q];  // (qy, cz)
+        Ty[q][j] = Dy[0][j] * B[0][q] + Dy[1][j] * B[1][q];  // (qx, cz)
+        Tz[q][j] = Dz[0][j] * B[0][q] + Dz[1][j] * B[1][q];  // (qx, cy)
+      }
+#pragma unroll
+    for (int qa = 0; qa < 2; ++qa)
+#pragma unroll
+      for (int qb = 0; qb < 2; ++qb) {
+        const double vx = Tx[qa][0] * B[0][qb] + Tx[qa][1] * B[1][qb];  // (qy=qa, qz=qb)
+        const double vy = Ty[qa][0] * B[0][qb] + Ty[qa][1] * B[1][qb];  // (qx=qa, qz=qb)
+        const double vz = Tz[qa][0] * B[0][qb] + Tz[qa][1] * B[1][qb];  // (qx=qa, qy=qb)
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          out[0][r][qa][qb] = vx;
+          out[1][qa][r][qb] = vy;
+          out[2][qa][qb][r] = vz;
+        }
+      }
+  };
+  grad8(W, A);
+  if (MODE == 0) grad8(U, Bg);
+  // values at the 8 points (mass / load terms)
+  double Wv[2][2][2], Uv[2][2][2];
+  auto value8 = [&](const double V[2][2][2], double out[2][2][2]) {
+    double s1[2][2][2], s2[2][2][2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) s1[q][i][j] = V[0][i][j] * B[0][q] + V[1][i][j] * B[1][q];
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+      for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) s2[q][r][j] = s1[q][0][j] * B[0][r] + s1[q][1][j] * B[1][r];
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+      for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int t = 0; t < 2; ++t) out[q][r][t] = s2[q][r][0] * B[0][t] + s2[q][r][1] * B[1][t];
+  };
+  const bool need_vals = (MODE == 1) || (km != 0.0);
+  if (need_vals) {
+    value8(W, Wv);
+    if (MODE == 0) value8(U, Uv);
+  }
+  const double c = 0.125 * adet;  // Gauss weights (1/2)^3
+  // Z_q for the 8 points, stored as Z[r][m][qx][qy][qz]
+  double Z[3][3][2][2][2];
+#pragma unroll
+  for (int qx = 0; qx < 2; ++qx)
+#pragma unroll
+    for (int qy = 0; qy < 2; ++qy)
+#pragma unroll
+      for (int qz = 0; qz < 2; ++qz) {
+        if (MODE == 0) {
+          double a[3], b[3], ap[3], bp[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            a[k] = A[k][qx][qy][qz];
+            b[k] = Bg[k][qx][qy][qz];
+          }
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            ap[k] = Mp[k][0] * a[0] + Mp[k][1] * a[1] + Mp[k][2] * a[2];
+            bp[k] = Mp[k][0] * b[0] + Mp[k][1] * b[1] + Mp[k][2] * b[2];
+          }
+          const double s = a[0] * bp[0] + a[1] * bp[1] + a[2] * bp[2];
+          const double wu = need_vals ? Wv[qx][qy][qz] * Uv[qx][qy][qz] : 0.0;
+          Ed += c * s;
+          Em += c * wu;
+          const double P = c * (kd * s + km * wu);
+          const double ck = c * kd;
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int mm = 0; mm < 3; ++mm)
+              Z[r][mm][qx][qy][qz] = (r == mm ? P : 0.0) - ck * (a[r] * bp[mm] + b[r] * ap[mm]);
+        } else {
+          const double wv = Wv[qx][qy][qz];
+          Ed += c * wv;
+          const double P = c * kd * wv;
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int mm = 0; mm < 3; ++mm) Z[r][mm][qx][qy][qz] = (r == mm ? P : 0.0);
+        }
+      }
+  // R_n[r] = sum_m sum_q Z[r][m](q) d_m phi_n(q): contract the quadrature
+  // index of direction m with the sign (derivative) and of the other two
+  // with B (transposed interpolation).
+  double R[2][2][2][3];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int k = 0; k < 2; ++k)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) R[i][j][k][r] = 0.0;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    // m = x: sum over qx, transform (qy, qz) -> (cy, cz); node sign +-1 by cx
+    double Sx[2][2], Sy[2][2], Sz[2][2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        Sx[i][j] = Z[r][0][0][i][j] + Z[r][0][1][i][j];  // (qy, qz)
+        Sy[i][j] = Z[r][1][i][0][j] + Z[r][1][i][1][j];  // (qx, qz)
+        Sz[i][j] = Z[r][2][i][j][0] + Z[r][2][i][j][1];  // (qx, qy)
+      }
+    double Hx[2][2], Hy[2][2], Hz[2][2];
+#pragma unroll
+    for (int ca = 0; ca < 2; ++ca)
+#pragma unroll
+      for (int cb = 0; cb < 2; ++cb) {
+        double hx = 0.0, hy = 0.0, hz = 0.0;
+#pragma unroll
+        for (int qa = 0; qa < 2; ++qa)
+#pragma unroll
+          for (int qb = 0; qb < 2; ++qb) {
+            const double f = B[ca][qa] * B[cb][qb];
+            hx += f * Sx[qa][qb];
+            hy += f * Sy[qa][qb];
+            hz += f * Sz[qa][qb];
+          }
+        Hx[ca][cb] = hx;
+        Hy[ca][cb] = hy;
+        Hz[ca][cb] = hz;
+      }
+#pragma unroll
+    for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+      for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+        for (int cz = 0; cz < 2; ++cz)
+          R[cx][cy][cz][r] = (cx ? Hx[cy][cz] : -Hx[cy][cz]) + (cy ? Hy[cx][cz] : -Hy[cx][cz]) +
+                             (cz ? Hz[cx][cy] : -Hz[cx][cy]);
+  }
+  // dE/dx_n = G^T R_n
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+    const double* Rn = R[c_hex_corner[n][0]][c_hex_corner[n][1]][c_hex_corner[n][2]];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) gx[n][k] = Gm[0][k] * Rn[0] + Gm[1][k] * Rn[1] + Gm[2][k] * Rn[2];
+  }
+}
+
 // mode 0: bilinear (diff, mass); mode 1: linear (load * v)
 template <int MODE>
 __global__ void hex_vjp_kernel(FemMesh m, FemBasis b, FemCoef cd, FemCoef cm,
@@ -251,7 +529,7 @@ __global__ void hex_vjp_kernel(FemMesh m, FemBasis b, FemCoef cd, FemCoef cm,
       if (c_hex_corner[n][2]) v = v + (x[6][k] - x[7][k]);
       affine = affine && (v == x[n][k]);
     }
-  const int nq = affine ? 2 : 4;
+  const int nq = affine ? 0 : 4;
   const double kd = coef_at(cd, e), km = MODE == 0 ? coef_at(cm, e) : 0.0;
   double Ed = 0.0, Em = 0.0;
   double gx[8][3];
@@ -259,10 +537,11 @@ __global__ void hex_vjp_kernel(FemMesh m, FemBasis b, FemCoef cd, FemCoef cm,
   for (int n = 0; n < 8; ++n)
 #pragma unroll
     for (int k = 0; k < 3; ++k) gx[n][k] = 0.0;
+  if (affine) hex_vjp_affine<MODE>(x, wl, ul, kd, km, Ed, Em, gx, status);
   for (int q = 0; q < nq * nq * nq; ++q) {
     const int qx = q % nq, qy = (q / nq) % nq, qz = q / (nq * nq);
-    const double* xs = affine ? c_gl2_x : c_gl4_x;
-    const double* ws = affine ? c_gl2_w : c_gl4_w;
+    const double* xs = c_gl4_x;
+    const double* ws = c_gl4_w;
     double phi[8], dphi[8][3];
     hex_shape(xs[qx], xs[qy], xs[qz], phi, dphi);
     const double wq = ws[qx] * ws[qy] * ws[qz];

@@ -301,6 +301,9 @@ def main():
         out.append(emit_reduced(tag, d, o))
     out.append(emit_bb_terms("TET2BB", 3))
     out.append(emit_bb_terms("TRI2BB", 2))
+    for tag, d, o in (("tri1", 2, 1), ("tri2", 2, 2), ("tet1", 3, 1), ("tet2", 3, 2)):
+        _, MM, _ = simplex_tables(d, o)
+        out.append(emit_array("c_%s_mm" % tag, MM))
     HS, HM, HL = hex_tables()
     out.append(emit_array("c_hex_S", HS))
     out.append(emit_array("c_hex_M", HM))
