@@ -72,6 +72,15 @@ __device__ __forceinline__ double coef_at(const FemCoef& c, int64_t e) {
   return c.field ? c.scale * c.field[e] : c.scale;
 }
 
+// Reference-cube corner (0/1 per axis) of Hex1 node n: node 0 sits at
+// (1,1,1) and node 7 at (0,0,0) (refdom.py:173-180).  constexpr so that
+// unrolled loops index registers, not memory.
+__host__ __device__ constexpr int hex_corner(int n, int ax) {
+  constexpr int tab[8][3] = {{1, 1, 1}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1},
+                             {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0, 0, 0}};
+  return tab[n][ax];
+}
+
 // Exclusive scan of n int32 counts into out (n+1 entries); device scratch
 // from the caller's allocation helper.  Returns the total via *total (host).
 int exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, int64_t* total,

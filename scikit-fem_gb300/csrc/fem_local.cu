@@ -24,6 +24,8 @@
 // separately rounded arithmetic -- as numpy evaluates them -- come out as
 // exact zeros; that build feeds the eliminate_zeros mask of the pattern.
 
+#include <type_traits>
+
 #include "fem_common.cuh"
 #include "fem_tables.cuh"
 
@@ -36,8 +38,23 @@
 namespace FEM_NS {
 
 using fem::coef_at;
+using fem::hex_corner;
 
 constexpr int kBlock = 128;
+
+// Compile-time loop: f(std::integral_constant<int, I>) for I = 0 .. N-1, so
+// that array indices derived from I are constants (registers, not memory).
+template <int I, int N, typename F>
+__device__ __forceinline__ void static_for_impl(F& f) {
+  if constexpr (I < N) {
+    f(std::integral_constant<int, I>{});
+    static_for_impl<I + 1, N>(f);
+  }
+}
+template <int N, typename F>
+__device__ __forceinline__ void static_for(F&& f) {
+  static_for_impl<0, N>(f);
+}
 
 // --------------------------------------------------------------- geometry
 // c[a] = det(A) * grad(lambda_a) for the barycentric coordinates of the
@@ -218,17 +235,18 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
   constexpr int NS = SimplexTraits<D, ORDER>::NB;  // scalar functions
   constexpr int NB = NS * D;                        // vector functions
   constexpr int NV = D + 1;
-  constexpr int NPAIR = NV * (NV + 1) / 2;
   constexpr int RB = D * NB;                        // values per node row block
   constexpr double FACT = SimplexTraits<D, ORDER>::FACT;
   extern __shared__ double smem[];
-  double* Es = smem;                                 // [NPAIR*D*D][BS]
-  double* rows = smem + NPAIR * D * D * BS;          // [BS][RB+1]
+  double* rows = smem;                               // [BS][RB+1]
   const int64_t e0 = (int64_t)blockIdx.x * BS;
   const int64_t e = e0 + threadIdx.x;
   const int tid = threadIdx.x;
   const bool live = e < m.nelems;
   double sm = 0.0;
+  // E[p][q][a][b] for p <= q, kept in registers: every index below is a
+  // compile-time constant once the block loops are unrolled.
+  double E[NV][NV][D][D];
   if (live) {
     check_coef_bits(f, e, ref_bits, status);
     Simplex<D> s;
@@ -240,9 +258,8 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
     const double lap = coef_at(f.lap, e) * s0;
     const double tr = coef_at(f.tr, e) * s0;
     sm = coef_at(f.mass, e) * (adet / FACT);
-    int pq = 0;
 #pragma unroll
-    for (int p = 0; p < NV; ++p) {
+    for (int p = 0; p < NV; ++p)
 #pragma unroll
       for (int q = p; q < NV; ++q) {
         const double g = lap * dotc<D>(s.c[p], s.c[q]);
@@ -252,20 +269,16 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
           for (int b = 0; b < D; ++b) {
             double v = lam * (s.c[p][a] * s.c[q][b]) + tr * (s.c[p][b] * s.c[q][a]);
             if (a == b) v = v + g;
-            Es[((pq * D + a) * D + b) * BS + tid] = v;
+            E[p][q][a][b] = v;
           }
-        ++pq;
       }
-    }
   }
-  // pair index of (p, q), p <= q
-  auto pidx = [](int p, int q) { return p * NV - (p * (p - 1)) / 2 + (q - p); };
-#pragma unroll 1
-  for (int i = 0; i < NS; ++i) {
+  static_for<NS>([&](auto ic) {
+    constexpr int i = decltype(ic)::value;
     if (live) {
       double* row = rows + tid * (RB + 1);
-#pragma unroll
-      for (int j = 0; j < NS; ++j) {
+      static_for<NS>([&](auto jc) {
+        constexpr int j = decltype(jc)::value;
         double blk[D][D];
 #pragma unroll
         for (int a = 0; a < D; ++a)
@@ -273,38 +286,29 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
           for (int b = 0; b < D; ++b) blk[a][b] = 0.0;
 #define T(p, q, c)                                                                   \
   {                                                                                  \
-    const int _pp = (p) <= (q) ? (p) : (q), _qq = (p) <= (q) ? (q) : (p);            \
-    const int _k = pidx(_pp, _qq);                                                   \
     _Pragma("unroll") for (int a = 0; a < D; ++a) _Pragma("unroll") for (int b = 0; b < D; ++b) { \
-      const double ev = (p) <= (q) ? Es[((_k * D + a) * D + b) * BS + tid]           \
-                                   : Es[((_k * D + b) * D + a) * BS + tid];          \
+      const double ev = (p) <= (q) ? E[(p)][(q)][a][b] : E[(q)][(p)][b][a];          \
       blk[a][b] = blk[a][b] + (c) * ev;                                              \
     }                                                                                \
   }
         if constexpr (D == 3 && ORDER == 2) {
-          switch (i) {
-            case 0: TET2BB_ROW0(j, T); break;
-            case 1: TET2BB_ROW1(j, T); break;
-            case 2: TET2BB_ROW2(j, T); break;
-            case 3: TET2BB_ROW3(j, T); break;
-            case 4: TET2BB_ROW4(j, T); break;
-            case 5: TET2BB_ROW5(j, T); break;
-            case 6: TET2BB_ROW6(j, T); break;
-            case 7: TET2BB_ROW7(j, T); break;
-            case 8: TET2BB_ROW8(j, T); break;
-            case 9: TET2BB_ROW9(j, T); break;
-            default: break;
-          }
+          if constexpr (i == 0) { TET2BB_ROW0(j, T); }
+          if constexpr (i == 1) { TET2BB_ROW1(j, T); }
+          if constexpr (i == 2) { TET2BB_ROW2(j, T); }
+          if constexpr (i == 3) { TET2BB_ROW3(j, T); }
+          if constexpr (i == 4) { TET2BB_ROW4(j, T); }
+          if constexpr (i == 5) { TET2BB_ROW5(j, T); }
+          if constexpr (i == 6) { TET2BB_ROW6(j, T); }
+          if constexpr (i == 7) { TET2BB_ROW7(j, T); }
+          if constexpr (i == 8) { TET2BB_ROW8(j, T); }
+          if constexpr (i == 9) { TET2BB_ROW9(j, T); }
         } else if constexpr (D == 2 && ORDER == 2) {
-          switch (i) {
-            case 0: TRI2BB_ROW0(j, T); break;
-            case 1: TRI2BB_ROW1(j, T); break;
-            case 2: TRI2BB_ROW2(j, T); break;
-            case 3: TRI2BB_ROW3(j, T); break;
-            case 4: TRI2BB_ROW4(j, T); break;
-            case 5: TRI2BB_ROW5(j, T); break;
-            default: break;
-          }
+          if constexpr (i == 0) { TRI2BB_ROW0(j, T); }
+          if constexpr (i == 1) { TRI2BB_ROW1(j, T); }
+          if constexpr (i == 2) { TRI2BB_ROW2(j, T); }
+          if constexpr (i == 3) { TRI2BB_ROW3(j, T); }
+          if constexpr (i == 4) { TRI2BB_ROW4(j, T); }
+          if constexpr (i == 5) { TRI2BB_ROW5(j, T); }
         } else {
           // P1: grad phi_i = grad lambda_i, BB[i][j][p][q] = delta_ip delta_jq
           T(i, j, 1.0);
@@ -326,7 +330,7 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
             if (a == b) v = v + sm * mij;
             row[a * NB + j * D + b] = v;
           }
-      }
+      });
     }
     // stream rows (i*D .. i*D+D-1) of every element of the block
     __syncthreads();
@@ -337,7 +341,7 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
       out[(e0 + el) * (int64_t)(NB * NB) + (int64_t)i * RB + k] = rows[el * (RB + 1) + k];
     }
     __syncthreads();
-  }
+  });
 }
 
 // ----------------------------------------------------------- hexahedron Q1
@@ -371,9 +375,9 @@ __device__ __forceinline__ bool hex_affine(const Hex& h, double J[3][3]) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       double v = h.x[7][k];
-      if (c_hex_corner[n][0]) v = v + J[k][0];
-      if (c_hex_corner[n][1]) v = v + J[k][1];
-      if (c_hex_corner[n][2]) v = v + J[k][2];
+      if (hex_corner(n, 0)) v = v + J[k][0];
+      if (hex_corner(n, 1)) v = v + J[k][1];
+      if (hex_corner(n, 2)) v = v + J[k][2];
       ok = ok && (v == h.x[n][k]);
     }
   }
@@ -414,7 +418,7 @@ __device__ __forceinline__ void hex_shape(double x, double y, double z, double p
                                           double dphi[8][3]) {
 #pragma unroll
   for (int n = 0; n < 8; ++n) {
-    const int cx = c_hex_corner[n][0], cy = c_hex_corner[n][1], cz = c_hex_corner[n][2];
+    const int cx = hex_corner(n, 0), cy = hex_corner(n, 1), cz = hex_corner(n, 2);
     const double fx = cx ? x : 1.0 - x, fy = cy ? y : 1.0 - y, fz = cz ? z : 1.0 - z;
     const double sx = cx ? 1.0 : -1.0, sy = cy ? 1.0 : -1.0, sz = cz ? 1.0 : -1.0;
     phi[n] = fx * fy * fz;
@@ -667,9 +671,9 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
     switch (fam) {
 #define LAUNCH_V(D, O)                                                                 \
   {                                                                                    \
-    constexpr int NS = SimplexTraits<D, O>::NB, NB = NS * D, NV = D + 1;               \
-    constexpr int NPAIR = NV * (NV + 1) / 2, RB = D * NB;                              \
-    const size_t sm = ((size_t)NPAIR * D * D * 64 + (size_t)64 * (RB + 1)) * sizeof(double); \
+    constexpr int NS = SimplexTraits<D, O>::NB, NB = NS * D;                          \
+    constexpr int RB = D * NB;                                                         \
+    const size_t sm = (size_t)64 * (RB + 1) * sizeof(double);                          \
     if ((rc = set_smem(simplex_vector_kernel<D, O>, sm))) return rc;                   \
     simplex_vector_kernel<D, O><<<(unsigned)vgrid, 64, sm, st>>>(m, f, out, ref_bits, status);           \
     break;                                                                             \

@@ -35,6 +35,7 @@ int build_incidence(const int32_t* dofs, int64_t nelems, int nb, int64_t nrows, 
 namespace fem_vjp {
 
 using fem::coef_at;
+using fem::hex_corner;
 
 template <int D, int ORDER>
 struct Traits;
@@ -254,7 +255,7 @@ __device__ __forceinline__ void hex_shape(double x, double y, double z, double p
                                           double dphi[8][3]) {
 #pragma unroll
   for (int n = 0; n < 8; ++n) {
-    const int cx = c_hex_corner[n][0], cy = c_hex_corner[n][1], cz = c_hex_corner[n][2];
+    const int cx = hex_corner(n, 0), cy = hex_corner(n, 1), cz = hex_corner(n, 2);
     const double fx = cx ? x : 1.0 - x, fy = cy ? y : 1.0 - y, fz = cz ? z : 1.0 - z;
     phi[n] = fx * fy * fz;
     dphi[n][0] = (cx ? 1.0 : -1.0) * (fy * fz);
@@ -324,15 +325,15 @@ __device__ __forceinline__ void hex_vjp_affine(const double x[8][3], const doubl
   double W[2][2][2], U[2][2][2];
 #pragma unroll
   for (int n = 0; n < 8; ++n) {
-    W[c_hex_corner[n][0]][c_hex_corner[n][1]][c_hex_corner[n][2]] = wl[n];
-    U[c_hex_corner[n][0]][c_hex_corner[n][1]][c_hex_corner[n][2]] = ul[n];
+    W[hex_corner(n, 0)][hex_corner(n, 1)][hex_corner(n, 2)] = wl[n];
+    U[hex_corner(n, 0)][hex_corner(n, 1)][hex_corner(n, 2)] = ul[n];
   }
   const double g0 = c_gl2_x[0], g1 = c_gl2_x[1];
   const double B[2][2] = {{1.0 - g0, 1.0 - g1}, {g0, g1}};
-  // reference gradients at the 8 points: A[k][qx][qy][qz]
-  double A[3][2][2][2], Bg[3][2][2][2];
-  auto grad8 = [&](const double V[2][2][2], double out[3][2][2][2]) {
-    // d_x: differences along x, interpolate in y, z (independent of qx)
+  // Reference gradients at the 8 points, stored compactly: d_x v depends on
+  // (qy, qz) only, d_y v on (qx, qz), d_z v on (qx, qy).
+  auto grad4 = [&](const double V[2][2][2], double gx_[2][2], double gy_[2][2],
+                   double gz_[2][2]) {
     double Dx[2][2], Dy[2][2], Dz[2][2];
 #pragma unroll
     for (int i = 0; i < 2; ++i)
@@ -342,54 +343,46 @@ __device__ __forceinline__ void hex_vjp_affine(const double x[8][3], const doubl
         Dy[i][j] = V[i][1][j] - V[i][0][j];  // (cx, cz)
         Dz[i][j] = V[i][j][1] - V[i][j][0];  // (cx, cy)
       }
-    double Tx[2][2], Ty[2][2], Tz[2][2];
-#pragma unroll
-    for (int q = 0; q < 2; ++q)
-#pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        Tx[q][j] = Dx[0][j] * B[0][q] + Dx[1][j] * B[1][q];  // (qy, cz)
-        Ty[q][j] = Dy[0][j] * B[0][q] + Dy[1][j] * B[1][q];  // (qx, cz)
-        Tz[q][j] = Dz[0][j] * B[0][q] + Dz[1][j] * B[1][q];  // (qx, cy)
-      }
 #pragma unroll
     for (int qa = 0; qa < 2; ++qa)
 #pragma unroll
       for (int qb = 0; qb < 2; ++qb) {
-        const double vx = Tx[qa][0] * B[0][qb] + Tx[qa][1] * B[1][qb];  // (qy=qa, qz=qb)
-        const double vy = Ty[qa][0] * B[0][qb] + Ty[qa][1] * B[1][qb];  // (qx=qa, qz=qb)
-        const double vz = Tz[qa][0] * B[0][qb] + Tz[qa][1] * B[1][qb];  // (qx=qa, qy=qb)
+        double tx = 0.0, ty = 0.0, tz = 0.0;
 #pragma unroll
-        for (int r = 0; r < 2; ++r) {
-          out[0][r][qa][qb] = vx;
-          out[1][qa][r][qb] = vy;
-          out[2][qa][qb][r] = vz;
-        }
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+          for (int j = 0; j < 2; ++j) {
+            const double f = B[i][qa] * B[j][qb];
+            tx += f * Dx[i][j];
+            ty += f * Dy[i][j];
+            tz += f * Dz[i][j];
+          }
+        gx_[qa][qb] = tx;
+        gy_[qa][qb] = ty;
+        gz_[qa][qb] = tz;
       }
   };
-  grad8(W, A);
-  if (MODE == 0) grad8(U, Bg);
+  double wx[2][2], wy[2][2], wz[2][2], ux[2][2], uy[2][2], uz[2][2];
+  grad4(W, wx, wy, wz);
+  if (MODE == 0) grad4(U, ux, uy, uz);
   // values at the 8 points (mass / load terms)
   double Wv[2][2][2], Uv[2][2][2];
   auto value8 = [&](const double V[2][2][2], double out[2][2][2]) {
-    double s1[2][2][2], s2[2][2][2];
-#pragma unroll
-    for (int q = 0; q < 2; ++q)
-#pragma unroll
-      for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 2; ++j) s1[q][i][j] = V[0][i][j] * B[0][q] + V[1][i][j] * B[1][q];
 #pragma unroll
     for (int q = 0; q < 2; ++q)
 #pragma unroll
       for (int r = 0; r < 2; ++r)
 #pragma unroll
-        for (int j = 0; j < 2; ++j) s2[q][r][j] = s1[q][0][j] * B[0][r] + s1[q][1][j] * B[1][r];
+        for (int t = 0; t < 2; ++t) {
+          double acc = 0.0;
 #pragma unroll
-    for (int q = 0; q < 2; ++q)
+          for (int i = 0; i < 2; ++i)
 #pragma unroll
-      for (int r = 0; r < 2; ++r)
+            for (int j = 0; j < 2; ++j)
 #pragma unroll
-        for (int t = 0; t < 2; ++t) out[q][r][t] = s2[q][r][0] * B[0][t] + s2[q][r][1] * B[1][t];
+              for (int k = 0; k < 2; ++k) acc += V[i][j][k] * (B[i][q] * B[j][r] * B[k][t]);
+          out[q][r][t] = acc;
+        }
   };
   const bool need_vals = (MODE == 1) || (km != 0.0);
   if (need_vals) {
@@ -397,21 +390,26 @@ __device__ __forceinline__ void hex_vjp_affine(const double x[8][3], const doubl
     if (MODE == 0) value8(U, Uv);
   }
   const double c = 0.125 * adet;  // Gauss weights (1/2)^3
-  // Z_q for the 8 points, stored as Z[r][m][qx][qy][qz]
-  double Z[3][3][2][2][2];
+  // Partial sums of Z_q over the quadrature index of each derivative
+  // direction: Sx[r][qy][qz] = sum_qx Z_q[r][x], Sy[r][qx][qz], Sz[r][qx][qy].
+  double Sx[3][2][2], Sy[3][2][2], Sz[3][2][2];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) Sx[r][i][j] = Sy[r][i][j] = Sz[r][i][j] = 0.0;
 #pragma unroll
   for (int qx = 0; qx < 2; ++qx)
 #pragma unroll
     for (int qy = 0; qy < 2; ++qy)
 #pragma unroll
       for (int qz = 0; qz < 2; ++qz) {
+        double Z[3][3];
         if (MODE == 0) {
-          double a[3], b[3], ap[3], bp[3];
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            a[k] = A[k][qx][qy][qz];
-            b[k] = Bg[k][qx][qy][qz];
-          }
+          const double a[3] = {wx[qy][qz], wy[qx][qz], wz[qx][qy]};
+          const double b[3] = {ux[qy][qz], uy[qx][qz], uz[qx][qy]};
+          double ap[3], bp[3];
 #pragma unroll
           for (int k = 0; k < 3; ++k) {
             ap[k] = Mp[k][0] * a[0] + Mp[k][1] * a[1] + Mp[k][2] * a[2];
@@ -427,7 +425,7 @@ __device__ __forceinline__ void hex_vjp_affine(const double x[8][3], const doubl
           for (int r = 0; r < 3; ++r)
 #pragma unroll
             for (int mm = 0; mm < 3; ++mm)
-              Z[r][mm][qx][qy][qz] = (r == mm ? P : 0.0) - ck * (a[r] * bp[mm] + b[r] * ap[mm]);
+              Z[r][mm] = (r == mm ? P : 0.0) - ck * (a[r] * bp[mm] + b[r] * ap[mm]);
         } else {
           const double wv = Wv[qx][qy][qz];
           Ed += c * wv;
@@ -435,33 +433,20 @@ __device__ __forceinline__ void hex_vjp_affine(const double x[8][3], const doubl
 #pragma unroll
           for (int r = 0; r < 3; ++r)
 #pragma unroll
-            for (int mm = 0; mm < 3; ++mm) Z[r][mm][qx][qy][qz] = (r == mm ? P : 0.0);
+            for (int mm = 0; mm < 3; ++mm) Z[r][mm] = (r == mm ? P : 0.0);
+        }
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          Sx[r][qy][qz] += Z[r][0];
+          Sy[r][qx][qz] += Z[r][1];
+          Sz[r][qx][qy] += Z[r][2];
         }
       }
-  // R_n[r] = sum_m sum_q Z[r][m](q) d_m phi_n(q): contract the quadrature
-  // index of direction m with the sign (derivative) and of the other two
-  // with B (transposed interpolation).
+  // R_n[r] = sum_m sum_q Z_q[r][m] d_m phi_n(q): transposed interpolation of
+  // the partial sums, sign by the node's corner in the derivative direction.
   double R[2][2][2][3];
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 2; ++j)
-#pragma unroll
-      for (int k = 0; k < 2; ++k)
-#pragma unroll
-        for (int r = 0; r < 3; ++r) R[i][j][k][r] = 0.0;
-#pragma unroll
   for (int r = 0; r < 3; ++r) {
-    // m = x: sum over qx, transform (qy, qz) -> (cy, cz); node sign +-1 by cx
-    double Sx[2][2], Sy[2][2], Sz[2][2];
-#pragma unroll
-    for (int i = 0; i < 2; ++i)
-#pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        Sx[i][j] = Z[r][0][0][i][j] + Z[r][0][1][i][j];  // (qy, qz)
-        Sy[i][j] = Z[r][1][i][0][j] + Z[r][1][i][1][j];  // (qx, qz)
-        Sz[i][j] = Z[r][2][i][j][0] + Z[r][2][i][j][1];  // (qx, qy)
-      }
     double Hx[2][2], Hy[2][2], Hz[2][2];
 #pragma unroll
     for (int ca = 0; ca < 2; ++ca)
@@ -473,9 +458,9 @@ __device__ __forceinline__ void hex_vjp_affine(const double x[8][3], const doubl
 #pragma unroll
           for (int qb = 0; qb < 2; ++qb) {
             const double f = B[ca][qa] * B[cb][qb];
-            hx += f * Sx[qa][qb];
-            hy += f * Sy[qa][qb];
-            hz += f * Sz[qa][qb];
+            hx += f * Sx[r][qa][qb];
+            hy += f * Sy[r][qa][qb];
+            hz += f * Sz[r][qa][qb];
           }
         Hx[ca][cb] = hx;
         Hy[ca][cb] = hy;
@@ -493,20 +478,21 @@ __device__ __forceinline__ void hex_vjp_affine(const double x[8][3], const doubl
   // dE/dx_n = G^T R_n
 #pragma unroll
   for (int n = 0; n < 8; ++n) {
-    const double* Rn = R[c_hex_corner[n][0]][c_hex_corner[n][1]][c_hex_corner[n][2]];
+    const double* Rn = R[hex_corner(n, 0)][hex_corner(n, 1)][hex_corner(n, 2)];
 #pragma unroll
     for (int k = 0; k < 3; ++k) gx[n][k] = Gm[0][k] * Rn[0] + Gm[1][k] * Rn[1] + Gm[2][k] * Rn[2];
   }
 }
 
-// mode 0: bilinear (diff, mass); mode 1: linear (load * v)
+// Non-parallelepiped cells: the 4x4x4 isoparametric rule (kept out of line
+// so that its registers do not load the common parallelepiped path).
 template <int MODE>
-__global__ void hex_vjp_kernel(FemMesh m, FemBasis b, FemCoef cd, FemCoef cm,
-                               const double* __restrict__ w, const double* __restrict__ u,
-                               double* __restrict__ dcd, double* __restrict__ dcm,
-                               double* __restrict__ scratch, int32_t* __restrict__ status) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= m.nelems) return;
+__device__ __noinline__ void hex_vjp_general(const FemMesh m, const FemBasis b, const FemCoef cd,
+                                             const FemCoef cm, const double* __restrict__ w,
+                                             const double* __restrict__ u, double* dcd,
+                                             double* dcm, double* scratch, int32_t* status,
+                                             int64_t e) {
+  const int nq = 4;
   double x[8][3], wl[8], ul[8];
 #pragma unroll
   for (int n = 0; n < 8; ++n) {
@@ -517,19 +503,6 @@ __global__ void hex_vjp_kernel(FemMesh m, FemBasis b, FemCoef cd, FemCoef cm,
     wl[n] = w[dof];
     ul[n] = MODE == 0 ? u[dof] : 0.0;
   }
-  // parallelepiped test (as the forward kernel)
-  bool affine = true;
-#pragma unroll
-  for (int n = 0; n < 8; ++n)
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      double v = x[7][k];
-      if (c_hex_corner[n][0]) v = v + (x[4][k] - x[7][k]);
-      if (c_hex_corner[n][1]) v = v + (x[5][k] - x[7][k]);
-      if (c_hex_corner[n][2]) v = v + (x[6][k] - x[7][k]);
-      affine = affine && (v == x[n][k]);
-    }
-  const int nq = affine ? 0 : 4;
   const double kd = coef_at(cd, e), km = MODE == 0 ? coef_at(cm, e) : 0.0;
   double Ed = 0.0, Em = 0.0;
   double gx[8][3];
@@ -537,7 +510,6 @@ __global__ void hex_vjp_kernel(FemMesh m, FemBasis b, FemCoef cd, FemCoef cm,
   for (int n = 0; n < 8; ++n)
 #pragma unroll
     for (int k = 0; k < 3; ++k) gx[n][k] = 0.0;
-  if (affine) hex_vjp_affine<MODE>(x, wl, ul, kd, km, Ed, Em, gx, status);
   for (int q = 0; q < nq * nq * nq; ++q) {
     const int qx = q % nq, qy = (q / nq) % nq, qz = q / (nq * nq);
     const double* xs = c_gl4_x;
@@ -616,6 +588,56 @@ __global__ void hex_vjp_kernel(FemMesh m, FemBasis b, FemCoef cd, FemCoef cm,
       for (int a = 0; a < 3; ++a)
         gx[n][a] += D[a][0] * dphi[n][0] + D[a][1] * dphi[n][1] + D[a][2] * dphi[n][2];
   }
+  if (dcd) dcd[e] = cd.scale * Ed;
+  if (MODE == 0 && dcm) dcm[e] = cm.scale * Em;
+#pragma unroll
+  for (int n = 0; n < 8; ++n)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) scratch[(e * 8 + n) * 3 + a] = gx[n][a];
+}
+
+// mode 0: bilinear (diff, mass); mode 1: linear (load * v)
+template <int MODE>
+__global__ void hex_vjp_kernel(FemMesh m, FemBasis b, FemCoef cd, FemCoef cm,
+                               const double* __restrict__ w, const double* __restrict__ u,
+                               double* __restrict__ dcd, double* __restrict__ dcm,
+                               double* __restrict__ scratch, int32_t* __restrict__ status) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.nelems) return;
+  double x[8][3], wl[8], ul[8];
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+    const int64_t v = m.t[n * m.nelems + e];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) x[n][k] = m.p[k * m.nverts + v];
+    const int64_t dof = b.element_dofs[n * m.nelems + e];
+    wl[n] = w[dof];
+    ul[n] = MODE == 0 ? u[dof] : 0.0;
+  }
+  // parallelepiped test (as the forward kernel)
+  bool affine = true;
+#pragma unroll
+  for (int n = 0; n < 8; ++n)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double v = x[7][k];
+      if (hex_corner(n, 0)) v = v + (x[4][k] - x[7][k]);
+      if (hex_corner(n, 1)) v = v + (x[5][k] - x[7][k]);
+      if (hex_corner(n, 2)) v = v + (x[6][k] - x[7][k]);
+      affine = affine && (v == x[n][k]);
+    }
+  const double kd = coef_at(cd, e), km = MODE == 0 ? coef_at(cm, e) : 0.0;
+  double Ed = 0.0, Em = 0.0;
+  double gx[8][3];
+#pragma unroll
+  for (int n = 0; n < 8; ++n)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) gx[n][k] = 0.0;
+  if (!affine) {
+    hex_vjp_general<MODE>(m, b, cd, cm, w, u, dcd, dcm, scratch, status, e);
+    return;
+  }
+  hex_vjp_affine<MODE>(x, wl, ul, kd, km, Ed, Em, gx, status);
   if (dcd) dcd[e] = cd.scale * Ed;
   if (MODE == 0 && dcm) dcm[e] = cm.scale * Em;
 #pragma unroll
