@@ -249,6 +249,22 @@ int fem_linear_vjp(const FemMesh* mesh, const FemBasis* basis, const FemLinear* 
                    const FemPattern* vertex_incidence, const double* w, double* dload, double* dX,
                    double* elem_scratch, fem_stream_t stream);
 
+/*
+ * Dirichlet condensation of a device CSR matrix (skfem/utils.py:462-600,
+ * condense): A_II = A[I][:, I] and b_I = b[I] - A[I][:, D] x[D].  map[r] is
+ * the position of DOF r among the kept DOFs I (ascending) or -1.  Phase 1
+ * writes out_indptr (nkeep+1) and *out_nnz (synchronises `stream`);
+ * phase 2 fills indices, values and, when out_b is given, the right-hand
+ * side (b and x may be NULL: zero).
+ */
+int fem_condense_pattern(const int32_t* indptr, const int32_t* indices, int64_t nrows,
+                         const int32_t* map, int64_t nkeep, int32_t* out_indptr, int64_t* out_nnz,
+                         fem_stream_t stream);
+int fem_condense_values(const int32_t* indptr, const int32_t* indices, const double* vals,
+                        int64_t nrows, const int32_t* map, const double* b, const double* x,
+                        const int32_t* out_indptr, int32_t* out_indices, double* out_vals,
+                        double* out_b, fem_stream_t stream);
+
 /* Vertex incidence of the mesh (rows = vertices), used by the adjoint's
  * fixed-order gather of per-element coordinate gradients. */
 int fem_vertex_incidence_build(const FemMesh* mesh, FemPattern** out, fem_stream_t stream);

@@ -597,7 +597,8 @@ class OBasis:
     """CellBasis restated: eager per-basis-function value/grad fields at all
     quadrature points, and dx = |detDF| * W (cell_basis.py:101-105)."""
 
-    def __init__(self, mesh: OMesh, elem: OElement, intorder: Optional[int] = None):
+    def __init__(self, mesh: OMesh, elem: OElement, intorder: Optional[int] = None,
+                 elements=None):
         refdom = {"tri": "tri", "tet": "tet", "hex": "hex"}[mesh.kind]
         if refdom != elem.refdom:
             raise ValueError("Incompatible Mesh and Element.")  # abstract_basis.py:55-56
@@ -605,6 +606,17 @@ class OBasis:
         self.element_dofs, self.N = element_dofs(mesh, elem)
         self.Nbfun = self.element_dofs.shape[0]
         self.nelems = mesh.nelements
+        if elements is not None:
+            # CellBasis(elements=...) (cell_basis.py:94-99): normalize_elements
+            # (mesh.py:1331-1369) with callables tested on cell midpoints
+            # (mesh.py:481-493); geometry and DOFs restricted to the subset
+            if callable(elements):
+                tind = np.nonzero(elements(mesh.p[:, mesh.t].mean(axis=1)))[0].astype(np.int32)
+            else:
+                tind = np.asarray(elements)
+            self.element_dofs = self.element_dofs[:, tind]
+            self.mesh = mesh = OMesh(mesh.p, mesh.t[:, tind], mesh.kind)
+            self.nelems = len(tind)
         self.X, self.W = quadrature(refdom, intorder if intorder is not None
                                     else 2 * elem.maxdeg)
         self.dim = mesh.p.shape[0]

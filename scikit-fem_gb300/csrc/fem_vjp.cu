@@ -330,6 +330,16 @@ __device__ __forceinline__ void hex_vjp_affine(const double x[8][3], const doubl
   }
   const double g0 = c_gl2_x[0], g1 = c_gl2_x[1];
   const double B[2][2] = {{1.0 - g0, 1.0 - g1}, {g0, g1}};
+  // BB[i][j][qa][qb] = B[i][qa] * B[j][qb], shared by every transform below
+  double BB[2][2][2][2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int qa = 0; qa < 2; ++qa)
+#pragma unroll
+        for (int qb = 0; qb < 2; ++qb) BB[i][j][qa][qb] = B[i][qa] * B[j][qb];
   // Reference gradients at the 8 points, stored compactly: d_x v depends on
   // (qy, qz) only, d_y v on (qx, qz), d_z v on (qx, qy).
   auto grad4 = [&](const double V[2][2][2], double gx_[2][2], double gy_[2][2],
@@ -352,7 +362,7 @@ __device__ __forceinline__ void hex_vjp_affine(const double x[8][3], const doubl
         for (int i = 0; i < 2; ++i)
 #pragma unroll
           for (int j = 0; j < 2; ++j) {
-            const double f = B[i][qa] * B[j][qb];
+            const double f = BB[i][j][qa][qb];
             tx += f * Dx[i][j];
             ty += f * Dy[i][j];
             tz += f * Dz[i][j];
@@ -421,11 +431,22 @@ __device__ __forceinline__ void hex_vjp_affine(const double x[8][3], const doubl
           Em += c * wu;
           const double P = c * (kd * s + km * wu);
           const double ck = c * kd;
+          // Z_q = P I - ck (a bp^T + b ap^T), added straight into the partial sums
 #pragma unroll
-          for (int r = 0; r < 3; ++r)
+          for (int k = 0; k < 3; ++k) {
+            ap[k] *= ck;
+            bp[k] *= ck;
+          }
 #pragma unroll
-            for (int mm = 0; mm < 3; ++mm)
-              Z[r][mm] = (r == mm ? P : 0.0) - ck * (a[r] * bp[mm] + b[r] * ap[mm]);
+          for (int r = 0; r < 3; ++r) {
+            Sx[r][qy][qz] = Sx[r][qy][qz] - a[r] * bp[0] - b[r] * ap[0];
+            Sy[r][qx][qz] = Sy[r][qx][qz] - a[r] * bp[1] - b[r] * ap[1];
+            Sz[r][qx][qy] = Sz[r][qx][qy] - a[r] * bp[2] - b[r] * ap[2];
+          }
+          Sx[0][qy][qz] += P;
+          Sy[1][qx][qz] += P;
+          Sz[2][qx][qy] += P;
+          continue;
         } else {
           const double wv = Wv[qx][qy][qz];
           Ed += c * wv;
@@ -457,7 +478,7 @@ __device__ __forceinline__ void hex_vjp_affine(const double x[8][3], const doubl
         for (int qa = 0; qa < 2; ++qa)
 #pragma unroll
           for (int qb = 0; qb < 2; ++qb) {
-            const double f = B[ca][qa] * B[cb][qb];
+            const double f = BB[ca][cb][qa][qb];
             hx += f * Sx[r][qa][qb];
             hy += f * Sy[r][qa][qb];
             hz += f * Sz[r][qa][qb];

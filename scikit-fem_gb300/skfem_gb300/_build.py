@@ -29,6 +29,7 @@ UNITS = [
     ("fem_abi.cu", "fem_abi.o", []),
     ("fem_noalloc.cu", "fem_noalloc.o", []),
     ("fem_faithful.cu", "fem_faithful.o", ["-fmad=false"]),
+    ("fem_condense.cu", "fem_condense.o", []),
 ]
 
 

@@ -88,6 +88,10 @@ _SIGS = {
     "fem_bilinear_vjp": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "fem_linear_vjp": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "fem_vertex_incidence_build": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_void_p), _P]),
+    "fem_condense_pattern": (ctypes.c_int, [_P, _P, ctypes.c_int64, _P, ctypes.c_int64, _P,
+                                            _I64P, _P]),
+    "fem_condense_values": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _P, _P, _P, _P, _P, _P,
+                                           _P, _P]),
     "fem_set_tuning": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "fem_assemble_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
 }

@@ -28,14 +28,20 @@ class CellBasis:
         if mapping is not None:
             raise NotImplementedError("custom mappings are not supported; the kernels use the "
                                       "mesh's own affine / isoparametric mapping")
-        if elements is not None:
-            raise NotImplementedError("element subsets are not implemented yet")
         self.mesh = mesh
         self.elem = elem
         self.dofs = Dofs(mesh, elem) if dofs is None else dofs
         self.Nbfun = self.dofs.element_dofs.shape[0]
-        self.nelems = mesh.nelements
-        self.tind = None
+        # element subset (cell_basis.py:94-99): the kernels run over the
+        # selected cells only, with the global DOF numbering unchanged
+        if elements is None:
+            self.tind = None
+            self.nelems = mesh.nelements
+        else:
+            self.tind = mesh.normalize_elements(elements)
+            if self.tind.size and (self.tind.min() < 0 or self.tind.max() >= mesh.nelements):
+                raise ValueError("element index out of range")
+            self.nelems = len(self.tind)
         self.intorder = intorder if intorder is not None else 2 * elem.maxdeg
         if quadrature is not None:
             raise NotImplementedError("custom quadrature rules are not supported by the kernels")
@@ -56,10 +62,11 @@ class CellBasis:
     # -------------------------------------------------------------- device
     def _upload(self):
         dev = self.device
+        t = self.mesh.t if self.tind is None else self.mesh.t[:, self.tind]
+        ed = self.element_dofs
         self.p_dev = torch.from_numpy(np.ascontiguousarray(self.mesh.p)).to(dev)
-        self.t_dev = torch.from_numpy(np.ascontiguousarray(self.mesh.t)).to(dev)
-        ed = self.dofs.element_dofs
-        if ed.shape == self.mesh.t.shape and np.array_equal(ed, self.mesh.t):
+        self.t_dev = torch.from_numpy(np.ascontiguousarray(t)).to(dev)
+        if ed.shape == t.shape and np.array_equal(ed, t):
             self.ed_dev = self.t_dev
         else:
             self.ed_dev = torch.from_numpy(np.ascontiguousarray(ed)).to(dev)
@@ -85,7 +92,10 @@ class CellBasis:
 
     @property
     def element_dofs(self):
-        return self.dofs.element_dofs
+        """abstract_basis.py:110-117 (restricted to the element subset)."""
+        if self.tind is None:
+            return self.dofs.element_dofs
+        return self.dofs.element_dofs[:, self.tind]
 
     def zero_w(self, dtype=None):
         """abstract_basis.py:378-382."""

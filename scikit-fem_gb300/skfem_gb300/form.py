@@ -201,8 +201,6 @@ class _PatternEntry:
             self.staging = torch.empty(max(1, self.pat.staging_bytes // 8), dtype=torch.float64,
                                        device=dev)
             torch.cuda.current_stream().synchronize()
-            self.indptr_h = self.indptr.cpu().numpy()
-            self.indices_h = self.indices.cpu().numpy()
         else:
             self.staging = torch.empty(max(1, basis.nelems * basis.Nbfun), dtype=torch.float64,
                                        device=dev)
@@ -258,10 +256,18 @@ class BilinearForm(Form):
             entry, vals, coeffs, key, _f = self._device_assemble(ubasis, vbasis, **kwargs)
             if self._check_status(ubasis, entry, key):
                 break
-        data = np.empty(entry.nnz, dtype=np.float64)
-        torch.from_numpy(data).copy_(vals)
-        K = sp.csr_matrix((data, entry.indices_h.copy(), entry.indptr_h.copy()),
-                          shape=(ubasis.N, ubasis.N))
+        # Device -> pinned host copies (torch's caching host allocator reuses
+        # the blocks of matrices the caller has dropped); the returned matrix
+        # owns its arrays through their numpy views.
+        data = torch.empty(entry.nnz, dtype=torch.float64, pin_memory=True)
+        indices = torch.empty(entry.nnz, dtype=torch.int32, pin_memory=True)
+        indptr = torch.empty(entry.nrows + 1, dtype=torch.int32, pin_memory=True)
+        data.copy_(vals, non_blocking=True)
+        indices.copy_(entry.indices, non_blocking=True)
+        indptr.copy_(entry.indptr, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        K = sp.csr_matrix((data.numpy(), indices.numpy(), indptr.numpy()),
+                          shape=(ubasis.N, ubasis.N), copy=False)
         K.has_sorted_indices = True
         K.has_canonical_format = True
         return K
@@ -316,9 +322,10 @@ class LinearForm(Form):
 
     def assemble(self, basis, vbasis=None, **kwargs):
         b, _ = self._device_assemble(basis, vbasis, **kwargs)
-        out = np.empty(basis.N, dtype=np.float64)
-        torch.from_numpy(out).copy_(b)
-        return out
+        out = torch.empty(basis.N, dtype=torch.float64, pin_memory=True)
+        out.copy_(b, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return out.numpy()
 
     def assemble_torch(self, basis, vbasis=None, **kwargs):
         b, _ = self._device_assemble(basis, vbasis, **kwargs)

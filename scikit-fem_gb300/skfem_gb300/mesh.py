@@ -56,6 +56,31 @@ class Mesh:
     def dim(self):
         return self.p.shape[0]
 
+    def elements_satisfying(self, test):
+        """Cells whose midpoints satisfy ``test`` (mesh.py:481-493)."""
+        midp = self.p[:, self.t].mean(axis=1)
+        return np.nonzero(test(midp))[0].astype(np.int32)
+
+    def normalize_elements(self, elements):
+        """Element indices from the reference's selectors (mesh.py:1331-1369):
+        True, an index, an index array (a boolean mask selects its True
+        cells), a callable on cell midpoints, or a list of those."""
+        if isinstance(elements, bool) and elements:
+            return np.arange(self.nelements, dtype=np.int32)
+        if isinstance(elements, (int, np.integer)):
+            return np.array([elements], dtype=np.int32)
+        if isinstance(elements, np.ndarray):
+            if elements.dtype == bool:
+                return np.nonzero(elements)[0].astype(np.int32)
+            return elements.astype(np.int32)
+        if callable(elements):
+            return self.elements_satisfying(elements)
+        if isinstance(elements, (tuple, list, set)):
+            return np.unique(np.concatenate([self.normalize_elements(e) for e in elements]))
+        if isinstance(elements, str):
+            raise ValueError("Subdomain '{}' not found.".format(elements))
+        raise NotImplementedError
+
     # ------------------------------------------------------------ entities
     def _build(self, name, local_pairs):
         if name not in self._entities:

@@ -184,6 +184,20 @@ def main():
     save("tet_p1_jitter_laplace", p=m.p, t=m.t, element_dofs=ib.element_dofs,
          X=ib.X, W=ib.W, b=unit_load.assemble(ib), **csr_arrays(laplace.assemble(ib)))
 
+    # 10. element subset: TriP2 k*Laplace on the cells with midpoint x < 0.5,
+    #     and TetP1 Laplace + load on an index subset
+    m = MeshTri.init_tensor(np.linspace(0, 1, 9), np.linspace(0, 1, 9))
+    ib = Basis(m, ElementTriP2(), elements=lambda x: x[0] < 0.5)
+    k = rng.lognormal(0.0, 0.5, ib.nelems)
+    K = k_laplace.assemble(ib, k=ib.zero_w() + k[:, None])
+    save("tri_p2_subset", p=m.p, t=m.t, element_dofs=ib.element_dofs, tind=ib.tind,
+         X=ib.X, W=ib.W, k=k, b=unit_load.assemble(ib), **csr_arrays(K))
+    m = MeshTet.init_tensor(*(np.linspace(0, 1, 5),) * 3)
+    tind = np.arange(0, m.t.shape[1], 3).astype(np.int32)
+    ib = Basis(m, ElementTetP1(), elements=tind)
+    save("tet_p1_subset", p=m.p, t=m.t, element_dofs=ib.element_dofs, tind=ib.tind,
+         X=ib.X, W=ib.W, b=unit_load.assemble(ib), **csr_arrays(laplace.assemble(ib)))
+
     # quadrature rules the configs use, exactly as the reference tabulates them
     from skfem.quadrature import get_quadrature_tet, get_quadrature_tri
     rules = {}

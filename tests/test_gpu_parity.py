@@ -290,3 +290,46 @@ def test_stale_pattern_is_rebuilt():
     assert K2.nnz < K1.nnz
     np.testing.assert_array_equal(K2.indptr, Ko.indptr)
     np.testing.assert_array_equal(K2.indices, Ko.indices)
+
+
+def test_element_subsets_vs_reference():
+    """CellBasis(elements=...) (cell_basis.py:94-99): a callable on cell
+    midpoints and an index array, against scikit-fem's own results."""
+    g = golden("tri_p2_subset")
+    b = F.Basis(F.MeshTri(g["p"], g["t"]), F.ElementTriP2(), elements=lambda x: x[0] < 0.5)
+    np.testing.assert_array_equal(b.tind, g["tind"])
+    check_matrix(k_laplace.assemble(b, k=b.zero_w() + g["k"][:, None]), g)
+    vec = unit_load.assemble(b)
+    assert np.max(np.abs(vec - g["b"])) <= REL_MAX * np.max(np.abs(g["b"]))
+    g = golden("tet_p1_subset")
+    b = F.Basis(F.MeshTet(g["p"], g["t"]), F.ElementTetP1(), elements=g["tind"])
+    check_matrix(laplace.assemble(b), g)
+    vec = unit_load.assemble(b)
+    assert np.max(np.abs(vec - g["b"])) <= REL_MAX * np.max(np.abs(g["b"]))
+
+
+def test_condense_on_device_matches_reference_semantics():
+    """utils.condense (utils.py:462-600) on the device CSR: A[I][:, I] and
+    b[I] - A[I][:, D] x[D], against scipy applied to the same matrix."""
+    from skfem_gb300.utils import condense
+    m = F.MeshTet.init_tensor(*(np.linspace(0, 1, 7),) * 3)
+    b = F.Basis(m, F.ElementTetP1())
+    rng = np.random.default_rng(2)
+    k = rng.lognormal(0, 1, m.nelements)
+    A = k_laplace_mass.assemble_torch(b, k=b.zero_w() + k[:, None])
+    rhs = torch.tensor(rng.standard_normal(b.N), device="cuda")
+    x = torch.tensor(rng.standard_normal(b.N), device="cuda")
+    p = m.p
+    D = np.nonzero(np.any((p < 1e-12) | (p > 1 - 1e-12), axis=0))[0]
+    AII, bI, xr, I = condense(A, rhs, x=x, D=D)
+    Ks = k_laplace_mass.assemble(b, k=b.zero_w() + k[:, None])
+    Iref = np.setdiff1d(np.arange(b.N), D)
+    Aref = Ks[Iref][:, Iref].tocsr()
+    bref = rhs.cpu().numpy()[Iref] - Ks[Iref][:, D] @ x.cpu().numpy()[D]
+    np.testing.assert_array_equal(AII.crow_indices().cpu().numpy(), Aref.indptr)
+    np.testing.assert_array_equal(AII.col_indices().cpu().numpy(), Aref.indices)
+    np.testing.assert_array_equal(AII.values().cpu().numpy(), Aref.data)
+    np.testing.assert_allclose(bI.cpu().numpy(), bref, rtol=1e-13, atol=1e-13 * np.abs(bref).max())
+    np.testing.assert_array_equal(I.cpu().numpy(), Iref)
+    # only A: the reference returns the matrix alone when b is None and expand=False
+    assert isinstance(condense(A, D=D, expand=False), torch.Tensor)

@@ -117,3 +117,16 @@ def test_closed_form_rules_match_reference_tables(refdom, order):
     Xc, Wc = O.skfem_oracle.quadrature_closed_form(refdom, order)
     np.testing.assert_allclose(Xc, X, rtol=0, atol=2e-15)
     np.testing.assert_allclose(Wc, W, rtol=0, atol=2e-15)
+
+
+def test_element_subsets():
+    g = load("tri_p2_subset")
+    m = O.OMesh(g["p"], g["t"], "tri")
+    b = O.OBasis(m, O.TriP2(), elements=lambda x: x[0] < 0.5)
+    np.testing.assert_array_equal(b.element_dofs, g["element_dofs"])
+    check_csr(O.bilinear_assemble(O.k_laplace, b, k=b.zero_w() + g["k"][:, None]), g)
+    np.testing.assert_allclose(O.linear_assemble(O.unit_load, b), g["b"], rtol=1e-13, atol=1e-17)
+    g = load("tet_p1_subset")
+    b = O.OBasis(O.OMesh(g["p"], g["t"], "tet"), O.TetP1(), elements=g["tind"])
+    check_csr(O.bilinear_assemble(O.laplace, b), g)
+    np.testing.assert_allclose(O.linear_assemble(O.unit_load, b), g["b"], rtol=1e-13, atol=1e-17)
