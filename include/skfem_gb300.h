@@ -110,8 +110,14 @@ typedef struct FemLinear {
  * order, for the exact-zero mask of the pattern build (see
  * fem_pattern_build).  Instruction k computes register k:
  *   op 0 CONST imm | 1 U a (trial quantity a) | 2 V a (test quantity a) |
- *   3 COEF a (coefficient slot a) | 4 ADD a b | 5 SUB a b | 6 MUL a b |
- *   7 DIV a b | 8 NEG a
+ *   3 COEF a (coefficient slot a at the point) | 4 ADD a b | 5 SUB a b |
+ *   6 MUL a b | 7 DIV a b | 8 NEG a | 9 X a (global coordinate a at the
+ *   point, MappingAffine.F / MappingIsoparametric.F arithmetic) | 10 H (mesh
+ *   parameter |detDF|**(1/dim)) | 11 SQRT a | 12 EXP a | 13 LOG a | 14 SIN a |
+ *   15 COS a | 16 TAN a | 17 TANH a | 18 ARCTAN a | 19 ABS a | 20 POW a b.
+ *   Operands a, b of arithmetic ops name earlier instructions.  Ops 12-18 and
+ *   20 use the CUDA math library (last-bit differences from numpy possible);
+ *   all others are correctly rounded and reproduce the reference bit for bit.
  * Quantity c is the value of component c, ncomp + c*dim + k the derivative
  * k of component c (ncomp = dim for vector bases, 1 for scalar ones).
  */
@@ -123,10 +129,14 @@ typedef struct FemInstr {
 typedef struct FemProgram {
   int32_t ninstr;         /* <= 512 */
   int32_t out;            /* register holding the integrand */
-  int32_t ncoef;          /* <= 8 */
-  int32_t nq;             /* quantity of quadrature points of the basis */
+  int32_t ncoef;          /* <= 16 */
+  int32_t nq;             /* quadrature points of the basis (<= 128) */
   const FemInstr* ins;    /* device array of ninstr instructions */
-  const double* coef[8];  /* per-element coefficient fields (device) */
+  const double* coef[16]; /* coefficient slots (device): one value per element
+                             (stride 0) or per quadrature point (stride nq) */
+  int32_t coef_stride[16];
+  const double* qX;       /* the basis's reference points (dim, nq), device; */
+  const double* qW;       /* and weights (nq); required by fem_program_*     */
 } FemProgram;
 
 /* Opaque one-time structure: row incidence, CSR pattern, local-to-slot map. */
@@ -264,6 +274,53 @@ int fem_condense_values(const int32_t* indptr, const int32_t* indices, const dou
                         int64_t nrows, const int32_t* map, const double* b, const double* x,
                         const int32_t* out_indptr, int32_t* out_indices, double* out_vals,
                         double* out_b, fem_stream_t stream);
+
+/*
+ * Generic forms.  Any form the tracer records as a FemProgram -- anisotropic
+ * or advection-type terms, coefficients varying inside cells, interpolated
+ * DOF-vector coefficients, quadrature-point coordinates -- is evaluated per
+ * quadrature point with the reference's own arithmetic (the replay of
+ * fem_pattern_build): the local entries are the reference's bit for bit.
+ * fem_program_local_matrices: local[(e*nbfun + i)*nbfun + j] (test i, trial j);
+ * fem_program_local_vectors: local[e*nbfun + i] (linear forms: trial-free program);
+ * fem_program_elemental: out[e] = integral over element e (Functional).
+ */
+int fem_program_local_matrices(const FemMesh* mesh, const FemBasis* basis,
+                               const FemProgram* program, double* local, int32_t* status,
+                               fem_stream_t stream);
+int fem_program_local_vectors(const FemMesh* mesh, const FemBasis* basis,
+                              const FemProgram* program, double* local, int32_t* status,
+                              fem_stream_t stream);
+int fem_program_elemental(const FemMesh* mesh, const FemBasis* basis, const FemProgram* program,
+                          double* out, int32_t* status, fem_stream_t stream);
+
+/* Pattern (incidence + CSR + slot map) whose eliminate_zeros mask is the
+ * given local matrices' exact zeros (local from fem_program_local_matrices). */
+int fem_pattern_build_local(const FemMesh* mesh, const FemBasis* basis, const double* local,
+                            FemPattern** out, fem_stream_t stream);
+
+/* Segmented sum that also verifies the zero structure: status receives
+ * FEM_ERR_STALE_PATTERN if a nonzero local entry has no CSR slot or a CSR
+ * entry has no nonzero contribution (exact zero masks, generic forms). */
+int fem_csr_sum_checked(const FemPattern* pat, const double* local, double* csr_values,
+                        int32_t* status, fem_stream_t stream);
+
+/*
+ * Basis.interpolate (skfem/assembly/basis/abstract_basis.py:271-322): the
+ * DOF vector w (device, ndofs) at the nq reference points X (device, (dim,
+ * nq)) of every element, with the reference's arithmetic (sum over local
+ * functions in order).  out (device) holds nquant x nelems x nq doubles,
+ * quantity-major: scalar bases value, d/dx_0 .. d/dx_{dim-1} (nquant =
+ * 1 + dim); vector bases the dim components, then grad[c][k] at
+ * dim + c*dim + k (nquant = dim + dim*dim).
+ */
+int fem_interpolate(const FemMesh* mesh, const FemBasis* basis, int32_t nq, const double* X,
+                    const double* w, double* out, fem_stream_t stream);
+
+/* np.sum of a contiguous device vector of n doubles in numpy's pairwise
+ * order (leaves of <= 128 values, split at n/2 rounded down to a multiple
+ * of 8); *out (device) receives the sum (Functional.assemble). */
+int fem_sum_pairwise(const double* x, int64_t n, double* out, fem_stream_t stream);
 
 /* Vertex incidence of the mesh (rows = vertices), used by the adjoint's
  * fixed-order gather of per-element coordinate gradients. */

@@ -705,6 +705,30 @@ class OBasis:
         G[c] = g
         return (DField(v, G),)
 
+    def default_parameters(self):
+        """CellBasis.default_parameters (cell_basis.py:124-141): global
+        coordinates of the quadrature points (MappingAffine.F,
+        mapping_affine.py:183-193; MappingIsoparametric.F,
+        mapping_isoparametric.py:50-58, 170-171) and the mesh parameter
+        h = |detDF|**(1/dim)."""
+        m, X, dim = self.mesh, self.X, self.dim
+        if m.affine:
+            x = np.empty((dim, self.nelems, X.shape[1]))
+            for i in range(dim):
+                s = 0.0
+                for j in range(dim):
+                    s = s + self.A[i, j][:, None] * X[j][None, :]
+                x[i] = s + self.b[i][:, None]
+        else:
+            x = np.zeros((dim, self.nelems, X.shape[1]))
+            el = Hex1()
+            for itr in range(m.t.shape[0]):
+                phi, _ = el.lbasis(X, itr)
+                for i in range(dim):
+                    x[i] += m.p[i, m.t[itr]][:, None] * phi
+        h = np.abs(self.detDF) ** (1.0 / dim)
+        return {"x": DField(x), "h": DField(h)}
+
     def zero_w(self):
         # abstract_basis.py:378-382
         return np.zeros((self.nelems, len(self.W)))
@@ -727,10 +751,20 @@ class OBasis:
 # 102-108, form.py:91-121)
 # --------------------------------------------------------------------------
 
+class OParams(dict):
+    """FormExtraParams (form.py:13-26): keys also readable as attributes."""
+
+    def __getattr__(self, name):
+        if name in self:
+            return self[name]
+        raise AttributeError("Attribute '{}' not found in 'w'.".format(name))
+
+
 def _normalize_w(basis: OBasis, w: Dict) -> Dict:
     # form.py:91-121: numbers pass through, 1-D arrays are DOF vectors that
-    # get interpolated, 2-D arrays become fields (checked against nqp).
-    out = {}
+    # get interpolated, 2-D arrays become fields (checked against nqp); the
+    # basis's default parameters come first (bilinear_form.py:77-80).
+    out = OParams(basis.default_parameters())
     for k, v in w.items():
         if isinstance(v, np.ndarray) and v.ndim == 1:
             out[k] = basis.interpolate(v)

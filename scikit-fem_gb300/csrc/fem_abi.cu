@@ -26,6 +26,12 @@ int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, 
 int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st);
 int vector_sum(const Pattern& P, const double* local, double* b, cudaStream_t st);
 void free_pattern(Pattern* P);
+int zero_check(const Pattern& P, const double* local, int32_t* status, cudaStream_t st);
+int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemProgram& prog,
+                 double* out, int32_t* status, cudaStream_t st);
+int interpolate(const FemMesh& m, const FemBasis& b, int nq, const double* X, const double* w,
+                double* out, cudaStream_t st);
+int sum_pairwise(const double* x, int64_t n, double* out, cudaStream_t st);
 int faithful_mask(const FemMesh& m, const FemBasis& b, const FemProgram& prog, int nq, double* local,
                   int32_t* status, cudaStream_t st);
 
@@ -368,6 +374,92 @@ int fem_assemble_vector(const FemMesh* mesh, const FemBasis* basis, const FemLin
   rc = fem_fast::local_vectors(*mesh, *basis, *form, staging, nullptr, st);
   if (rc) return rc;
   return fem::vector_sum(pat->P, staging, b, st);
+}
+
+static int program_entry(int mode, const FemMesh* mesh, const FemBasis* basis,
+                         const FemProgram* program, double* out, int32_t* status,
+                         fem_stream_t stream) {
+  int rc = validate(mesh, basis);
+  if (rc) return rc;
+  if (!program || !out || !status) {
+    set_error(FEM_ERR_ARGUMENT, "null program, output or status");
+    return FEM_ERR_ARGUMENT;
+  }
+  return fem::program_eval(mode, *mesh, *basis, *program, out, status, (cudaStream_t)stream);
+}
+
+int fem_program_local_matrices(const FemMesh* mesh, const FemBasis* basis,
+                               const FemProgram* program, double* local, int32_t* status,
+                               fem_stream_t stream) {
+  return program_entry(0, mesh, basis, program, local, status, stream);
+}
+
+int fem_program_local_vectors(const FemMesh* mesh, const FemBasis* basis,
+                              const FemProgram* program, double* local, int32_t* status,
+                              fem_stream_t stream) {
+  return program_entry(1, mesh, basis, program, local, status, stream);
+}
+
+int fem_program_elemental(const FemMesh* mesh, const FemBasis* basis, const FemProgram* program,
+                          double* out, int32_t* status, fem_stream_t stream) {
+  return program_entry(2, mesh, basis, program, out, status, stream);
+}
+
+int fem_pattern_build_local(const FemMesh* mesh, const FemBasis* basis, const double* local,
+                            FemPattern** out, fem_stream_t stream) {
+  int rc = validate(mesh, basis);
+  if (rc) return rc;
+  if (!out || (!local && mesh->nelems > 0)) {
+    set_error(FEM_ERR_ARGUMENT, "null local matrices or output handle");
+    return FEM_ERR_ARGUMENT;
+  }
+  *out = nullptr;
+  cudaStream_t st = (cudaStream_t)stream;
+  FemPattern* H = new FemPattern();
+  H->family = basis->family;
+  H->vector = basis->vector;
+  rc = fem::build_incidence(basis->element_dofs, mesh->nelems, basis->nbfun, basis->ndofs, &H->P, st);
+  if (!rc) rc = fem::build_csr(basis->element_dofs, basis->nbfun, basis->ndofs, local, &H->P, st);
+  if (rc) {
+    fem::free_pattern(new fem::Pattern(H->P));
+    delete H;
+    return rc;
+  }
+  *out = H;
+  return 0;
+}
+
+int fem_csr_sum_checked(const FemPattern* pat, const double* local, double* csr_values,
+                        int32_t* status, fem_stream_t stream) {
+  if (!pat || !local || !csr_values || !status) {
+    set_error(FEM_ERR_ARGUMENT, "null pattern, buffer or status");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (!pat->P.has_matrix) {
+    set_error(FEM_ERR_ARGUMENT, "pattern has no CSR structure");
+    return FEM_ERR_ARGUMENT;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = fem::zero_check(pat->P, local, status, st);
+  if (rc) return rc;
+  fem::Pattern P = pat->P;
+  P.sum_unroll = fem::tuning_for(pat->family).sum_unroll;
+  return fem::csr_sum(P, local, csr_values, st);
+}
+
+int fem_interpolate(const FemMesh* mesh, const FemBasis* basis, int32_t nq, const double* X,
+                    const double* w, double* out, fem_stream_t stream) {
+  int rc = validate(mesh, basis);
+  if (rc) return rc;
+  return fem::interpolate(*mesh, *basis, nq, X, w, out, (cudaStream_t)stream);
+}
+
+int fem_sum_pairwise(const double* x, int64_t n, double* out, fem_stream_t stream) {
+  if ((!x && n > 0) || !out || n < 0) {
+    set_error(FEM_ERR_ARGUMENT, "null input or output");
+    return FEM_ERR_ARGUMENT;
+  }
+  return fem::sum_pairwise(x, n, out, (cudaStream_t)stream);
 }
 
 }  // extern "C"

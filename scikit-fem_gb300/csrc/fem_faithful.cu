@@ -31,6 +31,8 @@
 
 #include "fem_faithful_core.cuh"
 
+#include <vector>
+
 namespace fem_faithful {
 
 __device__ bool rule_for(int refdim, bool hex, int nq, Rule& r) {
@@ -55,7 +57,9 @@ __global__ void mask_kernel(FemMesh m, FemBasis b, FemProgram prog, int nq, doub
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m.nelems) return;
   Rule rule;
-  if (!rule_for(D, b.family == FEM_HEX_1, nq, rule)) {
+  if (prog.qX && prog.qW) {
+    rule = {prog.qX, prog.qW, prog.nq};
+  } else if (!rule_for(D, b.family == FEM_HEX_1, nq, rule)) {
     atomicOr(status, 1 << FEM_ERR_UNSUPPORTED);
     return;
   }
@@ -63,31 +67,226 @@ __global__ void mask_kernel(FemMesh m, FemBasis b, FemProgram prog, int nq, doub
   double* Ke = local + e * (int64_t)NB * NB;
   double scale = 0.0;
   for (int k = 0; k < NB * NB; ++k) scale = fmax(scale, fabs(Ke[k]));
-  double coef[8];
-  for (int c = 0; c < prog.ncoef && c < 8; ++c) coef[c] = prog.coef[c] ? prog.coef[c][e] : 0.0;
   double R[kMaxProgram];
-  double vals[64];
+  double vals[kMaxPoints];
   for (int i = 0; i < NB; ++i) {      // test function (row)
     for (int j = 0; j < NB; ++j) {    // trial function (column)
       const double v = Ke[i * NB + j];
       if (fabs(v) > tau * scale) continue;
-      const double s = replay_entry<D>(m, b, prog, rule, e, i, j, coef, R, vals);
+      const double s = replay_entry<D>(m, b, prog, rule, e, i, j, R, vals);
       // the buffer only feeds the mask: mark exact zeros / noise nonzeros
       Ke[i * NB + j] = (s == 0.0) ? 0.0 : (v != 0.0 ? v : 1e-300);
     }
   }
 }
 
+// ------------------------------------------------------------ generic forms
+// One block takes EPB cells.  Stage 1: the geometry of every (cell, point)
+// pair into shared memory.  Stage 2: form * dx for every (cell, entry,
+// point) triple into shared memory.  Stage 3: numpy's pairwise sum over the
+// points of each entry.  MODE 0: bilinear (L = nbfun^2 entries, row = test
+// function), 1: linear (L = nbfun), 2: functional (L = 1).
+struct GenericShape {
+  int epb, L, nq;
+};
+
+template <int D, int MODE>
+__global__ void program_kernel(FemMesh m, FemBasis b, FemProgram prog, Rule rule, GenericShape s,
+                               double* __restrict__ out, int32_t* __restrict__ status) {
+  extern __shared__ double gsm[];
+  constexpr int kGeo = 14;  // inv 9, det, qx 4
+  double* geo = gsm;
+  double* val = gsm + (size_t)s.epb * s.nq * kGeo;
+  const bool hex = b.family == FEM_HEX_1;
+  const ProgFlags f = prog_flags(prog);
+  const int64_t e0 = (int64_t)blockIdx.x * s.epb;
+  const int nb = b.nbfun;
+  for (int k = threadIdx.x; k < s.epb * s.nq; k += blockDim.x) {
+    const int el = k / s.nq, q = k - el * s.nq;
+    const int64_t e = e0 + el;
+    if (e >= m.nelems) continue;
+    CellGeo c;
+    cell_geometry<D>(m, e, hex, c);
+    const double x = rule.X[q], y = rule.X[rule.nq + q];
+    const double z = D == 3 ? rule.X[2 * rule.nq + q] : 0.0;
+    PointGeo g;
+    point_geometry<D>(m, e, hex, c, f, x, y, z, g);
+    if (hex && g.det == 0.0) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
+    double* G = geo + (size_t)k * kGeo;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) G[i * 3 + j] = g.inv[i][j];
+    G[9] = g.det;
+    for (int i = 0; i < 4; ++i) G[10 + i] = g.qx[i];
+  }
+  __syncthreads();
+  double R[kMaxProgram];
+  const int per = s.L * s.nq;
+  for (int k = threadIdx.x; k < s.epb * per; k += blockDim.x) {
+    const int el = k / per;
+    const int rq = k - el * per;
+    const int r = rq / s.nq, q = rq - r * s.nq;
+    const int64_t e = e0 + el;
+    if (e >= m.nelems) continue;
+    const int i = MODE == 0 ? r / nb : (MODE == 1 ? r : 0);
+    const int j = MODE == 0 ? r - i * nb : 0;
+    const double* G = geo + ((size_t)el * s.nq + q) * kGeo;
+    PointGeo g;
+    for (int a = 0; a < 3; ++a)
+      for (int c = 0; c < 3; ++c) g.inv[a][c] = G[a * 3 + c];
+    g.det = G[9];
+    for (int a = 0; a < 4; ++a) g.qx[a] = G[10 + a];
+    const double x = rule.X[q], y = rule.X[rule.nq + q];
+    const double z = D == 3 ? rule.X[2 * rule.nq + q] : 0.0;
+    val[k] = point_value<D>(b, prog, e, q, i, j, x, y, z, g, rule.W[q], R);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < s.epb * s.L; k += blockDim.x) {
+    const int el = k / s.L;
+    const int64_t e = e0 + el;
+    if (e >= m.nelems) continue;
+    out[e0 * s.L + k] = np_pairwise_sum(val + (size_t)k * s.nq, s.nq);
+  }
+}
+
+// Basis.interpolate for one (cell, point) per thread: quantity k of the
+// field, out[(k * nelems + e) * nq + q] = 0*(w0 phi_0) + sum_i w_i phi_i
+// in local-function order (abstract_basis.py:295-304).
+template <int D>
+__global__ void interpolate_kernel(FemMesh m, FemBasis b, Rule rule, const double* __restrict__ w,
+                                   double* __restrict__ out) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m.nelems * rule.nq) return;
+  const int64_t e = t / rule.nq;
+  const int q = (int)(t - e * rule.nq);
+  const bool hex = b.family == FEM_HEX_1;
+  const bool vec = b.vector != 0;
+  CellGeo c;
+  cell_geometry<D>(m, e, hex, c);
+  const double x = rule.X[q], y = rule.X[rule.nq + q];
+  const double z = D == 3 ? rule.X[2 * rule.nq + q] : 0.0;
+  PointGeo g;
+  point_geometry<D>(m, e, hex, c, ProgFlags(), x, y, z, g);
+  constexpr int NQ = D + D * D;
+  const int nquant = vec ? D + D * D : 1 + D;
+  double acc[NQ], qq[NQ];
+  const double w0 = w[b.element_dofs[e]];
+  quantities<D>(b.family, vec, 0, x, y, z, g.inv, qq);
+  for (int k = 0; k < nquant; ++k) acc[k] = 0.0 * (w0 * qq[k]);
+  for (int i = 0; i < b.nbfun; ++i) {
+    const double wi = w[b.element_dofs[(int64_t)i * m.nelems + e]];
+    quantities<D>(b.family, vec, i, x, y, z, g.inv, qq);
+    for (int k = 0; k < nquant; ++k) acc[k] = acc[k] + wi * qq[k];
+  }
+  for (int k = 0; k < nquant; ++k) out[((int64_t)k * m.nelems + e) * rule.nq + q] = acc[k];
+}
+
+// numpy's pairwise sum of n doubles (np.sum of a contiguous vector): the
+// leaves (<= 128 values) in parallel, the combination tree by one thread.
+__global__ void pairwise_leaves_kernel(const double* __restrict__ x, int64_t n,
+                                       const int64_t* __restrict__ leaf_off,
+                                       const int32_t* __restrict__ leaf_len, int64_t nleaves,
+                                       double* __restrict__ leaf_sum) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nleaves) leaf_sum[k] = np_pairwise_sum(x + leaf_off[k], leaf_len[k]);
+}
+
+__global__ void pairwise_tree_kernel(const double* __restrict__ leaf_sum, int64_t n,
+                                     double* __restrict__ out) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  if (n == 0) {
+    *out = 0.0;
+    return;
+  }
+  // the same split recursion as np_pairwise_sum_any, consuming leaves in order
+  struct Frame { int64_t n; int state; double left; };
+  Frame st[64];
+  int sp = 0;
+  st[0] = {n, 0, 0.0};
+  int64_t leaf = 0;
+  double ret = 0.0;
+  while (sp >= 0) {
+    Frame& f = st[sp];
+    if (f.n <= 128) {
+      ret = leaf_sum[leaf++];
+      --sp;
+      continue;
+    }
+    int64_t n2 = f.n / 2;
+    n2 -= n2 % 8;
+    if (f.state == 0) {
+      f.state = 1;
+      st[sp + 1] = {n2, 0, 0.0};
+      ++sp;
+    } else if (f.state == 1) {
+      f.left = ret;
+      f.state = 2;
+      st[sp + 1] = {f.n - n2, 0, 0.0};
+      ++sp;
+    } else {
+      ret = f.left + ret;
+      --sp;
+    }
+  }
+  *out = ret;
+}
+
 }  // namespace fem_faithful
 namespace fem {
-int faithful_mask(const FemMesh& m, const FemBasis& b, const FemProgram& prog, int nq, double* local,
-                  int32_t* status, cudaStream_t st) {
-  if (prog.ninstr <= 0 || prog.ninstr > fem_faithful::kMaxProgram || prog.out < 0 ||
-      prog.out >= prog.ninstr || prog.ncoef > 8) {
-    set_error(FEM_ERR_UNSUPPORTED, "form program of %d instructions (limit %d)", prog.ninstr,
-              fem_faithful::kMaxProgram);
+
+// Host-side check of a form program before any kernel interprets it: every
+// operand names an earlier register, a basis quantity, a coefficient slot
+// or a coordinate that exists.
+int check_program(const FemProgram& prog, int dim, bool vec, bool need_rule) {
+  using namespace fem_faithful;
+  if (prog.ninstr <= 0 || prog.ninstr > kMaxProgram || prog.out < 0 ||
+      prog.out >= prog.ninstr || prog.ncoef < 0 || prog.ncoef > kMaxCoef || !prog.ins ||
+      prog.nq <= 0 || prog.nq > kMaxPoints) {
+    set_error(FEM_ERR_UNSUPPORTED,
+              "form program of %d instructions, %d coefficients, %d points (limits %d, %d, %d)",
+              prog.ninstr, prog.ncoef, prog.nq, kMaxProgram, kMaxCoef, kMaxPoints);
     return FEM_ERR_UNSUPPORTED;
   }
+  if (need_rule && (!prog.qX || !prog.qW)) {
+    set_error(FEM_ERR_ARGUMENT, "form program without quadrature points (qX, qW)");
+    return FEM_ERR_ARGUMENT;
+  }
+  for (int c = 0; c < prog.ncoef; ++c)
+    if (prog.coef_stride[c] != 0 && prog.coef_stride[c] != prog.nq) {
+      set_error(FEM_ERR_ARGUMENT, "coefficient slot %d: stride %d (0 or %d)", c,
+                prog.coef_stride[c], prog.nq);
+      return FEM_ERR_ARGUMENT;
+    }
+  FemInstr h[kMaxProgram];
+  FEM_TRY_CUDA(cudaMemcpy(h, prog.ins, prog.ninstr * sizeof(FemInstr), cudaMemcpyDefault));
+  const int nquant = vec ? dim + dim * dim : 1 + dim;
+  for (int k = 0; k < prog.ninstr; ++k) {
+    const FemInstr& I = h[k];
+    bool ok = true;
+    switch (I.op) {
+      case OP_CONST: case OP_H: break;
+      case OP_U: case OP_V: ok = I.a >= 0 && I.a < nquant; break;
+      case OP_COEF: ok = I.a >= 0 && I.a < prog.ncoef; break;
+      case OP_X: ok = I.a >= 0 && I.a < dim; break;
+      case OP_ADD: case OP_SUB: case OP_MUL: case OP_DIV: case OP_POW:
+        ok = I.a >= 0 && I.a < k && I.b >= 0 && I.b < k; break;
+      case OP_NEG: case OP_SQRT: case OP_EXP: case OP_LOG: case OP_SIN: case OP_COS:
+      case OP_TAN: case OP_TANH: case OP_ARCTAN: case OP_ABS:
+        ok = I.a >= 0 && I.a < k; break;
+      default: ok = false;
+    }
+    if (!ok) {
+      set_error(FEM_ERR_ARGUMENT, "form program instruction %d (op %d, a %d, b %d) is invalid", k,
+                I.op, I.a, I.b);
+      return FEM_ERR_ARGUMENT;
+    }
+  }
+  return 0;
+}
+
+int faithful_mask(const FemMesh& m, const FemBasis& b, const FemProgram& prog, int nq, double* local,
+                  int32_t* status, cudaStream_t st) {
+  int rc = check_program(prog, m.dim, b.vector != 0, false);
+  if (rc) return rc;
   if (m.nelems == 0) return 0;
   const unsigned grid = (unsigned)ceil_div(m.nelems, 64);
   if (m.dim == 2)
@@ -97,4 +296,111 @@ int faithful_mask(const FemMesh& m, const FemBasis& b, const FemProgram& prog, i
   FEM_LAUNCH_CHECK("faithful mask kernel");
   return 0;
 }
+
+// mode 0: local matrices, 1: local vectors, 2: per-cell functional values
+int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemProgram& prog,
+                 double* out, int32_t* status, cudaStream_t st) {
+  int rc = check_program(prog, m.dim, b.vector != 0, true);
+  if (rc) return rc;
+  if (m.nelems == 0) return 0;
+  const int nb = b.nbfun;
+  const int L = mode == 0 ? nb * nb : (mode == 1 ? nb : 1);
+  const int nq = prog.nq;
+  auto bytes = [&](int epb) { return (size_t)epb * nq * (14 + L) * sizeof(double); };
+  int epb = std::max(1, std::min(64, 2048 / (L * nq)));
+  while (epb > 1 && bytes(epb) > 96 * 1024) --epb;
+  const size_t smem = bytes(epb);
+  if (smem > 200 * 1024) {
+    set_error(FEM_ERR_CAPACITY, "%d local entries x %d points do not fit one block", L, nq);
+    return FEM_ERR_CAPACITY;
+  }
+  fem_faithful::GenericShape s{epb, L, nq};
+  const fem_faithful::Rule rule{prog.qX, prog.qW, nq};
+  const unsigned grid = (unsigned)ceil_div(m.nelems, epb);
+  const int threads = 256;
+  auto go = [&](auto kern) -> int {
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem);
+      if (e != cudaSuccess) return check_cuda(e, "program kernel smem");
+    }
+    kern<<<grid, threads, smem, st>>>(m, b, prog, rule, s, out, status);
+    return 0;
+  };
+  using namespace fem_faithful;
+  if (m.dim == 2)
+    rc = mode == 0 ? go(program_kernel<2, 0>) : mode == 1 ? go(program_kernel<2, 1>)
+                                                          : go(program_kernel<2, 2>);
+  else
+    rc = mode == 0 ? go(program_kernel<3, 0>) : mode == 1 ? go(program_kernel<3, 1>)
+                                                          : go(program_kernel<3, 2>);
+  if (rc) return rc;
+  FEM_LAUNCH_CHECK("program kernel");
+  return 0;
+}
+
+int interpolate(const FemMesh& m, const FemBasis& b, int nq, const double* X, const double* w,
+                double* out, cudaStream_t st) {
+  if (nq <= 0 || nq > fem_faithful::kMaxPoints || !X || !w || !out) {
+    set_error(FEM_ERR_ARGUMENT, "interpolate: %d points, X/w/out must be device arrays", nq);
+    return FEM_ERR_ARGUMENT;
+  }
+  const int64_t n = m.nelems * (int64_t)nq;
+  if (n == 0) return 0;
+  const fem_faithful::Rule rule{X, nullptr, nq};
+  const unsigned grid = (unsigned)ceil_div(n, 128);
+  if (m.dim == 2)
+    fem_faithful::interpolate_kernel<2><<<grid, 128, 0, st>>>(m, b, rule, w, out);
+  else
+    fem_faithful::interpolate_kernel<3><<<grid, 128, 0, st>>>(m, b, rule, w, out);
+  FEM_LAUNCH_CHECK("interpolate kernel");
+  return 0;
+}
+
+int sum_pairwise(const double* x, int64_t n, double* out, cudaStream_t st) {
+  // leaves of numpy's split recursion, in order
+  std::vector<int64_t> off;
+  std::vector<int32_t> len;
+  struct Seg { int64_t o, n; };
+  std::vector<Seg> stack{{0, n}};
+  while (!stack.empty()) {
+    Seg s = stack.back();
+    stack.pop_back();
+    if (s.n <= 128) {
+      if (n > 0) {
+        off.push_back(s.o);
+        len.push_back((int32_t)s.n);
+      }
+      continue;
+    }
+    int64_t n2 = s.n / 2;
+    n2 -= n2 % 8;
+    stack.push_back({s.o + n2, s.n - n2});  // right after left
+    stack.push_back({s.o, n2});
+  }
+  const int64_t nl = (int64_t)off.size();
+  int64_t* d_off = nullptr;
+  int32_t* d_len = nullptr;
+  double* d_sum = nullptr;
+  const size_t bytes = std::max<int64_t>(1, nl) * (sizeof(int64_t) + sizeof(int32_t) + sizeof(double));
+  char* blob = nullptr;
+  FEM_TRY_CUDA(cudaMallocAsync(&blob, bytes, st));
+  d_off = reinterpret_cast<int64_t*>(blob);
+  d_sum = reinterpret_cast<double*>(blob + std::max<int64_t>(1, nl) * sizeof(int64_t));
+  d_len = reinterpret_cast<int32_t*>(blob + std::max<int64_t>(1, nl) * 2 * sizeof(int64_t));
+  if (nl > 0) {
+    FEM_TRY_CUDA(cudaMemcpyAsync(d_off, off.data(), nl * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    FEM_TRY_CUDA(cudaMemcpyAsync(d_len, len.data(), nl * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    fem_faithful::pairwise_leaves_kernel<<<(unsigned)ceil_div(nl, 128), 128, 0, st>>>(
+        x, n, d_off, d_len, nl, d_sum);
+    FEM_LAUNCH_CHECK("pairwise leaves kernel");
+  }
+  fem_faithful::pairwise_tree_kernel<<<1, 32, 0, st>>>(d_sum, n, out);
+  FEM_LAUNCH_CHECK("pairwise tree kernel");
+  // the host vectors must outlive the asynchronous copies
+  FEM_TRY_CUDA(cudaStreamSynchronize(st));
+  cudaFreeAsync(blob, st);
+  return 0;
+}
+
 }  // namespace fem

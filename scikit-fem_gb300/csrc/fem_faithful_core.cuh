@@ -18,10 +18,18 @@
 namespace fem_faithful {
 
 constexpr int kMaxProgram = 512;
+constexpr int kMaxCoef = 16;
+constexpr int kMaxPoints = 128;
 
 using Instr = FemInstr;
 
-enum { OP_CONST = 0, OP_U, OP_V, OP_COEF, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG };
+// Program operations.  CONST..NEG, X, H, SQRT and ABS are correctly rounded
+// (bitwise the reference's); EXP..ARCTAN and POW call the CUDA / C math
+// library, whose last bits may differ from numpy's.
+enum {
+  OP_CONST = 0, OP_U, OP_V, OP_COEF, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_X, OP_H,
+  OP_SQRT, OP_EXP, OP_LOG, OP_SIN, OP_COS, OP_TAN, OP_TANH, OP_ARCTAN, OP_ABS, OP_POW
+};
 
 // ----------------------------------------------------------- reference bases
 FEM_HD void lbasis(int family, int i, double x, double y, double z, double& phi,
@@ -150,8 +158,9 @@ FEM_HD double np_pairwise_sum(const double* a, int n) {
 
 // ---------------------------------------------------------------- mappings
 template <int D>
-FEM_HD void affine_inverse(const FemMesh& m, int64_t e, double inv[3][3], double& det) {
-  double A[3][3];
+FEM_HD void affine_inverse(const FemMesh& m, int64_t e, double inv[3][3], double& det,
+                           double A[3][3], double x0[3]) {
+  for (int i = 0; i < D; ++i) x0[i] = m.p[i * m.nverts + m.t[e]];
   for (int i = 0; i < D; ++i)
     for (int j = 0; j < D; ++j)
       A[i][j] = m.p[i * m.nverts + m.t[(j + 1) * m.nelems + e]] - m.p[i * m.nverts + m.t[e]];
@@ -225,7 +234,7 @@ FEM_HD void quantities(int family, bool vec, int fn, double x, double y, double 
 }
 
 FEM_HD double run(const Instr* ins, int n, int out, const double* qu, const double* qv,
-                      const double* coef, double* R) {
+                      const double* coef, const double* qx, double* R) {
   for (int k = 0; k < n; ++k) {
     const Instr I = ins[k];
     double r = 0.0;
@@ -239,6 +248,18 @@ FEM_HD double run(const Instr* ins, int n, int out, const double* qu, const doub
       case OP_MUL: r = R[I.a] * R[I.b]; break;
       case OP_DIV: r = R[I.a] / R[I.b]; break;
       case OP_NEG: r = -R[I.a]; break;
+      case OP_X: r = qx[I.a]; break;
+      case OP_H: r = qx[3]; break;
+      case OP_SQRT: r = sqrt(R[I.a]); break;
+      case OP_EXP: r = exp(R[I.a]); break;
+      case OP_LOG: r = log(R[I.a]); break;
+      case OP_SIN: r = sin(R[I.a]); break;
+      case OP_COS: r = cos(R[I.a]); break;
+      case OP_TAN: r = tan(R[I.a]); break;
+      case OP_TANH: r = tanh(R[I.a]); break;
+      case OP_ARCTAN: r = atan(R[I.a]); break;
+      case OP_ABS: r = fabs(R[I.a]); break;
+      case OP_POW: r = pow(R[I.a], R[I.b]); break;
       default: break;
     }
     R[k] = r;
@@ -246,27 +267,156 @@ FEM_HD double run(const Instr* ins, int n, int out, const double* qu, const doub
   return R[out];
 }
 
-// The replayed value of local entry (row i, column j) of element e.
+// Global coordinates of a reference point: MappingAffine.F
+// (mapping_affine.py:183-193: sum_j A[i][j] X_j in j order, then + b_i) or
+// MappingIsoparametric.Fmap (mapping_isoparametric.py:50-58: sum over nodes
+// of p_i(node) phi_node(X) from 0).
+template <int D>
+FEM_HD void global_coords(const FemMesh& m, int64_t e, bool hex, const double A[3][3],
+                          const double x0[3], double x, double y, double z, double* qx) {
+  const double X[3] = {x, y, z};
+  if (!hex) {
+    for (int i = 0; i < D; ++i) {
+      double s = 0.0;
+      for (int j = 0; j < D; ++j) s = s + A[i][j] * X[j];
+      qx[i] = s + x0[i];
+    }
+    return;
+  }
+  for (int i = 0; i < 3; ++i) qx[i] = 0.0;
+  for (int itr = 0; itr < 8; ++itr) {
+    double phi, d[3];
+    lbasis(FEM_HEX_1, itr, x, y, z, phi, d);
+    const int64_t v = m.t[itr * m.nelems + e];
+    for (int i = 0; i < 3; ++i) qx[i] = qx[i] + m.p[i * m.nverts + v] * phi;
+  }
+}
+
+// What a program reads besides the basis functions.
+struct ProgFlags {
+  bool x = false, h = false;
+};
+FEM_HD ProgFlags prog_flags(const FemProgram& p) {
+  ProgFlags f;
+  for (int k = 0; k < p.ninstr; ++k) {
+    f.x = f.x || p.ins[k].op == OP_X;
+    f.h = f.h || p.ins[k].op == OP_H;
+  }
+  return f;
+}
+
+// Geometry of one quadrature point: invDF, detDF, global coordinates
+// (qx[0..2]) and the mesh parameter h = |detDF|**(1/dim) (qx[3],
+// cell_basis.py:136-141; numpy evaluates **0.5 as sqrt).
+struct PointGeo {
+  double inv[3][3];
+  double det;
+  double qx[4];
+};
+
+struct CellGeo {  // the affine map of a simplex (unused for Hex1)
+  double inv[3][3], det, A[3][3], x0[3];
+};
+
+template <int D>
+FEM_HD void cell_geometry(const FemMesh& m, int64_t e, bool hex, CellGeo& c) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) c.inv[i][j] = c.A[i][j] = 0.0;
+  c.x0[0] = c.x0[1] = c.x0[2] = 0.0;
+  c.det = 0.0;
+  if (!hex) affine_inverse<D>(m, e, c.inv, c.det, c.A, c.x0);
+}
+
+template <int D>
+FEM_HD void point_geometry(const FemMesh& m, int64_t e, bool hex, const CellGeo& c,
+                           ProgFlags f, double x, double y, double z, PointGeo& g) {
+  if (hex) {
+    hex_inverse(m, e, x, y, z, g.inv, g.det);
+  } else {
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) g.inv[i][j] = c.inv[i][j];
+    g.det = c.det;
+  }
+  g.qx[0] = g.qx[1] = g.qx[2] = g.qx[3] = 0.0;
+  if (f.x) global_coords<D>(m, e, hex, c.A, c.x0, x, y, z, g.qx);
+  if (f.h) g.qx[3] = D == 2 ? sqrt(fabs(g.det)) : pow(fabs(g.det), 1.0 / 3.0);
+}
+
+// form(u_j, v_i, w) * dx at quadrature point q (bilinear_form.py:150-151,
+// linear_form.py:48-49, functional.py:19-24): dx = |detDF| * W[q]
+// (cell_basis.py:104-105).  Coefficient slot c holds one value per element
+// (stride 0) or per quadrature point (stride nq).
+template <int D>
+FEM_HD double point_value(const FemBasis& b, const FemProgram& prog, int64_t e, int q, int i,
+                          int j, double x, double y, double z, const PointGeo& g, double wq,
+                          double* R) {
+  const bool vec = b.vector != 0;
+  double qu[D + D * D], qv[D + D * D], cq[kMaxCoef];
+  quantities<D>(b.family, vec, j, x, y, z, g.inv, qu);
+  quantities<D>(b.family, vec, i, x, y, z, g.inv, qv);
+  for (int c = 0; c < prog.ncoef && c < kMaxCoef; ++c)
+    cq[c] = prog.coef[c] ? prog.coef[c][prog.coef_stride[c] ? e * prog.coef_stride[c] + q : e]
+                         : 0.0;
+  const double f = run(prog.ins, prog.ninstr, prog.out, qu, qv, cq, g.qx, R);
+  return f * (fabs(g.det) * wq);
+}
+
+// The replayed value of local entry (row i, column j) of element e: the
+// reference's value bit for bit (for the correctly rounded operations).
 template <int D>
 FEM_HD double replay_entry(const FemMesh& m, const FemBasis& b, const FemProgram& prog,
-                           const Rule& rule, int64_t e, int i, int j, const double* coef,
-                           double* R, double* vals) {
+                           const Rule& rule, int64_t e, int i, int j, double* R,
+                           double* scratch) {
+  double own[kMaxPoints];
+  double* vals = scratch ? scratch : own;
   const bool hex = b.family == FEM_HEX_1;
-  const bool vec = b.vector != 0;
-  double inv[3][3], det = 0.0;
-  if (!hex) affine_inverse<D>(m, e, inv, det);
-  double qu[D + D * D], qv[D + D * D];
+  const ProgFlags f = prog_flags(prog);
+  CellGeo c;
+  cell_geometry<D>(m, e, hex, c);
   for (int q = 0; q < rule.nq; ++q) {
     const double x = rule.X[q];
     const double y = rule.X[rule.nq + q];
     const double z = D == 3 ? rule.X[2 * rule.nq + q] : 0.0;
-    if (hex) hex_inverse(m, e, x, y, z, inv, det);
-    quantities<D>(b.family, vec, j, x, y, z, inv, qu);
-    quantities<D>(b.family, vec, i, x, y, z, inv, qv);
-    const double f = run(prog.ins, prog.ninstr, prog.out, qu, qv, coef, R);
-    vals[q] = f * (fabs(det) * rule.W[q]);
+    PointGeo g;
+    point_geometry<D>(m, e, hex, c, f, x, y, z, g);
+    vals[q] = point_value<D>(b, prog, e, q, i, j, x, y, z, g, rule.W[q], R);
   }
   return np_pairwise_sum(vals, rule.nq);
+}
+
+// numpy's pairwise summation of a contiguous array of any length
+// (PW_BLOCKSIZE 128 leaves, split at n/2 rounded down to a multiple of 8).
+FEM_HD double np_pairwise_sum_any(const double* a, int64_t n) {
+  // explicit stack instead of recursion: depth <= 64
+  struct Frame { int64_t off, n; int state; double left; };
+  Frame st[64];
+  int sp = 0;
+  st[0] = {0, n, 0, 0.0};
+  double ret = 0.0;
+  while (sp >= 0) {
+    Frame& f = st[sp];
+    if (f.n <= 128) {
+      ret = np_pairwise_sum(a + f.off, (int)f.n);
+      --sp;
+      continue;
+    }
+    int64_t n2 = f.n / 2;
+    n2 -= n2 % 8;
+    if (f.state == 0) {
+      f.state = 1;
+      st[sp + 1] = {f.off, n2, 0, 0.0};
+      ++sp;
+    } else if (f.state == 1) {
+      f.left = ret;
+      f.state = 2;
+      st[sp + 1] = {f.off + n2, f.n - n2, 0, 0.0};
+      ++sp;
+    } else {
+      ret = f.left + ret;
+      --sp;
+    }
+  }
+  return ret;
 }
 
 }  // namespace fem_faithful

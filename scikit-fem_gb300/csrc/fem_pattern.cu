@@ -285,6 +285,32 @@ __global__ void vector_sum_kernel(const int32_t* __restrict__ inc_ptr, const int
   b[r] = s;
 }
 
+// Zero-structure check of a pattern against new local matrices (exact
+// masks): a nonzero entry without a CSR slot, or a CSR entry with no
+// nonzero contribution, means the pattern is stale.  One thread per row;
+// seen[] is the row's own range of a nnz-byte scratch.
+__global__ void zero_check_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                                  const uint16_t* __restrict__ slot, const int32_t* __restrict__ indptr,
+                                  const double* __restrict__ local, int64_t nrows, int nu,
+                                  uint8_t* __restrict__ seen, int32_t* __restrict__ status) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int32_t p0 = indptr[r], p1 = indptr[r + 1];
+  for (int32_t k = p0; k < p1; ++k) seen[k] = 0;
+  bool stale = false;
+  for (int32_t q = inc_ptr[r]; q < inc_ptr[r + 1]; ++q) {
+    const int64_t code = inc[q];
+    for (int j = 0; j < nu; ++j) {
+      const double v = local[code * nu + j];
+      const uint16_t s = slot[(int64_t)q * nu + j];
+      if (s == 0xFFFF) stale = stale || v != 0.0;
+      else if (v != 0.0) seen[p0 + s] = 1;
+    }
+  }
+  for (int32_t k = p0; k < p1; ++k) stale = stale || !seen[k];
+  if (stale) atomicOr(status, 1 << FEM_ERR_STALE_PATTERN);
+}
+
 __global__ void max_reduce_kernel(const int32_t* __restrict__ x, int64_t n, int32_t* out) {
   int32_t m = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -536,6 +562,18 @@ int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st
   }
   if (rc) return rc;
   FEM_LAUNCH_CHECK("csr_sum_kernel");
+  return 0;
+}
+
+int zero_check(const Pattern& P, const double* local, int32_t* status, cudaStream_t st) {
+  if (!P.has_matrix || P.nrows == 0) return 0;
+  uint8_t* seen = nullptr;
+  FEM_TRY_CUDA(cudaMallocAsync(&seen, std::max<int64_t>(1, P.nnz), st));
+  zero_check_kernel<<<(unsigned)ceil_div(P.nrows, 128), 128, 0, st>>>(
+      P.inc_ptr, P.inc, P.slot, P.indptr, local, P.nrows, P.nbfun_u, seen, status);
+  cudaError_t e = cudaGetLastError();
+  cudaFreeAsync(seen, st);
+  if (e != cudaSuccess) return check_cuda(e, "zero_check_kernel");
   return 0;
 }
 

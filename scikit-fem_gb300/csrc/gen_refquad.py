@@ -44,12 +44,17 @@ def main():
     open(path, "w").write("\n".join(out))
     # the same rules for the Python side (Basis.X / Basis.W)
     py = ['"""Generated by csrc/gen_refquad.py from reference-recorded fixtures (do not',
-          'edit): scikit-fem\'s triangle / tetrahedron quadrature rules of orders 1-4,',
-          'bit-exact, as hexadecimal floats."""', "", "RULES = {"]
+          'edit): scikit-fem\'s triangle / tetrahedron quadrature rules of orders 1-4',
+          'and its default hexahedral rule, bit-exact, as hexadecimal floats."""', "",
+          "RULES = {"]
     for key in sorted(k[:-2] for k in q if k.endswith("_X")):
         X, W = q[key + "_X"], q[key + "_W"]
         py.append("    %r: (%r,\n           %r)," % (
             key, [[float(v).hex() for v in row] for row in X], [float(v).hex() for v in W]))
+    # the default Hex1 rule (intorder 6-7, 4x4x4 leggauss points)
+    Xh, Wh = hexg["X"], hexg["W"]
+    py.append("    %r: (%r,\n           %r)," % (
+        "hex6", [[float(v).hex() for v in row] for row in Xh], [float(v).hex() for v in Wh]))
     py.append("}")
     pkg = os.path.join(os.path.dirname(HERE), "skfem_gb300", "_refquad.py")
     open(pkg, "w").write("\n".join(py) + "\n")

@@ -11,7 +11,8 @@ from .element import (Element, ElementH1, ElementTriP1, ElementTriP2, ElementTet
 from .quadrature import get_quadrature  # noqa: F401
 from .dofs import Dofs  # noqa: F401
 from .basis import Basis, CellBasis  # noqa: F401
-from .form import Form, BilinearForm, LinearForm, asm, ElementField  # noqa: F401
+from .form import Form, BilinearForm, LinearForm, Functional, asm, ElementField  # noqa: F401
+from .field import DiscreteField  # noqa: F401
 from . import helpers, models  # noqa: F401
 
 __version__ = "0.1.0"

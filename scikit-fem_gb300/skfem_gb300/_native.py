@@ -55,7 +55,9 @@ class FemInstr(ctypes.Structure):
 
 class FemProgram(ctypes.Structure):
     _fields_ = [("ninstr", ctypes.c_int32), ("out", ctypes.c_int32), ("ncoef", ctypes.c_int32),
-                ("nq", ctypes.c_int32), ("ins", ctypes.c_void_p), ("coef", ctypes.c_void_p * 8)]
+                ("nq", ctypes.c_int32), ("ins", ctypes.c_void_p), ("coef", ctypes.c_void_p * 16),
+                ("coef_stride", ctypes.c_int32 * 16), ("qX", ctypes.c_void_p),
+                ("qW", ctypes.c_void_p)]
 
 
 class FemError(RuntimeError):
@@ -92,6 +94,13 @@ _SIGS = {
                                             _I64P, _P]),
     "fem_condense_values": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _P, _P, _P, _P, _P, _P,
                                            _P, _P]),
+    "fem_program_local_matrices": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
+    "fem_program_local_vectors": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
+    "fem_program_elemental": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
+    "fem_pattern_build_local": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(ctypes.c_void_p), _P]),
+    "fem_csr_sum_checked": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "fem_interpolate": (ctypes.c_int, [_P, _P, ctypes.c_int32, _P, _P, _P, _P]),
+    "fem_sum_pairwise": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P]),
     "fem_set_tuning": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "fem_assemble_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
 }

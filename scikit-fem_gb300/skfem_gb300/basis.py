@@ -13,10 +13,13 @@ import torch
 
 from . import _native as N
 from .dofs import Dofs
+from .field import DiscreteField
 from .mesh import as_mesh
 from .quadrature import get_quadrature
 
 __all__ = ["CellBasis", "Basis"]
+
+MAX_POINTS = 128    # quadrature points per cell of the generic kernels
 
 
 class CellBasis:
@@ -44,17 +47,26 @@ class CellBasis:
             self.nelems = len(self.tind)
         self.intorder = intorder if intorder is not None else 2 * elem.maxdeg
         if quadrature is not None:
-            raise NotImplementedError("custom quadrature rules are not supported by the kernels")
-        self.X, self.W = get_quadrature(elem.refdom, self.intorder)
-        if elem.refdom == "hex" and self.X.shape[1] != 64:
-            # the isoparametric kernel integrates with the default 4x4x4 rule
-            raise NotImplementedError("ElementHex1 is assembled with the default 4x4x4 rule "
-                                      "(intorder 6 or 7)")
-        min_order = {1: 2, 2: 4}.get(elem.maxdeg, 0) if elem.refdom != "hex" else 0
-        if self.intorder < min_order:
-            raise NotImplementedError(
-                "intorder %d integrates the mass term of %s inexactly; the kernels integrate "
-                "exactly (intorder >= %d)" % (self.intorder, type(elem).__name__, min_order))
+            X, W = quadrature
+            self.X = np.ascontiguousarray(X, dtype=np.float64)
+            self.W = np.ascontiguousarray(W, dtype=np.float64)
+            if self.X.ndim != 2 or self.X.shape[0] != mesh.p.shape[0] or \
+                    self.W.shape != (self.X.shape[1],):
+                raise ValueError("quadrature must be (X (dim, nqp), W (nqp,))")
+        else:
+            self.X, self.W = get_quadrature(elem.refdom, self.intorder)
+        if self.X.shape[1] > MAX_POINTS:
+            raise NotImplementedError("%d quadrature points per cell (limit %d)"
+                                      % (self.X.shape[1], MAX_POINTS))
+        # The coefficient-channel kernels integrate exactly (simplices) or
+        # with the default 4x4x4 rule (Hex1); a basis whose rule gives other
+        # numbers -- too low an order, a custom rule, another Hex1 rule --
+        # assembles every form through the generic per-point kernels.
+        if elem.refdom == "hex":
+            self._fast_ok = quadrature is None and self.X.shape[1] == 64
+        else:
+            min_order = {1: 2, 2: 4}.get(elem.maxdeg, 0)
+            self._fast_ok = quadrature is None and self.intorder >= min_order
         self.device = N.require_cuda(device)
         self._patterns = {}
         self._upload()
@@ -75,6 +87,8 @@ class CellBasis:
                                 self.nelems, self.p_dev.data_ptr(), self.t_dev.data_ptr())
         self.c_basis = N.FemBasis(N.FAMILY[self.elem.family], int(self.elem.vector),
                                   self.Nbfun, 0, self.N, self.ed_dev.data_ptr())
+        self.X_dev = torch.from_numpy(np.ascontiguousarray(self.X, dtype=np.float64)).to(dev)
+        self.W_dev = torch.from_numpy(np.ascontiguousarray(self.W, dtype=np.float64)).to(dev)
 
     def update_coordinates(self, p):
         """Replace the node coordinates (same topology) -- used by shape
@@ -106,6 +120,41 @@ class CellBasis:
 
     def quadrature(self):
         return self.X, self.W
+
+    def interpolate_torch(self, w):
+        """Device interpolation of the DOF vector w: (nquant, nelems, nqp)
+        float64, quantity-major -- scalar bases value then the dim
+        derivatives; vector bases the components then grad[c][k] at
+        dim + c*dim + k (abstract_basis.py:271-322 arithmetic)."""
+        w = torch.as_tensor(w, dtype=torch.float64).to(self.device).contiguous()
+        if w.dim() != 1 or w.shape[0] != self.N:
+            raise ValueError("Input array has wrong size.")       # abstract_basis.py:284-285
+        dim = self.mesh.p.shape[0]
+        nquant = dim + dim * dim if self.elem.vector else 1 + dim
+        nq = self.X.shape[1]
+        out = torch.empty((nquant, self.nelems, nq), dtype=torch.float64, device=self.device)
+        N.check(N.lib().fem_interpolate(N.byref(self.c_mesh), N.byref(self.c_basis), nq,
+                                        N.ptr(self.X_dev), N.ptr(w), N.ptr(out),
+                                        N.stream_ptr()))
+        return out
+
+    def interpolate(self, w):
+        """Basis.interpolate (abstract_basis.py:271-322): a DiscreteField of
+        the values at the quadrature points, with ``grad``; computed on the
+        device (and kept there for forms that receive it)."""
+        if isinstance(w, np.ndarray) and (w.ndim != 1 or w.shape[0] != self.N):
+            raise ValueError("Input array has wrong size.")
+        dev = self.interpolate_torch(w)
+        host = dev.cpu().numpy()
+        dim = self.mesh.p.shape[0]
+        if self.elem.vector:
+            value = host[:dim]
+            grad = host[dim:].reshape((dim, dim) + host.shape[1:])
+        else:
+            value, grad = host[0], host[1:]
+        f = DiscreteField(value, grad)
+        f._dev = (dev, self)
+        return f
 
     def default_parameters(self):
         return {}

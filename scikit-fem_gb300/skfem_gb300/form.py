@@ -4,14 +4,19 @@
   Form._normalize_asm_kwargs      form.py:91-121 (coefficient formats)
   BilinearForm.assemble           bilinear_form.py:130-148 -> scipy CSR
   LinearForm.assemble             form.py:73-80 + linear_form.py:18-46 -> ndarray
+  Functional.elemental/assemble   functional.py:19-61 -> ndarray / float64
   asm                             skfem/assembly/__init__.py:69-97
 
 ``assemble`` returns what the reference returns (scipy.sparse.csr_matrix /
 numpy array, canonical CSR with the reference's pattern); ``assemble_torch``
 returns the device-resident result (torch sparse CSR / tensor) without a
-host round trip.  The form callable is traced once (tracer.py) and mapped to
-the CUDA kernels' coefficient channels; per-element coefficient fields stay
-on the device.
+host round trip.  The form callable is traced once (tracer.py).  Forms of
+the isotropic coefficient families run on the channel kernels (exact
+reference tensors, FP64); every other form -- anisotropic or advection
+terms, coefficients varying inside cells, interpolated DOF vectors, w.x and
+w.h, numpy functions -- runs on the generic kernels, which evaluate the
+traced program per quadrature point with the reference's own operation
+order.  Coefficients stay on the device.
 """
 
 import ctypes
@@ -22,10 +27,11 @@ import scipy.sparse as sp
 import torch
 
 from . import _native as N
-from .tracer import (bilinear_channels, linear_channels, trace_bilinear, trace_linear,
+from .field import DiscreteField
+from .tracer import (FieldSpec, bilinear_channels, linear_channels, trace_bilinear, trace_linear,
                      trace_tape)
 
-__all__ = ["Form", "BilinearForm", "LinearForm", "asm", "ElementField"]
+__all__ = ["Form", "BilinearForm", "LinearForm", "Functional", "asm", "ElementField"]
 
 
 class ElementField:
@@ -38,15 +44,25 @@ class ElementField:
 
 
 class _Coefficients:
-    """Form arguments normalised to device tensors (one value per element)."""
+    """Form arguments normalised to device tensors (form.py:91-121):
+
+      fields   name -> (nelems,)        one value per cell
+      qfields  name -> (nelems, nqp)    values varying inside cells
+      dfields  name -> (tensor (nquant, nelems, nqp), FieldSpec)
+               DiscreteFields: interpolated DOF vectors (1-D arrays of
+               length N, abstract_basis.py:271-322) or given fields
+    """
 
     def __init__(self, basis, kwargs):
         self.fields = {}
+        self.qfields = {}
+        self.dfields = {}
         self.numbers = {}
         self.keep = []
         dev = basis.device
         ne = basis.nelems
         nqp = basis.X.shape[-1]
+        dim = basis.mesh.p.shape[0]
         for k, v in kwargs.items():
             if isinstance(v, numbers.Number) or isinstance(v, tuple):
                 self.numbers[k] = v
@@ -58,15 +74,22 @@ class _Coefficients:
                                      % (k, t.numel(), ne))
                 self.fields[k] = t.contiguous()
                 continue
+            if isinstance(v, DiscreteField) or hasattr(v, "grad") and isinstance(v, np.ndarray):
+                self._discrete_field(k, v, basis, dim, ne, nqp)
+                continue
             if isinstance(v, torch.Tensor):
                 t = v.to(device=dev, dtype=torch.float64)
+                if t.dim() == 1 and t.shape[0] != ne:
+                    if t.shape[0] != basis.N:
+                        raise ValueError("Input array has wrong size.")
+                    self._dof_vector(k, t, basis, dim)
+                    continue
             elif isinstance(v, np.ndarray):
                 if v.ndim == 1:
                     if v.shape[0] != basis.N:
                         raise ValueError("Input array has wrong size.")  # abstract_basis.py:284-285
-                    raise NotImplementedError(
-                        "DOF-vector coefficients ('%s', interpolated by the reference) are not "
-                        "supported yet; pass per-element values (nelems, nqp) or ElementField" % k)
+                    self._dof_vector(k, v, basis, dim)
+                    continue
                 t = torch.from_numpy(np.ascontiguousarray(v, dtype=np.float64)).to(dev)
             elif isinstance(v, list):
                 raise NotImplementedError("list-valued coefficients are not supported")
@@ -83,10 +106,56 @@ class _Coefficients:
                                  "integration points as the basis object.".format(k))
             col = t[:, 0].contiguous()
             if nqp > 1 and not bool(torch.equal(t[:, 1:], col[:, None].expand(-1, nqp - 1))):
-                raise NotImplementedError(
-                    "coefficient '%s' varies inside cells; the kernels take per-element "
-                    "coefficients (constant over each cell's quadrature points)" % k)
-            self.fields[k] = col
+                self.qfields[k] = t.contiguous()      # varies inside cells: generic kernels
+            else:
+                self.fields[k] = col
+
+    def _dof_vector(self, name, w, basis, dim):
+        t = basis.interpolate_torch(w)
+        self.dfields[name] = (t, FieldSpec("field", dim if basis.elem.vector else 0, True))
+
+    def _discrete_field(self, name, v, basis, dim, ne, nqp):
+        dev = getattr(v, "_dev", None)
+        if dev is not None and dev[1] is basis:
+            self.dfields[name] = (dev[0], FieldSpec("field", dim if basis.elem.vector else 0,
+                                                    True))
+            return
+        value = np.asarray(v, dtype=np.float64)
+        if value.shape[-2:] != (ne, nqp):
+            raise ValueError("Quadrature mismatch: '{}' should have same number of "
+                             "integration points as the basis object.".format(name))
+        if value.ndim == 2:
+            ncomp, parts = 0, [value[None]]
+        elif value.ndim == 3:
+            ncomp, parts = value.shape[0], [value]
+        else:
+            raise NotImplementedError("fields of rank > 1 are not supported")
+        grad = getattr(v, "grad", None)
+        if grad is not None:
+            grad = np.asarray(grad, dtype=np.float64)
+            parts.append(grad.reshape((-1, ne, nqp)))
+        t = torch.from_numpy(np.ascontiguousarray(np.concatenate(parts, axis=0))).to(basis.device)
+        self.dfields[name] = (t, FieldSpec("field", ncomp, grad is not None))
+
+    @property
+    def generic(self):
+        """Arguments only the generic per-point kernels take."""
+        return bool(self.qfields or self.dfields)
+
+    def specs(self):
+        s = {k: FieldSpec("elem") for k in self.fields}
+        s.update({k: FieldSpec("qp") for k in self.qfields})
+        s.update({k: spec for k, (_, spec) in self.dfields.items()})
+        return s
+
+    def slot(self, key, ne, nq):
+        """Device pointer and stride of a program coefficient slot."""
+        if isinstance(key, tuple):
+            t, _ = self.dfields[key[0]]
+            return t.data_ptr() + key[1] * ne * nq * 8, nq
+        if key in self.qfields:
+            return self.qfields[key].data_ptr(), nq
+        return self.fields[key].data_ptr(), 0
 
     def coef(self, poly, ne, device):
         """Poly -> FemCoef (scale, field pointer)."""
@@ -140,20 +209,80 @@ class Form:
         return getattr(self.form, "__name__", "form")
 
     # tracing is cached per (element kind, field names, numbers)
+    def _key(self, basis, coeffs, kind):
+        return (kind, basis.elem.family, basis.elem.vector, basis.mesh.p.shape[0],
+                tuple(sorted((k, s.kind, s.ncomp, s.grad) for k, s in coeffs.specs().items())),
+                tuple(sorted(coeffs.numbers.items(), key=repr)))
+
     def _trace(self, basis, coeffs, kind):
-        key = (basis.elem.family, basis.elem.vector, basis.mesh.p.shape[0],
-               tuple(sorted(coeffs.fields)), tuple(sorted(coeffs.numbers.items(), key=repr)))
-        ch = self._traces.get(key)
-        if ch is None:
-            dim = basis.mesh.p.shape[0]
+        """The form's coefficient channels, or None when only the generic
+        per-point kernels can assemble it (a form outside the isotropic
+        channel families, arguments varying inside cells, w.x / w.h, numpy
+        functions, or a basis whose quadrature rule the channel kernels do
+        not integrate with)."""
+        if coeffs.generic or not basis._fast_ok:
+            return None
+        key = ("channels",) + self._key(basis, coeffs, kind)
+        if key in self._traces:
+            return self._traces[key]
+        dim = basis.mesh.p.shape[0]
+        try:
             if kind == "bilinear":
                 sym = trace_bilinear(self.form, basis.elem, dim, coeffs.fields, coeffs.numbers)
                 ch = bilinear_channels(sym, basis.elem, dim)
             else:
                 sym = trace_linear(self.form, basis.elem, dim, coeffs.fields, coeffs.numbers)
                 ch = linear_channels(sym, basis.elem, dim)
-            self._traces[key] = ch
+        except (NotImplementedError, TypeError):
+            ch = None
+        self._traces[key] = ch
         return ch
+
+    def _generic(self, basis, coeffs, kind):
+        """The form's program for the generic kernels (cached per argument
+        structure) and its cache key."""
+        key = ("program",) + self._key(basis, coeffs, kind)
+        g = self._traces.get(key)
+        if g is None:
+            ins, out, names = trace_tape(self.form, basis.elem, basis.mesh.p.shape[0],
+                                         coeffs.specs(), coeffs.numbers, kind=kind,
+                                         defaults=True)
+            g = _GenericProgram(ins, out, names)
+            self._traces[key] = g
+        return g, key
+
+
+class _GenericProgram:
+    """A traced form program and its per-device instruction arrays."""
+
+    def __init__(self, ins, out, names):
+        if len(ins) > MAX_PROGRAM:
+            raise NotImplementedError("the form traces to %d operations per point (limit %d)"
+                                      % (len(ins), MAX_PROGRAM))
+        if len(names) > MAX_COEF:
+            raise NotImplementedError("the form reads %d coefficient quantities (limit %d)"
+                                      % (len(names), MAX_COEF))
+        self.ins, self.out, self.names = ins, out, names
+        self._dev = {}
+
+    def struct(self, basis, coeffs):
+        dev = self._dev.get(basis.device)
+        if dev is None:
+            arr = (N.FemInstr * len(self.ins))(*[N.FemInstr(op, a, b, 0, imm)
+                                                  for op, a, b, imm in self.ins])
+            dev = torch.frombuffer(bytearray(arr), dtype=torch.uint8).to(basis.device)
+            self._dev[basis.device] = dev
+        nq = basis.X.shape[1]
+        prog = N.FemProgram(len(self.ins), self.out, len(self.names), nq, dev.data_ptr())
+        for k, n in enumerate(self.names):
+            prog.coef[k], prog.coef_stride[k] = coeffs.slot(n, basis.nelems, nq)
+        prog.qX = basis.X_dev.data_ptr()
+        prog.qW = basis.W_dev.data_ptr()
+        return prog
+
+
+MAX_PROGRAM = 512
+MAX_COEF = 16
 
 
 def _structure_key(ch):
@@ -162,7 +291,8 @@ def _structure_key(ch):
 
 
 def _program(form, basis, coeffs):
-    """The form's exact-order program (tracer.trace_tape) on the device."""
+    """The form's exact-order program (tracer.trace_tape) on the device, for
+    the exact-zero mask of the channel kernels' pattern build."""
     try:
         ins, out, names = trace_tape(form.form, basis.elem, basis.mesh.p.shape[0],
                                      list(coeffs.fields), coeffs.numbers)
@@ -170,62 +300,100 @@ def _program(form, basis, coeffs):
         # an operation the replay cannot reproduce bit for bit: the mask then
         # comes from the separately rounded tensor-form evaluation alone
         return None, None
-    if len(ins) > 512 or len(names) > 8:
+    if len(ins) > MAX_PROGRAM or len(names) > MAX_COEF:
         return None, None
     arr = (N.FemInstr * len(ins))(*[N.FemInstr(op, a, b, 0, imm) for op, a, b, imm in ins])
     dev = torch.frombuffer(bytearray(arr), dtype=torch.uint8).to(basis.device)
     prog = N.FemProgram(len(ins), out, len(names), basis.X.shape[1], dev.data_ptr())
     for k, n in enumerate(names):
         prog.coef[k] = coeffs.fields[n].data_ptr()
+    prog.qX = basis.X_dev.data_ptr()
+    prog.qW = basis.W_dev.data_ptr()
     return prog, dev
 
 
 class _PatternEntry:
-    def __init__(self, basis, c_form, stream, program=None):
+    def __init__(self, basis, c_form, stream, program=None, local=None):
         lib = N.lib()
         h = ctypes.c_void_p()
-        N.check(lib.fem_pattern_build(N.byref(basis.c_mesh), N.byref(basis.c_basis),
-                                      N.byref(c_form) if c_form is not None else None,
-                                      N.byref(program) if program is not None else None,
-                                      ctypes.byref(h), stream))
+        if local is not None:
+            N.check(lib.fem_pattern_build_local(N.byref(basis.c_mesh), N.byref(basis.c_basis),
+                                                N.ptr(local), ctypes.byref(h), stream))
+        else:
+            N.check(lib.fem_pattern_build(N.byref(basis.c_mesh), N.byref(basis.c_basis),
+                                          N.byref(c_form) if c_form is not None else None,
+                                          N.byref(program) if program is not None else None,
+                                          ctypes.byref(h), stream))
         self.pat = N.Pattern(h.value)
         dev = basis.device
         self.nrows = self.pat.nrows
         self.nnz = self.pat.nnz
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
-        if c_form is not None:
+        if c_form is not None or local is not None:
             self.indptr = torch.empty(self.nrows + 1, dtype=torch.int32, device=dev)
             self.indices = torch.empty(max(self.nnz, 1), dtype=torch.int32, device=dev)[:self.nnz]
             N.check(lib.fem_pattern_export(self.pat.handle, N.ptr(self.indptr),
                                            N.ptr(self.indices), stream))
-            self.staging = torch.empty(max(1, self.pat.staging_bytes // 8), dtype=torch.float64,
-                                       device=dev)
+            if local is None:
+                self.staging = torch.empty(max(1, self.pat.staging_bytes // 8),
+                                           dtype=torch.float64, device=dev)
             torch.cuda.current_stream().synchronize()
         else:
             self.staging = torch.empty(max(1, basis.nelems * basis.Nbfun), dtype=torch.float64,
                                        device=dev)
 
 
+def _raise_status(st):
+    if st & (1 << N.FEM_ERR_ZERO_JACOBIAN):
+        raise N.ZeroJacobianError("Zero Jacobian determinant")
+
+
+def _host_csr(entry, vals, n):
+    """Device CSR -> scipy.sparse.csr_matrix through pinned host buffers
+    (torch's caching host allocator reuses the blocks of matrices the
+    caller has dropped); the matrix owns its arrays through numpy views."""
+    data = torch.empty(entry.nnz, dtype=torch.float64, pin_memory=True)
+    indices = torch.empty(entry.nnz, dtype=torch.int32, pin_memory=True)
+    indptr = torch.empty(entry.nrows + 1, dtype=torch.int32, pin_memory=True)
+    data.copy_(vals, non_blocking=True)
+    indices.copy_(entry.indices, non_blocking=True)
+    indptr.copy_(entry.indptr, non_blocking=True)
+    torch.cuda.current_stream().synchronize()
+    K = sp.csr_matrix((data.numpy(), indices.numpy(), indptr.numpy()), shape=(n, n), copy=False)
+    K.has_sorted_indices = True
+    K.has_canonical_format = True
+    return K
+
+
 class BilinearForm(Form):
     """bilinear_form.py:19-151."""
 
     def _setup(self, ubasis, vbasis, kwargs):
+        """Coefficients, channels and FemBilinear of a form the channel
+        kernels take (NotImplementedError otherwise)."""
         if vbasis is not None and vbasis is not ubasis:
             raise NotImplementedError("different trial and test bases are not supported yet")
         coeffs = _Coefficients(ubasis, kwargs)
         ch = self._trace(ubasis, coeffs, "bilinear")
+        if ch is None:
+            raise NotImplementedError("this form / basis is assembled by the generic per-point "
+                                      "kernels only (no coefficient-channel form)")
+        return (coeffs, ch) + (self._c_form(ubasis, coeffs, ch),)
+
+    @staticmethod
+    def _c_form(ubasis, coeffs, ch):
         ne, dev = ubasis.nelems, ubasis.device
         z = N.FemCoef(0.0, None)
         if ubasis.elem.vector:
-            f = N.FemBilinear(z, coeffs.coef(ch["mass"], ne, dev), coeffs.coef(ch["lam"], ne, dev),
-                              coeffs.coef(ch["lap"], ne, dev), coeffs.coef(ch["tr"], ne, dev))
-        else:
-            f = N.FemBilinear(coeffs.coef(ch["diff"], ne, dev), coeffs.coef(ch["mass"], ne, dev),
-                              z, z, z)
-        return coeffs, ch, f
+            return N.FemBilinear(z, coeffs.coef(ch["mass"], ne, dev),
+                                 coeffs.coef(ch["lam"], ne, dev), coeffs.coef(ch["lap"], ne, dev),
+                                 coeffs.coef(ch["tr"], ne, dev))
+        return N.FemBilinear(coeffs.coef(ch["diff"], ne, dev), coeffs.coef(ch["mass"], ne, dev),
+                             z, z, z)
 
-    def _device_assemble(self, ubasis, vbasis=None, **kwargs):
-        coeffs, ch, c_form = self._setup(ubasis, vbasis, kwargs)
+    # ---------------------------------------------------- channel kernels
+    def _fast_once(self, ubasis, coeffs, ch):
+        c_form = self._c_form(ubasis, coeffs, ch)
         stream = N.stream_ptr()
         key = ("bilinear", _structure_key(ch))
         entry = ubasis._patterns.get(key)
@@ -239,52 +407,87 @@ class BilinearForm(Form):
         N.check(N.lib().fem_assemble(N.byref(ubasis.c_mesh), N.byref(ubasis.c_basis),
                                      N.byref(c_form), entry.pat.handle, N.ptr(entry.staging),
                                      N.ptr(vals), N.ptr(entry.status), stream))
-        return entry, vals, coeffs, key, c_form
+        return entry, vals, key
 
-    def _check_status(self, ubasis, entry, key):
-        st = int(entry.status.item())
-        if st & (1 << N.FEM_ERR_ZERO_JACOBIAN):
-            raise N.ZeroJacobianError("Zero Jacobian determinant")
-        if st & (1 << N.FEM_ERR_STALE_PATTERN):
+    # ---------------------------------------------------- generic kernels
+    def _local_generic(self, basis, coeffs):
+        g, key = self._generic(basis, coeffs, "bilinear")
+        prog = g.struct(basis, coeffs)
+        nb = basis.Nbfun
+        local = torch.empty(max(1, basis.nelems * nb * nb), dtype=torch.float64,
+                            device=basis.device)
+        status = torch.zeros(1, dtype=torch.int32, device=basis.device)
+        N.check(N.lib().fem_program_local_matrices(N.byref(basis.c_mesh), N.byref(basis.c_basis),
+                                                   N.byref(prog), N.ptr(local), N.ptr(status),
+                                                   N.stream_ptr()))
+        return local, status, key
+
+    def _generic_assemble(self, basis, coeffs, check):
+        local, status, key = self._local_generic(basis, coeffs)
+        stream = N.stream_ptr()
+        entry = basis._patterns.get(key)
+        fresh = entry is None
+        if fresh:
+            entry = _PatternEntry(basis, None, stream, local=local)
+            basis._patterns[key] = entry
+        vals = torch.empty(max(entry.nnz, 1), dtype=torch.float64, device=basis.device)[:entry.nnz]
+        N.check(N.lib().fem_csr_sum_checked(entry.pat.handle, N.ptr(local), N.ptr(vals),
+                                            N.ptr(status), stream))
+        if check or fresh:
+            st = int(status.item())
+            _raise_status(st)
+            if st & (1 << N.FEM_ERR_STALE_PATTERN):
+                # the exact-zero structure changed: rebuild from these local
+                # matrices (they are exact, so the new pattern is final)
+                entry = _PatternEntry(basis, None, stream, local=local)
+                basis._patterns[key] = entry
+                vals = torch.empty(max(entry.nnz, 1), dtype=torch.float64,
+                                   device=basis.device)[:entry.nnz]
+                N.check(N.lib().fem_csr_sum(entry.pat.handle, N.ptr(local), N.ptr(vals), None,
+                                            stream))
+        return entry, vals
+
+    # ------------------------------------------------------------- driver
+    def _assemble_device(self, ubasis, vbasis, kwargs, check=True):
+        if vbasis is not None and vbasis is not ubasis:
+            raise NotImplementedError("different trial and test bases are not supported yet")
+        coeffs = _Coefficients(ubasis, kwargs)
+        ch = self._trace(ubasis, coeffs, "bilinear")
+        if ch is None:
+            return self._generic_assemble(ubasis, coeffs, check)
+        for attempt in range(2):
+            entry, vals, key = self._fast_once(ubasis, coeffs, ch)
+            if not check:
+                break
+            st = int(entry.status.item())
+            _raise_status(st)
+            if not st & (1 << N.FEM_ERR_STALE_PATTERN):
+                break
             del ubasis._patterns[key]
-            return False
-        return True
+        return entry, vals
 
     def assemble(self, ubasis, vbasis=None, **kwargs):
         """Assemble into a scipy.sparse.csr_matrix (bilinear_form.py:130-148)."""
-        for _ in range(2):
-            entry, vals, coeffs, key, _f = self._device_assemble(ubasis, vbasis, **kwargs)
-            if self._check_status(ubasis, entry, key):
-                break
-        # Device -> pinned host copies (torch's caching host allocator reuses
-        # the blocks of matrices the caller has dropped); the returned matrix
-        # owns its arrays through their numpy views.
-        data = torch.empty(entry.nnz, dtype=torch.float64, pin_memory=True)
-        indices = torch.empty(entry.nnz, dtype=torch.int32, pin_memory=True)
-        indptr = torch.empty(entry.nrows + 1, dtype=torch.int32, pin_memory=True)
-        data.copy_(vals, non_blocking=True)
-        indices.copy_(entry.indices, non_blocking=True)
-        indptr.copy_(entry.indptr, non_blocking=True)
-        torch.cuda.current_stream().synchronize()
-        K = sp.csr_matrix((data.numpy(), indices.numpy(), indptr.numpy()),
-                          shape=(ubasis.N, ubasis.N), copy=False)
-        K.has_sorted_indices = True
-        K.has_canonical_format = True
-        return K
+        entry, vals = self._assemble_device(ubasis, vbasis, kwargs)
+        return _host_csr(entry, vals, ubasis.N)
 
     def assemble_torch(self, ubasis, vbasis=None, check=True, **kwargs):
         """Device-resident result: torch.sparse_csr_tensor (int32 indices,
         float64 values) sharing the cached pattern arrays."""
-        entry, vals, coeffs, key, _f = self._device_assemble(ubasis, vbasis, **kwargs)
-        if check and not self._check_status(ubasis, entry, key):
-            entry, vals, coeffs, key, _f = self._device_assemble(ubasis, vbasis, **kwargs)
+        entry, vals = self._assemble_device(ubasis, vbasis, kwargs, check=check)
         return torch.sparse_csr_tensor(entry.indptr, entry.indices, vals,
                                        size=(ubasis.N, ubasis.N))
 
     def elemental_torch(self, ubasis, **kwargs):
         """Local matrices (nelems, Nbfun, Nbfun), row = test function."""
-        coeffs, ch, c_form = self._setup(ubasis, None, kwargs)
+        coeffs = _Coefficients(ubasis, kwargs)
+        ch = self._trace(ubasis, coeffs, "bilinear")
         nb = ubasis.Nbfun
+        if ch is None:
+            local, status, _ = self._local_generic(ubasis, coeffs)
+            _raise_status(int(status.item()))
+            return local[:ubasis.nelems * nb * nb].view(ubasis.nelems, nb, nb)
+        c_form = self._c_form(ubasis, coeffs, ch)
         out = torch.empty((ubasis.nelems, nb, nb), dtype=torch.float64, device=ubasis.device)
         N.check(N.lib().fem_local_matrices(N.byref(ubasis.c_mesh), N.byref(ubasis.c_basis),
                                            N.byref(c_form), N.ptr(out), N.stream_ptr()))
@@ -292,7 +495,7 @@ class BilinearForm(Form):
 
     def pattern(self, ubasis, **kwargs):
         """(indptr, indices) device tensors of the cached CSR pattern."""
-        entry, _, _, _, _ = self._device_assemble(ubasis, None, **kwargs)
+        entry, _ = self._assemble_device(ubasis, None, kwargs)
         return entry.indptr, entry.indices
 
 
@@ -302,19 +505,44 @@ class LinearForm(Form):
     def _setup(self, basis, kwargs):
         coeffs = _Coefficients(basis, kwargs)
         ch = self._trace(basis, coeffs, "linear")
+        if ch is None:
+            raise NotImplementedError("this form / basis is assembled by the generic per-point "
+                                      "kernels only (no coefficient-channel form)")
         return coeffs, N.FemLinear(coeffs.coef(ch["load"], basis.nelems, basis.device))
 
-    def _device_assemble(self, basis, vbasis=None, **kwargs):
-        if vbasis is not None:
-            raise ValueError("LinearForm takes one basis")
-        coeffs, c_form = self._setup(basis, kwargs)
-        stream = N.stream_ptr()
+    def _incidence(self, basis, stream):
         key = ("incidence",)
         entry = basis._patterns.get(key)
         if entry is None:
             entry = _PatternEntry(basis, None, stream, None)
             basis._patterns[key] = entry
+        return entry
+
+    def _local_generic(self, basis, coeffs):
+        g, _ = self._generic(basis, coeffs, "linear")
+        prog = g.struct(basis, coeffs)
+        local = torch.empty(max(1, basis.nelems * basis.Nbfun), dtype=torch.float64,
+                            device=basis.device)
+        status = torch.zeros(1, dtype=torch.int32, device=basis.device)
+        N.check(N.lib().fem_program_local_vectors(N.byref(basis.c_mesh), N.byref(basis.c_basis),
+                                                  N.byref(prog), N.ptr(local), N.ptr(status),
+                                                  N.stream_ptr()))
+        return local, status
+
+    def _device_assemble(self, basis, vbasis=None, **kwargs):
+        if vbasis is not None:
+            raise ValueError("LinearForm takes one basis")
+        coeffs = _Coefficients(basis, kwargs)
+        ch = self._trace(basis, coeffs, "linear")
+        stream = N.stream_ptr()
+        entry = self._incidence(basis, stream)
         b = torch.empty(basis.N, dtype=torch.float64, device=basis.device)
+        if ch is None:
+            local, status = self._local_generic(basis, coeffs)
+            N.check(N.lib().fem_vector_sum(entry.pat.handle, N.ptr(local), N.ptr(b), stream))
+            _raise_status(int(status.item()))
+            return b, coeffs
+        c_form = N.FemLinear(coeffs.coef(ch["load"], basis.nelems, basis.device))
         N.check(N.lib().fem_assemble_vector(N.byref(basis.c_mesh), N.byref(basis.c_basis),
                                             N.byref(c_form), entry.pat.handle,
                                             N.ptr(entry.staging), N.ptr(b), stream))
@@ -332,12 +560,50 @@ class LinearForm(Form):
         return b
 
 
+class Functional(Form):
+    """functional.py:10-61: a form of ``w`` alone, integrated per cell
+    (``elemental``) or over the mesh (``assemble``, numpy's pairwise sum of
+    the per-cell values)."""
+
+    def _device_elemental(self, basis, kwargs):
+        coeffs = _Coefficients(basis, kwargs)
+        g, _ = self._generic(basis, coeffs, "functional")
+        prog = g.struct(basis, coeffs)
+        out = torch.empty(max(1, basis.nelems), dtype=torch.float64, device=basis.device)
+        status = torch.zeros(1, dtype=torch.int32, device=basis.device)
+        N.check(N.lib().fem_program_elemental(N.byref(basis.c_mesh), N.byref(basis.c_basis),
+                                              N.byref(prog), N.ptr(out), N.ptr(status),
+                                              N.stream_ptr()))
+        return out[:basis.nelems], status
+
+    def elemental_torch(self, basis, **kwargs):
+        out, status = self._device_elemental(basis, kwargs)
+        _raise_status(int(status.item()))
+        return out
+
+    def elemental(self, v, **kwargs):
+        """Per-cell values (functional.py:26-34) as a numpy array."""
+        return self.elemental_torch(v, **kwargs).cpu().numpy()
+
+    def assemble_torch(self, ubasis, vbasis=None, **kwargs):
+        assert vbasis is None
+        e, status = self._device_elemental(ubasis, kwargs)
+        total = torch.empty(1, dtype=torch.float64, device=ubasis.device)
+        N.check(N.lib().fem_sum_pairwise(N.ptr(e), ubasis.nelems, N.ptr(total), N.stream_ptr()))
+        _raise_status(int(status.item()))
+        return total[0]
+
+    def assemble(self, ubasis, vbasis=None, **kwargs):
+        """The functional's value (functional.py:36-61) as a numpy float64."""
+        return np.float64(self.assemble_torch(ubasis, vbasis, **kwargs).item())
+
+
 def asm(form, *args, **kwargs):
     """skfem/assembly/__init__.py:69-97 for a single basis (no list products)."""
     if not isinstance(form, Form):
         import inspect
         nargs = len(inspect.signature(form).parameters)
-        form = BilinearForm(form) if nargs == 3 else LinearForm(form)
+        form = {3: BilinearForm, 2: LinearForm, 1: Functional}[nargs](form)
     if any(isinstance(a, (list, tuple)) for a in args):
         raise NotImplementedError("asm over lists of bases is not supported")
     return form.assemble(*args, **kwargs)

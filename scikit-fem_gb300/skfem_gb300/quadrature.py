@@ -84,6 +84,13 @@ def get_quadrature(refdom, norder):
         t = _table(refdom, norder)
         if t is not None:
             return t
+    if refdom == "hex" and norder in (6, 7):
+        # the reference's default Hex1 rule as recorded (leggauss's last bits
+        # depend on the platform's eigenvalue solver)
+        from ._refquad import RULES
+        X, W = RULES["hex6"]
+        return (np.array([[float.fromhex(v) for v in row] for row in X]),
+                np.array([float.fromhex(v) for v in W]))
     return closed_form_quadrature(refdom, norder)
 
 

@@ -320,8 +320,19 @@ def linear_channels(sym, elem, dim):
 # CUDA mask kernel replays it for the local entries whose value is
 # rounding noise, so that the entries the reference computes as exactly
 # 0.0 -- and drops in eliminate_zeros -- are the entries dropped here.
+#
+# The same program is what the generic kernels evaluate for forms outside
+# the coefficient channels above (anisotropic and advection terms,
+# coefficients that vary inside cells, interpolated DOF vectors, the
+# default parameters w.x and w.h, numpy functions of fields).
 
-OP_CONST, OP_U, OP_V, OP_COEF, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG = range(9)
+(OP_CONST, OP_U, OP_V, OP_COEF, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_X, OP_H,
+ OP_SQRT, OP_EXP, OP_LOG, OP_SIN, OP_COS, OP_TAN, OP_TANH, OP_ARCTAN, OP_ABS,
+ OP_POW) = range(21)
+
+# ops that are correctly rounded on both sides (the rest use libm)
+EXACT_OPS = {OP_CONST, OP_U, OP_V, OP_COEF, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_X, OP_H,
+             OP_SQRT, OP_ABS}
 
 
 class Tape:
@@ -347,12 +358,49 @@ class Tape:
         return TapeNode(self, self.loads[(op, k)])
 
 
+def _unary(op):
+    def f(x):
+        if isinstance(x, TapeNode):
+            return TapeNode(x.tape, x.tape.emit(op, x.idx))
+        return _NUMPY_UNARY[op](x)
+    return f
+
+
+def _binary(fn):
+    return lambda a, b: fn(a, b)
+
+
+_NUMPY_UNARY = {OP_SQRT: np.sqrt, OP_EXP: np.exp, OP_LOG: np.log, OP_SIN: np.sin,
+                OP_COS: np.cos, OP_TAN: np.tan, OP_TANH: np.tanh, OP_ARCTAN: np.arctan,
+                OP_ABS: np.abs, OP_NEG: np.negative}
+
+_UFUNCS = {
+    np.sqrt: _unary(OP_SQRT), np.exp: _unary(OP_EXP), np.log: _unary(OP_LOG),
+    np.sin: _unary(OP_SIN), np.cos: _unary(OP_COS), np.tan: _unary(OP_TAN),
+    np.tanh: _unary(OP_TANH), np.arctan: _unary(OP_ARCTAN), np.absolute: _unary(OP_ABS),
+    np.negative: _unary(OP_NEG), np.positive: lambda x: x,
+    np.add: _binary(lambda a, b: a + b), np.subtract: _binary(lambda a, b: a - b),
+    np.multiply: _binary(lambda a, b: a * b), np.true_divide: _binary(lambda a, b: a / b),
+    np.power: _binary(lambda a, b: a ** b),
+    np.square: lambda x: x * x,
+}
+
+
 class TapeNode:
+    """One recorded value (a register of the form program)."""
     __slots__ = ("tape", "idx", "grad")
-    __array_ufunc__ = None
 
     def __init__(self, tape, idx):
         self.tape, self.idx, self.grad = tape, idx, None
+
+    def __array_ufunc__(self, ufunc, method, *inputs, **kwargs):
+        fn = _UFUNCS.get(ufunc)
+        if method != "__call__" or kwargs or fn is None:
+            raise NotImplementedError("numpy.%s is not supported in forms assembled on the GPU"
+                                      % getattr(ufunc, "__name__", ufunc))
+        if any(isinstance(x, np.ndarray) and x.ndim > 0 for x in inputs):
+            return np.frompyfunc(fn, len(inputs), 1)(*inputs)
+        return fn(*inputs)
 
     def _lift(self, o):
         if isinstance(o, TapeNode):
@@ -400,29 +448,93 @@ class TapeNode:
     def __pos__(self):
         return self
 
+    def __abs__(self):
+        return TapeNode(self.tape, self.tape.emit(OP_ABS, self.idx))
+
     def __pow__(self, n):
-        # numpy evaluates x**2 as x*x; other integer powers are not
-        # reproduced bit-exactly and are rejected
-        if n == 2:
-            return self * self
-        if n == 1:
-            return self
-        raise NotImplementedError("only **2 is supported in the exact-zero mask")
+        # numpy's scalar-exponent fast paths: x**2 = x*x, x**0.5 = sqrt(x),
+        # x**-1 = 1/x, x**1 = x, x**0 = 1; other exponents call pow
+        if isinstance(n, np.ndarray) and n.ndim == 0:
+            n = n.item()
+        if isinstance(n, numbers.Number) and not isinstance(n, TapeNode):
+            if n == 2:
+                return self * self
+            if n == 1:
+                return self
+            if n == 0.5:
+                return TapeNode(self.tape, self.tape.emit(OP_SQRT, self.idx))
+            if n == -1:
+                return self.tape.const(1.0) / self
+            if n == 0:
+                return self.tape.const(1.0)
+        return self._bin(OP_POW, n)
+
+    def __rpow__(self, o):
+        return self._bin(OP_POW, o, rev=True)
+
+    @property
+    def value(self):
+        return self
 
     @property
     def shape(self):
         return ()
 
 
+class FieldSpec:
+    """How a form argument appears to the program: 'elem' (one value per
+    cell) and 'qp' (one per quadrature point) are scalar slots; 'field' is
+    a DiscreteField -- ncomp value components (0: a scalar field) and, with
+    grad, the gradient components, each a per-point slot."""
+
+    def __init__(self, kind, ncomp=0, grad=False):
+        self.kind, self.ncomp, self.grad = kind, ncomp, grad
+
+    def quantities(self, dim):
+        n = max(self.ncomp, 1)
+        return n + (n * dim if self.grad else 0)
+
+
 class TapeParams(dict):
-    def __init__(self, tape, fields, numbers_):
+    def __init__(self, tape, fields, numbers_, dim=None, defaults=False):
         super().__init__()
         self.slots = {}
-        for k in fields:
-            self.slots[k] = len(self.slots)
-            self[k] = tape.load(OP_COEF, self.slots[k])
+        self.tape = tape
+        specs = fields if isinstance(fields, dict) else {k: FieldSpec("elem") for k in fields}
+        for k, s in specs.items():
+            if s.kind in ("elem", "qp"):
+                self[k] = self._slot(k)
+            else:
+                self[k] = self._field(k, s, dim)
         for k, v in numbers_.items():
             self[k] = v
+        if defaults:
+            # CellBasis.default_parameters (cell_basis.py:124-141)
+            if "x" not in self:
+                self["x"] = SymField(np.array([tape.load(OP_X, i) for i in range(dim)],
+                                              dtype=object))
+            if "h" not in self:
+                self["h"] = tape.load(OP_H, 0)
+
+    def _slot(self, key):
+        if key not in self.slots:
+            self.slots[key] = len(self.slots)
+        return self.tape.load(OP_COEF, self.slots[key])
+
+    def _field(self, name, s, dim):
+        if s.ncomp == 0:
+            node = self._slot((name, 0))
+            if s.grad:
+                node.grad = np.array([self._slot((name, 1 + k)) for k in range(dim)],
+                                     dtype=object)
+            return node
+        n = s.ncomp
+        val = np.array([self._slot((name, c)) for c in range(n)], dtype=object)
+        grad = None
+        if s.grad:
+            grad = np.array([[self._slot((name, n + c * dim + k)) for k in range(dim)]
+                             for c in range(n)], dtype=object)
+        return SymField(val, grad)
 
     __getattr__ = SymParams.__getattr__
     __getitem__ = SymParams.__getitem__
@@ -443,19 +555,60 @@ def _tape_field(tape, which, elem, dim):
     return SymField(val, grad)
 
 
-def trace_tape(form, elem, dim, fields, numbers_):
-    """Record the exact-order program of a bilinear form; returns
-    (instructions, output index, coefficient slot names)."""
+def _compact(ins, out, slots):
+    """Drop coefficient slots the output does not depend on (their loads
+    become constants) and renumber the rest densely."""
+    live = set()
+    stack = [out]
+    while stack:
+        k = stack.pop()
+        if k in live:
+            continue
+        live.add(k)
+        op, a, b, _ = ins[k]
+        if op in (OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_POW):
+            stack += [a, b]
+        elif op in (OP_NEG, OP_SQRT, OP_EXP, OP_LOG, OP_SIN, OP_COS, OP_TAN, OP_TANH,
+                    OP_ARCTAN, OP_ABS):
+            stack.append(a)
+    by_index = {v: k for k, v in slots.items()}
+    names, remap = [], {}
+    new = []
+    for k, (op, a, b, imm) in enumerate(ins):
+        if op == OP_COEF:
+            if k not in live:
+                new.append((OP_CONST, -1, -1, 0.0))
+                continue
+            if a not in remap:
+                remap[a] = len(names)
+                names.append(by_index[a])
+            new.append((op, remap[a], b, imm))
+        else:
+            new.append((op, a, b, imm))
+    return new, names
+
+
+def trace_tape(form, elem, dim, fields, numbers_, kind="bilinear", defaults=False):
+    """Record the exact-order program of a form; returns (instructions,
+    output index, coefficient slot keys).  kind: 'bilinear' (form(u, v, w)),
+    'linear' (form(v, w)) or 'functional' (form(w)).  fields: names of
+    per-element coefficients, or {name: FieldSpec}; slot keys are the names
+    ('elem'/'qp') or (name, quantity) pairs ('field')."""
     tape = Tape()
-    u = _tape_field(tape, "u", elem, dim)
-    v = _tape_field(tape, "v", elem, dim)
-    w = TapeParams(tape, fields, numbers_)
-    r = form(u, v, w)
+    w = TapeParams(tape, fields, numbers_, dim=dim, defaults=defaults)
+    if kind == "bilinear":
+        u = _tape_field(tape, "u", elem, dim)
+        v = _tape_field(tape, "v", elem, dim)
+        r = form(u, v, w)
+    elif kind == "linear":
+        r = form(_tape_field(tape, "v", elem, dim), w)
+    else:
+        r = form(w)
     if isinstance(r, np.ndarray):
         if r.ndim != 0:
             raise ValueError("form must return a scalar field")
         r = r.item()
     if not isinstance(r, TapeNode):
         r = tape.const(r)
-    names = sorted(w.slots, key=w.slots.get)
-    return tape.ins, r.idx, names
+    ins, names = _compact(tape.ins, r.idx, w.slots)
+    return ins, r.idx, names

@@ -198,6 +198,8 @@ def main():
     save("tet_p1_subset", p=m.p, t=m.t, element_dofs=ib.element_dofs, tind=ib.tind,
          X=ib.X, W=ib.W, b=unit_load.assemble(ib), **csr_arrays(laplace.assemble(ib)))
 
+    generic_cases()
+
     # quadrature rules the configs use, exactly as the reference tabulates them
     from skfem.quadrature import get_quadrature_tet, get_quadrature_tri
     rules = {}
@@ -213,5 +215,123 @@ def main():
                 % (skfem.__version__, np.__version__, sys.version.split()[0]))
 
 
+def generic_cases():
+    """Forms outside the isotropic coefficient channels: anisotropic and
+    advection terms, w.x / w.h, per-point coefficients, interpolated DOF
+    vectors, numpy functions, Functional; with the reference's interpolate
+    output and global coordinates."""
+    from skfem.helpers import ddot, div, sym_grad
+    rng = np.random.default_rng(20261204)
+
+    @BilinearForm
+    def aniso_adv(u, v, w):
+        x = w.x
+        return ((1.0 + x[0] * x[1]) * grad(u)[0] * grad(v)[0] + 0.5 * grad(u)[1] * grad(v)[1]
+                + (x[0] * grad(u)[0] + 2.0 * grad(u)[1]) * v + w.h * u * v)
+
+    @BilinearForm
+    def qp_coef(u, v, w):
+        return w.c * dot(grad(u), grad(v)) + w.c ** 2 * u * v
+
+    @BilinearForm
+    def newton(u, v, w):
+        s = w['s']
+        return (1.0 + s ** 2) * dot(grad(u), grad(v)) + 2.0 * s * u * dot(grad(s), grad(v))
+
+    @LinearForm
+    def trig_load(v, w):
+        return np.sin(np.pi * w.x[0]) * np.cos(np.pi * w.x[1]) * v
+
+    @LinearForm
+    def newton_res(v, w):
+        s = w['s']
+        return (1.0 + s ** 2) * dot(grad(s), grad(v)) - w.x[0] * v
+
+    @Functional
+    def energy(w):
+        s = w['s']
+        return s ** 2 + dot(grad(s), grad(s)) + w.x[0] * w.h
+
+    # TriP2 on a jittered 6x6 square
+    n = 6
+    m = MeshTri.init_tensor(np.linspace(0, 1, n + 1), np.linspace(0, 1, n + 1))
+    p = m.p.copy()
+    inner = jitter(m, rng, 0.2)
+    p[:, inner] += rng.uniform(-0.2 / n, 0.2 / n, size=(2, int(inner.sum())))
+    m = MeshTri(p, m.t)
+    ib = Basis(m, ElementTriP2())
+    c = rng.uniform(0.5, 2.0, (ib.nelems, ib.X.shape[1]))
+    s = rng.standard_normal(ib.N)
+    sf = ib.interpolate(s)
+    K1 = aniso_adv.assemble(ib)
+    K2 = qp_coef.assemble(ib, c=c)
+    K3 = newton.assemble(ib, s=s)
+    save("tri_p2_generic", p=m.p, t=m.t, element_dofs=ib.element_dofs, X=ib.X, W=ib.W,
+         c=c, s=s, s_value=np.asarray(sf), s_grad=sf.grad,
+         x=np.asarray(ib.global_coordinates()), h=np.asarray(ib.mesh_parameters()),
+         b_trig=trig_load.assemble(ib), b_newton=newton_res.assemble(ib, s=s),
+         e_energy=energy.elemental(ib, s=s), f_energy=np.float64(energy.assemble(ib, s=s)),
+         **{k + "_aniso": v for k, v in csr_arrays(K1).items()},
+         **{k + "_qp": v for k, v in csr_arrays(K2).items()},
+         **{k + "_newton": v for k, v in csr_arrays(K3).items()})
+
+    # TetP1 (4-point rule) and Hex1 (64 points) on jittered meshes
+    for name, mesh_cls, elem, n in (("tet_p1_generic", MeshTet, ElementTetP1(), 3),
+                                    ("hex1_generic", MeshHex, ElementHex1(), 3)):
+        m = mesh_cls.init_tensor(*(np.linspace(0, 1, n + 1),) * 3)
+        p = m.p.copy()
+        inner = jitter(m, rng, 0.2)
+        p[:, inner] += rng.uniform(-0.2 / n, 0.2 / n, size=(3, int(inner.sum())))
+        m = mesh_cls(p, m.t)
+        ib = Basis(m, elem)
+        c = rng.uniform(0.5, 2.0, (ib.nelems, ib.X.shape[1]))
+        s = rng.standard_normal(ib.N)
+        sf = ib.interpolate(s)
+
+        @BilinearForm
+        def aniso3(u, v, w):
+            x = w.x
+            return ((1.0 + x[2]) * grad(u)[0] * grad(v)[0] + grad(u)[1] * grad(v)[1]
+                    + 0.25 * grad(u)[2] * grad(v)[2] + x[1] * grad(u)[2] * v)
+
+        save(name, p=m.p, t=m.t, element_dofs=ib.element_dofs, X=ib.X, W=ib.W, c=c, s=s,
+             s_value=np.asarray(sf), s_grad=sf.grad, x=np.asarray(ib.global_coordinates()),
+             h=np.asarray(ib.mesh_parameters()),
+             b_newton=newton_res.assemble(ib, s=s), e_energy=energy.elemental(ib, s=s),
+             f_energy=np.float64(energy.assemble(ib, s=s)),
+             **{k + "_aniso": v for k, v in csr_arrays(aniso3.assemble(ib)).items()},
+             **{k + "_qp": v for k, v in csr_arrays(qp_coef.assemble(ib, c=c)).items()},
+             **{k + "_newton": v for k, v in csr_arrays(newton.assemble(ib, s=s)).items()})
+
+    # vector TetP2: elasticity plus a convection-like term with an
+    # interpolated vector field d
+    n = 2
+    m = MeshTet.init_tensor(*(np.linspace(0, 1, n + 1),) * 3)
+    p = m.p.copy()
+    inner = jitter(m, rng, 0.2)
+    p[:, inner] += rng.uniform(-0.2 / n, 0.2 / n, size=(3, int(inner.sum())))
+    m = MeshTet(p, m.t)
+    ib = Basis(m, ElementVector(ElementTetP2()), intorder=4)
+    d = rng.standard_normal(ib.N)
+    df = ib.interpolate(d)
+
+    @BilinearForm
+    def vec_conv(u, v, w):
+        return (ddot(sym_grad(u), sym_grad(v)) + div(u) * div(v)
+                + dot(np.einsum('ij...,j...->i...', grad(u), w['d']), v))
+
+    @Functional
+    def vec_energy(w):
+        return ddot(grad(w['d']), grad(w['d'])) + dot(w['d'], w['d'])
+
+    save("tet_p2_vec_generic", p=m.p, t=m.t, element_dofs=ib.element_dofs, X=ib.X, W=ib.W,
+         d=d, d_value=np.asarray(df), d_grad=df.grad,
+         e_energy=vec_energy.elemental(ib, d=d), f_energy=np.float64(vec_energy.assemble(ib, d=d)),
+         **{k + "_conv": v for k, v in csr_arrays(vec_conv.assemble(ib, d=d)).items()})
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["--generic"]:
+        generic_cases()
+    else:
+        main()

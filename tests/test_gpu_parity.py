@@ -273,7 +273,9 @@ def test_errors_match_reference_types():
     with pytest.raises(ValueError):
         k_laplace.assemble(b, k=np.zeros(b.N + 1))            # wrong DOF-vector length
     with pytest.raises(NotImplementedError):
-        F.BilinearForm(lambda u, v, w: u.grad[0] * v).assemble(b)
+        F.BilinearForm(lambda u, v, w: np.arcsinh(u) * v).assemble(b)
+    with pytest.raises(NotImplementedError):
+        F.BilinearForm(lambda u, v, w: u * v, dtype=np.complex128)
 
 
 def test_stale_pattern_is_rebuilt():

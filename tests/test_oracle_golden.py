@@ -130,3 +130,30 @@ def test_element_subsets():
     b = O.OBasis(O.OMesh(g["p"], g["t"], "tet"), O.TetP1(), elements=g["tind"])
     check_csr(O.bilinear_assemble(O.laplace, b), g)
     np.testing.assert_allclose(O.linear_assemble(O.unit_load, b), g["b"], rtol=1e-13, atol=1e-17)
+
+
+def test_oracle_generic_forms_vs_reference():
+    """The oracle's default parameters (w.x, w.h), DOF-vector interpolation
+    and per-point coefficients against scikit-fem's outputs on the forms of
+    the generic kernels."""
+    from _generic import SCALAR_CASES, fixture_csr, newton, qp_coef
+    kinds = {3: "tri", 4: "tet", 8: "hex"}
+    elems = {"tri_p2_generic": O.TriP2(), "tet_p1_generic": O.TetP1(),
+             "hex1_generic": O.Hex1()}
+    for name, _, forms in SCALAR_CASES:
+        g = load(name)
+        bo = O.OBasis(O.OMesh(g["p"], g["t"], kinds[g["t"].shape[0]]), elems[name])
+        d = bo.default_parameters()
+        np.testing.assert_array_equal(d["x"], g["x"])
+        np.testing.assert_allclose(d["h"], g["h"], rtol=1e-15, atol=0)
+        f = bo.interpolate(g["s"])
+        np.testing.assert_array_equal(np.asarray(f), g["s_value"])
+        np.testing.assert_array_equal(f.grad, g["s_grad"])
+        cases = [(forms["aniso"], {}, "aniso"), (qp_coef, {"c": g["c"]}, "qp"),
+                 (newton, {"s": g["s"]}, "newton")]
+        for form, kw, suffix in cases:
+            K = O.bilinear_assemble(form.form, bo, **kw)
+            ip, ix, dat = fixture_csr(g, suffix)
+            np.testing.assert_array_equal(K.indptr, ip)
+            np.testing.assert_array_equal(K.indices, ix)
+            np.testing.assert_array_equal(K.data, dat)
