@@ -288,7 +288,7 @@ def _abi_step(F, N, form, b, coefs):
 def secondary_workloads(args, only=None):
     """The other workloads of the assembly path, each timed on the device.
     ``only`` restricts the run to one of tri_p1 / tet_p2_vec / hex1_vjp /
-    batched (sizes from --vec-n, --hex-n, --batch)."""
+    batched / generic (sizes from --vec-n, --hex-n, --batch, --generic-n)."""
     want = (lambda name: only is None or only == name)
     import torch
 
@@ -297,6 +297,7 @@ def secondary_workloads(args, only=None):
     from skfem_gb300 import helpers as H
     from skfem_gb300.models.elasticity import linear_elasticity
     from skfem_gb300.models.poisson import laplace, unit_load
+    from skfem_gb300.form import _Coefficients
 
     hbm, _ = peaks()
     out = {}
@@ -448,6 +449,40 @@ def secondary_workloads(args, only=None):
             "ms_per_mesh_api_calls": ms_api, "speedup_vs_per_mesh_api": ms_api / ms_graph,
             "launches_per_step": ga.launches_per_step()}
 
+    if want("generic"):
+        # generic per-point kernels: a Newton-step matrix with an
+        # interpolated DOF vector (exact reference arithmetic, -fmad=false),
+        # and a FacetBasis load on the boundary of the same mesh
+        n = args.generic_n
+        m = F.MeshTet.init_tensor(*(np.linspace(0, 1, n + 1),) * 3)
+        b = F.Basis(m, F.ElementTetP1())
+        rng = np.random.default_rng(args.seed)
+        s = torch.as_tensor(rng.standard_normal(b.N), device="cuda")
+
+        @F.BilinearForm
+        def newton(u, v, w):
+            z = w["s"]
+            return (1.0 + z ** 2) * H.dot(H.grad(u), H.grad(v)) + 2.0 * z * u * H.dot(
+                H.grad(z), H.grad(v))
+
+        @F.LinearForm
+        def flux(v, w):
+            return H.dot(w.n, w.x) * v
+
+        newton.assemble_torch(b, s=s)                     # pattern built once
+        ms_asm = _time(lambda: newton.assemble_torch(b, check=False, s=s), 5)
+        ms_interp = _time(lambda: b.interpolate_torch(s), 5)
+        ms_local = _time(lambda: newton._local_generic(b, _Coefficients(b, {"s": s})), 5)
+        fb = F.FacetBasis(m, F.ElementTetP1())
+        flux.assemble_torch(fb)
+        ms_facet = _time(lambda: flux.assemble_torch(fb), 5)
+        out["generic_newton_tet_p1"] = {
+            "nelems": int(b.nelems), "nnz": int(newton.pattern(b, s=s)[1].numel()),
+            "ms_assemble": ms_asm, "ms_interpolate": ms_interp,
+            "ms_interpolate_plus_local": ms_local,
+            "elements_per_s": b.nelems / (ms_asm * 1e-3),
+            "facets": int(fb.nelems), "ms_facet_load": ms_facet}
+
     return out
 
 
@@ -514,8 +549,10 @@ def main():
     ap.add_argument("--batch", type=int, default=512, help="meshes of the batched workload")
     ap.add_argument("--vec-n", type=int, default=40, help="cells per axis, vector TetP2 workload")
     ap.add_argument("--hex-n", type=int, default=64, help="cells per axis, Hex1 adjoint workload")
+    ap.add_argument("--generic-n", type=int, default=60,
+                    help="cells per axis, generic-kernel TetP1 workload")
     ap.add_argument("--only", default=None,
-                    choices=["tri_p1", "tet_p2_vec", "hex1_vjp", "batched"],
+                    choices=["tri_p1", "tet_p2_vec", "hex1_vjp", "batched", "generic"],
                     help="run one secondary workload alone and print its record")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-secondary", action="store_true",

@@ -114,7 +114,8 @@ typedef struct FemLinear {
  *   6 MUL a b | 7 DIV a b | 8 NEG a | 9 X a (global coordinate a at the
  *   point, MappingAffine.F / MappingIsoparametric.F arithmetic) | 10 H (mesh
  *   parameter |detDF|**(1/dim)) | 11 SQRT a | 12 EXP a | 13 LOG a | 14 SIN a |
- *   15 COS a | 16 TAN a | 17 TANH a | 18 ARCTAN a | 19 ABS a | 20 POW a b.
+ *   15 COS a | 16 TAN a | 17 TANH a | 18 ARCTAN a | 19 ABS a | 20 POW a b |
+ *   21 N a (component a of the unit outward normal, facet programs).
  *   Operands a, b of arithmetic ops name earlier instructions.  Ops 12-18 and
  *   20 use the CUDA math library (last-bit differences from numpy possible);
  *   all others are correctly rounded and reproduce the reference bit for bit.
@@ -321,6 +322,36 @@ int fem_interpolate(const FemMesh* mesh, const FemBasis* basis, int32_t nq, cons
  * order (leaves of <= 128 values, split at n/2 rounded down to a multiple
  * of 8); *out (device) receives the sum (Functional.assemble). */
 int fem_sum_pairwise(const double* x, int64_t n, double* out, fem_stream_t stream);
+
+/*
+ * FacetBasis (skfem/assembly/basis/facet_basis.py:21-110) on affine simplex
+ * meshes: the facets integrated over, each with the cell whose basis is
+ * traced (f2t[side]) and the cell that orients the normal (f2t[0]).  The
+ * program's qX / qW are the facet rule (dim-1, nq); its X / H / N ops read
+ * the facet point's coordinates, |detDG|**(1/(dim-1)) and the unit outward
+ * normal.  Outputs are per facet, laid out as the cell versions'.
+ */
+typedef struct FemFacets {
+  int64_t nfacets;
+  const int32_t* fverts;    /* (dim, nfacets): the facets' vertices (Mesh.facets columns) */
+  const int32_t* tind;      /* (nfacets) */
+  const int32_t* tind_n;    /* (nfacets) */
+  const int32_t* lfacet_n;  /* (nfacets): row of t2f holding the facet in tind_n */
+} FemFacets;
+
+int fem_facet_program_local_matrices(const FemMesh* mesh, const FemBasis* basis,
+                                     const FemFacets* facets, const FemProgram* program,
+                                     double* local, int32_t* status, fem_stream_t stream);
+int fem_facet_program_local_vectors(const FemMesh* mesh, const FemBasis* basis,
+                                    const FemFacets* facets, const FemProgram* program,
+                                    double* local, int32_t* status, fem_stream_t stream);
+int fem_facet_program_elemental(const FemMesh* mesh, const FemBasis* basis,
+                                const FemFacets* facets, const FemProgram* program, double* out,
+                                int32_t* status, fem_stream_t stream);
+/* FacetBasis.interpolate: as fem_interpolate at the facet points X (dim-1, nq). */
+int fem_facet_interpolate(const FemMesh* mesh, const FemBasis* basis, const FemFacets* facets,
+                          int32_t nq, const double* X, const double* w, double* out,
+                          fem_stream_t stream);
 
 /* Vertex incidence of the mesh (rows = vertices), used by the adjoint's
  * fixed-order gather of per-element coordinate gradients. */

@@ -27,10 +27,10 @@ int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st
 int vector_sum(const Pattern& P, const double* local, double* b, cudaStream_t st);
 void free_pattern(Pattern* P);
 int zero_check(const Pattern& P, const double* local, int32_t* status, cudaStream_t st);
-int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemProgram& prog,
-                 double* out, int32_t* status, cudaStream_t st);
-int interpolate(const FemMesh& m, const FemBasis& b, int nq, const double* X, const double* w,
-                double* out, cudaStream_t st);
+int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets* fc,
+                 const FemProgram& prog, double* out, int32_t* status, cudaStream_t st);
+int interpolate(const FemMesh& m, const FemBasis& b, const FemFacets* fc, int nq, const double* X,
+                const double* w, double* out, int32_t* status, cudaStream_t st);
 int sum_pairwise(const double* x, int64_t n, double* out, cudaStream_t st);
 int faithful_mask(const FemMesh& m, const FemBasis& b, const FemProgram& prog, int nq, double* local,
                   int32_t* status, cudaStream_t st);
@@ -179,6 +179,29 @@ static int read_status(int32_t* dstatus, cudaStream_t st) {
     return FEM_ERR_UNSUPPORTED;
   }
   return 0;
+}
+
+// interpolation with a status word of its own (invalid facet cells)
+static int interp_with_status(const FemMesh* mesh, const FemBasis* basis, const FemFacets* facets,
+                              int32_t nq, const double* X, const double* w, double* out,
+                              fem_stream_t stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  int32_t* dstatus = nullptr;
+  FEM_TRY_CUDA(cudaMallocAsync(&dstatus, sizeof(int32_t), st));
+  cudaMemsetAsync(dstatus, 0, sizeof(int32_t), st);
+  int rc = fem::interpolate(*mesh, *basis, facets, nq, X, w, out, dstatus, st);
+  int32_t h = 0;
+  if (!rc) {
+    cudaMemcpyAsync(&h, dstatus, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = fem::check_cuda(e, "interpolate");
+  }
+  cudaFreeAsync(dstatus, st);
+  if (!rc && h) {
+    set_error(FEM_ERR_ARGUMENT, "facet with a cell index out of range");
+    rc = FEM_ERR_ARGUMENT;
+  }
+  return rc;
 }
 
 extern "C" {
@@ -377,32 +400,71 @@ int fem_assemble_vector(const FemMesh* mesh, const FemBasis* basis, const FemLin
 }
 
 static int program_entry(int mode, const FemMesh* mesh, const FemBasis* basis,
-                         const FemProgram* program, double* out, int32_t* status,
-                         fem_stream_t stream) {
+                         const FemFacets* facets, const FemProgram* program, double* out,
+                         int32_t* status, fem_stream_t stream) {
   int rc = validate(mesh, basis);
   if (rc) return rc;
   if (!program || !out || !status) {
     set_error(FEM_ERR_ARGUMENT, "null program, output or status");
     return FEM_ERR_ARGUMENT;
   }
-  return fem::program_eval(mode, *mesh, *basis, *program, out, status, (cudaStream_t)stream);
+  return fem::program_eval(mode, *mesh, *basis, facets, *program, out, status,
+                           (cudaStream_t)stream);
 }
 
 int fem_program_local_matrices(const FemMesh* mesh, const FemBasis* basis,
                                const FemProgram* program, double* local, int32_t* status,
                                fem_stream_t stream) {
-  return program_entry(0, mesh, basis, program, local, status, stream);
+  return program_entry(0, mesh, basis, nullptr, program, local, status, stream);
 }
 
 int fem_program_local_vectors(const FemMesh* mesh, const FemBasis* basis,
                               const FemProgram* program, double* local, int32_t* status,
                               fem_stream_t stream) {
-  return program_entry(1, mesh, basis, program, local, status, stream);
+  return program_entry(1, mesh, basis, nullptr, program, local, status, stream);
 }
 
 int fem_program_elemental(const FemMesh* mesh, const FemBasis* basis, const FemProgram* program,
                           double* out, int32_t* status, fem_stream_t stream) {
-  return program_entry(2, mesh, basis, program, out, status, stream);
+  return program_entry(2, mesh, basis, nullptr, program, out, status, stream);
+}
+
+static int facets_given(const FemFacets* facets) {
+  if (!facets) {
+    set_error(FEM_ERR_ARGUMENT, "null facets");
+    return FEM_ERR_ARGUMENT;
+  }
+  return 0;
+}
+
+int fem_facet_program_local_matrices(const FemMesh* mesh, const FemBasis* basis,
+                                     const FemFacets* facets, const FemProgram* program,
+                                     double* local, int32_t* status, fem_stream_t stream) {
+  if (int rc = facets_given(facets)) return rc;
+  return program_entry(0, mesh, basis, facets, program, local, status, stream);
+}
+
+int fem_facet_program_local_vectors(const FemMesh* mesh, const FemBasis* basis,
+                                    const FemFacets* facets, const FemProgram* program,
+                                    double* local, int32_t* status, fem_stream_t stream) {
+  if (int rc = facets_given(facets)) return rc;
+  return program_entry(1, mesh, basis, facets, program, local, status, stream);
+}
+
+int fem_facet_program_elemental(const FemMesh* mesh, const FemBasis* basis,
+                                const FemFacets* facets, const FemProgram* program, double* out,
+                                int32_t* status, fem_stream_t stream) {
+  if (int rc = facets_given(facets)) return rc;
+  return program_entry(2, mesh, basis, facets, program, out, status, stream);
+}
+
+int fem_facet_interpolate(const FemMesh* mesh, const FemBasis* basis, const FemFacets* facets,
+                          int32_t nq, const double* X, const double* w, double* out,
+                          fem_stream_t stream) {
+  int rc = validate(mesh, basis);
+  if (rc) return rc;
+  if ((rc = facets_given(facets))) return rc;
+  return interp_with_status(mesh, basis, facets, nq, X, w, out, stream);
 }
 
 int fem_pattern_build_local(const FemMesh* mesh, const FemBasis* basis, const double* local,
@@ -451,7 +513,7 @@ int fem_interpolate(const FemMesh* mesh, const FemBasis* basis, int32_t nq, cons
                     const double* w, double* out, fem_stream_t stream) {
   int rc = validate(mesh, basis);
   if (rc) return rc;
-  return fem::interpolate(*mesh, *basis, nq, X, w, out, (cudaStream_t)stream);
+  return fem::interpolate(*mesh, *basis, nullptr, nq, X, w, out, nullptr, (cudaStream_t)stream);
 }
 
 int fem_sum_pairwise(const double* x, int64_t n, double* out, fem_stream_t stream) {

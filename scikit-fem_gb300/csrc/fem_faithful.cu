@@ -81,20 +81,41 @@ __global__ void mask_kernel(FemMesh m, FemBasis b, FemProgram prog, int nq, doub
 }
 
 // ------------------------------------------------------------ generic forms
-// One block takes EPB cells.  Stage 1: the geometry of every (cell, point)
-// pair into shared memory.  Stage 2: form * dx for every (cell, entry,
-// point) triple into shared memory.  Stage 3: numpy's pairwise sum over the
-// points of each entry.  MODE 0: bilinear (L = nbfun^2 entries, row = test
-// function), 1: linear (L = nbfun), 2: functional (L = 1).
+// One block takes EPB cells (or facets).  Stage 1: the geometry of every
+// (cell, point) pair into shared memory.  Stage 2: form * dx for every
+// (cell, entry, point) triple into shared memory.  Stage 3: numpy's
+// pairwise sum over the points of each entry.  MODE 0: bilinear (L =
+// nbfun^2 entries, row = test function), 1: linear (L = nbfun), 2:
+// functional (L = 1).  FACET: the cells are a FacetBasis's facets.
 struct GenericShape {
   int epb, L, nq;
 };
 
-template <int D, int MODE>
-__global__ void program_kernel(FemMesh m, FemBasis b, FemProgram prog, Rule rule, GenericShape s,
-                               double* __restrict__ out, int32_t* __restrict__ status) {
+constexpr int kGeo = 20;  // inv 9, det, qx 7, reference point 3
+
+template <int D, bool FACET>
+__device__ bool geometry_at(const FemMesh& m, const FemBasis& b, const FemFacets& fc,
+                            const Rule& rule, ProgFlags f, int64_t e, int q, double Y[3],
+                            PointGeo& g) {
+  if (FACET) {
+    double Xf[2] = {rule.X[q], D == 3 ? rule.X[rule.nq + q] : 0.0};
+    return facet_point<D>(m, fc, e, Xf, Y, g);
+  }
+  const bool hex = b.family == FEM_HEX_1;
+  CellGeo c;
+  cell_geometry<D>(m, e, hex, c);
+  Y[0] = rule.X[q];
+  Y[1] = rule.X[rule.nq + q];
+  Y[2] = D == 3 ? rule.X[2 * rule.nq + q] : 0.0;
+  point_geometry<D>(m, e, hex, c, f, Y[0], Y[1], Y[2], g);
+  return true;
+}
+
+template <int D, int MODE, bool FACET>
+__global__ void program_kernel(FemMesh m, FemBasis b, FemFacets fc, FemProgram prog, Rule rule,
+                               GenericShape s, int64_t ncells, double* __restrict__ out,
+                               int32_t* __restrict__ status) {
   extern __shared__ double gsm[];
-  constexpr int kGeo = 14;  // inv 9, det, qx 4
   double* geo = gsm;
   double* val = gsm + (size_t)s.epb * s.nq * kGeo;
   const bool hex = b.family == FEM_HEX_1;
@@ -104,19 +125,21 @@ __global__ void program_kernel(FemMesh m, FemBasis b, FemProgram prog, Rule rule
   for (int k = threadIdx.x; k < s.epb * s.nq; k += blockDim.x) {
     const int el = k / s.nq, q = k - el * s.nq;
     const int64_t e = e0 + el;
-    if (e >= m.nelems) continue;
-    CellGeo c;
-    cell_geometry<D>(m, e, hex, c);
-    const double x = rule.X[q], y = rule.X[rule.nq + q];
-    const double z = D == 3 ? rule.X[2 * rule.nq + q] : 0.0;
+    if (e >= ncells) continue;
     PointGeo g;
-    point_geometry<D>(m, e, hex, c, f, x, y, z, g);
-    if (hex && g.det == 0.0) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
+    double Y[3];
+    if (!geometry_at<D, FACET>(m, b, fc, rule, f, e, q, Y, g)) {
+      atomicOr(status, 1 << FEM_ERR_ARGUMENT);
+      g = PointGeo{};
+      Y[0] = Y[1] = Y[2] = 0.0;
+    }
+    if (!FACET && hex && g.det == 0.0) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
     double* G = geo + (size_t)k * kGeo;
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) G[i * 3 + j] = g.inv[i][j];
     G[9] = g.det;
-    for (int i = 0; i < 4; ++i) G[10 + i] = g.qx[i];
+    for (int i = 0; i < 7; ++i) G[10 + i] = g.qx[i];
+    for (int i = 0; i < 3; ++i) G[17 + i] = Y[i];
   }
   __syncthreads();
   double R[kMaxProgram];
@@ -126,7 +149,7 @@ __global__ void program_kernel(FemMesh m, FemBasis b, FemProgram prog, Rule rule
     const int rq = k - el * per;
     const int r = rq / s.nq, q = rq - r * s.nq;
     const int64_t e = e0 + el;
-    if (e >= m.nelems) continue;
+    if (e >= ncells) continue;
     const int i = MODE == 0 ? r / nb : (MODE == 1 ? r : 0);
     const int j = MODE == 0 ? r - i * nb : 0;
     const double* G = geo + ((size_t)el * s.nq + q) * kGeo;
@@ -134,50 +157,50 @@ __global__ void program_kernel(FemMesh m, FemBasis b, FemProgram prog, Rule rule
     for (int a = 0; a < 3; ++a)
       for (int c = 0; c < 3; ++c) g.inv[a][c] = G[a * 3 + c];
     g.det = G[9];
-    for (int a = 0; a < 4; ++a) g.qx[a] = G[10 + a];
-    const double x = rule.X[q], y = rule.X[rule.nq + q];
-    const double z = D == 3 ? rule.X[2 * rule.nq + q] : 0.0;
-    val[k] = point_value<D>(b, prog, e, q, i, j, x, y, z, g, rule.W[q], R);
+    for (int a = 0; a < 7; ++a) g.qx[a] = G[10 + a];
+    val[k] = point_value<D>(b, prog, e, q, i, j, G[17], G[18], G[19], g, rule.W[q], R);
   }
   __syncthreads();
   for (int k = threadIdx.x; k < s.epb * s.L; k += blockDim.x) {
     const int el = k / s.L;
     const int64_t e = e0 + el;
-    if (e >= m.nelems) continue;
+    if (e >= ncells) continue;
     out[e0 * s.L + k] = np_pairwise_sum(val + (size_t)k * s.nq, s.nq);
   }
 }
 
 // Basis.interpolate for one (cell, point) per thread: quantity k of the
-// field, out[(k * nelems + e) * nq + q] = 0*(w0 phi_0) + sum_i w_i phi_i
-// in local-function order (abstract_basis.py:295-304).
-template <int D>
-__global__ void interpolate_kernel(FemMesh m, FemBasis b, Rule rule, const double* __restrict__ w,
-                                   double* __restrict__ out) {
+// field, out[(k * ncells + e) * nq + q] = 0*(w0 phi_0) + sum_i w_i phi_i
+// in local-function order (abstract_basis.py:295-304).  FACET: at the
+// facet points, with the basis of the cell f2t[side].
+template <int D, bool FACET>
+__global__ void interpolate_kernel(FemMesh m, FemBasis b, FemFacets fc, Rule rule, int64_t ncells,
+                                   const double* __restrict__ w, double* __restrict__ out,
+                                   int32_t* __restrict__ status) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= m.nelems * rule.nq) return;
+  if (t >= ncells * rule.nq) return;
   const int64_t e = t / rule.nq;
   const int q = (int)(t - e * rule.nq);
-  const bool hex = b.family == FEM_HEX_1;
   const bool vec = b.vector != 0;
-  CellGeo c;
-  cell_geometry<D>(m, e, hex, c);
-  const double x = rule.X[q], y = rule.X[rule.nq + q];
-  const double z = D == 3 ? rule.X[2 * rule.nq + q] : 0.0;
   PointGeo g;
-  point_geometry<D>(m, e, hex, c, ProgFlags(), x, y, z, g);
+  double Y[3];
+  if (!geometry_at<D, FACET>(m, b, fc, rule, ProgFlags(), e, q, Y, g)) {
+    if (status) atomicOr(status, 1 << FEM_ERR_ARGUMENT);
+    return;
+  }
+  const int64_t ec = FACET ? (int64_t)fc.tind[e] : e;   // the cell whose DOFs are read
   constexpr int NQ = D + D * D;
   const int nquant = vec ? D + D * D : 1 + D;
   double acc[NQ], qq[NQ];
-  const double w0 = w[b.element_dofs[e]];
-  quantities<D>(b.family, vec, 0, x, y, z, g.inv, qq);
+  const double w0 = w[b.element_dofs[ec]];
+  quantities<D>(b.family, vec, 0, Y[0], Y[1], Y[2], g.inv, qq);
   for (int k = 0; k < nquant; ++k) acc[k] = 0.0 * (w0 * qq[k]);
   for (int i = 0; i < b.nbfun; ++i) {
-    const double wi = w[b.element_dofs[(int64_t)i * m.nelems + e]];
-    quantities<D>(b.family, vec, i, x, y, z, g.inv, qq);
+    const double wi = w[b.element_dofs[(int64_t)i * m.nelems + ec]];
+    quantities<D>(b.family, vec, i, Y[0], Y[1], Y[2], g.inv, qq);
     for (int k = 0; k < nquant; ++k) acc[k] = acc[k] + wi * qq[k];
   }
-  for (int k = 0; k < nquant; ++k) out[((int64_t)k * m.nelems + e) * rule.nq + q] = acc[k];
+  for (int k = 0; k < nquant; ++k) out[((int64_t)k * ncells + e) * rule.nq + q] = acc[k];
 }
 
 // numpy's pairwise sum of n doubles (np.sum of a contiguous vector): the
@@ -266,7 +289,7 @@ int check_program(const FemProgram& prog, int dim, bool vec, bool need_rule) {
       case OP_CONST: case OP_H: break;
       case OP_U: case OP_V: ok = I.a >= 0 && I.a < nquant; break;
       case OP_COEF: ok = I.a >= 0 && I.a < prog.ncoef; break;
-      case OP_X: ok = I.a >= 0 && I.a < dim; break;
+      case OP_X: case OP_N: ok = I.a >= 0 && I.a < dim; break;
       case OP_ADD: case OP_SUB: case OP_MUL: case OP_DIV: case OP_POW:
         ok = I.a >= 0 && I.a < k && I.b >= 0 && I.b < k; break;
       case OP_NEG: case OP_SQRT: case OP_EXP: case OP_LOG: case OP_SIN: case OP_COS:
@@ -297,16 +320,35 @@ int faithful_mask(const FemMesh& m, const FemBasis& b, const FemProgram& prog, i
   return 0;
 }
 
-// mode 0: local matrices, 1: local vectors, 2: per-cell functional values
-int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemProgram& prog,
-                 double* out, int32_t* status, cudaStream_t st) {
+static bool facets_ok(const FemMesh& m, const FemBasis& b, const FemFacets* fc) {
+  if (!fc) return true;
+  if (b.family == FEM_HEX_1) {
+    set_error(FEM_ERR_UNSUPPORTED, "FacetBasis on Hex1 meshes is not implemented");
+    return false;
+  }
+  if (fc->nfacets < 0 || (fc->nfacets > 0 && (!fc->fverts || !fc->tind || !fc->tind_n ||
+                                               !fc->lfacet_n))) {
+    set_error(FEM_ERR_ARGUMENT, "invalid facet arrays");
+    return false;
+  }
+  (void)m;
+  return true;
+}
+
+// mode 0: local matrices, 1: local vectors, 2: per-cell functional values;
+// fc non-null: over the facets of a FacetBasis
+int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets* fc,
+                 const FemProgram& prog, double* out, int32_t* status, cudaStream_t st) {
+  if (!facets_ok(m, b, fc)) return fc && b.family == FEM_HEX_1 ? FEM_ERR_UNSUPPORTED
+                                                               : FEM_ERR_ARGUMENT;
   int rc = check_program(prog, m.dim, b.vector != 0, true);
   if (rc) return rc;
-  if (m.nelems == 0) return 0;
+  const int64_t ncells = fc ? fc->nfacets : m.nelems;
+  if (ncells == 0) return 0;
   const int nb = b.nbfun;
   const int L = mode == 0 ? nb * nb : (mode == 1 ? nb : 1);
   const int nq = prog.nq;
-  auto bytes = [&](int epb) { return (size_t)epb * nq * (14 + L) * sizeof(double); };
+  auto bytes = [&](int epb) { return (size_t)epb * nq * (fem_faithful::kGeo + L) * sizeof(double); };
   int epb = std::max(1, std::min(64, 2048 / (L * nq)));
   while (epb > 1 && bytes(epb) > 96 * 1024) --epb;
   const size_t smem = bytes(epb);
@@ -316,7 +358,8 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemProgram
   }
   fem_faithful::GenericShape s{epb, L, nq};
   const fem_faithful::Rule rule{prog.qX, prog.qW, nq};
-  const unsigned grid = (unsigned)ceil_div(m.nelems, epb);
+  const FemFacets F = fc ? *fc : FemFacets{};
+  const unsigned grid = (unsigned)ceil_div(ncells, epb);
   const int threads = 256;
   auto go = [&](auto kern) -> int {
     if (smem > 48 * 1024) {
@@ -324,35 +367,52 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemProgram
                                            (int)smem);
       if (e != cudaSuccess) return check_cuda(e, "program kernel smem");
     }
-    kern<<<grid, threads, smem, st>>>(m, b, prog, rule, s, out, status);
+    kern<<<grid, threads, smem, st>>>(m, b, F, prog, rule, s, ncells, out, status);
     return 0;
   };
   using namespace fem_faithful;
-  if (m.dim == 2)
-    rc = mode == 0 ? go(program_kernel<2, 0>) : mode == 1 ? go(program_kernel<2, 1>)
-                                                          : go(program_kernel<2, 2>);
-  else
-    rc = mode == 0 ? go(program_kernel<3, 0>) : mode == 1 ? go(program_kernel<3, 1>)
-                                                          : go(program_kernel<3, 2>);
+  if (fc) {
+    if (m.dim == 2)
+      rc = mode == 0 ? go(program_kernel<2, 0, true>) : mode == 1 ? go(program_kernel<2, 1, true>)
+                                                                  : go(program_kernel<2, 2, true>);
+    else
+      rc = mode == 0 ? go(program_kernel<3, 0, true>) : mode == 1 ? go(program_kernel<3, 1, true>)
+                                                                  : go(program_kernel<3, 2, true>);
+  } else {
+    if (m.dim == 2)
+      rc = mode == 0 ? go(program_kernel<2, 0, false>) : mode == 1 ? go(program_kernel<2, 1, false>)
+                                                                   : go(program_kernel<2, 2, false>);
+    else
+      rc = mode == 0 ? go(program_kernel<3, 0, false>) : mode == 1 ? go(program_kernel<3, 1, false>)
+                                                                   : go(program_kernel<3, 2, false>);
+  }
   if (rc) return rc;
   FEM_LAUNCH_CHECK("program kernel");
   return 0;
 }
 
-int interpolate(const FemMesh& m, const FemBasis& b, int nq, const double* X, const double* w,
-                double* out, cudaStream_t st) {
-  if (nq <= 0 || nq > fem_faithful::kMaxPoints || !X || !w || !out) {
+int interpolate(const FemMesh& m, const FemBasis& b, const FemFacets* fc, int nq, const double* X,
+                const double* w, double* out, int32_t* status, cudaStream_t st) {
+  if (nq <= 0 || nq > fem_faithful::kMaxPoints || !X || !w || !out || (fc && !status)) {
     set_error(FEM_ERR_ARGUMENT, "interpolate: %d points, X/w/out must be device arrays", nq);
     return FEM_ERR_ARGUMENT;
   }
-  const int64_t n = m.nelems * (int64_t)nq;
+  if (!facets_ok(m, b, fc)) return fc && b.family == FEM_HEX_1 ? FEM_ERR_UNSUPPORTED
+                                                               : FEM_ERR_ARGUMENT;
+  const int64_t ncells = fc ? fc->nfacets : m.nelems;
+  const int64_t n = ncells * (int64_t)nq;
   if (n == 0) return 0;
   const fem_faithful::Rule rule{X, nullptr, nq};
+  const FemFacets F = fc ? *fc : FemFacets{};
   const unsigned grid = (unsigned)ceil_div(n, 128);
-  if (m.dim == 2)
-    fem_faithful::interpolate_kernel<2><<<grid, 128, 0, st>>>(m, b, rule, w, out);
-  else
-    fem_faithful::interpolate_kernel<3><<<grid, 128, 0, st>>>(m, b, rule, w, out);
+  using namespace fem_faithful;
+  if (m.dim == 2) {
+    if (fc) interpolate_kernel<2, true><<<grid, 128, 0, st>>>(m, b, F, rule, ncells, w, out, status);
+    else interpolate_kernel<2, false><<<grid, 128, 0, st>>>(m, b, F, rule, ncells, w, out, status);
+  } else {
+    if (fc) interpolate_kernel<3, true><<<grid, 128, 0, st>>>(m, b, F, rule, ncells, w, out, status);
+    else interpolate_kernel<3, false><<<grid, 128, 0, st>>>(m, b, F, rule, ncells, w, out, status);
+  }
   FEM_LAUNCH_CHECK("interpolate kernel");
   return 0;
 }

@@ -28,7 +28,7 @@ using Instr = FemInstr;
 // library, whose last bits may differ from numpy's.
 enum {
   OP_CONST = 0, OP_U, OP_V, OP_COEF, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_X, OP_H,
-  OP_SQRT, OP_EXP, OP_LOG, OP_SIN, OP_COS, OP_TAN, OP_TANH, OP_ARCTAN, OP_ABS, OP_POW
+  OP_SQRT, OP_EXP, OP_LOG, OP_SIN, OP_COS, OP_TAN, OP_TANH, OP_ARCTAN, OP_ABS, OP_POW, OP_N
 };
 
 // ----------------------------------------------------------- reference bases
@@ -260,6 +260,7 @@ FEM_HD double run(const Instr* ins, int n, int out, const double* qu, const doub
       case OP_ARCTAN: r = atan(R[I.a]); break;
       case OP_ABS: r = fabs(R[I.a]); break;
       case OP_POW: r = pow(R[I.a], R[I.b]); break;
+      case OP_N: r = qx[4 + I.a]; break;
       default: break;
     }
     R[k] = r;
@@ -310,8 +311,8 @@ FEM_HD ProgFlags prog_flags(const FemProgram& p) {
 // cell_basis.py:136-141; numpy evaluates **0.5 as sqrt).
 struct PointGeo {
   double inv[3][3];
-  double det;
-  double qx[4];
+  double det;     // detDF (cells) or detDG (facets): dx = |det| * W
+  double qx[7];   // x, y, z, h, n_x, n_y, n_z
 };
 
 struct CellGeo {  // the affine map of a simplex (unused for Hex1)
@@ -337,9 +338,91 @@ FEM_HD void point_geometry(const FemMesh& m, int64_t e, bool hex, const CellGeo&
       for (int j = 0; j < 3; ++j) g.inv[i][j] = c.inv[i][j];
     g.det = c.det;
   }
-  g.qx[0] = g.qx[1] = g.qx[2] = g.qx[3] = 0.0;
+  for (int k = 0; k < 7; ++k) g.qx[k] = 0.0;
   if (f.x) global_coords<D>(m, e, hex, c.A, c.x0, x, y, z, g.qx);
   if (f.h) g.qx[3] = D == 2 ? sqrt(fabs(g.det)) : pow(fabs(g.det), 1.0 / 3.0);
+}
+
+// ------------------------------------------------------------------ facets
+// Outward normals of the reference cell's facets (refdom.py:60-62, 107-110).
+FEM_HD void ref_normal(int D, int lf, double N[3]) {
+  N[0] = N[1] = N[2] = 0.0;
+  if (D == 2) {
+    const double T[3][2] = {{0.0, -1.0}, {1.0, 1.0}, {-1.0, 0.0}};
+    N[0] = T[lf][0];
+    N[1] = T[lf][1];
+  } else {
+    const double T[4][3] = {{0.0, 0.0, -1.0}, {0.0, -1.0, 0.0}, {-1.0, 0.0, 0.0},
+                            {1.0, 1.0, 1.0}};
+    for (int i = 0; i < 3; ++i) N[i] = T[lf][i];
+  }
+}
+
+// FacetBasis geometry at facet reference point Xf (facet_basis.py:84-106,
+// affine simplices): the facet map G (mapping_affine.py:154-181, 234-245)
+// x = B Xf + c with B's columns p[facet[j+1]] - p[facet[0]], its measure
+// detDG (:166-180, 247-253), the cell's reference point Y = invA (x - b)
+// (invF, :195-203), the normal invA_n^T N_ref / |.| of the cell f2t[0]
+// (:255-281) and h = |detDG|**(1/(dim-1)) (facet_basis.py:129-135; numpy
+// evaluates **1.0 as a copy and **0.5 as sqrt).  Returns false for a facet
+// whose cell indices are out of range.
+template <int D>
+FEM_HD bool facet_point(const FemMesh& m, const FemFacets& fc, int64_t f, const double* Xf,
+                        double Y[3], PointGeo& g) {
+  const int64_t nf = fc.nfacets;
+  const int64_t e = fc.tind[f], en = fc.tind_n[f];
+  const int lf = fc.lfacet_n[f];
+  if (e < 0 || e >= m.nelems || en < 0 || en >= m.nelems || lf < 0 || lf > D) return false;
+  double cc[3], B[3][2];
+  for (int i = 0; i < D; ++i) {
+    cc[i] = m.p[i * m.nverts + fc.fverts[f]];
+    for (int j = 0; j < D - 1; ++j)
+      B[i][j] = m.p[i * m.nverts + fc.fverts[(j + 1) * nf + f]] - m.p[i * m.nverts + fc.fverts[f]];
+  }
+  double x[3] = {0.0, 0.0, 0.0};
+  for (int i = 0; i < D; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < D - 1; ++j) s = s + B[i][j] * Xf[j];
+    x[i] = s + cc[i];
+  }
+  double detB;
+  if (D == 2) {
+    detB = sqrt(B[0][0] * B[0][0] + B[1][0] * B[1][0]);
+  } else {
+    const double a = B[1][0] * B[2][1] - B[2][0] * B[1][1];
+    const double b = (-B[0][0]) * B[2][1] + B[2][0] * B[0][1];
+    const double c = B[0][0] * B[1][1] - B[1][0] * B[0][1];
+    detB = sqrt((a * a + b * b) + c * c);
+  }
+  double inv[3][3], det, A[3][3], x0[3];
+  affine_inverse<D>(m, e, inv, det, A, x0);
+  double y[3];
+  for (int i = 0; i < D; ++i) y[i] = x[i] - x0[i];
+  for (int i = 0; i < 3; ++i) Y[i] = 0.0;
+  for (int i = 0; i < D; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < D; ++j) s = s + inv[i][j] * y[j];
+    Y[i] = s;
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) g.inv[i][j] = inv[i][j];
+  g.det = detB;
+  for (int k = 0; k < 7; ++k) g.qx[k] = 0.0;
+  for (int i = 0; i < D; ++i) g.qx[i] = x[i];
+  g.qx[3] = D == 2 ? detB : sqrt(detB);
+  double invn[3][3], detn, An[3][3], xn[3], N[3], n[3];
+  affine_inverse<D>(m, en, invn, detn, An, xn);
+  ref_normal(D, lf, N);
+  for (int j = 0; j < D; ++j) {
+    double s = 0.0;
+    for (int i = 0; i < D; ++i) s = s + invn[i][j] * N[i];
+    n[j] = s;
+  }
+  double len2 = n[0] * n[0];
+  for (int j = 1; j < D; ++j) len2 = len2 + n[j] * n[j];
+  const double rl = 1.0 / sqrt(len2);
+  for (int j = 0; j < D; ++j) g.qx[4 + j] = n[j] * rl;
+  return true;
 }
 
 // form(u_j, v_i, w) * dx at quadrature point q (bilinear_form.py:150-151,

@@ -44,14 +44,21 @@ def main():
     open(path, "w").write("\n".join(out))
     # the same rules for the Python side (Basis.X / Basis.W)
     py = ['"""Generated by csrc/gen_refquad.py from reference-recorded fixtures (do not',
-          'edit): scikit-fem\'s triangle / tetrahedron quadrature rules of orders 1-4',
-          'and its default hexahedral rule, bit-exact, as hexadecimal floats."""', "",
+          'edit): scikit-fem\'s triangle / tetrahedron quadrature rules of orders 1-4,',
+          'its line rules of orders 1-10 and its default hexahedral rule, bit-exact, as',
+          'hexadecimal floats."""', "",
           "RULES = {"]
     for key in sorted(k[:-2] for k in q if k.endswith("_X")):
         X, W = q[key + "_X"], q[key + "_W"]
         py.append("    %r: (%r,\n           %r)," % (
             key, [[float(v).hex() for v in row] for row in X], [float(v).hex() for v in W]))
     # the default Hex1 rule (intorder 6-7, 4x4x4 leggauss points)
+    # Gauss-Legendre line rules (FacetBasis quadrature of triangle meshes)
+    lines = dict(np.load(os.path.join(GOLD, "line_rules.npz")))
+    for key in sorted((k[:-2] for k in lines if k.endswith("_X")), key=lambda k: int(k[4:])):
+        X, W = lines[key + "_X"], lines[key + "_W"]
+        py.append("    %r: (%r,\n           %r)," % (
+            key, [[float(v).hex() for v in row] for row in X], [float(v).hex() for v in W]))
     Xh, Wh = hexg["X"], hexg["W"]
     py.append("    %r: (%r,\n           %r)," % (
         "hex6", [[float(v).hex() for v in row] for row in Xh], [float(v).hex() for v in Wh]))

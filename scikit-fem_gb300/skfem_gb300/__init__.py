@@ -10,7 +10,7 @@ from .element import (Element, ElementH1, ElementTriP1, ElementTriP2, ElementTet
                       ElementTetP2, ElementHex1, ElementVector)
 from .quadrature import get_quadrature  # noqa: F401
 from .dofs import Dofs  # noqa: F401
-from .basis import Basis, CellBasis  # noqa: F401
+from .basis import Basis, CellBasis, FacetBasis  # noqa: F401
 from .form import Form, BilinearForm, LinearForm, Functional, asm, ElementField  # noqa: F401
 from .field import DiscreteField  # noqa: F401
 from . import helpers, models  # noqa: F401

@@ -53,6 +53,12 @@ class FemInstr(ctypes.Structure):
                 ("pad_", ctypes.c_int32), ("imm", ctypes.c_double)]
 
 
+class FemFacets(ctypes.Structure):
+    _fields_ = [("nfacets", ctypes.c_int64), ("fverts", ctypes.c_void_p),
+                ("tind", ctypes.c_void_p), ("tind_n", ctypes.c_void_p),
+                ("lfacet_n", ctypes.c_void_p)]
+
+
 class FemProgram(ctypes.Structure):
     _fields_ = [("ninstr", ctypes.c_int32), ("out", ctypes.c_int32), ("ncoef", ctypes.c_int32),
                 ("nq", ctypes.c_int32), ("ins", ctypes.c_void_p), ("coef", ctypes.c_void_p * 16),
@@ -101,6 +107,10 @@ _SIGS = {
     "fem_csr_sum_checked": (ctypes.c_int, [_P, _P, _P, _P, _P]),
     "fem_interpolate": (ctypes.c_int, [_P, _P, ctypes.c_int32, _P, _P, _P, _P]),
     "fem_sum_pairwise": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P]),
+    "fem_facet_program_local_matrices": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
+    "fem_facet_program_local_vectors": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
+    "fem_facet_program_elemental": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
+    "fem_facet_interpolate": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P, _P, _P, _P]),
     "fem_set_tuning": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "fem_assemble_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
 }

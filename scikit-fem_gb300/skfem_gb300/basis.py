@@ -17,7 +17,7 @@ from .field import DiscreteField
 from .mesh import as_mesh
 from .quadrature import get_quadrature
 
-__all__ = ["CellBasis", "Basis"]
+__all__ = ["CellBasis", "Basis", "FacetBasis"]
 
 MAX_POINTS = 128    # quadrature points per cell of the generic kernels
 
@@ -89,6 +89,15 @@ class CellBasis:
                                   self.Nbfun, 0, self.N, self.ed_dev.data_ptr())
         self.X_dev = torch.from_numpy(np.ascontiguousarray(self.X, dtype=np.float64)).to(dev)
         self.W_dev = torch.from_numpy(np.ascontiguousarray(self.W, dtype=np.float64)).to(dev)
+        # the (mesh, basis) pair the CSR pattern is built over
+        self.c_mesh_pat, self.c_basis_pat = self.c_mesh, self.c_basis
+
+    def _run_program(self, kind, prog, out, status):
+        """The generic kernel of a traced program over this basis's cells."""
+        fn = {"bilinear": "fem_program_local_matrices", "linear": "fem_program_local_vectors",
+              "functional": "fem_program_elemental"}[kind]
+        N.check(getattr(N.lib(), fn)(N.byref(self.c_mesh), N.byref(self.c_basis), N.byref(prog),
+                                     N.ptr(out), N.ptr(status), N.stream_ptr()))
 
     def update_coordinates(self, p):
         """Replace the node coordinates (same topology) -- used by shape
@@ -161,6 +170,119 @@ class CellBasis:
 
     def __repr__(self):
         return "CellBasis(%r, %r) on %s: %d DOFs" % (self.mesh, self.elem, self.device, self.N)
+
+
+BOUNDARY_REFDOM = {"tri": "line", "tet": "tri"}
+
+
+class FacetBasis(CellBasis):
+    """FacetBasis (skfem/assembly/basis/facet_basis.py:21-110) on affine
+    simplex meshes: integrates over a set of facets -- by default the
+    boundary -- with the basis of the cell on ``side`` (f2t[side]) and the
+    outward normal of the cell f2t[0].  Forms see ``w.x``, ``w.h`` and
+    ``w.n``; every form runs on the generic per-point kernels, over facets
+    instead of cells."""
+
+    def __init__(self, mesh, elem, mapping=None, intorder=None, quadrature=None, facets=None,
+                 dofs=None, side=0, disable_doflocs=False, device=None):
+        mesh = as_mesh(mesh)
+        if mesh.refdom != elem.refdom:
+            raise ValueError("Incompatible Mesh and Element.")
+        if mapping is not None:
+            raise NotImplementedError("custom mappings are not supported")
+        if mesh.refdom not in BOUNDARY_REFDOM:
+            raise NotImplementedError("FacetBasis on %s meshes is not implemented"
+                                      % type(mesh).__name__)
+        self.mesh, self.elem = mesh, elem
+        self.dofs = Dofs(mesh, elem) if dofs is None else dofs
+        self.Nbfun = self.dofs.element_dofs.shape[0]
+        self.find = np.asarray(mesh.normalize_facets(facets), dtype=np.int32)
+        f2t = mesh.f2t
+        self.tind = f2t[side, self.find]
+        self.tind_normals = f2t[0, self.find]
+        if np.any(self.tind < 0):
+            raise ValueError("side=%d has no cell on %d of the facets (boundary facets have "
+                             "one side)" % (side, int(np.sum(self.tind < 0))))
+        self.nelems = len(self.find)
+        self.intorder = intorder if intorder is not None else 2 * elem.maxdeg
+        brefdom = BOUNDARY_REFDOM[mesh.refdom]
+        if quadrature is not None:
+            self.X = np.ascontiguousarray(quadrature[0], dtype=np.float64)
+            self.W = np.ascontiguousarray(quadrature[1], dtype=np.float64)
+        else:
+            self.X, self.W = get_quadrature(brefdom, self.intorder)
+        if self.X.shape[0] != mesh.p.shape[0] - 1 or self.X.shape[1] > MAX_POINTS:
+            raise ValueError("facet quadrature must be (dim-1, nqp) with nqp <= %d" % MAX_POINTS)
+        self._fast_ok = False
+        self.device = N.require_cuda(device)
+        self._patterns = {}
+        self._upload_facets()
+
+    def _upload_facets(self):
+        dev = self.device
+        m = self.mesh
+        dim = m.p.shape[0]
+        t2f = m.t2f
+        lf = np.argmax(t2f[:, self.tind_normals] == self.find[None, :], axis=0).astype(np.int32)
+
+        def up(a, dtype=np.int32):
+            return torch.from_numpy(np.ascontiguousarray(a, dtype=dtype)).to(dev)
+
+        self.p_dev = up(m.p, np.float64)
+        self.t_dev = up(m.t)
+        self.ed_full_dev = up(self.dofs.element_dofs)
+        self.fv_dev = up(m.facets[:, self.find])
+        self.tind_dev = up(self.tind)
+        self.tindn_dev = up(self.tind_normals)
+        self.lf_dev = up(lf)
+        self.ed_dev = up(self.element_dofs)
+        fam = N.FAMILY[self.elem.family]
+        self.c_mesh = N.FemMesh(dim, m.t.shape[0], m.p.shape[1], m.t.shape[1],
+                                self.p_dev.data_ptr(), self.t_dev.data_ptr())
+        self.c_basis = N.FemBasis(fam, int(self.elem.vector), self.Nbfun, 0, self.N,
+                                  self.ed_full_dev.data_ptr())
+        self.c_facets = N.FemFacets(self.nelems, self.fv_dev.data_ptr(), self.tind_dev.data_ptr(),
+                                    self.tindn_dev.data_ptr(), self.lf_dev.data_ptr())
+        # the pattern is built over the facets with their cells' DOFs
+        self.c_mesh_pat = N.FemMesh(dim, m.t.shape[0], m.p.shape[1], self.nelems,
+                                    self.p_dev.data_ptr(), self.t_dev.data_ptr())
+        self.c_basis_pat = N.FemBasis(fam, int(self.elem.vector), self.Nbfun, 0, self.N,
+                                      self.ed_dev.data_ptr())
+        self.X_dev = up(self.X, np.float64)
+        self.W_dev = up(self.W, np.float64)
+
+    def update_coordinates(self, p):
+        raise NotImplementedError("FacetBasis.update_coordinates is not supported")
+
+    @property
+    def element_dofs(self):
+        """The DOFs of each facet's cell (abstract_basis.py:110-117 with tind)."""
+        return self.dofs.element_dofs[:, self.tind]
+
+    def _run_program(self, kind, prog, out, status):
+        fn = {"bilinear": "fem_facet_program_local_matrices",
+              "linear": "fem_facet_program_local_vectors",
+              "functional": "fem_facet_program_elemental"}[kind]
+        N.check(getattr(N.lib(), fn)(N.byref(self.c_mesh), N.byref(self.c_basis),
+                                     N.byref(self.c_facets), N.byref(prog), N.ptr(out),
+                                     N.ptr(status), N.stream_ptr()))
+
+    def interpolate_torch(self, w):
+        w = torch.as_tensor(w, dtype=torch.float64).to(self.device).contiguous()
+        if w.dim() != 1 or w.shape[0] != self.N:
+            raise ValueError("Input array has wrong size.")
+        dim = self.mesh.p.shape[0]
+        nquant = dim + dim * dim if self.elem.vector else 1 + dim
+        nq = self.X.shape[1]
+        out = torch.empty((nquant, self.nelems, nq), dtype=torch.float64, device=self.device)
+        N.check(N.lib().fem_facet_interpolate(N.byref(self.c_mesh), N.byref(self.c_basis),
+                                              N.byref(self.c_facets), nq, N.ptr(self.X_dev),
+                                              N.ptr(w), N.ptr(out), N.stream_ptr()))
+        return out
+
+    def __repr__(self):
+        return "FacetBasis(%r, %r) on %s: %d facets, %d DOFs" % (
+            self.mesh, self.elem, self.device, self.nelems, self.N)
 
 
 Basis = CellBasis

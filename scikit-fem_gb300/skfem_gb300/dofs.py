@@ -25,7 +25,7 @@ class Dofs:
                 rows.append(base + c)
         offset += nd * nv
         if element.dim == 3 and element.edge_dofs > 0:
-            edges, t2e = topo._build("edges", TET_EDGES)
+            edges, t2e = topo._build("edges", TET_EDGES)[:2]
             ed = element.edge_dofs
             for itr in range(t2e.shape[0]):
                 base = ed * t2e[itr].astype(np.int64) + offset
@@ -33,7 +33,7 @@ class Dofs:
                     rows.append(base + c)
             offset += ed * edges.shape[1]
         if element.dim == 2 and element.facet_dofs > 0:
-            facets, t2f = topo._build("facets", TRI_FACETS)
+            facets, t2f = topo._build("facets", TRI_FACETS)[:2]
             fd = element.facet_dofs
             for itr in range(t2f.shape[0]):
                 base = fd * t2f[itr].astype(np.int64) + offset

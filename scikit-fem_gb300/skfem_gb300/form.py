@@ -210,7 +210,8 @@ class Form:
 
     # tracing is cached per (element kind, field names, numbers)
     def _key(self, basis, coeffs, kind):
-        return (kind, basis.elem.family, basis.elem.vector, basis.mesh.p.shape[0],
+        return (kind, type(basis).__name__, basis.elem.family, basis.elem.vector,
+                basis.mesh.p.shape[0],
                 tuple(sorted((k, s.kind, s.ncomp, s.grad) for k, s in coeffs.specs().items())),
                 tuple(sorted(coeffs.numbers.items(), key=repr)))
 
@@ -246,7 +247,8 @@ class Form:
         if g is None:
             ins, out, names = trace_tape(self.form, basis.elem, basis.mesh.p.shape[0],
                                          coeffs.specs(), coeffs.numbers, kind=kind,
-                                         defaults=True)
+                                         defaults="facet" if hasattr(basis, "c_facets")
+                                         else "cell")
             g = _GenericProgram(ins, out, names)
             self._traces[key] = g
         return g, key
@@ -317,10 +319,11 @@ class _PatternEntry:
         lib = N.lib()
         h = ctypes.c_void_p()
         if local is not None:
-            N.check(lib.fem_pattern_build_local(N.byref(basis.c_mesh), N.byref(basis.c_basis),
-                                                N.ptr(local), ctypes.byref(h), stream))
+            N.check(lib.fem_pattern_build_local(N.byref(basis.c_mesh_pat),
+                                                N.byref(basis.c_basis_pat), N.ptr(local),
+                                                ctypes.byref(h), stream))
         else:
-            N.check(lib.fem_pattern_build(N.byref(basis.c_mesh), N.byref(basis.c_basis),
+            N.check(lib.fem_pattern_build(N.byref(basis.c_mesh_pat), N.byref(basis.c_basis_pat),
                                           N.byref(c_form) if c_form is not None else None,
                                           N.byref(program) if program is not None else None,
                                           ctypes.byref(h), stream))
@@ -346,6 +349,8 @@ class _PatternEntry:
 def _raise_status(st):
     if st & (1 << N.FEM_ERR_ZERO_JACOBIAN):
         raise N.ZeroJacobianError("Zero Jacobian determinant")
+    if st & (1 << N.FEM_ERR_ARGUMENT):
+        raise ValueError("a facet's cell index is out of range")
 
 
 def _host_csr(entry, vals, n):
@@ -417,9 +422,7 @@ class BilinearForm(Form):
         local = torch.empty(max(1, basis.nelems * nb * nb), dtype=torch.float64,
                             device=basis.device)
         status = torch.zeros(1, dtype=torch.int32, device=basis.device)
-        N.check(N.lib().fem_program_local_matrices(N.byref(basis.c_mesh), N.byref(basis.c_basis),
-                                                   N.byref(prog), N.ptr(local), N.ptr(status),
-                                                   N.stream_ptr()))
+        basis._run_program("bilinear", prog, local, status)
         return local, status, key
 
     def _generic_assemble(self, basis, coeffs, check):
@@ -524,9 +527,7 @@ class LinearForm(Form):
         local = torch.empty(max(1, basis.nelems * basis.Nbfun), dtype=torch.float64,
                             device=basis.device)
         status = torch.zeros(1, dtype=torch.int32, device=basis.device)
-        N.check(N.lib().fem_program_local_vectors(N.byref(basis.c_mesh), N.byref(basis.c_basis),
-                                                  N.byref(prog), N.ptr(local), N.ptr(status),
-                                                  N.stream_ptr()))
+        basis._run_program("linear", prog, local, status)
         return local, status
 
     def _device_assemble(self, basis, vbasis=None, **kwargs):
@@ -571,9 +572,7 @@ class Functional(Form):
         prog = g.struct(basis, coeffs)
         out = torch.empty(max(1, basis.nelems), dtype=torch.float64, device=basis.device)
         status = torch.zeros(1, dtype=torch.int32, device=basis.device)
-        N.check(N.lib().fem_program_elemental(N.byref(basis.c_mesh), N.byref(basis.c_basis),
-                                              N.byref(prog), N.ptr(out), N.ptr(status),
-                                              N.stream_ptr()))
+        basis._run_program("functional", prog, out, status)
         return out[:basis.nelems], status
 
     def elemental_torch(self, basis, **kwargs):

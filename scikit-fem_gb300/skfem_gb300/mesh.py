@@ -15,9 +15,13 @@ import numpy as np
 __all__ = ["Mesh", "MeshTri", "MeshTri1", "MeshTet", "MeshTet1", "MeshHex", "MeshHex1",
            "as_mesh"]
 
-# local vertex pairs of the entities, in the reference's order
+# local vertices of the entities, in the reference's order
 TRI_FACETS = np.array([[0, 1], [1, 2], [0, 2]])                           # refdom.py:60-62
 TET_EDGES = np.array([[0, 1], [1, 2], [0, 2], [0, 3], [1, 3], [2, 3]])    # refdom.py:101-106
+TET_FACETS = np.array([[0, 1, 2], [0, 1, 3], [0, 2, 3], [1, 2, 3]])       # refdom.py:96-99
+# outward normals of the reference cell's facets (refdom.py:60-62, 107-110)
+TRI_NORMALS = np.array([[0., -1.], [1., 1.], [-1., 0.]])
+TET_NORMALS = np.array([[0., 0., -1.], [0., -1., 0.], [-1., 0., 0.], [1., 1., 1.]])
 
 
 class Mesh:
@@ -82,20 +86,76 @@ class Mesh:
         raise NotImplementedError
 
     # ------------------------------------------------------------ entities
-    def _build(self, name, local_pairs):
+    def _build(self, name, local):
+        """Mesh.build_entities (mesh.py:1065-1082) with sort=True: every
+        cell's local vertex tuples, sorted per tuple, made unique in
+        lexicographic order; plus the inverse map (cell -> entity) and, as
+        Mesh.build_inverse (mesh.py:1084-1100) does, the first and last cell
+        that contain each entity (-1 when only one does)."""
         if name not in self._entities:
             t = self.t
-            a = t[local_pairs[:, 0]]
-            b = t[local_pairs[:, 1]]
-            lo = np.minimum(a, b).astype(np.int64).ravel()
-            hi = np.maximum(a, b).astype(np.int64).ravel()
-            # lexicographic (lo, hi) order == order of the scalar key lo*n + hi
-            n = max(self.nvertices, 1)
-            key = lo * n + hi
-            uk, inv = np.unique(key, return_inverse=True)
-            ent = np.vstack((uk // n, uk % n)).astype(np.int32)
-            self._entities[name] = (ent, inv.reshape(len(local_pairs), t.shape[1]).astype(np.int32))
+            ne = t.shape[1]
+            cols = np.sort(np.hstack([t[list(ix)] for ix in local]), axis=0)
+            M = cols.shape[1]
+            order = np.lexsort(cols[::-1])          # stable: positions ascend in a group
+            sc = cols[:, order]
+            new = np.ones(M, dtype=bool)
+            if M > 1:
+                new[1:] = np.any(sc[:, 1:] != sc[:, :-1], axis=0)
+            ids = np.cumsum(new) - 1
+            ent = np.ascontiguousarray(sc[:, new]).astype(np.int32)
+            inv = np.empty(M, dtype=np.int64)
+            inv[order] = ids
+            starts = np.nonzero(new)[0]
+            ends = np.r_[starts[1:], M] - 1
+            cell = np.tile(np.arange(ne, dtype=np.int32), len(local))
+            inverse = np.vstack((cell[order[starts]], cell[order[ends]])).astype(np.int32)
+            inverse[1, inverse[0] == inverse[1]] = -1
+            self._entities[name] = (ent, inv.reshape(len(local), ne).astype(np.int32), inverse)
         return self._entities[name]
+
+    # facets (mesh.py:98-113, 197-199, 426-456, 1291-1329)
+    facet_tuples = None
+    normals_ref = None
+
+    @property
+    def facets(self):
+        if self.facet_tuples is None:
+            raise NotImplementedError("facets of %s are not supported" % type(self).__name__)
+        return self._build("facets", self.facet_tuples)[0]
+
+    @property
+    def t2f(self):
+        return self._build("facets", self.facet_tuples)[1]
+
+    @property
+    def f2t(self):
+        return self._build("facets", self.facet_tuples)[2]
+
+    def boundary_facets(self):
+        return np.nonzero(self.f2t[1] == -1)[0].astype(np.int32)
+
+    def facets_satisfying(self, test, boundaries_only=False):
+        midp = self.p[:, self.facets].mean(axis=1)
+        facets = np.nonzero(test(midp))[0].astype(np.int32)
+        if boundaries_only:
+            facets = np.intersect1d(facets, self.boundary_facets())
+        return facets
+
+    def normalize_facets(self, facets):
+        if isinstance(facets, (int, np.integer)):
+            return np.array([facets])
+        if isinstance(facets, np.ndarray):
+            return facets
+        if facets is None:
+            return self.boundary_facets()
+        if isinstance(facets, (tuple, list, set)):
+            return np.unique(np.concatenate([self.normalize_facets(f) for f in facets]))
+        if callable(facets):
+            return self.facets_satisfying(facets)
+        if isinstance(facets, str):
+            raise ValueError("Boundary '{}' not found.".format(facets))
+        raise NotImplementedError
 
     def __repr__(self):
         return "%s(%d vertices, %d elements)" % (type(self).__name__, self.p.shape[1],
@@ -116,13 +176,8 @@ class MeshTri1(Mesh):
             t = np.array([[0, 1, 2], [1, 3, 2]]).T
         super().__init__(doflocs, t, **kwargs)
 
-    @property
-    def facets(self):
-        return self._build("facets", TRI_FACETS)[0]
-
-    @property
-    def t2f(self):
-        return self._build("facets", TRI_FACETS)[1]
+    facet_tuples = TRI_FACETS
+    normals_ref = TRI_NORMALS
 
     @classmethod
     def init_tensor(cls, x, y):
@@ -155,6 +210,9 @@ class MeshTet1(Mesh):
             t = np.array([[0, 1, 2, 3], [3, 5, 1, 7], [2, 3, 6, 7], [2, 3, 1, 7],
                           [1, 2, 4, 7]]).T
         super().__init__(doflocs, t, **kwargs)
+
+    facet_tuples = TET_FACETS
+    normals_ref = TET_NORMALS
 
     @property
     def edges(self):

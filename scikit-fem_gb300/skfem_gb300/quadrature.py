@@ -84,6 +84,15 @@ def get_quadrature(refdom, norder):
         t = _table(refdom, norder)
         if t is not None:
             return t
+    if refdom == "line":
+        from ._refquad import RULES
+        key = "line%d" % max(norder, 1)
+        if key in RULES:
+            X, W = RULES[key]
+            return (np.array([[float.fromhex(v) for v in row] for row in X]),
+                    np.array([float.fromhex(v) for v in W]))
+        x, w = gauss_line(norder)
+        return x[None, :], w
     if refdom == "hex" and norder in (6, 7):
         # the reference's default Hex1 rule as recorded (leggauss's last bits
         # depend on the platform's eigenvalue solver)

@@ -328,11 +328,11 @@ def linear_channels(sym, elem, dim):
 
 (OP_CONST, OP_U, OP_V, OP_COEF, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_X, OP_H,
  OP_SQRT, OP_EXP, OP_LOG, OP_SIN, OP_COS, OP_TAN, OP_TANH, OP_ARCTAN, OP_ABS,
- OP_POW) = range(21)
+ OP_POW, OP_N) = range(22)
 
 # ops that are correctly rounded on both sides (the rest use libm)
 EXACT_OPS = {OP_CONST, OP_U, OP_V, OP_COEF, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_NEG, OP_X, OP_H,
-             OP_SQRT, OP_ABS}
+             OP_SQRT, OP_ABS, OP_N}
 
 
 class Tape:
@@ -509,12 +509,16 @@ class TapeParams(dict):
         for k, v in numbers_.items():
             self[k] = v
         if defaults:
-            # CellBasis.default_parameters (cell_basis.py:124-141)
+            # CellBasis.default_parameters (cell_basis.py:124-141);
+            # FacetBasis adds the unit outward normal (facet_basis.py:112-118)
             if "x" not in self:
                 self["x"] = SymField(np.array([tape.load(OP_X, i) for i in range(dim)],
                                               dtype=object))
             if "h" not in self:
                 self["h"] = tape.load(OP_H, 0)
+            if defaults == "facet" and "n" not in self:
+                self["n"] = SymField(np.array([tape.load(OP_N, i) for i in range(dim)],
+                                              dtype=object))
 
     def _slot(self, key):
         if key not in self.slots:
@@ -591,7 +595,8 @@ def _compact(ins, out, slots):
 def trace_tape(form, elem, dim, fields, numbers_, kind="bilinear", defaults=False):
     """Record the exact-order program of a form; returns (instructions,
     output index, coefficient slot keys).  kind: 'bilinear' (form(u, v, w)),
-    'linear' (form(v, w)) or 'functional' (form(w)).  fields: names of
+    'linear' (form(v, w)) or 'functional' (form(w)).  defaults: True / 'cell'
+    adds w.x and w.h, 'facet' also w.n.  fields: names of
     per-element coefficients, or {name: FieldSpec}; slot keys are the names
     ('elem'/'qp') or (name, quantity) pairs ('field')."""
     tape = Tape()

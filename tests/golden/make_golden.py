@@ -199,6 +199,7 @@ def main():
          X=ib.X, W=ib.W, b=unit_load.assemble(ib), **csr_arrays(laplace.assemble(ib)))
 
     generic_cases()
+    facet_cases()
 
     # quadrature rules the configs use, exactly as the reference tabulates them
     from skfem.quadrature import get_quadrature_tet, get_quadrature_tri
@@ -330,8 +331,95 @@ def generic_cases():
          **{k + "_conv": v for k, v in csr_arrays(vec_conv.assemble(ib, d=d)).items()})
 
 
+def facet_cases():
+    """FacetBasis (boundary, interior with side 0/1, callable subsets) on
+    affine simplices: boundary mass, Robin / normal-derivative terms,
+    Neumann loads with w.n / w.x / w.h, Functional, interpolate; plus the
+    reference's line rules (FacetBasis quadrature of triangle meshes)."""
+    from skfem import FacetBasis
+    from skfem.quadrature import get_quadrature_line
+    rng = np.random.default_rng(20261205)
+
+    @BilinearForm
+    def robin(u, v, w):
+        return (1.0 + w.x[0]) * u * v + dot(w.n, grad(u)) * v
+
+    @LinearForm
+    def neumann(v, w):
+        return dot(w.n, w.x) * v + w.h * v
+
+    @Functional
+    def length(w):
+        return 1.0 + 0.0 * w.x[0]
+
+    @Functional
+    def s_energy(w):
+        return w['s'] ** 2 + dot(w.n, grad(w['s']))
+
+    def facet_arrays(fb, s, prefix=""):
+        sf = fb.interpolate(s)
+        out = dict(find=fb.find, tind=fb.tind, X=fb.X, W=fb.W,
+                   x=np.asarray(fb.global_coordinates()), h=np.asarray(fb.mesh_parameters()),
+                   n=np.asarray(fb.normals), s_value=np.asarray(sf), s_grad=sf.grad,
+                   b_neumann=neumann.assemble(fb), e_length=length.elemental(fb),
+                   f_length=np.float64(length.assemble(fb)),
+                   e_energy=s_energy.elemental(fb, s=s),
+                   f_energy=np.float64(s_energy.assemble(fb, s=s)))
+        out.update({k + "_mass": v for k, v in csr_arrays(mass.assemble(fb)).items()})
+        out.update({k + "_robin": v for k, v in csr_arrays(robin.assemble(fb)).items()})
+        return {prefix + k: v for k, v in out.items()}
+
+    for name, mesh_cls, elem, shape in (
+            ("tri_p1_facet", MeshTri, ElementTriP1(), (7, 6)),
+            ("tri_p2_facet", MeshTri, ElementTriP2(), (5, 5)),
+            ("tet_p1_facet", MeshTet, ElementTetP1(), (4, 4, 4)),
+            ("tet_p2_facet", MeshTet, ElementTetP2(), (3, 3, 3))):
+        m = mesh_cls.init_tensor(*[np.linspace(0, 1, k) for k in shape])
+        p = m.p.copy()
+        inner = jitter(m, rng, 0.2)
+        hh = 1.0 / (max(shape) - 1)
+        p[:, inner] += rng.uniform(-0.2 * hh, 0.2 * hh, size=(p.shape[0], int(inner.sum())))
+        m = mesh_cls(p, m.t)
+        s = rng.standard_normal(Basis(m, elem).N)
+        arrs = dict(p=m.p, t=m.t, facets=m.facets, f2t=m.f2t, t2f=m.t2f, s=s)
+        arrs.update(facet_arrays(FacetBasis(m, elem), s))
+        interior = np.nonzero(m.f2t[1] >= 0)[0].astype(np.int32)
+        arrs.update(facet_arrays(FacetBasis(m, elem, facets=interior, side=0), s, "in0_"))
+        arrs.update(facet_arrays(FacetBasis(m, elem, facets=interior, side=1), s, "in1_"))
+        arrs.update(facet_arrays(FacetBasis(m, elem, facets=lambda x: x[1] < 0.3), s, "cb_"))
+        save(name, **arrs)
+
+    # vector TetP2: boundary mass and a traction load
+    m = MeshTet.init_tensor(*(np.linspace(0, 1, 3),) * 3)
+    p = m.p.copy()
+    inner = jitter(m, rng, 0.2)
+    p[:, inner] += rng.uniform(-0.1, 0.1, size=(3, int(inner.sum())))
+    m = MeshTet(p, m.t)
+    fb = FacetBasis(m, ElementVector(ElementTetP2()))
+
+    @BilinearForm
+    def vmass(u, v, w):
+        return dot(u, v)
+
+    @LinearForm
+    def traction(v, w):
+        return (1.0 + w.x[2]) * dot(w.n, v)
+
+    save("tet_p2_vec_facet", p=m.p, t=m.t, X=fb.X, W=fb.W, find=fb.find,
+         b_traction=traction.assemble(fb),
+         **{k + "_vmass": v for k, v in csr_arrays(vmass.assemble(fb)).items()})
+
+    rules = {}
+    for o in range(1, 11):
+        X, W = get_quadrature_line(o)
+        rules["line%d_X" % o], rules["line%d_W" % o] = X, W
+    save("line_rules", **rules)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["--generic"]:
         generic_cases()
+    elif sys.argv[1:] == ["--facet"]:
+        facet_cases()
     else:
         main()

@@ -107,3 +107,91 @@ extern "C" int faithful_points_host(const FemMesh* m, const FemBasis* b, int nq,
   }
   return 0;
 }
+
+// FacetBasis versions: the facet-point geometry (facet_point) and the same
+// per-entry replay; prog->qX is the facet rule (dim-1, nq).
+template <int D>
+static double facet_entry(const FemMesh& m, const FemBasis& b, const FemFacets& fc,
+                          const FemProgram& prog, int64_t f, int i, int j, double* R) {
+  using namespace fem_faithful;
+  double vals[kMaxPoints];
+  const int nq = prog.nq;
+  for (int q = 0; q < nq; ++q) {
+    double Xf[2] = {prog.qX[q], D == 3 ? prog.qX[nq + q] : 0.0};
+    double Y[3];
+    PointGeo g;
+    facet_point<D>(m, fc, f, Xf, Y, g);
+    vals[q] = point_value<D>(b, prog, f, q, i, j, Y[0], Y[1], Y[2], g, prog.qW[q], R);
+  }
+  return np_pairwise_sum(vals, nq);
+}
+
+extern "C" int faithful_facet_program_host(int mode, const FemMesh* m, const FemBasis* b,
+                                           const FemFacets* fc, const FemProgram* prog,
+                                           double* out) {
+  using namespace fem_faithful;
+  if (prog->ninstr > kMaxProgram || prog->nq > kMaxPoints) return 1;
+  const int nb = b->nbfun;
+  const int L = mode == 0 ? nb * nb : (mode == 1 ? nb : 1);
+  double R[kMaxProgram];
+  for (int64_t f = 0; f < fc->nfacets; ++f)
+    for (int r = 0; r < L; ++r) {
+      const int i = mode == 0 ? r / nb : (mode == 1 ? r : 0);
+      const int j = mode == 0 ? r % nb : 0;
+      out[f * L + r] = m->dim == 2 ? facet_entry<2>(*m, *b, *fc, *prog, f, i, j, R)
+                                   : facet_entry<3>(*m, *b, *fc, *prog, f, i, j, R);
+    }
+  return 0;
+}
+
+// x (dim), h, n (dim) at every facet point: out[(k*nfacets + f)*nq + q], k < 7
+extern "C" int faithful_facet_points_host(const FemMesh* m, const FemFacets* fc, int nq,
+                                          const double* X, double* out) {
+  using namespace fem_faithful;
+  for (int64_t f = 0; f < fc->nfacets; ++f)
+    for (int q = 0; q < nq; ++q) {
+      double Xf[2] = {X[q], m->dim == 3 ? X[nq + q] : 0.0};
+      double Y[3];
+      PointGeo g;
+      const bool ok = m->dim == 2 ? facet_point<2>(*m, *fc, f, Xf, Y, g)
+                                  : facet_point<3>(*m, *fc, f, Xf, Y, g);
+      if (!ok) return 1;
+      for (int k = 0; k < 7; ++k) out[((int64_t)k * fc->nfacets + f) * nq + q] = g.qx[k];
+    }
+  return 0;
+}
+
+template <int D>
+static void facet_interp_host(const FemMesh& m, const FemBasis& b, const FemFacets& fc, int nq,
+                              const double* X, const double* w, double* out) {
+  using namespace fem_faithful;
+  const bool vec = b.vector != 0;
+  const int nquant = vec ? D + D * D : 1 + D;
+  for (int64_t f = 0; f < fc.nfacets; ++f) {
+    const int64_t ec = fc.tind[f];
+    for (int q = 0; q < nq; ++q) {
+      double Xf[2] = {X[q], D == 3 ? X[nq + q] : 0.0};
+      double Y[3];
+      PointGeo g;
+      facet_point<D>(m, fc, f, Xf, Y, g);
+      double acc[D + D * D], qq[D + D * D];
+      const double w0 = w[b.element_dofs[ec]];
+      quantities<D>(b.family, vec, 0, Y[0], Y[1], Y[2], g.inv, qq);
+      for (int k = 0; k < nquant; ++k) acc[k] = 0.0 * (w0 * qq[k]);
+      for (int i = 0; i < b.nbfun; ++i) {
+        const double wi = w[b.element_dofs[(int64_t)i * m.nelems + ec]];
+        quantities<D>(b.family, vec, i, Y[0], Y[1], Y[2], g.inv, qq);
+        for (int k = 0; k < nquant; ++k) acc[k] = acc[k] + wi * qq[k];
+      }
+      for (int k = 0; k < nquant; ++k) out[((int64_t)k * fc.nfacets + f) * nq + q] = acc[k];
+    }
+  }
+}
+
+extern "C" int faithful_facet_interpolate_host(const FemMesh* m, const FemBasis* b,
+                                               const FemFacets* fc, int nq, const double* X,
+                                               const double* w, double* out) {
+  if (m->dim == 2) facet_interp_host<2>(*m, *b, *fc, nq, X, w, out);
+  else facet_interp_host<3>(*m, *b, *fc, nq, X, w, out);
+  return 0;
+}
