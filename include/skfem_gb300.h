@@ -46,7 +46,9 @@ enum FemStatus {
   FEM_ERR_CUDA = 3,          /* CUDA runtime error */
   FEM_ERR_ZERO_JACOBIAN = 4, /* isoparametric detDF == 0 (mapping_isoparametric.py:195-196) */
   FEM_ERR_STALE_PATTERN = 5, /* exact-zero structure of the local matrices changed: rebuild */
-  FEM_ERR_CAPACITY = 6       /* a CSR row exceeds the per-row working-set limit */
+  FEM_ERR_CAPACITY = 6,      /* a CSR row exceeds the per-row working-set limit */
+  FEM_ERR_VARYING = 7        /* a strided coefficient is not constant over a cell's
+                                points (status word only): use the generic kernels */
 };
 
 /* Element families (the reference classes they stand for). */
@@ -82,6 +84,10 @@ typedef struct FemBasis {
 typedef struct FemCoef {
   double scale;
   const double* field;
+  int64_t stride;   /* 0 or 1: field[e]; > 1: field[e * stride], a (nelems, stride)
+                       per-point array whose rows the local kernels of
+                       fem_assemble check are constant (FEM_ERR_VARYING in the
+                       status word otherwise) */
 } FemCoef;
 
 /*
@@ -229,6 +235,20 @@ int fem_assemble_noalloc(const FemMesh* mesh, const FemBasis* basis, const FemBi
                          fem_stream_t stream);
 
 /* Segmented sum only (local matrices already in `local`). */
+/*
+ * fem_assemble with the result streamed to the host: the local kernel, then
+ * the segmented sum in nchunks row ranges of about equal nnz, each range's
+ * values copied into host_values (pinned host memory, nnz doubles) on
+ * copy_stream as soon as it is summed, overlapping the copy with the next
+ * range's sum.  csr_values is the device buffer the sum writes first.  The
+ * caller synchronises copy_stream (and reads status) before using
+ * host_values.
+ */
+int fem_assemble_to_host(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
+                         const FemPattern* pat, double* staging, double* csr_values,
+                         double* host_values, int32_t* status, int32_t nchunks,
+                         fem_stream_t stream, fem_stream_t copy_stream);
+
 int fem_csr_sum(const FemPattern* pat, const double* local, double* csr_values, int32_t* status,
                 fem_stream_t stream);
 

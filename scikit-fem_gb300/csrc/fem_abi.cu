@@ -5,6 +5,9 @@
 
 #include "fem_common.cuh"
 
+#include <algorithm>
+#include <vector>
+
 namespace fem_fast {
 int local_matrices(const FemMesh&, const FemBasis&, const FemBilinear&, double*, int32_t*,
                    cudaStream_t);
@@ -23,7 +26,6 @@ int build_incidence(const int32_t* dofs, int64_t nelems, int nb, int64_t nrows, 
                     cudaStream_t st);
 int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, Pattern* P,
               cudaStream_t st);
-int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st);
 int vector_sum(const Pattern& P, const double* local, double* b, cudaStream_t st);
 void free_pattern(Pattern* P);
 int zero_check(const Pattern& P, const double* local, int32_t* status, cudaStream_t st);
@@ -104,6 +106,7 @@ Tuning tuning_for(int family) {
 struct FemPattern {
   fem::Pattern P;
   uint8_t* coef_bits = nullptr;  // nelems, or null when built without a form
+  std::vector<int32_t> host_indptr;  // host copy of indptr (row ranges of fem_assemble_to_host)
   int family = 0, vector = 0;
 };
 
@@ -126,6 +129,14 @@ int new_pattern_handle(Pattern* P, FemPattern** out) {
   return 0;
 }
 }  // namespace fem
+
+static int host_row_pointer(FemPattern* H, cudaStream_t st) {
+  H->host_indptr.resize(H->P.nrows + 1);
+  FEM_TRY_CUDA(cudaMemcpyAsync(H->host_indptr.data(), H->P.indptr,
+                               (H->P.nrows + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  FEM_TRY_CUDA(cudaStreamSynchronize(st));
+  return 0;
+}
 
 static int validate(const FemMesh* m, const FemBasis* b) {
   if (!m || !b) {
@@ -281,6 +292,7 @@ int fem_pattern_build(const FemMesh* mesh, const FemBasis* basis, const FemBilin
     if (!rc && program) rc = fem::faithful_mask(*mesh, *basis, *program, program->nq, local, dstatus, st);
     if (!rc) rc = read_status(dstatus, st);
     if (!rc) rc = fem::build_csr(basis->element_dofs, nb, basis->ndofs, local, &H->P, st);
+    if (!rc) rc = host_row_pointer(H, st);
     if (!rc && mesh->nelems > 0) {
       cudaError_t e2 = cudaMallocAsync(&H->coef_bits, mesh->nelems, st);
       if (e2 != cudaSuccess) rc = fem::check_cuda(e2, "cudaMallocAsync(coef_bits)");
@@ -359,6 +371,56 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
   fem::Pattern P = pat->P;
   P.sum_unroll = fem::tuning_for(basis->family).sum_unroll;
   return fem::csr_sum(P, staging, csr_values, st);
+}
+
+int fem_assemble_to_host(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
+                         const FemPattern* pat, double* staging, double* csr_values,
+                         double* host_values, int32_t* status, int32_t nchunks,
+                         fem_stream_t stream, fem_stream_t copy_stream) {
+  int rc = validate(mesh, basis);
+  if (rc) return rc;
+  if (!form || !pat || !staging || !csr_values || !host_values || nchunks < 1 || nchunks > 64) {
+    set_error(FEM_ERR_ARGUMENT, "null form, pattern or buffer, or chunks outside 1..64");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (pat->P.nelems != mesh->nelems || pat->P.nbfun_v != basis->nbfun || !pat->P.has_matrix) {
+    set_error(FEM_ERR_ARGUMENT, "pattern does not belong to this mesh / basis");
+    return FEM_ERR_ARGUMENT;
+  }
+  cudaStream_t st = (cudaStream_t)stream, cs = (cudaStream_t)copy_stream;
+  rc = fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
+                                        status ? pat->coef_bits : nullptr, status, st);
+  if (rc) return rc;
+  fem::Pattern P = pat->P;
+  P.sum_unroll = fem::tuning_for(basis->family).sum_unroll;
+  // row ranges of about equal nnz, cut with the pattern's host copy of indptr
+  const std::vector<int32_t>& ip = pat->host_indptr;
+  if ((int64_t)ip.size() != P.nrows + 1) {
+    set_error(FEM_ERR_ARGUMENT, "pattern has no host row pointer");
+    return FEM_ERR_ARGUMENT;
+  }
+  int64_t row = 0;
+  for (int c = 0; c < nchunks && row < P.nrows; ++c) {
+    const int64_t target = (int64_t)P.nnz * (c + 1) / nchunks;
+    int64_t row1 = c == nchunks - 1
+        ? P.nrows
+        : (int64_t)(std::upper_bound(ip.begin() + row, ip.end(), (int32_t)target) - ip.begin()) - 1;
+    if (row1 <= row) row1 = std::min<int64_t>(P.nrows, row + 1);
+    rc = fem::csr_sum(P, staging, csr_values, st, row, row1);
+    if (rc) return rc;
+    const int64_t a = ip[row], b = ip[row1];
+    if (b > a) {
+      cudaEvent_t ev;
+      FEM_TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+      FEM_TRY_CUDA(cudaEventRecord(ev, st));
+      FEM_TRY_CUDA(cudaStreamWaitEvent(cs, ev, 0));
+      cudaEventDestroy(ev);
+      FEM_TRY_CUDA(cudaMemcpyAsync(host_values + a, csr_values + a, (b - a) * sizeof(double),
+                                   cudaMemcpyDeviceToHost, cs));
+    }
+    row = row1;
+  }
+  return 0;
 }
 
 int fem_csr_sum(const FemPattern* pat, const double* local, double* csr_values, int32_t* status,
@@ -482,6 +544,7 @@ int fem_pattern_build_local(const FemMesh* mesh, const FemBasis* basis, const do
   H->vector = basis->vector;
   rc = fem::build_incidence(basis->element_dofs, mesh->nelems, basis->nbfun, basis->ndofs, &H->P, st);
   if (!rc) rc = fem::build_csr(basis->element_dofs, basis->nbfun, basis->ndofs, local, &H->P, st);
+  if (!rc) rc = host_row_pointer(H, st);
   if (rc) {
     fem::free_pattern(new fem::Pattern(H->P));
     delete H;

@@ -69,7 +69,18 @@ inline int num_sms() {
 }
 
 __device__ __forceinline__ double coef_at(const FemCoef& c, int64_t e) {
-  return c.field ? c.scale * c.field[e] : c.scale;
+  return c.field ? c.scale * c.field[c.stride > 1 ? e * c.stride : e] : c.scale;
+}
+
+// A strided (per-point) coefficient must be constant over the cell's points
+// for the channel kernels; otherwise flag FEM_ERR_VARYING.
+__device__ __forceinline__ void check_row(const FemCoef& c, int64_t e, int32_t* status) {
+  if (!c.field || c.stride <= 1) return;
+  const double* r = c.field + e * c.stride;
+  const double v0 = r[0];
+  bool same = true;
+  for (int64_t q = 1; q < c.stride; ++q) same = same && r[q] == v0;
+  if (!same && status) atomicOr(status, 1 << FEM_ERR_VARYING);
 }
 
 // Reference-cube corner (0/1 per axis) of Hex1 node n: node 0 sits at
@@ -93,6 +104,11 @@ struct Tuning {
   int sum_unroll = 8;     // incidence entries loaded together in the sum
 };
 Tuning tuning_for(int family);
+
+// Fixed-order segmented sum of local matrices into CSR values, rows
+// [row0, row1) (row1 < 0: to the last row).
+int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st,
+            int64_t row0 = 0, int64_t row1 = -1);
 
 int basis_nb_scalar(int family);
 int basis_dim(int family);

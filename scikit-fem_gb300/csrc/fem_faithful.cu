@@ -87,23 +87,30 @@ __global__ void mask_kernel(FemMesh m, FemBasis b, FemProgram prog, int nq, doub
 // pairwise sum over the points of each entry.  MODE 0: bilinear (L =
 // nbfun^2 entries, row = test function), 1: linear (L = nbfun), 2:
 // functional (L = 1).  FACET: the cells are a FacetBasis's facets.
-struct GenericShape {
-  int epb, L, nq;
-};
-
 constexpr int kGeo = 20;  // inv 9, det, qx 7, reference point 3
+constexpr int kCell = 22; // affine cell map: inv 9, det, A 9, x0 3
 
 template <int D, bool FACET>
 __device__ bool geometry_at(const FemMesh& m, const FemBasis& b, const FemFacets& fc,
                             const Rule& rule, ProgFlags f, int64_t e, int q, double Y[3],
-                            PointGeo& g) {
+                            PointGeo& g, const double* cell = nullptr) {
   if (FACET) {
     double Xf[2] = {rule.X[q], D == 3 ? rule.X[rule.nq + q] : 0.0};
     return facet_point<D>(m, fc, e, Xf, Y, g);
   }
   const bool hex = b.family == FEM_HEX_1;
   CellGeo c;
-  cell_geometry<D>(m, e, hex, c);
+  if (cell && !hex) {   // the cell's affine map, computed once per cell
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        c.inv[i][j] = cell[i * 3 + j];
+        c.A[i][j] = cell[10 + i * 3 + j];
+      }
+    c.det = cell[9];
+    for (int i = 0; i < 3; ++i) c.x0[i] = cell[19 + i];
+  } else {
+    cell_geometry<D>(m, e, hex, c);
+  }
   Y[0] = rule.X[q];
   Y[1] = rule.X[rule.nq + q];
   Y[2] = D == 3 ? rule.X[2 * rule.nq + q] : 0.0;
@@ -111,24 +118,60 @@ __device__ bool geometry_at(const FemMesh& m, const FemBasis& b, const FemFacets
   return true;
 }
 
+// Shared-memory layout of one block of program_kernel.
+struct GenericLayout {
+  int epb, L, nq, nb, nquant;
+  bool cells, quants;  // per-cell affine maps staged; basis quantities staged
+  __host__ __device__ size_t geo() const { return 0; }
+  __host__ __device__ size_t val() const { return (size_t)epb * nq * kGeo; }
+  __host__ __device__ size_t cell() const { return val() + (size_t)epb * L * nq; }
+  __host__ __device__ size_t quant() const { return cell() + (cells ? (size_t)epb * kCell : 0); }
+  __host__ __device__ size_t total() const {
+    return quant() + (quants ? (size_t)epb * nq * nb * nquant : 0);
+  }
+};
+
 template <int D, int MODE, bool FACET>
 __global__ void program_kernel(FemMesh m, FemBasis b, FemFacets fc, FemProgram prog, Rule rule,
-                               GenericShape s, int64_t ncells, double* __restrict__ out,
+                               GenericLayout s, int64_t ncells, double* __restrict__ out,
                                int32_t* __restrict__ status) {
   extern __shared__ double gsm[];
-  double* geo = gsm;
-  double* val = gsm + (size_t)s.epb * s.nq * kGeo;
+  double* geo = gsm + s.geo();
+  double* val = gsm + s.val();
+  double* cgeo = gsm + s.cell();
+  double* Q = gsm + s.quant();
   const bool hex = b.family == FEM_HEX_1;
+  const bool vec = b.vector != 0;
   const ProgFlags f = prog_flags(prog);
   const int64_t e0 = (int64_t)blockIdx.x * s.epb;
-  const int nb = b.nbfun;
+  const int nb = b.nbfun, NQ = s.nquant;
+  // stage 0: affine cell maps (9 divisions each), once per cell
+  if (s.cells) {
+    for (int el = threadIdx.x; el < s.epb; el += blockDim.x) {
+      const int64_t e = e0 + el;
+      if (e >= ncells) continue;
+      CellGeo c;
+      cell_geometry<D>(m, e, false, c);
+      double* C = cgeo + (size_t)el * kCell;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          C[i * 3 + j] = c.inv[i][j];
+          C[10 + i * 3 + j] = c.A[i][j];
+        }
+      C[9] = c.det;
+      for (int i = 0; i < 3; ++i) C[19 + i] = c.x0[i];
+    }
+    __syncthreads();
+  }
+  // stage 1: point geometry
   for (int k = threadIdx.x; k < s.epb * s.nq; k += blockDim.x) {
     const int el = k / s.nq, q = k - el * s.nq;
     const int64_t e = e0 + el;
     if (e >= ncells) continue;
     PointGeo g;
     double Y[3];
-    if (!geometry_at<D, FACET>(m, b, fc, rule, f, e, q, Y, g)) {
+    if (!geometry_at<D, FACET>(m, b, fc, rule, f, e, q, Y, g,
+                               s.cells ? cgeo + (size_t)el * kCell : nullptr)) {
       atomicOr(status, 1 << FEM_ERR_ARGUMENT);
       g = PointGeo{};
       Y[0] = Y[1] = Y[2] = 0.0;
@@ -142,6 +185,22 @@ __global__ void program_kernel(FemMesh m, FemBasis b, FemFacets fc, FemProgram p
     for (int i = 0; i < 3; ++i) G[17 + i] = Y[i];
   }
   __syncthreads();
+  // stage 1b: every basis function's quantities at every point, once
+  if (s.quants) {
+    for (int k = threadIdx.x; k < s.epb * s.nq * nb; k += blockDim.x) {
+      const int p = k / nb, fn = k - p * nb;    // p = el * nq + q
+      if (e0 + p / s.nq >= ncells) continue;
+      const double* G = geo + (size_t)p * kGeo;
+      double inv[3][3];
+      for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) inv[a][c] = G[a * 3 + c];
+      double qq[D + D * D];
+      quantities<D>(b.family, vec, fn, G[17], G[18], G[19], inv, qq);
+      for (int a = 0; a < NQ; ++a) Q[(size_t)k * NQ + a] = qq[a];
+    }
+    __syncthreads();
+  }
+  // stage 2: form * dx
   double R[kMaxProgram];
   const int per = s.L * s.nq;
   for (int k = threadIdx.x; k < s.epb * per; k += blockDim.x) {
@@ -158,7 +217,17 @@ __global__ void program_kernel(FemMesh m, FemBasis b, FemFacets fc, FemProgram p
       for (int c = 0; c < 3; ++c) g.inv[a][c] = G[a * 3 + c];
     g.det = G[9];
     for (int a = 0; a < 7; ++a) g.qx[a] = G[10 + a];
-    val[k] = point_value<D>(b, prog, e, q, i, j, G[17], G[18], G[19], g, rule.W[q], R);
+    double qu[D + D * D], qv[D + D * D];
+    if (s.quants) {
+      const double* Qp = Q + ((size_t)(el * s.nq + q) * nb) * NQ;
+      for (int a = 0; a < NQ; ++a) {
+        qu[a] = Qp[(size_t)j * NQ + a];
+        qv[a] = Qp[(size_t)i * NQ + a];
+      }
+    } else {
+      for (int a = 0; a < D + D * D; ++a) qu[a] = qv[a] = 0.0;
+    }
+    val[k] = point_value_q(prog, e, q, qu, qv, g, rule.W[q], R);
   }
   __syncthreads();
   for (int k = threadIdx.x; k < s.epb * s.L; k += blockDim.x) {
@@ -169,38 +238,57 @@ __global__ void program_kernel(FemMesh m, FemBasis b, FemFacets fc, FemProgram p
   }
 }
 
-// Basis.interpolate for one (cell, point) per thread: quantity k of the
-// field, out[(k * ncells + e) * nq + q] = 0*(w0 phi_0) + sum_i w_i phi_i
-// in local-function order (abstract_basis.py:295-304).  FACET: at the
-// facet points, with the basis of the cell f2t[side].
+// Basis.interpolate, one cell (or facet) per thread, its points in turn:
+// quantity k of the field, out[(k * ncells + e) * nq + q] =
+// 0*(w0 phi_0) + sum_i w_i phi_i in local-function order
+// (abstract_basis.py:295-304).  FACET: at the facet points, with the basis
+// of the cell f2t[side].
 template <int D, bool FACET>
 __global__ void interpolate_kernel(FemMesh m, FemBasis b, FemFacets fc, Rule rule, int64_t ncells,
                                    const double* __restrict__ w, double* __restrict__ out,
                                    int32_t* __restrict__ status) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncells * rule.nq) return;
-  const int64_t e = t / rule.nq;
-  const int q = (int)(t - e * rule.nq);
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ncells) return;
   const bool vec = b.vector != 0;
-  PointGeo g;
-  double Y[3];
-  if (!geometry_at<D, FACET>(m, b, fc, rule, ProgFlags(), e, q, Y, g)) {
+  const bool hex = b.family == FEM_HEX_1;
+  const int64_t ec = FACET ? (int64_t)fc.tind[e] : e;   // the cell whose DOFs are read
+  if (FACET && (ec < 0 || ec >= m.nelems)) {
     if (status) atomicOr(status, 1 << FEM_ERR_ARGUMENT);
     return;
   }
-  const int64_t ec = FACET ? (int64_t)fc.tind[e] : e;   // the cell whose DOFs are read
+  double cell[kCell];
+  if (!FACET && !hex) {
+    CellGeo c;
+    cell_geometry<D>(m, e, false, c);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        cell[i * 3 + j] = c.inv[i][j];
+        cell[10 + i * 3 + j] = c.A[i][j];
+      }
+    cell[9] = c.det;
+    for (int i = 0; i < 3; ++i) cell[19 + i] = c.x0[i];
+  }
   constexpr int NQ = D + D * D;
   const int nquant = vec ? D + D * D : 1 + D;
-  double acc[NQ], qq[NQ];
   const double w0 = w[b.element_dofs[ec]];
-  quantities<D>(b.family, vec, 0, Y[0], Y[1], Y[2], g.inv, qq);
-  for (int k = 0; k < nquant; ++k) acc[k] = 0.0 * (w0 * qq[k]);
-  for (int i = 0; i < b.nbfun; ++i) {
-    const double wi = w[b.element_dofs[(int64_t)i * m.nelems + ec]];
-    quantities<D>(b.family, vec, i, Y[0], Y[1], Y[2], g.inv, qq);
-    for (int k = 0; k < nquant; ++k) acc[k] = acc[k] + wi * qq[k];
+  for (int q = 0; q < rule.nq; ++q) {
+    PointGeo g;
+    double Y[3];
+    if (!geometry_at<D, FACET>(m, b, fc, rule, ProgFlags(), e, q, Y, g,
+                               (!FACET && !hex) ? cell : nullptr)) {
+      if (status) atomicOr(status, 1 << FEM_ERR_ARGUMENT);
+      return;
+    }
+    double acc[NQ], qq[NQ];
+    quantities<D>(b.family, vec, 0, Y[0], Y[1], Y[2], g.inv, qq);
+    for (int k = 0; k < nquant; ++k) acc[k] = 0.0 * (w0 * qq[k]);
+    for (int i = 0; i < b.nbfun; ++i) {
+      const double wi = w[b.element_dofs[(int64_t)i * m.nelems + ec]];
+      quantities<D>(b.family, vec, i, Y[0], Y[1], Y[2], g.inv, qq);
+      for (int k = 0; k < nquant; ++k) acc[k] = acc[k] + wi * qq[k];
+    }
+    for (int k = 0; k < nquant; ++k) out[((int64_t)k * ncells + e) * rule.nq + q] = acc[k];
   }
-  for (int k = 0; k < nquant; ++k) out[((int64_t)k * ncells + e) * rule.nq + q] = acc[k];
 }
 
 // numpy's pairwise sum of n doubles (np.sum of a contiguous vector): the
@@ -348,15 +436,26 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets*
   const int nb = b.nbfun;
   const int L = mode == 0 ? nb * nb : (mode == 1 ? nb : 1);
   const int nq = prog.nq;
-  auto bytes = [&](int epb) { return (size_t)epb * nq * (fem_faithful::kGeo + L) * sizeof(double); };
+  fem_faithful::GenericLayout s;
+  s.L = L;
+  s.nq = nq;
+  s.nb = nb;
+  s.nquant = b.vector ? m.dim + m.dim * m.dim : 1 + m.dim;
+  s.cells = !fc && b.family != FEM_HEX_1;
+  s.quants = mode != 2;   // a functional reads no basis function
+  auto bytes = [&](int epb) {
+    fem_faithful::GenericLayout t = s;
+    t.epb = epb;
+    return t.total() * sizeof(double);
+  };
   int epb = std::max(1, std::min(64, 2048 / (L * nq)));
   while (epb > 1 && bytes(epb) > 96 * 1024) --epb;
+  s.epb = epb;
   const size_t smem = bytes(epb);
   if (smem > 200 * 1024) {
     set_error(FEM_ERR_CAPACITY, "%d local entries x %d points do not fit one block", L, nq);
     return FEM_ERR_CAPACITY;
   }
-  fem_faithful::GenericShape s{epb, L, nq};
   const fem_faithful::Rule rule{prog.qX, prog.qW, nq};
   const FemFacets F = fc ? *fc : FemFacets{};
   const unsigned grid = (unsigned)ceil_div(ncells, epb);
@@ -400,11 +499,10 @@ int interpolate(const FemMesh& m, const FemBasis& b, const FemFacets* fc, int nq
   if (!facets_ok(m, b, fc)) return fc && b.family == FEM_HEX_1 ? FEM_ERR_UNSUPPORTED
                                                                : FEM_ERR_ARGUMENT;
   const int64_t ncells = fc ? fc->nfacets : m.nelems;
-  const int64_t n = ncells * (int64_t)nq;
-  if (n == 0) return 0;
+  if (ncells == 0) return 0;
   const fem_faithful::Rule rule{X, nullptr, nq};
   const FemFacets F = fc ? *fc : FemFacets{};
-  const unsigned grid = (unsigned)ceil_div(n, 128);
+  const unsigned grid = (unsigned)ceil_div(ncells, 128);
   using namespace fem_faithful;
   if (m.dim == 2) {
     if (fc) interpolate_kernel<2, true><<<grid, 128, 0, st>>>(m, b, F, rule, ncells, w, out, status);

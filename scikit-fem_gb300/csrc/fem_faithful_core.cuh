@@ -429,19 +429,26 @@ FEM_HD bool facet_point(const FemMesh& m, const FemFacets& fc, int64_t f, const 
 // linear_form.py:48-49, functional.py:19-24): dx = |detDF| * W[q]
 // (cell_basis.py:104-105).  Coefficient slot c holds one value per element
 // (stride 0) or per quadrature point (stride nq).
-template <int D>
-FEM_HD double point_value(const FemBasis& b, const FemProgram& prog, int64_t e, int q, int i,
-                          int j, double x, double y, double z, const PointGeo& g, double wq,
-                          double* R) {
-  const bool vec = b.vector != 0;
-  double qu[D + D * D], qv[D + D * D], cq[kMaxCoef];
-  quantities<D>(b.family, vec, j, x, y, z, g.inv, qu);
-  quantities<D>(b.family, vec, i, x, y, z, g.inv, qv);
+// ... with the trial (qu) and test (qv) quantities already evaluated
+FEM_HD double point_value_q(const FemProgram& prog, int64_t e, int q, const double* qu,
+                            const double* qv, const PointGeo& g, double wq, double* R) {
+  double cq[kMaxCoef];
   for (int c = 0; c < prog.ncoef && c < kMaxCoef; ++c)
     cq[c] = prog.coef[c] ? prog.coef[c][prog.coef_stride[c] ? e * prog.coef_stride[c] + q : e]
                          : 0.0;
   const double f = run(prog.ins, prog.ninstr, prog.out, qu, qv, cq, g.qx, R);
   return f * (fabs(g.det) * wq);
+}
+
+template <int D>
+FEM_HD double point_value(const FemBasis& b, const FemProgram& prog, int64_t e, int q, int i,
+                          int j, double x, double y, double z, const PointGeo& g, double wq,
+                          double* R) {
+  const bool vec = b.vector != 0;
+  double qu[D + D * D], qv[D + D * D];
+  quantities<D>(b.family, vec, j, x, y, z, g.inv, qu);
+  quantities<D>(b.family, vec, i, x, y, z, g.inv, qv);
+  return point_value_q(prog, e, q, qu, qv, g, wq, R);
 }
 
 // The replayed value of local entry (row i, column j) of element e: the

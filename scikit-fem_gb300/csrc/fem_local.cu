@@ -153,6 +153,11 @@ template <> struct SimplexTraits<3, 2> { static constexpr int NB = 10; static co
 __device__ __forceinline__ void check_coef_bits(const FemBilinear& f, int64_t e,
                                                 const uint8_t* __restrict__ ref,
                                                 int32_t* __restrict__ status) {
+  fem::check_row(f.diff, e, status);
+  fem::check_row(f.mass, e, status);
+  fem::check_row(f.lam, e, status);
+  fem::check_row(f.lap, e, status);
+  fem::check_row(f.tr, e, status);
   if (!ref) return;
   uint8_t bits = 0;
   bits |= (coef_at(f.diff, e) == 0.0) ? 1u : 0u;

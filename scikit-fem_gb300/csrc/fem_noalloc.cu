@@ -31,7 +31,6 @@ int local_matrices(const FemMesh&, const FemBasis&, const FemBilinear&, double*,
                    cudaStream_t);
 }
 namespace fem {
-int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st);
 const Pattern* pattern_of(const FemPattern* h);
 const uint8_t* pattern_coef_bits(const FemPattern* h);
 int coef_check(const FemBilinear& f, int64_t n, const uint8_t* ref, int32_t* status,

@@ -223,8 +223,8 @@ __global__ void row_fill_kernel(const int32_t* __restrict__ inc_ptr, const int32
 template <int G, int U>
 __global__ void csr_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                                const uint16_t* __restrict__ slot, const int32_t* __restrict__ indptr,
-                               const double* __restrict__ local, int64_t nrows, int nu, int stride,
-                               double* __restrict__ vals) {
+                               const double* __restrict__ local, int64_t row0, int64_t nrows,
+                               int nu, int stride, double* __restrict__ vals) {
   extern __shared__ double acc_smem[];
   constexpr int RPW = 32 / G;  // rows per warp
   const int lane = threadIdx.x & 31;
@@ -233,7 +233,7 @@ __global__ void csr_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_
   const int wib = threadIdx.x >> 5;
   double* acc = acc_smem + ((size_t)wib * RPW + sub) * stride;
   const int64_t rows_per_block = (int64_t)(blockDim.x >> 5) * RPW;
-  for (int64_t rb = (int64_t)blockIdx.x * rows_per_block; rb < nrows;
+  for (int64_t rb = row0 + (int64_t)blockIdx.x * rows_per_block; rb < nrows;
        rb += (int64_t)gridDim.x * rows_per_block) {
     const int64_t r = rb + (int64_t)wib * RPW + sub;
     const bool live = r < nrows;
@@ -525,12 +525,15 @@ int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, 
   return 0;
 }
 
-int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st) {
+int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st, int64_t row0,
+            int64_t row1) {
   if (!P.has_matrix) {
     set_error(FEM_ERR_ARGUMENT, "pattern has no CSR structure (built without local matrices)");
     return FEM_ERR_ARGUMENT;
   }
-  if (P.nrows == 0 || P.nnz == 0) return 0;
+  if (row1 < 0 || row1 > P.nrows) row1 = P.nrows;
+  if (row0 < 0) row0 = 0;
+  if (row1 <= row0 || P.nnz == 0) return 0;
   const int nu = P.nbfun_u;
   const int stride = std::max(1, P.max_row_nnz);
   const int threads = 128;
@@ -544,9 +547,9 @@ int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st
       if (e != cudaSuccess) return check_cuda(e, "csr_sum smem");
     }
     const int64_t rows_per_block = (int64_t)warps * rpw;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(P.nrows, rows_per_block),
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(row1 - row0, rows_per_block),
                                                                 (int64_t)num_sms() * 64));
-    kern<<<grid, threads, smem, st>>>(P.inc_ptr, P.inc, P.slot, P.indptr, local, P.nrows, nu,
+    kern<<<grid, threads, smem, st>>>(P.inc_ptr, P.inc, P.slot, P.indptr, local, row0, row1, nu,
                                       stride, vals);
     return 0;
   };

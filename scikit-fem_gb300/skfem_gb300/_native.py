@@ -19,6 +19,7 @@ FEM_ERR_CUDA = 3
 FEM_ERR_ZERO_JACOBIAN = 4
 FEM_ERR_STALE_PATTERN = 5
 FEM_ERR_CAPACITY = 6
+FEM_ERR_VARYING = 7
 
 FAMILY = {"TriP1": 1, "TriP2": 2, "TetP1": 3, "TetP2": 4, "Hex1": 5}
 
@@ -36,7 +37,8 @@ class FemBasis(ctypes.Structure):
 
 
 class FemCoef(ctypes.Structure):
-    _fields_ = [("scale", ctypes.c_double), ("field", ctypes.c_void_p)]
+    _fields_ = [("scale", ctypes.c_double), ("field", ctypes.c_void_p),
+                ("stride", ctypes.c_int64)]
 
 
 class FemBilinear(ctypes.Structure):
@@ -111,6 +113,8 @@ _SIGS = {
     "fem_facet_program_local_vectors": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "fem_facet_program_elemental": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "fem_facet_interpolate": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P, _P, _P, _P]),
+    "fem_assemble_to_host": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, ctypes.c_int32,
+                                            _P, _P]),
     "fem_set_tuning": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "fem_assemble_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
 }

@@ -53,11 +53,12 @@ class _Coefficients:
                length N, abstract_basis.py:271-322) or given fields
     """
 
-    def __init__(self, basis, kwargs):
+    def __init__(self, basis, kwargs, strided=False):
         self.fields = {}
         self.qfields = {}
         self.dfields = {}
         self.numbers = {}
+        self.strided = {}   # name -> (nelems, nqp) device copy checked inside the kernels
         self.keep = []
         dev = basis.device
         ne = basis.nelems
@@ -91,6 +92,12 @@ class _Coefficients:
                     self._dof_vector(k, v, basis, dim)
                     continue
                 t = torch.from_numpy(np.ascontiguousarray(v, dtype=np.float64)).to(dev)
+                if strided and tuple(t.shape) == (ne, nqp) and nqp > 1 and ne > 0:
+                    # the channel kernels read column 0 and check each row
+                    # is constant (FEM_ERR_VARYING), no separate pass
+                    self.strided[k] = t
+                    self.fields[k] = None
+                    continue
             elif isinstance(v, list):
                 raise NotImplementedError("list-valued coefficients are not supported")
             else:
@@ -158,7 +165,7 @@ class _Coefficients:
         return self.fields[key].data_ptr(), 0
 
     def coef(self, poly, ne, device):
-        """Poly -> FemCoef (scale, field pointer)."""
+        """Poly -> FemCoef (scale, field pointer, stride)."""
         items = [(names, c) for names, c in poly.items() if c != 0.0]
         if not items:
             return N.FemCoef(0.0, None)
@@ -167,7 +174,13 @@ class _Coefficients:
             if names == ():
                 return N.FemCoef(c, None)
             if len(names) == 1:
-                return N.FemCoef(c, self.fields[names[0]].data_ptr())
+                n = names[0]
+                if n in self.strided:
+                    a = self.strided[n]
+                    return N.FemCoef(c, a.data_ptr(), a.shape[1])
+                return N.FemCoef(c, self.fields[n].data_ptr())
+        if any(n in self.strided for names, _ in items for n in names):
+            raise _StridedFieldInProduct()
         acc = torch.zeros(ne, dtype=torch.float64, device=device)
         for names, c in items:
             term = torch.full((ne,), c, dtype=torch.float64, device=device)
@@ -176,6 +189,11 @@ class _Coefficients:
             acc = acc + term
         self.keep.append(acc)
         return N.FemCoef(1.0, acc.data_ptr())
+
+
+class _StridedFieldInProduct(Exception):
+    """A strided (unchecked) coefficient enters a product of fields: the
+    caller normalises the coefficients with a separate check instead."""
 
 
 class Form:
@@ -308,7 +326,11 @@ def _program(form, basis, coeffs):
     dev = torch.frombuffer(bytearray(arr), dtype=torch.uint8).to(basis.device)
     prog = N.FemProgram(len(ins), out, len(names), basis.X.shape[1], dev.data_ptr())
     for k, n in enumerate(names):
-        prog.coef[k] = coeffs.fields[n].data_ptr()
+        if n in coeffs.strided:
+            prog.coef[k] = coeffs.strided[n].data_ptr()
+            prog.coef_stride[k] = coeffs.strided[n].shape[1]
+        else:
+            prog.coef[k] = coeffs.fields[n].data_ptr()
     prog.qX = basis.X_dev.data_ptr()
     prog.qW = basis.W_dev.data_ptr()
     return prog, dev
@@ -344,6 +366,18 @@ class _PatternEntry:
         else:
             self.staging = torch.empty(max(1, basis.nelems * basis.Nbfun), dtype=torch.float64,
                                        device=dev)
+
+
+_SIDE = {}
+HOST_CHUNKS = 8     # row ranges whose device->host copies overlap the segmented sum
+
+
+def _side_stream(device):
+    """A per-device stream for copies that overlap the assembly kernels."""
+    s = _SIDE.get(device)
+    if s is None:
+        s = _SIDE[device] = torch.cuda.Stream(device=device)
+    return s
 
 
 def _raise_status(st):
@@ -451,10 +485,11 @@ class BilinearForm(Form):
         return entry, vals
 
     # ------------------------------------------------------------- driver
-    def _assemble_device(self, ubasis, vbasis, kwargs, check=True):
+    def _assemble_device(self, ubasis, vbasis, kwargs, check=True, coeffs=None):
         if vbasis is not None and vbasis is not ubasis:
             raise NotImplementedError("different trial and test bases are not supported yet")
-        coeffs = _Coefficients(ubasis, kwargs)
+        if coeffs is None:
+            coeffs = _Coefficients(ubasis, kwargs)
         ch = self._trace(ubasis, coeffs, "bilinear")
         if ch is None:
             return self._generic_assemble(ubasis, coeffs, check)
@@ -470,9 +505,76 @@ class BilinearForm(Form):
         return entry, vals
 
     def assemble(self, ubasis, vbasis=None, **kwargs):
-        """Assemble into a scipy.sparse.csr_matrix (bilinear_form.py:130-148)."""
-        entry, vals = self._assemble_device(ubasis, vbasis, kwargs)
+        """Assemble into a scipy.sparse.csr_matrix (bilinear_form.py:130-148).
+
+        On the channel kernels (nelems, nqp) coefficient arrays are copied
+        whole and their rows checked inside the local kernel, the pattern's
+        index arrays are copied to the host on a side stream while the
+        kernels run, and the call synchronises once before returning."""
+        if vbasis is not None and vbasis is not ubasis:
+            raise NotImplementedError("different trial and test bases are not supported yet")
+        coeffs = _Coefficients(ubasis, kwargs, strided=True)
+        ch = self._trace(ubasis, coeffs, "bilinear")
+        if ch is not None:
+            try:
+                K = self._assemble_to_host(ubasis, coeffs, ch)
+            except _StridedFieldInProduct:
+                K = None
+            if K is not None:
+                return K
+        if coeffs.strided or ch is not None:
+            coeffs = _Coefficients(ubasis, kwargs)          # rows checked up front
+        entry, vals = self._assemble_device(ubasis, None, kwargs, coeffs=coeffs)
         return _host_csr(entry, vals, ubasis.N)
+
+    def _assemble_to_host(self, ubasis, coeffs, ch):
+        """Channel kernels, results copied to pinned host memory; None when
+        a per-point coefficient varies inside a cell."""
+        main = torch.cuda.current_stream()
+        for attempt in range(2):
+            c_form = self._c_form(ubasis, coeffs, ch)
+            stream = N.stream_ptr(main)
+            key = ("bilinear", _structure_key(ch))
+            entry = ubasis._patterns.get(key)
+            if entry is None:
+                prog, keep = _program(self, ubasis, coeffs)
+                entry = _PatternEntry(ubasis, c_form, stream, prog)
+                del keep
+                ubasis._patterns[key] = entry
+            data = torch.empty(entry.nnz, dtype=torch.float64, pin_memory=True)
+            indices = torch.empty(entry.nnz, dtype=torch.int32, pin_memory=True)
+            indptr = torch.empty(entry.nrows + 1, dtype=torch.int32, pin_memory=True)
+            side = _side_stream(ubasis.device)
+            side.wait_stream(main)
+            with torch.cuda.stream(side):
+                indices.copy_(entry.indices, non_blocking=True)
+                indptr.copy_(entry.indptr, non_blocking=True)
+            vals = torch.empty(max(entry.nnz, 1), dtype=torch.float64, device=ubasis.device)
+            entry.status.zero_()
+            if entry.nnz:
+                # values stream to the host range by range behind the sum
+                N.check(N.lib().fem_assemble_to_host(
+                    N.byref(ubasis.c_mesh), N.byref(ubasis.c_basis), N.byref(c_form),
+                    entry.pat.handle, N.ptr(entry.staging), N.ptr(vals),
+                    ctypes.c_void_p(data.data_ptr()), N.ptr(entry.status), HOST_CHUNKS,
+                    stream, N.stream_ptr(side)))
+            st_h = torch.empty(1, dtype=torch.int32, pin_memory=True)
+            st_h.copy_(entry.status, non_blocking=True)
+            main.synchronize()
+            side.synchronize()
+            st = int(st_h[0])
+            _raise_status(st)
+            if st & (1 << N.FEM_ERR_VARYING):
+                return None
+            if st & (1 << N.FEM_ERR_STALE_PATTERN):
+                del ubasis._patterns[key]
+                continue
+            K = sp.csr_matrix((data.numpy(), indices.numpy(), indptr.numpy()),
+                              shape=(ubasis.N, ubasis.N), copy=False)
+            K.has_sorted_indices = True
+            K.has_canonical_format = True
+            return K
+        raise RuntimeError("the CSR pattern went stale twice in one call")
 
     def assemble_torch(self, ubasis, vbasis=None, check=True, **kwargs):
         """Device-resident result: torch.sparse_csr_tensor (int32 indices,

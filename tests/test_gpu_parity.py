@@ -335,3 +335,31 @@ def test_condense_on_device_matches_reference_semantics():
     np.testing.assert_array_equal(I.cpu().numpy(), Iref)
     # only A: the reference returns the matrix alone when b is None and expand=False
     assert isinstance(condense(A, D=D, expand=False), torch.Tensor)
+
+
+def test_host_coefficients_checked_in_kernel():
+    """assemble() with (nelems, nqp) host coefficient arrays: the rows are
+    checked inside the local kernel and the values stream to pinned host
+    memory by row ranges -- the same bits as the device-resident call; a row
+    that varies inside a cell falls back to the generic kernels."""
+    g = golden("tet_p1_k_laplace_mass")
+    b = basis_of(g, F.ElementTetP1())
+    kw = b.zero_w() + g["k"][:, None]
+    K1 = k_laplace_mass.assemble(b, k=kw)
+    K2 = k_laplace_mass.assemble_torch(b, k=torch.as_tensor(g["k"], device="cuda"))
+    np.testing.assert_array_equal(K1.indptr, K2.crow_indices().cpu().numpy())
+    np.testing.assert_array_equal(K1.indices, K2.col_indices().cpu().numpy())
+    np.testing.assert_array_equal(K1.data, K2.values().cpu().numpy())
+    check_matrix(K1, g)
+    kv = kw.copy()
+    kv[5, 2] *= 3.0
+    kv[40, 0] = 0.0
+    Kv = k_laplace_mass.assemble(b, k=kv)
+    bo = O.OBasis(O.OMesh(g["p"], g["t"], "tet"), O.TetP1())
+    Ko = O.bilinear_assemble(O.k_laplace_mass, bo, k=kv)
+    same, extra, missing, noise, rf, rm = csr_diff(Kv.indptr, Kv.indices, Kv.data, Ko.indptr,
+                                                   Ko.indices, Ko.data, Kv.shape)
+    assert same and rf <= REL_FRO and rm <= REL_MAX, (extra, missing, rf, rm)
+    # the plain call afterwards is back on the channel kernels
+    K3 = k_laplace_mass.assemble(b, k=kw)
+    np.testing.assert_array_equal(K3.data, K1.data)
