@@ -30,7 +30,18 @@
 #ifndef SKFEM_GB300_H
 #define SKFEM_GB300_H
 
+#ifndef __CUDACC_RTC__
 #include <stdint.h>
+#else
+typedef signed char int8_t;
+typedef unsigned char uint8_t;
+typedef short int16_t;
+typedef unsigned short uint16_t;
+typedef int int32_t;
+typedef unsigned int uint32_t;
+typedef long long int64_t;
+typedef unsigned long long uint64_t;
+#endif
 
 #ifdef __cplusplus
 extern "C" {
@@ -144,7 +155,31 @@ typedef struct FemProgram {
   int32_t coef_stride[16];
   const double* qX;       /* the basis's reference points (dim, nq), device; */
   const double* qW;       /* and weights (nq); required by fem_program_*     */
+  const struct FemCompiled* compiled;  /* optional: this program compiled by
+                                          fem_program_compile (same dim, mode,
+                                          facet use); null: interpreted */
 } FemProgram;
+
+/*
+ * Compile a form program (ins: HOST array of ninstr instructions, as traced)
+ * into a kernel for dim, mode (0 local matrices, 1 local vectors, 2 per-cell
+ * values) and facet (0 cells, 1 FacetBasis facets): NVRTC, sm_103a,
+ * -fmad=false, the program as straight-line code -- the interpreter's
+ * operations in the same order, so results are bitwise the interpreter's.
+ * Returns FEM_ERR_UNSUPPORTED when libnvrtc is unavailable.  Release with
+ * fem_program_release.
+ */
+typedef struct FemCompiled FemCompiled;
+int fem_program_compile(const FemInstr* ins, int32_t ninstr, int32_t out, int32_t ncoef,
+                        int32_t dim, int32_t vector, int32_t mode, int32_t facet,
+                        FemCompiled** compiled);
+void fem_program_release(FemCompiled* compiled);
+/* The complete source fem_program_compile compiles for these arguments (its
+ * headers: fem_faithful_core.cuh, fem_program_kernel.cuh and this file, by
+ * name); *needed receives its length + 1.  Host-only, no GPU needed. */
+int fem_program_source(const FemInstr* ins, int32_t ninstr, int32_t out, int32_t ncoef,
+                       int32_t dim, int32_t vector, int32_t mode, int32_t facet, char* buf,
+                       int64_t size, int64_t* needed);
 
 /* Opaque one-time structure: row incidence, CSR pattern, local-to-slot map. */
 typedef struct FemPattern FemPattern;

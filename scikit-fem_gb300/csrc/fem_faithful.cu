@@ -30,6 +30,8 @@
 #include "fem_refquad.cuh"
 
 #include "fem_faithful_core.cuh"
+#include "fem_program_kernel.cuh"
+#include "fem_jit.h"
 
 #include <vector>
 
@@ -81,161 +83,11 @@ __global__ void mask_kernel(FemMesh m, FemBasis b, FemProgram prog, int nq, doub
 }
 
 // ------------------------------------------------------------ generic forms
-// One block takes EPB cells (or facets).  Stage 1: the geometry of every
-// (cell, point) pair into shared memory.  Stage 2: form * dx for every
-// (cell, entry, point) triple into shared memory.  Stage 3: numpy's
-// pairwise sum over the points of each entry.  MODE 0: bilinear (L =
-// nbfun^2 entries, row = test function), 1: linear (L = nbfun), 2:
-// functional (L = 1).  FACET: the cells are a FacetBasis's facets.
-constexpr int kGeo = 20;  // inv 9, det, qx 7, reference point 3
-constexpr int kCell = 22; // affine cell map: inv 9, det, A 9, x0 3
-
-template <int D, bool FACET>
-__device__ bool geometry_at(const FemMesh& m, const FemBasis& b, const FemFacets& fc,
-                            const Rule& rule, ProgFlags f, int64_t e, int q, double Y[3],
-                            PointGeo& g, const double* cell = nullptr) {
-  if (FACET) {
-    double Xf[2] = {rule.X[q], D == 3 ? rule.X[rule.nq + q] : 0.0};
-    return facet_point<D>(m, fc, e, Xf, Y, g);
-  }
-  const bool hex = b.family == FEM_HEX_1;
-  CellGeo c;
-  if (cell && !hex) {   // the cell's affine map, computed once per cell
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        c.inv[i][j] = cell[i * 3 + j];
-        c.A[i][j] = cell[10 + i * 3 + j];
-      }
-    c.det = cell[9];
-    for (int i = 0; i < 3; ++i) c.x0[i] = cell[19 + i];
-  } else {
-    cell_geometry<D>(m, e, hex, c);
-  }
-  Y[0] = rule.X[q];
-  Y[1] = rule.X[rule.nq + q];
-  Y[2] = D == 3 ? rule.X[2 * rule.nq + q] : 0.0;
-  point_geometry<D>(m, e, hex, c, f, Y[0], Y[1], Y[2], g);
-  return true;
-}
-
-// Shared-memory layout of one block of program_kernel.
-struct GenericLayout {
-  int epb, L, nq, nb, nquant;
-  bool cells, quants;  // per-cell affine maps staged; basis quantities staged
-  __host__ __device__ size_t geo() const { return 0; }
-  __host__ __device__ size_t val() const { return (size_t)epb * nq * kGeo; }
-  __host__ __device__ size_t cell() const { return val() + (size_t)epb * L * nq; }
-  __host__ __device__ size_t quant() const { return cell() + (cells ? (size_t)epb * kCell : 0); }
-  __host__ __device__ size_t total() const {
-    return quant() + (quants ? (size_t)epb * nq * nb * nquant : 0);
-  }
-};
-
 template <int D, int MODE, bool FACET>
 __global__ void program_kernel(FemMesh m, FemBasis b, FemFacets fc, FemProgram prog, Rule rule,
                                GenericLayout s, int64_t ncells, double* __restrict__ out,
                                int32_t* __restrict__ status) {
-  extern __shared__ double gsm[];
-  double* geo = gsm + s.geo();
-  double* val = gsm + s.val();
-  double* cgeo = gsm + s.cell();
-  double* Q = gsm + s.quant();
-  const bool hex = b.family == FEM_HEX_1;
-  const bool vec = b.vector != 0;
-  const ProgFlags f = prog_flags(prog);
-  const int64_t e0 = (int64_t)blockIdx.x * s.epb;
-  const int nb = b.nbfun, NQ = s.nquant;
-  // stage 0: affine cell maps (9 divisions each), once per cell
-  if (s.cells) {
-    for (int el = threadIdx.x; el < s.epb; el += blockDim.x) {
-      const int64_t e = e0 + el;
-      if (e >= ncells) continue;
-      CellGeo c;
-      cell_geometry<D>(m, e, false, c);
-      double* C = cgeo + (size_t)el * kCell;
-      for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-          C[i * 3 + j] = c.inv[i][j];
-          C[10 + i * 3 + j] = c.A[i][j];
-        }
-      C[9] = c.det;
-      for (int i = 0; i < 3; ++i) C[19 + i] = c.x0[i];
-    }
-    __syncthreads();
-  }
-  // stage 1: point geometry
-  for (int k = threadIdx.x; k < s.epb * s.nq; k += blockDim.x) {
-    const int el = k / s.nq, q = k - el * s.nq;
-    const int64_t e = e0 + el;
-    if (e >= ncells) continue;
-    PointGeo g;
-    double Y[3];
-    if (!geometry_at<D, FACET>(m, b, fc, rule, f, e, q, Y, g,
-                               s.cells ? cgeo + (size_t)el * kCell : nullptr)) {
-      atomicOr(status, 1 << FEM_ERR_ARGUMENT);
-      g = PointGeo{};
-      Y[0] = Y[1] = Y[2] = 0.0;
-    }
-    if (!FACET && hex && g.det == 0.0) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
-    double* G = geo + (size_t)k * kGeo;
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) G[i * 3 + j] = g.inv[i][j];
-    G[9] = g.det;
-    for (int i = 0; i < 7; ++i) G[10 + i] = g.qx[i];
-    for (int i = 0; i < 3; ++i) G[17 + i] = Y[i];
-  }
-  __syncthreads();
-  // stage 1b: every basis function's quantities at every point, once
-  if (s.quants) {
-    for (int k = threadIdx.x; k < s.epb * s.nq * nb; k += blockDim.x) {
-      const int p = k / nb, fn = k - p * nb;    // p = el * nq + q
-      if (e0 + p / s.nq >= ncells) continue;
-      const double* G = geo + (size_t)p * kGeo;
-      double inv[3][3];
-      for (int a = 0; a < 3; ++a)
-        for (int c = 0; c < 3; ++c) inv[a][c] = G[a * 3 + c];
-      double qq[D + D * D];
-      quantities<D>(b.family, vec, fn, G[17], G[18], G[19], inv, qq);
-      for (int a = 0; a < NQ; ++a) Q[(size_t)k * NQ + a] = qq[a];
-    }
-    __syncthreads();
-  }
-  // stage 2: form * dx
-  double R[kMaxProgram];
-  const int per = s.L * s.nq;
-  for (int k = threadIdx.x; k < s.epb * per; k += blockDim.x) {
-    const int el = k / per;
-    const int rq = k - el * per;
-    const int r = rq / s.nq, q = rq - r * s.nq;
-    const int64_t e = e0 + el;
-    if (e >= ncells) continue;
-    const int i = MODE == 0 ? r / nb : (MODE == 1 ? r : 0);
-    const int j = MODE == 0 ? r - i * nb : 0;
-    const double* G = geo + ((size_t)el * s.nq + q) * kGeo;
-    PointGeo g;
-    for (int a = 0; a < 3; ++a)
-      for (int c = 0; c < 3; ++c) g.inv[a][c] = G[a * 3 + c];
-    g.det = G[9];
-    for (int a = 0; a < 7; ++a) g.qx[a] = G[10 + a];
-    double qu[D + D * D], qv[D + D * D];
-    if (s.quants) {
-      const double* Qp = Q + ((size_t)(el * s.nq + q) * nb) * NQ;
-      for (int a = 0; a < NQ; ++a) {
-        qu[a] = Qp[(size_t)j * NQ + a];
-        qv[a] = Qp[(size_t)i * NQ + a];
-      }
-    } else {
-      for (int a = 0; a < D + D * D; ++a) qu[a] = qv[a] = 0.0;
-    }
-    val[k] = point_value_q(prog, e, q, qu, qv, g, rule.W[q], R);
-  }
-  __syncthreads();
-  for (int k = threadIdx.x; k < s.epb * s.L; k += blockDim.x) {
-    const int el = k / s.L;
-    const int64_t e = e0 + el;
-    if (e >= ncells) continue;
-    out[e0 * s.L + k] = np_pairwise_sum(val + (size_t)k * s.nq, s.nq);
-  }
+  program_body<D, MODE, FACET>(m, b, fc, prog, rule, s, ncells, out, status);
 }
 
 // Basis.interpolate, one cell (or facet) per thread, its points in turn:
@@ -344,6 +196,8 @@ __global__ void pairwise_tree_kernel(const double* __restrict__ leaf_sum, int64_
 }  // namespace fem_faithful
 namespace fem {
 
+int check_instructions(const FemInstr* h, int ninstr, int ncoef, int dim, bool vec);
+
 // Host-side check of a form program before any kernel interprets it: every
 // operand names an earlier register, a basis quantity, a coefficient slot
 // or a coordinate that exists.
@@ -369,14 +223,20 @@ int check_program(const FemProgram& prog, int dim, bool vec, bool need_rule) {
     }
   FemInstr h[kMaxProgram];
   FEM_TRY_CUDA(cudaMemcpy(h, prog.ins, prog.ninstr * sizeof(FemInstr), cudaMemcpyDefault));
+  return check_instructions(h, prog.ninstr, prog.ncoef, dim, vec);
+}
+
+// Operand checks of a program held in host memory.
+int check_instructions(const FemInstr* h, int ninstr, int ncoef, int dim, bool vec) {
+  using namespace fem_faithful;
   const int nquant = vec ? dim + dim * dim : 1 + dim;
-  for (int k = 0; k < prog.ninstr; ++k) {
+  for (int k = 0; k < ninstr; ++k) {
     const FemInstr& I = h[k];
     bool ok = true;
     switch (I.op) {
       case OP_CONST: case OP_H: break;
       case OP_U: case OP_V: ok = I.a >= 0 && I.a < nquant; break;
-      case OP_COEF: ok = I.a >= 0 && I.a < prog.ncoef; break;
+      case OP_COEF: ok = I.a >= 0 && I.a < ncoef; break;
       case OP_X: case OP_N: ok = I.a >= 0 && I.a < dim; break;
       case OP_ADD: case OP_SUB: case OP_MUL: case OP_DIV: case OP_POW:
         ok = I.a >= 0 && I.a < k && I.b >= 0 && I.b < k; break;
@@ -460,6 +320,25 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets*
   const FemFacets F = fc ? *fc : FemFacets{};
   const unsigned grid = (unsigned)ceil_div(ncells, epb);
   const int threads = 256;
+  if (prog.compiled) {
+    const FemCompiled* k = prog.compiled;
+    if (k->dim != m.dim || k->mode != mode || k->facet != (fc ? 1 : 0)) {
+      set_error(FEM_ERR_ARGUMENT, "compiled program is for dim %d mode %d facet %d", k->dim,
+                k->mode, k->facet);
+      return FEM_ERR_ARGUMENT;
+    }
+    FemMesh mm = m;
+    FemBasis bb = b;
+    FemFacets ff = F;
+    FemProgram pp = prog;
+    fem_faithful::Rule rr = rule;
+    fem_faithful::GenericLayout ss = s;
+    int64_t nc = ncells;
+    double* o = out;
+    int32_t* stp = status;
+    void* args[] = {&mm, &bb, &ff, &pp, &rr, &ss, &nc, &o, &stp};
+    return jit_launch(k, dim3(grid), dim3(threads), smem, st, args);
+  }
   auto go = [&](auto kern) -> int {
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,

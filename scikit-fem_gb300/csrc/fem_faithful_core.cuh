@@ -4,15 +4,17 @@
 // Compile with -fmad=false (device) and without FMA contraction (host).
 #pragma once
 
+#ifndef __CUDACC_RTC__
 #include <cmath>
 #include <stdint.h>
+#endif
 
 #include "../../include/skfem_gb300.h"
 
 #ifdef __CUDACC__
-#define FEM_HD __host__ __device__
+#define FEM_HD __host__ __device__ inline
 #else
-#define FEM_HD
+#define FEM_HD inline
 #endif
 
 namespace fem_faithful {
@@ -429,6 +431,13 @@ FEM_HD bool facet_point(const FemMesh& m, const FemFacets& fc, int64_t f, const 
 // linear_form.py:48-49, functional.py:19-24): dx = |detDF| * W[q]
 // (cell_basis.py:104-105).  Coefficient slot c holds one value per element
 // (stride 0) or per quadrature point (stride nq).
+// The form at one point: the program interpreter, or (kernels compiled
+// from a traced program) the program's own straight-line code.
+#ifndef FEM_FORM_EVAL
+#define FEM_FORM_EVAL(prog, qu, qv, cq, qx, R) \
+  run((prog).ins, (prog).ninstr, (prog).out, qu, qv, cq, qx, R)
+#endif
+
 // ... with the trial (qu) and test (qv) quantities already evaluated
 FEM_HD double point_value_q(const FemProgram& prog, int64_t e, int q, const double* qu,
                             const double* qv, const PointGeo& g, double wq, double* R) {
@@ -436,7 +445,7 @@ FEM_HD double point_value_q(const FemProgram& prog, int64_t e, int q, const doub
   for (int c = 0; c < prog.ncoef && c < kMaxCoef; ++c)
     cq[c] = prog.coef[c] ? prog.coef[c][prog.coef_stride[c] ? e * prog.coef_stride[c] + q : e]
                          : 0.0;
-  const double f = run(prog.ins, prog.ninstr, prog.out, qu, qv, cq, g.qx, R);
+  const double f = FEM_FORM_EVAL(prog, qu, qv, cq, g.qx, R);
   return f * (fabs(g.det) * wq);
 }
 

@@ -30,7 +30,25 @@ UNITS = [
     ("fem_noalloc.cu", "fem_noalloc.o", []),
     ("fem_faithful.cu", "fem_faithful.o", ["-fmad=false"]),
     ("fem_condense.cu", "fem_condense.o", []),
+    ("fem_jit.cu", "fem_jit.o", ["-I", OUT_DIR]),
 ]
+
+# headers the run-time compiler of form programs needs, embedded as text
+JIT_SOURCES = [("kJitCoreSrc", os.path.join(CSRC, "fem_faithful_core.cuh")),
+               ("kJitKernelSrc", os.path.join(CSRC, "fem_program_kernel.cuh")),
+               ("kJitAbiSrc", os.path.join(os.path.dirname(ROOT), "include", "skfem_gb300.h"))]
+
+
+def write_jit_sources():
+    out = ["// Generated by skfem_gb300/_build.py: header texts for fem_jit.cu."]
+    for name, path in JIT_SOURCES:
+        text = open(path).read()
+        if ")FEMSRC\"" in text:
+            raise RuntimeError("raw-string delimiter found in %s" % path)
+        out.append('static const char* %s = R"FEMSRC(%s)FEMSRC";' % (name, text))
+    tmp = os.path.join(OUT_DIR, "fem_jit_sources.inc.tmp")
+    open(tmp, "w").write("\n".join(out) + "\n")
+    os.replace(tmp, os.path.join(OUT_DIR, "fem_jit_sources.inc"))
 
 
 def nvcc():
@@ -60,6 +78,7 @@ def build(force=False, verbose=False):
     # gen_refquad.py and committed: regenerating them on another platform
     # could change the last bits of numpy-computed quadrature nodes.
     cc = nvcc()
+    write_jit_sources()
     units = [u for u in UNITS if os.path.exists(os.path.join(CSRC, u[0]))]
 
     def compile_unit(u):
@@ -78,7 +97,8 @@ def build(force=False, verbose=False):
             if l.strip():
                 print(l)
     tmp = LIB + ".tmp"
-    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + [os.path.join(OUT_DIR, u[1]) for u in units]
+    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + [os.path.join(OUT_DIR, u[1]) for u in units] + [
+        "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))

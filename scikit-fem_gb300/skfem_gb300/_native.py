@@ -65,7 +65,7 @@ class FemProgram(ctypes.Structure):
     _fields_ = [("ninstr", ctypes.c_int32), ("out", ctypes.c_int32), ("ncoef", ctypes.c_int32),
                 ("nq", ctypes.c_int32), ("ins", ctypes.c_void_p), ("coef", ctypes.c_void_p * 16),
                 ("coef_stride", ctypes.c_int32 * 16), ("qX", ctypes.c_void_p),
-                ("qW", ctypes.c_void_p)]
+                ("qW", ctypes.c_void_p), ("compiled", ctypes.c_void_p)]
 
 
 class FemError(RuntimeError):
@@ -115,6 +115,14 @@ _SIGS = {
     "fem_facet_interpolate": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P, _P, _P, _P]),
     "fem_assemble_to_host": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, ctypes.c_int32,
                                             _P, _P]),
+    "fem_program_compile": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                           ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                           ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
+    "fem_program_release": (None, [_P]),
+    "fem_program_source": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                          ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                          ctypes.c_int32, ctypes.c_char_p, ctypes.c_int64,
+                                          ctypes.POINTER(ctypes.c_int64)]),
     "fem_set_tuning": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "fem_assemble_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
 }

@@ -21,6 +21,7 @@ order.  Coefficients stay on the device.
 
 import ctypes
 import numbers
+import os
 
 import numpy as np
 import scipy.sparse as sp
@@ -283,14 +284,15 @@ class _GenericProgram:
             raise NotImplementedError("the form reads %d coefficient quantities (limit %d)"
                                       % (len(names), MAX_COEF))
         self.ins, self.out, self.names = ins, out, names
+        self._host = (N.FemInstr * len(ins))(*[N.FemInstr(op, a, b, 0, imm)
+                                               for op, a, b, imm in ins])
         self._dev = {}
+        self._compiled = {}
 
-    def struct(self, basis, coeffs):
+    def struct(self, basis, coeffs, kind):
         dev = self._dev.get(basis.device)
         if dev is None:
-            arr = (N.FemInstr * len(self.ins))(*[N.FemInstr(op, a, b, 0, imm)
-                                                  for op, a, b, imm in self.ins])
-            dev = torch.frombuffer(bytearray(arr), dtype=torch.uint8).to(basis.device)
+            dev = torch.frombuffer(bytearray(self._host), dtype=torch.uint8).to(basis.device)
             self._dev[basis.device] = dev
         nq = basis.X.shape[1]
         prog = N.FemProgram(len(self.ins), self.out, len(self.names), nq, dev.data_ptr())
@@ -298,7 +300,41 @@ class _GenericProgram:
             prog.coef[k], prog.coef_stride[k] = coeffs.slot(n, basis.nelems, nq)
         prog.qX = basis.X_dev.data_ptr()
         prog.qW = basis.W_dev.data_ptr()
+        prog.compiled = self._kernel(basis, kind)
         return prog
+
+    def _kernel(self, basis, kind):
+        """The program compiled to straight-line code for this basis kind
+        (once; None keeps the interpreter: compilation disabled with
+        SKFEM_GB300_JIT=0 or unavailable)."""
+        if os.environ.get("SKFEM_GB300_JIT", "1") == "0":
+            return None
+        mode = {"bilinear": 0, "linear": 1, "functional": 2}[kind]
+        facet = int(hasattr(basis, "c_facets"))
+        dim = basis.mesh.p.shape[0]
+        key = (str(basis.device), dim, int(basis.elem.vector), mode, facet)
+        if key not in self._compiled:
+            h = ctypes.c_void_p()
+            with torch.cuda.device(basis.device):
+                rc = N.lib().fem_program_compile(ctypes.addressof(self._host), len(self.ins),
+                                                 self.out, len(self.names), dim,
+                                                 int(basis.elem.vector), mode, facet,
+                                                 ctypes.byref(h))
+            if rc == N.FEM_ERR_UNSUPPORTED:
+                self._compiled[key] = None
+            else:
+                N.check(rc)
+                self._compiled[key] = h
+        h = self._compiled[key]
+        return h.value if h is not None else None
+
+    def __del__(self):
+        try:
+            for h in self._compiled.values():
+                if h is not None:
+                    N.lib().fem_program_release(h)
+        except Exception:
+            pass
 
 
 MAX_PROGRAM = 512
@@ -451,7 +487,7 @@ class BilinearForm(Form):
     # ---------------------------------------------------- generic kernels
     def _local_generic(self, basis, coeffs):
         g, key = self._generic(basis, coeffs, "bilinear")
-        prog = g.struct(basis, coeffs)
+        prog = g.struct(basis, coeffs, "bilinear")
         nb = basis.Nbfun
         local = torch.empty(max(1, basis.nelems * nb * nb), dtype=torch.float64,
                             device=basis.device)
@@ -625,7 +661,7 @@ class LinearForm(Form):
 
     def _local_generic(self, basis, coeffs):
         g, _ = self._generic(basis, coeffs, "linear")
-        prog = g.struct(basis, coeffs)
+        prog = g.struct(basis, coeffs, "linear")
         local = torch.empty(max(1, basis.nelems * basis.Nbfun), dtype=torch.float64,
                             device=basis.device)
         status = torch.zeros(1, dtype=torch.int32, device=basis.device)
@@ -671,7 +707,7 @@ class Functional(Form):
     def _device_elemental(self, basis, kwargs):
         coeffs = _Coefficients(basis, kwargs)
         g, _ = self._generic(basis, coeffs, "functional")
-        prog = g.struct(basis, coeffs)
+        prog = g.struct(basis, coeffs, "functional")
         out = torch.empty(max(1, basis.nelems), dtype=torch.float64, device=basis.device)
         status = torch.zeros(1, dtype=torch.int32, device=basis.device)
         basis._run_program("functional", prog, out, status)

@@ -180,3 +180,25 @@ def test_helpers_mul_and_trace_in_generic_forms():
     same, extra, missing, noise, rf, rm = csr_diff(K.indptr, K.indices, K.data, Ko.indptr,
                                                    Ko.indices, Ko.data, K.shape)
     assert rf <= REL_FRO and rm <= REL_MAX, (rf, rm)
+
+
+def test_compiled_programs_equal_the_interpreter(monkeypatch):
+    """Programs compiled to straight-line code (NVRTC, -fmad=false) give the
+    interpreter's local matrices, vectors and functional values bit for bit."""
+    from _facet import robin, s_energy
+    from skfem_gb300.tracer import FieldSpec  # noqa: F401
+    g = golden("tri_p2_generic")
+    b = basis_of(g, F.ElementTriP2())
+    gf = golden("tet_p1_facet")
+    fb = F.FacetBasis(F.MeshTet(gf["p"], gf["t"]), F.ElementTetP1())
+    runs = []
+    for jit in ("1", "0"):
+        monkeypatch.setenv("SKFEM_GB300_JIT", jit)
+        runs.append([newton.elemental_torch(b, s=g["s"]).cpu().numpy(),
+                     qp_coef.elemental_torch(b, c=g["c"]).cpu().numpy(),
+                     energy.elemental(b, s=g["s"]),
+                     robin.elemental_torch(fb).cpu().numpy(),
+                     s_energy.elemental(fb, s=gf["s"]),
+                     newton_res.assemble(b, s=g["s"])])
+    for a, c in zip(*runs):
+        np.testing.assert_array_equal(a, c)
