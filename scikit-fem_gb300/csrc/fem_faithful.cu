@@ -90,57 +90,74 @@ __global__ void program_kernel(FemMesh m, FemBasis b, FemFacets fc, FemProgram p
   program_body<D, MODE, FACET>(m, b, fc, prog, rule, s, ncells, out, status);
 }
 
-// Basis.interpolate, one cell (or facet) per thread, its points in turn:
-// quantity k of the field, out[(k * ncells + e) * nq + q] =
-// 0*(w0 phi_0) + sum_i w_i phi_i in local-function order
-// (abstract_basis.py:295-304).  FACET: at the facet points, with the basis
-// of the cell f2t[side].
+// Basis.interpolate: a block takes CPB cells (or facets); stage 0 stages
+// each cell's affine map and DOF values in shared memory, stage 1 gives one
+// (cell, point) pair per thread: quantity k of the field,
+// out[(k * ncells + e) * nq + q] = 0*(w0 phi_0) + sum_i w_i phi_i in
+// local-function order (abstract_basis.py:295-304).  FACET: at the facet
+// points, with the basis of the cell f2t[side].
 template <int D, bool FACET>
 __global__ void interpolate_kernel(FemMesh m, FemBasis b, FemFacets fc, Rule rule, int64_t ncells,
-                                   const double* __restrict__ w, double* __restrict__ out,
+                                   int cpb, const double* __restrict__ w, double* __restrict__ out,
                                    int32_t* __restrict__ status) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= ncells) return;
+  extern __shared__ double ism[];
   const bool vec = b.vector != 0;
   const bool hex = b.family == FEM_HEX_1;
-  const int64_t ec = FACET ? (int64_t)fc.tind[e] : e;   // the cell whose DOFs are read
-  if (FACET && (ec < 0 || ec >= m.nelems)) {
+  const bool maps = !FACET && !hex;
+  const int nb = b.nbfun;
+  const int per = kCell + nb;           // per cell: affine map, DOF values
+  const int64_t e0 = (int64_t)blockIdx.x * cpb;
+  for (int k = threadIdx.x; k < cpb; k += blockDim.x) {
+    const int64_t e = e0 + k;
+    if (e >= ncells) continue;
+    double* S = ism + (size_t)k * per;
+    const int64_t ec = FACET ? (int64_t)fc.tind[e] : e;   // the cell whose DOFs are read
+    if (ec < 0 || ec >= m.nelems) {
+      if (status) atomicOr(status, 1 << FEM_ERR_ARGUMENT);
+      for (int i = 0; i < nb; ++i) S[kCell + i] = 0.0;
+      continue;
+    }
+    if (maps) {
+      CellGeo cg;
+      cell_geometry<D>(m, e, false, cg);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          S[i * 3 + j] = cg.inv[i][j];
+          S[10 + i * 3 + j] = cg.A[i][j];
+        }
+      S[9] = cg.det;
+      for (int i = 0; i < 3; ++i) S[19 + i] = cg.x0[i];
+    }
+    for (int i = 0; i < nb; ++i) S[kCell + i] = w[b.element_dofs[(int64_t)i * m.nelems + ec]];
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  const int k = t / rule.nq, q = t - k * rule.nq;
+  const int64_t e = e0 + k;
+  if (k >= cpb || e >= ncells) return;
+  const double* S = ism + (size_t)k * per;
+  if (FACET) {
+    const int64_t ec = fc.tind[e];
+    if (ec < 0 || ec >= m.nelems) return;
+  }
+  PointGeo g;
+  double Y[3];
+  if (!geometry_at<D, FACET>(m, b, fc, rule, ProgFlags(), e, q, Y, g, maps ? S : nullptr)) {
     if (status) atomicOr(status, 1 << FEM_ERR_ARGUMENT);
     return;
   }
-  double cell[kCell];
-  if (!FACET && !hex) {
-    CellGeo c;
-    cell_geometry<D>(m, e, false, c);
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        cell[i * 3 + j] = c.inv[i][j];
-        cell[10 + i * 3 + j] = c.A[i][j];
-      }
-    cell[9] = c.det;
-    for (int i = 0; i < 3; ++i) cell[19 + i] = c.x0[i];
-  }
   constexpr int NQ = D + D * D;
   const int nquant = vec ? D + D * D : 1 + D;
-  const double w0 = w[b.element_dofs[ec]];
-  for (int q = 0; q < rule.nq; ++q) {
-    PointGeo g;
-    double Y[3];
-    if (!geometry_at<D, FACET>(m, b, fc, rule, ProgFlags(), e, q, Y, g,
-                               (!FACET && !hex) ? cell : nullptr)) {
-      if (status) atomicOr(status, 1 << FEM_ERR_ARGUMENT);
-      return;
-    }
-    double acc[NQ], qq[NQ];
-    quantities<D>(b.family, vec, 0, Y[0], Y[1], Y[2], g.inv, qq);
-    for (int k = 0; k < nquant; ++k) acc[k] = 0.0 * (w0 * qq[k]);
-    for (int i = 0; i < b.nbfun; ++i) {
-      const double wi = w[b.element_dofs[(int64_t)i * m.nelems + ec]];
-      quantities<D>(b.family, vec, i, Y[0], Y[1], Y[2], g.inv, qq);
-      for (int k = 0; k < nquant; ++k) acc[k] = acc[k] + wi * qq[k];
-    }
-    for (int k = 0; k < nquant; ++k) out[((int64_t)k * ncells + e) * rule.nq + q] = acc[k];
+  double acc[NQ], qq[NQ];
+  const double w0 = S[kCell];
+  quantities<D>(b.family, vec, 0, Y[0], Y[1], Y[2], g.inv, qq);
+  for (int a = 0; a < nquant; ++a) acc[a] = 0.0 * (w0 * qq[a]);
+  for (int i = 0; i < nb; ++i) {
+    const double wi = S[kCell + i];
+    quantities<D>(b.family, vec, i, Y[0], Y[1], Y[2], g.inv, qq);
+    for (int a = 0; a < nquant; ++a) acc[a] = acc[a] + wi * qq[a];
   }
+  for (int a = 0; a < nquant; ++a) out[((int64_t)a * ncells + e) * rule.nq + q] = acc[a];
 }
 
 // numpy's pairwise sum of n doubles (np.sum of a contiguous vector): the
@@ -303,6 +320,7 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets*
   s.nquant = b.vector ? m.dim + m.dim * m.dim : 1 + m.dim;
   s.cells = !fc && b.family != FEM_HEX_1;
   s.quants = mode != 2;   // a functional reads no basis function
+  s.npoint = prog.compiled ? prog.compiled->npoint : 0;
   auto bytes = [&](int epb) {
     fem_faithful::GenericLayout t = s;
     t.epb = epb;
@@ -381,14 +399,18 @@ int interpolate(const FemMesh& m, const FemBasis& b, const FemFacets* fc, int nq
   if (ncells == 0) return 0;
   const fem_faithful::Rule rule{X, nullptr, nq};
   const FemFacets F = fc ? *fc : FemFacets{};
-  const unsigned grid = (unsigned)ceil_div(ncells, 128);
+  // one (cell, point) pair per thread: blocks of cpb cells x nq points
+  const int cpb = std::max(1, 128 / nq);
+  const int threads = cpb * nq;
+  const size_t smem = (size_t)cpb * (fem_faithful::kCell + b.nbfun) * sizeof(double);
+  const unsigned grid = (unsigned)ceil_div(ncells, cpb);
   using namespace fem_faithful;
   if (m.dim == 2) {
-    if (fc) interpolate_kernel<2, true><<<grid, 128, 0, st>>>(m, b, F, rule, ncells, w, out, status);
-    else interpolate_kernel<2, false><<<grid, 128, 0, st>>>(m, b, F, rule, ncells, w, out, status);
+    if (fc) interpolate_kernel<2, true><<<grid, threads, smem, st>>>(m, b, F, rule, ncells, cpb, w, out, status);
+    else interpolate_kernel<2, false><<<grid, threads, smem, st>>>(m, b, F, rule, ncells, cpb, w, out, status);
   } else {
-    if (fc) interpolate_kernel<3, true><<<grid, 128, 0, st>>>(m, b, F, rule, ncells, w, out, status);
-    else interpolate_kernel<3, false><<<grid, 128, 0, st>>>(m, b, F, rule, ncells, w, out, status);
+    if (fc) interpolate_kernel<3, true><<<grid, threads, smem, st>>>(m, b, F, rule, ncells, cpb, w, out, status);
+    else interpolate_kernel<3, false><<<grid, threads, smem, st>>>(m, b, F, rule, ncells, cpb, w, out, status);
   }
   FEM_LAUNCH_CHECK("interpolate kernel");
   return 0;

@@ -68,17 +68,11 @@ std::string dbl(double v) {
   return buf;
 }
 
-// The program as straight-line code; the caller has validated operands.
-std::string program_source(const FemInstr* ins, int n, int out) {
-  std::string s;
-  s += "__device__ __forceinline__ double jit_form(const double* qu, const double* qv, "
-       "const double* cq, const double* qx) {\n";
-  char line[256];
-  for (int k = 0; k < n; ++k) {
-    const FemInstr& I = ins[k];
-    std::string rhs;
-    auto r = [](int i) { return "r" + std::to_string(i); };
-    switch (I.op) {
+// Right-hand side of instruction k.
+std::string rhs_of(const FemInstr& I) {
+  std::string rhs;
+  auto r = [](int i) { return "r" + std::to_string(i); };
+  switch (I.op) {
       case fem_faithful::OP_CONST: rhs = dbl(I.imm); break;
       case fem_faithful::OP_U: rhs = "qu[" + std::to_string(I.a) + "]"; break;
       case fem_faithful::OP_V: rhs = "qv[" + std::to_string(I.a) + "]"; break;
@@ -102,9 +96,81 @@ std::string program_source(const FemInstr* ins, int n, int out) {
       case fem_faithful::OP_POW: rhs = "pow(" + r(I.a) + ", " + r(I.b) + ")"; break;
       case fem_faithful::OP_N: rhs = "qx[" + std::to_string(4 + I.a) + "]"; break;
       default: rhs = "0.0";
+  }
+  return rhs;
+}
+
+bool binary(int op) {
+  using namespace fem_faithful;
+  return op == OP_ADD || op == OP_SUB || op == OP_MUL || op == OP_DIV || op == OP_POW;
+}
+bool unary(int op) {
+  using namespace fem_faithful;
+  return op == OP_NEG || op == OP_SQRT || op == OP_EXP || op == OP_LOG || op == OP_SIN ||
+         op == OP_COS || op == OP_TAN || op == OP_TANH || op == OP_ARCTAN || op == OP_ABS;
+}
+
+// The program as straight-line code; the caller has validated operands.
+// hoist: split it into jit_point (instructions that depend on neither u
+// nor v, once per point, their values needed later stored in P) and
+// jit_form_hoisted (the rest, reading P); *npoint receives |P|.
+std::string program_source(const FemInstr* ins, int n, int out, bool hoist, int* npoint) {
+  std::string s;
+  char line[256];
+  *npoint = 0;
+  if (!hoist) {
+    s += "__device__ __forceinline__ double jit_form(const double* qu, const double* qv, "
+         "const double* cq, const double* qx) {\n";
+    for (int k = 0; k < n; ++k) {
+      std::snprintf(line, sizeof line, "  const double r%d = ", k);
+      s += line + rhs_of(ins[k]) + ";\n";
     }
+    s += "  return r" + std::to_string(out) + ";\n}\n";
+    return s;
+  }
+  std::vector<char> dep(n, 0), need(n, 0);
+  for (int k = 0; k < n; ++k) {
+    const FemInstr& I = ins[k];
+    if (I.op == fem_faithful::OP_U || I.op == fem_faithful::OP_V) dep[k] = 1;
+    else if (binary(I.op)) dep[k] = dep[I.a] | dep[I.b];
+    else if (unary(I.op)) dep[k] = dep[I.a];
+  }
+  for (int k = 0; k < n; ++k) {
+    const FemInstr& I = ins[k];
+    if (!dep[k]) continue;
+    if (binary(I.op)) {
+      if (!dep[I.a]) need[I.a] = 1;
+      if (!dep[I.b]) need[I.b] = 1;
+    } else if (unary(I.op) && !dep[I.a]) {
+      need[I.a] = 1;
+    }
+  }
+  if (!dep[out]) need[out] = 1;
+  std::vector<int> slot(n, -1);
+  for (int k = 0; k < n; ++k)
+    if (need[k]) slot[k] = (*npoint)++;
+  s += "__device__ __forceinline__ void jit_point(const double* cq, const double* qx, "
+       "double* P) {\n";
+  for (int k = 0; k < n; ++k) {
+    if (dep[k]) continue;
     std::snprintf(line, sizeof line, "  const double r%d = ", k);
-    s += line + rhs + ";\n";
+    s += line + rhs_of(ins[k]) + ";\n";
+  }
+  for (int k = 0; k < n; ++k)
+    if (slot[k] >= 0) {
+      std::snprintf(line, sizeof line, "  P[%d] = r%d;\n", slot[k], k);
+      s += line;
+    }
+  s += "}\n__device__ __forceinline__ double jit_form_hoisted(const double* qu, "
+       "const double* qv, const double* P) {\n";
+  for (int k = 0; k < n; ++k) {
+    if (slot[k] >= 0) {
+      std::snprintf(line, sizeof line, "  const double r%d = P[%d];\n", k, slot[k]);
+      s += line;
+    } else if (dep[k]) {
+      std::snprintf(line, sizeof line, "  const double r%d = ", k);
+      s += line + rhs_of(ins[k]) + ";\n";
+    }
   }
   s += "  return r" + std::to_string(out) + ";\n}\n";
   return s;
@@ -112,7 +178,7 @@ std::string program_source(const FemInstr* ins, int n, int out) {
 
 // The complete source compiled for a program (headers by name).
 int kernel_source(const FemInstr* ins, int ninstr, int out, int ncoef, int dim, int vector,
-                  int mode, int facet, std::string& src);
+                  int mode, int facet, std::string& src, int* npoint);
 
 }  // namespace
 
@@ -133,7 +199,7 @@ int jit_launch(const FemCompiled* k, dim3 grid, dim3 block, size_t smem, cudaStr
 
 namespace {
 int kernel_source(const FemInstr* ins, int ninstr, int out, int ncoef, int dim, int vector,
-                  int mode, int facet, std::string& src) {
+                  int mode, int facet, std::string& src, int* npoint) {
   using fem::set_error;
   if (!ins || (dim != 2 && dim != 3) || mode < 0 || mode > 2 || ninstr <= 0 ||
       ninstr > fem_faithful::kMaxProgram || out < 0 || out >= ninstr || ncoef < 0 ||
@@ -144,11 +210,21 @@ int kernel_source(const FemInstr* ins, int ninstr, int out, int ncoef, int dim, 
   // operand checks (the same as the interpreter's)
   if (int rc = fem::check_instructions(ins, ninstr, ncoef, dim, vector != 0)) return rc;
   src.clear();
-  src += "namespace fem_faithful {\n__device__ __forceinline__ double jit_form(const double*, "
-         "const double*, const double*, const double*);\n}\n";
-  src += "#define FEM_FORM_EVAL(prog, qu, qv, cq, qx, R) jit_form(qu, qv, cq, qx)\n";
-  src += "#include \"fem_faithful_core.cuh\"\n#include \"fem_program_kernel.cuh\"\n";
-  src += "namespace fem_faithful {\n" + program_source(ins, ninstr, out) + "}\n";
+  // bilinear and linear forms evaluate each point's u/v-free part once;
+  // a functional has one entry per cell and runs the program whole
+  const bool hoist = mode != 2;
+  const std::string body = program_source(ins, ninstr, out, hoist, npoint);
+  if (hoist) {
+    src += "#define FEM_JIT_HOIST 1\n#include \"fem_faithful_core.cuh\"\n";
+    src += "namespace fem_faithful {\n" + body + "}\n";
+    src += "#include \"fem_program_kernel.cuh\"\n";
+  } else {
+    src += "namespace fem_faithful {\n__device__ __forceinline__ double jit_form(const double*, "
+           "const double*, const double*, const double*);\n}\n";
+    src += "#define FEM_FORM_EVAL(prog, qu, qv, cq, qx, R) jit_form(qu, qv, cq, qx)\n";
+    src += "#include \"fem_faithful_core.cuh\"\n#include \"fem_program_kernel.cuh\"\n";
+    src += "namespace fem_faithful {\n" + body + "}\n";
+  }
   char tail[512];
   std::snprintf(tail, sizeof tail,
                 "extern \"C\" __global__ void fem_jit_program(FemMesh m, FemBasis b, FemFacets fc, "
@@ -168,7 +244,9 @@ int fem_program_source(const FemInstr* ins, int32_t ninstr, int32_t out, int32_t
                        int32_t dim, int32_t vector, int32_t mode, int32_t facet, char* buf,
                        int64_t size, int64_t* needed) {
   std::string src;
-  if (int rc = kernel_source(ins, ninstr, out, ncoef, dim, vector, mode, facet, src)) return rc;
+  int npoint = 0;
+  if (int rc = kernel_source(ins, ninstr, out, ncoef, dim, vector, mode, facet, src, &npoint))
+    return rc;
   if (needed) *needed = (int64_t)src.size() + 1;
   if (buf && size > 0) {
     const size_t n = std::min<size_t>(src.size(), (size_t)size - 1);
@@ -188,7 +266,9 @@ int fem_program_compile(const FemInstr* ins, int32_t ninstr, int32_t out, int32_
   }
   *compiled = nullptr;
   std::string src;
-  if (int rc = kernel_source(ins, ninstr, out, ncoef, dim, vector, mode, facet, src)) return rc;
+  int npoint = 0;
+  if (int rc = kernel_source(ins, ninstr, out, ncoef, dim, vector, mode, facet, src, &npoint))
+    return rc;
   std::lock_guard<std::mutex> lock(g_mu);
   if (!load_nvrtc()) {
     set_error(FEM_ERR_UNSUPPORTED, "libnvrtc is not available: programs are interpreted");
@@ -225,6 +305,7 @@ int fem_program_compile(const FemInstr* ins, int32_t ninstr, int32_t out, int32_
   k->dim = dim;
   k->mode = mode;
   k->facet = facet ? 1 : 0;
+  k->npoint = npoint;
   cudaError_t e = cudaLibraryLoadData(&k->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
   if (e == cudaSuccess) e = cudaLibraryGetKernel(&k->kernel, k->lib, "fem_jit_program");
   if (e != cudaSuccess) {

@@ -11,6 +11,7 @@ struct FemCompiled {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t kernel = nullptr;
   int dim = 0, mode = 0, facet = 0;
+  int npoint = 0;                  // per-point hoisted values (GenericLayout::npoint)
   size_t smem_limit = 48 * 1024;   // dynamic shared memory the kernel is enabled for
 };
 

@@ -47,13 +47,15 @@ __device__ bool geometry_at(const FemMesh& m, const FemBasis& b, const FemFacets
 struct GenericLayout {
   int epb, L, nq, nb, nquant;
   bool cells, quants;  // per-cell affine maps staged; basis quantities staged
+  int npoint;          // compiled programs: values hoisted per point (0: none)
   __host__ __device__ size_t geo() const { return 0; }
   __host__ __device__ size_t val() const { return (size_t)epb * nq * kGeo; }
   __host__ __device__ size_t cell() const { return val() + (size_t)epb * L * nq; }
   __host__ __device__ size_t quant() const { return cell() + (cells ? (size_t)epb * kCell : 0); }
-  __host__ __device__ size_t total() const {
+  __host__ __device__ size_t point() const {
     return quant() + (quants ? (size_t)epb * nq * nb * nquant : 0);
   }
+  __host__ __device__ size_t total() const { return point() + (size_t)epb * nq * npoint; }
 };
 
 template <int D, int MODE, bool FACET>
@@ -127,6 +129,22 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
     }
     __syncthreads();
   }
+#ifdef FEM_JIT_HOIST
+  // stage 1c (compiled programs): the instructions that depend on neither
+  // the trial nor the test function, once per point
+  double* P = gsm + s.point();
+  for (int k = threadIdx.x; k < s.epb * s.nq; k += blockDim.x) {
+    const int el = k / s.nq, q = k - el * s.nq;
+    const int64_t e = e0 + el;
+    if (e >= ncells) continue;
+    double cq[kMaxCoef];
+    for (int c = 0; c < prog.ncoef && c < kMaxCoef; ++c)
+      cq[c] = prog.coef[c] ? prog.coef[c][prog.coef_stride[c] ? e * prog.coef_stride[c] + q : e]
+                           : 0.0;
+    jit_point(cq, geo + (size_t)k * kGeo + 10, P + (size_t)k * s.npoint);
+  }
+  __syncthreads();
+#endif
   // stage 2: form * dx
   double R[kMaxProgram];
   const int per = s.L * s.nq;
@@ -154,7 +172,13 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
     } else {
       for (int a = 0; a < D + D * D; ++a) qu[a] = qv[a] = 0.0;
     }
+#ifdef FEM_JIT_HOIST
+    const double fq = jit_form_hoisted(qu, qv, P + ((size_t)el * s.nq + q) * s.npoint);
+    val[k] = fq * (fabs(g.det) * rule.W[q]);
+    (void)R;
+#else
     val[k] = point_value_q(prog, e, q, qu, qv, g, rule.W[q], R);
+#endif
   }
   __syncthreads();
   for (int k = threadIdx.x; k < s.epb * s.L; k += blockDim.x) {
