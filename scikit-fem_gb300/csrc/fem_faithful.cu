@@ -33,6 +33,7 @@
 #include "fem_program_kernel.cuh"
 #include "fem_jit.h"
 
+#include <type_traits>
 #include <vector>
 
 namespace fem_faithful {
@@ -83,11 +84,11 @@ __global__ void mask_kernel(FemMesh m, FemBasis b, FemProgram prog, int nq, doub
 }
 
 // ------------------------------------------------------------ generic forms
-template <int D, int MODE, bool FACET>
+template <int D, int MODE, bool FACET, bool VEC>
 __global__ void program_kernel(FemMesh m, FemBasis b, FemFacets fc, FemProgram prog, Rule rule,
                                GenericLayout s, int64_t ncells, double* __restrict__ out,
                                int32_t* __restrict__ status) {
-  program_body<D, MODE, FACET>(m, b, fc, prog, rule, s, ncells, out, status);
+  program_body<D, MODE, FACET, VEC>(m, b, fc, prog, rule, s, ncells, out, status);
 }
 
 // Basis.interpolate: a block takes CPB cells (or facets); stage 0 stages
@@ -96,12 +97,12 @@ __global__ void program_kernel(FemMesh m, FemBasis b, FemFacets fc, FemProgram p
 // out[(k * ncells + e) * nq + q] = 0*(w0 phi_0) + sum_i w_i phi_i in
 // local-function order (abstract_basis.py:295-304).  FACET: at the facet
 // points, with the basis of the cell f2t[side].
-template <int D, bool FACET>
+template <int D, bool FACET, bool VEC>
 __global__ void interpolate_kernel(FemMesh m, FemBasis b, FemFacets fc, Rule rule, int64_t ncells,
                                    int cpb, const double* __restrict__ w, double* __restrict__ out,
                                    int32_t* __restrict__ status) {
   extern __shared__ double ism[];
-  const bool vec = b.vector != 0;
+  constexpr bool vec = VEC;
   const bool hex = b.family == FEM_HEX_1;
   const bool maps = !FACET && !hex;
   const int nb = b.nbfun;
@@ -147,16 +148,19 @@ __global__ void interpolate_kernel(FemMesh m, FemBasis b, FemFacets fc, Rule rul
     return;
   }
   constexpr int NQ = D + D * D;
-  const int nquant = vec ? D + D * D : 1 + D;
+  constexpr int nquant = VEC ? D + D * D : 1 + D;
   double acc[NQ], qq[NQ];
   const double w0 = S[kCell];
   quantities<D>(b.family, vec, 0, Y[0], Y[1], Y[2], g.inv, qq);
+#pragma unroll
   for (int a = 0; a < nquant; ++a) acc[a] = 0.0 * (w0 * qq[a]);
   for (int i = 0; i < nb; ++i) {
     const double wi = S[kCell + i];
     quantities<D>(b.family, vec, i, Y[0], Y[1], Y[2], g.inv, qq);
+#pragma unroll
     for (int a = 0; a < nquant; ++a) acc[a] = acc[a] + wi * qq[a];
   }
+#pragma unroll
   for (int a = 0; a < nquant; ++a) out[((int64_t)a * ncells + e) * rule.nq + q] = acc[a];
 }
 
@@ -367,21 +371,19 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets*
     return 0;
   };
   using namespace fem_faithful;
-  if (fc) {
+  // <dim, mode, facet, vector> instantiations
+  auto pick = [&](auto facet_tag, auto vec_tag) -> int {
+    constexpr bool FC = decltype(facet_tag)::value, VC = decltype(vec_tag)::value;
     if (m.dim == 2)
-      rc = mode == 0 ? go(program_kernel<2, 0, true>) : mode == 1 ? go(program_kernel<2, 1, true>)
-                                                                  : go(program_kernel<2, 2, true>);
-    else
-      rc = mode == 0 ? go(program_kernel<3, 0, true>) : mode == 1 ? go(program_kernel<3, 1, true>)
-                                                                  : go(program_kernel<3, 2, true>);
-  } else {
-    if (m.dim == 2)
-      rc = mode == 0 ? go(program_kernel<2, 0, false>) : mode == 1 ? go(program_kernel<2, 1, false>)
-                                                                   : go(program_kernel<2, 2, false>);
-    else
-      rc = mode == 0 ? go(program_kernel<3, 0, false>) : mode == 1 ? go(program_kernel<3, 1, false>)
-                                                                   : go(program_kernel<3, 2, false>);
-  }
+      return mode == 0 ? go(program_kernel<2, 0, FC, VC>)
+                       : mode == 1 ? go(program_kernel<2, 1, FC, VC>) : go(program_kernel<2, 2, FC, VC>);
+    return mode == 0 ? go(program_kernel<3, 0, FC, VC>)
+                     : mode == 1 ? go(program_kernel<3, 1, FC, VC>) : go(program_kernel<3, 2, FC, VC>);
+  };
+  using T = std::true_type;
+  using Fl = std::false_type;
+  if (fc) rc = b.vector ? pick(T{}, T{}) : pick(T{}, Fl{});
+  else rc = b.vector ? pick(Fl{}, T{}) : pick(Fl{}, Fl{});
   if (rc) return rc;
   FEM_LAUNCH_CHECK("program kernel");
   return 0;
@@ -405,12 +407,14 @@ int interpolate(const FemMesh& m, const FemBasis& b, const FemFacets* fc, int nq
   const size_t smem = (size_t)cpb * (fem_faithful::kCell + b.nbfun) * sizeof(double);
   const unsigned grid = (unsigned)ceil_div(ncells, cpb);
   using namespace fem_faithful;
+  auto go = [&](auto kern) { kern<<<grid, threads, smem, st>>>(m, b, F, rule, ncells, cpb, w, out, status); };
+  const bool v = b.vector != 0;
   if (m.dim == 2) {
-    if (fc) interpolate_kernel<2, true><<<grid, threads, smem, st>>>(m, b, F, rule, ncells, cpb, w, out, status);
-    else interpolate_kernel<2, false><<<grid, threads, smem, st>>>(m, b, F, rule, ncells, cpb, w, out, status);
+    if (fc) v ? go(interpolate_kernel<2, true, true>) : go(interpolate_kernel<2, true, false>);
+    else v ? go(interpolate_kernel<2, false, true>) : go(interpolate_kernel<2, false, false>);
   } else {
-    if (fc) interpolate_kernel<3, true><<<grid, threads, smem, st>>>(m, b, F, rule, ncells, cpb, w, out, status);
-    else interpolate_kernel<3, false><<<grid, threads, smem, st>>>(m, b, F, rule, ncells, cpb, w, out, status);
+    if (fc) v ? go(interpolate_kernel<3, true, true>) : go(interpolate_kernel<3, true, false>);
+    else v ? go(interpolate_kernel<3, false, true>) : go(interpolate_kernel<3, false, false>);
   }
   FEM_LAUNCH_CHECK("interpolate kernel");
   return 0;

@@ -230,9 +230,9 @@ int kernel_source(const FemInstr* ins, int ninstr, int out, int ncoef, int dim, 
                 "extern \"C\" __global__ void fem_jit_program(FemMesh m, FemBasis b, FemFacets fc, "
                 "FemProgram prog, fem_faithful::Rule rule, fem_faithful::GenericLayout s, "
                 "int64_t ncells, double* out, int32_t* status) {\n"
-                "  fem_faithful::program_body<%d, %d, %s>(m, b, fc, prog, rule, s, ncells, out, "
-                "status);\n}\n",
-                dim, mode, facet ? "true" : "false");
+                "  fem_faithful::program_body<%d, %d, %s, %s>(m, b, fc, prog, rule, s, ncells, "
+                "out, status);\n}\n",
+                dim, mode, facet ? "true" : "false", vector ? "true" : "false");
   src += tail;
   return 0;
 }

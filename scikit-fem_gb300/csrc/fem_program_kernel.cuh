@@ -58,7 +58,7 @@ struct GenericLayout {
   __host__ __device__ size_t total() const { return point() + (size_t)epb * nq * npoint; }
 };
 
-template <int D, int MODE, bool FACET>
+template <int D, int MODE, bool FACET, bool VEC>
 __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b,
                                              const FemFacets& fc, const FemProgram& prog,
                                              const Rule& rule, const GenericLayout& s,
@@ -70,10 +70,11 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
   double* cgeo = gsm + s.cell();
   double* Q = gsm + s.quant();
   const bool hex = b.family == FEM_HEX_1;
-  const bool vec = b.vector != 0;
+  constexpr bool vec = VEC;
+  constexpr int NQ = VEC ? D + D * D : 1 + D;   // quantities per basis function
   const ProgFlags f = prog_flags(prog);
   const int64_t e0 = (int64_t)blockIdx.x * s.epb;
-  const int nb = b.nbfun, NQ = s.nquant;
+  const int nb = b.nbfun;
   // stage 0: affine cell maps (9 divisions each), once per cell
   if (s.cells) {
     for (int el = threadIdx.x; el < s.epb; el += blockDim.x) {
@@ -125,6 +126,7 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
         for (int c = 0; c < 3; ++c) inv[a][c] = G[a * 3 + c];
       double qq[D + D * D];
       quantities<D>(b.family, vec, fn, G[17], G[18], G[19], inv, qq);
+#pragma unroll
       for (int a = 0; a < NQ; ++a) Q[(size_t)k * NQ + a] = qq[a];
     }
     __syncthreads();
@@ -138,9 +140,11 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
     const int64_t e = e0 + el;
     if (e >= ncells) continue;
     double cq[kMaxCoef];
-    for (int c = 0; c < prog.ncoef && c < kMaxCoef; ++c)
-      cq[c] = prog.coef[c] ? prog.coef[c][prog.coef_stride[c] ? e * prog.coef_stride[c] + q : e]
-                           : 0.0;
+#pragma unroll
+    for (int c = 0; c < kMaxCoef; ++c)
+      cq[c] = (c < prog.ncoef && prog.coef[c])
+                  ? prog.coef[c][prog.coef_stride[c] ? e * prog.coef_stride[c] + q : e]
+                  : 0.0;
     jit_point(cq, geo + (size_t)k * kGeo + 10, P + (size_t)k * s.npoint);
   }
   __syncthreads();
@@ -165,12 +169,14 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
     double qu[D + D * D], qv[D + D * D];
     if (s.quants) {
       const double* Qp = Q + ((size_t)(el * s.nq + q) * nb) * NQ;
+#pragma unroll
       for (int a = 0; a < NQ; ++a) {
         qu[a] = Qp[(size_t)j * NQ + a];
         qv[a] = Qp[(size_t)i * NQ + a];
       }
     } else {
-      for (int a = 0; a < D + D * D; ++a) qu[a] = qv[a] = 0.0;
+#pragma unroll
+      for (int a = 0; a < NQ; ++a) qu[a] = qv[a] = 0.0;
     }
 #ifdef FEM_JIT_HOIST
     const double fq = jit_form_hoisted(qu, qv, P + ((size_t)el * s.nq + q) * s.npoint);
