@@ -284,6 +284,18 @@ int fem_assemble_to_host(const FemMesh* mesh, const FemBasis* basis, const FemBi
                          double* host_values, int32_t* status, int32_t nchunks,
                          fem_stream_t stream, fem_stream_t copy_stream);
 
+/* The two halves of fem_assemble_to_host, for callers that pipeline the
+ * coefficients' upload with the local kernel: local matrices of the cells
+ * [cell_begin, cell_end) into staging (with the coefficient and
+ * stale-pattern checks of fem_assemble), then the row-range sum streamed to
+ * host_values. */
+int fem_assemble_local(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
+                       const FemPattern* pat, double* staging, int32_t* status, int64_t cell_begin,
+                       int64_t cell_end, fem_stream_t stream);
+int fem_csr_sum_to_host(const FemPattern* pat, const double* staging, double* csr_values,
+                        double* host_values, int32_t nchunks, fem_stream_t stream,
+                        fem_stream_t copy_stream);
+
 int fem_csr_sum(const FemPattern* pat, const double* local, double* csr_values, int32_t* status,
                 fem_stream_t stream);
 

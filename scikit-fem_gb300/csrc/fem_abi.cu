@@ -11,8 +11,10 @@
 namespace fem_fast {
 int local_matrices(const FemMesh&, const FemBasis&, const FemBilinear&, double*, int32_t*,
                    cudaStream_t);
+// cells [ebeg, eend) only (eend < 0: to the last cell)
 int local_matrices_checked(const FemMesh&, const FemBasis&, const FemBilinear&, double*,
-                           const uint8_t*, int32_t*, cudaStream_t);
+                           const uint8_t*, int32_t*, cudaStream_t, int64_t ebeg = 0,
+                           int64_t eend = -1);
 int local_vectors(const FemMesh&, const FemBasis&, const FemLinear&, double*, int32_t*,
                   cudaStream_t);
 }  // namespace fem_fast
@@ -373,26 +375,44 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
   return fem::csr_sum(P, staging, csr_values, st);
 }
 
-int fem_assemble_to_host(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
-                         const FemPattern* pat, double* staging, double* csr_values,
-                         double* host_values, int32_t* status, int32_t nchunks,
-                         fem_stream_t stream, fem_stream_t copy_stream) {
+int fem_assemble_local(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
+                       const FemPattern* pat, double* staging, int32_t* status, int64_t cell_begin,
+                       int64_t cell_end, fem_stream_t stream) {
   int rc = validate(mesh, basis);
   if (rc) return rc;
-  if (!form || !pat || !staging || !csr_values || !host_values || nchunks < 1 || nchunks > 64) {
-    set_error(FEM_ERR_ARGUMENT, "null form, pattern or buffer, or chunks outside 1..64");
+  if (!form || !pat || !staging) {
+    set_error(FEM_ERR_ARGUMENT, "null form, pattern or staging");
     return FEM_ERR_ARGUMENT;
   }
   if (pat->P.nelems != mesh->nelems || pat->P.nbfun_v != basis->nbfun || !pat->P.has_matrix) {
     set_error(FEM_ERR_ARGUMENT, "pattern does not belong to this mesh / basis");
     return FEM_ERR_ARGUMENT;
   }
+  if (cell_begin < 0 || cell_end > mesh->nelems || cell_end < cell_begin) {
+    set_error(FEM_ERR_ARGUMENT, "cell range [%lld, %lld) outside [0, %lld)",
+              (long long)cell_begin, (long long)cell_end, (long long)mesh->nelems);
+    return FEM_ERR_ARGUMENT;
+  }
+  if (cell_end == cell_begin) return 0;
+  return fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
+                                          status ? pat->coef_bits : nullptr, status,
+                                          (cudaStream_t)stream, cell_begin, cell_end);
+}
+
+int fem_csr_sum_to_host(const FemPattern* pat, const double* staging, double* csr_values,
+                        double* host_values, int32_t nchunks, fem_stream_t stream,
+                        fem_stream_t copy_stream) {
+  if (!pat || !staging || !csr_values || !host_values || nchunks < 1 || nchunks > 64) {
+    set_error(FEM_ERR_ARGUMENT, "null pattern or buffer, or chunks outside 1..64");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (!pat->P.has_matrix) {
+    set_error(FEM_ERR_ARGUMENT, "pattern has no CSR structure");
+    return FEM_ERR_ARGUMENT;
+  }
   cudaStream_t st = (cudaStream_t)stream, cs = (cudaStream_t)copy_stream;
-  rc = fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
-                                        status ? pat->coef_bits : nullptr, status, st);
-  if (rc) return rc;
   fem::Pattern P = pat->P;
-  P.sum_unroll = fem::tuning_for(basis->family).sum_unroll;
+  P.sum_unroll = fem::tuning_for(pat->family).sum_unroll;
   // row ranges of about equal nnz, cut with the pattern's host copy of indptr
   const std::vector<int32_t>& ip = pat->host_indptr;
   if ((int64_t)ip.size() != P.nrows + 1) {
@@ -406,7 +426,7 @@ int fem_assemble_to_host(const FemMesh* mesh, const FemBasis* basis, const FemBi
         ? P.nrows
         : (int64_t)(std::upper_bound(ip.begin() + row, ip.end(), (int32_t)target) - ip.begin()) - 1;
     if (row1 <= row) row1 = std::min<int64_t>(P.nrows, row + 1);
-    rc = fem::csr_sum(P, staging, csr_values, st, row, row1);
+    int rc = fem::csr_sum(P, staging, csr_values, st, row, row1);
     if (rc) return rc;
     const int64_t a = ip[row], b = ip[row1];
     if (b > a) {
@@ -421,6 +441,19 @@ int fem_assemble_to_host(const FemMesh* mesh, const FemBasis* basis, const FemBi
     row = row1;
   }
   return 0;
+}
+
+int fem_assemble_to_host(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
+                         const FemPattern* pat, double* staging, double* csr_values,
+                         double* host_values, int32_t* status, int32_t nchunks,
+                         fem_stream_t stream, fem_stream_t copy_stream) {
+  if (!mesh) {
+    set_error(FEM_ERR_ARGUMENT, "null mesh");
+    return FEM_ERR_ARGUMENT;
+  }
+  int rc = fem_assemble_local(mesh, basis, form, pat, staging, status, 0, mesh->nelems, stream);
+  if (rc) return rc;
+  return fem_csr_sum_to_host(pat, staging, csr_values, host_values, nchunks, stream, copy_stream);
 }
 
 int fem_csr_sum(const FemPattern* pat, const double* local, double* csr_values, int32_t* status,

@@ -172,16 +172,17 @@ template <int D, int ORDER, int BS>
 __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBilinear f,
                                                                 double* __restrict__ out,
                                                                 const uint8_t* __restrict__ ref_bits,
-                                                                int32_t* __restrict__ status) {
+                                                                int32_t* __restrict__ status,
+                                                                int64_t ebeg, int64_t eend) {
   constexpr int NB = SimplexTraits<D, ORDER>::NB;
   constexpr int L = NB * NB;
   constexpr double INV_FACT = 1.0 / SimplexTraits<D, ORDER>::FACT;
   extern __shared__ double smem[];
   // grid-stride over element tiles of BS cells (persistent when the grid is
   // smaller than the number of tiles)
-  for (int64_t e0 = (int64_t)blockIdx.x * BS; e0 < m.nelems; e0 += (int64_t)gridDim.x * BS) {
+  for (int64_t e0 = ebeg + (int64_t)blockIdx.x * BS; e0 < eend; e0 += (int64_t)gridDim.x * BS) {
   const int64_t e = e0 + threadIdx.x;
-  if (e < m.nelems) {
+  if (e < eend) {
     check_coef_bits(f, e, ref_bits, status);
     Simplex<D> s;
     simplex_geometry<D>(m, e, s);
@@ -221,7 +222,7 @@ __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBiline
 #undef KS
 #undef KM
   }
-  flush_rows<L, BS>(smem, out, e0, m.nelems);
+  flush_rows<L, BS>(smem, out, e0, eend);
   }
 }
 
@@ -235,7 +236,8 @@ template <int D, int ORDER>
 __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBilinear f,
                                                             double* __restrict__ out,
                                                             const uint8_t* __restrict__ ref_bits,
-                                                            int32_t* __restrict__ status) {
+                                                            int32_t* __restrict__ status,
+                                                            int64_t ebeg, int64_t eend) {
   constexpr int BS = 64;
   constexpr int NS = SimplexTraits<D, ORDER>::NB;  // scalar functions
   constexpr int NB = NS * D;                        // vector functions
@@ -244,10 +246,10 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
   constexpr double FACT = SimplexTraits<D, ORDER>::FACT;
   extern __shared__ double smem[];
   double* rows = smem;                               // [BS][RB+1]
-  const int64_t e0 = (int64_t)blockIdx.x * BS;
+  const int64_t e0 = ebeg + (int64_t)blockIdx.x * BS;
   const int64_t e = e0 + threadIdx.x;
   const int tid = threadIdx.x;
-  const bool live = e < m.nelems;
+  const bool live = e < eend;
   double sm = 0.0;
   // E[p][q][a][b] for p <= q, kept in registers: every index below is a
   // compile-time constant once the block loops are unrolled.
@@ -339,7 +341,7 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
     }
     // stream rows (i*D .. i*D+D-1) of every element of the block
     __syncthreads();
-    const int64_t nb = ((m.nelems - e0) < (int64_t)BS ? (m.nelems - e0) : (int64_t)BS);
+    const int64_t nb = ((eend - e0) < (int64_t)BS ? (eend - e0) : (int64_t)BS);
     for (int64_t g = threadIdx.x; g < nb * RB; g += blockDim.x) {
       const int el = (int)(g / RB);
       const int k = (int)(g - (int64_t)el * RB);
@@ -436,12 +438,13 @@ __device__ __forceinline__ void hex_shape(double x, double y, double z, double p
 __global__ void __launch_bounds__(kBlock) hex_scalar_kernel(FemMesh m, FemBilinear f,
                                                             double* __restrict__ out,
                                                             const uint8_t* __restrict__ ref_bits,
-                                                            int32_t* __restrict__ status) {
+                                                            int32_t* __restrict__ status,
+                                                            int64_t ebeg, int64_t eend) {
   constexpr int L = 64;
   extern __shared__ double smem[];
-  const int64_t e0 = (int64_t)blockIdx.x * kBlock;
+  const int64_t e0 = ebeg + (int64_t)blockIdx.x * kBlock;
   const int64_t e = e0 + threadIdx.x;
-  if (e < m.nelems) {
+  if (e < eend) {
     check_coef_bits(f, e, ref_bits, status);
     Hex h;
     hex_load(m, e, h);
@@ -521,7 +524,7 @@ __global__ void __launch_bounds__(kBlock) hex_scalar_kernel(FemMesh m, FemBiline
         for (int j = 0; j < i; ++j) row[i * 8 + j] = row[j * 8 + i];
     }
   }
-  flush_rows<L>(smem, out, e0, m.nelems);
+  flush_rows<L>(smem, out, e0, eend);
 }
 
 // ------------------------------------------------------------ load vectors
@@ -625,45 +628,51 @@ static int set_smem(K kernel, size_t bytes) {
 template <int D, int O, int BS>
 static int launch_scalar(const FemMesh& m, const FemBilinear& f, double* out,
                          const uint8_t* ref_bits, int32_t* status, int persistent,
-                         cudaStream_t st) {
+                         cudaStream_t st, int64_t ebeg, int64_t eend) {
   constexpr int NB = SimplexTraits<D, O>::NB;
   const size_t sm = (size_t)BS * (NB * NB + 1) * sizeof(double);
   int rc = set_smem(simplex_scalar_kernel<D, O, BS>, sm);
   if (rc) return rc;
-  int64_t grid = fem::ceil_div(m.nelems, BS);
+  int64_t grid = fem::ceil_div(eend - ebeg, BS);
   if (persistent > 0) grid = std::min<int64_t>(grid, (int64_t)persistent * fem::num_sms());
-  simplex_scalar_kernel<D, O, BS><<<(unsigned)grid, BS, sm, st>>>(m, f, out, ref_bits, status);
+  simplex_scalar_kernel<D, O, BS><<<(unsigned)grid, BS, sm, st>>>(m, f, out, ref_bits, status,
+                                                                  ebeg, eend);
   return 0;
 }
 
 template <int D, int O>
 static int launch_scalar_tuned(const FemMesh& m, const FemBilinear& f, double* out,
-                               const uint8_t* ref_bits, int32_t* status, cudaStream_t st) {
+                               const uint8_t* ref_bits, int32_t* status, cudaStream_t st,
+                               int64_t ebeg, int64_t eend) {
   const fem::Tuning t = fem::tuning_for(D == 2 ? (O == 1 ? FEM_TRI_P1 : FEM_TRI_P2)
                                                : (O == 1 ? FEM_TET_P1 : FEM_TET_P2));
   switch (t.local_block) {
-    case 64: return launch_scalar<D, O, 64>(m, f, out, ref_bits, status, t.persistent, st);
-    case 256: return launch_scalar<D, O, 256>(m, f, out, ref_bits, status, t.persistent, st);
-    default: return launch_scalar<D, O, 128>(m, f, out, ref_bits, status, t.persistent, st);
+    case 64: return launch_scalar<D, O, 64>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend);
+    case 256: return launch_scalar<D, O, 256>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend);
+    default: return launch_scalar<D, O, 128>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend);
   }
 }
 
 int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinear& f, double* out,
-                           const uint8_t* ref_bits, int32_t* status, cudaStream_t st) {
-  if (m.nelems == 0) return 0;
+                           const uint8_t* ref_bits, int32_t* status, cudaStream_t st,
+                           int64_t ebeg, int64_t eend) {
+  if (eend < 0 || eend > m.nelems) eend = m.nelems;
+  if (ebeg < 0) ebeg = 0;
+  if (eend <= ebeg) return 0;
   const int fam = b.family;
-  const int64_t grid = fem::ceil_div(m.nelems, kBlock);
+  const int64_t grid = fem::ceil_div(eend - ebeg, kBlock);
   int rc = 0;
   if (!b.vector) {
     switch (fam) {
-      case FEM_TRI_P1: rc = launch_scalar_tuned<2, 1>(m, f, out, ref_bits, status, st); break;
-      case FEM_TRI_P2: rc = launch_scalar_tuned<2, 2>(m, f, out, ref_bits, status, st); break;
-      case FEM_TET_P1: rc = launch_scalar_tuned<3, 1>(m, f, out, ref_bits, status, st); break;
-      case FEM_TET_P2: rc = launch_scalar_tuned<3, 2>(m, f, out, ref_bits, status, st); break;
+      case FEM_TRI_P1: rc = launch_scalar_tuned<2, 1>(m, f, out, ref_bits, status, st, ebeg, eend); break;
+      case FEM_TRI_P2: rc = launch_scalar_tuned<2, 2>(m, f, out, ref_bits, status, st, ebeg, eend); break;
+      case FEM_TET_P1: rc = launch_scalar_tuned<3, 1>(m, f, out, ref_bits, status, st, ebeg, eend); break;
+      case FEM_TET_P2: rc = launch_scalar_tuned<3, 2>(m, f, out, ref_bits, status, st, ebeg, eend); break;
       case FEM_HEX_1: {
         const size_t sm = (size_t)kBlock * 65 * sizeof(double);
         if ((rc = set_smem(hex_scalar_kernel, sm))) return rc;
-        hex_scalar_kernel<<<(unsigned)grid, kBlock, sm, st>>>(m, f, out, ref_bits, status);
+        hex_scalar_kernel<<<(unsigned)grid, kBlock, sm, st>>>(m, f, out, ref_bits, status, ebeg,
+                                                              eend);
         break;
       }
       default:
@@ -672,7 +681,7 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
     }
     if (rc) return rc;
   } else {
-    const int64_t vgrid = fem::ceil_div(m.nelems, 64);
+    const int64_t vgrid = fem::ceil_div(eend - ebeg, 64);
     switch (fam) {
 #define LAUNCH_V(D, O)                                                                 \
   {                                                                                    \
@@ -680,7 +689,7 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
     constexpr int RB = D * NB;                                                         \
     const size_t sm = (size_t)64 * (RB + 1) * sizeof(double);                          \
     if ((rc = set_smem(simplex_vector_kernel<D, O>, sm))) return rc;                   \
-    simplex_vector_kernel<D, O><<<(unsigned)vgrid, 64, sm, st>>>(m, f, out, ref_bits, status);           \
+    simplex_vector_kernel<D, O><<<(unsigned)vgrid, 64, sm, st>>>(m, f, out, ref_bits, status, ebeg, eend); \
     break;                                                                             \
   }
       case FEM_TRI_P1: LAUNCH_V(2, 1)
@@ -700,7 +709,7 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
 
 int local_matrices(const FemMesh& m, const FemBasis& b, const FemBilinear& f, double* out,
                    int32_t* status, cudaStream_t st) {
-  return local_matrices_checked(m, b, f, out, nullptr, status, st);
+  return local_matrices_checked(m, b, f, out, nullptr, status, st, 0, -1);
 }
 
 int local_vectors(const FemMesh& m, const FemBasis& b, const FemLinear& f, double* out,

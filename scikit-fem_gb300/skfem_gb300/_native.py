@@ -123,6 +123,9 @@ _SIGS = {
                                           ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                           ctypes.c_int32, ctypes.c_char_p, ctypes.c_int64,
                                           ctypes.POINTER(ctypes.c_int64)]),
+    "fem_assemble_local": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_int64,
+                                          _P]),
+    "fem_csr_sum_to_host": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32, _P, _P]),
     "fem_set_tuning": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "fem_assemble_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
 }

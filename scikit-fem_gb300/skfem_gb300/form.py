@@ -60,6 +60,7 @@ class _Coefficients:
         self.dfields = {}
         self.numbers = {}
         self.strided = {}   # name -> (nelems, nqp) device copy checked inside the kernels
+        self.strided_host = {}   # name -> its host array, not yet uploaded
         self.keep = []
         dev = basis.device
         ne = basis.nelems
@@ -92,13 +93,15 @@ class _Coefficients:
                         raise ValueError("Input array has wrong size.")  # abstract_basis.py:284-285
                     self._dof_vector(k, v, basis, dim)
                     continue
-                t = torch.from_numpy(np.ascontiguousarray(v, dtype=np.float64)).to(dev)
-                if strided and tuple(t.shape) == (ne, nqp) and nqp > 1 and ne > 0:
+                if strided and v.shape == (ne, nqp) and nqp > 1 and ne > 0:
                     # the channel kernels read column 0 and check each row
-                    # is constant (FEM_ERR_VARYING), no separate pass
-                    self.strided[k] = t
+                    # is constant (FEM_ERR_VARYING), no separate pass; the
+                    # upload is left to the caller (pipelined with the kernels)
+                    self.strided[k] = torch.empty((ne, nqp), dtype=torch.float64, device=dev)
+                    self.strided_host[k] = np.ascontiguousarray(v, dtype=np.float64)
                     self.fields[k] = None
                     continue
+                t = torch.from_numpy(np.ascontiguousarray(v, dtype=np.float64)).to(dev)
             elif isinstance(v, list):
                 raise NotImplementedError("list-valued coefficients are not supported")
             else:
@@ -144,6 +147,16 @@ class _Coefficients:
             parts.append(grad.reshape((-1, ne, nqp)))
         t = torch.from_numpy(np.ascontiguousarray(np.concatenate(parts, axis=0))).to(basis.device)
         self.dfields[name] = (t, FieldSpec("field", ncomp, grad is not None))
+
+    def upload(self, begin=0, end=None, stream=None):
+        """Copy rows [begin, end) of the strided host arrays to the device."""
+        for k, t in self.strided.items():
+            h = torch.from_numpy(self.strided_host[k][begin:end])
+            if stream is None:
+                t[begin:end].copy_(h)
+            else:
+                with torch.cuda.stream(stream):
+                    t[begin:end].copy_(h, non_blocking=True)
 
     @property
     def generic(self):
@@ -405,7 +418,17 @@ class _PatternEntry:
 
 
 _SIDE = {}
+_COPY = {}
 HOST_CHUNKS = 8     # row ranges whose device->host copies overlap the segmented sum
+UPLOAD_CHUNKS = 4   # cell ranges whose coefficient uploads overlap the local kernel
+
+
+def _copy_stream(device):
+    """A per-device stream for host->device coefficient uploads."""
+    s = _COPY.get(device)
+    if s is None:
+        s = _COPY[device] = torch.cuda.Stream(device=device)
+    return s
 
 
 def _side_stream(device):
@@ -565,14 +588,22 @@ class BilinearForm(Form):
 
     def _assemble_to_host(self, ubasis, coeffs, ch):
         """Channel kernels, results copied to pinned host memory; None when
-        a per-point coefficient varies inside a cell."""
+        a per-point coefficient varies inside a cell.
+
+        Strided host coefficients are uploaded in UPLOAD_CHUNKS cell ranges
+        on a copy stream, each range's local kernel waiting only for its
+        own rows, so the upload overlaps the FP64-bound local kernel."""
         main = torch.cuda.current_stream()
+        uploaded = False
         for attempt in range(2):
             c_form = self._c_form(ubasis, coeffs, ch)
             stream = N.stream_ptr(main)
             key = ("bilinear", _structure_key(ch))
             entry = ubasis._patterns.get(key)
             if entry is None:
+                if not uploaded:
+                    coeffs.upload()
+                    uploaded = True
                 prog, keep = _program(self, ubasis, coeffs)
                 entry = _PatternEntry(ubasis, c_form, stream, prog)
                 del keep
@@ -587,13 +618,31 @@ class BilinearForm(Form):
                 indptr.copy_(entry.indptr, non_blocking=True)
             vals = torch.empty(max(entry.nnz, 1), dtype=torch.float64, device=ubasis.device)
             entry.status.zero_()
+            lib = N.lib()
+            ne = ubasis.nelems
+            if coeffs.strided and not uploaded:
+                up = _copy_stream(ubasis.device)
+                up.wait_stream(main)
+                nch = UPLOAD_CHUNKS if ne >= UPLOAD_CHUNKS * 4096 else 1
+                for c in range(nch):
+                    a, b = ne * c // nch, ne * (c + 1) // nch
+                    coeffs.upload(a, b, up)
+                    ev = torch.cuda.Event()
+                    ev.record(up)
+                    main.wait_event(ev)
+                    N.check(lib.fem_assemble_local(
+                        N.byref(ubasis.c_mesh), N.byref(ubasis.c_basis), N.byref(c_form),
+                        entry.pat.handle, N.ptr(entry.staging), N.ptr(entry.status), a, b, stream))
+                uploaded = True
+            else:
+                N.check(lib.fem_assemble_local(
+                    N.byref(ubasis.c_mesh), N.byref(ubasis.c_basis), N.byref(c_form),
+                    entry.pat.handle, N.ptr(entry.staging), N.ptr(entry.status), 0, ne, stream))
             if entry.nnz:
                 # values stream to the host range by range behind the sum
-                N.check(N.lib().fem_assemble_to_host(
-                    N.byref(ubasis.c_mesh), N.byref(ubasis.c_basis), N.byref(c_form),
+                N.check(lib.fem_csr_sum_to_host(
                     entry.pat.handle, N.ptr(entry.staging), N.ptr(vals),
-                    ctypes.c_void_p(data.data_ptr()), N.ptr(entry.status), HOST_CHUNKS,
-                    stream, N.stream_ptr(side)))
+                    ctypes.c_void_p(data.data_ptr()), HOST_CHUNKS, stream, N.stream_ptr(side)))
             st_h = torch.empty(1, dtype=torch.int32, pin_memory=True)
             st_h.copy_(entry.status, non_blocking=True)
             main.synchronize()
