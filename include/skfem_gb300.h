@@ -58,8 +58,10 @@ enum FemStatus {
   FEM_ERR_ZERO_JACOBIAN = 4, /* isoparametric detDF == 0 (mapping_isoparametric.py:195-196) */
   FEM_ERR_STALE_PATTERN = 5, /* exact-zero structure of the local matrices changed: rebuild */
   FEM_ERR_CAPACITY = 6,      /* a CSR row exceeds the per-row working-set limit */
-  FEM_ERR_VARYING = 7        /* a strided coefficient is not constant over a cell's
+  FEM_ERR_VARYING = 7,       /* a strided coefficient is not constant over a cell's
                                 points (status word only): use the generic kernels */
+  FEM_ERR_NEWTON = 8         /* the inverse isoparametric map did not converge
+                                (status word only, fem_facet_geometry) */
 };
 
 /* Element families (the reference classes they stand for). */
@@ -400,11 +402,30 @@ int fem_sum_pairwise(const double* x, int64_t n, double* out, fem_stream_t strea
  */
 typedef struct FemFacets {
   int64_t nfacets;
-  const int32_t* fverts;    /* (dim, nfacets): the facets' vertices (Mesh.facets columns) */
+  const int32_t* fverts;    /* (nfv, nfacets): the facets' vertices (Mesh.facets columns);
+                               nfv = dim for simplices, 4 for Hex1 quadrilaterals */
   const int32_t* tind;      /* (nfacets) */
   const int32_t* tind_n;    /* (nfacets) */
   const int32_t* lfacet_n;  /* (nfacets): row of t2f holding the facet in tind_n */
+  const double* geo;        /* Hex1: (nfacets, nq, 20) point geometry from
+                               fem_facet_geometry; null for simplices */
 } FemFacets;
+
+/*
+ * Hex1 FacetBasis geometry, once per basis: facet map G and detDG of the
+ * bilinear quadrilateral facet (ElementQuad1 node sums, mapping_isoparametric.py
+ * :60-110, 137-155), the cells' reference points by the reference's Newton
+ * iteration invF (:157-168: X = 0.5, dX = invDF (x - F(X)), X = clip(X + dX,
+ * 0, 1), stopped at the first iteration at which every facet's max over
+ * points of sum |dX_i| is below 1e-12 -- a count common to all facets, found
+ * by a first pass), and the normals invDF(Y0)^T N_ref / |.| of the cells
+ * f2t[0].  geo (device, nfacets * nq * 20 doubles) per point: invDF (9,
+ * row-major), detDG, x (3), h, n (3), reference point (3).  status receives
+ * 1 << FEM_ERR_NEWTON when the iteration does not converge in 50 steps.
+ */
+int fem_facet_geometry(const FemMesh* mesh, const FemBasis* basis, const FemFacets* facets,
+                       int32_t nq, const double* X, double* geo, int32_t* status,
+                       fem_stream_t stream);
 
 int fem_facet_program_local_matrices(const FemMesh* mesh, const FemBasis* basis,
                                      const FemFacets* facets, const FemProgram* program,

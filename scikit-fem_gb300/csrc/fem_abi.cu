@@ -36,6 +36,8 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets*
 int interpolate(const FemMesh& m, const FemBasis& b, const FemFacets* fc, int nq, const double* X,
                 const double* w, double* out, int32_t* status, cudaStream_t st);
 int sum_pairwise(const double* x, int64_t n, double* out, cudaStream_t st);
+int facet_geometry(const FemMesh& m, const FemBasis& b, const FemFacets& fc, int nq,
+                   const double* X, double* geo, int32_t* status, cudaStream_t st);
 int faithful_mask(const FemMesh& m, const FemBasis& b, const FemProgram& prog, int nq, double* local,
                   int32_t* status, cudaStream_t st);
 
@@ -610,6 +612,15 @@ int fem_interpolate(const FemMesh* mesh, const FemBasis* basis, int32_t nq, cons
   int rc = validate(mesh, basis);
   if (rc) return rc;
   return fem::interpolate(*mesh, *basis, nullptr, nq, X, w, out, nullptr, (cudaStream_t)stream);
+}
+
+int fem_facet_geometry(const FemMesh* mesh, const FemBasis* basis, const FemFacets* facets,
+                       int32_t nq, const double* X, double* geo, int32_t* status,
+                       fem_stream_t stream) {
+  int rc = validate(mesh, basis);
+  if (rc) return rc;
+  if ((rc = facets_given(facets))) return rc;
+  return fem::facet_geometry(*mesh, *basis, *facets, nq, X, geo, status, (cudaStream_t)stream);
 }
 
 int fem_sum_pairwise(const double* x, int64_t n, double* out, fem_stream_t stream) {

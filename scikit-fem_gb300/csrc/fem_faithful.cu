@@ -164,6 +164,26 @@ __global__ void interpolate_kernel(FemMesh m, FemBasis b, FemFacets fc, Rule rul
   for (int a = 0; a < nquant; ++a) out[((int64_t)a * ncells + e) * rule.nq + q] = acc[a];
 }
 
+// ------------------------------------------------------ Hex1 facet geometry
+__global__ void hex_facet_newton_count(FemMesh m, FemFacets fc, Rule rule, int which,
+                                       int32_t* __restrict__ kmax) {
+  const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= fc.nfacets) return;
+  atomicMax(kmax + which, hex_facet_newton_iters(m, fc, f, which, rule.X, rule.nq));
+}
+
+__global__ void hex_facet_geometry_kernel(FemMesh m, FemFacets fc, Rule rule,
+                                          const int32_t* __restrict__ kmax,
+                                          double* __restrict__ geo, int32_t* __restrict__ status) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= fc.nfacets * rule.nq) return;
+  const int64_t f = t / rule.nq;
+  const int q = (int)(t - f * rule.nq);
+  const int st = hex_facet_point(m, fc, f, q, rule.X, rule.nq, kmax[0], kmax[1],
+                                 geo + (size_t)t * kGeo);
+  if (st) atomicOr(status, st);
+}
+
 // numpy's pairwise sum of n doubles (np.sum of a contiguous vector): the
 // leaves (<= 128 values) in parallel, the combination tree by one thread.
 __global__ void pairwise_leaves_kernel(const double* __restrict__ x, int64_t n,
@@ -291,8 +311,8 @@ int faithful_mask(const FemMesh& m, const FemBasis& b, const FemProgram& prog, i
 
 static bool facets_ok(const FemMesh& m, const FemBasis& b, const FemFacets* fc) {
   if (!fc) return true;
-  if (b.family == FEM_HEX_1) {
-    set_error(FEM_ERR_UNSUPPORTED, "FacetBasis on Hex1 meshes is not implemented");
+  if (b.family == FEM_HEX_1 && !fc->geo) {
+    set_error(FEM_ERR_ARGUMENT, "Hex1 facets need their geometry (fem_facet_geometry)");
     return false;
   }
   if (fc->nfacets < 0 || (fc->nfacets > 0 && (!fc->fverts || !fc->tind || !fc->tind_n ||
@@ -308,8 +328,7 @@ static bool facets_ok(const FemMesh& m, const FemBasis& b, const FemFacets* fc) 
 // fc non-null: over the facets of a FacetBasis
 int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets* fc,
                  const FemProgram& prog, double* out, int32_t* status, cudaStream_t st) {
-  if (!facets_ok(m, b, fc)) return fc && b.family == FEM_HEX_1 ? FEM_ERR_UNSUPPORTED
-                                                               : FEM_ERR_ARGUMENT;
+  if (!facets_ok(m, b, fc)) return FEM_ERR_ARGUMENT;
   int rc = check_program(prog, m.dim, b.vector != 0, true);
   if (rc) return rc;
   const int64_t ncells = fc ? fc->nfacets : m.nelems;
@@ -395,8 +414,7 @@ int interpolate(const FemMesh& m, const FemBasis& b, const FemFacets* fc, int nq
     set_error(FEM_ERR_ARGUMENT, "interpolate: %d points, X/w/out must be device arrays", nq);
     return FEM_ERR_ARGUMENT;
   }
-  if (!facets_ok(m, b, fc)) return fc && b.family == FEM_HEX_1 ? FEM_ERR_UNSUPPORTED
-                                                               : FEM_ERR_ARGUMENT;
+  if (!facets_ok(m, b, fc)) return FEM_ERR_ARGUMENT;
   const int64_t ncells = fc ? fc->nfacets : m.nelems;
   if (ncells == 0) return 0;
   const fem_faithful::Rule rule{X, nullptr, nq};
@@ -417,6 +435,33 @@ int interpolate(const FemMesh& m, const FemBasis& b, const FemFacets* fc, int nq
     else v ? go(interpolate_kernel<3, false, true>) : go(interpolate_kernel<3, false, false>);
   }
   FEM_LAUNCH_CHECK("interpolate kernel");
+  return 0;
+}
+
+int facet_geometry(const FemMesh& m, const FemBasis& b, const FemFacets& fc, int nq,
+                   const double* X, double* geo, int32_t* status, cudaStream_t st) {
+  if (b.family != FEM_HEX_1) {
+    set_error(FEM_ERR_ARGUMENT, "facet geometry is precomputed for Hex1 meshes only");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (nq <= 0 || nq > fem_faithful::kMaxPoints || !X || !geo || !status || fc.nfacets < 0 ||
+      (fc.nfacets > 0 && (!fc.fverts || !fc.tind || !fc.tind_n || !fc.lfacet_n))) {
+    set_error(FEM_ERR_ARGUMENT, "invalid facet geometry arguments");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (fc.nfacets == 0) return 0;
+  int32_t* kmax = nullptr;
+  FEM_TRY_CUDA(cudaMallocAsync(&kmax, 2 * sizeof(int32_t), st));
+  FEM_TRY_CUDA(cudaMemsetAsync(kmax, 0, 2 * sizeof(int32_t), st));
+  const fem_faithful::Rule rule{X, nullptr, nq};
+  const unsigned g1 = (unsigned)ceil_div(fc.nfacets, 64);
+  fem_faithful::hex_facet_newton_count<<<g1, 64, 0, st>>>(m, fc, rule, 0, kmax);
+  fem_faithful::hex_facet_newton_count<<<g1, 64, 0, st>>>(m, fc, rule, 1, kmax);
+  const unsigned g2 = (unsigned)ceil_div(fc.nfacets * (int64_t)nq, 128);
+  fem_faithful::hex_facet_geometry_kernel<<<g2, 128, 0, st>>>(m, fc, rule, kmax, geo, status);
+  cudaError_t e = cudaGetLastError();
+  cudaFreeAsync(kmax, st);
+  if (e != cudaSuccess) return check_cuda(e, "hex facet geometry kernels");
   return 0;
 }
 

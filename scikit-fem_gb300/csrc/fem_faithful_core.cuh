@@ -347,8 +347,14 @@ FEM_HD void point_geometry(const FemMesh& m, int64_t e, bool hex, const CellGeo&
 
 // ------------------------------------------------------------------ facets
 // Outward normals of the reference cell's facets (refdom.py:60-62, 107-110).
-FEM_HD void ref_normal(int D, int lf, double N[3]) {
+FEM_HD void ref_normal(int D, int lf, double N[3], bool hex = false) {
   N[0] = N[1] = N[2] = 0.0;
+  if (hex) {   // refdom.py:182-187
+    const double T[6][3] = {{1.0, 0.0, 0.0},  {0.0, 0.0, 1.0},  {0.0, 1.0, 0.0},
+                            {0.0, -1.0, 0.0}, {0.0, 0.0, -1.0}, {-1.0, 0.0, 0.0}};
+    for (int i = 0; i < 3; ++i) N[i] = T[lf][i];
+    return;
+  }
   if (D == 2) {
     const double T[3][2] = {{0.0, -1.0}, {1.0, 1.0}, {-1.0, 0.0}};
     N[0] = T[lf][0];
@@ -425,6 +431,132 @@ FEM_HD bool facet_point(const FemMesh& m, const FemFacets& fc, int64_t f, const 
   const double rl = 1.0 / sqrt(len2);
   for (int j = 0; j < D; ++j) g.qx[4 + j] = n[j] * rl;
   return true;
+}
+
+// ---------------------------------------------------------- Hex1 facets
+// ElementQuad1.lbasis (element_quad1.py:24-38), the facets' bilinear map.
+FEM_HD void quad1_lbasis(int i, double x, double y, double& phi, double d[2]) {
+  switch (i) {
+    case 0: phi = (1.0 - x) * (1.0 - y); d[0] = -1.0 + y; d[1] = -1.0 + x; break;
+    case 1: phi = x * (1.0 - y); d[0] = 1.0 - y; d[1] = -x; break;
+    case 2: phi = x * y; d[0] = y; d[1] = x; break;
+    default: phi = (1.0 - x) * y; d[0] = -y; d[1] = 1.0 - x; break;
+  }
+}
+
+// G(X) and detDG of a quadrilateral facet (mapping_isoparametric.py:60-110,
+// 137-155): node sums from 0 in facet-vertex order.
+FEM_HD void quad_facet_map(const FemMesh& m, const FemFacets& fc, int64_t f, double u, double v,
+                           double x[3], double& detB) {
+  double J[3][2];
+  for (int i = 0; i < 3; ++i) {
+    x[i] = 0.0;
+    J[i][0] = J[i][1] = 0.0;
+  }
+  for (int itr = 0; itr < 4; ++itr) {
+    double phi, d[2];
+    quad1_lbasis(itr, u, v, phi, d);
+    const int64_t vtx = fc.fverts[itr * fc.nfacets + f];
+    for (int i = 0; i < 3; ++i) {
+      const double pv = m.p[i * m.nverts + vtx];
+      x[i] = x[i] + pv * phi;
+      J[i][0] = J[i][0] + pv * d[0];
+      J[i][1] = J[i][1] + pv * d[1];
+    }
+  }
+  const double a = J[1][0] * J[2][1] - J[2][0] * J[1][1];
+  const double b = (-J[0][0]) * J[2][1] + J[2][0] * J[0][1];
+  const double c = J[0][0] * J[1][1] - J[1][0] * J[0][1];
+  detB = sqrt((a * a + b * b) + c * c);
+}
+
+// One step of MappingIsoparametric.invF's Newton iteration (:157-168) for
+// cell e at the global point x; returns sum_i |dX_i| (the per-point term of
+// its stopping norm).
+FEM_HD double newton_step(const FemMesh& m, int64_t e, const double x[3], double X[3]) {
+  double F[3], inv[3][3], det;
+  const double unusedA[3][3] = {}, unusedx0[3] = {};   // affine map: not used for Hex1
+  global_coords<3>(m, e, true, unusedA, unusedx0, X[0], X[1], X[2], F);
+  hex_inverse(m, e, X[0], X[1], X[2], inv, det);
+  double r[3], dX[3];
+  for (int j = 0; j < 3; ++j) r[j] = x[j] - F[j];
+  for (int i = 0; i < 3; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < 3; ++j) s = s + inv[i][j] * r[j];
+    dX[i] = s;
+  }
+  for (int i = 0; i < 3; ++i) {
+    const double t = X[i] + dX[i];
+    X[i] = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);   // np.clip
+  }
+  return (fabs(dX[0]) + fabs(dX[1])) + fabs(dX[2]);
+}
+
+// First pass of the Hex1 facet geometry: the first Newton iteration at
+// which facet f's stopping norm (max over its points of sum_i |dX_i|) is
+// below 1e-12 for the cell f2t[side] (which = 0) or f2t[0] (which = 1); 51
+// if none of the 50 does.  invF stops for all facets at once, so the
+// maximum over facets is every facet's iteration count.
+FEM_HD int hex_facet_newton_iters(const FemMesh& m, const FemFacets& fc, int64_t f, int which,
+                                  const double* X, int nq) {
+  const int64_t e = which ? fc.tind_n[f] : fc.tind[f];
+  if (e < 0 || e >= m.nelems || nq > kMaxPoints) return 0;
+  double xs[kMaxPoints][3], Xs[kMaxPoints][3];
+  for (int q = 0; q < nq; ++q) {
+    double detB;
+    quad_facet_map(m, fc, f, X[q], X[nq + q], xs[q], detB);
+    Xs[q][0] = Xs[q][1] = Xs[q][2] = 0.5;
+  }
+  for (int it = 1; it <= 50; ++it) {
+    double norm = 0.0;
+    for (int q = 0; q < nq; ++q) {
+      const double s = newton_step(m, e, xs[q], Xs[q]);
+      if (s > norm || s != s) norm = s;   // np.max, NaN propagating
+    }
+    if (norm < 1e-12) return it;
+  }
+  return 51;
+}
+
+// Second pass: point q of facet f with the common iteration counts ks
+// (cells f2t[side]) and kn (cells f2t[0]); writes the 20 doubles of the
+// generic kernels' point geometry (invDF, detDG, x, h, n, reference point)
+// and returns a status word.
+FEM_HD int hex_facet_point(const FemMesh& m, const FemFacets& fc, int64_t f, int q,
+                           const double* X, int nq, int ks, int kn, double* G) {
+  const int64_t e = fc.tind[f], en = fc.tind_n[f];
+  const int lf = fc.lfacet_n[f];
+  if (e < 0 || e >= m.nelems || en < 0 || en >= m.nelems || lf < 0 || lf > 5) {
+    for (int i = 0; i < 20; ++i) G[i] = 0.0;
+    return 1 << FEM_ERR_ARGUMENT;
+  }
+  int st = 0;
+  if (ks > 50 || kn > 50) st |= 1 << FEM_ERR_NEWTON;
+  double x[3], detB;
+  quad_facet_map(m, fc, f, X[q], X[nq + q], x, detB);
+  double Y[3] = {0.5, 0.5, 0.5}, Y0[3] = {0.5, 0.5, 0.5};
+  for (int it = 0; it < ks && it < 50; ++it) newton_step(m, e, x, Y);
+  for (int it = 0; it < kn && it < 50; ++it) newton_step(m, en, x, Y0);
+  double inv[3][3], det, invn[3][3], detn;
+  hex_inverse(m, e, Y[0], Y[1], Y[2], inv, det);
+  hex_inverse(m, en, Y0[0], Y0[1], Y0[2], invn, detn);
+  if (det == 0.0 || detn == 0.0) st |= 1 << FEM_ERR_ZERO_JACOBIAN;
+  double N[3], n[3];
+  ref_normal(3, lf, N, true);
+  for (int j = 0; j < 3; ++j) {
+    double s = 0.0;
+    for (int i = 0; i < 3; ++i) s = s + invn[i][j] * N[i];
+    n[j] = s;
+  }
+  const double rl = 1.0 / sqrt((n[0] * n[0] + n[1] * n[1]) + n[2] * n[2]);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) G[i * 3 + j] = inv[i][j];
+  G[9] = detB;
+  for (int i = 0; i < 3; ++i) G[10 + i] = x[i];
+  G[13] = sqrt(detB);
+  for (int j = 0; j < 3; ++j) G[14 + j] = n[j] * rl;
+  for (int i = 0; i < 3; ++i) G[17 + i] = Y[i];
+  return st;
 }
 
 // form(u_j, v_i, w) * dx at quadrature point q (bilinear_form.py:150-151,

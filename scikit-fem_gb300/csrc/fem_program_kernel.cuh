@@ -20,6 +20,15 @@ __device__ bool geometry_at(const FemMesh& m, const FemBasis& b, const FemFacets
                             const Rule& rule, ProgFlags f, int64_t e, int q, double Y[3],
                             PointGeo& g, const double* cell = nullptr) {
   if (FACET) {
+    if (fc.geo) {   // Hex1 facets: precomputed by fem_facet_geometry
+      const double* G = fc.geo + ((size_t)e * rule.nq + q) * kGeo;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) g.inv[i][j] = G[i * 3 + j];
+      g.det = G[9];
+      for (int i = 0; i < 7; ++i) g.qx[i] = G[10 + i];
+      for (int i = 0; i < 3; ++i) Y[i] = G[17 + i];
+      return true;
+    }
     double Xf[2] = {rule.X[q], D == 3 ? rule.X[rule.nq + q] : 0.0};
     return facet_point<D>(m, fc, e, Xf, Y, g);
   }

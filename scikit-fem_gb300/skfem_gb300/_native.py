@@ -20,6 +20,7 @@ FEM_ERR_ZERO_JACOBIAN = 4
 FEM_ERR_STALE_PATTERN = 5
 FEM_ERR_CAPACITY = 6
 FEM_ERR_VARYING = 7
+FEM_ERR_NEWTON = 8
 
 FAMILY = {"TriP1": 1, "TriP2": 2, "TetP1": 3, "TetP2": 4, "Hex1": 5}
 
@@ -58,7 +59,7 @@ class FemInstr(ctypes.Structure):
 class FemFacets(ctypes.Structure):
     _fields_ = [("nfacets", ctypes.c_int64), ("fverts", ctypes.c_void_p),
                 ("tind", ctypes.c_void_p), ("tind_n", ctypes.c_void_p),
-                ("lfacet_n", ctypes.c_void_p)]
+                ("lfacet_n", ctypes.c_void_p), ("geo", ctypes.c_void_p)]
 
 
 class FemProgram(ctypes.Structure):
@@ -126,6 +127,7 @@ _SIGS = {
     "fem_assemble_local": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_int64,
                                           _P]),
     "fem_csr_sum_to_host": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32, _P, _P]),
+    "fem_facet_geometry": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P, _P, _P, _P]),
     "fem_set_tuning": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "fem_assemble_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
 }

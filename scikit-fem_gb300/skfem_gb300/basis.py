@@ -172,7 +172,7 @@ class CellBasis:
         return "CellBasis(%r, %r) on %s: %d DOFs" % (self.mesh, self.elem, self.device, self.N)
 
 
-BOUNDARY_REFDOM = {"tri": "line", "tet": "tri"}
+BOUNDARY_REFDOM = {"tri": "line", "tet": "tri", "hex": "quad"}
 
 
 class FacetBasis(CellBasis):
@@ -242,7 +242,7 @@ class FacetBasis(CellBasis):
         self.c_basis = N.FemBasis(fam, int(self.elem.vector), self.Nbfun, 0, self.N,
                                   self.ed_full_dev.data_ptr())
         self.c_facets = N.FemFacets(self.nelems, self.fv_dev.data_ptr(), self.tind_dev.data_ptr(),
-                                    self.tindn_dev.data_ptr(), self.lf_dev.data_ptr())
+                                    self.tindn_dev.data_ptr(), self.lf_dev.data_ptr(), None)
         # the pattern is built over the facets with their cells' DOFs
         self.c_mesh_pat = N.FemMesh(dim, m.t.shape[0], m.p.shape[1], self.nelems,
                                     self.p_dev.data_ptr(), self.t_dev.data_ptr())
@@ -250,6 +250,25 @@ class FacetBasis(CellBasis):
                                       self.ed_dev.data_ptr())
         self.X_dev = up(self.X, np.float64)
         self.W_dev = up(self.W, np.float64)
+        if m.refdom == "hex":
+            # isoparametric facets: the point geometry (Newton-iterated
+            # reference points, normals) once, as the reference precomputes it
+            nq = self.X.shape[1]
+            self.geo_dev = torch.empty(max(1, self.nelems * nq * 20), dtype=torch.float64,
+                                       device=dev)
+            status = torch.zeros(1, dtype=torch.int32, device=dev)
+            N.check(N.lib().fem_facet_geometry(N.byref(self.c_mesh), N.byref(self.c_basis),
+                                               N.byref(self.c_facets), nq, N.ptr(self.X_dev),
+                                               N.ptr(self.geo_dev), N.ptr(status),
+                                               N.stream_ptr()))
+            st = int(status.item())
+            if st & (1 << N.FEM_ERR_ZERO_JACOBIAN):
+                raise N.ZeroJacobianError("Zero Jacobian determinant")
+            if st & (1 << N.FEM_ERR_NEWTON):
+                raise Exception("Newton iteration didn't converge up to TOL=1e-12")
+            if st:
+                raise ValueError("invalid facet arrays")
+            self.c_facets.geo = self.geo_dev.data_ptr()
 
     def update_coordinates(self, p):
         raise NotImplementedError("FacetBasis.update_coordinates is not supported")

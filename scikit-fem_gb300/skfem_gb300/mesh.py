@@ -22,6 +22,10 @@ TET_FACETS = np.array([[0, 1, 2], [0, 1, 3], [0, 2, 3], [1, 2, 3]])       # refd
 # outward normals of the reference cell's facets (refdom.py:60-62, 107-110)
 TRI_NORMALS = np.array([[0., -1.], [1., 1.], [-1., 0.]])
 TET_NORMALS = np.array([[0., 0., -1.], [0., -1., 0.], [-1., 0., 0.], [1., 1., 1.]])
+HEX_FACETS = np.array([[0, 1, 4, 2], [0, 2, 6, 3], [0, 3, 5, 1], [2, 4, 7, 6], [1, 5, 7, 4],
+                       [3, 6, 7, 5]])                                     # refdom.py:188-193
+HEX_NORMALS = np.array([[1., 0., 0.], [0., 0., 1.], [0., 1., 0.], [0., -1., 0.], [0., 0., -1.],
+                        [-1., 0., 0.]])                                   # refdom.py:182-187
 
 
 class Mesh:
@@ -86,16 +90,19 @@ class Mesh:
         raise NotImplementedError
 
     # ------------------------------------------------------------ entities
-    def _build(self, name, local):
-        """Mesh.build_entities (mesh.py:1065-1082) with sort=True: every
-        cell's local vertex tuples, sorted per tuple, made unique in
-        lexicographic order; plus the inverse map (cell -> entity) and, as
-        Mesh.build_inverse (mesh.py:1084-1100) does, the first and last cell
-        that contain each entity (-1 when only one does)."""
+    def _build(self, name, local, sort=True):
+        """Mesh.build_entities (mesh.py:1065-1082): every cell's local vertex
+        tuples, made unique in the lexicographic order of the sorted tuples
+        and stored sorted (sort=True) or in the vertex order of their first
+        occurrence (sort=False, MeshHex1 facets, mesh_hex_1.py:49-55); plus
+        the inverse map (cell -> entity) and, as Mesh.build_inverse
+        (mesh.py:1084-1100) does, the first and last cell that contain each
+        entity (-1 when only one does)."""
         if name not in self._entities:
             t = self.t
             ne = t.shape[1]
-            cols = np.sort(np.hstack([t[list(ix)] for ix in local]), axis=0)
+            raw = np.hstack([t[list(ix)] for ix in local])
+            cols = np.sort(raw, axis=0)
             M = cols.shape[1]
             order = np.lexsort(cols[::-1])          # stable: positions ascend in a group
             sc = cols[:, order]
@@ -103,7 +110,10 @@ class Mesh:
             if M > 1:
                 new[1:] = np.any(sc[:, 1:] != sc[:, :-1], axis=0)
             ids = np.cumsum(new) - 1
-            ent = np.ascontiguousarray(sc[:, new]).astype(np.int32)
+            if sort:
+                ent = np.ascontiguousarray(sc[:, new]).astype(np.int32)
+            else:
+                ent = np.ascontiguousarray(raw[:, order[new]]).astype(np.int32)
             inv = np.empty(M, dtype=np.int64)
             inv[order] = ids
             starts = np.nonzero(new)[0]
@@ -116,21 +126,22 @@ class Mesh:
 
     # facets (mesh.py:98-113, 197-199, 426-456, 1291-1329)
     facet_tuples = None
+    facet_sort = True
     normals_ref = None
 
     @property
     def facets(self):
         if self.facet_tuples is None:
             raise NotImplementedError("facets of %s are not supported" % type(self).__name__)
-        return self._build("facets", self.facet_tuples)[0]
+        return self._build("facets", self.facet_tuples, self.facet_sort)[0]
 
     @property
     def t2f(self):
-        return self._build("facets", self.facet_tuples)[1]
+        return self._build("facets", self.facet_tuples, self.facet_sort)[1]
 
     @property
     def f2t(self):
-        return self._build("facets", self.facet_tuples)[2]
+        return self._build("facets", self.facet_tuples, self.facet_sort)[2]
 
     def boundary_facets(self):
         return np.nonzero(self.f2t[1] == -1)[0].astype(np.int32)
@@ -236,6 +247,9 @@ class MeshHex1(Mesh):
     kind = refdom = "hex"
     affine = False
     nloc = 8
+    facet_tuples = HEX_FACETS
+    facet_sort = False
+    normals_ref = HEX_NORMALS
 
     def __init__(self, doflocs=None, t=None, **kwargs):
         if doflocs is None:

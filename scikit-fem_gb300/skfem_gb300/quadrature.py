@@ -93,6 +93,13 @@ def get_quadrature(refdom, norder):
                     np.array([float.fromhex(v) for v in W]))
         x, w = gauss_line(norder)
         return x[None, :], w
+    if refdom == "quad":
+        # tensor product of the line rule (quadrature.py:55-62)
+        x, w = get_quadrature("line", norder)
+        A, B = np.meshgrid(x[0], x[0])
+        X = np.vstack((A.flatten(order="F"), B.flatten(order="F")))
+        A, B = np.meshgrid(w, w)
+        return X, (A * B).flatten(order="F")
     if refdom == "hex" and norder in (6, 7):
         # the reference's default Hex1 rule as recorded (leggauss's last bits
         # depend on the platform's eigenvalue solver)

@@ -45,7 +45,8 @@ def traction(v, w):
 CASES = [("tri_p1_facet", F.MeshTri, F.ElementTriP1),
          ("tri_p2_facet", F.MeshTri, F.ElementTriP2),
          ("tet_p1_facet", F.MeshTet, F.ElementTetP1),
-         ("tet_p2_facet", F.MeshTet, F.ElementTetP2)]
+         ("tet_p2_facet", F.MeshTet, F.ElementTetP2),
+         ("hex1_facet", F.MeshHex, F.ElementHex1)]
 
 
 def facet_args(m, g, prefix):

@@ -414,6 +414,56 @@ def facet_cases():
         X, W = get_quadrature_line(o)
         rules["line%d_X" % o], rules["line%d_W" % o] = X, W
     save("line_rules", **rules)
+    hex_facet_case()
+
+
+def hex_facet_case():
+    """FacetBasis on a jittered Hex1 mesh: quadrilateral facets, Newton
+    iterated reference points, normals of the isoparametric cells."""
+    from skfem import FacetBasis
+    rng = np.random.default_rng(20261206)
+
+    @BilinearForm
+    def robin(u, v, w):
+        return (1.0 + w.x[0]) * u * v + dot(w.n, grad(u)) * v
+
+    @LinearForm
+    def neumann(v, w):
+        return dot(w.n, w.x) * v + w.h * v
+
+    @Functional
+    def length(w):
+        return 1.0 + 0.0 * w.x[0]
+
+    @Functional
+    def s_energy(w):
+        return w['s'] ** 2 + dot(w.n, grad(w['s']))
+
+    n = 3
+    m = MeshHex.init_tensor(*(np.linspace(0, 1, n + 1),) * 3)
+    p = m.p.copy()
+    inner = jitter(m, rng, 0.2)
+    p[:, inner] += rng.uniform(-0.2 / n, 0.2 / n, size=(3, int(inner.sum())))
+    m = MeshHex(p, m.t)
+    s = rng.standard_normal(Basis(m, ElementHex1()).N)
+    arrs = dict(p=m.p, t=m.t, facets=m.facets, f2t=m.f2t, t2f=m.t2f, s=s)
+    interior = np.nonzero(m.f2t[1] >= 0)[0].astype(np.int32)
+    for pre, kw in (("", {}), ("in0_", dict(facets=interior, side=0)),
+                    ("in1_", dict(facets=interior, side=1)),
+                    ("cb_", dict(facets=lambda x: x[1] < 0.3))):
+        fb = FacetBasis(m, ElementHex1(), **kw)
+        sf = fb.interpolate(s)
+        out = dict(find=fb.find, tind=fb.tind, X=fb.X, W=fb.W,
+                   x=np.asarray(fb.global_coordinates()), h=np.asarray(fb.mesh_parameters()),
+                   n=np.asarray(fb.normals), s_value=np.asarray(sf), s_grad=sf.grad,
+                   b_neumann=neumann.assemble(fb), e_length=length.elemental(fb),
+                   f_length=np.float64(length.assemble(fb)),
+                   e_energy=s_energy.elemental(fb, s=s),
+                   f_energy=np.float64(s_energy.assemble(fb, s=s)))
+        out.update({k + "_mass": v for k, v in csr_arrays(mass.assemble(fb)).items()})
+        out.update({k + "_robin": v for k, v in csr_arrays(robin.assemble(fb)).items()})
+        arrs.update({pre + k: v for k, v in out.items()})
+    save("hex1_facet", **arrs)
 
 
 if __name__ == "__main__":
@@ -421,5 +471,7 @@ if __name__ == "__main__":
         generic_cases()
     elif sys.argv[1:] == ["--facet"]:
         facet_cases()
+    elif sys.argv[1:] == ["--hex-facet"]:
+        hex_facet_case()
     else:
         main()

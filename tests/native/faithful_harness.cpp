@@ -108,6 +108,40 @@ extern "C" int faithful_points_host(const FemMesh* m, const FemBasis* b, int nq,
   return 0;
 }
 
+// Point geometry of a facet: precomputed (Hex1, fc.geo) or facet_point.
+template <int D>
+static bool facet_geo(const FemMesh& m, const FemFacets& fc, int64_t f, int q, const double* X,
+                      int nq, double Y[3], fem_faithful::PointGeo& g) {
+  if (fc.geo) {
+    const double* G = fc.geo + ((size_t)f * nq + q) * 20;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) g.inv[i][j] = G[i * 3 + j];
+    g.det = G[9];
+    for (int i = 0; i < 7; ++i) g.qx[i] = G[10 + i];
+    for (int i = 0; i < 3; ++i) Y[i] = G[17 + i];
+    return true;
+  }
+  double Xf[2] = {X[q], D == 3 ? X[nq + q] : 0.0};
+  return fem_faithful::facet_point<D>(m, fc, f, Xf, Y, g);
+}
+
+// Hex1 facet geometry (both passes) on the host.
+extern "C" int faithful_hex_facet_geometry_host(const FemMesh* m, const FemFacets* fc, int nq,
+                                                const double* X, double* geo) {
+  using namespace fem_faithful;
+  int k[2] = {0, 0};
+  for (int which = 0; which < 2; ++which)
+    for (int64_t f = 0; f < fc->nfacets; ++f) {
+      const int it = hex_facet_newton_iters(*m, *fc, f, which, X, nq);
+      if (it > k[which]) k[which] = it;
+    }
+  int st = 0;
+  for (int64_t f = 0; f < fc->nfacets; ++f)
+    for (int q = 0; q < nq; ++q)
+      st |= hex_facet_point(*m, *fc, f, q, X, nq, k[0], k[1], geo + ((size_t)f * nq + q) * 20);
+  return st;
+}
+
 // FacetBasis versions: the facet-point geometry (facet_point) and the same
 // per-entry replay; prog->qX is the facet rule (dim-1, nq).
 template <int D>
@@ -117,10 +151,9 @@ static double facet_entry(const FemMesh& m, const FemBasis& b, const FemFacets& 
   double vals[kMaxPoints];
   const int nq = prog.nq;
   for (int q = 0; q < nq; ++q) {
-    double Xf[2] = {prog.qX[q], D == 3 ? prog.qX[nq + q] : 0.0};
     double Y[3];
     PointGeo g;
-    facet_point<D>(m, fc, f, Xf, Y, g);
+    facet_geo<D>(m, fc, f, q, prog.qX, nq, Y, g);
     vals[q] = point_value<D>(b, prog, f, q, i, j, Y[0], Y[1], Y[2], g, prog.qW[q], R);
   }
   return np_pairwise_sum(vals, nq);
@@ -150,11 +183,10 @@ extern "C" int faithful_facet_points_host(const FemMesh* m, const FemFacets* fc,
   using namespace fem_faithful;
   for (int64_t f = 0; f < fc->nfacets; ++f)
     for (int q = 0; q < nq; ++q) {
-      double Xf[2] = {X[q], m->dim == 3 ? X[nq + q] : 0.0};
       double Y[3];
       PointGeo g;
-      const bool ok = m->dim == 2 ? facet_point<2>(*m, *fc, f, Xf, Y, g)
-                                  : facet_point<3>(*m, *fc, f, Xf, Y, g);
+      const bool ok = m->dim == 2 ? facet_geo<2>(*m, *fc, f, q, X, nq, Y, g)
+                                  : facet_geo<3>(*m, *fc, f, q, X, nq, Y, g);
       if (!ok) return 1;
       for (int k = 0; k < 7; ++k) out[((int64_t)k * fc->nfacets + f) * nq + q] = g.qx[k];
     }
@@ -170,10 +202,9 @@ static void facet_interp_host(const FemMesh& m, const FemBasis& b, const FemFace
   for (int64_t f = 0; f < fc.nfacets; ++f) {
     const int64_t ec = fc.tind[f];
     for (int q = 0; q < nq; ++q) {
-      double Xf[2] = {X[q], D == 3 ? X[nq + q] : 0.0};
       double Y[3];
       PointGeo g;
-      facet_point<D>(m, fc, f, Xf, Y, g);
+      facet_geo<D>(m, fc, f, q, X, nq, Y, g);
       double acc[D + D * D], qq[D + D * D];
       const double w0 = w[b.element_dofs[ec]];
       quantities<D>(b.family, vec, 0, Y[0], Y[1], Y[2], g.inv, qq);

@@ -1,7 +1,8 @@
 """FacetBasis on the host: the mesh's facets / f2t / t2f, the facet-point
-geometry (coordinates, h, outward normals) and the replayed facet
-integrals, against scikit-fem's own outputs (tests/golden facet cases),
-bit for bit -- every operation on this path is correctly rounded."""
+geometry (coordinates, h, outward normals; on Hex1 meshes the reference's
+Newton-iterated inverse map) and the replayed facet integrals, against
+scikit-fem's own outputs (tests/golden facet cases), bit for bit -- every
+operation on this path is correctly rounded."""
 import ctypes
 
 import numpy as np
@@ -22,6 +23,7 @@ def _lib():
     lib.faithful_facet_program_host.argtypes = [ctypes.c_int] + [V] * 5
     lib.faithful_facet_points_host.argtypes = [V, V, ctypes.c_int, V, V]
     lib.faithful_facet_interpolate_host.argtypes = [V, V, V, ctypes.c_int, V, V, V]
+    lib.faithful_hex_facet_geometry_host.argtypes = [V, V, ctypes.c_int, V, V]
     lib.faithful_sum_host.argtypes = [V, ctypes.c_int64]
     lib.faithful_sum_host.restype = ctypes.c_double
     return lib
@@ -50,8 +52,15 @@ class HostFacets:
         self.basis = N.FemBasis(N.FAMILY[elem.family], int(elem.vector), self.ed.shape[0], 0,
                                 self.N, self.ed.ctypes.data)
         self.fc = N.FemFacets(self.nf, self.fv.ctypes.data, self.tind.ctypes.data,
-                              self.tindn.ctypes.data, self.lf.ctypes.data)
+                              self.tindn.ctypes.data, self.lf.ctypes.data, None)
         self.keep = []
+        if elem.refdom == "hex":
+            # Newton-iterated point geometry, as fem_facet_geometry computes it
+            self.geo = np.zeros(self.nf * self.nq * 20)
+            assert _lib().faithful_hex_facet_geometry_host(
+                ctypes.byref(self.mesh), ctypes.byref(self.fc), self.nq, self.X.ctypes.data,
+                self.geo.ctypes.data) == 0
+            self.fc.geo = self.geo.ctypes.data
 
     def points(self):
         out = np.zeros((7, self.nf, self.nq))
