@@ -38,6 +38,11 @@ UNIT = "elements/s"
 
 # algorithmic bytes per element of a steady-state TetP1 assembly
 # (element ids 16 B + coefficient 8 B) + coordinates + CSR values, see the design doc
+# DRAM bytes per cell of one steady-state TetP1 step (local kernel 120.2 B +
+# segmented sum 193.8 B), from the ncu capture on the 61^3-node cube
+TRAFFIC_B_PER_CELL = 120.2 + 193.8
+
+
 def algorithmic_bytes(nelems, nverts, nnz, dim=3, nloc=4):
     return nelems * (nloc * 4 + 8) + nverts * dim * 8 + nnz * 8
 
@@ -237,7 +242,11 @@ def gpu_arm(args):
                    "l2": "inputs+staging larger than L2 (no flush)", "parallelism": "replicas",
                    "pattern_build_s": pattern_s},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                     "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": TRAFFIC_B_PER_CELL * nel,
+                     "traffic_source": "ncu dram__bytes_read+write of the local kernel and the "
+                                       "segmented sum on the 1.3M-cell case, %.1f B/cell, "
+                                       "scaled by cells" % TRAFFIC_B_PER_CELL,
                      "peak_kind": peak_kind, "algorithmic_bytes_per_step": B,
                      "kernel": "whole assembly step (local + segmented sum)"},
         "fp64": {"kernel": "local matrices (simplex_scalar_kernel<3,1>)",
