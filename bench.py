@@ -43,6 +43,23 @@ UNIT = "elements/s"
 TRAFFIC_B_PER_CELL = 120.2 + 193.8
 
 
+def max_over_ranks(ms, dist=None, device="cpu"):
+    """Replicas: every rank times its own copy of the workload; the job's
+    step time is the slowest rank's (one all-reduce, after the timed region)."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(cells_per_rank, world, ms):
+    """Whole-job throughput of ``world`` replicas: all cells of all ranks
+    over the slowest rank's step time."""
+    return cells_per_rank * world / (ms * 1e-3)
+
+
 def algorithmic_bytes(nelems, nverts, nnz, dim=3, nloc=4):
     return nelems * (nloc * 4 + 8) + nverts * dim * 8 + nnz * 8
 
@@ -154,6 +171,9 @@ def gpu_arm(args):
     pattern_s = time.perf_counter() - t0
     entry = next(iter(b._patterns.values()))
     nnz = entry.nnz
+    # launch parameters by the autotuner on this workload (setup, untimed)
+    from skfem_gb300 import autotune
+    tuned, _ = autotune.tune(form, b, {"k": kd}, reps=3, use_cache=False)
 
     # a bare C-ABI step: inputs in HBM, results in HBM
     coeffs, ch, c_form = form._setup(b, None, {"k": kd})
@@ -183,11 +203,7 @@ def gpu_arm(args):
         ev1.record(stream)
         torch.cuda.synchronize()
         time.sleep(0.2)
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = t.item()
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, dist, "cuda")
     assert int(status.item()) == 0, "assembly status %d" % int(status.item())
     assert torch.equal(vals, K0.values()), "repeated assembly not bitwise identical"
 
@@ -233,14 +249,14 @@ def gpu_arm(args):
     flops_per_el = 102.0  # FP64 ops of the TetP1 local kernel, counted in the design doc
     fp64_achieved = nel * flops_per_el / (t_local * 1e-3) / 1e9
     res = {
-        "metric": METRIC, "value": nel * world / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
+        "metric": METRIC, "value": replica_value(nel, world, ms), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak" if world > 1 else "replicas only",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded tensor mesh, lognormal k)",
         "config": {"workload": "TetP1 k*laplace+mass, 101^3-node unit cube tensor mesh, 6 tets/cell",
                    "nelems": nel, "nverts": int(m.p.shape[1]), "nnz": nnz,
                    "l2": "inputs+staging larger than L2 (no flush)", "parallelism": "replicas",
-                   "pattern_build_s": pattern_s},
+                   "pattern_build_s": pattern_s, "autotuned": tuned},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": TRAFFIC_B_PER_CELL * nel,
@@ -258,7 +274,7 @@ def gpu_arm(args):
                 "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s,
                 "s_per_step_median": sorted(e2e_times)[len(e2e_times) // 2],
                 "api": "BilinearForm.assemble(basis, k=(nelems, nqp) host array) -> scipy CSR"},
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": 2 * args.steps,   # local kernel + segmented sum per step
     }
     if rank == 0 and not args.no_secondary:
         res["secondary"] = secondary_workloads(args)

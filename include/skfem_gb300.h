@@ -337,6 +337,15 @@ int fem_linear_vjp(const FemMesh* mesh, const FemBasis* basis, const FemLinear* 
  * phase 2 fills indices, values and, when out_b is given, the right-hand
  * side (b and x may be NULL: zero).
  */
+/* enforce (skfem/utils.py:327-400) on a device CSR, in place: rows[0..nd)
+ * (sorted, unique, < nrows) are zeroed with diag on their diagonal -- the
+ * entries stay in the pattern as stored zeros, as scipy keeps them -- and,
+ * if b is given, b[r] = x[r] (0 without x).  *missing (device) is
+ * incremented for every such row that has no diagonal entry. */
+int fem_enforce(const int32_t* indptr, const int32_t* indices, double* vals, int64_t nrows,
+                const int32_t* rows, int64_t nd, double diag, double* b, const double* x,
+                int32_t* missing, fem_stream_t stream);
+
 int fem_condense_pattern(const int32_t* indptr, const int32_t* indices, int64_t nrows,
                          const int32_t* map, int64_t nkeep, int32_t* out_indptr, int64_t* out_nnz,
                          fem_stream_t stream);

@@ -53,7 +53,42 @@ __global__ void condense_fill_kernel(const int32_t* __restrict__ indptr,
 
 }  // namespace
 
+// enforce (utils.py:327-400): the rows D become zero with `diag` on their
+// diagonal, in place (the pattern keeps its entries, as scipy keeps explicit
+// zeros); b[D] = x[D].  missing counts D rows without a diagonal entry.
+__global__ void enforce_kernel(const int32_t* __restrict__ indptr,
+                               const int32_t* __restrict__ indices, double* __restrict__ vals,
+                               const int32_t* __restrict__ rows, int64_t nd, double diag,
+                               double* __restrict__ b, const double* __restrict__ x,
+                               int32_t* __restrict__ missing) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nd) return;
+  const int32_t r = rows[k];
+  bool found = false;
+  for (int32_t p = indptr[r]; p < indptr[r + 1]; ++p) {
+    const bool d = indices[p] == r;
+    vals[p] = d ? diag : 0.0;
+    found = found || d;
+  }
+  if (!found) atomicAdd(missing, 1);
+  if (b) b[r] = x ? x[r] : 0.0;
+}
+
 extern "C" {
+
+int fem_enforce(const int32_t* indptr, const int32_t* indices, double* vals, int64_t nrows,
+                const int32_t* rows, int64_t nd, double diag, double* b, const double* x,
+                int32_t* missing, fem_stream_t stream) {
+  if (!indptr || !indices || !vals || (!rows && nd > 0) || nd < 0 || nrows < 0 || !missing) {
+    fem::set_error(FEM_ERR_ARGUMENT, "invalid enforce arguments");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (nd == 0) return 0;
+  enforce_kernel<<<(unsigned)fem::ceil_div(nd, 256), 256, 0, (cudaStream_t)stream>>>(
+      indptr, indices, vals, rows, nd, diag, b, x, missing);
+  FEM_LAUNCH_CHECK("enforce_kernel");
+  return 0;
+}
 
 int fem_condense_pattern(const int32_t* indptr, const int32_t* indices, int64_t nrows,
                          const int32_t* map, int64_t nkeep, int32_t* out_indptr, int64_t* out_nnz,

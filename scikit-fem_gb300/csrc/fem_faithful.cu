@@ -242,7 +242,8 @@ int check_instructions(const FemInstr* h, int ninstr, int ncoef, int dim, bool v
 // Host-side check of a form program before any kernel interprets it: every
 // operand names an earlier register, a basis quantity, a coefficient slot
 // or a coordinate that exists.
-int check_program(const FemProgram& prog, int dim, bool vec, bool need_rule) {
+int check_program(const FemProgram& prog, int dim, bool vec, bool need_rule,
+                  bool instructions = true) {
   using namespace fem_faithful;
   if (prog.ninstr <= 0 || prog.ninstr > kMaxProgram || prog.out < 0 ||
       prog.out >= prog.ninstr || prog.ncoef < 0 || prog.ncoef > kMaxCoef || !prog.ins ||
@@ -262,6 +263,8 @@ int check_program(const FemProgram& prog, int dim, bool vec, bool need_rule) {
                 prog.coef_stride[c], prog.nq);
       return FEM_ERR_ARGUMENT;
     }
+  // a compiled program's operands were checked when it was compiled
+  if (!instructions) return 0;
   FemInstr h[kMaxProgram];
   FEM_TRY_CUDA(cudaMemcpy(h, prog.ins, prog.ninstr * sizeof(FemInstr), cudaMemcpyDefault));
   return check_instructions(h, prog.ninstr, prog.ncoef, dim, vec);
@@ -329,7 +332,7 @@ static bool facets_ok(const FemMesh& m, const FemBasis& b, const FemFacets* fc) 
 int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets* fc,
                  const FemProgram& prog, double* out, int32_t* status, cudaStream_t st) {
   if (!facets_ok(m, b, fc)) return FEM_ERR_ARGUMENT;
-  int rc = check_program(prog, m.dim, b.vector != 0, true);
+  int rc = check_program(prog, m.dim, b.vector != 0, true, prog.compiled == nullptr);
   if (rc) return rc;
   const int64_t ncells = fc ? fc->nfacets : m.nelems;
   if (ncells == 0) return 0;

@@ -128,6 +128,8 @@ _SIGS = {
                                           _P]),
     "fem_csr_sum_to_host": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32, _P, _P]),
     "fem_facet_geometry": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P, _P, _P, _P]),
+    "fem_enforce": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _P, ctypes.c_int64,
+                                   ctypes.c_double, _P, _P, _P, _P]),
     "fem_set_tuning": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "fem_assemble_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
 }

@@ -1,6 +1,7 @@
 """Consumers of the assembled system, on the device.
 
-``condense`` follows skfem.utils.condense (skfem/utils.py:462-600) for the
+``condense`` follows skfem.utils.condense (skfem/utils.py:462-600) and
+``enforce`` skfem.utils.enforce (skfem/utils.py:327-400) for the
 device-resident results of ``assemble_torch``: a torch sparse CSR matrix and
 torch vectors stay in HBM; the condensed matrix is again a canonical CSR.
 """
@@ -10,7 +11,7 @@ import torch
 
 from . import _native as N
 
-__all__ = ["condense"]
+__all__ = ["condense", "enforce"]
 
 
 def _dofs(S, n, device):
@@ -85,3 +86,60 @@ def condense(A, b=None, x=None, I=None, D=None, expand=True):
     if expand:
         ret += (x, I_t)
     return ret if len(ret) > 1 else ret[0]
+
+
+def _bc_sets(n, I, D):
+    Dn, In = _dofs(D, n, None), _dofs(I, n, None)
+    if In is None and Dn is None:
+        raise Exception("Either I or D must be given!")
+    if In is not None and Dn is not None:
+        raise Exception("Give only I or only D!")
+    if Dn is None:
+        Dn = np.setdiff1d(np.arange(n), In)
+    return Dn
+
+
+def _rows_to_identity(M, rows, nd, d, rhs, x, overwrite):
+    dev = M.device
+    crow = M.crow_indices().to(torch.int32).contiguous()
+    col = M.col_indices().to(torch.int32).contiguous()
+    val = M.values() if overwrite else M.values().clone()
+    missing = torch.zeros(1, dtype=torch.int32, device=dev)
+    N.check(N.lib().fem_enforce(N.ptr(crow), N.ptr(col), N.ptr(val), M.shape[0], N.ptr(rows),
+                                nd, float(d), N.ptr(rhs), N.ptr(x), N.ptr(missing),
+                                N.stream_ptr()))
+    if int(missing.item()):
+        raise NotImplementedError("enforce: %d constrained rows have no diagonal entry in the "
+                                  "pattern" % int(missing.item()))
+    if overwrite:
+        return M
+    return torch.sparse_csr_tensor(M.crow_indices(), M.col_indices(), val, size=M.shape)
+
+
+def enforce(A, b=None, x=None, I=None, D=None, diag=1., overwrite=False):
+    """Set the rows D of A to zero with ``diag`` on the diagonal and b[D] =
+    x[D] (utils.py:327-400) on a device CSR (torch sparse CSR of
+    ``assemble_torch``); a sparse ``b`` (mass matrix) gets its rows D
+    zeroed with a zero diagonal.  Returns (A, b) or A like the reference;
+    ``overwrite`` modifies the inputs in place."""
+    if not (isinstance(A, torch.Tensor) and A.layout == torch.sparse_csr):
+        raise TypeError("enforce on the GPU takes the torch CSR of assemble_torch")
+    n = A.shape[0]
+    dev = A.device
+    Dn = _bc_sets(n, I, D)
+    rows = torch.from_numpy(Dn.astype(np.int32)).to(dev)
+    if x is not None:
+        x = torch.as_tensor(x, dtype=torch.float64, device=dev).contiguous()
+        if b is None:
+            b = torch.zeros(n, dtype=torch.float64, device=dev)     # utils.py:321-322
+    sparse_b = isinstance(b, torch.Tensor) and b.layout == torch.sparse_csr
+    bout = None
+    if b is not None and not sparse_b:
+        bt = torch.as_tensor(b, dtype=torch.float64, device=dev)
+        bout = bt if (overwrite and bt.is_contiguous()) else bt.clone().contiguous()
+    Aout = _rows_to_identity(A, rows, len(Dn), diag, bout, x, overwrite)
+    if b is None:
+        return Aout
+    if sparse_b:
+        return Aout, _rows_to_identity(b, rows, len(Dn), 0.0, None, None, overwrite)
+    return Aout, bout

@@ -5,6 +5,7 @@ relative Frobenius and 1e-13 * max|K| entrywise, load vectors the same,
 repeated runs bitwise identical."""
 import numpy as np
 import pytest
+import scipy.sparse as sp
 import torch
 
 import oracle as O
@@ -363,3 +364,34 @@ def test_host_coefficients_checked_in_kernel():
     # the plain call afterwards is back on the channel kernels
     K3 = k_laplace_mass.assemble(b, k=kw)
     np.testing.assert_array_equal(K3.data, K1.data)
+
+
+def test_enforce_on_device_matches_reference_semantics():
+    """enforce (utils.py:327-400): rows D zero with 1 on the diagonal,
+    entries kept as stored zeros, b[D] = x[D] -- compared with scipy doing the
+    same on the host copy."""
+    from skfem_gb300.utils import enforce
+    m = F.MeshTri.init_tensor(np.linspace(0, 1, 9), np.linspace(0, 1, 7))
+    b = F.Basis(m, F.ElementTriP2())
+    A = laplace.assemble_torch(b)
+    rhs = unit_load.assemble_torch(b)
+    D = np.unique(b.element_dofs[:, :5])
+    x = np.arange(b.N, dtype=np.float64)
+    Ae, be = enforce(A, rhs, x=x, D=D)
+    Ah = laplace.assemble(b).tolil()
+    for r in D:
+        Ah[r, :] = 0.0
+        Ah[r, r] = 1.0
+    Ah = Ah.tocsr()
+    Ae_h = sp.csr_matrix((Ae.values().cpu().numpy(), Ae.col_indices().cpu().numpy(),
+                          Ae.crow_indices().cpu().numpy()), shape=Ah.shape)
+    np.testing.assert_array_equal(Ae_h.toarray(), Ah.toarray())
+    assert Ae._nnz() == A._nnz()                              # pattern kept
+    bh = unit_load.assemble(b)
+    bh[D] = x[D]
+    np.testing.assert_array_equal(be.cpu().numpy(), bh)
+    # a mass matrix as b: its rows D are zeroed with a zero diagonal
+    M = mass.assemble_torch(b)
+    _, Me = enforce(A, M, D=D)
+    Mh = Me.to_dense().cpu().numpy()
+    assert np.all(Mh[D] == 0.0)
