@@ -311,14 +311,6 @@ __global__ void zero_check_kernel(const int32_t* __restrict__ inc_ptr, const int
   if (stale) atomicOr(status, 1 << FEM_ERR_STALE_PATTERN);
 }
 
-__global__ void max_reduce_kernel(const int32_t* __restrict__ x, int64_t n, int32_t* out) {
-  int32_t m = 0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    m = max(m, x[i]);
-  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
-}
 
 int grid_for(int64_t n, int block) {
   const int64_t g = ceil_div(n, block);
