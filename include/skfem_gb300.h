@@ -164,8 +164,9 @@ typedef struct FemProgram {
 
 /*
  * Compile a form program (ins: HOST array of ninstr instructions, as traced)
- * into a kernel for dim, mode (0 local matrices, 1 local vectors, 2 per-cell
- * values) and facet (0 cells, 1 FacetBasis facets): NVRTC, sm_103a,
+ * into a kernel for dim, the test (vector) and trial (vector_u) bases' vector
+ * flags, mode (0 local matrices, 1 local vectors, 2 per-cell values) and
+ * facet (0 cells, 1 FacetBasis facets): NVRTC, sm_103a,
  * -fmad=false, the program as straight-line code -- the interpreter's
  * operations in the same order, so results are bitwise the interpreter's.
  * Returns FEM_ERR_UNSUPPORTED when libnvrtc is unavailable.  Release with
@@ -173,15 +174,15 @@ typedef struct FemProgram {
  */
 typedef struct FemCompiled FemCompiled;
 int fem_program_compile(const FemInstr* ins, int32_t ninstr, int32_t out, int32_t ncoef,
-                        int32_t dim, int32_t vector, int32_t mode, int32_t facet,
-                        FemCompiled** compiled);
+                        int32_t dim, int32_t vector, int32_t vector_u, int32_t mode,
+                        int32_t facet, FemCompiled** compiled);
 void fem_program_release(FemCompiled* compiled);
 /* The complete source fem_program_compile compiles for these arguments (its
  * headers: fem_faithful_core.cuh, fem_program_kernel.cuh and this file, by
  * name); *needed receives its length + 1.  Host-only, no GPU needed. */
 int fem_program_source(const FemInstr* ins, int32_t ninstr, int32_t out, int32_t ncoef,
-                       int32_t dim, int32_t vector, int32_t mode, int32_t facet, char* buf,
-                       int64_t size, int64_t* needed);
+                       int32_t dim, int32_t vector, int32_t vector_u, int32_t mode, int32_t facet,
+                       char* buf, int64_t size, int64_t* needed);
 
 /* Opaque one-time structure: row incidence, CSR pattern, local-to-slot map. */
 typedef struct FemPattern FemPattern;
@@ -367,6 +368,16 @@ int fem_condense_values(const int32_t* indptr, const int32_t* indices, const dou
 int fem_program_local_matrices(const FemMesh* mesh, const FemBasis* basis,
                                const FemProgram* program, double* local, int32_t* status,
                                fem_stream_t stream);
+/* Local matrices of a bilinear form with different trial (ubasis) and test
+ * (vbasis) bases on the same cells and points (BilinearForm.assemble(ubasis,
+ * vbasis), bilinear_form.py:58-128): local[(e*nv + i)*nu + j]. */
+int fem_program_local_matrices_mixed(const FemMesh* mesh, const FemBasis* vbasis,
+                                     const FemBasis* ubasis, const FemProgram* program,
+                                     double* local, int32_t* status, fem_stream_t stream);
+/* Pattern of the (ndofs_v x ndofs_u) matrix of such local matrices. */
+int fem_pattern_build_local_mixed(const FemMesh* mesh, const FemBasis* vbasis,
+                                  const FemBasis* ubasis, const double* local, FemPattern** out,
+                                  fem_stream_t stream);
 int fem_program_local_vectors(const FemMesh* mesh, const FemBasis* basis,
                               const FemProgram* program, double* local, int32_t* status,
                               fem_stream_t stream);

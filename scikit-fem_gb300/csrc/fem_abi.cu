@@ -32,7 +32,8 @@ int vector_sum(const Pattern& P, const double* local, double* b, cudaStream_t st
 void free_pattern(Pattern* P);
 int zero_check(const Pattern& P, const double* local, int32_t* status, cudaStream_t st);
 int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets* fc,
-                 const FemProgram& prog, double* out, int32_t* status, cudaStream_t st);
+                 const FemProgram& prog, double* out, int32_t* status, cudaStream_t st,
+                 const FemBasis* bu);
 int interpolate(const FemMesh& m, const FemBasis& b, const FemFacets* fc, int nq, const double* X,
                 const double* w, double* out, int32_t* status, cudaStream_t st);
 int sum_pairwise(const double* x, int64_t n, double* out, cudaStream_t st);
@@ -506,7 +507,49 @@ static int program_entry(int mode, const FemMesh* mesh, const FemBasis* basis,
     return FEM_ERR_ARGUMENT;
   }
   return fem::program_eval(mode, *mesh, *basis, facets, *program, out, status,
-                           (cudaStream_t)stream);
+                           (cudaStream_t)stream, nullptr);
+}
+
+int fem_program_local_matrices_mixed(const FemMesh* mesh, const FemBasis* vbasis,
+                                     const FemBasis* ubasis, const FemProgram* program,
+                                     double* local, int32_t* status, fem_stream_t stream) {
+  int rc = validate(mesh, vbasis);
+  if (!rc) rc = validate(mesh, ubasis);
+  if (rc) return rc;
+  if (!program || !local || !status) {
+    set_error(FEM_ERR_ARGUMENT, "null program, output or status");
+    return FEM_ERR_ARGUMENT;
+  }
+  return fem::program_eval(0, *mesh, *vbasis, nullptr, *program, local, status,
+                           (cudaStream_t)stream, ubasis);
+}
+
+int fem_pattern_build_local_mixed(const FemMesh* mesh, const FemBasis* vbasis,
+                                  const FemBasis* ubasis, const double* local, FemPattern** out,
+                                  fem_stream_t stream) {
+  int rc = validate(mesh, vbasis);
+  if (!rc) rc = validate(mesh, ubasis);
+  if (rc) return rc;
+  if (!out || (!local && mesh->nelems > 0)) {
+    set_error(FEM_ERR_ARGUMENT, "null local matrices or output handle");
+    return FEM_ERR_ARGUMENT;
+  }
+  *out = nullptr;
+  cudaStream_t st = (cudaStream_t)stream;
+  FemPattern* H = new FemPattern();
+  H->family = vbasis->family;
+  H->vector = vbasis->vector;
+  rc = fem::build_incidence(vbasis->element_dofs, mesh->nelems, vbasis->nbfun, vbasis->ndofs,
+                            &H->P, st);
+  if (!rc) rc = fem::build_csr(ubasis->element_dofs, ubasis->nbfun, ubasis->ndofs, local, &H->P, st);
+  if (!rc) rc = host_row_pointer(H, st);
+  if (rc) {
+    fem::free_pattern(new fem::Pattern(H->P));
+    delete H;
+    return rc;
+  }
+  *out = H;
+  return 0;
 }
 
 int fem_program_local_matrices(const FemMesh* mesh, const FemBasis* basis,

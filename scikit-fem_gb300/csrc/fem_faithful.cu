@@ -84,11 +84,11 @@ __global__ void mask_kernel(FemMesh m, FemBasis b, FemProgram prog, int nq, doub
 }
 
 // ------------------------------------------------------------ generic forms
-template <int D, int MODE, bool FACET, bool VEC>
-__global__ void program_kernel(FemMesh m, FemBasis b, FemFacets fc, FemProgram prog, Rule rule,
-                               GenericLayout s, int64_t ncells, double* __restrict__ out,
-                               int32_t* __restrict__ status) {
-  program_body<D, MODE, FACET, VEC>(m, b, fc, prog, rule, s, ncells, out, status);
+template <int D, int MODE, bool FACET, bool VEC, bool VECU>
+__global__ void program_kernel(FemMesh m, FemBasis b, FemBasis bu, FemFacets fc, FemProgram prog,
+                               Rule rule, GenericLayout s, int64_t ncells,
+                               double* __restrict__ out, int32_t* __restrict__ status) {
+  program_body<D, MODE, FACET, VEC, VECU>(m, b, bu, fc, prog, rule, s, ncells, out, status);
 }
 
 // Basis.interpolate: a block takes CPB cells (or facets); stage 0 stages
@@ -330,14 +330,26 @@ static bool facets_ok(const FemMesh& m, const FemBasis& b, const FemFacets* fc) 
 // mode 0: local matrices, 1: local vectors, 2: per-cell functional values;
 // fc non-null: over the facets of a FacetBasis
 int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets* fc,
-                 const FemProgram& prog, double* out, int32_t* status, cudaStream_t st) {
+                 const FemProgram& prog, double* out, int32_t* status, cudaStream_t st,
+                 const FemBasis* bu) {
   if (!facets_ok(m, b, fc)) return FEM_ERR_ARGUMENT;
-  int rc = check_program(prog, m.dim, b.vector != 0, true, prog.compiled == nullptr);
+  int rc = check_program(prog, m.dim, b.vector != 0 || (bu && bu->vector != 0), true,
+                         prog.compiled == nullptr);
   if (rc) return rc;
   const int64_t ncells = fc ? fc->nfacets : m.nelems;
   if (ncells == 0) return 0;
   const int nb = b.nbfun;
-  const int L = mode == 0 ? nb * nb : (mode == 1 ? nb : 1);
+  const bool mixed = bu && mode == 0;
+  const FemBasis& ub = mixed ? *bu : b;
+  if (mixed && fc) {
+    set_error(FEM_ERR_UNSUPPORTED, "different trial and test bases on facets are not supported");
+    return FEM_ERR_UNSUPPORTED;
+  }
+  if (mixed && prog.compiled && prog.compiled->vector_u != (ub.vector ? 1 : 0)) {
+    set_error(FEM_ERR_ARGUMENT, "compiled program is for another trial basis");
+    return FEM_ERR_ARGUMENT;
+  }
+  const int L = mode == 0 ? nb * ub.nbfun : (mode == 1 ? nb : 1);
   const int nq = prog.nq;
   fem_faithful::GenericLayout s;
   s.L = L;
@@ -347,6 +359,9 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets*
   s.cells = !fc && b.family != FEM_HEX_1;
   s.quants = mode != 2;   // a functional reads no basis function
   s.npoint = prog.compiled ? prog.compiled->npoint : 0;
+  s.mixed = mixed;
+  s.nbu = ub.nbfun;
+  s.nquantu = ub.vector ? m.dim + m.dim * m.dim : 1 + m.dim;
   auto bytes = [&](int epb) {
     fem_faithful::GenericLayout t = s;
     t.epb = epb;
@@ -373,6 +388,7 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets*
     }
     FemMesh mm = m;
     FemBasis bb = b;
+    FemBasis bbu = ub;
     FemFacets ff = F;
     FemProgram pp = prog;
     fem_faithful::Rule rr = rule;
@@ -380,7 +396,7 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets*
     int64_t nc = ncells;
     double* o = out;
     int32_t* stp = status;
-    void* args[] = {&mm, &bb, &ff, &pp, &rr, &ss, &nc, &o, &stp};
+    void* args[] = {&mm, &bb, &bbu, &ff, &pp, &rr, &ss, &nc, &o, &stp};
     return jit_launch(k, dim3(grid), dim3(threads), smem, st, args);
   }
   auto go = [&](auto kern) -> int {
@@ -389,7 +405,7 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets*
                                            (int)smem);
       if (e != cudaSuccess) return check_cuda(e, "program kernel smem");
     }
-    kern<<<grid, threads, smem, st>>>(m, b, F, prog, rule, s, ncells, out, status);
+    kern<<<grid, threads, smem, st>>>(m, b, ub, F, prog, rule, s, ncells, out, status);
     return 0;
   };
   using namespace fem_faithful;
@@ -397,14 +413,24 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets*
   auto pick = [&](auto facet_tag, auto vec_tag) -> int {
     constexpr bool FC = decltype(facet_tag)::value, VC = decltype(vec_tag)::value;
     if (m.dim == 2)
-      return mode == 0 ? go(program_kernel<2, 0, FC, VC>)
-                       : mode == 1 ? go(program_kernel<2, 1, FC, VC>) : go(program_kernel<2, 2, FC, VC>);
-    return mode == 0 ? go(program_kernel<3, 0, FC, VC>)
-                     : mode == 1 ? go(program_kernel<3, 1, FC, VC>) : go(program_kernel<3, 2, FC, VC>);
+      return mode == 0 ? go(program_kernel<2, 0, FC, VC, VC>)
+                       : mode == 1 ? go(program_kernel<2, 1, FC, VC, VC>)
+                                   : go(program_kernel<2, 2, FC, VC, VC>);
+    return mode == 0 ? go(program_kernel<3, 0, FC, VC, VC>)
+                     : mode == 1 ? go(program_kernel<3, 1, FC, VC, VC>)
+                                 : go(program_kernel<3, 2, FC, VC, VC>);
+  };
+  // different trial and test bases (bilinear forms on cells)
+  auto pick_mixed = [&](auto vv, auto vu) -> int {
+    constexpr bool V = decltype(vv)::value, U = decltype(vu)::value;
+    return m.dim == 2 ? go(program_kernel<2, 0, false, V, U>) : go(program_kernel<3, 0, false, V, U>);
   };
   using T = std::true_type;
   using Fl = std::false_type;
-  if (fc) rc = b.vector ? pick(T{}, T{}) : pick(T{}, Fl{});
+  if (mixed)
+    rc = b.vector ? (ub.vector ? pick_mixed(T{}, T{}) : pick_mixed(T{}, Fl{}))
+                  : (ub.vector ? pick_mixed(Fl{}, T{}) : pick_mixed(Fl{}, Fl{}));
+  else if (fc) rc = b.vector ? pick(T{}, T{}) : pick(T{}, Fl{});
   else rc = b.vector ? pick(Fl{}, T{}) : pick(Fl{}, Fl{});
   if (rc) return rc;
   FEM_LAUNCH_CHECK("program kernel");

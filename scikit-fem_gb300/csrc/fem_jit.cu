@@ -178,7 +178,7 @@ std::string program_source(const FemInstr* ins, int n, int out, bool hoist, int*
 
 // The complete source compiled for a program (headers by name).
 int kernel_source(const FemInstr* ins, int ninstr, int out, int ncoef, int dim, int vector,
-                  int mode, int facet, std::string& src, int* npoint);
+                  int vector_u, int mode, int facet, std::string& src, int* npoint);
 
 }  // namespace
 
@@ -199,7 +199,7 @@ int jit_launch(const FemCompiled* k, dim3 grid, dim3 block, size_t smem, cudaStr
 
 namespace {
 int kernel_source(const FemInstr* ins, int ninstr, int out, int ncoef, int dim, int vector,
-                  int mode, int facet, std::string& src, int* npoint) {
+                  int vector_u, int mode, int facet, std::string& src, int* npoint) {
   using fem::set_error;
   if (!ins || (dim != 2 && dim != 3) || mode < 0 || mode > 2 || ninstr <= 0 ||
       ninstr > fem_faithful::kMaxProgram || out < 0 || out >= ninstr || ncoef < 0 ||
@@ -207,8 +207,10 @@ int kernel_source(const FemInstr* ins, int ninstr, int out, int ncoef, int dim, 
     set_error(FEM_ERR_ARGUMENT, "form program: invalid arguments");
     return FEM_ERR_ARGUMENT;
   }
-  // operand checks (the same as the interpreter's)
-  if (int rc = fem::check_instructions(ins, ninstr, ncoef, dim, vector != 0)) return rc;
+  // operand checks (the same as the interpreter's; trial quantities of a
+  // vector trial basis may index further)
+  if (int rc = fem::check_instructions(ins, ninstr, ncoef, dim, vector != 0 || vector_u != 0))
+    return rc;
   src.clear();
   // bilinear and linear forms evaluate each point's u/v-free part once;
   // a functional has one entry per cell and runs the program whole
@@ -227,12 +229,13 @@ int kernel_source(const FemInstr* ins, int ninstr, int out, int ncoef, int dim, 
   }
   char tail[512];
   std::snprintf(tail, sizeof tail,
-                "extern \"C\" __global__ void fem_jit_program(FemMesh m, FemBasis b, FemFacets fc, "
-                "FemProgram prog, fem_faithful::Rule rule, fem_faithful::GenericLayout s, "
-                "int64_t ncells, double* out, int32_t* status) {\n"
-                "  fem_faithful::program_body<%d, %d, %s, %s>(m, b, fc, prog, rule, s, ncells, "
-                "out, status);\n}\n",
-                dim, mode, facet ? "true" : "false", vector ? "true" : "false");
+                "extern \"C\" __global__ void fem_jit_program(FemMesh m, FemBasis b, FemBasis bu, "
+                "FemFacets fc, FemProgram prog, fem_faithful::Rule rule, "
+                "fem_faithful::GenericLayout s, int64_t ncells, double* out, int32_t* status) {\n"
+                "  fem_faithful::program_body<%d, %d, %s, %s, %s>(m, b, bu, fc, prog, rule, s, "
+                "ncells, out, status);\n}\n",
+                dim, mode, facet ? "true" : "false", vector ? "true" : "false",
+                (mode == 0 ? vector_u : vector) ? "true" : "false");
   src += tail;
   return 0;
 }
@@ -241,11 +244,12 @@ int kernel_source(const FemInstr* ins, int ninstr, int out, int ncoef, int dim, 
 extern "C" {
 
 int fem_program_source(const FemInstr* ins, int32_t ninstr, int32_t out, int32_t ncoef,
-                       int32_t dim, int32_t vector, int32_t mode, int32_t facet, char* buf,
-                       int64_t size, int64_t* needed) {
+                       int32_t dim, int32_t vector, int32_t vector_u, int32_t mode, int32_t facet,
+                       char* buf, int64_t size, int64_t* needed) {
   std::string src;
   int npoint = 0;
-  if (int rc = kernel_source(ins, ninstr, out, ncoef, dim, vector, mode, facet, src, &npoint))
+  if (int rc = kernel_source(ins, ninstr, out, ncoef, dim, vector, vector_u, mode, facet, src,
+                             &npoint))
     return rc;
   if (needed) *needed = (int64_t)src.size() + 1;
   if (buf && size > 0) {
@@ -257,8 +261,8 @@ int fem_program_source(const FemInstr* ins, int32_t ninstr, int32_t out, int32_t
 }
 
 int fem_program_compile(const FemInstr* ins, int32_t ninstr, int32_t out, int32_t ncoef,
-                        int32_t dim, int32_t vector, int32_t mode, int32_t facet,
-                        FemCompiled** compiled) {
+                        int32_t dim, int32_t vector, int32_t vector_u, int32_t mode,
+                        int32_t facet, FemCompiled** compiled) {
   using fem::set_error;
   if (!compiled) {
     set_error(FEM_ERR_ARGUMENT, "fem_program_compile: null output");
@@ -267,7 +271,8 @@ int fem_program_compile(const FemInstr* ins, int32_t ninstr, int32_t out, int32_
   *compiled = nullptr;
   std::string src;
   int npoint = 0;
-  if (int rc = kernel_source(ins, ninstr, out, ncoef, dim, vector, mode, facet, src, &npoint))
+  if (int rc = kernel_source(ins, ninstr, out, ncoef, dim, vector, vector_u, mode, facet, src,
+                             &npoint))
     return rc;
   std::lock_guard<std::mutex> lock(g_mu);
   if (!load_nvrtc()) {
@@ -306,6 +311,7 @@ int fem_program_compile(const FemInstr* ins, int32_t ninstr, int32_t out, int32_
   k->mode = mode;
   k->facet = facet ? 1 : 0;
   k->npoint = npoint;
+  k->vector_u = mode == 0 ? (vector_u ? 1 : 0) : (vector ? 1 : 0);
   cudaError_t e = cudaLibraryLoadData(&k->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
   if (e == cudaSuccess) e = cudaLibraryGetKernel(&k->kernel, k->lib, "fem_jit_program");
   if (e != cudaSuccess) {

@@ -57,18 +57,25 @@ struct GenericLayout {
   int epb, L, nq, nb, nquant;
   bool cells, quants;  // per-cell affine maps staged; basis quantities staged
   int npoint;          // compiled programs: values hoisted per point (0: none)
+  bool mixed;          // a trial basis of its own (nbu functions, nquantu quantities)
+  int nbu, nquantu;
   __host__ __device__ size_t geo() const { return 0; }
   __host__ __device__ size_t val() const { return (size_t)epb * nq * kGeo; }
   __host__ __device__ size_t cell() const { return val() + (size_t)epb * L * nq; }
   __host__ __device__ size_t quant() const { return cell() + (cells ? (size_t)epb * kCell : 0); }
-  __host__ __device__ size_t point() const {
+  __host__ __device__ size_t quantu() const {
     return quant() + (quants ? (size_t)epb * nq * nb * nquant : 0);
+  }
+  __host__ __device__ size_t point() const {
+    return quantu() + (mixed ? (size_t)epb * nq * nbu * nquantu : 0);
   }
   __host__ __device__ size_t total() const { return point() + (size_t)epb * nq * npoint; }
 };
 
-template <int D, int MODE, bool FACET, bool VEC>
+// b: the test basis (and trial basis unless s.mixed); bu: the trial basis.
+template <int D, int MODE, bool FACET, bool VEC, bool VECU>
 __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b,
+                                             const FemBasis& bu,
                                              const FemFacets& fc, const FemProgram& prog,
                                              const Rule& rule, const GenericLayout& s,
                                              int64_t ncells, double* __restrict__ out,
@@ -81,9 +88,12 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
   const bool hex = b.family == FEM_HEX_1;
   constexpr bool vec = VEC;
   constexpr int NQ = VEC ? D + D * D : 1 + D;   // quantities per basis function
+  constexpr int NQU = VECU ? D + D * D : 1 + D; // ... of the trial basis
   const ProgFlags f = prog_flags(prog);
   const int64_t e0 = (int64_t)blockIdx.x * s.epb;
   const int nb = b.nbfun;
+  const int nbu = s.mixed ? bu.nbfun : nb;      // trial functions
+  double* Qu = s.mixed ? gsm + s.quantu() : Q;
   // stage 0: affine cell maps (9 divisions each), once per cell
   if (s.cells) {
     for (int el = threadIdx.x; el < s.epb; el += blockDim.x) {
@@ -138,6 +148,20 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
 #pragma unroll
       for (int a = 0; a < NQ; ++a) Q[(size_t)k * NQ + a] = qq[a];
     }
+    if (s.mixed) {
+      for (int k = threadIdx.x; k < s.epb * s.nq * nbu; k += blockDim.x) {
+        const int p = k / nbu, fn = k - p * nbu;
+        if (e0 + p / s.nq >= ncells) continue;
+        const double* G = geo + (size_t)p * kGeo;
+        double inv[3][3];
+        for (int a = 0; a < 3; ++a)
+          for (int c = 0; c < 3; ++c) inv[a][c] = G[a * 3 + c];
+        double qq[D + D * D];
+        quantities<D>(bu.family, VECU, fn, G[17], G[18], G[19], inv, qq);
+#pragma unroll
+        for (int a = 0; a < NQU; ++a) Qu[(size_t)k * NQU + a] = qq[a];
+      }
+    }
     __syncthreads();
   }
 #ifdef FEM_JIT_HOIST
@@ -167,8 +191,8 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
     const int r = rq / s.nq, q = rq - r * s.nq;
     const int64_t e = e0 + el;
     if (e >= ncells) continue;
-    const int i = MODE == 0 ? r / nb : (MODE == 1 ? r : 0);
-    const int j = MODE == 0 ? r - i * nb : 0;
+    const int i = MODE == 0 ? r / nbu : (MODE == 1 ? r : 0);
+    const int j = MODE == 0 ? r - i * nbu : 0;
     const double* G = geo + ((size_t)el * s.nq + q) * kGeo;
     PointGeo g;
     for (int a = 0; a < 3; ++a)
@@ -178,14 +202,16 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
     double qu[D + D * D], qv[D + D * D];
     if (s.quants) {
       const double* Qp = Q + ((size_t)(el * s.nq + q) * nb) * NQ;
+      const double* Qup = Qu + ((size_t)(el * s.nq + q) * nbu) * NQU;
 #pragma unroll
-      for (int a = 0; a < NQ; ++a) {
-        qu[a] = Qp[(size_t)j * NQ + a];
-        qv[a] = Qp[(size_t)i * NQ + a];
-      }
+      for (int a = 0; a < NQU; ++a) qu[a] = Qup[(size_t)j * NQU + a];
+#pragma unroll
+      for (int a = 0; a < NQ; ++a) qv[a] = Qp[(size_t)i * NQ + a];
     } else {
 #pragma unroll
-      for (int a = 0; a < NQ; ++a) qu[a] = qv[a] = 0.0;
+      for (int a = 0; a < NQU; ++a) qu[a] = 0.0;
+#pragma unroll
+      for (int a = 0; a < NQ; ++a) qv[a] = 0.0;
     }
 #ifdef FEM_JIT_HOIST
     const double fq = jit_form_hoisted(qu, qv, P + ((size_t)el * s.nq + q) * s.npoint);

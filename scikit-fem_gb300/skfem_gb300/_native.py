@@ -118,12 +118,16 @@ _SIGS = {
                                             _P, _P]),
     "fem_program_compile": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                            ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
-                                           ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
+                                           ctypes.c_int32, ctypes.c_int32,
+                                           ctypes.POINTER(ctypes.c_void_p)]),
+    "fem_program_local_matrices_mixed": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
+    "fem_pattern_build_local_mixed": (ctypes.c_int, [_P, _P, _P, _P,
+                                                     ctypes.POINTER(ctypes.c_void_p), _P]),
     "fem_program_release": (None, [_P]),
     "fem_program_source": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                           ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
-                                          ctypes.c_int32, ctypes.c_char_p, ctypes.c_int64,
-                                          ctypes.POINTER(ctypes.c_int64)]),
+                                          ctypes.c_int32, ctypes.c_int32, ctypes.c_char_p,
+                                          ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]),
     "fem_assemble_local": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_int64,
                                           _P]),
     "fem_csr_sum_to_host": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32, _P, _P]),

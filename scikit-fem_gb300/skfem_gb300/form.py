@@ -271,16 +271,20 @@ class Form:
         self._traces[key] = ch
         return ch
 
-    def _generic(self, basis, coeffs, kind):
+    def _generic(self, basis, coeffs, kind, ubasis=None):
         """The form's program for the generic kernels (cached per argument
-        structure) and its cache key."""
+        structure) and its cache key.  basis: the test basis; ubasis: a trial
+        basis of its own (bilinear forms)."""
         key = ("program",) + self._key(basis, coeffs, kind)
+        if ubasis is not None:
+            key += ("trial", ubasis.elem.family, ubasis.elem.vector)
         g = self._traces.get(key)
         if g is None:
             ins, out, names = trace_tape(self.form, basis.elem, basis.mesh.p.shape[0],
                                          coeffs.specs(), coeffs.numbers, kind=kind,
                                          defaults="facet" if hasattr(basis, "c_facets")
-                                         else "cell")
+                                         else "cell",
+                                         uelem=ubasis.elem if ubasis is not None else None)
             g = _GenericProgram(ins, out, names)
             self._traces[key] = g
         return g, key
@@ -302,7 +306,7 @@ class _GenericProgram:
         self._dev = {}
         self._compiled = {}
 
-    def struct(self, basis, coeffs, kind):
+    def struct(self, basis, coeffs, kind, ubasis=None):
         dev = self._dev.get(basis.device)
         if dev is None:
             dev = torch.frombuffer(bytearray(self._host), dtype=torch.uint8).to(basis.device)
@@ -313,10 +317,10 @@ class _GenericProgram:
             prog.coef[k], prog.coef_stride[k] = coeffs.slot(n, basis.nelems, nq)
         prog.qX = basis.X_dev.data_ptr()
         prog.qW = basis.W_dev.data_ptr()
-        prog.compiled = self._kernel(basis, kind)
+        prog.compiled = self._kernel(basis, kind, ubasis)
         return prog
 
-    def _kernel(self, basis, kind):
+    def _kernel(self, basis, kind, ubasis=None):
         """The program compiled to straight-line code for this basis kind
         (once; None keeps the interpreter: compilation disabled with
         SKFEM_GB300_JIT=0 or unavailable)."""
@@ -325,13 +329,14 @@ class _GenericProgram:
         mode = {"bilinear": 0, "linear": 1, "functional": 2}[kind]
         facet = int(hasattr(basis, "c_facets"))
         dim = basis.mesh.p.shape[0]
-        key = (str(basis.device), dim, int(basis.elem.vector), mode, facet)
+        vec_u = int((ubasis if ubasis is not None else basis).elem.vector)
+        key = (str(basis.device), dim, int(basis.elem.vector), vec_u, mode, facet)
         if key not in self._compiled:
             h = ctypes.c_void_p()
             with torch.cuda.device(basis.device):
                 rc = N.lib().fem_program_compile(ctypes.addressof(self._host), len(self.ins),
                                                  self.out, len(self.names), dim,
-                                                 int(basis.elem.vector), mode, facet,
+                                                 int(basis.elem.vector), vec_u, mode, facet,
                                                  ctypes.byref(h))
             if rc == N.FEM_ERR_UNSUPPORTED:
                 self._compiled[key] = None
@@ -386,10 +391,15 @@ def _program(form, basis, coeffs):
 
 
 class _PatternEntry:
-    def __init__(self, basis, c_form, stream, program=None, local=None):
+    def __init__(self, basis, c_form, stream, program=None, local=None, ubasis=None):
         lib = N.lib()
         h = ctypes.c_void_p()
-        if local is not None:
+        if ubasis is not None:
+            # basis: the test basis (rows), ubasis: the trial basis (columns)
+            N.check(lib.fem_pattern_build_local_mixed(N.byref(basis.c_mesh), N.byref(basis.c_basis),
+                                                      N.byref(ubasis.c_basis), N.ptr(local),
+                                                      ctypes.byref(h), stream))
+        elif local is not None:
             N.check(lib.fem_pattern_build_local(N.byref(basis.c_mesh_pat),
                                                 N.byref(basis.c_basis_pat), N.ptr(local),
                                                 ctypes.byref(h), stream))
@@ -403,7 +413,7 @@ class _PatternEntry:
         self.nrows = self.pat.nrows
         self.nnz = self.pat.nnz
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
-        if c_form is not None or local is not None:
+        if c_form is not None or local is not None or ubasis is not None:
             self.indptr = torch.empty(self.nrows + 1, dtype=torch.int32, device=dev)
             self.indices = torch.empty(max(self.nnz, 1), dtype=torch.int32, device=dev)[:self.nnz]
             N.check(lib.fem_pattern_export(self.pat.handle, N.ptr(self.indptr),
@@ -446,7 +456,7 @@ def _raise_status(st):
         raise ValueError("a facet's cell index is out of range")
 
 
-def _host_csr(entry, vals, n):
+def _host_csr(entry, vals, n, ncols=None):
     """Device CSR -> scipy.sparse.csr_matrix through pinned host buffers
     (torch's caching host allocator reuses the blocks of matrices the
     caller has dropped); the matrix owns its arrays through numpy views."""
@@ -457,7 +467,8 @@ def _host_csr(entry, vals, n):
     indices.copy_(entry.indices, non_blocking=True)
     indptr.copy_(entry.indptr, non_blocking=True)
     torch.cuda.current_stream().synchronize()
-    K = sp.csr_matrix((data.numpy(), indices.numpy(), indptr.numpy()), shape=(n, n), copy=False)
+    K = sp.csr_matrix((data.numpy(), indices.numpy(), indptr.numpy()),
+                      shape=(n, n if ncols is None else ncols), copy=False)
     K.has_sorted_indices = True
     K.has_canonical_format = True
     return K
@@ -543,6 +554,56 @@ class BilinearForm(Form):
                                             stream))
         return entry, vals
 
+    # ---------------------------------------------- different trial / test
+    def _check_pair(self, ubasis, vbasis):
+        """bilinear_form.py:64-70: both bases on the same cells and points."""
+        if hasattr(ubasis, "c_facets") or hasattr(vbasis, "c_facets"):
+            raise NotImplementedError("different trial and test FacetBases are not supported")
+        if ubasis.X.shape[1] != vbasis.X.shape[1] or not np.array_equal(ubasis.X, vbasis.X):
+            raise ValueError("Quadrature mismatch: trial and test functions should have "
+                             "same number of integration points.")
+        same_mesh = ubasis.mesh is vbasis.mesh or (
+            np.array_equal(ubasis.mesh.p, vbasis.mesh.p) and
+            np.array_equal(ubasis.mesh.t, vbasis.mesh.t))
+        same_cells = (ubasis.tind is None and vbasis.tind is None) or (
+            ubasis.tind is not None and vbasis.tind is not None and
+            np.array_equal(ubasis.tind, vbasis.tind))
+        if not (same_mesh and same_cells):
+            raise NotImplementedError("trial and test bases on different cells are not supported")
+
+    def _mixed_assemble(self, ubasis, vbasis, kwargs, check=True):
+        self._check_pair(ubasis, vbasis)
+        coeffs = _Coefficients(ubasis, kwargs)                 # form.py:91-121 (ubasis)
+        g, key = self._generic(vbasis, coeffs, "bilinear", ubasis)
+        prog = g.struct(vbasis, coeffs, "bilinear", ubasis)
+        nl = vbasis.nelems * vbasis.Nbfun * ubasis.Nbfun
+        local = torch.empty(max(1, nl), dtype=torch.float64, device=vbasis.device)
+        status = torch.zeros(1, dtype=torch.int32, device=vbasis.device)
+        stream = N.stream_ptr()
+        N.check(N.lib().fem_program_local_matrices_mixed(
+            N.byref(vbasis.c_mesh), N.byref(vbasis.c_basis), N.byref(ubasis.c_basis),
+            N.byref(prog), N.ptr(local), N.ptr(status), stream))
+        pkey = key + ("trial-dofs", ubasis.N)
+        entry = vbasis._patterns.get(pkey)
+        fresh = entry is None
+        if fresh:
+            entry = _PatternEntry(vbasis, None, stream, local=local, ubasis=ubasis)
+            vbasis._patterns[pkey] = entry
+        vals = torch.empty(max(entry.nnz, 1), dtype=torch.float64, device=vbasis.device)[:entry.nnz]
+        N.check(N.lib().fem_csr_sum_checked(entry.pat.handle, N.ptr(local), N.ptr(vals),
+                                            N.ptr(status), stream))
+        if check or fresh:
+            st = int(status.item())
+            _raise_status(st)
+            if st & (1 << N.FEM_ERR_STALE_PATTERN):
+                entry = _PatternEntry(vbasis, None, stream, local=local, ubasis=ubasis)
+                vbasis._patterns[pkey] = entry
+                vals = torch.empty(max(entry.nnz, 1), dtype=torch.float64,
+                                   device=vbasis.device)[:entry.nnz]
+                N.check(N.lib().fem_csr_sum(entry.pat.handle, N.ptr(local), N.ptr(vals), None,
+                                            stream))
+        return entry, vals
+
     # ------------------------------------------------------------- driver
     def _assemble_device(self, ubasis, vbasis, kwargs, check=True, coeffs=None):
         if vbasis is not None and vbasis is not ubasis:
@@ -571,7 +632,8 @@ class BilinearForm(Form):
         index arrays are copied to the host on a side stream while the
         kernels run, and the call synchronises once before returning."""
         if vbasis is not None and vbasis is not ubasis:
-            raise NotImplementedError("different trial and test bases are not supported yet")
+            entry, vals = self._mixed_assemble(ubasis, vbasis, kwargs)
+            return _host_csr(entry, vals, vbasis.N, ubasis.N)
         coeffs = _Coefficients(ubasis, kwargs, strided=True)
         ch = self._trace(ubasis, coeffs, "bilinear")
         if ch is not None:
@@ -664,6 +726,10 @@ class BilinearForm(Form):
     def assemble_torch(self, ubasis, vbasis=None, check=True, **kwargs):
         """Device-resident result: torch.sparse_csr_tensor (int32 indices,
         float64 values) sharing the cached pattern arrays."""
+        if vbasis is not None and vbasis is not ubasis:
+            entry, vals = self._mixed_assemble(ubasis, vbasis, kwargs, check=check)
+            return torch.sparse_csr_tensor(entry.indptr, entry.indices, vals,
+                                           size=(vbasis.N, ubasis.N))
         entry, vals = self._assemble_device(ubasis, vbasis, kwargs, check=check)
         return torch.sparse_csr_tensor(entry.indptr, entry.indices, vals,
                                        size=(ubasis.N, ubasis.N))

@@ -592,17 +592,18 @@ def _compact(ins, out, slots):
     return new, names
 
 
-def trace_tape(form, elem, dim, fields, numbers_, kind="bilinear", defaults=False):
+def trace_tape(form, elem, dim, fields, numbers_, kind="bilinear", defaults=False, uelem=None):
     """Record the exact-order program of a form; returns (instructions,
     output index, coefficient slot keys).  kind: 'bilinear' (form(u, v, w)),
     'linear' (form(v, w)) or 'functional' (form(w)).  defaults: True / 'cell'
     adds w.x and w.h, 'facet' also w.n.  fields: names of
     per-element coefficients, or {name: FieldSpec}; slot keys are the names
-    ('elem'/'qp') or (name, quantity) pairs ('field')."""
+    ('elem'/'qp') or (name, quantity) pairs ('field').  uelem: the trial
+    element when it differs from the test element ``elem``."""
     tape = Tape()
     w = TapeParams(tape, fields, numbers_, dim=dim, defaults=defaults)
     if kind == "bilinear":
-        u = _tape_field(tape, "u", elem, dim)
+        u = _tape_field(tape, "u", uelem if uelem is not None else elem, dim)
         v = _tape_field(tape, "v", elem, dim)
         r = form(u, v, w)
     elif kind == "linear":

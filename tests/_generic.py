@@ -97,3 +97,18 @@ def reference_vector(local, element_dofs, n):
 
 def fixture_csr(g, suffix):
     return (g["indptr_" + suffix], g["indices_" + suffix], g["data_" + suffix])
+
+
+@F.BilinearForm
+def bdiv(u, v, w):
+    return div(u) * v
+
+
+@F.BilinearForm
+def bdiv_t(u, v, w):
+    return u * div(v)
+
+
+@F.BilinearForm
+def coupling(u, v, w):
+    return (1.0 + w['s'] ** 2) * u * v + dot(grad(u), grad(v)) + w.x[0] * grad(u)[0] * v

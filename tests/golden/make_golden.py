@@ -200,6 +200,7 @@ def main():
 
     generic_cases()
     facet_cases()
+    mixed_cases()
 
     # quadrature rules the configs use, exactly as the reference tabulates them
     from skfem.quadrature import get_quadrature_tet, get_quadrature_tri
@@ -466,6 +467,50 @@ def hex_facet_case():
     save("hex1_facet", **arrs)
 
 
+def mixed_cases():
+    """BilinearForm.assemble(ubasis, vbasis) with different trial and test
+    bases on one mesh (mixed methods): the Stokes divergence block and its
+    transpose, a P2 x P1 coupling with an interpolated trial-side field."""
+    from skfem.helpers import div
+    rng = np.random.default_rng(20261207)
+
+    @BilinearForm
+    def bdiv(u, v, w):
+        return div(u) * v
+
+    @BilinearForm
+    def bdiv_t(u, v, w):
+        return u * div(v)
+
+    @BilinearForm
+    def coupling(u, v, w):
+        return (1.0 + w['s'] ** 2) * u * v + dot(grad(u), grad(v)) + w.x[0] * grad(u)[0] * v
+
+    n = 5
+    m = MeshTri.init_tensor(np.linspace(0, 1, n + 1), np.linspace(0, 1, n + 1))
+    p = m.p.copy()
+    inner = jitter(m, rng, 0.2)
+    p[:, inner] += rng.uniform(-0.2 / n, 0.2 / n, size=(2, int(inner.sum())))
+    m = MeshTri(p, m.t)
+    ub = Basis(m, ElementVector(ElementTriP2()))
+    pb = Basis(m, ElementTriP1(), intorder=4)
+    sb = Basis(m, ElementTriP2())
+    s = rng.standard_normal(sb.N)
+    save("tri_mixed", p=m.p, t=m.t, s=s,
+         **{k + "_bdiv": v for k, v in csr_arrays(bdiv.assemble(ub, pb)).items()},
+         **{k + "_bdivt": v for k, v in csr_arrays(bdiv_t.assemble(pb, ub)).items()},
+         **{k + "_coupling": v for k, v in csr_arrays(coupling.assemble(sb, pb, s=s)).items()})
+    m = MeshTet.init_tensor(*(np.linspace(0, 1, 3),) * 3)
+    p = m.p.copy()
+    inner = jitter(m, rng, 0.2)
+    p[:, inner] += rng.uniform(-0.1, 0.1, size=(3, int(inner.sum())))
+    m = MeshTet(p, m.t)
+    ub = Basis(m, ElementVector(ElementTetP2()))
+    pb = Basis(m, ElementTetP1(), intorder=4)
+    save("tet_mixed", p=m.p, t=m.t,
+         **{k + "_bdiv": v for k, v in csr_arrays(bdiv.assemble(ub, pb)).items()})
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["--generic"]:
         generic_cases()
@@ -473,5 +518,7 @@ if __name__ == "__main__":
         facet_cases()
     elif sys.argv[1:] == ["--hex-facet"]:
         hex_facet_case()
+    elif sys.argv[1:] == ["--mixed"]:
+        mixed_cases()
     else:
         main()

@@ -202,3 +202,33 @@ def test_compiled_programs_equal_the_interpreter(monkeypatch):
                      newton_res.assemble(b, s=g["s"])])
     for a, c in zip(*runs):
         np.testing.assert_array_equal(a, c)
+
+
+def test_mixed_bases_vs_reference():
+    """Different trial and test bases (Stokes divergence block, its
+    transpose, a P2 x P1 coupling with a trial-side DOF vector) against the
+    reference: rectangular CSR, pattern bit-exact, values within the bounds."""
+    from _generic import bdiv, bdiv_t, coupling
+    g = golden("tri_mixed")
+    m = F.MeshTri(g["p"], g["t"])
+    ub = F.Basis(m, F.ElementVector(F.ElementTriP2()))
+    pb = F.Basis(m, F.ElementTriP1(), intorder=4)
+    sb = F.Basis(m, F.ElementTriP2())
+    for K, sfx in ((bdiv.assemble(ub, pb), "bdiv"), (bdiv_t.assemble(pb, ub), "bdivt"),
+                   (coupling.assemble(sb, pb, s=g["s"]), "coupling")):
+        assert tuple(K.shape) == tuple(g["shape_" + sfx])
+        same, extra, missing, noise, rf, rm = csr_diff(
+            K.indptr, K.indices, K.data, g["indptr_" + sfx], g["indices_" + sfx],
+            g["data_" + sfx], K.shape)
+        assert same and rf <= REL_FRO and rm <= REL_MAX, (sfx, extra, missing, rf, rm)
+    T = bdiv.assemble_torch(ub, pb)
+    assert tuple(T.shape) == (pb.N, ub.N)
+    with pytest.raises(ValueError):
+        bdiv.assemble(ub, F.Basis(m, F.ElementTriP1()))       # quadrature mismatch
+    gt = golden("tet_mixed")
+    mt = F.MeshTet(gt["p"], gt["t"])
+    K = bdiv.assemble(F.Basis(mt, F.ElementVector(F.ElementTetP2())),
+                      F.Basis(mt, F.ElementTetP1(), intorder=4))
+    same, extra, missing, noise, rf, rm = csr_diff(K.indptr, K.indices, K.data, gt["indptr_bdiv"],
+                                                   gt["indices_bdiv"], gt["data_bdiv"], K.shape)
+    assert same and rf <= REL_FRO and rm <= REL_MAX

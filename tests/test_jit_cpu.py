@@ -36,12 +36,12 @@ def source_of(form, elem, dim, specs, kind, mode, facet):
     arr = (N.FemInstr * len(ins))(*[N.FemInstr(op, a, b, 0, imm) for op, a, b, imm in ins])
     need = ctypes.c_int64()
     lib = N.lib()
-    assert lib.fem_program_source(ctypes.addressof(arr), len(ins), out, len(names), dim,
-                                  int(elem.vector), mode, int(facet), None, 0,
-                                  ctypes.byref(need)) == 0
+    v = int(elem.vector)
+    assert lib.fem_program_source(ctypes.addressof(arr), len(ins), out, len(names), dim, v, v,
+                                  mode, int(facet), None, 0, ctypes.byref(need)) == 0
     buf = ctypes.create_string_buffer(need.value)
-    assert lib.fem_program_source(ctypes.addressof(arr), len(ins), out, len(names), dim,
-                                  int(elem.vector), mode, int(facet), buf, need.value, None) == 0
+    assert lib.fem_program_source(ctypes.addressof(arr), len(ins), out, len(names), dim, v, v,
+                                  mode, int(facet), buf, need.value, None) == 0
     return buf.value.decode(), len(ins)
 
 
@@ -85,5 +85,5 @@ def test_program_source_compiles_for_sm103a(name, form, elem, dim, specs, kind, 
 
 def test_program_source_rejects_bad_operands():
     bad = (N.FemInstr * 2)(N.FemInstr(1, 0, -1, 0, 0.0), N.FemInstr(4, 0, 5, 0, 0.0))
-    assert N.lib().fem_program_source(ctypes.addressof(bad), 2, 1, 0, 2, 0, 0, 0, None, 0,
+    assert N.lib().fem_program_source(ctypes.addressof(bad), 2, 1, 0, 2, 0, 0, 0, 0, None, 0,
                                       None) == N.FEM_ERR_ARGUMENT

@@ -157,3 +157,21 @@ def test_oracle_generic_forms_vs_reference():
             np.testing.assert_array_equal(K.indptr, ip)
             np.testing.assert_array_equal(K.indices, ix)
             np.testing.assert_array_equal(K.data, dat)
+
+
+def test_oracle_mixed_bases_vs_reference():
+    """BilinearForm.assemble(ubasis, vbasis) with different trial and test
+    bases (bilinear_form.py:58-128): the oracle's two-basis loop against the
+    reference, bit for bit."""
+    from _generic import bdiv, bdiv_t, coupling
+    g = load("tri_mixed")
+    m = O.OMesh(g["p"], g["t"], "tri")
+    ub = O.OBasis(m, O.Vector(O.TriP2()))
+    pb = O.OBasis(m, O.TriP1(), intorder=4)
+    sb = O.OBasis(m, O.TriP2())
+    for form, u, v, kw, sfx in ((bdiv, ub, pb, {}, "bdiv"), (bdiv_t, pb, ub, {}, "bdivt"),
+                                (coupling, sb, pb, {"s": g["s"]}, "coupling")):
+        K = O.bilinear_assemble(form.form, u, v, **kw)
+        np.testing.assert_array_equal(K.indptr, g["indptr_" + sfx])
+        np.testing.assert_array_equal(K.indices, g["indices_" + sfx])
+        np.testing.assert_array_equal(K.data, g["data_" + sfx])
