@@ -143,7 +143,9 @@ static int host_row_pointer(FemPattern* H, cudaStream_t st) {
   return 0;
 }
 
-static int validate(const FemMesh* m, const FemBasis* b) {
+// generic: the entry point runs the generic kernels, which also take
+// ElementVector(ElementHex1); the channel kernels do not.
+static int validate(const FemMesh* m, const FemBasis* b, bool generic = false) {
   if (!m || !b) {
     set_error(FEM_ERR_ARGUMENT, "null mesh or basis");
     return FEM_ERR_ARGUMENT;
@@ -174,8 +176,8 @@ static int validate(const FemMesh* m, const FemBasis* b) {
     set_error(FEM_ERR_ARGUMENT, "invalid mesh arrays");
     return FEM_ERR_ARGUMENT;
   }
-  if (b->vector && b->family == FEM_HEX_1) {
-    set_error(FEM_ERR_UNSUPPORTED, "ElementVector(ElementHex1) is not implemented");
+  if (b->vector && b->family == FEM_HEX_1 && !generic) {
+    set_error(FEM_ERR_UNSUPPORTED, "ElementVector(ElementHex1) runs on the generic kernels only");
     return FEM_ERR_UNSUPPORTED;
   }
   return 0;
@@ -500,7 +502,7 @@ int fem_assemble_vector(const FemMesh* mesh, const FemBasis* basis, const FemLin
 static int program_entry(int mode, const FemMesh* mesh, const FemBasis* basis,
                          const FemFacets* facets, const FemProgram* program, double* out,
                          int32_t* status, fem_stream_t stream) {
-  int rc = validate(mesh, basis);
+  int rc = validate(mesh, basis, true);
   if (rc) return rc;
   if (!program || !out || !status) {
     set_error(FEM_ERR_ARGUMENT, "null program, output or status");
@@ -513,8 +515,8 @@ static int program_entry(int mode, const FemMesh* mesh, const FemBasis* basis,
 int fem_program_local_matrices_mixed(const FemMesh* mesh, const FemBasis* vbasis,
                                      const FemBasis* ubasis, const FemProgram* program,
                                      double* local, int32_t* status, fem_stream_t stream) {
-  int rc = validate(mesh, vbasis);
-  if (!rc) rc = validate(mesh, ubasis);
+  int rc = validate(mesh, vbasis, true);
+  if (!rc) rc = validate(mesh, ubasis, true);
   if (rc) return rc;
   if (!program || !local || !status) {
     set_error(FEM_ERR_ARGUMENT, "null program, output or status");
@@ -527,8 +529,8 @@ int fem_program_local_matrices_mixed(const FemMesh* mesh, const FemBasis* vbasis
 int fem_pattern_build_local_mixed(const FemMesh* mesh, const FemBasis* vbasis,
                                   const FemBasis* ubasis, const double* local, FemPattern** out,
                                   fem_stream_t stream) {
-  int rc = validate(mesh, vbasis);
-  if (!rc) rc = validate(mesh, ubasis);
+  int rc = validate(mesh, vbasis, true);
+  if (!rc) rc = validate(mesh, ubasis, true);
   if (rc) return rc;
   if (!out || (!local && mesh->nelems > 0)) {
     set_error(FEM_ERR_ARGUMENT, "null local matrices or output handle");
@@ -601,7 +603,7 @@ int fem_facet_program_elemental(const FemMesh* mesh, const FemBasis* basis,
 int fem_facet_interpolate(const FemMesh* mesh, const FemBasis* basis, const FemFacets* facets,
                           int32_t nq, const double* X, const double* w, double* out,
                           fem_stream_t stream) {
-  int rc = validate(mesh, basis);
+  int rc = validate(mesh, basis, true);
   if (rc) return rc;
   if ((rc = facets_given(facets))) return rc;
   return interp_with_status(mesh, basis, facets, nq, X, w, out, stream);
@@ -609,7 +611,7 @@ int fem_facet_interpolate(const FemMesh* mesh, const FemBasis* basis, const FemF
 
 int fem_pattern_build_local(const FemMesh* mesh, const FemBasis* basis, const double* local,
                             FemPattern** out, fem_stream_t stream) {
-  int rc = validate(mesh, basis);
+  int rc = validate(mesh, basis, true);
   if (rc) return rc;
   if (!out || (!local && mesh->nelems > 0)) {
     set_error(FEM_ERR_ARGUMENT, "null local matrices or output handle");
@@ -652,7 +654,7 @@ int fem_csr_sum_checked(const FemPattern* pat, const double* local, double* csr_
 
 int fem_interpolate(const FemMesh* mesh, const FemBasis* basis, int32_t nq, const double* X,
                     const double* w, double* out, fem_stream_t stream) {
-  int rc = validate(mesh, basis);
+  int rc = validate(mesh, basis, true);
   if (rc) return rc;
   return fem::interpolate(*mesh, *basis, nullptr, nq, X, w, out, nullptr, (cudaStream_t)stream);
 }
@@ -660,7 +662,7 @@ int fem_interpolate(const FemMesh* mesh, const FemBasis* basis, int32_t nq, cons
 int fem_facet_geometry(const FemMesh* mesh, const FemBasis* basis, const FemFacets* facets,
                        int32_t nq, const double* X, double* geo, int32_t* status,
                        fem_stream_t stream) {
-  int rc = validate(mesh, basis);
+  int rc = validate(mesh, basis, true);
   if (rc) return rc;
   if ((rc = facets_given(facets))) return rc;
   return fem::facet_geometry(*mesh, *basis, *facets, nq, X, geo, status, (cudaStream_t)stream);

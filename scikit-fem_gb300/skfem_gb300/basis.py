@@ -63,7 +63,7 @@ class CellBasis:
         # numbers -- too low an order, a custom rule, another Hex1 rule --
         # assembles every form through the generic per-point kernels.
         if elem.refdom == "hex":
-            self._fast_ok = quadrature is None and self.X.shape[1] == 64
+            self._fast_ok = quadrature is None and self.X.shape[1] == 64 and not elem.vector
         else:
             min_order = {1: 2, 2: 4}.get(elem.maxdeg, 0)
             self._fast_ok = quadrature is None and self.intorder >= min_order

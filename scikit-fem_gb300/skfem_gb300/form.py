@@ -850,12 +850,28 @@ class Functional(Form):
         return np.float64(self.assemble_torch(ubasis, vbasis, **kwargs).item())
 
 
-def asm(form, *args, **kwargs):
-    """skfem/assembly/__init__.py:69-97 for a single basis (no list products)."""
+def asm(form, *args, to=None, **kwargs):
+    """skfem/assembly/__init__.py:69-97: assemble ``form`` on its bases; an
+    argument that is a list of bases assembles every combination (the
+    product over the lists) and sums the results -- e.g. one form over
+    several element subsets or facet sets."""
     if not isinstance(form, Form):
         import inspect
         nargs = len(inspect.signature(form).parameters)
         form = {3: BilinearForm, 2: LinearForm, 1: Functional}[nargs](form)
-    if any(isinstance(a, (list, tuple)) for a in args):
-        raise NotImplementedError("asm over lists of bases is not supported")
-    return form.assemble(*args, **kwargs)
+    if to is not None:
+        raise NotImplementedError("asm(to=...) is not supported; the results are summed")
+    lists = [a if isinstance(a, list) else [a] for a in args]
+    if all(len(a) == 1 for a in lists):
+        return form.assemble(*[a[0] for a in lists], **kwargs)
+    from itertools import product
+    parts = [form.assemble(*combo, **kwargs) for combo in product(*lists)]
+    if sp.issparse(parts[0]):
+        # concatenated COO then CSR, as COOData.__add__ + todefault: an entry
+        # is kept when any part has it, even if the sum cancels to zero
+        coo = [P.tocoo() for P in parts]
+        K = sp.coo_matrix((np.concatenate([P.data for P in coo]),
+                           (np.concatenate([P.row for P in coo]),
+                            np.concatenate([P.col for P in coo]))), shape=parts[0].shape)
+        return K.tocsr()
+    return sum(parts[1:], parts[0])

@@ -201,6 +201,7 @@ def main():
     generic_cases()
     facet_cases()
     mixed_cases()
+    vector_hex_case()
 
     # quadrature rules the configs use, exactly as the reference tabulates them
     from skfem.quadrature import get_quadrature_tet, get_quadrature_tri
@@ -511,6 +512,32 @@ def mixed_cases():
          **{k + "_bdiv": v for k, v in csr_arrays(bdiv.assemble(ub, pb)).items()})
 
 
+def vector_hex_case():
+    """ElementVector(ElementHex1): linear elasticity on a jittered Hex1 mesh,
+    a traction load on its boundary, the interpolated displacement."""
+    from skfem import FacetBasis
+    rng = np.random.default_rng(20261208)
+    n = 2
+    m = MeshHex.init_tensor(*(np.linspace(0, 1, n + 1),) * 3)
+    p = m.p.copy()
+    inner = jitter(m, rng, 0.2)
+    p[:, inner] += rng.uniform(-0.1, 0.1, size=(3, int(inner.sum())))
+    m = MeshHex(p, m.t)
+    e = ElementVector(ElementHex1())
+    ib = Basis(m, e)
+    fb = FacetBasis(m, e)
+    d = rng.standard_normal(ib.N)
+    df = ib.interpolate(d)
+
+    @LinearForm
+    def traction(v, w):
+        return (1.0 + w.x[2]) * dot(w.n, v)
+
+    save("hex1_vec", p=m.p, t=m.t, element_dofs=ib.element_dofs, d=d, d_value=np.asarray(df),
+         d_grad=df.grad, b_traction=traction.assemble(fb),
+         **{k + "_elast": v for k, v in csr_arrays(linear_elasticity(1.0, 0.5).assemble(ib)).items()})
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["--generic"]:
         generic_cases()
@@ -520,5 +547,7 @@ if __name__ == "__main__":
         hex_facet_case()
     elif sys.argv[1:] == ["--mixed"]:
         mixed_cases()
+    elif sys.argv[1:] == ["--vector-hex"]:
+        vector_hex_case()
     else:
         main()

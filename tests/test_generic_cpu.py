@@ -185,3 +185,23 @@ def test_numpy_pairwise_sum_order():
     for n in (0, 1, 7, 8, 127, 128, 129, 1000, 4097, 100_003):
         x = rng.standard_normal(n) * np.exp(rng.uniform(-30, 30, n))
         assert _lib().faithful_sum_host(x.ctypes.data, n) == np.sum(x)
+
+
+def test_vector_hex_bitwise():
+    """ElementVector(ElementHex1) (generic kernels only): interpolation and
+    linear elasticity replayed on the host equal the reference bit for bit."""
+    from skfem_gb300.models.elasticity import linear_elasticity
+    g = golden("hex1_vec")
+    e = F.ElementVector(F.ElementHex1())
+    X, W = F.get_quadrature("hex", 6)
+    g = dict(g, X=X, W=W)
+    h = HostCase(g, e)
+    q = h.interpolate(g["d"])
+    np.testing.assert_array_equal(q[:3], g["d_value"])
+    np.testing.assert_array_equal(q[3:].reshape(3, 3, h.nel, h.nq), g["d_grad"])
+    local = h.run(linear_elasticity(1.0, 0.5), "bilinear", {})
+    K = reference_csr(local, h.ed, h.N)
+    ip, ix, d = fixture_csr(g, "elast")
+    np.testing.assert_array_equal(K.indptr, ip)
+    np.testing.assert_array_equal(K.indices, ix)
+    np.testing.assert_array_equal(K.data, d)

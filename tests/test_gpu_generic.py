@@ -232,3 +232,38 @@ def test_mixed_bases_vs_reference():
     same, extra, missing, noise, rf, rm = csr_diff(K.indptr, K.indices, K.data, gt["indptr_bdiv"],
                                                    gt["indices_bdiv"], gt["data_bdiv"], K.shape)
     assert same and rf <= REL_FRO and rm <= REL_MAX
+
+
+def test_asm_sums_over_lists_of_bases():
+    """asm(form, [b1, b2]) sums the assemblies over both bases (here two
+    element subsets covering the mesh), as COOData addition does."""
+    m = F.MeshTri.init_tensor(np.linspace(0, 1, 7), np.linspace(0, 1, 6))
+    left = F.Basis(m, F.ElementTriP2(), elements=lambda x: x[0] < 0.5)
+    right = F.Basis(m, F.ElementTriP2(), elements=lambda x: x[0] >= 0.5)
+    full = F.Basis(m, F.ElementTriP2())
+    K = F.asm(laplace, [left, right])
+    Kf = laplace.assemble(full)
+    np.testing.assert_array_equal(K.indptr, Kf.indptr)
+    np.testing.assert_array_equal(K.indices, Kf.indices)
+    np.testing.assert_allclose(K.data, Kf.data, rtol=0, atol=1e-13 * np.abs(Kf.data).max())
+    b = F.asm(F.LinearForm(lambda v, w: 1.0 * v), [left, right])
+    np.testing.assert_allclose(b, F.LinearForm(lambda v, w: 1.0 * v).assemble(full), atol=1e-15)
+
+
+def test_vector_hex_vs_reference():
+    """ElementVector(ElementHex1) on the generic kernels: elasticity matrix,
+    FacetBasis traction load and interpolation against the reference."""
+    from skfem_gb300.models.elasticity import linear_elasticity
+    g = golden("hex1_vec")
+    m = F.MeshHex(g["p"], g["t"])
+    e = F.ElementVector(F.ElementHex1())
+    b = F.Basis(m, e)
+    np.testing.assert_array_equal(b.element_dofs, g["element_dofs"])
+    check_csr(linear_elasticity(1.0, 0.5).assemble(b), *fixture_csr(g, "elast"))
+    f = b.interpolate(g["d"])
+    np.testing.assert_array_equal(np.asarray(f), g["d_value"])
+    np.testing.assert_array_equal(f.grad, g["d_grad"])
+    fb = F.FacetBasis(m, e)
+    traction = F.LinearForm(lambda v, w: (1.0 + w.x[2]) * H.dot(w.n, v))
+    bt = traction.assemble(fb)
+    np.testing.assert_allclose(bt, g["b_traction"], rtol=0, atol=1e-13 * np.abs(bt).max())
