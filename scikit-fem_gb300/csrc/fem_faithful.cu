@@ -367,6 +367,8 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets*
     t.epb = epb;
     return t.total() * sizeof(double);
   };
+  s.entry_loop = false;
+  if (bytes(1) > 96 * 1024) s.entry_loop = true;   // no per-(entry, point) value stage
   int epb = std::max(1, std::min(64, 2048 / (L * nq)));
   while (epb > 1 && bytes(epb) > 96 * 1024) --epb;
   s.epb = epb;

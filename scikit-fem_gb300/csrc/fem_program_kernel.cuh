@@ -59,9 +59,12 @@ struct GenericLayout {
   int npoint;          // compiled programs: values hoisted per point (0: none)
   bool mixed;          // a trial basis of its own (nbu functions, nquantu quantities)
   int nbu, nquantu;
+  bool entry_loop;     // one thread per entry looping over the points (no value stage)
   __host__ __device__ size_t geo() const { return 0; }
   __host__ __device__ size_t val() const { return (size_t)epb * nq * kGeo; }
-  __host__ __device__ size_t cell() const { return val() + (size_t)epb * L * nq; }
+  __host__ __device__ size_t cell() const {
+    return val() + (entry_loop ? 0 : (size_t)epb * L * nq);
+  }
   __host__ __device__ size_t quant() const { return cell() + (cells ? (size_t)epb * kCell : 0); }
   __host__ __device__ size_t quantu() const {
     return quant() + (quants ? (size_t)epb * nq * nb * nquant : 0);
@@ -182,6 +185,49 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
   }
   __syncthreads();
 #endif
+  if (s.entry_loop) {
+    // large local matrices: a thread takes an entry, its points in turn
+    double R[kMaxProgram];
+    double vals[kMaxPoints];
+    for (int k = threadIdx.x; k < s.epb * s.L; k += blockDim.x) {
+      const int el = k / s.L, r = k - el * s.L;
+      const int64_t e = e0 + el;
+      if (e >= ncells) continue;
+      const int i = MODE == 0 ? r / nbu : (MODE == 1 ? r : 0);
+      const int j = MODE == 0 ? r - i * nbu : 0;
+      for (int q = 0; q < s.nq; ++q) {
+        const double* G = geo + ((size_t)el * s.nq + q) * kGeo;
+        PointGeo g;
+        for (int a = 0; a < 3; ++a)
+          for (int c = 0; c < 3; ++c) g.inv[a][c] = G[a * 3 + c];
+        g.det = G[9];
+        for (int a = 0; a < 7; ++a) g.qx[a] = G[10 + a];
+        double qu[D + D * D], qv[D + D * D];
+        if (s.quants) {
+          const double* Qp = Q + ((size_t)(el * s.nq + q) * nb) * NQ;
+          const double* Qup = Qu + ((size_t)(el * s.nq + q) * nbu) * NQU;
+#pragma unroll
+          for (int a = 0; a < NQU; ++a) qu[a] = Qup[(size_t)j * NQU + a];
+#pragma unroll
+          for (int a = 0; a < NQ; ++a) qv[a] = Qp[(size_t)i * NQ + a];
+        } else {
+#pragma unroll
+          for (int a = 0; a < NQU; ++a) qu[a] = 0.0;
+#pragma unroll
+          for (int a = 0; a < NQ; ++a) qv[a] = 0.0;
+        }
+#ifdef FEM_JIT_HOIST
+        const double fq = jit_form_hoisted(qu, qv, P + ((size_t)el * s.nq + q) * s.npoint);
+        vals[q] = fq * (fabs(g.det) * rule.W[q]);
+        (void)R;
+#else
+        vals[q] = point_value_q(prog, e, q, qu, qv, g, rule.W[q], R);
+#endif
+      }
+      out[e0 * s.L + k] = np_pairwise_sum(vals, s.nq);
+    }
+    return;
+  }
   // stage 2: form * dx
   double R[kMaxProgram];
   const int per = s.L * s.nq;
