@@ -266,7 +266,7 @@ int fem_local_vectors(const FemMesh* mesh, const FemBasis* basis, const FemLinea
 
 int fem_pattern_build(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
                       const FemProgram* program, FemPattern** out, fem_stream_t stream) {
-  int rc = validate(mesh, basis);
+  int rc = validate(mesh, basis, form == nullptr);   // incidence only: any basis
   if (rc) return rc;
   if (!out) {
     set_error(FEM_ERR_ARGUMENT, "null output handle");
