@@ -130,6 +130,16 @@ class CellBasis:
     def quadrature(self):
         return self.X, self.W
 
+    def get_dofs(self, facets=None, elements=None):
+        """Global DOF numbers on facets (default: the boundary) or of cells
+        (abstract_basis.py:125-260): a DofsView, ``.flatten()`` for the
+        sorted array condense / enforce take."""
+        if elements is not None:
+            if facets is not None:
+                raise ValueError("Give only facets or only elements")
+            return self.dofs.get_element_dofs(self.mesh.normalize_elements(elements))
+        return self.dofs.get_facet_dofs(self.mesh.normalize_facets(facets))
+
     def interpolate_torch(self, w):
         """Device interpolation of the DOF vector w: (nquant, nelems, nqp)
         float64, quantity-major -- scalar bases value then the dim

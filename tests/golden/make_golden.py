@@ -202,6 +202,8 @@ def main():
     facet_cases()
     mixed_cases()
     vector_hex_case()
+    dofs_case()
+    poisson_case()
 
     # quadrature rules the configs use, exactly as the reference tabulates them
     from skfem.quadrature import get_quadrature_tet, get_quadrature_tri
@@ -538,6 +540,38 @@ def vector_hex_case():
          **{k + "_elast": v for k, v in csr_arrays(linear_elasticity(1.0, 0.5).assemble(ib)).items()})
 
 
+def dofs_case():
+    """Basis.get_dofs (abstract_basis.py:125-260): boundary DOFs, DOFs on the
+    facets a callable selects, DOFs of the cells a callable selects."""
+    out = {}
+    meshes = {"tri": MeshTri.init_tensor(np.linspace(0, 1, 5), np.linspace(0, 1, 4)),
+              "tet": MeshTet.init_tensor(*(np.linspace(0, 1, 4),) * 3),
+              "hex": MeshHex.init_tensor(*(np.linspace(0, 1, 4),) * 3)}
+    elems = {"tri": (ElementTriP1, ElementTriP2), "tet": (ElementTetP1, ElementTetP2),
+             "hex": (ElementHex1,)}
+    for kind, m in meshes.items():
+        for E in elems[kind]:
+            for vec in (0, 1):
+                b = Basis(m, ElementVector(E()) if vec else E())
+                key = "%s_%s_%d" % (kind, E.__name__, vec)
+                out[key + "_boundary"] = b.get_dofs().flatten()
+                out[key + "_y0"] = b.get_dofs(lambda x: np.isclose(x[1], 0)).flatten()
+                out[key + "_left"] = b.get_dofs(elements=lambda x: x[0] < 0.5).flatten()
+    save("get_dofs", **out)
+
+
+def poisson_case():
+    """A whole solve as users write it (docs/examples/ex01.py): -lap u = 1 on
+    the unit square, u = 0 on the boundary, condense and spsolve."""
+    from skfem import condense, solve
+    m = MeshTri.init_tensor(np.linspace(0, 1, 33), np.linspace(0, 1, 33))
+    b = Basis(m, ElementTriP2())
+    A = laplace.assemble(b)
+    f = unit_load.assemble(b)
+    u = solve(*condense(A, f, D=b.get_dofs()))
+    save("poisson_tri_p2", u=u)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["--generic"]:
         generic_cases()
@@ -549,5 +583,9 @@ if __name__ == "__main__":
         mixed_cases()
     elif sys.argv[1:] == ["--vector-hex"]:
         vector_hex_case()
+    elif sys.argv[1:] == ["--dofs"]:
+        dofs_case()
+    elif sys.argv[1:] == ["--poisson"]:
+        poisson_case()
     else:
         main()

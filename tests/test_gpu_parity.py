@@ -395,3 +395,23 @@ def test_enforce_on_device_matches_reference_semantics():
     _, Me = enforce(A, M, D=D)
     Mh = Me.to_dense().cpu().numpy()
     assert np.all(Mh[D] == 0.0)
+
+
+def test_poisson_solve_as_users_write_it():
+    """ex01-style: assemble on the GPU, condense on the device with the
+    boundary DOFs of get_dofs, solve with scipy; the solution equals the
+    reference's own solve."""
+    import scipy.sparse.linalg as spla
+    from skfem_gb300.utils import condense
+    g = golden("poisson_tri_p2")
+    m = F.MeshTri.init_tensor(np.linspace(0, 1, 33), np.linspace(0, 1, 33))
+    b = F.Basis(m, F.ElementTriP2())
+    A = laplace.assemble_torch(b)
+    f = unit_load.assemble_torch(b)
+    D = b.get_dofs()
+    AII, fI, x, I = condense(A, f, D=D)
+    Kh = sp.csr_matrix((AII.values().cpu().numpy(), AII.col_indices().cpu().numpy(),
+                        AII.crow_indices().cpu().numpy()), shape=AII.shape)
+    u = np.zeros(b.N)
+    u[I.cpu().numpy()] = spla.spsolve(Kh.tocsc(), fI.cpu().numpy())
+    np.testing.assert_allclose(u, g["u"], rtol=0, atol=1e-12)

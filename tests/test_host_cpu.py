@@ -83,3 +83,32 @@ def test_trace_rejects_unsupported_forms():
 def test_basis_rejects_mismatch_without_gpu():
     with pytest.raises(ValueError):
         F.Basis(F.MeshTri(), F.ElementTetP1())
+
+
+def test_get_dofs_match_reference():
+    """Basis.get_dofs: boundary facets, a facet callable, a cell callable,
+    for every element family and its vector version (dofs.py:539-662)."""
+    import numpy as np
+    import skfem_gb300 as F
+    from skfem_gb300.dofs import Dofs
+    from _util import golden
+    g = golden("get_dofs")
+    meshes = {"tri": F.MeshTri.init_tensor(np.linspace(0, 1, 5), np.linspace(0, 1, 4)),
+              "tet": F.MeshTet.init_tensor(*(np.linspace(0, 1, 4),) * 3),
+              "hex": F.MeshHex.init_tensor(*(np.linspace(0, 1, 4),) * 3)}
+    elems = {"tri": ("ElementTriP1", "ElementTriP2"), "tet": ("ElementTetP1", "ElementTetP2"),
+             "hex": ("ElementHex1",)}
+    for kind, m in meshes.items():
+        for name in elems[kind]:
+            for vec in (0, 1):
+                e = getattr(F, name)()
+                d = Dofs(m, F.ElementVector(e) if vec else e)
+                key = "%s_%s_%d" % (kind, name, vec)
+                np.testing.assert_array_equal(
+                    d.get_facet_dofs(m.normalize_facets(None)).flatten(), g[key + "_boundary"])
+                np.testing.assert_array_equal(
+                    d.get_facet_dofs(m.normalize_facets(lambda x: np.isclose(x[1], 0))).flatten(),
+                    g[key + "_y0"])
+                np.testing.assert_array_equal(
+                    d.get_element_dofs(m.normalize_elements(lambda x: x[0] < 0.5)).flatten(),
+                    g[key + "_left"])
