@@ -30,7 +30,6 @@ int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, 
               cudaStream_t st);
 int vector_sum(const Pattern& P, const double* local, double* b, cudaStream_t st);
 void free_pattern(Pattern* P);
-int zero_check(const Pattern& P, const double* local, int32_t* status, cudaStream_t st);
 int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets* fc,
                  const FemProgram& prog, double* out, int32_t* status, cudaStream_t st,
                  const FemBasis* bu);
@@ -644,12 +643,9 @@ int fem_csr_sum_checked(const FemPattern* pat, const double* local, double* csr_
     set_error(FEM_ERR_ARGUMENT, "pattern has no CSR structure");
     return FEM_ERR_ARGUMENT;
   }
-  cudaStream_t st = (cudaStream_t)stream;
-  int rc = fem::zero_check(pat->P, local, status, st);
-  if (rc) return rc;
   fem::Pattern P = pat->P;
   P.sum_unroll = fem::tuning_for(pat->family).sum_unroll;
-  return fem::csr_sum(P, local, csr_values, st);
+  return fem::csr_sum(P, local, csr_values, (cudaStream_t)stream, 0, -1, status);
 }
 
 int fem_interpolate(const FemMesh* mesh, const FemBasis* basis, int32_t nq, const double* X,

@@ -106,9 +106,10 @@ struct Tuning {
 Tuning tuning_for(int family);
 
 // Fixed-order segmented sum of local matrices into CSR values, rows
-// [row0, row1) (row1 < 0: to the last row).
+// [row0, row1) (row1 < 0: to the last row); check_status non-null: also
+// verify the exact-zero structure (FEM_ERR_STALE_PATTERN).
 int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st,
-            int64_t row0 = 0, int64_t row1 = -1);
+            int64_t row0 = 0, int64_t row1 = -1, int32_t* check_status = nullptr);
 
 int basis_nb_scalar(int family);
 int basis_dim(int family);

@@ -23,6 +23,8 @@
 
 #include "fem_common.cuh"
 
+#include <type_traits>
+
 namespace fem {
 
 namespace {
@@ -220,11 +222,15 @@ __global__ void row_fill_kernel(const int32_t* __restrict__ inc_ptr, const int32
 // (independent of each other), then added in order -- entry q's additions
 // complete (__syncwarp) before entry q+1's, so every slot sums its
 // contributions in ascending (element, local row) order.
-template <int G, int U>
+// CHECK: also verify the zero structure (exact local masks, generic path):
+// a nonzero local entry without a slot, or a CSR entry that no nonzero
+// local entry reaches, sets FEM_ERR_STALE_PATTERN in *status.
+template <int G, int U, bool CHECK>
 __global__ void csr_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                                const uint16_t* __restrict__ slot, const int32_t* __restrict__ indptr,
                                const double* __restrict__ local, int64_t row0, int64_t nrows,
-                               int nu, int stride, double* __restrict__ vals) {
+                               int nu, int stride, double* __restrict__ vals,
+                               int32_t* __restrict__ status) {
   extern __shared__ double acc_smem[];
   constexpr int RPW = 32 / G;  // rows per warp
   const int lane = threadIdx.x & 31;
@@ -232,6 +238,9 @@ __global__ void csr_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_
   const int j = lane - sub * G;  // local column
   const int wib = threadIdx.x >> 5;
   double* acc = acc_smem + ((size_t)wib * RPW + sub) * stride;
+  uint8_t* seen = reinterpret_cast<uint8_t*>(acc_smem + (size_t)(blockDim.x >> 5) * RPW * stride) +
+                  ((size_t)wib * RPW + sub) * stride;
+  bool stale = false;
   const int64_t rows_per_block = (int64_t)(blockDim.x >> 5) * RPW;
   for (int64_t rb = row0 + (int64_t)blockIdx.x * rows_per_block; rb < nrows;
        rb += (int64_t)gridDim.x * rows_per_block) {
@@ -244,7 +253,10 @@ __global__ void csr_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_
       p0 = indptr[r];
       nnz = indptr[r + 1] - p0;
     }
-    for (int k = j; k < nnz; k += G) acc[k] = 0.0;
+    for (int k = j; k < nnz; k += G) {
+      acc[k] = 0.0;
+      if (CHECK) seen[k] = 0;
+    }
     int maxlen = len;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
@@ -265,13 +277,22 @@ __global__ void csr_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_
       }
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        if (s[u] != 0xFFFF) acc[s[u]] += v[u];
+        if (s[u] != 0xFFFF) {
+          acc[s[u]] += v[u];
+          if (CHECK && v[u] != 0.0) seen[s[u]] = 1;
+        } else if (CHECK && v[u] != 0.0) {
+          stale = true;
+        }
         __syncwarp();
       }
     }
-    for (int k = j; k < nnz; k += G) vals[p0 + k] = acc[k];
+    for (int k = j; k < nnz; k += G) {
+      vals[p0 + k] = acc[k];
+      if (CHECK) stale = stale || !seen[k];
+    }
     __syncwarp();
   }
+  if (CHECK && stale) atomicOr(status, 1 << FEM_ERR_STALE_PATTERN);
 }
 
 __global__ void vector_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
@@ -284,33 +305,6 @@ __global__ void vector_sum_kernel(const int32_t* __restrict__ inc_ptr, const int
   for (int32_t q = p0; q < p1; ++q) s += local[inc[q]];
   b[r] = s;
 }
-
-// Zero-structure check of a pattern against new local matrices (exact
-// masks): a nonzero entry without a CSR slot, or a CSR entry with no
-// nonzero contribution, means the pattern is stale.  One thread per row;
-// seen[] is the row's own range of a nnz-byte scratch.
-__global__ void zero_check_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
-                                  const uint16_t* __restrict__ slot, const int32_t* __restrict__ indptr,
-                                  const double* __restrict__ local, int64_t nrows, int nu,
-                                  uint8_t* __restrict__ seen, int32_t* __restrict__ status) {
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrows) return;
-  const int32_t p0 = indptr[r], p1 = indptr[r + 1];
-  for (int32_t k = p0; k < p1; ++k) seen[k] = 0;
-  bool stale = false;
-  for (int32_t q = inc_ptr[r]; q < inc_ptr[r + 1]; ++q) {
-    const int64_t code = inc[q];
-    for (int j = 0; j < nu; ++j) {
-      const double v = local[code * nu + j];
-      const uint16_t s = slot[(int64_t)q * nu + j];
-      if (s == 0xFFFF) stale = stale || v != 0.0;
-      else if (v != 0.0) seen[p0 + s] = 1;
-    }
-  }
-  for (int32_t k = p0; k < p1; ++k) stale = stale || !seen[k];
-  if (stale) atomicOr(status, 1 << FEM_ERR_STALE_PATTERN);
-}
-
 
 int grid_for(int64_t n, int block) {
   const int64_t g = ceil_div(n, block);
@@ -518,14 +512,14 @@ int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, 
 }
 
 int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st, int64_t row0,
-            int64_t row1) {
+            int64_t row1, int32_t* check_status) {
   if (!P.has_matrix) {
     set_error(FEM_ERR_ARGUMENT, "pattern has no CSR structure (built without local matrices)");
     return FEM_ERR_ARGUMENT;
   }
   if (row1 < 0 || row1 > P.nrows) row1 = P.nrows;
   if (row0 < 0) row0 = 0;
-  if (row1 <= row0 || P.nnz == 0) return 0;
+  if (row1 <= row0 || (P.nnz == 0 && !check_status)) return 0;
   const int nu = P.nbfun_u;
   const int stride = std::max(1, P.max_row_nnz);
   const int threads = 128;
@@ -533,7 +527,7 @@ int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st
   int rc = 0;
   auto launch = [&](auto kern, int G) -> int {
     const int rpw = 32 / G;
-    const size_t smem = (size_t)warps * rpw * stride * sizeof(double);
+    const size_t smem = (size_t)warps * rpw * stride * (sizeof(double) + (check_status ? 1 : 0));
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return check_cuda(e, "csr_sum smem");
@@ -542,35 +536,28 @@ int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(row1 - row0, rows_per_block),
                                                                 (int64_t)num_sms() * 64));
     kern<<<grid, threads, smem, st>>>(P.inc_ptr, P.inc, P.slot, P.indptr, local, row0, row1, nu,
-                                      stride, vals);
+                                      stride, vals, check_status);
     return 0;
   };
   const int U = P.sum_unroll;
-  if (nu <= 2) rc = U >= 16 ? launch(csr_sum_kernel<2, 16>, 2) : U >= 8 ? launch(csr_sum_kernel<2, 8>, 2) : launch(csr_sum_kernel<2, 4>, 2);
-  else if (nu <= 4) rc = U >= 16 ? launch(csr_sum_kernel<4, 16>, 4) : U >= 8 ? launch(csr_sum_kernel<4, 8>, 4) : launch(csr_sum_kernel<4, 4>, 4);
-  else if (nu <= 8) rc = U >= 16 ? launch(csr_sum_kernel<8, 16>, 8) : U >= 8 ? launch(csr_sum_kernel<8, 8>, 8) : launch(csr_sum_kernel<8, 4>, 8);
-  else if (nu <= 16) rc = U >= 8 ? launch(csr_sum_kernel<16, 8>, 16) : launch(csr_sum_kernel<16, 4>, 16);
-  else if (nu <= 32) rc = U >= 8 ? launch(csr_sum_kernel<32, 8>, 32) : launch(csr_sum_kernel<32, 4>, 32);
-  else {
+  auto pick = [&](auto check_tag) -> int {
+    constexpr bool C = decltype(check_tag)::value;
+    if (nu <= 2) return U >= 16 ? launch(csr_sum_kernel<2, 16, C>, 2) : U >= 8 ? launch(csr_sum_kernel<2, 8, C>, 2) : launch(csr_sum_kernel<2, 4, C>, 2);
+    if (nu <= 4) return U >= 16 ? launch(csr_sum_kernel<4, 16, C>, 4) : U >= 8 ? launch(csr_sum_kernel<4, 8, C>, 4) : launch(csr_sum_kernel<4, 4, C>, 4);
+    if (nu <= 8) return U >= 16 ? launch(csr_sum_kernel<8, 16, C>, 8) : U >= 8 ? launch(csr_sum_kernel<8, 8, C>, 8) : launch(csr_sum_kernel<8, 4, C>, 8);
+    if (nu <= 16) return U >= 8 ? launch(csr_sum_kernel<16, 8, C>, 16) : launch(csr_sum_kernel<16, 4, C>, 16);
+    return U >= 8 ? launch(csr_sum_kernel<32, 8, C>, 32) : launch(csr_sum_kernel<32, 4, C>, 32);
+  };
+  if (nu > 32) {
     set_error(FEM_ERR_UNSUPPORTED, "more than 32 local functions per cell (%d)", nu);
     return FEM_ERR_UNSUPPORTED;
   }
+  rc = check_status ? pick(std::true_type{}) : pick(std::false_type{});
   if (rc) return rc;
   FEM_LAUNCH_CHECK("csr_sum_kernel");
   return 0;
 }
 
-int zero_check(const Pattern& P, const double* local, int32_t* status, cudaStream_t st) {
-  if (!P.has_matrix || P.nrows == 0) return 0;
-  uint8_t* seen = nullptr;
-  FEM_TRY_CUDA(cudaMallocAsync(&seen, std::max<int64_t>(1, P.nnz), st));
-  zero_check_kernel<<<(unsigned)ceil_div(P.nrows, 128), 128, 0, st>>>(
-      P.inc_ptr, P.inc, P.slot, P.indptr, local, P.nrows, P.nbfun_u, seen, status);
-  cudaError_t e = cudaGetLastError();
-  cudaFreeAsync(seen, st);
-  if (e != cudaSuccess) return check_cuda(e, "zero_check_kernel");
-  return 0;
-}
 
 int vector_sum(const Pattern& P, const double* local, double* b, cudaStream_t st) {
   if (P.nrows == 0) return 0;
