@@ -90,7 +90,7 @@ __global__ void coef_zero_bits_kernel(FemBilinear f, int64_t n, const uint8_t* _
   uint8_t bits = 0;
 #pragma unroll
   for (int k = 0; k < 5; ++k)
-    if (coef_at(*c[k], e) == 0.0) bits |= (uint8_t)(1u << k);
+    if (coef_zero(*c[k], e)) bits |= (uint8_t)(1u << k);
   if (out) out[e] = bits;
   if (ref && ref[e] != bits) atomicOr(status, 1 << FEM_ERR_STALE_PATTERN);
 }

@@ -72,15 +72,55 @@ __device__ __forceinline__ double coef_at(const FemCoef& c, int64_t e) {
   return c.field ? c.scale * c.field[c.stride > 1 ? e * c.stride : e] : c.scale;
 }
 
+// Bit tests and |x| on the integer pipes: the FP64 pipe bounds the local
+// kernels, so comparisons and sign masks stay off it.  The bit pattern is
+// moved through an inline-PTX mov, which the optimizer cannot see through
+// (it would otherwise fold the integer test back into an FP64 compare).
+// zero_bits(x) is x == 0.0 (either sign; false for NaN).
+__device__ __forceinline__ unsigned long long dbits(double x) {
+  unsigned long long u;
+  asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
+  return u;
+}
+__device__ __forceinline__ double dfrombits(unsigned long long u) {
+  double x;
+  asm("mov.b64 %0, %1;" : "=d"(x) : "l"(u));
+  return x;
+}
+__device__ __forceinline__ bool zero_bits(double x) { return (dbits(x) << 1) == 0ull; }
+__device__ __forceinline__ double abs_bits(double x) {
+  return dfrombits(dbits(x) & 0x7fffffffffffffffull);
+}
+
+// coef_at(c, e) is zero because its scale or its field value is exactly 0
+// (either sign) -- the zero bit of a channel, tested without forming the
+// product (an underflow of the product itself is not tracked).  The
+// pattern build and every later call use this same definition.
+__device__ __forceinline__ bool coef_zero(const FemCoef& c, int64_t e) {
+  if (zero_bits(c.scale)) return true;
+  return c.field ? zero_bits(c.field[c.stride > 1 ? e * c.stride : e]) : false;
+}
+
 // A strided (per-point) coefficient must be constant over the cell's points
-// for the channel kernels; otherwise flag FEM_ERR_VARYING.
-__device__ __forceinline__ void check_row(const FemCoef& c, int64_t e, int32_t* status) {
-  if (!c.field || c.stride <= 1) return;
+// for the channel kernels -- bitwise, with +0.0 and -0.0 taken as equal --
+// otherwise the status bit FEM_ERR_VARYING (the caller then takes the
+// generic path).  Returns the bit instead of publishing it, so the kernels
+// keep their flags in a register and issue one atomic at the end.
+__device__ __forceinline__ int32_t row_status(const FemCoef& c, int64_t e) {
+  if (!c.field || c.stride <= 1) return 0;
   const double* r = c.field + e * c.stride;
-  const double v0 = r[0];
+  const unsigned long long v0 = dbits(r[0]);
   bool same = true;
-  for (int64_t q = 1; q < c.stride; ++q) same = same && r[q] == v0;
-  if (!same && status) atomicOr(status, 1 << FEM_ERR_VARYING);
+  for (int64_t q = 1; q < c.stride; ++q) {
+    const unsigned long long vq = dbits(r[q]);
+    same = same && (vq == v0 || ((vq | v0) << 1) == 0ull);
+  }
+  return same ? 0 : (1 << FEM_ERR_VARYING);
+}
+
+// Publishes a thread's accumulated status bits (one atomic per thread).
+__device__ __forceinline__ void publish_status(int32_t* status, int32_t bits) {
+  if (bits && status) atomicOr(status, bits);
 }
 
 // Reference-cube corner (0/1 per axis) of Hex1 node n: node 0 sits at

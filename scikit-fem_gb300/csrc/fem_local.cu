@@ -147,29 +147,37 @@ template <> struct SimplexTraits<2, 2> { static constexpr int NB = 6; static con
 template <> struct SimplexTraits<3, 1> { static constexpr int NB = 4; static constexpr double FACT = 6.0; };
 template <> struct SimplexTraits<3, 2> { static constexpr int NB = 10; static constexpr double FACT = 6.0; };
 
-// Per-element zero bits of the form's coefficients (bit k: channel k of
-// diff, mass, lam, lap, tr is exactly 0); compared with the bits recorded
-// at pattern build, a change means the zero structure may have changed.
-__device__ __forceinline__ void check_coef_bits(const FemBilinear& f, int64_t e,
-                                                const uint8_t* __restrict__ ref,
-                                                int32_t* __restrict__ status) {
-  fem::check_row(f.diff, e, status);
-  fem::check_row(f.mass, e, status);
-  fem::check_row(f.lam, e, status);
-  fem::check_row(f.lap, e, status);
-  fem::check_row(f.tr, e, status);
-  if (!ref) return;
-  uint8_t bits = 0;
-  bits |= (coef_at(f.diff, e) == 0.0) ? 1u : 0u;
-  bits |= (coef_at(f.mass, e) == 0.0) ? 2u : 0u;
-  bits |= (coef_at(f.lam, e) == 0.0) ? 4u : 0u;
-  bits |= (coef_at(f.lap, e) == 0.0) ? 8u : 0u;
-  bits |= (coef_at(f.tr, e) == 0.0) ? 16u : 0u;
-  if (bits != ref[e] && status) atomicOr(status, 1 << FEM_ERR_STALE_PATTERN);
+// Status bits of one element's coefficients: FEM_ERR_VARYING for a strided
+// row that is not constant; with ref, FEM_ERR_STALE_PATTERN when the zero
+// bits (bit k: channel k of diff, mass, lam, lap, tr is exactly 0) differ
+// from the ones recorded at pattern build -- the zero structure may have
+// changed.  No side effects: the kernels OR the bits into a register and
+// publish them once (an atomic in the middle of the element would make
+// every later load re-read memory the atomic may have written).
+// ref is the element's recorded byte, or -1 without a record; the kernels
+// load it before the element's geometry and call this after its values, so
+// that the load's latency overlaps the arithmetic.
+__device__ __forceinline__ int32_t coef_status(const FemBilinear& f, int64_t e, int ref) {
+  int32_t st = fem::row_status(f.diff, e) | fem::row_status(f.mass, e) |
+               fem::row_status(f.lam, e) | fem::row_status(f.lap, e) | fem::row_status(f.tr, e);
+  if (ref < 0) return st;
+  int bits = 0;
+  bits |= fem::coef_zero(f.diff, e) ? 1 : 0;
+  bits |= fem::coef_zero(f.mass, e) ? 2 : 0;
+  bits |= fem::coef_zero(f.lam, e) ? 4 : 0;
+  bits |= fem::coef_zero(f.lap, e) ? 8 : 0;
+  bits |= fem::coef_zero(f.tr, e) ? 16 : 0;
+  if (bits != ref) st |= 1 << FEM_ERR_STALE_PATTERN;
+  return st;
+}
+
+__device__ __forceinline__ int ref_byte(const uint8_t* __restrict__ ref, int64_t e) {
+  return ref ? (int)__ldg(ref + e) : -1;
 }
 
 template <int D, int ORDER, int BS>
 __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBilinear f,
+                                                                FemCoef kdiff,
                                                                 double* __restrict__ out,
                                                                 const uint8_t* __restrict__ ref_bits,
                                                                 int32_t* __restrict__ status,
@@ -178,18 +186,21 @@ __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBiline
   constexpr int L = NB * NB;
   constexpr double INV_FACT = 1.0 / SimplexTraits<D, ORDER>::FACT;
   extern __shared__ double smem[];
+  int32_t flags = 0;
   // grid-stride over element tiles of BS cells (persistent when the grid is
   // smaller than the number of tiles)
   for (int64_t e0 = ebeg + (int64_t)blockIdx.x * BS; e0 < eend; e0 += (int64_t)gridDim.x * BS) {
   const int64_t e = e0 + threadIdx.x;
   if (e < eend) {
-    check_coef_bits(f, e, ref_bits, status);
+    const int rb = ref_byte(ref_bits, e);
     Simplex<D> s;
     simplex_geometry<D>(m, e, s);
-    const double adet = fabs(s.det);
-    // stiffness scale kd / (d! |det|); mass scale km |det| / d!
-    const double sd = coef_at(f.diff, e) * ((1.0 / adet) * INV_FACT);
-    const double sm = coef_at(f.mass, e) * (adet * INV_FACT);
+    const double adet = fem::abs_bits(s.det);
+    // stiffness scale kd / (d! |det|) (kdiff is f.diff with its scale
+    // multiplied by 1/d! on the host); mass scale km |det| (the 1/d! of the
+    // mass goes into the table constants, folded at compile time)
+    const double sd = coef_at(kdiff, e) * (1.0 / adet);
+    const double sm = coef_at(f.mass, e) * adet;
     // Gram of c_1..c_D, then row 0 from c_0 = -sum c_m
     double gram[D + 1][D + 1];
 #pragma unroll
@@ -198,22 +209,22 @@ __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBiline
       for (int b = a; b <= D; ++b) gram[a][b] = dotc<D>(s.c[a], s.c[b]);
 #pragma unroll
     for (int b = 1; b <= D; ++b) {
-      double acc = 0.0;
+      double acc = (1 <= b ? gram[1][b] : gram[b][1]);
 #pragma unroll
-      for (int a = 1; a <= D; ++a) acc = acc + (a <= b ? gram[a][b] : gram[b][a]);
+      for (int a = 2; a <= D; ++a) acc = acc + (a <= b ? gram[a][b] : gram[b][a]);
       gram[0][b] = -acc;
     }
     {
-      double acc = 0.0;
+      double acc = gram[0][1];
 #pragma unroll
-      for (int b = 1; b <= D; ++b) acc = acc + gram[0][b];
+      for (int b = 2; b <= D; ++b) acc = acc + gram[0][b];
       gram[0][0] = -acc;
     }
     double* row = smem + threadIdx.x * (L + 1);
     double kst[NB][NB];
 #define G(a, b) ((a) <= (b) ? gram[a][b] : gram[b][a])
 #define KS(i, j, v) { kst[i][j] = (v); }
-#define KM(i, j, v) { const double _v = sd * kst[i][j] + sm * (v); row[(i) * NB + (j)] = _v; row[(j) * NB + (i)] = _v; }
+#define KM(i, j, v) { constexpr double _m = (v) * INV_FACT; const double _v = sd * kst[i][j] + sm * _m; row[(i) * NB + (j)] = _v; row[(j) * NB + (i)] = _v; }
     if constexpr (D == 2 && ORDER == 1) { TRI1_STIFF(G, KS); TRI1_MASS(KM); }
     if constexpr (D == 2 && ORDER == 2) { TRI2_STIFF(G, KS); TRI2_MASS(KM); }
     if constexpr (D == 3 && ORDER == 1) { TET1_STIFF(G, KS); TET1_MASS(KM); }
@@ -221,9 +232,11 @@ __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBiline
 #undef G
 #undef KS
 #undef KM
+    if (status) flags |= coef_status(f, e, rb);
   }
   flush_rows<L, BS>(smem, out, e0, eend);
   }
+  fem::publish_status(status, flags);
 }
 
 // -------------------------------------------- simplex, vector P2 (and P1)
@@ -254,12 +267,13 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
   // E[p][q][a][b] for p <= q, kept in registers: every index below is a
   // compile-time constant once the block loops are unrolled.
   double E[NV][NV][D][D];
+  int32_t flags = 0;
   if (live) {
-    check_coef_bits(f, e, ref_bits, status);
+    const int rb = ref_byte(ref_bits, e);
     Simplex<D> s;
     simplex_geometry<D>(m, e, s);
     simplex_c0<D>(s);
-    const double adet = fabs(s.det);
+    const double adet = fem::abs_bits(s.det);
     const double s0 = 1.0 / (FACT * adet);
     const double lam = coef_at(f.lam, e) * s0;
     const double lap = coef_at(f.lap, e) * s0;
@@ -279,6 +293,7 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
             E[p][q][a][b] = v;
           }
       }
+    if (status) flags = coef_status(f, e, rb);
   }
   static_for<NS>([&](auto ic) {
     constexpr int i = decltype(ic)::value;
@@ -349,6 +364,7 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
     }
     __syncthreads();
   });
+  fem::publish_status(status, flags);
 }
 
 // ----------------------------------------------------------- hexahedron Q1
@@ -410,7 +426,7 @@ __device__ __forceinline__ double adj3(const double J[3][3], double ad[3][3]) {
 // M = |det| J^{-1} J^{-T} = adj adj^T / |det|  (symmetric)
 __device__ __forceinline__ void hex_metric(const double ad[3][3], double det, double w,
                                            double M[3][3]) {
-  const double s = w / fabs(det);
+  const double s = w / fem::abs_bits(det);
 #pragma unroll
   for (int k = 0; k < 3; ++k)
 #pragma unroll
@@ -444,8 +460,9 @@ __global__ void __launch_bounds__(kBlock) hex_scalar_kernel(FemMesh m, FemBiline
   extern __shared__ double smem[];
   const int64_t e0 = ebeg + (int64_t)blockIdx.x * kBlock;
   const int64_t e = e0 + threadIdx.x;
+  int32_t flags = 0;
   if (e < eend) {
-    check_coef_bits(f, e, ref_bits, status);
+    const int rb = ref_byte(ref_bits, e);
     Hex h;
     hex_load(m, e, h);
     const double kd = coef_at(f.diff, e);
@@ -455,10 +472,10 @@ __global__ void __launch_bounds__(kBlock) hex_scalar_kernel(FemMesh m, FemBiline
     if (hex_affine(h, J)) {
       double ad[3][3];
       const double det = adj3(J, ad);
-      if (det == 0.0) if (status) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
+      if (fem::zero_bits(det)) flags |= 1 << FEM_ERR_ZERO_JACOBIAN;
       double M[3][3];
       hex_metric(ad, det, kd, M);
-      const double sm = km * fabs(det);
+      const double sm = km * fem::abs_bits(det);
 #pragma unroll
       for (int i = 0; i < 8; ++i)
 #pragma unroll
@@ -496,13 +513,13 @@ __global__ void __launch_bounds__(kBlock) hex_scalar_kernel(FemMesh m, FemBiline
               }
             double ad[3][3];
             const double det = adj3(Jq, ad);
-            if (det == 0.0) {
-              if (status) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
+            if (fem::zero_bits(det)) {
+              flags |= 1 << FEM_ERR_ZERO_JACOBIAN;
               continue;
             }
             double M[3][3];
             hex_metric(ad, det, w * kd, M);
-            const double sm = w * km * fabs(det);
+            const double sm = w * km * fem::abs_bits(det);
             double hv[8][3];
 #pragma unroll
             for (int i = 0; i < 8; ++i)
@@ -523,7 +540,9 @@ __global__ void __launch_bounds__(kBlock) hex_scalar_kernel(FemMesh m, FemBiline
 #pragma unroll
         for (int j = 0; j < i; ++j) row[i * 8 + j] = row[j * 8 + i];
     }
+    if (status) flags |= coef_status(f, e, rb);
   }
+  fem::publish_status(status, flags);
   flush_rows<L>(smem, out, e0, eend);
 }
 
@@ -554,7 +573,7 @@ __global__ void simplex_load_kernel(FemMesh m, FemLinear f, int ncomp, double* _
           A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
           A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
   }
-  const double s = coef_at(f.load, e) * (fabs(det) / FACT);
+  const double s = coef_at(f.load, e) * (fem::abs_bits(det) / FACT);
 #pragma unroll
   for (int i = 0; i < NS; ++i) {
     double lv;
@@ -579,8 +598,8 @@ __global__ void hex_load_kernel(FemMesh m, FemLinear f, int ncomp, double* __res
   if (hex_affine(h, J)) {
     double ad[3][3];
     const double det = adj3(J, ad);
-    if (det == 0.0) if (status) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
-    const double v = fe * fabs(det) * 0.125;
+    if (fem::zero_bits(det)) if (status) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
+    const double v = fe * fem::abs_bits(det) * 0.125;
 #pragma unroll
     for (int i = 0; i < 8; ++i) b[i] = v;
   } else {
@@ -603,8 +622,8 @@ __global__ void hex_load_kernel(FemMesh m, FemLinear f, int ncomp, double* __res
         }
       double ad[3][3];
       const double det = adj3(Jq, ad);
-      if (det == 0.0) if (status) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
-      const double s = fe * w * fabs(det);
+      if (fem::zero_bits(det)) if (status) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
+      const double s = fe * w * fem::abs_bits(det);
 #pragma unroll
       for (int i = 0; i < 8; ++i) b[i] = b[i] + s * phi[i];
     }
@@ -635,8 +654,10 @@ static int launch_scalar(const FemMesh& m, const FemBilinear& f, double* out,
   if (rc) return rc;
   int64_t grid = fem::ceil_div(eend - ebeg, BS);
   if (persistent > 0) grid = std::min<int64_t>(grid, (int64_t)persistent * fem::num_sms());
-  simplex_scalar_kernel<D, O, BS><<<(unsigned)grid, BS, sm, st>>>(m, f, out, ref_bits, status,
-                                                                  ebeg, eend);
+  FemCoef kdiff = f.diff;
+  kdiff.scale = f.diff.scale * (1.0 / SimplexTraits<D, O>::FACT);
+  simplex_scalar_kernel<D, O, BS><<<(unsigned)grid, BS, sm, st>>>(m, f, kdiff, out, ref_bits,
+                                                                  status, ebeg, eend);
   return 0;
 }
 

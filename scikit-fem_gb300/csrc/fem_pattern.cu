@@ -279,8 +279,8 @@ __global__ void csr_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_
       for (int u = 0; u < U; ++u) {
         if (s[u] != 0xFFFF) {
           acc[s[u]] += v[u];
-          if (CHECK && v[u] != 0.0) seen[s[u]] = 1;
-        } else if (CHECK && v[u] != 0.0) {
+          if (CHECK && !zero_bits(v[u])) seen[s[u]] = 1;
+        } else if (CHECK && !zero_bits(v[u])) {
           stale = true;
         }
         __syncwarp();

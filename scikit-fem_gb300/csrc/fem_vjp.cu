@@ -90,7 +90,7 @@ __device__ __forceinline__ void simplex_grads(const FemMesh& m, int64_t e, doubl
     }
     g[0][k] = -s;
   }
-  vol = fabs(det) / Traits<D, 1>::FACT;
+  vol = fem::abs_bits(det) / Traits<D, 1>::FACT;
 }
 
 // local DOF of the P2 edge function between vertices a != c (element_tri_p2.py:
@@ -302,11 +302,11 @@ __device__ __forceinline__ void hex_vjp_affine(const double x[8][3], const doubl
   }
   double ad[3][3];
   const double det = adj3(J, ad);
-  if (det == 0.0) {
+  if (fem::zero_bits(det)) {
     if (status) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
     return;
   }
-  const double inv = 1.0 / det, adet = fabs(det);
+  const double inv = 1.0 / det, adet = fem::abs_bits(det);
   double Gm[3][3];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
@@ -550,11 +550,11 @@ __device__ __noinline__ void hex_vjp_general(const FemMesh m, const FemBasis b, 
       }
     double ad[3][3];
     const double det = adj3(J, ad);
-    if (det == 0.0) {
+    if (fem::zero_bits(det)) {
       if (status) atomicOr(status, 1 << FEM_ERR_ZERO_JACOBIAN);
       continue;
     }
-    const double inv = 1.0 / det, adet = fabs(det);
+    const double inv = 1.0 / det, adet = fem::abs_bits(det);
     double Gm[3][3];  // G = J^{-1}
 #pragma unroll
     for (int a = 0; a < 3; ++a)
