@@ -299,6 +299,43 @@ int fem_csr_sum_to_host(const FemPattern* pat, const double* staging, double* cs
                         double* host_values, int32_t nchunks, fem_stream_t stream,
                         fem_stream_t copy_stream);
 
+/* Rows of one strided host coefficient: row e (max(stride, 1) doubles) at
+ * host + e * stride, copied to dev + e * stride. */
+typedef struct FemHostRows {
+  const double* host; /* pageable host memory */
+  double* dev;
+  int64_t stride;
+} FemHostRows;
+
+/* *supported = 1 when kernels on the current device can read pageable host
+ * memory (cudaDevAttrPageableMemoryAccess) -- the condition for passing
+ * host rows to fem_assemble_to_host_pipelined. */
+int fem_host_memory_access(int32_t* supported);
+
+/*
+ * fem_assemble_to_host pipelined by data dependence.  The cells are taken
+ * in order of their smallest DOF, in nchunks chunks of about equal size;
+ * once every cell whose smallest DOF is below m has its local matrix, the
+ * rows [0, m) are final.  Per chunk: the host rows of its cells' strided
+ * coefficients (nfields of them, 0..16) are copied to their device arrays
+ * on upload_stream by a kernel that reads the host memory directly; the
+ * chunk's local kernel runs on stream after them; the rows it completes
+ * are summed and their values copied to host_values (pinned, nnz doubles)
+ * on copy_stream behind the sum.  The upload, the local kernels and the
+ * copy of the values back overlap on any mesh, and the call returns
+ * without waiting for any of it (the caller synchronises copy_stream and
+ * reads status).  Results are the same, bit for bit, as fem_assemble.
+ * The cell order and the chunks' row bounds are computed once per pattern
+ * and chunk count (synchronous, on first use).  Host rows need
+ * fem_host_memory_access (FEM_ERR_UNSUPPORTED otherwise).
+ */
+int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
+                                   const FemBilinear* form, const FemPattern* pat,
+                                   double* staging, double* csr_values, double* host_values,
+                                   int32_t* status, const FemHostRows* rows, int32_t nfields,
+                                   int32_t nchunks, fem_stream_t stream,
+                                   fem_stream_t upload_stream, fem_stream_t copy_stream);
+
 int fem_csr_sum(const FemPattern* pat, const double* local, double* csr_values, int32_t* status,
                 fem_stream_t stream);
 

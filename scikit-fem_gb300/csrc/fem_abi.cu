@@ -12,9 +12,11 @@ namespace fem_fast {
 int local_matrices(const FemMesh&, const FemBasis&, const FemBilinear&, double*, int32_t*,
                    cudaStream_t);
 // cells [ebeg, eend) only (eend < 0: to the last cell)
+// cells [ebeg, eend) only (eend < 0: to the last cell); with a cell list,
+// the cells cells[ebeg .. eend-1]
 int local_matrices_checked(const FemMesh&, const FemBasis&, const FemBilinear&, double*,
                            const uint8_t*, int32_t*, cudaStream_t, int64_t ebeg = 0,
-                           int64_t eend = -1);
+                           int64_t eend = -1, const int32_t* cells = nullptr);
 int local_vectors(const FemMesh&, const FemBasis&, const FemLinear&, double*, int32_t*,
                   cudaStream_t);
 }  // namespace fem_fast
@@ -112,6 +114,14 @@ struct FemPattern {
   uint8_t* coef_bits = nullptr;  // nelems, or null when built without a form
   std::vector<int32_t> host_indptr;  // host copy of indptr (row ranges of fem_assemble_to_host)
   int family = 0, vector = 0;
+  // Plan of fem_assemble_to_host_pipelined, built once per chunk count:
+  // the cells sorted by their smallest DOF (device), the chunks' bounds in
+  // that order, and the rows complete after each chunk.
+  mutable std::mutex plan_mu;
+  mutable int plan_nchunks = 0;
+  mutable int32_t* plan_cells = nullptr;
+  mutable std::vector<int64_t> plan_bounds;   // plan_nchunks + 1 positions
+  mutable std::vector<int64_t> plan_rows;     // plan_nchunks: rows [0, plan_rows[c]) final
 };
 
 using fem::set_error;
@@ -352,6 +362,7 @@ void fem_pattern_destroy(FemPattern* pat) {
   if (!pat) return;
   fem::free_pattern(new fem::Pattern(pat->P));
   cudaFree(pat->coef_bits);
+  cudaFree(pat->plan_cells);
   delete pat;
 }
 
@@ -403,6 +414,47 @@ int fem_assemble_local(const FemMesh* mesh, const FemBasis* basis, const FemBili
                                           (cudaStream_t)stream, cell_begin, cell_end);
 }
 
+namespace {
+// Row bounds of nchunks ranges of about equal nnz, cut with the pattern's
+// host copy of indptr; every range non-empty in rows.
+std::vector<int64_t> row_ranges(const std::vector<int32_t>& ip, int64_t nrows, int64_t nnz,
+                                int nchunks) {
+  std::vector<int64_t> b{0};
+  int64_t row = 0;
+  for (int c = 0; c < nchunks && row < nrows; ++c) {
+    const int64_t target = nnz * (c + 1) / nchunks;
+    int64_t row1 = c == nchunks - 1
+        ? nrows
+        : (int64_t)(std::upper_bound(ip.begin() + row, ip.end(), (int32_t)target) - ip.begin()) - 1;
+    if (row1 <= row) row1 = std::min<int64_t>(nrows, row + 1);
+    b.push_back(row1);
+    row = row1;
+  }
+  return b;
+}
+
+// Sums rows [row0, row1) and queues their values' copy to the host on cs
+// behind the sum.
+int sum_rows_to_host(const fem::Pattern& P, const std::vector<int32_t>& ip, const double* staging,
+                     double* csr_values, double* host_values, int64_t row0, int64_t row1,
+                     cudaStream_t st, cudaStream_t cs) {
+  int rc = fem::csr_sum(P, staging, csr_values, st, row0, row1);
+  if (rc) return rc;
+  const int64_t a = ip[row0], b = ip[row1];
+  if (b > a) {
+    cudaEvent_t ev;
+    FEM_TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaError_t e = cudaEventRecord(ev, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev, 0);
+    cudaEventDestroy(ev);
+    if (e != cudaSuccess) return fem::check_cuda(e, "sum -> copy event");
+    FEM_TRY_CUDA(cudaMemcpyAsync(host_values + a, csr_values + a, (b - a) * sizeof(double),
+                                 cudaMemcpyDeviceToHost, cs));
+  }
+  return 0;
+}
+}  // namespace
+
 int fem_csr_sum_to_host(const FemPattern* pat, const double* staging, double* csr_values,
                         double* host_values, int32_t nchunks, fem_stream_t stream,
                         fem_stream_t copy_stream) {
@@ -423,27 +475,333 @@ int fem_csr_sum_to_host(const FemPattern* pat, const double* staging, double* cs
     set_error(FEM_ERR_ARGUMENT, "pattern has no host row pointer");
     return FEM_ERR_ARGUMENT;
   }
-  int64_t row = 0;
-  for (int c = 0; c < nchunks && row < P.nrows; ++c) {
-    const int64_t target = (int64_t)P.nnz * (c + 1) / nchunks;
-    int64_t row1 = c == nchunks - 1
-        ? P.nrows
-        : (int64_t)(std::upper_bound(ip.begin() + row, ip.end(), (int32_t)target) - ip.begin()) - 1;
-    if (row1 <= row) row1 = std::min<int64_t>(P.nrows, row + 1);
-    int rc = fem::csr_sum(P, staging, csr_values, st, row, row1);
+  const std::vector<int64_t> b = row_ranges(ip, P.nrows, P.nnz, nchunks);
+  for (size_t k = 0; k + 1 < b.size(); ++k) {
+    int rc = sum_rows_to_host(P, ip, staging, csr_values, host_values, b[k], b[k + 1], st, cs);
     if (rc) return rc;
-    const int64_t a = ip[row], b = ip[row1];
-    if (b > a) {
-      cudaEvent_t ev;
-      FEM_TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-      FEM_TRY_CUDA(cudaEventRecord(ev, st));
-      FEM_TRY_CUDA(cudaStreamWaitEvent(cs, ev, 0));
-      cudaEventDestroy(ev);
-      FEM_TRY_CUDA(cudaMemcpyAsync(host_values + a, csr_values + a, (b - a) * sizeof(double),
-                                   cudaMemcpyDeviceToHost, cs));
-    }
-    row = row1;
   }
+  return 0;
+}
+
+namespace {
+// Smallest DOF of each cell (the sort key of the pipeline plan).
+// A DOF outside [0, nrows) sets *bad and the cell is left out (the plan
+// is then refused).
+__global__ void cell_min_dof_kernel(const int32_t* __restrict__ dofs, int64_t nelems, int nb,
+                                    int64_t nrows, int32_t* __restrict__ key,
+                                    int32_t* __restrict__ hist, int32_t* __restrict__ bad) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nelems) return;
+  int32_t k = dofs[e];
+  for (int i = 1; i < nb; ++i) k = min(k, dofs[(int64_t)i * nelems + e]);
+  if (k < 0 || k >= nrows) {
+    atomicOr(bad, 1);
+    key[e] = -1;
+    return;
+  }
+  key[e] = k;
+  atomicAdd(hist + k, 1);
+}
+
+// Chunk of each cell: chunk c takes the keys [kb[c], kb[c+1]).
+__global__ void cell_chunk_kernel(const int32_t* __restrict__ key, int64_t nelems,
+                                  const int32_t* __restrict__ kb, int nchunks,
+                                  int32_t* __restrict__ chunk) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nelems) return;
+  const int32_t k = key[e];
+  int lo = 0, hi = nchunks - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (kb[mid] <= k) lo = mid;
+    else hi = mid - 1;
+  }
+  chunk[e] = lo;
+}
+
+__global__ void chunk_flag_kernel(const int32_t* __restrict__ chunk, int64_t nelems, int c,
+                                  int32_t* __restrict__ flag) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < nelems) flag[e] = chunk[e] == c ? 1 : 0;
+  else if (e == nelems) flag[e] = 0;
+}
+
+// Stable compaction: the cells of chunk c, ascending.
+__global__ void chunk_scatter_kernel(const int32_t* __restrict__ chunk, int64_t nelems, int c,
+                                     const int32_t* __restrict__ pos, int32_t* __restrict__ out) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < nelems && chunk[e] == c) out[pos[e]] = (int32_t)e;
+}
+
+// Builds pat's pipeline plan for nchunks chunks (synchronous, once): the
+// cells are split by their smallest DOF at key bounds chosen for chunks of
+// about equal size, and each chunk lists its cells in ascending order (so
+// that its coefficient rows, geometry and staging rows are read and
+// written in runs).
+int pipeline_plan(const FemPattern* pat, const FemBasis& b, int64_t nelems, int nchunks,
+                  cudaStream_t st) {
+  std::lock_guard<std::mutex> lock(pat->plan_mu);
+  if (pat->plan_nchunks == nchunks && pat->plan_cells) return 0;
+  const int64_t nrows = pat->P.nrows;
+  int32_t *key = nullptr, *hist = nullptr, *cum = nullptr, *chunk = nullptr, *flag = nullptr,
+          *pos = nullptr, *kb = nullptr, *cells = nullptr;
+  int32_t bad_h = 0;
+  auto cleanup = [&]() {
+    for (int32_t* q : {key, hist, cum, chunk, flag, pos, kb}) cudaFreeAsync(q, st);
+  };
+  const int64_t ne1 = std::max<int64_t>(1, nelems);
+  cudaError_t e = cudaMallocAsync(&key, ne1 * 4, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&hist, (nrows + 2) * 4, st);  // + the bad flag
+  if (e == cudaSuccess) e = cudaMallocAsync(&cum, (nrows + 1) * 4, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&chunk, ne1 * 4, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&flag, (ne1 + 1) * 4, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&pos, (ne1 + 1) * 4, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&kb, (nchunks + 1) * 4, st);
+  if (e == cudaSuccess) e = cudaMalloc(&cells, ne1 * 4);
+  if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, (nrows + 2) * 4, st);
+  if (e != cudaSuccess) {
+    cleanup();
+    cudaFree(cells);
+    return fem::check_cuda(e, "pipeline plan buffers");
+  }
+  const unsigned grid = (unsigned)fem::ceil_div(ne1 + 1, 256);
+  std::vector<int64_t> bounds(nchunks + 1, 0);
+  std::vector<int32_t> kbh(nchunks + 1, (int32_t)nrows);
+  int rc = 0;
+  if (nelems > 0) {
+    int32_t* bad = hist + nrows + 1;
+    cell_min_dof_kernel<<<grid, 256, 0, st>>>(b.element_dofs, nelems, b.nbfun, nrows, key, hist,
+                                              bad);
+    e = cudaMemcpyAsync(&bad_h, bad, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = fem::check_cuda(e, "pipeline plan keys");
+    else if (bad_h) {
+      fem::set_error(FEM_ERR_ARGUMENT, "element DOFs outside the pattern's %lld rows",
+                     (long long)nrows);
+      rc = FEM_ERR_ARGUMENT;
+    }
+    // cum[k] = cells whose key is below k; chunk c takes the keys from the
+    // first k with cum[k] >= c * nelems / nchunks
+    std::vector<int32_t> cumh(nrows + 1);
+    if (!rc) rc = fem::exclusive_scan_i32(hist, cum, nrows, nullptr, st);
+    if (!rc) {
+      e = cudaMemcpyAsync(cumh.data(), cum, (nrows + 1) * 4, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) rc = fem::check_cuda(e, "pipeline plan histogram");
+    }
+    if (!rc) {
+      kbh[0] = 0;
+      for (int k = 1; k < nchunks; ++k) {
+        const int64_t target = nelems * k / nchunks;
+        kbh[k] = (int32_t)(std::lower_bound(cumh.begin(), cumh.end(), (int32_t)target) -
+                           cumh.begin());
+        kbh[k] = std::min<int32_t>(std::max(kbh[k], kbh[k - 1]), (int32_t)nrows);
+      }
+      kbh[nchunks] = (int32_t)nrows;
+      for (int k = 0; k < nchunks; ++k) bounds[k] = cumh[kbh[k]];
+      bounds[nchunks] = nelems;
+      e = cudaMemcpyAsync(kb, kbh.data(), (nchunks + 1) * 4, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) {
+        cell_chunk_kernel<<<grid, 256, 0, st>>>(key, nelems, kb, nchunks, chunk);
+        e = cudaGetLastError();
+      }
+      for (int c = 0; c < nchunks && e == cudaSuccess && !rc; ++c) {
+        if (bounds[c + 1] == bounds[c]) continue;
+        chunk_flag_kernel<<<grid, 256, 0, st>>>(chunk, nelems, c, flag);
+        rc = fem::exclusive_scan_i32(flag, pos, nelems, nullptr, st);
+        if (!rc) {
+          chunk_scatter_kernel<<<grid, 256, 0, st>>>(chunk, nelems, c, pos, cells + bounds[c]);
+          e = cudaGetLastError();
+        }
+      }
+      // kbh stays alive until the stream has read it
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (!rc && e != cudaSuccess) rc = fem::check_cuda(e, "pipeline plan");
+    }
+  }
+  cleanup();
+  if (rc) {
+    cudaFree(cells);
+    return rc;
+  }
+  cudaFree(pat->plan_cells);
+  pat->plan_cells = cells;
+  pat->plan_bounds = bounds;
+  // rows below the first key of chunk c+1 are final once chunks 0..c are done
+  pat->plan_rows.assign(nchunks, nrows);
+  for (int k = 0; k + 1 < nchunks; ++k) pat->plan_rows[k] = std::min<int64_t>(kbh[k + 1], nrows);
+  pat->plan_nchunks = nchunks;
+  return 0;
+}
+
+// Copies the host rows of the cells cells[a .. b) (stride doubles each)
+// into the device array, reading host memory directly (the device's
+// pageable-memory access); 16-byte loads when the layout allows them.  The
+// copy is bound by the host link's latency, not by the SMs: a small grid
+// keeps kGatherUnroll independent loads in flight per thread and leaves
+// the SMs to the local kernels that run beside it.
+constexpr int kGatherUnroll = 4;
+
+__global__ void gather_host_rows_kernel(FemHostRows r, const int32_t* __restrict__ cells,
+                                        int64_t a, int64_t b, int wide) {
+  const int64_t stride = r.stride > 1 ? r.stride : 1;
+  const int64_t per = wide ? stride / 2 : stride;  // loads per row
+  const int64_t n = (b - a) * per;
+  const int64_t nt = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t g0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g0 < n;
+       g0 += nt * kGatherUnroll) {
+    int64_t off[kGatherUnroll];
+#pragma unroll
+    for (int u = 0; u < kGatherUnroll; ++u) {
+      const int64_t g = g0 + u * nt;
+      off[u] = -1;
+      if (g < n) {
+        const int64_t i = g / per, q = g - i * per;
+        off[u] = (int64_t)__ldg(cells + a + i) * per + q;  // in load units
+      }
+    }
+    if (wide) {
+      double2 v[kGatherUnroll];
+#pragma unroll
+      for (int u = 0; u < kGatherUnroll; ++u)
+        if (off[u] >= 0) v[u] = reinterpret_cast<const double2*>(r.host)[off[u]];
+#pragma unroll
+      for (int u = 0; u < kGatherUnroll; ++u)
+        if (off[u] >= 0) reinterpret_cast<double2*>(r.dev)[off[u]] = v[u];
+    } else {
+      double v[kGatherUnroll];
+#pragma unroll
+      for (int u = 0; u < kGatherUnroll; ++u)
+        if (off[u] >= 0) v[u] = r.host[off[u]];
+#pragma unroll
+      for (int u = 0; u < kGatherUnroll; ++u)
+        if (off[u] >= 0) r.dev[off[u]] = v[u];
+    }
+  }
+}
+}  // namespace
+
+int fem_host_memory_access(int32_t* supported) {
+  if (!supported) {
+    set_error(FEM_ERR_ARGUMENT, "null output");
+    return FEM_ERR_ARGUMENT;
+  }
+  int dev = 0, v = 0;
+  FEM_TRY_CUDA(cudaGetDevice(&dev));
+  FEM_TRY_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev));
+  *supported = v ? 1 : 0;
+  return 0;
+}
+
+int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
+                                   const FemBilinear* form, const FemPattern* pat,
+                                   double* staging, double* csr_values, double* host_values,
+                                   int32_t* status, const FemHostRows* rows, int32_t nfields,
+                                   int32_t nchunks, fem_stream_t stream,
+                                   fem_stream_t upload_stream, fem_stream_t copy_stream) {
+  int rc = validate(mesh, basis);
+  if (rc) return rc;
+  if (!form || !pat || !staging || !csr_values || !host_values || nchunks < 1 ||
+      nchunks > 256 || nfields < 0 || nfields > 16 || (nfields > 0 && !rows)) {
+    set_error(FEM_ERR_ARGUMENT, "null argument, chunks outside 1..256 or fields outside 0..16");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (pat->P.nelems != mesh->nelems || pat->P.nbfun_v != basis->nbfun || !pat->P.has_matrix ||
+      pat->P.nrows != basis->ndofs || (int64_t)pat->host_indptr.size() != pat->P.nrows + 1) {
+    set_error(FEM_ERR_ARGUMENT, "pattern does not belong to this mesh / basis");
+    return FEM_ERR_ARGUMENT;
+  }
+  for (int k = 0; k < nfields; ++k)
+    if (!rows[k].host || !rows[k].dev || rows[k].stride < 0) {
+      set_error(FEM_ERR_ARGUMENT, "host rows %d: null pointer or negative stride", k);
+      return FEM_ERR_ARGUMENT;
+    }
+  if (nfields > 0) {
+    int32_t ok = 0;
+    if ((rc = fem_host_memory_access(&ok))) return rc;
+    if (!ok) {
+      set_error(FEM_ERR_UNSUPPORTED, "kernels on this device cannot read pageable host memory "
+                "(upload the coefficients first, then pass no host rows)");
+      return FEM_ERR_UNSUPPORTED;
+    }
+  }
+  cudaStream_t st = (cudaStream_t)stream, up = (cudaStream_t)upload_stream,
+               cs = (cudaStream_t)copy_stream;
+  const int64_t ne = mesh->nelems;
+  if ((rc = pipeline_plan(pat, *basis, ne, nchunks, st))) return rc;
+  fem::Pattern P = pat->P;
+  P.sum_unroll = fem::tuning_for(pat->family).sum_unroll;
+  const std::vector<int64_t>& cb = pat->plan_bounds;
+  const std::vector<int64_t>& done = pat->plan_rows;
+  const int32_t* cells = pat->plan_cells;
+  std::vector<cudaEvent_t> evs;
+  auto event = [&](cudaEvent_t* ev) -> cudaError_t {
+    cudaError_t e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) evs.push_back(*ev);
+    return e;
+  };
+  auto release = [&]() {
+    for (cudaEvent_t ev : evs) cudaEventDestroy(ev);
+  };
+  // the coefficient rows of every chunk, queued on the upload stream
+  std::vector<cudaEvent_t> ready(nchunks, nullptr);
+  if (nfields > 0) {
+    cudaEvent_t start;
+    cudaError_t e = event(&start);
+    if (e == cudaSuccess) e = cudaEventRecord(start, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(up, start, 0);
+    for (int c = 0; c < nchunks && e == cudaSuccess; ++c) {
+      const int64_t n = cb[c + 1] - cb[c];
+      for (int k = 0; k < nfields && n > 0; ++k) {
+        const int64_t s = rows[k].stride > 1 ? rows[k].stride : 1;
+        const int wide = (s % 2 == 0) && ((uintptr_t)rows[k].host % 16 == 0) &&
+                         ((uintptr_t)rows[k].dev % 16 == 0);
+        const int64_t work = n * (wide ? s / 2 : s);
+        const unsigned grid = (unsigned)std::max<int64_t>(
+            1, std::min<int64_t>(fem::ceil_div(work, 256 * kGatherUnroll),
+                                 (int64_t)fem::num_sms() / 2));
+        gather_host_rows_kernel<<<grid, 256, 0, up>>>(rows[k], cells, cb[c], cb[c + 1], wide);
+      }
+      e = cudaGetLastError();
+      if (e == cudaSuccess) e = event(&ready[c]);
+      if (e == cudaSuccess) e = cudaEventRecord(ready[c], up);
+    }
+    if (e != cudaSuccess) {
+      release();
+      return fem::check_cuda(e, "host row gather");
+    }
+  }
+  int64_t row = 0;
+  for (int c = 0; c < nchunks; ++c) {
+    if (ready[c]) {
+      cudaError_t e = cudaStreamWaitEvent(st, ready[c], 0);
+      if (e != cudaSuccess) {
+        release();
+        return fem::check_cuda(e, "wait for host rows");
+      }
+    }
+    if (cb[c + 1] > cb[c]) {
+      rc = fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
+                                            status ? pat->coef_bits : nullptr, status, st,
+                                            cb[c], cb[c + 1], cells);
+      if (rc) {
+        release();
+        return rc;
+      }
+    }
+    // rows below the smallest DOF of the next chunk's first cell are final
+    const int64_t row1 = done[c];
+    if (row1 > row) {
+      rc = sum_rows_to_host(P, pat->host_indptr, staging, csr_values, host_values, row, row1, st,
+                            cs);
+      if (rc) {
+        release();
+        return rc;
+      }
+      row = row1;
+    }
+  }
+  release();
   return 0;
 }
 

@@ -122,19 +122,34 @@ __device__ __forceinline__ double dotc(const double* a, const double* b) {
 }
 
 // ----------------------------------------------------------- smem epilogue
+// The cells of a launch: positions [ebeg, eend) of the list `cells`, or the
+// cells ebeg .. eend-1 themselves when cells is null.
+__device__ __forceinline__ int64_t cell_at(const int32_t* __restrict__ cells, int64_t pos) {
+  return cells ? (int64_t)__ldg(cells + pos) : pos;
+}
+
 // Each thread writes its element's matrix into a padded row of shared
-// memory; the block then streams the rows out contiguously.
+// memory; the block then streams the rows out (each cell's row contiguous,
+// consecutive cells contiguous without a cell list).
 template <int L, int BS = kBlock>
 __device__ __forceinline__ void flush_rows(double* smem, double* __restrict__ out, int64_t e0,
-                                           int64_t nelems) {
+                                           int64_t nelems, const int32_t* __restrict__ cells) {
   __syncthreads();
   const int64_t nb = ((nelems - e0) < (int64_t)BS ? (nelems - e0) : (int64_t)BS);
   const int64_t total = nb * L;
-  double* dst = out + e0 * L;
-  for (int64_t g = threadIdx.x; g < total; g += blockDim.x) {
-    const int el = (int)(g / L);
-    const int k = (int)(g - (int64_t)el * L);
-    dst[g] = smem[el * (L + 1) + k];
+  if (!cells) {
+    double* dst = out + e0 * L;
+    for (int64_t g = threadIdx.x; g < total; g += blockDim.x) {
+      const int el = (int)(g / L);
+      const int k = (int)(g - (int64_t)el * L);
+      dst[g] = smem[el * (L + 1) + k];
+    }
+  } else {
+    for (int64_t g = threadIdx.x; g < total; g += blockDim.x) {
+      const int el = (int)(g / L);
+      const int k = (int)(g - (int64_t)el * L);
+      out[(int64_t)__ldg(cells + e0 + el) * L + k] = smem[el * (L + 1) + k];
+    }
   }
   __syncthreads();
 }
@@ -181,6 +196,7 @@ __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBiline
                                                                 double* __restrict__ out,
                                                                 const uint8_t* __restrict__ ref_bits,
                                                                 int32_t* __restrict__ status,
+                                                                const int32_t* __restrict__ cells,
                                                                 int64_t ebeg, int64_t eend) {
   constexpr int NB = SimplexTraits<D, ORDER>::NB;
   constexpr int L = NB * NB;
@@ -190,8 +206,9 @@ __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBiline
   // grid-stride over element tiles of BS cells (persistent when the grid is
   // smaller than the number of tiles)
   for (int64_t e0 = ebeg + (int64_t)blockIdx.x * BS; e0 < eend; e0 += (int64_t)gridDim.x * BS) {
-  const int64_t e = e0 + threadIdx.x;
-  if (e < eend) {
+  const int64_t pos = e0 + threadIdx.x;
+  if (pos < eend) {
+    const int64_t e = cell_at(cells, pos);
     const int rb = ref_byte(ref_bits, e);
     Simplex<D> s;
     simplex_geometry<D>(m, e, s);
@@ -234,7 +251,7 @@ __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBiline
 #undef KM
     if (status) flags |= coef_status(f, e, rb);
   }
-  flush_rows<L, BS>(smem, out, e0, eend);
+  flush_rows<L, BS>(smem, out, e0, eend, cells);
   }
   fem::publish_status(status, flags);
 }
@@ -250,6 +267,7 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
                                                             double* __restrict__ out,
                                                             const uint8_t* __restrict__ ref_bits,
                                                             int32_t* __restrict__ status,
+                                                            const int32_t* __restrict__ cells,
                                                             int64_t ebeg, int64_t eend) {
   constexpr int BS = 64;
   constexpr int NS = SimplexTraits<D, ORDER>::NB;  // scalar functions
@@ -260,9 +278,9 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
   extern __shared__ double smem[];
   double* rows = smem;                               // [BS][RB+1]
   const int64_t e0 = ebeg + (int64_t)blockIdx.x * BS;
-  const int64_t e = e0 + threadIdx.x;
   const int tid = threadIdx.x;
-  const bool live = e < eend;
+  const bool live = e0 + tid < eend;
+  const int64_t e = live ? cell_at(cells, e0 + tid) : 0;
   double sm = 0.0;
   // E[p][q][a][b] for p <= q, kept in registers: every index below is a
   // compile-time constant once the block loops are unrolled.
@@ -360,7 +378,8 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
     for (int64_t g = threadIdx.x; g < nb * RB; g += blockDim.x) {
       const int el = (int)(g / RB);
       const int k = (int)(g - (int64_t)el * RB);
-      out[(e0 + el) * (int64_t)(NB * NB) + (int64_t)i * RB + k] = rows[el * (RB + 1) + k];
+      out[cell_at(cells, e0 + el) * (int64_t)(NB * NB) + (int64_t)i * RB + k] =
+          rows[el * (RB + 1) + k];
     }
     __syncthreads();
   });
@@ -455,13 +474,14 @@ __global__ void __launch_bounds__(kBlock) hex_scalar_kernel(FemMesh m, FemBiline
                                                             double* __restrict__ out,
                                                             const uint8_t* __restrict__ ref_bits,
                                                             int32_t* __restrict__ status,
+                                                            const int32_t* __restrict__ cells,
                                                             int64_t ebeg, int64_t eend) {
   constexpr int L = 64;
   extern __shared__ double smem[];
   const int64_t e0 = ebeg + (int64_t)blockIdx.x * kBlock;
-  const int64_t e = e0 + threadIdx.x;
   int32_t flags = 0;
-  if (e < eend) {
+  if (e0 + threadIdx.x < eend) {
+    const int64_t e = cell_at(cells, e0 + threadIdx.x);
     const int rb = ref_byte(ref_bits, e);
     Hex h;
     hex_load(m, e, h);
@@ -543,7 +563,7 @@ __global__ void __launch_bounds__(kBlock) hex_scalar_kernel(FemMesh m, FemBiline
     if (status) flags |= coef_status(f, e, rb);
   }
   fem::publish_status(status, flags);
-  flush_rows<L>(smem, out, e0, eend);
+  flush_rows<L>(smem, out, e0, eend, cells);
 }
 
 // ------------------------------------------------------------ load vectors
@@ -647,7 +667,7 @@ static int set_smem(K kernel, size_t bytes) {
 template <int D, int O, int BS>
 static int launch_scalar(const FemMesh& m, const FemBilinear& f, double* out,
                          const uint8_t* ref_bits, int32_t* status, int persistent,
-                         cudaStream_t st, int64_t ebeg, int64_t eend) {
+                         cudaStream_t st, int64_t ebeg, int64_t eend, const int32_t* cells) {
   constexpr int NB = SimplexTraits<D, O>::NB;
   const size_t sm = (size_t)BS * (NB * NB + 1) * sizeof(double);
   int rc = set_smem(simplex_scalar_kernel<D, O, BS>, sm);
@@ -657,26 +677,26 @@ static int launch_scalar(const FemMesh& m, const FemBilinear& f, double* out,
   FemCoef kdiff = f.diff;
   kdiff.scale = f.diff.scale * (1.0 / SimplexTraits<D, O>::FACT);
   simplex_scalar_kernel<D, O, BS><<<(unsigned)grid, BS, sm, st>>>(m, f, kdiff, out, ref_bits,
-                                                                  status, ebeg, eend);
+                                                                  status, cells, ebeg, eend);
   return 0;
 }
 
 template <int D, int O>
 static int launch_scalar_tuned(const FemMesh& m, const FemBilinear& f, double* out,
                                const uint8_t* ref_bits, int32_t* status, cudaStream_t st,
-                               int64_t ebeg, int64_t eend) {
+                               int64_t ebeg, int64_t eend, const int32_t* cells) {
   const fem::Tuning t = fem::tuning_for(D == 2 ? (O == 1 ? FEM_TRI_P1 : FEM_TRI_P2)
                                                : (O == 1 ? FEM_TET_P1 : FEM_TET_P2));
   switch (t.local_block) {
-    case 64: return launch_scalar<D, O, 64>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend);
-    case 256: return launch_scalar<D, O, 256>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend);
-    default: return launch_scalar<D, O, 128>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend);
+    case 64: return launch_scalar<D, O, 64>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend, cells);
+    case 256: return launch_scalar<D, O, 256>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend, cells);
+    default: return launch_scalar<D, O, 128>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend, cells);
   }
 }
 
 int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinear& f, double* out,
                            const uint8_t* ref_bits, int32_t* status, cudaStream_t st,
-                           int64_t ebeg, int64_t eend) {
+                           int64_t ebeg, int64_t eend, const int32_t* cells) {
   if (eend < 0 || eend > m.nelems) eend = m.nelems;
   if (ebeg < 0) ebeg = 0;
   if (eend <= ebeg) return 0;
@@ -685,15 +705,15 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
   int rc = 0;
   if (!b.vector) {
     switch (fam) {
-      case FEM_TRI_P1: rc = launch_scalar_tuned<2, 1>(m, f, out, ref_bits, status, st, ebeg, eend); break;
-      case FEM_TRI_P2: rc = launch_scalar_tuned<2, 2>(m, f, out, ref_bits, status, st, ebeg, eend); break;
-      case FEM_TET_P1: rc = launch_scalar_tuned<3, 1>(m, f, out, ref_bits, status, st, ebeg, eend); break;
-      case FEM_TET_P2: rc = launch_scalar_tuned<3, 2>(m, f, out, ref_bits, status, st, ebeg, eend); break;
+      case FEM_TRI_P1: rc = launch_scalar_tuned<2, 1>(m, f, out, ref_bits, status, st, ebeg, eend, cells); break;
+      case FEM_TRI_P2: rc = launch_scalar_tuned<2, 2>(m, f, out, ref_bits, status, st, ebeg, eend, cells); break;
+      case FEM_TET_P1: rc = launch_scalar_tuned<3, 1>(m, f, out, ref_bits, status, st, ebeg, eend, cells); break;
+      case FEM_TET_P2: rc = launch_scalar_tuned<3, 2>(m, f, out, ref_bits, status, st, ebeg, eend, cells); break;
       case FEM_HEX_1: {
         const size_t sm = (size_t)kBlock * 65 * sizeof(double);
         if ((rc = set_smem(hex_scalar_kernel, sm))) return rc;
-        hex_scalar_kernel<<<(unsigned)grid, kBlock, sm, st>>>(m, f, out, ref_bits, status, ebeg,
-                                                              eend);
+        hex_scalar_kernel<<<(unsigned)grid, kBlock, sm, st>>>(m, f, out, ref_bits, status, cells,
+                                                              ebeg, eend);
         break;
       }
       default:
@@ -710,7 +730,7 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
     constexpr int RB = D * NB;                                                         \
     const size_t sm = (size_t)64 * (RB + 1) * sizeof(double);                          \
     if ((rc = set_smem(simplex_vector_kernel<D, O>, sm))) return rc;                   \
-    simplex_vector_kernel<D, O><<<(unsigned)vgrid, 64, sm, st>>>(m, f, out, ref_bits, status, ebeg, eend); \
+    simplex_vector_kernel<D, O><<<(unsigned)vgrid, 64, sm, st>>>(m, f, out, ref_bits, status, cells, ebeg, eend); \
     break;                                                                             \
   }
       case FEM_TRI_P1: LAUNCH_V(2, 1)
@@ -730,7 +750,7 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
 
 int local_matrices(const FemMesh& m, const FemBasis& b, const FemBilinear& f, double* out,
                    int32_t* status, cudaStream_t st) {
-  return local_matrices_checked(m, b, f, out, nullptr, status, st, 0, -1);
+  return local_matrices_checked(m, b, f, out, nullptr, status, st, 0, -1, nullptr);
 }
 
 int local_vectors(const FemMesh& m, const FemBasis& b, const FemLinear& f, double* out,

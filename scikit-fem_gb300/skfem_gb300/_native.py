@@ -42,6 +42,10 @@ class FemCoef(ctypes.Structure):
                 ("stride", ctypes.c_int64)]
 
 
+class FemHostRows(ctypes.Structure):
+    _fields_ = [("host", ctypes.c_void_p), ("dev", ctypes.c_void_p), ("stride", ctypes.c_int64)]
+
+
 class FemBilinear(ctypes.Structure):
     _fields_ = [("diff", FemCoef), ("mass", FemCoef), ("lam", FemCoef),
                 ("lap", FemCoef), ("tr", FemCoef)]
@@ -131,6 +135,10 @@ _SIGS = {
     "fem_assemble_local": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_int64,
                                           _P]),
     "fem_csr_sum_to_host": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32, _P, _P]),
+    "fem_host_memory_access": (ctypes.c_int, [_P]),
+    "fem_assemble_to_host_pipelined": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                                      ctypes.c_int32, ctypes.c_int32, _P, _P,
+                                                      _P]),
     "fem_facet_geometry": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P, _P, _P, _P]),
     "fem_enforce": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _P, ctypes.c_int64,
                                    ctypes.c_double, _P, _P, _P, _P]),
@@ -159,6 +167,19 @@ def lib():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+_host_access = None
+
+
+def host_memory_access():
+    """Whether kernels on the current device read pageable host memory."""
+    global _host_access
+    if _host_access is None:
+        v = ctypes.c_int32(0)
+        check(lib().fem_host_memory_access(ctypes.byref(v)))
+        _host_access = bool(v.value)
+    return _host_access
 
 
 def require_cuda(device=None):

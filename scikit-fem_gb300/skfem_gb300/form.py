@@ -429,15 +429,18 @@ class _PatternEntry:
 
 _SIDE = {}
 _COPY = {}
-HOST_CHUNKS = 8     # row ranges whose device->host copies overlap the segmented sum
-UPLOAD_CHUNKS = 4   # cell ranges whose coefficient uploads overlap the local kernel
+HOST_CHUNKS = 16    # row ranges whose device->host copies overlap the segmented sum
+UPLOAD_CHUNKS = 8   # cell ranges whose coefficient uploads overlap the local kernel
 
 
 def _copy_stream(device):
-    """A per-device stream for host->device coefficient uploads."""
+    """A per-device stream for host->device coefficient uploads, at the
+    highest priority: its kernels (host-row gathers) take SMs ahead of the
+    local kernels that wait for them."""
     s = _COPY.get(device)
     if s is None:
-        s = _COPY[device] = torch.cuda.Stream(device=device)
+        hi = torch.cuda.Stream.priority_range()[1]
+        s = _COPY[device] = torch.cuda.Stream(device=device, priority=hi)
     return s
 
 
@@ -652,9 +655,14 @@ class BilinearForm(Form):
         """Channel kernels, results copied to pinned host memory; None when
         a per-point coefficient varies inside a cell.
 
-        Strided host coefficients are uploaded in UPLOAD_CHUNKS cell ranges
-        on a copy stream, each range's local kernel waiting only for its
-        own rows, so the upload overlaps the FP64-bound local kernel."""
+        One native call queues the pipeline: the cells in order of their
+        smallest DOF, in UPLOAD_CHUNKS chunks; per chunk the strided host
+        coefficients' rows are read from host memory by a kernel on a copy
+        stream, the chunk's local kernel follows, and the rows it completes
+        are summed and copied back behind their sum -- the upload, the
+        FP64-bound local kernel and the copy of the values overlap.  Where
+        kernels cannot read pageable host memory the coefficients are
+        uploaded first."""
         main = torch.cuda.current_stream()
         uploaded = False
         for attempt in range(2):
@@ -682,29 +690,29 @@ class BilinearForm(Form):
             entry.status.zero_()
             lib = N.lib()
             ne = ubasis.nelems
+            nch = UPLOAD_CHUNKS if ne >= UPLOAD_CHUNKS * 4096 else 1
+            rows, nrows = None, 0
             if coeffs.strided and not uploaded:
-                up = _copy_stream(ubasis.device)
-                up.wait_stream(main)
-                nch = UPLOAD_CHUNKS if ne >= UPLOAD_CHUNKS * 4096 else 1
-                for c in range(nch):
-                    a, b = ne * c // nch, ne * (c + 1) // nch
-                    coeffs.upload(a, b, up)
-                    ev = torch.cuda.Event()
-                    ev.record(up)
-                    main.wait_event(ev)
-                    N.check(lib.fem_assemble_local(
-                        N.byref(ubasis.c_mesh), N.byref(ubasis.c_basis), N.byref(c_form),
-                        entry.pat.handle, N.ptr(entry.staging), N.ptr(entry.status), a, b, stream))
+                if entry.nnz and N.host_memory_access():
+                    fields = [(coeffs.strided_host[k], t) for k, t in coeffs.strided.items()]
+                    rows = (N.FemHostRows * len(fields))(*[
+                        N.FemHostRows(h.ctypes.data, t.data_ptr(), h.shape[1] if h.ndim > 1 else 0)
+                        for h, t in fields])
+                    nrows = len(fields)
+                else:
+                    coeffs.upload()
                 uploaded = True
+            if entry.nnz:
+                up = _copy_stream(ubasis.device)
+                N.check(lib.fem_assemble_to_host_pipelined(
+                    N.byref(ubasis.c_mesh), N.byref(ubasis.c_basis), N.byref(c_form),
+                    entry.pat.handle, N.ptr(entry.staging), N.ptr(vals),
+                    ctypes.c_void_p(data.data_ptr()), N.ptr(entry.status), rows, nrows, nch,
+                    stream, N.stream_ptr(up), N.stream_ptr(side)))
             else:
                 N.check(lib.fem_assemble_local(
                     N.byref(ubasis.c_mesh), N.byref(ubasis.c_basis), N.byref(c_form),
                     entry.pat.handle, N.ptr(entry.staging), N.ptr(entry.status), 0, ne, stream))
-            if entry.nnz:
-                # values stream to the host range by range behind the sum
-                N.check(lib.fem_csr_sum_to_host(
-                    entry.pat.handle, N.ptr(entry.staging), N.ptr(vals),
-                    ctypes.c_void_p(data.data_ptr()), HOST_CHUNKS, stream, N.stream_ptr(side)))
             st_h = torch.empty(1, dtype=torch.int32, pin_memory=True)
             st_h.copy_(entry.status, non_blocking=True)
             main.synchronize()
