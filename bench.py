@@ -38,9 +38,9 @@ UNIT = "elements/s"
 
 # algorithmic bytes per element of a steady-state TetP1 assembly
 # (element ids 16 B + coefficient 8 B) + coordinates + CSR values, see the design doc
-# DRAM bytes per cell of one steady-state TetP1 step (local kernel 120.2 B +
-# segmented sum 193.8 B), from the ncu capture on the 61^3-node cube
-TRAFFIC_B_PER_CELL = 120.2 + 193.8
+# DRAM bytes per cell of one steady-state TetP1 step (local kernel 110.2 B +
+# segmented sum 193.9 B), from the ncu capture on the 61^3-node cube
+TRAFFIC_B_PER_CELL = 110.2 + 193.9
 
 
 def max_over_ranks(ms, dist=None, device="cpu"):
@@ -246,7 +246,9 @@ def gpu_arm(args):
     nel = m.nelements
     B = algorithmic_bytes(nel, m.p.shape[1], nnz)
     achieved = B / (ms * 1e-3) / 1e9
-    flops_per_el = 102.0  # FP64 ops of the TetP1 local kernel, counted in the design doc
+    # FP64 work of the TetP1 local kernel per cell, from its ncu instruction
+    # counts: 18 DADD + 21 DMUL + 38 DFMA (2 FLOP each)
+    flops_per_el = 115.0
     fp64_achieved = nel * flops_per_el / (t_local * 1e-3) / 1e9
     res = {
         "metric": METRIC, "value": replica_value(nel, world, ms), "unit": UNIT, "n_gpus": world,
