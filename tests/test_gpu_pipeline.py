@@ -67,3 +67,18 @@ def test_host_pipeline_varying_rows_fall_back_to_generic():
     Kg = k_lap_mass.assemble_torch(b, k=torch.from_numpy(kq).cuda())
     np.testing.assert_array_equal(K.indices, Kg.col_indices().cpu().numpy())
     np.testing.assert_array_equal(K.data, Kg.values().cpu().numpy())
+
+
+def test_host_pipeline_vector_elasticity():
+    """Vector TetP2 linear elasticity (no coefficient fields: the pipeline
+    runs with no host rows) on 34,992 cells, eight chunks, against the
+    device path."""
+    from skfem_gb300.models.elasticity import linear_elasticity
+    m = F.MeshTet.init_tensor(*(np.linspace(0, 1, 19),) * 3)
+    b = F.Basis(m, F.ElementVector(F.ElementTetP2()))
+    form = linear_elasticity(1.0, 0.5)
+    Kd = form.assemble_torch(b)
+    Kh = form.assemble(b)
+    np.testing.assert_array_equal(Kh.indptr, Kd.crow_indices().cpu().numpy())
+    np.testing.assert_array_equal(Kh.indices, Kd.col_indices().cpu().numpy())
+    np.testing.assert_array_equal(Kh.data, Kd.values().cpu().numpy())
