@@ -415,3 +415,43 @@ def test_poisson_solve_as_users_write_it():
     u = np.zeros(b.N)
     u[I.cpu().numpy()] = spla.spsolve(Kh.tocsc(), fI.cpu().numpy())
     np.testing.assert_allclose(u, g["u"], rtol=0, atol=1e-12)
+
+
+def test_device_csr_feeds_a_device_solver():
+    """The device CSR goes to a solver without a host copy: condensed on the
+    device, handed over by DLPack (what CuPy / cuDSS-style consumers take)
+    and solved by conjugate gradients on the GPU; the solution equals the
+    reference's own solve."""
+    from torch.utils.dlpack import from_dlpack, to_dlpack
+    from skfem_gb300.utils import condense
+    g = golden("poisson_tri_p2")
+    m = F.MeshTri.init_tensor(np.linspace(0, 1, 33), np.linspace(0, 1, 33))
+    b = F.Basis(m, F.ElementTriP2())
+    A = laplace.assemble_torch(b)
+    f = unit_load.assemble_torch(b)
+    AII, fI, x, I = condense(A, f, D=b.get_dofs())
+    crow, col, val = AII.crow_indices(), AII.col_indices(), AII.values()
+    assert crow.dtype == torch.int32 and col.dtype == torch.int32 and val.dtype == torch.float64
+    assert crow.is_cuda and col.is_cuda and val.is_cuda
+    # the consumer's view: the same device arrays, no copy
+    crow2, col2, val2 = (from_dlpack(to_dlpack(t)) for t in (crow, col, val))
+    assert (crow2.data_ptr(), col2.data_ptr(), val2.data_ptr()) == \
+        (crow.data_ptr(), col.data_ptr(), val.data_ptr())
+    K = torch.sparse_csr_tensor(crow2, col2, val2, size=AII.shape)
+    u = torch.zeros_like(fI)
+    r = fI.clone()
+    p = r.clone()
+    rr = torch.dot(r, r)
+    for _ in range(2000):
+        Kp = torch.mv(K, p)
+        alpha = rr / torch.dot(p, Kp)
+        u += alpha * p
+        r -= alpha * Kp
+        rr_new = torch.dot(r, r)
+        if float(rr_new.sqrt()) <= 1e-14 * float(fI.norm()):
+            break
+        p = r + (rr_new / rr) * p
+        rr = rr_new
+    full = np.zeros(b.N)
+    full[I.cpu().numpy()] = u.cpu().numpy()
+    np.testing.assert_allclose(full, g["u"], rtol=0, atol=1e-11)
