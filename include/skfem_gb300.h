@@ -235,7 +235,13 @@ int fem_pattern_build(const FemMesh* mesh, const FemBasis* basis, const FemBilin
                       const FemProgram* program, FemPattern** out, fem_stream_t stream);
 
 /* Sizes: nnz of the CSR pattern, number of rows (N), and the bytes of the
- * local-matrix staging buffer fem_assemble needs. */
+ * local-matrix staging buffer fem_assemble needs.  The staging holds the
+ * local matrices in the pattern's layout: full for scalar bases; for vector
+ * bases (symmetric channel forms) only the dim x dim blocks on and above
+ * the block diagonal are written, and the sums of fem_assemble,
+ * fem_csr_sum_to_host and fem_assemble_to_host_pipelined read the others at
+ * their transposed positions.  fem_local_matrices always writes full
+ * matrices, and fem_csr_sum takes full matrices. */
 int fem_pattern_info(const FemPattern* pat, int64_t* nnz, int64_t* nrows, int64_t* staging_bytes);
 
 /* Copy the CSR structure out: indptr (nrows+1), indices (nnz), both int32. */
@@ -289,9 +295,9 @@ int fem_assemble_to_host(const FemMesh* mesh, const FemBasis* basis, const FemBi
 
 /* The two halves of fem_assemble_to_host, for callers that pipeline the
  * coefficients' upload with the local kernel: local matrices of the cells
- * [cell_begin, cell_end) into staging (with the coefficient and
- * stale-pattern checks of fem_assemble), then the row-range sum streamed to
- * host_values. */
+ * [cell_begin, cell_end) into staging in the pattern's layout (with the
+ * coefficient and stale-pattern checks of fem_assemble), then the
+ * row-range sum streamed to host_values. */
 int fem_assemble_local(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
                        const FemPattern* pat, double* staging, int32_t* status, int64_t cell_begin,
                        int64_t cell_end, fem_stream_t stream);

@@ -13,10 +13,11 @@ int local_matrices(const FemMesh&, const FemBasis&, const FemBilinear&, double*,
                    cudaStream_t);
 // cells [ebeg, eend) only (eend < 0: to the last cell)
 // cells [ebeg, eend) only (eend < 0: to the last cell); with a cell list,
-// the cells cells[ebeg .. eend-1]
+// the cells cells[ebeg .. eend-1]; upper: vector bases write only the
+// blocks on and above the block diagonal (Pattern::staging_sym)
 int local_matrices_checked(const FemMesh&, const FemBasis&, const FemBilinear&, double*,
                            const uint8_t*, int32_t*, cudaStream_t, int64_t ebeg = 0,
-                           int64_t eend = -1, const int32_t* cells = nullptr);
+                           int64_t eend = -1, const int32_t* cells = nullptr, int upper = 0);
 int local_vectors(const FemMesh&, const FemBasis&, const FemLinear&, double*, int32_t*,
                   cudaStream_t);
 }  // namespace fem_fast
@@ -308,6 +309,9 @@ int fem_pattern_build(const FemMesh* mesh, const FemBasis* basis, const FemBilin
     if (!rc && program) rc = fem::faithful_mask(*mesh, *basis, *program, program->nq, local, dstatus, st);
     if (!rc) rc = read_status(dstatus, st);
     if (!rc) rc = fem::build_csr(basis->element_dofs, nb, basis->ndofs, local, &H->P, st);
+    // the vector channel forms are symmetric: their local kernels write the
+    // blocks on and above the block diagonal only, the sum mirrors the rest
+    if (!rc && basis->vector) H->P.staging_sym = mesh->dim;
     if (!rc) rc = host_row_pointer(H, st);
     if (!rc && mesh->nelems > 0) {
       cudaError_t e2 = cudaMallocAsync(&H->coef_bits, mesh->nelems, st);
@@ -383,11 +387,12 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
   // the local kernel also compares each element's coefficient zero bits
   // with the pattern's (FEM_ERR_STALE_PATTERN)
   rc = fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
-                                        status ? pat->coef_bits : nullptr, status, st);
+                                        status ? pat->coef_bits : nullptr, status, st, 0, -1,
+                                        nullptr, pat->P.staging_sym > 0);
   if (rc) return rc;
   fem::Pattern P = pat->P;
   P.sum_unroll = fem::tuning_for(basis->family).sum_unroll;
-  return fem::csr_sum(P, staging, csr_values, st);
+  return fem::csr_sum(P, staging, csr_values, st, 0, -1, nullptr, P.staging_sym);
 }
 
 int fem_assemble_local(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
@@ -411,7 +416,8 @@ int fem_assemble_local(const FemMesh* mesh, const FemBasis* basis, const FemBili
   if (cell_end == cell_begin) return 0;
   return fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
                                           status ? pat->coef_bits : nullptr, status,
-                                          (cudaStream_t)stream, cell_begin, cell_end);
+                                          (cudaStream_t)stream, cell_begin, cell_end, nullptr,
+                                          pat->P.staging_sym > 0);
 }
 
 namespace {
@@ -438,7 +444,7 @@ std::vector<int64_t> row_ranges(const std::vector<int32_t>& ip, int64_t nrows, i
 int sum_rows_to_host(const fem::Pattern& P, const std::vector<int32_t>& ip, const double* staging,
                      double* csr_values, double* host_values, int64_t row0, int64_t row1,
                      cudaStream_t st, cudaStream_t cs) {
-  int rc = fem::csr_sum(P, staging, csr_values, st, row0, row1);
+  int rc = fem::csr_sum(P, staging, csr_values, st, row0, row1, nullptr, P.staging_sym);
   if (rc) return rc;
   const int64_t a = ip[row0], b = ip[row1];
   if (b > a) {
@@ -783,7 +789,7 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
     if (cb[c + 1] > cb[c]) {
       rc = fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
                                             status ? pat->coef_bits : nullptr, status, st,
-                                            cb[c], cb[c + 1], cells);
+                                            cb[c], cb[c + 1], cells, pat->P.staging_sym > 0);
       if (rc) {
         release();
         return rc;

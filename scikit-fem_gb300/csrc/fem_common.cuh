@@ -52,6 +52,12 @@ struct Pattern {
   uint16_t* slot = nullptr;     // ninc * nbfun_u
   bool has_matrix = false;
   int sum_unroll = 8;    // set from the family's tuning when the pattern is built
+  // Layout of the staging that fem_assemble_local writes for this pattern:
+  // 0 full local matrices; D > 0 (vector bases of dimension D) the local
+  // matrices' D x D blocks on and above the block diagonal only -- the
+  // sum reads the others at their transposed positions (the vector
+  // channel forms are symmetric).
+  int staging_sym = 0;
 };
 
 // ---------------------------------------------------------------- helpers
@@ -147,9 +153,11 @@ Tuning tuning_for(int family);
 
 // Fixed-order segmented sum of local matrices into CSR values, rows
 // [row0, row1) (row1 < 0: to the last row); check_status non-null: also
-// verify the exact-zero structure (FEM_ERR_STALE_PATTERN).
+// verify the exact-zero structure (FEM_ERR_STALE_PATTERN).  sym > 0: the
+// local matrices hold their sym x sym blocks on and above the block
+// diagonal only (Pattern::staging_sym), square patterns.
 int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st,
-            int64_t row0 = 0, int64_t row1 = -1, int32_t* check_status = nullptr);
+            int64_t row0 = 0, int64_t row1 = -1, int32_t* check_status = nullptr, int sym = 0);
 
 int basis_nb_scalar(int family);
 int basis_dim(int family);

@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBiline
 // s0 = 1/(d! |det|), E_qp = E_pq^T; plus mass delta_ab sm MM[i][j].
 // The element's 3 (or 2) rows of one scalar node are produced at a time
 // and streamed out through shared memory.
-template <int D, int ORDER>
+template <int D, int ORDER, bool UPPER>
 __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBilinear f,
                                                             double* __restrict__ out,
                                                             const uint8_t* __restrict__ ref_bits,
@@ -319,6 +319,7 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
       double* row = rows + tid * (RB + 1);
       static_for<NS>([&](auto jc) {
         constexpr int j = decltype(jc)::value;
+        if constexpr (!UPPER || j >= i) {
         double blk[D][D];
 #pragma unroll
         for (int a = 0; a < D; ++a)
@@ -356,7 +357,7 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
 #undef T
         // mass: delta_ab sm MM[i][j] (elasticity has none: uniform branch)
         double mij = 0.0;
-        if (sm != 0.0) {
+        if (!fem::zero_bits(sm)) {
           if constexpr (D == 3 && ORDER == 2) mij = c_tet2_mm[i][j];
           else if constexpr (D == 2 && ORDER == 2) mij = c_tri2_mm[i][j];
           else if constexpr (D == 3) mij = c_tet1_mm[i][j];
@@ -370,14 +371,20 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
             if (a == b) v = v + sm * mij;
             row[a * NB + j * D + b] = v;
           }
+        }
       });
     }
-    // stream rows (i*D .. i*D+D-1) of every element of the block
+    // stream rows (i*D .. i*D+D-1) of every element of the block (UPPER:
+    // their columns from i*D on, the blocks on and above the diagonal)
     __syncthreads();
     const int64_t nb = ((eend - e0) < (int64_t)BS ? (eend - e0) : (int64_t)BS);
-    for (int64_t g = threadIdx.x; g < nb * RB; g += blockDim.x) {
-      const int el = (int)(g / RB);
-      const int k = (int)(g - (int64_t)el * RB);
+    constexpr int W = UPPER ? NB - i * D : NB;  // columns streamed per row
+    constexpr int C0 = NB - W;                  // first column streamed
+    for (int64_t g = threadIdx.x; g < nb * (D * W); g += blockDim.x) {
+      const int el = (int)(g / (D * W));
+      const int kk = (int)(g - (int64_t)el * (D * W));
+      const int a = kk / W;
+      const int k = a * NB + C0 + (kk - a * W);
       out[cell_at(cells, e0 + el) * (int64_t)(NB * NB) + (int64_t)i * RB + k] =
           rows[el * (RB + 1) + k];
     }
@@ -696,7 +703,7 @@ static int launch_scalar_tuned(const FemMesh& m, const FemBilinear& f, double* o
 
 int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinear& f, double* out,
                            const uint8_t* ref_bits, int32_t* status, cudaStream_t st,
-                           int64_t ebeg, int64_t eend, const int32_t* cells) {
+                           int64_t ebeg, int64_t eend, const int32_t* cells, int upper) {
   if (eend < 0 || eend > m.nelems) eend = m.nelems;
   if (ebeg < 0) ebeg = 0;
   if (eend <= ebeg) return 0;
@@ -729,8 +736,13 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
     constexpr int NS = SimplexTraits<D, O>::NB, NB = NS * D;                          \
     constexpr int RB = D * NB;                                                         \
     const size_t sm = (size_t)64 * (RB + 1) * sizeof(double);                          \
-    if ((rc = set_smem(simplex_vector_kernel<D, O>, sm))) return rc;                   \
-    simplex_vector_kernel<D, O><<<(unsigned)vgrid, 64, sm, st>>>(m, f, out, ref_bits, status, cells, ebeg, eend); \
+    if (upper) {                                                                       \
+      if ((rc = set_smem(simplex_vector_kernel<D, O, true>, sm))) return rc;           \
+      simplex_vector_kernel<D, O, true><<<(unsigned)vgrid, 64, sm, st>>>(m, f, out, ref_bits, status, cells, ebeg, eend); \
+    } else {                                                                           \
+      if ((rc = set_smem(simplex_vector_kernel<D, O, false>, sm))) return rc;          \
+      simplex_vector_kernel<D, O, false><<<(unsigned)vgrid, 64, sm, st>>>(m, f, out, ref_bits, status, cells, ebeg, eend); \
+    }                                                                                  \
     break;                                                                             \
   }
       case FEM_TRI_P1: LAUNCH_V(2, 1)
@@ -750,7 +762,7 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
 
 int local_matrices(const FemMesh& m, const FemBasis& b, const FemBilinear& f, double* out,
                    int32_t* status, cudaStream_t st) {
-  return local_matrices_checked(m, b, f, out, nullptr, status, st, 0, -1, nullptr);
+  return local_matrices_checked(m, b, f, out, nullptr, status, st, 0, -1, nullptr, 0);
 }
 
 int local_vectors(const FemMesh& m, const FemBasis& b, const FemLinear& f, double* out,

@@ -225,12 +225,17 @@ __global__ void row_fill_kernel(const int32_t* __restrict__ inc_ptr, const int32
 // CHECK: also verify the zero structure (exact local masks, generic path):
 // a nonzero local entry without a slot, or a CSR entry that no nonzero
 // local entry reaches, sets FEM_ERR_STALE_PATTERN in *status.
-template <int G, int U, bool CHECK>
+// SYM > 0: the local matrices hold their SYM x SYM blocks on and above the
+// block diagonal only; entry (i, j) of a block below it is read at (j, i).
+// The cell of an incidence code is code / nu (square patterns), taken as
+// the high word of code * div_magic (div_magic = ceil(2^64 / nu), exact
+// for codes below 2^32).
+template <int G, int U, bool CHECK, int SYM = 0>
 __global__ void csr_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                                const uint16_t* __restrict__ slot, const int32_t* __restrict__ indptr,
                                const double* __restrict__ local, int64_t row0, int64_t nrows,
                                int nu, int stride, double* __restrict__ vals,
-                               int32_t* __restrict__ status) {
+                               int32_t* __restrict__ status, unsigned long long div_magic = 0) {
   extern __shared__ double acc_smem[];
   constexpr int RPW = 32 / G;  // rows per warp
   const int lane = threadIdx.x & 31;
@@ -272,7 +277,13 @@ __global__ void csr_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_
         if (q < len && j < nu) {
           const int64_t code = __ldg(inc + b + q);
           s[u] = __ldg(slot + ((int64_t)b + q) * nu + j);
-          v[u] = __ldg(local + code * nu + j);
+          int64_t at = code * nu + j;
+          if constexpr (SYM > 0) {
+            const int64_t e = (int64_t)__umul64hi((unsigned long long)code, div_magic);
+            const int il = (int)(code - e * nu);
+            if (j / SYM < il / SYM) at = (e * nu + j) * nu + il;
+          }
+          v[u] = __ldg(local + at);
         }
       }
 #pragma unroll
@@ -512,7 +523,7 @@ int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, 
 }
 
 int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st, int64_t row0,
-            int64_t row1, int32_t* check_status) {
+            int64_t row1, int32_t* check_status, int sym) {
   if (!P.has_matrix) {
     set_error(FEM_ERR_ARGUMENT, "pattern has no CSR structure (built without local matrices)");
     return FEM_ERR_ARGUMENT;
@@ -536,7 +547,7 @@ int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(row1 - row0, rows_per_block),
                                                                 (int64_t)num_sms() * 64));
     kern<<<grid, threads, smem, st>>>(P.inc_ptr, P.inc, P.slot, P.indptr, local, row0, row1, nu,
-                                      stride, vals, check_status);
+                                      stride, vals, check_status, 0ull);
     return 0;
   };
   const int U = P.sum_unroll;
@@ -552,7 +563,42 @@ int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st
     set_error(FEM_ERR_UNSUPPORTED, "more than 32 local functions per cell (%d)", nu);
     return FEM_ERR_UNSUPPORTED;
   }
-  rc = check_status ? pick(std::true_type{}) : pick(std::false_type{});
+  if (sym > 0) {
+    // block-upper staging of vector channel kernels (no zero-structure check)
+    if (check_status || (sym != 2 && sym != 3) || P.nbfun_u != P.nbfun_v || nu % sym) {
+      set_error(FEM_ERR_ARGUMENT, "block-symmetric staging needs a square pattern, blocks of 2 or 3");
+      return FEM_ERR_ARGUMENT;
+    }
+    const int64_t ncodes = P.nelems * (int64_t)P.nbfun_v;
+    if (ncodes >= ((int64_t)1 << 32)) {
+      set_error(FEM_ERR_CAPACITY, "%lld incidence codes exceed 2^32", (long long)ncodes);
+      return FEM_ERR_CAPACITY;
+    }
+    const unsigned long long magic = ~0ull / (unsigned long long)nu + 1ull;
+    auto launch_sym = [&](auto kern, int G) -> int {
+      const int rpw = 32 / G;
+      const size_t smem = (size_t)warps * rpw * stride * sizeof(double);
+      if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return check_cuda(e, "csr_sum smem");
+      }
+      const int64_t rows_per_block = (int64_t)warps * rpw;
+      const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(row1 - row0, rows_per_block),
+                                                                  (int64_t)num_sms() * 64));
+      kern<<<grid, threads, smem, st>>>(P.inc_ptr, P.inc, P.slot, P.indptr, local, row0, row1, nu,
+                                        stride, vals, nullptr, magic);
+      return 0;
+    };
+#define FEM_SYM_PICK(S)                                                                        \
+    if (nu <= 8) rc = U >= 8 ? launch_sym(csr_sum_kernel<8, 8, false, S>, 8) : launch_sym(csr_sum_kernel<8, 4, false, S>, 8); \
+    else if (nu <= 16) rc = U >= 8 ? launch_sym(csr_sum_kernel<16, 8, false, S>, 16) : launch_sym(csr_sum_kernel<16, 4, false, S>, 16); \
+    else rc = U >= 8 ? launch_sym(csr_sum_kernel<32, 8, false, S>, 32) : launch_sym(csr_sum_kernel<32, 4, false, S>, 32);
+    if (sym == 2) { FEM_SYM_PICK(2) }
+    else { FEM_SYM_PICK(3) }
+#undef FEM_SYM_PICK
+  } else {
+    rc = check_status ? pick(std::true_type{}) : pick(std::false_type{});
+  }
   if (rc) return rc;
   FEM_LAUNCH_CHECK("csr_sum_kernel");
   return 0;
