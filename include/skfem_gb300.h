@@ -234,6 +234,22 @@ int fem_local_vectors(const FemMesh* mesh, const FemBasis* basis, const FemLinea
 int fem_pattern_build(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
                       const FemProgram* program, FemPattern** out, fem_stream_t stream);
 
+/*
+ * Per-cell geometry cache (CellBasis keeps its mapping the same way,
+ * cell_basis.py:101-105): for scalar TriP1/P2 and TetP1/P2 bases, the
+ * coefficient-free part of the local kernel -- the Gram matrix of the
+ * barycentric gradients scaled by 1/(d! |det DF|), and |det DF|: 7 (2D) or
+ * 11 (3D) doubles per cell -- computed from mesh->p and kept in the pattern.
+ * fem_assemble, fem_assemble_local and fem_assemble_to_host_pipelined then
+ * read it instead of the coordinates whenever the mesh they are given has
+ * the same p pointer; after changing the coordinates in place, call this
+ * again (or fem_pattern_drop_geometry).  Other families: no cache, no-op.
+ * Stream-ordered; not concurrently with assembly calls on the pattern.
+ */
+int fem_pattern_cache_geometry(FemPattern* pat, const FemMesh* mesh, const FemBasis* basis,
+                               fem_stream_t stream);
+void fem_pattern_drop_geometry(FemPattern* pat);
+
 /* Sizes: nnz of the CSR pattern, number of rows (N), and the bytes of the
  * local-matrix staging buffer fem_assemble needs.  The staging holds the
  * local matrices in the pattern's layout: full for scalar bases; for vector

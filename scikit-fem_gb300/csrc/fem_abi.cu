@@ -17,7 +17,12 @@ int local_matrices(const FemMesh&, const FemBasis&, const FemBilinear&, double*,
 // blocks on and above the block diagonal (Pattern::staging_sym)
 int local_matrices_checked(const FemMesh&, const FemBasis&, const FemBilinear&, double*,
                            const uint8_t*, int32_t*, cudaStream_t, int64_t ebeg = 0,
-                           int64_t eend = -1, const int32_t* cells = nullptr, int upper = 0);
+                           int64_t eend = -1, const int32_t* cells = nullptr, int upper = 0,
+                           const double* geo = nullptr);
+// per-cell geometry cache of the scalar simplex kernels: doubles per cell
+// (0: none for this family) and the kernel that fills it
+int geometry_count(const FemMesh&, const FemBasis&);
+int geometry_cache(const FemMesh&, const FemBasis&, double* geo, cudaStream_t);
 int local_vectors(const FemMesh&, const FemBasis&, const FemLinear&, double*, int32_t*,
                   cudaStream_t);
 }  // namespace fem_fast
@@ -123,7 +128,20 @@ struct FemPattern {
   mutable int32_t* plan_cells = nullptr;
   mutable std::vector<int64_t> plan_bounds;   // plan_nchunks + 1 positions
   mutable std::vector<int64_t> plan_rows;     // plan_nchunks: rows [0, plan_rows[c]) final
+  // Per-cell geometry of the scalar simplex kernels (fem_pattern_cache_geometry),
+  // computed from the coordinates at geo_p; used only for meshes whose p is
+  // that same pointer.
+  double* geo = nullptr;
+  const double* geo_p = nullptr;
 };
+
+namespace {
+// The pattern's geometry cache when it was computed from this mesh's
+// coordinate array, else null (the kernels then compute the geometry).
+const double* cached_geometry(const FemPattern* pat, const FemMesh* mesh) {
+  return (pat->geo && pat->geo_p == mesh->p) ? pat->geo : nullptr;
+}
+}  // namespace
 
 using fem::set_error;
 
@@ -367,7 +385,40 @@ void fem_pattern_destroy(FemPattern* pat) {
   fem::free_pattern(new fem::Pattern(pat->P));
   cudaFree(pat->coef_bits);
   cudaFree(pat->plan_cells);
+  cudaFree(pat->geo);
   delete pat;
+}
+
+int fem_pattern_cache_geometry(FemPattern* pat, const FemMesh* mesh, const FemBasis* basis,
+                               fem_stream_t stream) {
+  int rc = validate(mesh, basis);
+  if (rc) return rc;
+  if (!pat || pat->P.nelems != mesh->nelems || pat->P.nbfun_v != basis->nbfun) {
+    set_error(FEM_ERR_ARGUMENT, "pattern does not belong to this mesh / basis");
+    return FEM_ERR_ARGUMENT;
+  }
+  const int ng = fem_fast::geometry_count(*mesh, *basis);
+  if (ng == 0) return 0;  // families without a cache compute their geometry per call
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!pat->geo) {
+    cudaError_t e = cudaMalloc(&pat->geo, std::max<int64_t>(1, mesh->nelems) * ng * sizeof(double));
+    if (e != cudaSuccess) {
+      pat->geo = nullptr;
+      return fem::check_cuda(e, "cudaMalloc(geometry cache)");
+    }
+  }
+  pat->geo_p = nullptr;  // not valid until the kernel below has been queued
+  rc = fem_fast::geometry_cache(*mesh, *basis, pat->geo, st);
+  if (rc) return rc;
+  pat->geo_p = mesh->p;
+  return 0;
+}
+
+void fem_pattern_drop_geometry(FemPattern* pat) {
+  if (!pat) return;
+  cudaFree(pat->geo);
+  pat->geo = nullptr;
+  pat->geo_p = nullptr;
 }
 
 int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
@@ -388,7 +439,8 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
   // with the pattern's (FEM_ERR_STALE_PATTERN)
   rc = fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
                                         status ? pat->coef_bits : nullptr, status, st, 0, -1,
-                                        nullptr, pat->P.staging_sym > 0);
+                                        nullptr, pat->P.staging_sym > 0,
+                                        cached_geometry(pat, mesh));
   if (rc) return rc;
   fem::Pattern P = pat->P;
   P.sum_unroll = fem::tuning_for(basis->family).sum_unroll;
@@ -417,7 +469,7 @@ int fem_assemble_local(const FemMesh* mesh, const FemBasis* basis, const FemBili
   return fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
                                           status ? pat->coef_bits : nullptr, status,
                                           (cudaStream_t)stream, cell_begin, cell_end, nullptr,
-                                          pat->P.staging_sym > 0);
+                                          pat->P.staging_sym > 0, cached_geometry(pat, mesh));
 }
 
 namespace {
@@ -789,7 +841,8 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
     if (cb[c + 1] > cb[c]) {
       rc = fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
                                             status ? pat->coef_bits : nullptr, status, st,
-                                            cb[c], cb[c + 1], cells, pat->P.staging_sym > 0);
+                                            cb[c], cb[c + 1], cells, pat->P.staging_sym > 0,
+                                            cached_geometry(pat, mesh));
       if (rc) {
         release();
         return rc;

@@ -190,13 +190,72 @@ __device__ __forceinline__ int ref_byte(const uint8_t* __restrict__ ref, int64_t
   return ref ? (int)__ldg(ref + e) : -1;
 }
 
-template <int D, int ORDER, int BS>
+// The coefficient-free geometry of a simplex: the Gram matrix of
+// c_a = det(A) grad(lambda_a) (entries a <= b; row 0 from c_0 = -sum c_m),
+// |det A| and its reciprocal.  The scalar kernels compute it per cell, or
+// read it from a per-cell cache (simplex_geometry_cache_kernel): the Gram
+// entries already scaled by 1/(d! |det|), and |det|.
+template <int D>
+constexpr int kGramCount = (D + 1) * (D + 2) / 2;
+template <int D>
+constexpr int kGeoCount = kGramCount<D> + 1;  // scaled Gram entries, |det|
+template <int D>
+constexpr double kInvFact = D == 2 ? 0.5 : 1.0 / 6.0;
+
+template <int D>
+__device__ __forceinline__ void simplex_gram(const FemMesh& m, int64_t e, double gram[D + 1][D + 1],
+                                             double& adet, double& rinv) {
+  Simplex<D> s;
+  simplex_geometry<D>(m, e, s);
+  adet = fem::abs_bits(s.det);
+  rinv = 1.0 / adet;
+#pragma unroll
+  for (int a = 1; a <= D; ++a)
+#pragma unroll
+    for (int b = a; b <= D; ++b) gram[a][b] = dotc<D>(s.c[a], s.c[b]);
+#pragma unroll
+  for (int b = 1; b <= D; ++b) {
+    double acc = (1 <= b ? gram[1][b] : gram[b][1]);
+#pragma unroll
+    for (int a = 2; a <= D; ++a) acc = acc + (a <= b ? gram[a][b] : gram[b][a]);
+    gram[0][b] = -acc;
+  }
+  {
+    double acc = gram[0][1];
+#pragma unroll
+    for (int b = 2; b <= D; ++b) acc = acc + gram[0][b];
+    gram[0][0] = -acc;
+  }
+}
+
+// geo[k * nelems + e]: the Gram entries (a <= b, row-major) times
+// 1/(d! |det|) -- the stiffness per unit coefficient -- then |det|
+template <int D>
+__global__ void simplex_geometry_cache_kernel(FemMesh m, double* __restrict__ geo) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.nelems) return;
+  double gram[D + 1][D + 1], adet, rinv;
+  simplex_gram<D>(m, e, gram, adet, rinv);
+  const double s = rinv * kInvFact<D>;
+  int k = 0;
+#pragma unroll
+  for (int a = 0; a <= D; ++a)
+#pragma unroll
+    for (int b = a; b <= D; ++b) geo[(int64_t)(k++) * m.nelems + e] = gram[a][b] * s;
+  geo[(int64_t)k * m.nelems + e] = adet;
+}
+
+// CACHED: the geometry comes from geo (simplex_geometry_cache_kernel on the
+// same coordinates) instead of the mesh -- coefficient changes then cost
+// the ~14 FP64 operations per cell of the form alone.
+template <int D, int ORDER, int BS, bool CACHED>
 __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBilinear f,
                                                                 FemCoef kdiff,
                                                                 double* __restrict__ out,
                                                                 const uint8_t* __restrict__ ref_bits,
                                                                 int32_t* __restrict__ status,
                                                                 const int32_t* __restrict__ cells,
+                                                                const double* __restrict__ geo,
                                                                 int64_t ebeg, int64_t eend) {
   constexpr int NB = SimplexTraits<D, ORDER>::NB;
   constexpr int L = NB * NB;
@@ -210,38 +269,31 @@ __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBiline
   if (pos < eend) {
     const int64_t e = cell_at(cells, pos);
     const int rb = ref_byte(ref_bits, e);
-    Simplex<D> s;
-    simplex_geometry<D>(m, e, s);
-    const double adet = fem::abs_bits(s.det);
-    // stiffness scale kd / (d! |det|) (kdiff is f.diff with its scale
-    // multiplied by 1/d! on the host); mass scale km |det| (the 1/d! of the
-    // mass goes into the table constants, folded at compile time)
-    const double sd = coef_at(kdiff, e) * (1.0 / adet);
+    // stiffness scale sd times the Gram entries: kd / (d! |det|) (kdiff is
+    // f.diff with its scale multiplied by 1/d! on the host; the cache holds
+    // the Gram entries already scaled by 1/(d! |det|)); mass scale km |det|
+    // (the 1/d! of the mass goes into the table constants, folded at
+    // compile time)
+    double gram[D + 1][D + 1], adet, sd;
+    if constexpr (CACHED) {
+      int k = 0;
+#pragma unroll
+      for (int a = 0; a <= D; ++a)
+#pragma unroll
+        for (int b = a; b <= D; ++b) gram[a][b] = __ldg(geo + (int64_t)(k++) * m.nelems + e);
+      adet = __ldg(geo + (int64_t)k * m.nelems + e);
+      sd = coef_at(f.diff, e);
+    } else {
+      double rinv;
+      simplex_gram<D>(m, e, gram, adet, rinv);
+      sd = coef_at(kdiff, e) * rinv;
+    }
     const double sm = coef_at(f.mass, e) * adet;
-    // Gram of c_1..c_D, then row 0 from c_0 = -sum c_m
-    double gram[D + 1][D + 1];
-#pragma unroll
-    for (int a = 1; a <= D; ++a)
-#pragma unroll
-      for (int b = a; b <= D; ++b) gram[a][b] = dotc<D>(s.c[a], s.c[b]);
-#pragma unroll
-    for (int b = 1; b <= D; ++b) {
-      double acc = (1 <= b ? gram[1][b] : gram[b][1]);
-#pragma unroll
-      for (int a = 2; a <= D; ++a) acc = acc + (a <= b ? gram[a][b] : gram[b][a]);
-      gram[0][b] = -acc;
-    }
-    {
-      double acc = gram[0][1];
-#pragma unroll
-      for (int b = 2; b <= D; ++b) acc = acc + gram[0][b];
-      gram[0][0] = -acc;
-    }
     double* row = smem + threadIdx.x * (L + 1);
     double kst[NB][NB];
 #define G(a, b) ((a) <= (b) ? gram[a][b] : gram[b][a])
 #define KS(i, j, v) { kst[i][j] = (v); }
-#define KM(i, j, v) { constexpr double _m = (v) * INV_FACT; const double _v = sd * kst[i][j] + sm * _m; row[(i) * NB + (j)] = _v; row[(j) * NB + (i)] = _v; }
+#define KM(i, j, v) { constexpr double _m = (v) * INV_FACT; const double _v = __fma_rn(sd, kst[i][j], sm * _m); row[(i) * NB + (j)] = _v; row[(j) * NB + (i)] = _v; }
     if constexpr (D == 2 && ORDER == 1) { TRI1_STIFF(G, KS); TRI1_MASS(KM); }
     if constexpr (D == 2 && ORDER == 2) { TRI2_STIFF(G, KS); TRI2_MASS(KM); }
     if constexpr (D == 3 && ORDER == 1) { TET1_STIFF(G, KS); TET1_MASS(KM); }
@@ -674,36 +726,46 @@ static int set_smem(K kernel, size_t bytes) {
 template <int D, int O, int BS>
 static int launch_scalar(const FemMesh& m, const FemBilinear& f, double* out,
                          const uint8_t* ref_bits, int32_t* status, int persistent,
-                         cudaStream_t st, int64_t ebeg, int64_t eend, const int32_t* cells) {
+                         cudaStream_t st, int64_t ebeg, int64_t eend, const int32_t* cells,
+                         const double* geo) {
   constexpr int NB = SimplexTraits<D, O>::NB;
   const size_t sm = (size_t)BS * (NB * NB + 1) * sizeof(double);
-  int rc = set_smem(simplex_scalar_kernel<D, O, BS>, sm);
-  if (rc) return rc;
   int64_t grid = fem::ceil_div(eend - ebeg, BS);
   if (persistent > 0) grid = std::min<int64_t>(grid, (int64_t)persistent * fem::num_sms());
   FemCoef kdiff = f.diff;
   kdiff.scale = f.diff.scale * (1.0 / SimplexTraits<D, O>::FACT);
-  simplex_scalar_kernel<D, O, BS><<<(unsigned)grid, BS, sm, st>>>(m, f, kdiff, out, ref_bits,
-                                                                  status, cells, ebeg, eend);
+  if (geo) {
+    int rc = set_smem(simplex_scalar_kernel<D, O, BS, true>, sm);
+    if (rc) return rc;
+    simplex_scalar_kernel<D, O, BS, true><<<(unsigned)grid, BS, sm, st>>>(
+        m, f, kdiff, out, ref_bits, status, cells, geo, ebeg, eend);
+  } else {
+    int rc = set_smem(simplex_scalar_kernel<D, O, BS, false>, sm);
+    if (rc) return rc;
+    simplex_scalar_kernel<D, O, BS, false><<<(unsigned)grid, BS, sm, st>>>(
+        m, f, kdiff, out, ref_bits, status, cells, nullptr, ebeg, eend);
+  }
   return 0;
 }
 
 template <int D, int O>
 static int launch_scalar_tuned(const FemMesh& m, const FemBilinear& f, double* out,
                                const uint8_t* ref_bits, int32_t* status, cudaStream_t st,
-                               int64_t ebeg, int64_t eend, const int32_t* cells) {
+                               int64_t ebeg, int64_t eend, const int32_t* cells,
+                               const double* geo) {
   const fem::Tuning t = fem::tuning_for(D == 2 ? (O == 1 ? FEM_TRI_P1 : FEM_TRI_P2)
                                                : (O == 1 ? FEM_TET_P1 : FEM_TET_P2));
   switch (t.local_block) {
-    case 64: return launch_scalar<D, O, 64>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend, cells);
-    case 256: return launch_scalar<D, O, 256>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend, cells);
-    default: return launch_scalar<D, O, 128>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend, cells);
+    case 64: return launch_scalar<D, O, 64>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend, cells, geo);
+    case 256: return launch_scalar<D, O, 256>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend, cells, geo);
+    default: return launch_scalar<D, O, 128>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend, cells, geo);
   }
 }
 
 int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinear& f, double* out,
                            const uint8_t* ref_bits, int32_t* status, cudaStream_t st,
-                           int64_t ebeg, int64_t eend, const int32_t* cells, int upper) {
+                           int64_t ebeg, int64_t eend, const int32_t* cells, int upper,
+                           const double* geo) {
   if (eend < 0 || eend > m.nelems) eend = m.nelems;
   if (ebeg < 0) ebeg = 0;
   if (eend <= ebeg) return 0;
@@ -712,10 +774,10 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
   int rc = 0;
   if (!b.vector) {
     switch (fam) {
-      case FEM_TRI_P1: rc = launch_scalar_tuned<2, 1>(m, f, out, ref_bits, status, st, ebeg, eend, cells); break;
-      case FEM_TRI_P2: rc = launch_scalar_tuned<2, 2>(m, f, out, ref_bits, status, st, ebeg, eend, cells); break;
-      case FEM_TET_P1: rc = launch_scalar_tuned<3, 1>(m, f, out, ref_bits, status, st, ebeg, eend, cells); break;
-      case FEM_TET_P2: rc = launch_scalar_tuned<3, 2>(m, f, out, ref_bits, status, st, ebeg, eend, cells); break;
+      case FEM_TRI_P1: rc = launch_scalar_tuned<2, 1>(m, f, out, ref_bits, status, st, ebeg, eend, cells, geo); break;
+      case FEM_TRI_P2: rc = launch_scalar_tuned<2, 2>(m, f, out, ref_bits, status, st, ebeg, eend, cells, geo); break;
+      case FEM_TET_P1: rc = launch_scalar_tuned<3, 1>(m, f, out, ref_bits, status, st, ebeg, eend, cells, geo); break;
+      case FEM_TET_P2: rc = launch_scalar_tuned<3, 2>(m, f, out, ref_bits, status, st, ebeg, eend, cells, geo); break;
       case FEM_HEX_1: {
         const size_t sm = (size_t)kBlock * 65 * sizeof(double);
         if ((rc = set_smem(hex_scalar_kernel, sm))) return rc;
@@ -762,7 +824,27 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
 
 int local_matrices(const FemMesh& m, const FemBasis& b, const FemBilinear& f, double* out,
                    int32_t* status, cudaStream_t st) {
-  return local_matrices_checked(m, b, f, out, nullptr, status, st, 0, -1, nullptr, 0);
+  return local_matrices_checked(m, b, f, out, nullptr, status, st, 0, -1, nullptr, 0, nullptr);
+}
+
+// Doubles per cell of the geometry cache of the scalar simplex kernels (0:
+// the family has none).
+int geometry_count(const FemMesh& m, const FemBasis& b) {
+  if (b.vector) return 0;
+  switch (b.family) {
+    case FEM_TRI_P1: case FEM_TRI_P2: return m.dim == 2 ? kGeoCount<2> : 0;
+    case FEM_TET_P1: case FEM_TET_P2: return m.dim == 3 ? kGeoCount<3> : 0;
+    default: return 0;
+  }
+}
+
+int geometry_cache(const FemMesh& m, const FemBasis& b, double* geo, cudaStream_t st) {
+  if (!geometry_count(m, b) || m.nelems == 0) return 0;
+  const unsigned grid = (unsigned)fem::ceil_div(m.nelems, 128);
+  if (m.dim == 2) simplex_geometry_cache_kernel<2><<<grid, 128, 0, st>>>(m, geo);
+  else simplex_geometry_cache_kernel<3><<<grid, 128, 0, st>>>(m, geo);
+  FEM_LAUNCH_CHECK("simplex_geometry_cache_kernel");
+  return 0;
 }
 
 int local_vectors(const FemMesh& m, const FemBasis& b, const FemLinear& f, double* out,

@@ -123,6 +123,7 @@ class GraphedAssembly:
         lib = N.lib()
         b = self.basis
         s = N.stream_ptr()
+        self.entry.refresh_geometry(b, s)
         N.check(lib.fem_assemble(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(self.c_form),
                                  self.entry.pat.handle, N.ptr(self.entry.staging),
                                  N.ptr(self.values), N.ptr(self.status), s))

@@ -425,6 +425,26 @@ class _PatternEntry:
         else:
             self.staging = torch.empty(max(1, basis.nelems * basis.Nbfun), dtype=torch.float64,
                                        device=dev)
+        self.geo_key = None
+        if c_form is not None and local is None and ubasis is None:
+            self.refresh_geometry(basis, stream)
+
+    def refresh_geometry(self, basis, stream=None):
+        """The channel pattern's per-cell geometry cache (scalar simplex
+        bases; CellBasis keeps its mapping the same way), recomputed when
+        the basis's coordinates changed -- in place (the tensor's version
+        counter) or replaced (its pointer).  While the mesh points at other
+        coordinates (the adjoint's X) the kernels compute the geometry."""
+        p = basis.p_dev
+        if basis.c_mesh.p != p.data_ptr():
+            return
+        key = (p.data_ptr(), p._version)
+        if key == self.geo_key:
+            return
+        N.check(N.lib().fem_pattern_cache_geometry(
+            self.pat.handle, N.byref(basis.c_mesh), N.byref(basis.c_basis),
+            stream if stream is not None else N.stream_ptr()))
+        self.geo_key = key
 
 
 _SIDE = {}
@@ -514,6 +534,7 @@ class BilinearForm(Form):
             entry = _PatternEntry(ubasis, c_form, stream, prog)
             del keep
             ubasis._patterns[key] = entry
+        entry.refresh_geometry(ubasis, stream)
         vals = torch.empty(max(entry.nnz, 1), dtype=torch.float64, device=ubasis.device)[:entry.nnz]
         entry.status.zero_()
         N.check(N.lib().fem_assemble(N.byref(ubasis.c_mesh), N.byref(ubasis.c_basis),
@@ -678,6 +699,7 @@ class BilinearForm(Form):
                 entry = _PatternEntry(ubasis, c_form, stream, prog)
                 del keep
                 ubasis._patterns[key] = entry
+            entry.refresh_geometry(ubasis, stream)
             data = torch.empty(entry.nnz, dtype=torch.float64, pin_memory=True)
             indices = torch.empty(entry.nnz, dtype=torch.int32, pin_memory=True)
             indptr = torch.empty(entry.nrows + 1, dtype=torch.int32, pin_memory=True)
