@@ -130,14 +130,16 @@ __device__ __forceinline__ int64_t cell_at(const int32_t* __restrict__ cells, in
 
 // Each thread writes its element's matrix into a padded row of shared
 // memory; the block then streams the rows out (each cell's row contiguous,
-// consecutive cells contiguous without a cell list).
+// consecutive cells contiguous without a cell list).  With a cell list the
+// block's cell ids sit in shared memory (cid, one per thread, written by
+// the thread that computed the cell).
 template <int L, int BS = kBlock>
 __device__ __forceinline__ void flush_rows(double* smem, double* __restrict__ out, int64_t e0,
-                                           int64_t nelems, const int32_t* __restrict__ cells) {
+                                           int64_t nelems, const int64_t* cid) {
   __syncthreads();
   const int64_t nb = ((nelems - e0) < (int64_t)BS ? (nelems - e0) : (int64_t)BS);
   const int64_t total = nb * L;
-  if (!cells) {
+  if (!cid) {
     double* dst = out + e0 * L;
     for (int64_t g = threadIdx.x; g < total; g += blockDim.x) {
       const int el = (int)(g / L);
@@ -148,11 +150,15 @@ __device__ __forceinline__ void flush_rows(double* smem, double* __restrict__ ou
     for (int64_t g = threadIdx.x; g < total; g += blockDim.x) {
       const int el = (int)(g / L);
       const int k = (int)(g - (int64_t)el * L);
-      out[(int64_t)__ldg(cells + e0 + el) * L + k] = smem[el * (L + 1) + k];
+      out[cid[el] * L + k] = smem[el * (L + 1) + k];
     }
   }
   __syncthreads();
 }
+
+// Shared-memory bytes of a cell-list launch beyond the row buffer.
+template <int BS>
+constexpr size_t kCidBytes = (size_t)BS * sizeof(int64_t);
 
 // ------------------------------------------------ simplex, scalar P1 / P2
 template <int D, int ORDER>
@@ -261,6 +267,7 @@ __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBiline
   constexpr int L = NB * NB;
   constexpr double INV_FACT = 1.0 / SimplexTraits<D, ORDER>::FACT;
   extern __shared__ double smem[];
+  int64_t* cid = cells ? reinterpret_cast<int64_t*>(smem + (size_t)BS * (L + 1)) : nullptr;
   int32_t flags = 0;
   // grid-stride over element tiles of BS cells (persistent when the grid is
   // smaller than the number of tiles)
@@ -268,6 +275,7 @@ __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBiline
   const int64_t pos = e0 + threadIdx.x;
   if (pos < eend) {
     const int64_t e = cell_at(cells, pos);
+    if (cid) cid[threadIdx.x] = e;
     const int rb = ref_byte(ref_bits, e);
     // stiffness scale sd times the Gram entries: kd / (d! |det|) (kdiff is
     // f.diff with its scale multiplied by 1/d! on the host; the cache holds
@@ -303,7 +311,7 @@ __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBiline
 #undef KM
     if (status) flags |= coef_status(f, e, rb);
   }
-  flush_rows<L, BS>(smem, out, e0, eend, cells);
+  flush_rows<L, BS>(smem, out, e0, eend, cid);
   }
   fem::publish_status(status, flags);
 }
@@ -329,10 +337,12 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
   constexpr double FACT = SimplexTraits<D, ORDER>::FACT;
   extern __shared__ double smem[];
   double* rows = smem;                               // [BS][RB+1]
+  int64_t* cid = cells ? reinterpret_cast<int64_t*>(smem + (size_t)BS * (RB + 1)) : nullptr;
   const int64_t e0 = ebeg + (int64_t)blockIdx.x * BS;
   const int tid = threadIdx.x;
   const bool live = e0 + tid < eend;
   const int64_t e = live ? cell_at(cells, e0 + tid) : 0;
+  if (cid) cid[tid] = e;
   double sm = 0.0;
   // E[p][q][a][b] for p <= q, kept in registers: every index below is a
   // compile-time constant once the block loops are unrolled.
@@ -437,7 +447,7 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
       const int kk = (int)(g - (int64_t)el * (D * W));
       const int a = kk / W;
       const int k = a * NB + C0 + (kk - a * W);
-      out[cell_at(cells, e0 + el) * (int64_t)(NB * NB) + (int64_t)i * RB + k] =
+      out[(cid ? cid[el] : e0 + el) * (int64_t)(NB * NB) + (int64_t)i * RB + k] =
           rows[el * (RB + 1) + k];
     }
     __syncthreads();
@@ -537,10 +547,12 @@ __global__ void __launch_bounds__(kBlock) hex_scalar_kernel(FemMesh m, FemBiline
                                                             int64_t ebeg, int64_t eend) {
   constexpr int L = 64;
   extern __shared__ double smem[];
+  int64_t* cid = cells ? reinterpret_cast<int64_t*>(smem + (size_t)kBlock * (L + 1)) : nullptr;
   const int64_t e0 = ebeg + (int64_t)blockIdx.x * kBlock;
   int32_t flags = 0;
   if (e0 + threadIdx.x < eend) {
     const int64_t e = cell_at(cells, e0 + threadIdx.x);
+    if (cid) cid[threadIdx.x] = e;
     const int rb = ref_byte(ref_bits, e);
     Hex h;
     hex_load(m, e, h);
@@ -622,7 +634,7 @@ __global__ void __launch_bounds__(kBlock) hex_scalar_kernel(FemMesh m, FemBiline
     if (status) flags |= coef_status(f, e, rb);
   }
   fem::publish_status(status, flags);
-  flush_rows<L>(smem, out, e0, eend, cells);
+  flush_rows<L>(smem, out, e0, eend, cid);
 }
 
 // ------------------------------------------------------------ load vectors
@@ -729,7 +741,7 @@ static int launch_scalar(const FemMesh& m, const FemBilinear& f, double* out,
                          cudaStream_t st, int64_t ebeg, int64_t eend, const int32_t* cells,
                          const double* geo) {
   constexpr int NB = SimplexTraits<D, O>::NB;
-  const size_t sm = (size_t)BS * (NB * NB + 1) * sizeof(double);
+  const size_t sm = (size_t)BS * (NB * NB + 1) * sizeof(double) + (cells ? kCidBytes<BS> : 0);
   int64_t grid = fem::ceil_div(eend - ebeg, BS);
   if (persistent > 0) grid = std::min<int64_t>(grid, (int64_t)persistent * fem::num_sms());
   FemCoef kdiff = f.diff;
@@ -779,7 +791,7 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
       case FEM_TET_P1: rc = launch_scalar_tuned<3, 1>(m, f, out, ref_bits, status, st, ebeg, eend, cells, geo); break;
       case FEM_TET_P2: rc = launch_scalar_tuned<3, 2>(m, f, out, ref_bits, status, st, ebeg, eend, cells, geo); break;
       case FEM_HEX_1: {
-        const size_t sm = (size_t)kBlock * 65 * sizeof(double);
+        const size_t sm = (size_t)kBlock * 65 * sizeof(double) + (cells ? kCidBytes<kBlock> : 0);
         if ((rc = set_smem(hex_scalar_kernel, sm))) return rc;
         hex_scalar_kernel<<<(unsigned)grid, kBlock, sm, st>>>(m, f, out, ref_bits, status, cells,
                                                               ebeg, eend);
@@ -797,7 +809,7 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
   {                                                                                    \
     constexpr int NS = SimplexTraits<D, O>::NB, NB = NS * D;                          \
     constexpr int RB = D * NB;                                                         \
-    const size_t sm = (size_t)64 * (RB + 1) * sizeof(double);                          \
+    const size_t sm = (size_t)64 * (RB + 1) * sizeof(double) + (cells ? kCidBytes<64> : 0); \
     if (upper) {                                                                       \
       if ((rc = set_smem(simplex_vector_kernel<D, O, true>, sm))) return rc;           \
       simplex_vector_kernel<D, O, true><<<(unsigned)vgrid, 64, sm, st>>>(m, f, out, ref_bits, status, cells, ebeg, eend); \
