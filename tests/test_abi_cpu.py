@@ -37,3 +37,33 @@ def test_argument_errors_without_gpu():
     b = N.FemBasis(99, 0, 4, 0, 4, None)
     rc = lib.fem_local_matrices(ctypes.byref(m), ctypes.byref(b), ctypes.byref(f), None, None)
     assert rc == N.FEM_ERR_UNSUPPORTED
+
+
+def test_pipeline_and_cache_entry_points_validate_on_the_host():
+    """The host-pipelined assembly and the geometry cache refuse bad
+    arguments before any CUDA call."""
+    from skfem_gb300 import _build, _native as N
+    lib = ctypes.CDLL(_build.build())
+    lib.fem_last_error.restype = ctypes.c_char_p
+    m = N.FemMesh(3, 4, 4, 1, None, None)
+    b = N.FemBasis(N.FAMILY["TetP1"], 0, 4, 0, 4, None)
+    f = N.FemBilinear()
+    V = ctypes.c_void_p
+    # null pattern / buffers
+    lib.fem_assemble_to_host_pipelined.argtypes = [V] * 8 + [V, ctypes.c_int32, ctypes.c_int32,
+                                                             V, V, V]
+    rc = lib.fem_assemble_to_host_pipelined(ctypes.addressof(m), ctypes.addressof(b),
+                                            ctypes.addressof(f), None, None, None, None, None,
+                                            None, 0, 8, None, None, None)
+    assert rc == N.FEM_ERR_ARGUMENT
+    # chunk count out of range, host rows announced but not given
+    for nfields, nchunks in ((0, 0), (0, 257), (2, 8), (17, 8)):
+        rc = lib.fem_assemble_to_host_pipelined(ctypes.addressof(m), ctypes.addressof(b),
+                                                ctypes.addressof(f), None, None, None, None,
+                                                None, None, nfields, nchunks, None, None, None)
+        assert rc == N.FEM_ERR_ARGUMENT
+    lib.fem_pattern_cache_geometry.argtypes = [V, V, V, V]
+    rc = lib.fem_pattern_cache_geometry(None, ctypes.addressof(m), ctypes.addressof(b), None)
+    assert rc == N.FEM_ERR_ARGUMENT
+    lib.fem_pattern_drop_geometry.argtypes = [V]
+    lib.fem_pattern_drop_geometry(None)          # null: a no-op
