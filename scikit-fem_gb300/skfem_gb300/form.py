@@ -726,11 +726,16 @@ class BilinearForm(Form):
                 uploaded = True
             if entry.nnz:
                 up = _copy_stream(ubasis.device)
-                N.check(lib.fem_assemble_to_host_pipelined(
+                rc = lib.fem_assemble_to_host_pipelined(
                     N.byref(ubasis.c_mesh), N.byref(ubasis.c_basis), N.byref(c_form),
                     entry.pat.handle, N.ptr(entry.staging), N.ptr(vals),
                     ctypes.c_void_p(data.data_ptr()), N.ptr(entry.status), rows, nrows, nch,
-                    stream, N.stream_ptr(up), N.stream_ptr(side)))
+                    stream, N.stream_ptr(up), N.stream_ptr(side))
+                if rc:
+                    # gathers already queued read the host arrays and write the
+                    # device ones: let them finish before either can be freed
+                    up.synchronize()
+                    N.check(rc)
             else:
                 N.check(lib.fem_assemble_local(
                     N.byref(ubasis.c_mesh), N.byref(ubasis.c_basis), N.byref(c_form),
