@@ -243,7 +243,9 @@ int fem_pattern_build(const FemMesh* mesh, const FemBasis* basis, const FemBilin
  * fem_assemble, fem_assemble_local and fem_assemble_to_host_pipelined then
  * read it instead of the coordinates whenever the mesh they are given has
  * the same p pointer; after changing the coordinates in place, call this
- * again (or fem_pattern_drop_geometry).  Other families: no cache, no-op.
+ * again (or fem_pattern_drop_geometry).  Other families, or no device
+ * memory left for the cache: no cache, returns 0 (the kernels then compute
+ * the geometry per call).
  * Stream-ordered; not concurrently with assembly calls on the pattern.
  */
 int fem_pattern_cache_geometry(FemPattern* pat, const FemMesh* mesh, const FemBasis* basis,

@@ -402,6 +402,14 @@ int fem_pattern_cache_geometry(FemPattern* pat, const FemMesh* mesh, const FemBa
   cudaStream_t st = (cudaStream_t)stream;
   if (!pat->geo) {
     cudaError_t e = cudaMalloc(&pat->geo, std::max<int64_t>(1, mesh->nelems) * ng * sizeof(double));
+    if (e == cudaErrorMemoryAllocation) {
+      // the cache is an optimisation: without room for it the kernels
+      // compute the geometry per call
+      cudaGetLastError();
+      pat->geo = nullptr;
+      pat->geo_p = nullptr;
+      return 0;
+    }
     if (e != cudaSuccess) {
       pat->geo = nullptr;
       return fem::check_cuda(e, "cudaMalloc(geometry cache)");
