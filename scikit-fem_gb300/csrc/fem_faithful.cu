@@ -362,13 +362,21 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets*
   s.mixed = mixed;
   s.nbu = ub.nbfun;
   s.nquantu = ub.vector ? m.dim + m.dim * m.dim : 1 + m.dim;
+  s.uv = prog.compiled && prog.compiled->uv;
+  s.nuval = prog.compiled ? prog.compiled->nuval : 0;
+  s.nvval = prog.compiled ? prog.compiled->nvval : 0;
   auto bytes = [&](int epb) {
     fem_faithful::GenericLayout t = s;
     t.epb = epb;
     return t.total() * sizeof(double);
   };
   s.entry_loop = false;
-  if (bytes(1) > 96 * 1024) s.entry_loop = true;   // no per-(entry, point) value stage
+  if (bytes(1) > 96 * 1024) {
+    // no per-(entry, point) value stage; a compiled program evaluates its
+    // trial-only and test-only parts per entry (in registers)
+    s.entry_loop = true;
+    s.uv = false;
+  }
   int epb = std::max(1, std::min(64, 2048 / (L * nq)));
   while (epb > 1 && bytes(epb) > 96 * 1024) --epb;
   s.epb = epb;

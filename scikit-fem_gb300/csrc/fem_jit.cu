@@ -110,6 +110,116 @@ bool unary(int op) {
          op == OP_COS || op == OP_TAN || op == OP_TANH || op == OP_ARCTAN || op == OP_ABS;
 }
 
+// Bilinear programs split four ways by what an instruction depends on: jit_point
+// (neither u nor v: once per point, the values needed later in P), jit_u (the
+// trial function only: once per point and trial function, into U), jit_v
+// (the test function only: once per point and test function, into V) and
+// jit_form_uv (the rest, reading P, U and V).  Every instruction keeps its
+// operands and so its value, bit for bit; only where it is evaluated moves.
+std::string program_source_uv(const FemInstr* ins, int n, int out, int* npoint, int* nuval,
+                              int* nvval) {
+  std::string s;
+  char line[256];
+  // dep bit 1: trial quantity, bit 2: test quantity
+  std::vector<int> dep(n, 0);
+  for (int k = 0; k < n; ++k) {
+    const FemInstr& I = ins[k];
+    if (I.op == fem_faithful::OP_U) dep[k] = 1;
+    else if (I.op == fem_faithful::OP_V) dep[k] = 2;
+    else if (binary(I.op)) dep[k] = dep[I.a] | dep[I.b];
+    else if (unary(I.op)) dep[k] = dep[I.a];
+  }
+  // an instruction's value is stored when an instruction of another class
+  // (or the output, evaluated in jit_form_uv) reads it
+  std::vector<char> need(n, 0);
+  auto use = [&](int k, int operand) {
+    if (dep[operand] != dep[k]) need[operand] = 1;
+  };
+  for (int k = 0; k < n; ++k) {
+    const FemInstr& I = ins[k];
+    if (binary(I.op)) {
+      use(k, I.a);
+      use(k, I.b);
+    } else if (unary(I.op)) {
+      use(k, I.a);
+    }
+  }
+  if (dep[out] != 3) need[out] = 1;
+  std::vector<int> slot(n, -1);
+  int cnt[4] = {0, 0, 0, 0};
+  for (int k = 0; k < n; ++k)
+    if (need[k]) slot[k] = cnt[dep[k]]++;
+  *npoint = cnt[0];
+  *nuval = cnt[1];
+  *nvval = cnt[2];
+  const char* store[3] = {"P", "U", "V"};
+  auto operand_load = [&](int k, int cls, std::string& body) {
+    // the operands of class-cls instructions that live in another class's slots
+    std::vector<char> loaded(n, 0);
+    for (int i = 0; i < n; ++i) {
+      if (dep[i] != cls) continue;
+      const FemInstr& I = ins[i];
+      int ops[2] = {-1, -1};
+      if (binary(I.op)) {
+        ops[0] = I.a;
+        ops[1] = I.b;
+      } else if (unary(I.op)) {
+        ops[0] = I.a;
+      }
+      for (int o : ops)
+        if (o >= 0 && dep[o] != cls && !loaded[o]) {
+          loaded[o] = 1;
+          std::snprintf(line, sizeof line, "  const double r%d = %s[%d];\n", o, store[dep[o]],
+                        slot[o]);
+          body += line;
+        }
+    }
+    (void)k;
+  };
+  auto emit_class = [&](int cls, std::string& body) {
+    operand_load(0, cls, body);
+    for (int k = 0; k < n; ++k) {
+      if (dep[k] != cls) continue;
+      std::snprintf(line, sizeof line, "  const double r%d = ", k);
+      body += line + rhs_of(ins[k]) + ";\n";
+    }
+  };
+  std::snprintf(line, sizeof line, "#define FEM_JIT_NUVAL %d\n#define FEM_JIT_NVVAL %d\n",
+                std::max(1, cnt[1]), std::max(1, cnt[2]));
+  s += line;
+  s += "__device__ __forceinline__ void jit_point(const double* cq, const double* qx, "
+       "double* P) {\n";
+  emit_class(0, s);
+  for (int k = 0; k < n; ++k)
+    if (dep[k] == 0 && slot[k] >= 0) {
+      std::snprintf(line, sizeof line, "  P[%d] = r%d;\n", slot[k], k);
+      s += line;
+    }
+  s += "}\n";
+  const char* fn[3] = {"", "jit_u(const double* qu, const double* P, double* U)",
+                       "jit_v(const double* qv, const double* P, double* V)"};
+  for (int cls = 1; cls <= 2; ++cls) {
+    s += std::string("__device__ __forceinline__ void ") + fn[cls] + " {\n";
+    emit_class(cls, s);
+    for (int k = 0; k < n; ++k)
+      if (dep[k] == cls && slot[k] >= 0) {
+        std::snprintf(line, sizeof line, "  %s[%d] = r%d;\n", store[cls], slot[k], k);
+        s += line;
+      }
+    s += "  (void)P;\n}\n";
+  }
+  s += "__device__ __forceinline__ double jit_form_uv(const double* P, const double* U, "
+       "const double* V) {\n";
+  emit_class(3, s);
+  if (dep[out] != 3) {
+    std::snprintf(line, sizeof line, "  const double r%d = %s[%d];\n", out, store[dep[out]],
+                  slot[out]);
+    s += line;
+  }
+  s += "  (void)P; (void)U; (void)V;\n  return r" + std::to_string(out) + ";\n}\n";
+  return s;
+}
+
 // The program as straight-line code; the caller has validated operands.
 // hoist: split it into jit_point (instructions that depend on neither u
 // nor v, once per point, their values needed later stored in P) and
@@ -178,7 +288,8 @@ std::string program_source(const FemInstr* ins, int n, int out, bool hoist, int*
 
 // The complete source compiled for a program (headers by name).
 int kernel_source(const FemInstr* ins, int ninstr, int out, int ncoef, int dim, int vector,
-                  int vector_u, int mode, int facet, std::string& src, int* npoint);
+                  int vector_u, int mode, int facet, std::string& src, int* npoint,
+                  int* nuval, int* nvval);
 
 }  // namespace
 
@@ -199,8 +310,10 @@ int jit_launch(const FemCompiled* k, dim3 grid, dim3 block, size_t smem, cudaStr
 
 namespace {
 int kernel_source(const FemInstr* ins, int ninstr, int out, int ncoef, int dim, int vector,
-                  int vector_u, int mode, int facet, std::string& src, int* npoint) {
+                  int vector_u, int mode, int facet, std::string& src, int* npoint,
+                  int* nuval, int* nvval) {
   using fem::set_error;
+  *nuval = *nvval = 0;
   if (!ins || (dim != 2 && dim != 3) || mode < 0 || mode > 2 || ninstr <= 0 ||
       ninstr > fem_faithful::kMaxProgram || out < 0 || out >= ninstr || ncoef < 0 ||
       ncoef > fem_faithful::kMaxCoef) {
@@ -215,6 +328,14 @@ int kernel_source(const FemInstr* ins, int ninstr, int out, int ncoef, int dim, 
   // bilinear and linear forms evaluate each point's u/v-free part once;
   // a functional has one entry per cell and runs the program whole
   const bool hoist = mode != 2;
+  if (mode == 0) {
+    // bilinear: trial-only and test-only parts once per point and function
+    const std::string body = program_source_uv(ins, ninstr, out, npoint, nuval, nvval);
+    src += "#define FEM_JIT_HOIST 1\n#define FEM_JIT_HOIST_UV 1\n"
+           "#include \"fem_faithful_core.cuh\"\n";
+    src += "namespace fem_faithful {\n" + body + "}\n";
+    src += "#include \"fem_program_kernel.cuh\"\n";
+  } else {
   const std::string body = program_source(ins, ninstr, out, hoist, npoint);
   if (hoist) {
     src += "#define FEM_JIT_HOIST 1\n#include \"fem_faithful_core.cuh\"\n";
@@ -226,6 +347,7 @@ int kernel_source(const FemInstr* ins, int ninstr, int out, int ncoef, int dim, 
     src += "#define FEM_FORM_EVAL(prog, qu, qv, cq, qx, R) jit_form(qu, qv, cq, qx)\n";
     src += "#include \"fem_faithful_core.cuh\"\n#include \"fem_program_kernel.cuh\"\n";
     src += "namespace fem_faithful {\n" + body + "}\n";
+  }
   }
   char tail[512];
   std::snprintf(tail, sizeof tail,
@@ -247,9 +369,9 @@ int fem_program_source(const FemInstr* ins, int32_t ninstr, int32_t out, int32_t
                        int32_t dim, int32_t vector, int32_t vector_u, int32_t mode, int32_t facet,
                        char* buf, int64_t size, int64_t* needed) {
   std::string src;
-  int npoint = 0;
+  int npoint = 0, nuval = 0, nvval = 0;
   if (int rc = kernel_source(ins, ninstr, out, ncoef, dim, vector, vector_u, mode, facet, src,
-                             &npoint))
+                             &npoint, &nuval, &nvval))
     return rc;
   if (needed) *needed = (int64_t)src.size() + 1;
   if (buf && size > 0) {
@@ -270,9 +392,9 @@ int fem_program_compile(const FemInstr* ins, int32_t ninstr, int32_t out, int32_
   }
   *compiled = nullptr;
   std::string src;
-  int npoint = 0;
+  int npoint = 0, nuval = 0, nvval = 0;
   if (int rc = kernel_source(ins, ninstr, out, ncoef, dim, vector, vector_u, mode, facet, src,
-                             &npoint))
+                             &npoint, &nuval, &nvval))
     return rc;
   std::lock_guard<std::mutex> lock(g_mu);
   if (!load_nvrtc()) {
@@ -311,6 +433,9 @@ int fem_program_compile(const FemInstr* ins, int32_t ninstr, int32_t out, int32_
   k->mode = mode;
   k->facet = facet ? 1 : 0;
   k->npoint = npoint;
+  k->nuval = mode == 0 ? nuval : 0;
+  k->nvval = mode == 0 ? nvval : 0;
+  k->uv = mode == 0;
   k->vector_u = mode == 0 ? (vector_u ? 1 : 0) : (vector ? 1 : 0);
   cudaError_t e = cudaLibraryLoadData(&k->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
   if (e == cudaSuccess) e = cudaLibraryGetKernel(&k->kernel, k->lib, "fem_jit_program");

@@ -12,6 +12,8 @@ struct FemCompiled {
   cudaKernel_t kernel = nullptr;
   int dim = 0, mode = 0, facet = 0;
   int npoint = 0;                  // per-point hoisted values (GenericLayout::npoint)
+  int uv = 0;                      // bilinear: trial-only / test-only values hoisted
+  int nuval = 0, nvval = 0;        // ... per point and function (GenericLayout::nuval/nvval)
   int vector_u = 0;                // the trial basis's vector flag (bilinear forms)
   size_t smem_limit = 48 * 1024;   // dynamic shared memory the kernel is enabled for
 };

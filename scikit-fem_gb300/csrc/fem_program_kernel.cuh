@@ -60,6 +60,8 @@ struct GenericLayout {
   bool mixed;          // a trial basis of its own (nbu functions, nquantu quantities)
   int nbu, nquantu;
   bool entry_loop;     // one thread per entry looping over the points (no value stage)
+  bool uv;             // compiled bilinear programs: trial-only / test-only values staged
+  int nuval, nvval;    // ... per (point, trial function) / (point, test function)
   __host__ __device__ size_t geo() const { return 0; }
   __host__ __device__ size_t val() const { return (size_t)epb * nq * kGeo; }
   __host__ __device__ size_t cell() const {
@@ -72,7 +74,13 @@ struct GenericLayout {
   __host__ __device__ size_t point() const {
     return quantu() + (mixed ? (size_t)epb * nq * nbu * nquantu : 0);
   }
-  __host__ __device__ size_t total() const { return point() + (size_t)epb * nq * npoint; }
+  __host__ __device__ size_t uval() const { return point() + (size_t)epb * nq * npoint; }
+  __host__ __device__ size_t vval() const {
+    return uval() + (uv ? (size_t)epb * nq * (mixed ? nbu : nb) * nuval : 0);
+  }
+  __host__ __device__ size_t total() const {
+    return vval() + (uv ? (size_t)epb * nq * nb * nvval : 0);
+  }
 };
 
 // b: the test basis (and trial basis unless s.mixed); bu: the trial basis.
@@ -185,6 +193,32 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
   }
   __syncthreads();
 #endif
+#ifdef FEM_JIT_HOIST_UV
+  // stage 1d (compiled bilinear programs): the instructions that depend on the
+  // trial function only, once per point and trial function, and those on the
+  // test function only, once per point and test function
+  double* UU = gsm + s.uval();
+  double* VV = gsm + s.vval();
+  if (s.uv) {
+    for (int k = threadIdx.x; k < s.epb * s.nq * nbu; k += blockDim.x) {
+      const int p = k / nbu;                    // p = el * nq + q
+      if (e0 + p / s.nq >= ncells) continue;
+      double qu[D + D * D];
+#pragma unroll
+      for (int a = 0; a < NQU; ++a) qu[a] = Qu[(size_t)k * NQU + a];
+      jit_u(qu, P + (size_t)p * s.npoint, UU + (size_t)k * s.nuval);
+    }
+    for (int k = threadIdx.x; k < s.epb * s.nq * nb; k += blockDim.x) {
+      const int p = k / nb;
+      if (e0 + p / s.nq >= ncells) continue;
+      double qv[D + D * D];
+#pragma unroll
+      for (int a = 0; a < NQ; ++a) qv[a] = Q[(size_t)k * NQ + a];
+      jit_v(qv, P + (size_t)p * s.npoint, VV + (size_t)k * s.nvval);
+    }
+    __syncthreads();
+  }
+#endif
   if (s.entry_loop) {
     // large local matrices: a thread takes an entry, its points in turn
     double R[kMaxProgram];
@@ -216,7 +250,15 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
 #pragma unroll
           for (int a = 0; a < NQ; ++a) qv[a] = 0.0;
         }
-#ifdef FEM_JIT_HOIST
+#if defined(FEM_JIT_HOIST_UV)
+        const double* Pp = P + ((size_t)el * s.nq + q) * s.npoint;
+        double Ut[FEM_JIT_NUVAL], Vt[FEM_JIT_NVVAL];
+        jit_u(qu, Pp, Ut);
+        jit_v(qv, Pp, Vt);
+        const double fq = jit_form_uv(Pp, Ut, Vt);
+        vals[q] = fq * (fabs(g.det) * rule.W[q]);
+        (void)R;
+#elif defined(FEM_JIT_HOIST)
         const double fq = jit_form_hoisted(qu, qv, P + ((size_t)el * s.nq + q) * s.npoint);
         vals[q] = fq * (fabs(g.det) * rule.W[q]);
         (void)R;
@@ -245,6 +287,15 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
       for (int c = 0; c < 3; ++c) g.inv[a][c] = G[a * 3 + c];
     g.det = G[9];
     for (int a = 0; a < 7; ++a) g.qx[a] = G[10 + a];
+#if defined(FEM_JIT_HOIST_UV)
+    if (s.uv) {
+      const size_t p = (size_t)el * s.nq + q;
+      const double fq = jit_form_uv(P + p * s.npoint, UU + (p * nbu + j) * s.nuval,
+                                    VV + (p * nb + i) * s.nvval);
+      val[k] = fq * (fabs(g.det) * rule.W[q]);
+      continue;
+    }
+#endif
     double qu[D + D * D], qv[D + D * D];
     if (s.quants) {
       const double* Qp = Q + ((size_t)(el * s.nq + q) * nb) * NQ;
@@ -259,7 +310,16 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
 #pragma unroll
       for (int a = 0; a < NQ; ++a) qv[a] = 0.0;
     }
-#ifdef FEM_JIT_HOIST
+#if defined(FEM_JIT_HOIST_UV)
+    {
+      const double* Pp = P + ((size_t)el * s.nq + q) * s.npoint;
+      double Ut[FEM_JIT_NUVAL], Vt[FEM_JIT_NVVAL];
+      jit_u(qu, Pp, Ut);
+      jit_v(qv, Pp, Vt);
+      val[k] = jit_form_uv(Pp, Ut, Vt) * (fabs(g.det) * rule.W[q]);
+      (void)R;
+    }
+#elif defined(FEM_JIT_HOIST)
     const double fq = jit_form_hoisted(qu, qv, P + ((size_t)el * s.nq + q) * s.npoint);
     val[k] = fq * (fabs(g.det) * rule.W[q]);
     (void)R;
