@@ -106,7 +106,11 @@ __global__ void interpolate_kernel(FemMesh m, FemBasis b, FemFacets fc, Rule rul
   const bool hex = b.family == FEM_HEX_1;
   const bool maps = !FACET && !hex;
   const int nb = b.nbfun;
-  const int per = kCell + nb;           // per cell: affine map, DOF values
+  constexpr int NQ = D + D * D;
+  // P1 on affine cells: each function's quantities at the cell's first
+  // point are staged; the other points take their derivative part
+  const bool p1 = maps && point_free_gradients(b.family);
+  const int per = kCell + nb + (p1 ? nb * NQ : 0);  // per cell: map, DOF values, quantities
   const int64_t e0 = (int64_t)blockIdx.x * cpb;
   for (int k = threadIdx.x; k < cpb; k += blockDim.x) {
     const int64_t e = e0 + k;
@@ -130,6 +134,13 @@ __global__ void interpolate_kernel(FemMesh m, FemBasis b, FemFacets fc, Rule rul
       for (int i = 0; i < 3; ++i) S[19 + i] = cg.x0[i];
     }
     for (int i = 0; i < nb; ++i) S[kCell + i] = w[b.element_dofs[(int64_t)i * m.nelems + ec]];
+    if (p1) {
+      PointGeo g0;
+      double Y0[3];
+      geometry_at<D, FACET>(m, b, fc, rule, ProgFlags(), e, 0, Y0, g0, S);
+      for (int i = 0; i < nb; ++i)
+        quantities<D>(b.family, VEC, i, Y0[0], Y0[1], Y0[2], g0.inv, S + kCell + nb + i * NQ);
+    }
   }
   __syncthreads();
   const int t = threadIdx.x;
@@ -147,16 +158,21 @@ __global__ void interpolate_kernel(FemMesh m, FemBasis b, FemFacets fc, Rule rul
     if (status) atomicOr(status, 1 << FEM_ERR_ARGUMENT);
     return;
   }
-  constexpr int NQ = D + D * D;
   constexpr int nquant = VEC ? D + D * D : 1 + D;
   double acc[NQ], qq[NQ];
+  auto quant = [&](int i) {
+    if (p1) quantities_values<D>(b.family, vec, i, Y[0], Y[1], Y[2], S + kCell + nb + i * NQ, qq);
+    else quantities<D>(b.family, vec, i, Y[0], Y[1], Y[2], g.inv, qq);
+  };
   const double w0 = S[kCell];
-  quantities<D>(b.family, vec, 0, Y[0], Y[1], Y[2], g.inv, qq);
+  quant(0);   // function 0: the start 0*(w0 q0) and the first term
 #pragma unroll
   for (int a = 0; a < nquant; ++a) acc[a] = 0.0 * (w0 * qq[a]);
-  for (int i = 0; i < nb; ++i) {
+#pragma unroll
+  for (int a = 0; a < nquant; ++a) acc[a] = acc[a] + w0 * qq[a];
+  for (int i = 1; i < nb; ++i) {
     const double wi = S[kCell + i];
-    quantities<D>(b.family, vec, i, Y[0], Y[1], Y[2], g.inv, qq);
+    quant(i);
 #pragma unroll
     for (int a = 0; a < nquant; ++a) acc[a] = acc[a] + wi * qq[a];
   }
@@ -461,10 +477,19 @@ int interpolate(const FemMesh& m, const FemBasis& b, const FemFacets* fc, int nq
   // one (cell, point) pair per thread: blocks of cpb cells x nq points
   const int cpb = std::max(1, 128 / nq);
   const int threads = cpb * nq;
-  const size_t smem = (size_t)cpb * (fem_faithful::kCell + b.nbfun) * sizeof(double);
+  // per cell: the affine map, the DOF values and, P1 on affine cells, every
+  // function's quantities at the first point (interpolate_kernel)
+  const bool p1 = !fc && b.family != FEM_HEX_1 && fem_faithful::point_free_gradients(b.family);
+  const int nqmax = m.dim + m.dim * m.dim;
+  const size_t smem = (size_t)cpb * (fem_faithful::kCell + b.nbfun + (p1 ? b.nbfun * nqmax : 0)) *
+                      sizeof(double);
   const unsigned grid = (unsigned)ceil_div(ncells, cpb);
   using namespace fem_faithful;
-  auto go = [&](auto kern) { kern<<<grid, threads, smem, st>>>(m, b, F, rule, ncells, cpb, w, out, status); };
+  auto go = [&](auto kern) {
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<grid, threads, smem, st>>>(m, b, F, rule, ncells, cpb, w, out, status);
+  };
   const bool v = b.vector != 0;
   if (m.dim == 2) {
     if (fc) v ? go(interpolate_kernel<2, true, true>) : go(interpolate_kernel<2, true, false>);

@@ -235,6 +235,30 @@ FEM_HD void quantities(int family, bool vec, int fn, double x, double y, double 
   }
 }
 
+// P1 families: the reference gradients are constant (lbasis writes them as
+// c + 0*x), so on an affine cell every quantity's derivative part is the
+// same at every point -- computed once and reused, the same numbers.
+FEM_HD bool point_free_gradients(int family) {
+  return family == FEM_TRI_P1 || family == FEM_TET_P1;
+}
+
+// quantities() with the derivative part taken from qg (the quantities of the
+// same function at another point of the same affine cell, P1 families) and
+// the values evaluated here.
+template <int D>
+FEM_HD void quantities_values(int family, bool vec, int fn, double x, double y, double z,
+                              const double* qg, double* q) {
+  const int sfn = vec ? fn / D : fn;
+  const int comp = vec ? fn % D : 0;
+  const int ncomp = vec ? D : 1;
+  double phi, d[3];
+  lbasis(family, sfn, x, y, z, phi, d);
+  for (int c = 0; c < ncomp; ++c) {
+    q[c] = (c == comp) ? phi : 0.0;
+    for (int k = 0; k < D; ++k) q[ncomp + c * D + k] = qg[ncomp + c * D + k];
+  }
+}
+
 FEM_HD double run(const Instr* ins, int n, int out, const double* qu, const double* qv,
                       const double* coef, const double* qx, double* R) {
   for (int k = 0; k < n; ++k) {

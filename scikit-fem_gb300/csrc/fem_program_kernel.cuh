@@ -145,11 +145,15 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
     for (int i = 0; i < 3; ++i) G[17 + i] = Y[i];
   }
   __syncthreads();
-  // stage 1b: every basis function's quantities at every point, once
+  // stage 1b: every basis function's quantities at every point, once.  P1
+  // on affine cells: the full quantities at each cell's first point, then
+  // at the other points the values with the same derivative part
   if (s.quants) {
+    const bool p1 = !FACET && s.cells && point_free_gradients(b.family);
     for (int k = threadIdx.x; k < s.epb * s.nq * nb; k += blockDim.x) {
       const int p = k / nb, fn = k - p * nb;    // p = el * nq + q
       if (e0 + p / s.nq >= ncells) continue;
+      if (p1 && p % s.nq != 0) continue;
       const double* G = geo + (size_t)p * kGeo;
       double inv[3][3];
       for (int a = 0; a < 3; ++a)
@@ -158,6 +162,19 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
       quantities<D>(b.family, vec, fn, G[17], G[18], G[19], inv, qq);
 #pragma unroll
       for (int a = 0; a < NQ; ++a) Q[(size_t)k * NQ + a] = qq[a];
+    }
+    if (p1) {
+      __syncthreads();
+      for (int k = threadIdx.x; k < s.epb * s.nq * nb; k += blockDim.x) {
+        const int p = k / nb, fn = k - p * nb;
+        if (e0 + p / s.nq >= ncells || p % s.nq == 0) continue;
+        const double* G = geo + (size_t)p * kGeo;
+        const size_t k0 = ((size_t)(p - p % s.nq) * nb + fn) * NQ;   // first point, same fn
+        double qq[D + D * D];
+        quantities_values<D>(b.family, vec, fn, G[17], G[18], G[19], Q + k0, qq);
+#pragma unroll
+        for (int a = 0; a < NQ; ++a) Q[(size_t)k * NQ + a] = qq[a];
+      }
     }
     if (s.mixed) {
       for (int k = threadIdx.x; k < s.epb * s.nq * nbu; k += blockDim.x) {
