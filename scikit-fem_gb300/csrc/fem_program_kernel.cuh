@@ -78,9 +78,10 @@ struct GenericLayout {
   __host__ __device__ size_t vval() const {
     return uval() + (uv ? (size_t)epb * nq * (mixed ? nbu : nb) * nuval : 0);
   }
-  __host__ __device__ size_t total() const {
+  __host__ __device__ size_t dx() const {
     return vval() + (uv ? (size_t)epb * nq * nb * nvval : 0);
   }
+  __host__ __device__ size_t total() const { return dx() + (size_t)epb * nq; }
 };
 
 // b: the test basis (and trial basis unless s.mixed); bu: the trial basis.
@@ -96,6 +97,7 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
   double* val = gsm + s.val();
   double* cgeo = gsm + s.cell();
   double* Q = gsm + s.quant();
+  double* dxs = gsm + s.dx();   // |det| W_q per (cell, point): dx, the same for every entry
   const bool hex = b.family == FEM_HEX_1;
   constexpr bool vec = VEC;
   constexpr int NQ = VEC ? D + D * D : 1 + D;   // quantities per basis function
@@ -143,6 +145,7 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
     G[9] = g.det;
     for (int i = 0; i < 7; ++i) G[10 + i] = g.qx[i];
     for (int i = 0; i < 3; ++i) G[17 + i] = Y[i];
+    dxs[k] = fabs(g.det) * rule.W[q];
   }
   __syncthreads();
   // stage 1b: every basis function's quantities at every point, once.  P1
@@ -273,11 +276,11 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
         jit_u(qu, Pp, Ut);
         jit_v(qv, Pp, Vt);
         const double fq = jit_form_uv(Pp, Ut, Vt);
-        vals[q] = fq * (fabs(g.det) * rule.W[q]);
+        vals[q] = fq * dxs[(size_t)el * s.nq + q];
         (void)R;
 #elif defined(FEM_JIT_HOIST)
         const double fq = jit_form_hoisted(qu, qv, P + ((size_t)el * s.nq + q) * s.npoint);
-        vals[q] = fq * (fabs(g.det) * rule.W[q]);
+        vals[q] = fq * dxs[(size_t)el * s.nq + q];
         (void)R;
 #else
         vals[q] = point_value_q(prog, e, q, qu, qv, g, rule.W[q], R);
@@ -298,21 +301,21 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
     if (e >= ncells) continue;
     const int i = MODE == 0 ? r / nbu : (MODE == 1 ? r : 0);
     const int j = MODE == 0 ? r - i * nbu : 0;
+#if defined(FEM_JIT_HOIST_UV)
+    if (s.uv) {
+      const size_t p = (size_t)el * s.nq + q;
+      const double fq = jit_form_uv(P + p * s.npoint, UU + (p * nbu + j) * s.nuval,
+                                    VV + (p * nb + i) * s.nvval);
+      val[k] = fq * dxs[p];
+      continue;
+    }
+#endif
     const double* G = geo + ((size_t)el * s.nq + q) * kGeo;
     PointGeo g;
     for (int a = 0; a < 3; ++a)
       for (int c = 0; c < 3; ++c) g.inv[a][c] = G[a * 3 + c];
     g.det = G[9];
     for (int a = 0; a < 7; ++a) g.qx[a] = G[10 + a];
-#if defined(FEM_JIT_HOIST_UV)
-    if (s.uv) {
-      const size_t p = (size_t)el * s.nq + q;
-      const double fq = jit_form_uv(P + p * s.npoint, UU + (p * nbu + j) * s.nuval,
-                                    VV + (p * nb + i) * s.nvval);
-      val[k] = fq * (fabs(g.det) * rule.W[q]);
-      continue;
-    }
-#endif
     double qu[D + D * D], qv[D + D * D];
     if (s.quants) {
       const double* Qp = Q + ((size_t)(el * s.nq + q) * nb) * NQ;
@@ -333,12 +336,12 @@ __device__ __forceinline__ void program_body(const FemMesh& m, const FemBasis& b
       double Ut[FEM_JIT_NUVAL], Vt[FEM_JIT_NVVAL];
       jit_u(qu, Pp, Ut);
       jit_v(qv, Pp, Vt);
-      val[k] = jit_form_uv(Pp, Ut, Vt) * (fabs(g.det) * rule.W[q]);
+      val[k] = jit_form_uv(Pp, Ut, Vt) * dxs[(size_t)el * s.nq + q];
       (void)R;
     }
 #elif defined(FEM_JIT_HOIST)
     const double fq = jit_form_hoisted(qu, qv, P + ((size_t)el * s.nq + q) * s.npoint);
-    val[k] = fq * (fabs(g.det) * rule.W[q]);
+    val[k] = fq * dxs[(size_t)el * s.nq + q];
     (void)R;
 #else
     val[k] = point_value_q(prog, e, q, qu, qv, g, rule.W[q], R);
