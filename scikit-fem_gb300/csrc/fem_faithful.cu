@@ -393,8 +393,10 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets*
     s.entry_loop = true;
     s.uv = false;
   }
-  int epb = std::max(1, std::min(64, 2048 / (L * nq)));
-  while (epb > 1 && bytes(epb) > 96 * 1024) --epb;
+  // blocks of 128 threads holding at most ~44 KB: five blocks per SM, so
+  // that the stage barriers of one block are covered by the others
+  int epb = std::max(1, std::min(32, 1024 / (L * nq)));
+  while (epb > 1 && bytes(epb) > 44 * 1024) --epb;
   s.epb = epb;
   const size_t smem = bytes(epb);
   if (smem > 200 * 1024) {
@@ -404,7 +406,7 @@ int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets*
   const fem_faithful::Rule rule{prog.qX, prog.qW, nq};
   const FemFacets F = fc ? *fc : FemFacets{};
   const unsigned grid = (unsigned)ceil_div(ncells, epb);
-  const int threads = 256;
+  const int threads = 128;
   if (prog.compiled) {
     const FemCompiled* k = prog.compiled;
     if (k->dim != m.dim || k->mode != mode || k->facet != (fc ? 1 : 0)) {
