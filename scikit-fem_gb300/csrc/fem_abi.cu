@@ -434,7 +434,8 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
                  fem_stream_t stream) {
   int rc = validate(mesh, basis);
   if (rc) return rc;
-  if (!form || !pat || !staging || !csr_values) {
+  // an empty pattern (no cells, or only exact zeros) takes no value buffer
+  if (!form || !pat || !staging || (!csr_values && pat->P.nnz > 0)) {
     set_error(FEM_ERR_ARGUMENT, "null form, pattern or buffer");
     return FEM_ERR_ARGUMENT;
   }
@@ -888,6 +889,7 @@ int fem_assemble_to_host(const FemMesh* mesh, const FemBasis* basis, const FemBi
 int fem_csr_sum(const FemPattern* pat, const double* local, double* csr_values, int32_t* status,
                 fem_stream_t stream) {
   (void)status;
+  if (pat && pat->P.nnz == 0) return 0;   // nothing to sum: buffers may be null
   if (!pat || !local || !csr_values) {
     set_error(FEM_ERR_ARGUMENT, "null pattern or buffer");
     return FEM_ERR_ARGUMENT;
@@ -1060,7 +1062,7 @@ int fem_pattern_build_local(const FemMesh* mesh, const FemBasis* basis, const do
 
 int fem_csr_sum_checked(const FemPattern* pat, const double* local, double* csr_values,
                         int32_t* status, fem_stream_t stream) {
-  if (!pat || !local || !csr_values || !status) {
+  if (!pat || (!local && pat->P.nelems > 0) || (!csr_values && pat->P.nnz > 0) || !status) {
     set_error(FEM_ERR_ARGUMENT, "null pattern, buffer or status");
     return FEM_ERR_ARGUMENT;
   }

@@ -572,8 +572,41 @@ def poisson_case():
     save("poisson_tri_p2", u=u)
 
 
+def edge_cases():
+    """Meshes at the edges of the path: a node no cell uses (the reference
+    numbers DOFs up to max(t), mesh.py nvertices), a single cell, an empty
+    element subset (cell_basis.py:94-99), for TetP1 k*laplace + mass, the
+    unit load and TriP2 Laplace."""
+    out = {}
+    m = MeshTet()
+    p = np.hstack([m.p, [[2.0], [2.0], [2.0]]])
+    k9 = np.linspace(0.5, 1.5, m.t.shape[1])
+    for name, mesh, elements in (("unused_node", MeshTet(p, m.t), None),
+                                 ("single", MeshTet(m.p[:, m.t[:, 0]],
+                                                    np.arange(4).reshape(4, 1)), None),
+                                 ("empty_subset", m, np.array([], dtype=np.int64))):
+        b = Basis(mesh, ElementTetP1(), elements=elements)
+        k = np.ones(b.nelems) if name != "unused_node" else k9
+        K = k_laplace_mass.assemble(b, k=b.zero_w() + k[:, None])
+        f = unit_load.assemble(b)
+        out[name + "_p"] = mesh.p
+        out[name + "_t"] = mesh.t
+        out[name + "_k"] = k
+        out[name + "_N"] = np.array(b.N)
+        for key, val in csr_arrays(K).items():
+            out[name + "_" + key] = val
+        out[name + "_b"] = f
+    mt = MeshTri()
+    b = Basis(MeshTri(mt.p[:, mt.t[:, 0]], np.arange(3).reshape(3, 1)), ElementTriP2())
+    for key, val in csr_arrays(laplace.assemble(b)).items():
+        out["tri2_single_" + key] = val
+    save("edge_cases", **out)
+
+
 if __name__ == "__main__":
-    if sys.argv[1:] == ["--generic"]:
+    if sys.argv[1:] == ["--edge"]:
+        edge_cases()
+    elif sys.argv[1:] == ["--generic"]:
         generic_cases()
     elif sys.argv[1:] == ["--facet"]:
         facet_cases()

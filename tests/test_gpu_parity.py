@@ -455,3 +455,45 @@ def test_device_csr_feeds_a_device_solver():
     full = np.zeros(b.N)
     full[I.cpu().numpy()] = u.cpu().numpy()
     np.testing.assert_allclose(full, g["u"], rtol=0, atol=1e-11)
+
+
+@pytest.mark.parametrize("name", ["unused_node", "single", "empty_subset"])
+def test_edge_cases(name):
+    """A node no cell uses (no DOF: the reference numbers DOFs up to
+    max(t)), a single cell and an empty element subset, through the public
+    API on both paths: CSR and load vector as the reference's."""
+    g = {k[len(name) + 1:]: v for k, v in golden("edge_cases").items()
+         if k.startswith(name + "_")}
+    m = F.MeshTet(g["p"], g["t"])
+    b = F.Basis(m, F.ElementTetP1(), elements=np.array([], dtype=np.int64)
+                if name == "empty_subset" else None)
+    assert b.N == int(g["N"])
+    kw = {"k": b.zero_w() + g["k"][:, None]}
+    for K in (k_laplace_mass.assemble(b, **kw),
+              _host(k_laplace_mass.assemble_torch(b, k=torch.as_tensor(g["k"], device="cuda")))):
+        assert K.shape == tuple(g["shape"])
+        np.testing.assert_array_equal(K.indptr, g["indptr"])
+        np.testing.assert_array_equal(K.indices, g["indices"])
+        if len(g["data"]):
+            *_, fro, mx = csr_diff(K.indptr, K.indices, K.data, g["indptr"], g["indices"],
+                                   g["data"], K.shape)
+            assert fro <= REL_FRO and mx <= REL_MAX
+    np.testing.assert_allclose(unit_load.assemble(b), g["b"], rtol=1e-13, atol=0)
+
+
+def _host(T):
+    return sp.csr_matrix((T.values().cpu().numpy(), T.col_indices().cpu().numpy(),
+                          T.crow_indices().cpu().numpy()), shape=tuple(T.shape))
+
+
+def test_single_tri_p2_cell():
+    g = {k[len("tri2_single_"):]: v for k, v in golden("edge_cases").items()
+         if k.startswith("tri2_single_")}
+    mt = F.MeshTri()
+    b = F.Basis(F.MeshTri(mt.p[:, mt.t[:, 0]], np.arange(3).reshape(3, 1)), F.ElementTriP2())
+    K = laplace.assemble(b)
+    np.testing.assert_array_equal(K.indptr, g["indptr"])
+    np.testing.assert_array_equal(K.indices, g["indices"])
+    *_, fro, mx = csr_diff(K.indptr, K.indices, K.data, g["indptr"], g["indices"], g["data"],
+                           K.shape)
+    assert fro <= REL_FRO and mx <= REL_MAX

@@ -175,3 +175,26 @@ def test_oracle_mixed_bases_vs_reference():
         np.testing.assert_array_equal(K.indptr, g["indptr_" + sfx])
         np.testing.assert_array_equal(K.indices, g["indices_" + sfx])
         np.testing.assert_array_equal(K.data, g["data_" + sfx])
+
+
+def _edge(name, g):
+    sub = {k[len(name) + 1:]: v for k, v in g.items() if k.startswith(name + "_")}
+    return sub
+
+
+@pytest.mark.parametrize("name", ["unused_node", "single", "empty_subset"])
+def test_edge_cases(name):
+    """A node no cell uses (no DOF: the reference numbers up to max(t)), a
+    single cell, an empty element subset -- CSR and load as the reference."""
+    g = _edge(name, load("edge_cases"))
+    m = O.OMesh(g["p"], g["t"], "tet")
+    b = O.OBasis(m, O.TetP1(), elements=np.array([], dtype=np.int64)
+                 if name == "empty_subset" else None)
+    assert b.N == int(g["N"])
+    K = O.bilinear_assemble(O.k_laplace_mass, b, k=b.zero_w() + g["k"][:, None])
+    assert K.shape == tuple(g["shape"])
+    np.testing.assert_array_equal(K.indptr, g["indptr"])
+    np.testing.assert_array_equal(K.indices, g["indices"])
+    if K.nnz:
+        check_csr(K, g)
+    np.testing.assert_allclose(O.linear_assemble(O.unit_load, b), g["b"], rtol=1e-13, atol=0)
