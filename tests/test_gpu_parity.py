@@ -497,3 +497,31 @@ def test_single_tri_p2_cell():
     *_, fro, mx = csr_diff(K.indptr, K.indices, K.data, g["indptr"], g["indices"], g["data"],
                            K.shape)
     assert fro <= REL_FRO and mx <= REL_MAX
+
+
+def test_empty_cell_and_facet_sets():
+    """No cells / no facets on every path, as the reference: an (N, N)
+    matrix without entries, a zero load, a functional of 0.0."""
+    m = F.MeshTet.init_tensor(*(np.linspace(0, 1, 3),) * 3)
+    none = np.array([], dtype=np.int64)
+
+    @F.BilinearForm
+    def gx(u, v, w):
+        return (1 + w.x[0]) * H.dot(H.grad(u), H.grad(v))
+
+    @F.Functional
+    def fx(w):
+        return w.x[0]
+
+    b = F.Basis(m, F.ElementTetP1(), elements=none)
+    for K in (gx.assemble(b), k_laplace_mass.assemble(b, k=b.zero_w())):
+        assert K.shape == (27, 27) and K.nnz == 0
+    assert fx.assemble(b) == 0.0
+    np.testing.assert_array_equal(unit_load.assemble(b), np.zeros(27))
+    fb = F.FacetBasis(m, F.ElementTetP1(), facets=none)
+    K = gx.assemble(fb)
+    assert K.shape == (27, 27) and K.nnz == 0
+    assert fx.assemble(fb) == 0.0
+    bv = F.Basis(m, F.ElementVector(F.ElementTetP2()), elements=none)
+    K = linear_elasticity(1.0, 0.5).assemble(bv)
+    assert K.shape == (375, 375) and K.nnz == 0
