@@ -13,6 +13,7 @@ import torch
 
 from . import _native as N
 from .dofs import Dofs
+from .element import ElementHex1
 from .field import DiscreteField
 from .mesh import as_mesh
 from .quadrature import get_quadrature
@@ -91,6 +92,47 @@ class CellBasis:
         self.W_dev = torch.from_numpy(np.ascontiguousarray(self.W, dtype=np.float64)).to(dev)
         # the (mesh, basis) pair the CSR pattern is built over
         self.c_mesh_pat, self.c_basis_pat = self.c_mesh, self.c_basis
+
+    @property
+    def doflocs(self):
+        """Global DOF locations (abstract_basis.py:60-71): the mesh's mapping
+        F of the element's reference DOF locations, cell by cell, written
+        into the global numbering (a DOF shared by cells takes the value of
+        the last cell and local DOF to reach it, as numpy's fancy assignment
+        does).  Host arrays, computed once; every cell of the mesh, as the
+        reference maps them all."""
+        if getattr(self, "_doflocs", None) is None:
+            p, t = self.mesh.p, self.mesh.t
+            X = self.elem.doflocs                       # (nloc, dim)
+            dim = p.shape[0]
+            if self.elem.refdom == "hex":
+                # MappingIsoparametric.F: sum over the nodes of p(t_n) phi_n(X)
+                corner = ElementHex1.doflocs
+                x = np.zeros((dim, X.shape[0], t.shape[1]))
+                for n in range(t.shape[0]):
+                    f = np.ones(X.shape[0])
+                    for a in range(3):
+                        f = f * (X[:, a] if corner[n, a] else 1.0 - X[:, a])
+                    x = x + p[:, t[n]][:, None, :] * f[None, :, None]
+            else:
+                # MappingAffine.F: sum_j A_ij X_j + b_i, A = [p(t_j+1) - p(t_0)], b = p(t_0)
+                A = np.stack([p[:, t[j + 1]] - p[:, t[0]] for j in range(dim)], axis=1)
+                x = np.einsum('ijk,lj->ilk', A, X) + p[:, t[0]][:, None, :]
+            ed = self.dofs.element_dofs
+            out = np.zeros((dim, self.N))
+            for itr in range(dim):
+                for jtr in range(ed.shape[0]):
+                    out[itr, ed[jtr]] = x[itr, jtr, :]
+            self._doflocs = out
+        return self._doflocs
+
+    def complement_dofs(self, *D):
+        """abstract_basis.py:119-123: the DOFs outside D (arrays of DOFs, DOF
+        views, or one dict of them)."""
+        if type(D[0]) is dict:
+            D = tuple(D[0][key].all() for key in D[0])
+        D = tuple(d if isinstance(d, np.ndarray) else d.all() for d in D)
+        return np.setdiff1d(np.arange(self.N), np.concatenate(D))
 
     def _run_program(self, kind, prog, out, status):
         """The generic kernel of a traced program over this basis's cells."""

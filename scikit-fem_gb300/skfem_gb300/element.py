@@ -10,6 +10,8 @@ kernels and the exact reference tensors of csrc/fem_tables.cuh).
   ElementVector skfem/element/element_vector.py
 """
 
+import numpy as np
+
 __all__ = ["Element", "ElementTriP1", "ElementTriP2", "ElementTetP1", "ElementTetP2",
            "ElementHex1", "ElementVector", "ElementH1"]
 
@@ -41,26 +43,39 @@ class ElementH1(Element):
 class ElementTriP1(ElementH1):
     family, refdom, dim, maxdeg = "TriP1", "tri", 2, 1
     nodal_dofs, nbfun_scalar = 1, 3
+    # reference DOF locations (element_tri_p1.py:13-15)
+    doflocs = np.array([[0., 0.], [1., 0.], [0., 1.]])
 
 
 class ElementTriP2(ElementH1):
     family, refdom, dim, maxdeg = "TriP2", "tri", 2, 2
     nodal_dofs, facet_dofs, nbfun_scalar = 1, 1, 6
+    # vertices, then edge midpoints (element_tri_p2.py:14-19)
+    doflocs = np.array([[0., 0.], [1., 0.], [0., 1.], [.5, 0.], [.5, .5], [0., .5]])
 
 
 class ElementTetP1(ElementH1):
     family, refdom, dim, maxdeg = "TetP1", "tet", 3, 1
     nodal_dofs, nbfun_scalar = 1, 4
+    # element_tet_p1.py:13-16
+    doflocs = np.array([[0., 0., 0.], [1., 0., 0.], [0., 1., 0.], [0., 0., 1.]])
 
 
 class ElementTetP2(ElementH1):
     family, refdom, dim, maxdeg = "TetP2", "tet", 3, 2
     nodal_dofs, edge_dofs, nbfun_scalar = 1, 1, 10
+    # vertices, then edge midpoints in the reference's edge order (element_tet_p2.py:14-23)
+    doflocs = np.array([[0., 0., 0.], [1., 0., 0.], [0., 1., 0.], [0., 0., 1.],
+                        [.5, 0., 0.], [.5, .5, 0.], [0., .5, 0.], [0., 0., .5],
+                        [.5, 0., .5], [0., .5, .5]])
 
 
 class ElementHex1(ElementH1):
     family, refdom, dim, maxdeg = "Hex1", "hex", 3, 3
     nodal_dofs, nbfun_scalar = 1, 8
+    # element_hex1.py:13-20 (node k at the corner of refdom.py's node k)
+    doflocs = np.array([[1., 1., 1.], [1., 1., 0.], [1., 0., 1.], [0., 1., 1.],
+                        [1., 0., 0.], [0., 1., 0.], [0., 0., 1.], [0., 0., 0.]])
 
 
 class ElementVector(Element):
@@ -84,6 +99,9 @@ class ElementVector(Element):
         self.facet_dofs = elem.facet_dofs * self.dim
         self.interior_dofs = elem.interior_dofs * self.dim
         self.nbfun_scalar = elem.nbfun_scalar
+        # each scalar location once per component (element_vector.py:26-29)
+        self.doflocs = np.array([elem.doflocs[i // self.dim]
+                                 for i in range(self.dim * elem.doflocs.shape[0])])
 
     @property
     def nbfun(self):

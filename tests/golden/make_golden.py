@@ -603,8 +603,31 @@ def edge_cases():
     save("edge_cases", **out)
 
 
+def doflocs_case():
+    """Basis.doflocs (abstract_basis.py:60-71) on jittered meshes."""
+    rng = np.random.default_rng(11)
+    out = {}
+    meshes = {"tri": MeshTri.init_tensor(np.linspace(0, 1, 5), np.linspace(0, 1, 4)),
+              "tet": MeshTet.init_tensor(*(np.linspace(0, 1, 4),) * 3),
+              "hex": MeshHex.init_tensor(*(np.linspace(0, 1, 4),) * 3)}
+    elems = {"tri": (ElementTriP1, ElementTriP2), "tet": (ElementTetP1, ElementTetP2),
+             "hex": (ElementHex1,)}
+    for kind, m0 in meshes.items():
+        p = m0.p + rng.uniform(-0.05, 0.05, m0.p.shape)
+        m = type(m0)(p, m0.t)
+        out[kind + "_p"] = m.p
+        out[kind + "_t"] = m.t
+        for E in elems[kind]:
+            for vec in (0, 1):
+                b = Basis(m, ElementVector(E()) if vec else E())
+                out["%s_%s_%d" % (kind, E.__name__, vec)] = b.doflocs
+    save("doflocs", **out)
+
+
 if __name__ == "__main__":
-    if sys.argv[1:] == ["--edge"]:
+    if sys.argv[1:] == ["--doflocs"]:
+        doflocs_case()
+    elif sys.argv[1:] == ["--edge"]:
         edge_cases()
     elif sys.argv[1:] == ["--generic"]:
         generic_cases()

@@ -525,3 +525,36 @@ def test_empty_cell_and_facet_sets():
     bv = F.Basis(m, F.ElementVector(F.ElementTetP2()), elements=none)
     K = linear_elasticity(1.0, 0.5).assemble(bv)
     assert K.shape == (375, 375) and K.nnz == 0
+
+
+PATCH_CASES = [
+    # (mesh, element, exact harmonic functions the element reproduces)
+    (lambda: F.MeshTri.init_tensor(*(np.linspace(0, 1, 9),) * 2), F.ElementTriP1,
+     [lambda x: 1 + x[0] + 2 * x[1]]),
+    (lambda: F.MeshTri.init_tensor(*(np.linspace(0, 1, 9),) * 2), F.ElementTriP2,
+     [lambda x: 1 + x[0] * x[1], lambda x: x[0] ** 2 - x[1] ** 2 + x[0]]),
+    (lambda: F.MeshTet.init_tensor(*(np.linspace(0, 1, 5),) * 3), F.ElementTetP1,
+     [lambda x: 1 + x[0] - x[1] + 3 * x[2]]),
+    (lambda: F.MeshTet.init_tensor(*(np.linspace(0, 1, 5),) * 3), F.ElementTetP2,
+     [lambda x: 1 + x[0] * x[1] + x[1] * x[2], lambda x: x[0] ** 2 - x[2] ** 2]),
+    (lambda: F.MeshHex.init_tensor(*(np.linspace(0, 1, 9),) * 3), F.ElementHex1,
+     [lambda x: 1 + x[0] * x[1] * x[2], lambda x: 1 + x[0] * x[1] + x[1] * x[2] + x[0]]),
+]
+
+
+@pytest.mark.parametrize("mesh,elem,funs", PATCH_CASES,
+                         ids=[c[1].__name__ for c in PATCH_CASES])
+def test_patch_exact_solutions(mesh, elem, funs):
+    """tests/test_manufactured.py:142-232 of the reference: Laplace with the
+    exact values of a harmonic function the element holds on the boundary
+    reproduces it inside to 1e-10."""
+    import scipy.sparse.linalg as spla
+    b = F.Basis(mesh(), elem())
+    A = laplace.assemble(b)
+    D = b.get_dofs().all()
+    I = b.complement_dofs(D)
+    for fun in funs:
+        x = fun(b.doflocs)
+        u = x.copy()
+        u[I] = spla.spsolve(A[I][:, I].tocsc(), -(A[I][:, D] @ x[D]))
+        assert np.max(np.abs(u - x)) <= 1e-10

@@ -112,3 +112,38 @@ def test_get_dofs_match_reference():
                 np.testing.assert_array_equal(
                     d.get_element_dofs(m.normalize_elements(lambda x: x[0] < 0.5)).flatten(),
                     g[key + "_left"])
+
+
+def _host_basis(m, elem):
+    """A CellBasis's host-side attributes only (no device arrays)."""
+    from skfem_gb300.basis import CellBasis
+    from skfem_gb300.dofs import Dofs
+    b = CellBasis.__new__(CellBasis)
+    b.mesh, b.elem, b.dofs = m, elem, Dofs(m, elem)
+    return b
+
+
+def test_doflocs_match_reference():
+    """Basis.doflocs (abstract_basis.py:60-71) on jittered meshes, bit for bit."""
+    import skfem_gb300 as F
+    g = golden("doflocs")
+    meshes = {"tri": F.MeshTri, "tet": F.MeshTet, "hex": F.MeshHex}
+    elems = {"tri": (F.ElementTriP1, F.ElementTriP2), "tet": (F.ElementTetP1, F.ElementTetP2),
+             "hex": (F.ElementHex1,)}
+    for kind, cls in meshes.items():
+        m = cls(g[kind + "_p"], g[kind + "_t"])
+        for E in elems[kind]:
+            for vec in (0, 1):
+                b = _host_basis(m, F.ElementVector(E()) if vec else E())
+                np.testing.assert_array_equal(b.doflocs, g["%s_%s_%d" % (kind, E.__name__, vec)],
+                                              err_msg="%s %s %d" % (kind, E.__name__, vec))
+
+
+def test_complement_dofs():
+    import skfem_gb300 as F
+    m = F.MeshTri.init_tensor(np.linspace(0, 1, 4), np.linspace(0, 1, 3))
+    b = _host_basis(m, F.ElementTriP1())
+    D = np.array([0, 3, 5])
+    np.testing.assert_array_equal(b.complement_dofs(D), np.setdiff1d(np.arange(b.N), D))
+    np.testing.assert_array_equal(b.complement_dofs(np.array([1]), np.array([2, 7])),
+                                  np.setdiff1d(np.arange(b.N), [1, 2, 7]))
