@@ -44,11 +44,12 @@ def main():
     open(path, "w").write("\n".join(out))
     # the same rules for the Python side (Basis.X / Basis.W)
     py = ['"""Generated by csrc/gen_refquad.py from reference-recorded fixtures (do not',
-          'edit): scikit-fem\'s triangle / tetrahedron quadrature rules of orders 1-4,',
+          'edit): scikit-fem\'s triangle (orders 1-19) / tetrahedron (1-9) quadrature rules,',
           'its line rules of orders 1-10 and its default hexahedral rule, bit-exact, as',
           'hexadecimal floats."""', "",
           "RULES = {"]
-    for key in sorted(k[:-2] for k in q if k.endswith("_X")):
+    for key in sorted((k[:-2] for k in q if k.endswith("_X")),
+                      key=lambda k: (k[:3], int(k[3:]))):
         X, W = q[key + "_X"], q[key + "_W"]
         py.append("    %r: (%r,\n           %r)," % (
             key, [[float(v).hex() for v in row] for row in X], [float(v).hex() for v in W]))

@@ -205,19 +205,25 @@ def main():
     dofs_case()
     poisson_case()
 
-    # quadrature rules the configs use, exactly as the reference tabulates them
-    from skfem.quadrature import get_quadrature_tet, get_quadrature_tri
-    rules = {}
-    for o in (1, 2, 3, 4):
-        X, W = get_quadrature_tri(o)
-        rules["tri%d_X" % o], rules["tri%d_W" % o] = X, W
-        X, W = get_quadrature_tet(o)
-        rules["tet%d_X" % o], rules["tet%d_W" % o] = X, W
-    save("quadrature_rules", **rules)
+    quadrature_rules()
 
     with open(os.path.join(OUT, "VERSION"), "w") as f:
         f.write("scikit-fem %s, numpy %s, python %s\n"
                 % (skfem.__version__, np.__version__, sys.version.split()[0]))
+
+
+def quadrature_rules():
+    """Every triangle (orders 1-19) and tetrahedron (orders 1-9) rule the
+    reference tabulates (quadrature.py:80-2836), exactly as it returns them."""
+    from skfem.quadrature import get_quadrature_tet, get_quadrature_tri
+    rules = {}
+    for o in range(1, 20):
+        X, W = get_quadrature_tri(o)
+        rules["tri%d_X" % o], rules["tri%d_W" % o] = X, W
+    for o in range(1, 10):
+        X, W = get_quadrature_tet(o)
+        rules["tet%d_X" % o], rules["tet%d_W" % o] = X, W
+    save("quadrature_rules", **rules)
 
 
 def generic_cases():
@@ -625,7 +631,9 @@ def doflocs_case():
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] == ["--doflocs"]:
+    if sys.argv[1:] == ["--quadrature"]:
+        quadrature_rules()
+    elif sys.argv[1:] == ["--doflocs"]:
         doflocs_case()
     elif sys.argv[1:] == ["--edge"]:
         edge_cases()

@@ -558,3 +558,38 @@ def test_patch_exact_solutions(mesh, elem, funs):
         u = x.copy()
         u[I] = spla.spsolve(A[I][:, I].tocsc(), -(A[I][:, D] @ x[D]))
         assert np.max(np.abs(u - x)) <= 1e-10
+
+
+@pytest.mark.parametrize("elem,rate", [(F.ElementTriP1, 2.0), (F.ElementTriP2, 3.0)],
+                         ids=["TriP1", "TriP2"])
+def test_convergence_rate(elem, rate):
+    """tests/test_convergence.py of the reference, on the GPU path end to
+    end: -lap u = f with u = sin(pi x) sin(pi y) (a load of w.x, the generic
+    kernels), the L2 error by a Functional of the interpolated solution;
+    the rate over three halvings of h is the element's."""
+    import scipy.sparse.linalg as spla
+
+    @F.LinearForm
+    def load(v, w):
+        x = w.x
+        return 2 * np.pi ** 2 * np.sin(np.pi * x[0]) * np.sin(np.pi * x[1]) * v
+
+    @F.Functional
+    def l2err(w):
+        x = w.x
+        return (w["uh"] - np.sin(np.pi * x[0]) * np.sin(np.pi * x[1])) ** 2
+
+    errs, hs = [], []
+    for n in (8, 16, 32):
+        m = F.MeshTri.init_tensor(*(np.linspace(0, 1, n + 1),) * 2)
+        b = F.Basis(m, elem(), intorder=6)
+        A = laplace.assemble(b)
+        f = load.assemble(b)
+        D = b.get_dofs().all()
+        I = b.complement_dofs(D)
+        u = np.zeros(b.N)
+        u[I] = spla.spsolve(A[I][:, I].tocsc(), f[I])
+        errs.append(np.sqrt(l2err.assemble(b, uh=b.interpolate(u))))
+        hs.append(1.0 / n)
+    rates = np.log(np.array(errs[:-1]) / np.array(errs[1:])) / np.log(2.0)
+    assert np.all(np.abs(rates - rate) < 0.15), rates
