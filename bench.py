@@ -37,7 +37,8 @@ METRIC = "elements/s & %HBM roofline: plain vs adjoint/batched assemble, rel err
 UNIT = "elements/s"
 
 # algorithmic bytes per element of a steady-state TetP1 assembly
-# (element ids 16 B + coefficient 8 B) + coordinates + CSR values, see the design doc
+# (element ids 16 B + coefficient 8 B) + coordinates + CSR values, which is
+# the minimum one pass has to move (algorithmic_bytes below)
 # DRAM bytes per cell of one steady-state TetP1 step, from the ncu capture on
 # the 61^3-node cube: local kernel on the cached geometry + segmented sum
 LOCAL_B_PER_CELL = 233.0

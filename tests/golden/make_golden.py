@@ -73,7 +73,7 @@ def main():
     save("tri_default_mass", p=m.p, t=m.t, element_dofs=ib.element_dofs,
          X=ib.X, W=ib.W, **csr_arrays(mass.assemble(ib)))
 
-    # 2. TriP1 Laplace + unit load on a 16x16 tensor mesh (configs[0] shape)
+    # 2. TriP1 Laplace + unit load on a 16x16 tensor mesh (the CPU-sized Poisson case)
     m = MeshTri.init_tensor(np.linspace(0, 1, 17), np.linspace(0, 1, 17))
     ib = Basis(m, ElementTriP1())
     save("tri_p1_laplace", p=m.p, t=m.t, element_dofs=ib.element_dofs,
@@ -119,7 +119,7 @@ def main():
     save("tri_p2_k_laplace", p=m.p, t=m.t, element_dofs=ib.element_dofs,
          X=ib.X, W=ib.W, k=k, b=unit_load.assemble(ib), **csr_arrays(K))
 
-    # 7. Hex1 theta*Laplace on the 4^3 cube (configs[3] submesh) + adjoint oracles
+    # 7. Hex1 theta*Laplace on the 4^3 cube (a small SIMP-style case) + adjoint oracles
     m = MeshHex.init_tensor(*(np.linspace(0, 1, 5),) * 3)
     ib = Basis(m, ElementHex1())
     theta = rng.uniform(0.01, 1.0, m.t.shape[1])
