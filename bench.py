@@ -226,7 +226,7 @@ def gpu_arm(args):
                                        entry.pat.handle, N.ptr(local_buf), N.ptr(status), 0, nel,
                                        sp))
         e1.record(stream)
-        N.check(lib.fem_csr_sum(entry.pat.handle, N.ptr(local_buf), N.ptr(vals), None, sp))
+        N.check(lib.fem_csr_sum_staged(entry.pat.handle, N.ptr(local_buf), N.ptr(vals), sp))
         e2.record(stream)
         torch.cuda.synchronize()
         t_local += e0.elapsed_time(e1)

@@ -254,12 +254,13 @@ void fem_pattern_drop_geometry(FemPattern* pat);
 
 /* Sizes: nnz of the CSR pattern, number of rows (N), and the bytes of the
  * local-matrix staging buffer fem_assemble needs.  The staging holds the
- * local matrices in the pattern's layout: full for scalar bases; for vector
- * bases (symmetric channel forms) only the dim x dim blocks on and above
- * the block diagonal are written, and the sums of fem_assemble,
- * fem_csr_sum_to_host and fem_assemble_to_host_pipelined read the others at
- * their transposed positions.  fem_local_matrices always writes full
- * matrices, and fem_csr_sum takes full matrices. */
+ * local matrices cell after cell in the pattern's layout: full for scalar
+ * bases; for vector bases (symmetric channel forms) only the dim x dim
+ * blocks on and above the block diagonal are written, and the sums of
+ * fem_assemble, fem_csr_sum_staged, fem_csr_sum_to_host and
+ * fem_assemble_to_host_pipelined read the others at their transposed
+ * positions.  fem_local_matrices always writes full matrices, and
+ * fem_csr_sum takes full matrices. */
 int fem_pattern_info(const FemPattern* pat, int64_t* nnz, int64_t* nrows, int64_t* staging_bytes);
 
 /* Copy the CSR structure out: indptr (nrows+1), indices (nnz), both int32. */
@@ -360,8 +361,14 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
                                    int32_t nchunks, fem_stream_t stream,
                                    fem_stream_t upload_stream, fem_stream_t copy_stream);
 
+/* Segmented sum of full local matrices, cell after cell (nelems x nbfun x
+ * nbfun, e.g. from fem_local_matrices), into CSR values. */
 int fem_csr_sum(const FemPattern* pat, const double* local, double* csr_values, int32_t* status,
                 fem_stream_t stream);
+/* The sum half of fem_assemble: staging as fem_assemble_local wrote it, in
+ * the pattern's layout, into CSR values on the device. */
+int fem_csr_sum_staged(const FemPattern* pat, const double* staging, double* csr_values,
+                       fem_stream_t stream);
 
 /* Load vector b (nrows) from local vectors (incidence order, no atomics). */
 int fem_vector_sum(const FemPattern* pat, const double* local, double* b, fem_stream_t stream);

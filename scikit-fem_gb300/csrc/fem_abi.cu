@@ -11,7 +11,6 @@
 namespace fem_fast {
 int local_matrices(const FemMesh&, const FemBasis&, const FemBilinear&, double*, int32_t*,
                    cudaStream_t);
-// cells [ebeg, eend) only (eend < 0: to the last cell)
 // cells [ebeg, eend) only (eend < 0: to the last cell); with a cell list,
 // the cells cells[ebeg .. eend-1]; upper: vector bases write only the
 // blocks on and above the block diagonal (Pattern::staging_sym)
@@ -897,6 +896,18 @@ int fem_csr_sum(const FemPattern* pat, const double* local, double* csr_values, 
   fem::Pattern P = pat->P;
   P.sum_unroll = fem::tuning_for(pat->family).sum_unroll;
   return fem::csr_sum(P, local, csr_values, (cudaStream_t)stream);
+}
+
+int fem_csr_sum_staged(const FemPattern* pat, const double* staging, double* csr_values,
+                       fem_stream_t stream) {
+  if (pat && pat->P.nnz == 0) return 0;
+  if (!pat || !staging || !csr_values) {
+    set_error(FEM_ERR_ARGUMENT, "null pattern or buffer");
+    return FEM_ERR_ARGUMENT;
+  }
+  fem::Pattern P = pat->P;
+  P.sum_unroll = fem::tuning_for(pat->family).sum_unroll;
+  return fem::csr_sum(P, staging, csr_values, (cudaStream_t)stream, 0, -1, nullptr, P.staging_sym);
 }
 
 int fem_vector_sum(const FemPattern* pat, const double* local, double* b, fem_stream_t stream) {

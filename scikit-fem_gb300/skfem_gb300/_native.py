@@ -98,6 +98,7 @@ _SIGS = {
     "fem_pattern_destroy": (None, [_P]),
     "fem_assemble": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "fem_csr_sum": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "fem_csr_sum_staged": (ctypes.c_int, [_P, _P, _P, _P]),
     "fem_vector_sum": (ctypes.c_int, [_P, _P, _P, _P]),
     "fem_assemble_vector": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "fem_bilinear_vjp": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),

@@ -67,3 +67,16 @@ def test_pipeline_and_cache_entry_points_validate_on_the_host():
     assert rc == N.FEM_ERR_ARGUMENT
     lib.fem_pattern_drop_geometry.argtypes = [V]
     lib.fem_pattern_drop_geometry(None)          # null: a no-op
+
+
+def test_staged_sum_validates_on_the_host():
+    """fem_csr_sum_staged (the sum half of fem_assemble in the pattern's
+    staging layout) refuses a null pattern before any CUDA call."""
+    from skfem_gb300 import _build, _native as N
+    lib = ctypes.CDLL(_build.build())
+    lib.fem_last_error.restype = ctypes.c_char_p
+    V = ctypes.c_void_p
+    lib.fem_csr_sum_staged.argtypes = [V, V, V, V]
+    rc = lib.fem_csr_sum_staged(None, None, None, None)
+    assert rc == N.FEM_ERR_ARGUMENT
+    assert b"null pattern" in lib.fem_last_error()
