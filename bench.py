@@ -4,10 +4,11 @@ Default workload: TetP1 k*dot(grad u, grad v) + u*v on the unit-cube tensor
 mesh with 101 nodes per axis (6,000,000 tets, 1,030,301 nodes), per-element
 k ~ lognormal(0, 1) (seeded), float64, plain forward assembly to CSR.
 
-One step = one assembly of the whole mesh into the CSR pattern (local
-matrices + fixed-order segmented sum), inputs resident in HBM.  The working
-set (staging 768 MB, CSR 122 MB) is far larger than L2, so no flush is
-needed between steps.  ``e2e`` times the public API call a user makes --
+One step = one assembly of the whole mesh into the CSR pattern (coefficient
+checks + one fixed-order fused sum over the basis's cached stiffness rows and
+unit mass matrix), inputs resident in HBM.  The working set (stiffness rows
+768 MB, CSR 122 MB) is far larger than L2, so no flush is needed between
+steps.  ``e2e`` times the public API call a user makes --
 ``form.assemble(basis, k=<(nelems, nqp) host array>)`` returning a
 scipy.sparse.csr_matrix -- including the host->device copy of k and the
 device->host copy of the CSR.
@@ -39,11 +40,18 @@ UNIT = "elements/s"
 # algorithmic bytes per element of a steady-state TetP1 assembly
 # (element ids 16 B + coefficient 8 B) + coordinates + CSR values, which is
 # the minimum one pass has to move (algorithmic_bytes below)
-# DRAM bytes per cell of one steady-state TetP1 step, from the ncu capture on
-# the 61^3-node cube: local kernel on the cached geometry + segmented sum
+# DRAM bytes per cell of one steady-state TetP1 step: the fused sum over the
+# cached stiffness rows (128 B) with its slots (32 B), incidence codes (16 B),
+# per-cell coefficient (8 B), unit-mass values read and CSR values written
+# (2 x 20.3 B) and row pointers; the coefficient checks (k 8 B, zero bits 1 B)
+FUSED_B_PER_CELL = 225.0
+CHECK_B_PER_CELL = 9.0
+TRAFFIC_B_PER_CELL = FUSED_B_PER_CELL + CHECK_B_PER_CELL
+TRAFFIC_SOURCE = "algorithmic count of the arrays each kernel streams (per cell)"
+# the two-pass kernels (local kernel on the cached geometry, staging sum),
+# from the ncu capture on the 61^3-node cube
 LOCAL_B_PER_CELL = 233.0
 SUM_B_PER_CELL = 193.9
-TRAFFIC_B_PER_CELL = LOCAL_B_PER_CELL + SUM_B_PER_CELL
 
 
 def max_over_ranks(ms, dist=None, device="cpu"):
@@ -212,15 +220,24 @@ def gpu_arm(args):
     assert int(status.item()) == 0, "assembly status %d" % int(status.item())
     assert torch.equal(vals, K0.values()), "repeated assembly not bitwise identical"
 
-    # per-kernel split (same stream, CUDA events): the step's two kernels --
-    # the local kernel on the basis's cached geometry (with the step's
-    # checks) and the segmented sum -- and, for reference, the local kernel
-    # computing its geometry from the coordinates (fem_local_matrices)
+    # per-kernel split (same stream, CUDA events): the step is the coefficient
+    # checks and the fused sum over the basis's cached stiffness rows and
+    # unit mass matrix; the same call without a status runs the fused sum
+    # alone.  For comparison, the two-pass kernels (the local kernel on the
+    # cached geometry + the staging sum, as fem_assemble_local and
+    # fem_csr_sum_staged run them) and the local kernel computing its
+    # geometry from the coordinates (fem_local_matrices)
     local_buf = entry.staging
     e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-    t_local, t_sum, t_geom = 0.0, 0.0, 0.0
+    t_local, t_sum, t_geom, t_fused = 0.0, 0.0, 0.0, 0.0
     reps = max(3, args.steps)
     for _ in range(reps):
+        e0.record(stream)
+        N.check(lib.fem_assemble(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
+                                 entry.pat.handle, N.ptr(entry.staging), N.ptr(vals), None, sp))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_fused += e0.elapsed_time(e1)
         e0.record(stream)
         N.check(lib.fem_assemble_local(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
                                        entry.pat.handle, N.ptr(local_buf), N.ptr(status), 0, nel,
@@ -240,6 +257,8 @@ def gpu_arm(args):
     t_local /= reps
     t_sum /= reps
     t_geom /= reps
+    t_fused /= reps
+    t_checks = max(0.0, ms - t_fused)
 
     # e2e: public API with host buffers (k as the reference takes it)
     kw_host = b.zero_w() + k[:, None]
@@ -277,33 +296,38 @@ def gpu_arm(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": TRAFFIC_B_PER_CELL * nel,
-                     "traffic_source": "ncu dram__bytes_read+write of the local kernel and the "
-                                       "segmented sum on the 1.3M-cell case, %.1f B/cell, "
-                                       "scaled by cells" % TRAFFIC_B_PER_CELL,
+                     "traffic_source": "%s, %.1f B/cell, scaled by cells"
+                                       % (TRAFFIC_SOURCE, TRAFFIC_B_PER_CELL),
                      "peak_kind": peak_kind, "algorithmic_bytes_per_step": B,
-                     "kernel": "whole assembly step (local + segmented sum)"},
+                     "kernel": "whole assembly step (coefficient checks + fused sum)"},
         "kernels": {
-            "local": {"kernel": "simplex_scalar_kernel<3,1,BS,cached geometry>", "ms": t_local,
-                      "dram_bytes_per_cell": LOCAL_B_PER_CELL,
-                      "gbs": LOCAL_B_PER_CELL * nel / (t_local * 1e-3) / 1e9,
-                      "frac_hbm": LOCAL_B_PER_CELL * nel / (t_local * 1e-3) / 1e9 / hbm},
-            "csr_sum": {"kernel": "csr_sum_kernel<4,U,0>", "ms": t_sum,
-                        "dram_bytes_per_cell": SUM_B_PER_CELL,
-                        "gbs": SUM_B_PER_CELL * nel / (t_sum * 1e-3) / 1e9,
-                        "frac_hbm": SUM_B_PER_CELL * nel / (t_sum * 1e-3) / 1e9 / hbm},
-            "bytes_source": "ncu dram__bytes_read+write per launch on the 1.3M-cell case, "
-                            "per cell"},
+            "fused_sum": {"kernel": "csr_scaled_kernel<4,U> (cached stiffness rows, unit mass)",
+                          "ms": t_fused, "dram_bytes_per_cell": FUSED_B_PER_CELL,
+                          "gbs": FUSED_B_PER_CELL * nel / (t_fused * 1e-3) / 1e9,
+                          "frac_hbm": FUSED_B_PER_CELL * nel / (t_fused * 1e-3) / 1e9 / hbm},
+            "coef_checks": {"kernel": "coef_status_kernel (step time minus the fused sum)",
+                            "ms": t_checks, "dram_bytes_per_cell": CHECK_B_PER_CELL},
+            "two_pass_local": {"kernel": "simplex_scalar_kernel<3,1,BS,cached geometry>",
+                               "ms": t_local, "dram_bytes_per_cell": LOCAL_B_PER_CELL,
+                               "frac_hbm": LOCAL_B_PER_CELL * nel / (t_local * 1e-3) / 1e9 / hbm},
+            "two_pass_sum": {"kernel": "csr_sum_kernel<4,U,0>", "ms": t_sum,
+                             "dram_bytes_per_cell": SUM_B_PER_CELL,
+                             "frac_hbm": SUM_B_PER_CELL * nel / (t_sum * 1e-3) / 1e9 / hbm},
+            "bytes_source": TRAFFIC_SOURCE + " (fused sum, checks); ncu dram__bytes_read+write "
+                            "per launch on the 1.3M-cell case (two-pass kernels)"},
         "fp64": {"kernel": "local matrices computing their geometry (fem_local_matrices; the "
                            "step reads the basis's cached geometry instead)",
                  "ms": t_geom, "gflops": fp64_achieved, "peak_gflops": FP64_PEAK_GFLOPS,
                  "frac": fp64_achieved / FP64_PEAK_GFLOPS},
-        "kernels_ms": {"local": t_local, "csr_sum": t_sum, "local_computing_geometry": t_geom},
+        "kernels_ms": {"fused_sum": t_fused, "coef_checks": t_checks,
+                       "two_pass_local": t_local, "two_pass_sum": t_sum,
+                       "local_computing_geometry": t_geom},
         "clocks": clk.summary(),
         "e2e": {"value": nel / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s,
                 "s_per_step_median": sorted(e2e_times)[len(e2e_times) // 2],
                 "api": "BilinearForm.assemble(basis, k=(nelems, nqp) host array) -> scipy CSR"},
-        "gpu_launches": 2 * args.steps,   # local kernel + segmented sum per step
+        "gpu_launches": 2 * args.steps,   # coefficient checks + fused sum per step
     }
     if rank == 0 and not args.no_secondary:
         res["secondary"] = secondary_workloads(args)

@@ -22,6 +22,9 @@ int local_matrices_checked(const FemMesh&, const FemBasis&, const FemBilinear&, 
 // (0: none for this family) and the kernel that fills it
 int geometry_count(const FemMesh&, const FemBasis&);
 int geometry_cache(const FemMesh&, const FemBasis&, double* geo, cudaStream_t);
+// the channel kernels' coefficient checks alone (status null: none)
+int coef_checks(const FemBilinear& f, const uint8_t* ref_bits, int32_t* status, cudaStream_t st,
+                int64_t ebeg, int64_t eend, const int32_t* cells);
 int local_vectors(const FemMesh&, const FemBasis&, const FemLinear&, double*, int32_t*,
                   cudaStream_t);
 }  // namespace fem_fast
@@ -132,6 +135,11 @@ struct FemPattern {
   // that same pointer.
   double* geo = nullptr;
   const double* geo_p = nullptr;
+  // Fused assembly cache of scalar simplex bases, built with geo (same
+  // validity): the geometry-only stiffness rows in incidence order (ninc x
+  // nbfun) and the CSR values of the unit-coefficient mass matrix (nnz).
+  double* stiff = nullptr;
+  double* mass1 = nullptr;
 };
 
 namespace {
@@ -139,6 +147,89 @@ namespace {
 // coordinate array, else null (the kernels then compute the geometry).
 const double* cached_geometry(const FemPattern* pat, const FemMesh* mesh) {
   return (pat->geo && pat->geo_p == mesh->p) ? pat->geo : nullptr;
+}
+
+// The fused assembly of one call: K = diff * sum_e k_e S_e + mass * M from
+// the pattern's cache, for scalar forms whose mass coefficient is one
+// constant (the stiffness coefficient may vary per cell).
+struct FusedSum {
+  const double* stiff;   // null: the stiffness coefficient is exactly 0
+  FemCoef diff;
+  const double* mass1;
+  double mscale;
+};
+
+bool fused_sum(const FemPattern* pat, const FemMesh* mesh, const FemBasis* basis,
+               const FemBilinear* form, FusedSum* fs) {
+  if (!pat->stiff || !pat->mass1 || !cached_geometry(pat, mesh) || basis->vector ||
+      form->mass.field)
+    return false;
+  const bool no_stiffness = !form->diff.field && form->diff.scale == 0.0;
+  fs->stiff = no_stiffness ? nullptr : pat->stiff;
+  fs->diff = form->diff;
+  fs->mass1 = pat->mass1;
+  fs->mscale = form->mass.scale;
+  return true;
+}
+
+void drop_fused(FemPattern* pat) {
+  cudaFree(pat->stiff);
+  cudaFree(pat->mass1);
+  pat->stiff = nullptr;
+  pat->mass1 = nullptr;
+}
+
+// Builds the fused cache from the geometry cache just queued: the local
+// kernels with unit stiffness (then unit mass) coefficients, the first
+// gathered into incidence order, the second summed into CSR values.
+// Without room for it the cache is left out (the calls run the local
+// kernel and the staging sum).
+int cache_fused(FemPattern* pat, const FemMesh* mesh, const FemBasis* basis, cudaStream_t st) {
+  const fem::Pattern& P = pat->P;
+  if (basis->vector || !P.has_matrix || P.nbfun_u != P.nbfun_v) return 0;
+  const int64_t nl = P.ninc * (int64_t)P.nbfun_u;
+  auto room = [&](double** ptr, int64_t n, const char* what) -> int {
+    if (*ptr) return 0;
+    cudaError_t e = cudaMalloc(ptr, std::max<int64_t>(1, n) * sizeof(double));
+    if (e == cudaSuccess) return 0;
+    *ptr = nullptr;
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      return -1;
+    }
+    return fem::check_cuda(e, what);
+  };
+  int rc = room(&pat->stiff, nl, "cudaMalloc(stiffness cache)");
+  if (!rc) rc = room(&pat->mass1, P.nnz, "cudaMalloc(mass cache)");
+  double* tmp = nullptr;
+  if (!rc) {
+    cudaError_t e = cudaMallocAsync(&tmp, std::max<int64_t>(1, nl) * sizeof(double), st);
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      tmp = nullptr;
+      rc = -1;
+    } else if (e != cudaSuccess) {
+      tmp = nullptr;
+      rc = fem::check_cuda(e, "cudaMallocAsync(fused cache scratch)");
+    }
+  }
+  if (!rc && mesh->nelems > 0) {
+    FemBilinear unit{};
+    unit.diff.scale = 1.0;
+    rc = fem_fast::local_matrices_checked(*mesh, *basis, unit, tmp, nullptr, nullptr, st, 0, -1,
+                                          nullptr, 0, pat->geo);
+    if (!rc) rc = fem::incidence_rows(P, tmp, pat->stiff, st);
+    FemBilinear mass{};
+    mass.mass.scale = 1.0;
+    if (!rc) rc = fem_fast::local_matrices_checked(*mesh, *basis, mass, tmp, nullptr, nullptr, st,
+                                                   0, -1, nullptr, 0, pat->geo);
+    fem::Pattern Q = P;
+    Q.sum_unroll = fem::tuning_for(pat->family).sum_unroll;
+    if (!rc) rc = fem::csr_sum(Q, tmp, pat->mass1, st);
+  }
+  if (tmp) cudaFreeAsync(tmp, st);
+  if (rc) drop_fused(pat);
+  return rc < 0 ? 0 : rc;
 }
 }  // namespace
 
@@ -385,6 +476,7 @@ void fem_pattern_destroy(FemPattern* pat) {
   cudaFree(pat->coef_bits);
   cudaFree(pat->plan_cells);
   cudaFree(pat->geo);
+  drop_fused(pat);
   delete pat;
 }
 
@@ -414,8 +506,10 @@ int fem_pattern_cache_geometry(FemPattern* pat, const FemMesh* mesh, const FemBa
       return fem::check_cuda(e, "cudaMalloc(geometry cache)");
     }
   }
-  pat->geo_p = nullptr;  // not valid until the kernel below has been queued
+  pat->geo_p = nullptr;  // not valid until the kernels below have been queued
   rc = fem_fast::geometry_cache(*mesh, *basis, pat->geo, st);
+  if (rc) return rc;
+  rc = cache_fused(pat, mesh, basis, st);
   if (rc) return rc;
   pat->geo_p = mesh->p;
   return 0;
@@ -426,6 +520,7 @@ void fem_pattern_drop_geometry(FemPattern* pat) {
   cudaFree(pat->geo);
   pat->geo = nullptr;
   pat->geo_p = nullptr;
+  drop_fused(pat);
 }
 
 int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
@@ -443,6 +538,15 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
     return FEM_ERR_ARGUMENT;
   }
   cudaStream_t st = (cudaStream_t)stream;
+  FusedSum fs;
+  if (fused_sum(pat, mesh, basis, form, &fs)) {
+    // the coefficient checks, then one fused sum over the cached matrices
+    rc = fem_fast::coef_checks(*form, pat->coef_bits, status, st, 0, mesh->nelems, nullptr);
+    if (rc) return rc;
+    fem::Pattern P = pat->P;
+    P.sum_unroll = fem::tuning_for(basis->family).sum_unroll;
+    return fem::csr_sum_scaled(P, fs.stiff, fs.diff, fs.mass1, fs.mscale, csr_values, st);
+  }
   // the local kernel also compares each element's coefficient zero bits
   // with the pattern's (FEM_ERR_STALE_PATTERN)
   rc = fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
@@ -499,12 +603,15 @@ std::vector<int64_t> row_ranges(const std::vector<int32_t>& ip, int64_t nrows, i
   return b;
 }
 
-// Sums rows [row0, row1) and queues their values' copy to the host on cs
+// Sums rows [row0, row1) -- from the staging, or fused from the pattern's
+// cache when fs is given -- and queues their values' copy to the host on cs
 // behind the sum.
 int sum_rows_to_host(const fem::Pattern& P, const std::vector<int32_t>& ip, const double* staging,
                      double* csr_values, double* host_values, int64_t row0, int64_t row1,
-                     cudaStream_t st, cudaStream_t cs) {
-  int rc = fem::csr_sum(P, staging, csr_values, st, row0, row1, nullptr, P.staging_sym);
+                     cudaStream_t st, cudaStream_t cs, const FusedSum* fs = nullptr) {
+  int rc = fs ? fem::csr_sum_scaled(P, fs->stiff, fs->diff, fs->mass1, fs->mscale, csr_values, st,
+                                    row0, row1)
+              : fem::csr_sum(P, staging, csr_values, st, row0, row1, nullptr, P.staging_sym);
   if (rc) return rc;
   const int64_t a = ip[row0], b = ip[row1];
   if (b > a) {
@@ -800,6 +907,8 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
   const std::vector<int64_t>& cb = pat->plan_bounds;
   const std::vector<int64_t>& done = pat->plan_rows;
   const int32_t* cells = pat->plan_cells;
+  FusedSum fs;
+  const bool fused = fused_sum(pat, mesh, basis, form, &fs);
   std::vector<cudaEvent_t> evs;
   auto event = [&](cudaEvent_t* ev) -> cudaError_t {
     cudaError_t e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
@@ -847,10 +956,12 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
       }
     }
     if (cb[c + 1] > cb[c]) {
-      rc = fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
-                                            status ? pat->coef_bits : nullptr, status, st,
-                                            cb[c], cb[c + 1], cells, pat->P.staging_sym > 0,
-                                            cached_geometry(pat, mesh));
+      rc = fused ? fem_fast::coef_checks(*form, pat->coef_bits, status, st, cb[c], cb[c + 1], cells)
+                 : fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
+                                                    status ? pat->coef_bits : nullptr, status, st,
+                                                    cb[c], cb[c + 1], cells,
+                                                    pat->P.staging_sym > 0,
+                                                    cached_geometry(pat, mesh));
       if (rc) {
         release();
         return rc;
@@ -860,7 +971,7 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
     const int64_t row1 = done[c];
     if (row1 > row) {
       rc = sum_rows_to_host(P, pat->host_indptr, staging, csr_values, host_values, row, row1, st,
-                            cs);
+                            cs, fused ? &fs : nullptr);
       if (rc) {
         release();
         return rc;

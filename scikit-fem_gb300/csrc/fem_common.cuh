@@ -159,6 +159,18 @@ Tuning tuning_for(int family);
 int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st,
             int64_t row0 = 0, int64_t row1 = -1, int32_t* check_status = nullptr, int sym = 0);
 
+// Fused assembly of a scalar form k_e * S_e + mscale * M on cached geometry
+// (rows [row0, row1)): stiff = the cells' geometry-only stiffness rows in
+// incidence order (incidence_rows), mass1 = the CSR values of the
+// unit-coefficient mass matrix (null: no mass part); the stiffness factor
+// is diff (scale and per-cell field).
+int csr_sum_scaled(const Pattern& P, const double* stiff, const FemCoef& diff,
+                   const double* mass1, double mscale, double* vals, cudaStream_t st,
+                   int64_t row0 = 0, int64_t row1 = -1);
+// Element-major full local rows (nelems x nbfun x nbfun) into incidence
+// order (ninc x nbfun) for csr_sum_scaled.
+int incidence_rows(const Pattern& P, const double* local, double* out, cudaStream_t st);
+
 int basis_nb_scalar(int family);
 int basis_dim(int family);
 

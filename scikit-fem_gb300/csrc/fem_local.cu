@@ -834,6 +834,31 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
   return 0;
 }
 
+// The coefficient checks of the channel kernels (coef_status) without the
+// local matrices, for assemblies that take the matrices from a cache: cells
+// [ebeg, eend) (positions of `cells` when it is given).
+__global__ void coef_status_kernel(FemBilinear f, const uint8_t* __restrict__ ref_bits,
+                                   int32_t* __restrict__ status, const int32_t* __restrict__ cells,
+                                   int64_t ebeg, int64_t eend) {
+  int32_t flags = 0;
+  for (int64_t pos = ebeg + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < eend;
+       pos += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = cell_at(cells, pos);
+    flags |= coef_status(f, e, ref_byte(ref_bits, e));
+  }
+  fem::publish_status(status, flags);
+}
+
+int coef_checks(const FemBilinear& f, const uint8_t* ref_bits, int32_t* status, cudaStream_t st,
+                int64_t ebeg, int64_t eend, const int32_t* cells) {
+  if (!status || eend <= ebeg) return 0;
+  // one cell per thread: every cell's loads are in flight at once
+  const int64_t grid = std::min<int64_t>(fem::ceil_div(eend - ebeg, 256), (int64_t)1 << 30);
+  coef_status_kernel<<<(unsigned)grid, 256, 0, st>>>(f, ref_bits, status, cells, ebeg, eend);
+  FEM_LAUNCH_CHECK("coef_status_kernel");
+  return 0;
+}
+
 int local_matrices(const FemMesh& m, const FemBasis& b, const FemBilinear& f, double* out,
                    int32_t* status, cudaStream_t st) {
   return local_matrices_checked(m, b, f, out, nullptr, status, st, 0, -1, nullptr, 0, nullptr);

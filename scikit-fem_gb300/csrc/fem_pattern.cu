@@ -306,6 +306,95 @@ __global__ void csr_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_
   if (CHECK && stale) atomicOr(status, 1 << FEM_ERR_STALE_PATTERN);
 }
 
+// Fused assembly of a scalar form  k_e * S_e + m * M_e  on cached geometry:
+// stiff holds every cell's geometry-only stiffness rows in incidence order
+// (row q of the incidence list at stiff + q * nu), mass1 the CSR values of
+// the unit-coefficient mass matrix.  Per CSR row the slots accumulate
+// fma(k_e, S_e[il][j], acc) in ascending (element, local row) order, as
+// csr_sum_kernel adds local entries, then the entry is
+// fma(mscale, mass1[p], dscale * acc).  field: the per-cell factor k_e of
+// the stiffness (field[e * fstride]; null: 1); stiff null: no stiffness
+// part.  The cell of an incidence code is code / nu by the same magic
+// division as the block-upper sum.
+template <int G, int U>
+__global__ void csr_scaled_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                                  const uint16_t* __restrict__ slot, const int32_t* __restrict__ indptr,
+                                  const double* __restrict__ stiff, const double* __restrict__ field,
+                                  int64_t fstride, double dscale, const double* __restrict__ mass1,
+                                  double mscale, int64_t row0, int64_t nrows, int nu, int stride,
+                                  double* __restrict__ vals, unsigned long long div_magic) {
+  extern __shared__ double acc_smem[];
+  constexpr int RPW = 32 / G;
+  const int lane = threadIdx.x & 31;
+  const int sub = lane / G;
+  const int j = lane - sub * G;
+  const int wib = threadIdx.x >> 5;
+  double* acc = acc_smem + ((size_t)wib * RPW + sub) * stride;
+  const int64_t rows_per_block = (int64_t)(blockDim.x >> 5) * RPW;
+  for (int64_t rb = row0 + (int64_t)blockIdx.x * rows_per_block; rb < nrows;
+       rb += (int64_t)gridDim.x * rows_per_block) {
+    const int64_t r = rb + (int64_t)wib * RPW + sub;
+    const bool live = r < nrows;
+    int32_t b = 0, len = 0, p0 = 0, nnz = 0;
+    if (live) {
+      b = inc_ptr[r];
+      len = stiff ? inc_ptr[r + 1] - b : 0;
+      p0 = indptr[r];
+      nnz = indptr[r + 1] - p0;
+    }
+    for (int k = j; k < nnz; k += G) acc[k] = 0.0;
+    int maxlen = len;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
+    __syncwarp();
+    for (int q0 = 0; q0 < maxlen; q0 += U) {
+      double v[U], kv[U];
+      int s[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int q = q0 + u;
+        s[u] = 0xFFFF;
+        v[u] = 0.0;
+        kv[u] = 1.0;
+        if (q < len && j < nu) {
+          const int64_t at = ((int64_t)b + q) * nu + j;
+          s[u] = __ldg(slot + at);
+          v[u] = __ldg(stiff + at);
+          if (field) {
+            const unsigned long long code = (unsigned long long)__ldg(inc + b + q);
+            const int64_t e = (int64_t)__umul64hi(code, div_magic);
+            kv[u] = __ldg(field + e * fstride);
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (s[u] != 0xFFFF) acc[s[u]] = __fma_rn(kv[u], v[u], acc[s[u]]);
+        __syncwarp();
+      }
+    }
+    for (int k = j; k < nnz; k += G) {
+      double a = dscale * acc[k];
+      if (mass1) a = __fma_rn(mscale, __ldg(mass1 + p0 + k), a);
+      vals[p0 + k] = a;
+    }
+    __syncwarp();
+  }
+}
+
+// out[q * nu + j] = local[inc[q] * nu + j]: element-major local rows
+// gathered into incidence order.
+__global__ void incidence_rows_kernel(const int32_t* __restrict__ inc, int64_t ninc, int nu,
+                                      const double* __restrict__ local, double* __restrict__ out) {
+  const int64_t n = ninc * nu;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = idx / nu;
+    const int j = (int)(idx - q * nu);
+    out[idx] = local[(int64_t)__ldg(inc + q) * nu + j];
+  }
+}
+
 __global__ void vector_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                                   const double* __restrict__ local, int64_t nrows,
                                   double* __restrict__ b) {
@@ -604,6 +693,66 @@ int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st
   return 0;
 }
 
+
+int incidence_rows(const Pattern& P, const double* local, double* out, cudaStream_t st) {
+  const int64_t n = P.ninc * (int64_t)P.nbfun_u;
+  if (n == 0) return 0;
+  incidence_rows_kernel<<<grid_for(n, 256), 256, 0, st>>>(P.inc, P.ninc, P.nbfun_u, local, out);
+  FEM_LAUNCH_CHECK("incidence_rows_kernel");
+  return 0;
+}
+
+int csr_sum_scaled(const Pattern& P, const double* stiff, const FemCoef& diff,
+                   const double* mass1, double mscale, double* vals, cudaStream_t st,
+                   int64_t row0, int64_t row1) {
+  if (!P.has_matrix || P.nbfun_u != P.nbfun_v) {
+    set_error(FEM_ERR_ARGUMENT, "the fused sum needs a square matrix pattern");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (row1 < 0 || row1 > P.nrows) row1 = P.nrows;
+  if (row0 < 0) row0 = 0;
+  if (row1 <= row0 || P.nnz == 0) return 0;
+  const int nu = P.nbfun_u;
+  if (nu > 32) {
+    set_error(FEM_ERR_UNSUPPORTED, "more than 32 local functions per cell (%d)", nu);
+    return FEM_ERR_UNSUPPORTED;
+  }
+  const int64_t ncodes = P.nelems * (int64_t)nu;
+  if (ncodes >= ((int64_t)1 << 32)) {
+    set_error(FEM_ERR_CAPACITY, "%lld incidence codes exceed 2^32", (long long)ncodes);
+    return FEM_ERR_CAPACITY;
+  }
+  const unsigned long long magic = ~0ull / (unsigned long long)nu + 1ull;
+  const double* field = diff.field;
+  const int64_t fstride = diff.stride > 1 ? diff.stride : 1;
+  const int stride = std::max(1, P.max_row_nnz);
+  const int threads = 128;
+  const int warps = threads / 32;
+  auto launch = [&](auto kern, int G) -> int {
+    const int rpw = 32 / G;
+    const size_t smem = (size_t)warps * rpw * stride * sizeof(double);
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return check_cuda(e, "csr_scaled smem");
+    }
+    const int64_t rows_per_block = (int64_t)warps * rpw;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(row1 - row0, rows_per_block),
+                                                                (int64_t)num_sms() * 64));
+    kern<<<grid, threads, smem, st>>>(P.inc_ptr, P.inc, P.slot, P.indptr, stiff, field, fstride,
+                                      diff.scale, mass1, mscale, row0, row1, nu, stride, vals,
+                                      magic);
+    return 0;
+  };
+  const int U = P.sum_unroll;
+  int rc;
+  if (nu <= 4) rc = U >= 16 ? launch(csr_scaled_kernel<4, 16>, 4) : U >= 8 ? launch(csr_scaled_kernel<4, 8>, 4) : launch(csr_scaled_kernel<4, 4>, 4);
+  else if (nu <= 8) rc = U >= 16 ? launch(csr_scaled_kernel<8, 16>, 8) : U >= 8 ? launch(csr_scaled_kernel<8, 8>, 8) : launch(csr_scaled_kernel<8, 4>, 8);
+  else if (nu <= 16) rc = U >= 8 ? launch(csr_scaled_kernel<16, 8>, 16) : launch(csr_scaled_kernel<16, 4>, 16);
+  else rc = U >= 8 ? launch(csr_scaled_kernel<32, 8>, 32) : launch(csr_scaled_kernel<32, 4>, 32);
+  if (rc) return rc;
+  FEM_LAUNCH_CHECK("csr_scaled_kernel");
+  return 0;
+}
 
 int vector_sum(const Pattern& P, const double* local, double* b, cudaStream_t st) {
   if (P.nrows == 0) return 0;

@@ -50,12 +50,18 @@ def test_split_entry_points_equal_fem_assemble(name, shuffle):
         form, kw = k_lap_mass, {"k": k}
     K = form.assemble_torch(b, **kw)
     entry = next(e for key, e in b._patterns.items() if key[0] == "bilinear")
-    ref = K.values()
     coeffs, ch, c_form = form._setup(b, None, kw)
     lib = N.lib()
     s = N.stream_ptr()
-    vals = torch.full_like(ref, np.nan)
+    # without the geometry cache (and the fused sum it enables) fem_assemble
+    # runs the local kernel and the staging sum, as the split entry points do
+    lib.fem_pattern_drop_geometry(entry.pat.handle)
+    entry.geo_key = None
+    ref = torch.full_like(K.values(), np.nan)
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    N.check(lib.fem_assemble(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
+                             entry.pat.handle, N.ptr(entry.staging), N.ptr(ref), N.ptr(status), s))
+    vals = torch.full_like(ref, np.nan)
     # whole mesh
     N.check(lib.fem_assemble_local(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
                                    entry.pat.handle, N.ptr(entry.staging), N.ptr(status), 0,
@@ -75,4 +81,53 @@ def test_split_entry_points_equal_fem_assemble(name, shuffle):
     N.check(lib.fem_csr_sum_staged(entry.pat.handle, N.ptr(entry.staging), N.ptr(vals), s))
     torch.cuda.synchronize()
     assert torch.equal(vals, ref)
+    del coeffs, ch
+
+
+@F.BilinearForm
+def lap_mass_const(u, v, w):
+    return 2.5 * H.dot(H.grad(u), H.grad(v)) + 0.75 * u * v
+
+
+@F.BilinearForm
+def mass_only(u, v, w):
+    return 3.0 * u * v
+
+
+FUSED = [(F.MeshTri, 2, 33, F.ElementTriP1), (F.MeshTri, 2, 17, F.ElementTriP2),
+         (F.MeshTet, 3, 11, F.ElementTetP1), (F.MeshTet, 3, 7, F.ElementTetP2)]
+
+
+@pytest.mark.parametrize("form", ["k_lap_mass", "lap_mass_const", "mass_only"])
+@pytest.mark.parametrize("cls,dim,n,elem", FUSED, ids=[c[3].__name__ for c in FUSED])
+def test_fused_sum_equals_staging_sum(cls, dim, n, elem, form):
+    """Scalar simplex forms with a constant mass coefficient assemble in one
+    fused sum over the basis's cached stiffness rows and unit mass matrix
+    (K = diff * sum_e k_e S_e + mass * M): equal to the local kernel plus
+    staging sum within 1e-14 of max|K| (the additions are grouped
+    differently), with the same CSR structure, and bitwise on reruns."""
+    m = cls.init_tensor(*(np.linspace(0, 1, n),) * dim)
+    p = m.p.copy()
+    inner = np.all((p > 1e-12) & (p < 1 - 1e-12), axis=0)
+    p[:, inner] += np.random.default_rng(5).uniform(-0.2 / n, 0.2 / n, (dim, int(inner.sum())))
+    b = F.Basis(cls(p, m.t), elem())
+    f = {"k_lap_mass": k_lap_mass, "lap_mass_const": lap_mass_const, "mass_only": mass_only}[form]
+    kw = {"k": torch.from_numpy(np.random.default_rng(6).lognormal(0, 1, b.nelems)).cuda()} \
+        if form == "k_lap_mass" else {}
+    Kf = f.assemble_torch(b, **kw)
+    Kf2 = f.assemble_torch(b, **kw)
+    assert torch.equal(Kf.values(), Kf2.values())
+    entry = next(e for key, e in b._patterns.items() if key[0] == "bilinear")
+    coeffs, ch, c_form = f._setup(b, None, kw)
+    lib = N.lib()
+    lib.fem_pattern_drop_geometry(entry.pat.handle)
+    entry.geo_key = None
+    ref = torch.full_like(Kf.values(), np.nan)
+    N.check(lib.fem_assemble(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
+                             entry.pat.handle, N.ptr(entry.staging), N.ptr(ref), None,
+                             N.stream_ptr()))
+    torch.cuda.synchronize()
+    a, r = Kf.values().cpu().numpy(), ref.cpu().numpy()
+    assert np.isfinite(r).all()
+    assert np.abs(a - r).max() <= 1e-14 * np.abs(r).max()
     del coeffs, ch
