@@ -835,27 +835,72 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
 }
 
 // The coefficient checks of the channel kernels (coef_status) without the
-// local matrices, for assemblies that take the matrices from a cache: cells
-// [ebeg, eend) (positions of `cells` when it is given).
-__global__ void coef_status_kernel(FemBilinear f, const uint8_t* __restrict__ ref_bits,
+// local matrices, for assemblies that take the matrices from a cache.  The
+// host splits the form once per call: the channels with a field (pointer,
+// stride, whether the scale is 0) are read per cell; the zero bits of the
+// others follow from their scales alone (const_bits).  Each cell gets the
+// status coef_status gives it: FEM_ERR_VARYING for a strided row that is not
+// constant, FEM_ERR_STALE_PATTERN when its zero bits differ from ref.
+struct FieldChecks {
+  const double* field[5];
+  int64_t stride[5];
+  int bit[5];
+  int scale_zero[5];
+  int n;
+  int const_bits;
+};
+
+__global__ void coef_fields_kernel(FieldChecks c, const uint8_t* __restrict__ ref_bits,
                                    int32_t* __restrict__ status, const int32_t* __restrict__ cells,
                                    int64_t ebeg, int64_t eend) {
-  int32_t flags = 0;
-  for (int64_t pos = ebeg + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < eend;
-       pos += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t e = cell_at(cells, pos);
-    flags |= coef_status(f, e, ref_byte(ref_bits, e));
+  const int64_t pos = ebeg + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= eend) return;
+  const int64_t e = cell_at(cells, pos);
+  const int rb = ref_byte(ref_bits, e);
+  int32_t st = 0;
+  int bits = c.const_bits;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    if (k < c.n) {
+      const int64_t s = c.stride[k];
+      const double* r = c.field[k] + (s > 1 ? e * s : e);
+      const unsigned long long v0 = fem::dbits(__ldg(r));
+      if (s > 1) {
+        bool same = true;
+        for (int64_t q = 1; q < s; ++q) {
+          const unsigned long long vq = fem::dbits(__ldg(r + q));
+          same = same && (vq == v0 || ((vq | v0) << 1) == 0ull);
+        }
+        if (!same) st |= 1 << FEM_ERR_VARYING;
+      }
+      if (c.scale_zero[k] || (v0 << 1) == 0ull) bits |= 1 << c.bit[k];
+    }
   }
-  fem::publish_status(status, flags);
+  if (rb >= 0 && bits != rb) st |= 1 << FEM_ERR_STALE_PATTERN;
+  fem::publish_status(status, st);
 }
 
 int coef_checks(const FemBilinear& f, const uint8_t* ref_bits, int32_t* status, cudaStream_t st,
                 int64_t ebeg, int64_t eend, const int32_t* cells) {
   if (!status || eend <= ebeg) return 0;
+  const FemCoef* ch[5] = {&f.diff, &f.mass, &f.lam, &f.lap, &f.tr};
+  FieldChecks c{};
+  for (int k = 0; k < 5; ++k) {
+    if (ch[k]->field) {
+      c.field[c.n] = ch[k]->field;
+      c.stride[c.n] = ch[k]->stride;
+      c.bit[c.n] = k;
+      c.scale_zero[c.n] = ch[k]->scale == 0.0;
+      ++c.n;
+    } else if (ch[k]->scale == 0.0) {
+      c.const_bits |= 1 << k;
+    }
+  }
+  if (c.n == 0 && !ref_bits) return 0;   // nothing varies per cell, nothing to compare
   // one cell per thread: every cell's loads are in flight at once
-  const int64_t grid = std::min<int64_t>(fem::ceil_div(eend - ebeg, 256), (int64_t)1 << 30);
-  coef_status_kernel<<<(unsigned)grid, 256, 0, st>>>(f, ref_bits, status, cells, ebeg, eend);
-  FEM_LAUNCH_CHECK("coef_status_kernel");
+  const int64_t grid = fem::ceil_div(eend - ebeg, 256);
+  coef_fields_kernel<<<(unsigned)grid, 256, 0, st>>>(c, ref_bits, status, cells, ebeg, eend);
+  FEM_LAUNCH_CHECK("coef_fields_kernel");
   return 0;
 }
 

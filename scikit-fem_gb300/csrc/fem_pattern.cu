@@ -314,9 +314,10 @@ __global__ void csr_sum_kernel(const int32_t* __restrict__ inc_ptr, const int32_
 // csr_sum_kernel adds local entries, then the entry is
 // fma(mscale, mass1[p], dscale * acc).  field: the per-cell factor k_e of
 // the stiffness (field[e * fstride]; null: 1); stiff null: no stiffness
-// part.  The cell of an incidence code is code / nu by the same magic
-// division as the block-upper sum.
-template <int G, int U>
+// part.  The cell of an incidence code is code / NU when the row length is
+// a compile-time NU (a shift for TetP1's 4), else code / nu by the same
+// magic division as the block-upper sum.
+template <int G, int U, int NU = 0>
 __global__ void csr_scaled_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                                   const uint16_t* __restrict__ slot, const int32_t* __restrict__ indptr,
                                   const double* __restrict__ stiff, const double* __restrict__ field,
@@ -362,7 +363,7 @@ __global__ void csr_scaled_kernel(const int32_t* __restrict__ inc_ptr, const int
           v[u] = __ldg(stiff + at);
           if (field) {
             const unsigned long long code = (unsigned long long)__ldg(inc + b + q);
-            const int64_t e = (int64_t)__umul64hi(code, div_magic);
+            const int64_t e = NU > 0 ? (int64_t)(code / NU) : (int64_t)__umul64hi(code, div_magic);
             kv[u] = __ldg(field + e * fstride);
           }
         }
@@ -745,7 +746,8 @@ int csr_sum_scaled(const Pattern& P, const double* stiff, const FemCoef& diff,
   };
   const int U = P.sum_unroll;
   int rc;
-  if (nu <= 4) rc = U >= 16 ? launch(csr_scaled_kernel<4, 16>, 4) : U >= 8 ? launch(csr_scaled_kernel<4, 8>, 4) : launch(csr_scaled_kernel<4, 4>, 4);
+  if (nu == 4) rc = U >= 16 ? launch(csr_scaled_kernel<4, 16, 4>, 4) : U >= 8 ? launch(csr_scaled_kernel<4, 8, 4>, 4) : launch(csr_scaled_kernel<4, 4, 4>, 4);
+  else if (nu < 4) rc = U >= 16 ? launch(csr_scaled_kernel<4, 16>, 4) : U >= 8 ? launch(csr_scaled_kernel<4, 8>, 4) : launch(csr_scaled_kernel<4, 4>, 4);
   else if (nu <= 8) rc = U >= 16 ? launch(csr_scaled_kernel<8, 16>, 8) : U >= 8 ? launch(csr_scaled_kernel<8, 8>, 8) : launch(csr_scaled_kernel<8, 4>, 8);
   else if (nu <= 16) rc = U >= 8 ? launch(csr_scaled_kernel<16, 8>, 16) : launch(csr_scaled_kernel<16, 4>, 16);
   else rc = U >= 8 ? launch(csr_scaled_kernel<32, 8>, 32) : launch(csr_scaled_kernel<32, 4>, 32);

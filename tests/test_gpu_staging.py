@@ -131,3 +131,50 @@ def test_fused_sum_equals_staging_sum(cls, dim, n, elem, form):
     assert np.isfinite(r).all()
     assert np.abs(a - r).max() <= 1e-14 * np.abs(r).max()
     del coeffs, ch
+
+
+def test_fused_checks_report_stale_and_varying():
+    """The coefficient checks of the fused path: a coefficient that became
+    exactly zero on some cells sets FEM_ERR_STALE_PATTERN, a per-point
+    coefficient that varies inside a cell sets FEM_ERR_VARYING, and a
+    constant per-point row (with +0.0 / -0.0 taken as equal) sets neither --
+    the same bits as the local kernel's checks without the cache."""
+    m = F.MeshTet.init_tensor(*(np.linspace(0, 1, 9),) * 3)
+    b = F.Basis(m, F.ElementTetP1())
+    rng = np.random.default_rng(7)
+    k = rng.lognormal(0, 1, b.nelems)
+    k_lap_mass.assemble_torch(b, k=torch.from_numpy(k).cuda())
+    entry = next(e for key, e in b._patterns.items() if key[0] == "bilinear")
+    nq = b.zero_w().shape[1]
+    k_zero = k.copy()
+    k_zero[[3, 17, 200]] = 0.0
+    k_vary = np.repeat(k[:, None], nq, axis=1)
+    k_vary[5, 1] *= 1.5
+    k_signed = np.repeat(k_zero[:, None], nq, axis=1)
+    k_signed[3, 2] = -0.0
+    cases = [(torch.from_numpy(k_zero).cuda(), 1 << N.FEM_ERR_STALE_PATTERN),
+             (torch.from_numpy(k_vary).cuda(), 1 << N.FEM_ERR_VARYING),
+             (torch.from_numpy(k_signed).cuda(), 1 << N.FEM_ERR_STALE_PATTERN),
+             (torch.from_numpy(k).cuda(), 0)]
+    lib = N.lib()
+    vals = torch.empty(entry.nnz, dtype=torch.float64, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    seen = []
+    for cached in (True, False):
+        if not cached:
+            lib.fem_pattern_drop_geometry(entry.pat.handle)
+            entry.geo_key = None
+        for kd, want in cases:
+            k1 = kd[:, 0].contiguous() if kd.dim() > 1 else kd
+            coeffs, ch, c_form = k_lap_mass._setup(b, None, {"k": k1})
+            if kd.dim() > 1:
+                # per-point rows (nelems, nqp), as the host path hands them over
+                c_form.diff = N.FemCoef(c_form.diff.scale, kd.data_ptr(), kd.shape[1])
+            status.zero_()
+            N.check(lib.fem_assemble(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
+                                     entry.pat.handle, N.ptr(entry.staging), N.ptr(vals),
+                                     N.ptr(status), N.stream_ptr()))
+            torch.cuda.synchronize()
+            seen.append(int(status.item()))
+            assert seen[-1] == want, (cached, want, seen[-1])
+            del coeffs, ch
