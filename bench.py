@@ -40,14 +40,15 @@ UNIT = "elements/s"
 # algorithmic bytes per element of a steady-state TetP1 assembly
 # (element ids 16 B + coefficient 8 B) + coordinates + CSR values, which is
 # the minimum one pass has to move (algorithmic_bytes below)
-# DRAM bytes per cell of one steady-state TetP1 step: the fused sum over the
-# cached stiffness rows (128 B) with its slots (32 B), incidence codes (16 B),
-# per-cell coefficient (8 B), unit-mass values read and CSR values written
-# (2 x 20.3 B) and row pointers; the coefficient checks (k 8 B, zero bits 1 B)
-FUSED_B_PER_CELL = 225.0
+# DRAM bytes per cell of one steady-state TetP1 step, from the ncu capture on
+# the 61^3-node cube (1,296,000 cells): the fused sum (cached stiffness rows
+# 128 B, slots 32 B, incidence codes 16 B, per-cell coefficient 8 B, unit
+# mass values read and CSR values written 2 x 20 B, row pointers) and the
+# coefficient checks (k 8 B, zero bits 1 B)
+FUSED_B_PER_CELL = 221.4
 CHECK_B_PER_CELL = 9.0
 TRAFFIC_B_PER_CELL = FUSED_B_PER_CELL + CHECK_B_PER_CELL
-TRAFFIC_SOURCE = "algorithmic count of the arrays each kernel streams (per cell)"
+TRAFFIC_SOURCE = "ncu dram__bytes_read+write per launch on the 1.3M-cell case, per cell"
 # the two-pass kernels (local kernel on the cached geometry, staging sum),
 # from the ncu capture on the 61^3-node cube
 LOCAL_B_PER_CELL = 233.0
@@ -301,11 +302,11 @@ def gpu_arm(args):
                      "peak_kind": peak_kind, "algorithmic_bytes_per_step": B,
                      "kernel": "whole assembly step (coefficient checks + fused sum)"},
         "kernels": {
-            "fused_sum": {"kernel": "csr_scaled_kernel<4,U> (cached stiffness rows, unit mass)",
+            "fused_sum": {"kernel": "csr_scaled_kernel<4,U,4> (cached stiffness rows, unit mass)",
                           "ms": t_fused, "dram_bytes_per_cell": FUSED_B_PER_CELL,
                           "gbs": FUSED_B_PER_CELL * nel / (t_fused * 1e-3) / 1e9,
                           "frac_hbm": FUSED_B_PER_CELL * nel / (t_fused * 1e-3) / 1e9 / hbm},
-            "coef_checks": {"kernel": "coef_status_kernel (step time minus the fused sum)",
+            "coef_checks": {"kernel": "coef_fields_kernel (step time minus the fused sum)",
                             "ms": t_checks, "dram_bytes_per_cell": CHECK_B_PER_CELL},
             "two_pass_local": {"kernel": "simplex_scalar_kernel<3,1,BS,cached geometry>",
                                "ms": t_local, "dram_bytes_per_cell": LOCAL_B_PER_CELL,
@@ -313,8 +314,7 @@ def gpu_arm(args):
             "two_pass_sum": {"kernel": "csr_sum_kernel<4,U,0>", "ms": t_sum,
                              "dram_bytes_per_cell": SUM_B_PER_CELL,
                              "frac_hbm": SUM_B_PER_CELL * nel / (t_sum * 1e-3) / 1e9 / hbm},
-            "bytes_source": TRAFFIC_SOURCE + " (fused sum, checks); ncu dram__bytes_read+write "
-                            "per launch on the 1.3M-cell case (two-pass kernels)"},
+            "bytes_source": TRAFFIC_SOURCE},
         "fp64": {"kernel": "local matrices computing their geometry (fem_local_matrices; the "
                            "step reads the basis's cached geometry instead)",
                  "ms": t_geom, "gflops": fp64_achieved, "peak_gflops": FP64_PEAK_GFLOPS,
