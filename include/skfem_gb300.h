@@ -197,10 +197,12 @@ const char* fem_version(void);
  * Launch parameters of one element family, set by the autotuner
  * (skfem_gb300.autotune): cells per CTA of the local kernel (64, 128, 256),
  * persistent grid (0: one CTA per tile; k > 0: at most k CTAs per SM,
- * grid-stride) and incidence entries loaded together by the segmented sum
- * (4, 8, 16).  Process-wide; affects later launches.
+ * grid-stride), incidence entries loaded together by the segmented sum
+ * (4, 8, 16) and lanes per CSR row of the fused sum of 4-function bases
+ * (4, or 2: each lane takes two columns).  Process-wide; affects later
+ * launches, never the values.
  */
-int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll);
+int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll, int sum_lanes);
 
 /*
  * Local (element) matrices: local[(e * nbfun + i) * nbfun + j] = K_e[i][j],

@@ -383,6 +383,77 @@ __global__ void csr_scaled_kernel(const int32_t* __restrict__ inc_ptr, const int
   }
 }
 
+// csr_scaled_kernel for 4 local functions (TetP1) with 2 lanes per CSR row:
+// lane h takes columns 2h and 2h+1 of each incidence entry -- one 16-byte
+// load of its two stiffness values, one 4-byte load of their two slots, one
+// coefficient gather for both -- so a warp keeps 16 rows' entries in
+// flight.  The two columns of an entry have distinct slots, and entries
+// are still added in ascending order (__syncwarp between them): the values
+// are bit for bit those of csr_scaled_kernel.
+template <int U>
+__global__ void csr_scaled_pair_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                                       const uint16_t* __restrict__ slot, const int32_t* __restrict__ indptr,
+                                       const double* __restrict__ stiff, const double* __restrict__ field,
+                                       int64_t fstride, double dscale, const double* __restrict__ mass1,
+                                       double mscale, int64_t row0, int64_t nrows, int stride,
+                                       double* __restrict__ vals) {
+  extern __shared__ double acc_smem[];
+  constexpr int RPW = 16;
+  const int lane = threadIdx.x & 31;
+  const int sub = lane >> 1;
+  const int h = lane & 1;
+  const int wib = threadIdx.x >> 5;
+  double* acc = acc_smem + ((size_t)wib * RPW + sub) * stride;
+  const int64_t rows_per_block = (int64_t)(blockDim.x >> 5) * RPW;
+  for (int64_t rb = row0 + (int64_t)blockIdx.x * rows_per_block; rb < nrows;
+       rb += (int64_t)gridDim.x * rows_per_block) {
+    const int64_t r = rb + (int64_t)wib * RPW + sub;
+    int32_t b = 0, len = 0, p0 = 0, nnz = 0;
+    if (r < nrows) {
+      b = inc_ptr[r];
+      len = stiff ? inc_ptr[r + 1] - b : 0;
+      p0 = indptr[r];
+      nnz = indptr[r + 1] - p0;
+    }
+    for (int k = h; k < nnz; k += 2) acc[k] = 0.0;
+    int maxlen = len;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
+    __syncwarp();
+    for (int q0 = 0; q0 < maxlen; q0 += U) {
+      double2 v[U];
+      double kv[U];
+      uint32_t s[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int q = q0 + u;
+        s[u] = 0xFFFFFFFFu;
+        v[u] = make_double2(0.0, 0.0);
+        kv[u] = 1.0;
+        if (q < len) {
+          const int64_t at = ((int64_t)b + q) * 4 + 2 * h;
+          s[u] = __ldg(reinterpret_cast<const uint32_t*>(slot + at));
+          v[u] = __ldg(reinterpret_cast<const double2*>(stiff + at));
+          if (field) kv[u] = __ldg(field + (int64_t)(__ldg(inc + b + q) >> 2) * fstride);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const uint32_t s0 = s[u] & 0xFFFFu, s1 = s[u] >> 16;
+        if (s0 != 0xFFFFu) acc[s0] = __fma_rn(kv[u], v[u].x, acc[s0]);
+        if (s1 != 0xFFFFu) acc[s1] = __fma_rn(kv[u], v[u].y, acc[s1]);
+        __syncwarp();
+      }
+    }
+    for (int k = h; k < nnz; k += 2) {
+      double a = dscale * acc[k];
+      if (mass1) a = __fma_rn(mscale, __ldg(mass1 + p0 + k), a);
+      vals[p0 + k] = a;
+    }
+    __syncwarp();
+  }
+}
+
 // out[q * nu + j] = local[inc[q] * nu + j]: element-major local rows
 // gathered into incidence order.
 __global__ void incidence_rows_kernel(const int32_t* __restrict__ inc, int64_t ninc, int nu,
@@ -746,6 +817,21 @@ int csr_sum_scaled(const Pattern& P, const double* stiff, const FemCoef& diff,
   };
   const int U = P.sum_unroll;
   int rc;
+  if (nu == 4 && P.sum_lanes == 2) {
+    auto kern = U >= 16 ? csr_scaled_pair_kernel<16> : U >= 8 ? csr_scaled_pair_kernel<8> : csr_scaled_pair_kernel<4>;
+    const size_t smem = (size_t)warps * 16 * stride * sizeof(double);
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return check_cuda(e, "csr_scaled smem");
+    }
+    const int64_t rows_per_block = (int64_t)warps * 16;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(row1 - row0, rows_per_block),
+                                                                (int64_t)num_sms() * 64));
+    kern<<<grid, threads, smem, st>>>(P.inc_ptr, P.inc, P.slot, P.indptr, stiff, field, fstride,
+                                      diff.scale, mass1, mscale, row0, row1, stride, vals);
+    FEM_LAUNCH_CHECK("csr_scaled_pair_kernel");
+    return 0;
+  }
   if (nu == 4) rc = U >= 16 ? launch(csr_scaled_kernel<4, 16, 4>, 4) : U >= 8 ? launch(csr_scaled_kernel<4, 8, 4>, 4) : launch(csr_scaled_kernel<4, 4, 4>, 4);
   else if (nu < 4) rc = U >= 16 ? launch(csr_scaled_kernel<4, 16>, 4) : U >= 8 ? launch(csr_scaled_kernel<4, 8>, 4) : launch(csr_scaled_kernel<4, 4>, 4);
   else if (nu <= 8) rc = U >= 16 ? launch(csr_scaled_kernel<8, 16>, 8) : U >= 8 ? launch(csr_scaled_kernel<8, 8>, 8) : launch(csr_scaled_kernel<8, 4>, 8);

@@ -145,7 +145,7 @@ _SIGS = {
     "fem_facet_geometry": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P, _P, _P, _P]),
     "fem_enforce": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _P, ctypes.c_int64,
                                    ctypes.c_double, _P, _P, _P, _P]),
-    "fem_set_tuning": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "fem_set_tuning": (ctypes.c_int, [ctypes.c_int] * 5),
     "fem_assemble_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
 }
 

@@ -1,5 +1,6 @@
 """Autotuner of the launch parameters (cells per CTA of the local kernel,
-persistent grid, incidence entries loaded together by the segmented sum).
+persistent grid, incidence entries loaded together by the segmented sum,
+and for TetP1 the lanes per CSR row of the fused sum).
 
 Times ``fem_assemble`` on the caller's own basis and form for every
 candidate (CUDA events, after warm-up), keeps the fastest and sets it with
@@ -20,6 +21,9 @@ CANDIDATES = {
     "persistent": (0, 4),
     "sum_unroll": (4, 8, 16),
 }
+# lanes per CSR row of the fused sum: only bases with 4 local functions have
+# the 2-lane variant
+LANES = {"TetP1": (4, 2)}
 
 
 def _cache_path():
@@ -37,7 +41,7 @@ def _key(basis):
 
 def apply(family_code, cfg):
     N.check(N.lib().fem_set_tuning(family_code, cfg["local_block"], cfg["persistent"],
-                                   cfg["sum_unroll"]))
+                                   cfg["sum_unroll"], cfg.get("sum_lanes", 4)))
 
 
 def tune(form, basis, coefs, reps=3, use_cache=True):
@@ -60,8 +64,9 @@ def tune(form, basis, coefs, reps=3, use_cache=True):
     vals = torch.empty(entry.nnz, dtype=torch.float64, device=basis.device)
     lib = N.lib()
     timings = []
-    for lb, pers, un in itertools.product(*CANDIDATES.values()):
-        cfg = {"local_block": lb, "persistent": pers, "sum_unroll": un}
+    lanes = LANES.get(basis.elem.family, (4,)) if not basis.elem.vector else (4,)
+    for lb, pers, un, ln in itertools.product(*CANDIDATES.values(), lanes):
+        cfg = {"local_block": lb, "persistent": pers, "sum_unroll": un, "sum_lanes": ln}
         apply(fam, cfg)
         s = N.stream_ptr()
 
