@@ -273,7 +273,14 @@ void fem_pattern_destroy(FemPattern* pat);
 /*
  * Steady-state assembly into an existing pattern: local matrices into
  * `staging` (fem_pattern_info bytes), then a fixed-order, atomic-free
- * segmented sum into csr_values (nnz).  status (device int32, may be NULL)
+ * segmented sum into csr_values (nnz).  When the pattern holds the fused
+ * cache of this mesh's coordinates (fem_pattern_cache_geometry, scalar
+ * simplex bases) and the form's mass coefficient is one constant, the
+ * coefficient checks and one fused sum diff * sum_e k_e S_e + mass * M
+ * replace both (staging untouched); its additions are grouped differently,
+ * so the values may differ from the two-pass ones in the last bits (within
+ * 1e-14 of max|K|), and are bitwise the same on every call and through
+ * fem_assemble_to_host_pipelined.  status (device int32, may be NULL)
  * receives FEM_ERR_STALE_PATTERN when the exact-zero structure of the local
  * matrices may have changed: some per-element coefficient became exactly
  * zero or stopped being zero since the pattern was built.  The caller then
@@ -367,8 +374,9 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
  * nbfun, e.g. from fem_local_matrices), into CSR values. */
 int fem_csr_sum(const FemPattern* pat, const double* local, double* csr_values, int32_t* status,
                 fem_stream_t stream);
-/* The sum half of fem_assemble: staging as fem_assemble_local wrote it, in
- * the pattern's layout, into CSR values on the device. */
+/* The two-pass sum: staging as fem_assemble_local wrote it, in the
+ * pattern's layout, into CSR values on the device (fem_assemble's sum when
+ * it does not take the fused path). */
 int fem_csr_sum_staged(const FemPattern* pat, const double* staging, double* csr_values,
                        fem_stream_t stream);
 
