@@ -306,7 +306,7 @@ def gpu_arm(args):
                      "peak_kind": peak_kind, "algorithmic_bytes_per_step": B,
                      "kernel": "whole assembly step (coefficient checks + fused sum)"},
         "kernels": {
-            "fused_sum": {"kernel": "csr_scaled_pair_kernel<U> or csr_scaled_kernel<4,U,4> (autotuned lanes; cached stiffness rows, unit mass)",
+            "fused_sum": {"kernel": "csr_scaled_pair_kernel<4,U> or csr_scaled_kernel<4,U,4> (autotuned columns per lane; cached stiffness rows, unit mass)",
                           "ms": t_fused, "dram_bytes_per_cell": FUSED_B_PER_CELL,
                           "gbs": FUSED_B_PER_CELL * nel / (t_fused * 1e-3) / 1e9,
                           "frac_hbm": FUSED_B_PER_CELL * nel / (t_fused * 1e-3) / 1e9 / hbm},

@@ -198,11 +198,12 @@ const char* fem_version(void);
  * (skfem_gb300.autotune): cells per CTA of the local kernel (64, 128, 256),
  * persistent grid (0: one CTA per tile; k > 0: at most k CTAs per SM,
  * grid-stride), incidence entries loaded together by the segmented sum
- * (4, 8, 16) and lanes per CSR row of the fused sum of 4-function bases
- * (4, or 2: each lane takes two columns).  Process-wide; affects later
- * launches, never the values.
+ * (4, 8, 16) and columns per lane of the fused sum (1, or 2 for bases
+ * with 4, 6 or 10 local functions: each lane then takes two columns of an
+ * incidence entry).  Process-wide; affects later launches, never the
+ * values.
  */
-int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll, int sum_lanes);
+int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll, int sum_cols);
 
 /*
  * Local (element) matrices: local[(e * nbfun + i) * nbfun + j] = K_e[i][j],

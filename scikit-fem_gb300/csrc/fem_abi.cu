@@ -346,20 +346,20 @@ const char* fem_last_error(void) { return fem::g_err.c_str(); }
 
 const char* fem_version(void) { return "skfem_gb300 0.1 (sm_103a)"; }
 
-int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll, int sum_lanes) {
+int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll, int sum_cols) {
   if (family < 1 || family > 5 || (local_block != 64 && local_block != 128 && local_block != 256) ||
       persistent < 0 || (sum_unroll != 4 && sum_unroll != 8 && sum_unroll != 16) ||
-      (sum_lanes != 2 && sum_lanes != 4)) {
+      (sum_cols != 1 && sum_cols != 2)) {
     set_error(FEM_ERR_ARGUMENT,
-              "invalid tuning (family %d, block %d, persistent %d, unroll %d, lanes %d)", family,
-              local_block, persistent, sum_unroll, sum_lanes);
+              "invalid tuning (family %d, block %d, persistent %d, unroll %d, columns %d)", family,
+              local_block, persistent, sum_unroll, sum_cols);
     return FEM_ERR_ARGUMENT;
   }
   std::lock_guard<std::mutex> lock(fem::g_tuning_mu);
   fem::g_tuning[family].local_block = local_block;
   fem::g_tuning[family].persistent = persistent;
   fem::g_tuning[family].sum_unroll = sum_unroll;
-  fem::g_tuning[family].sum_lanes = sum_lanes;
+  fem::g_tuning[family].sum_cols = sum_cols;
   return 0;
 }
 
@@ -549,7 +549,7 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
     fem::Pattern P = pat->P;
     const fem::Tuning t = fem::tuning_for(basis->family);
     P.sum_unroll = t.sum_unroll;
-    P.sum_lanes = t.sum_lanes;
+    P.sum_cols = t.sum_cols;
     return fem::csr_sum_scaled(P, fs.stiff, fs.diff, fs.mass1, fs.mscale, csr_values, st);
   }
   // the local kernel also compares each element's coefficient zero bits
@@ -910,7 +910,7 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
   fem::Pattern P = pat->P;
   const fem::Tuning tune = fem::tuning_for(pat->family);
   P.sum_unroll = tune.sum_unroll;
-  P.sum_lanes = tune.sum_lanes;
+  P.sum_cols = tune.sum_cols;
   const std::vector<int64_t>& cb = pat->plan_bounds;
   const std::vector<int64_t>& done = pat->plan_rows;
   const int32_t* cells = pat->plan_cells;

@@ -52,7 +52,7 @@ struct Pattern {
   uint16_t* slot = nullptr;     // ninc * nbfun_u
   bool has_matrix = false;
   int sum_unroll = 8;    // set from the family's tuning when the pattern is built
-  int sum_lanes = 4;     // fused sum of 4-function bases: lanes per CSR row (4 or 2)
+  int sum_cols = 1;      // fused sum: columns per lane (1, or 2 for an even row length)
   // Layout of the staging that fem_assemble_local writes for this pattern:
   // 0 full local matrices; D > 0 (vector bases of dimension D) the local
   // matrices' D x D blocks on and above the block diagonal only -- the
@@ -149,7 +149,7 @@ struct Tuning {
   int local_block = 128;  // threads (= cells) per CTA of the local kernel
   int persistent = 0;     // >0: grid capped at persistent * SMs (grid-stride)
   int sum_unroll = 8;     // incidence entries loaded together in the sum
-  int sum_lanes = 4;      // fused sum of 4-function bases: lanes per CSR row (4 or 2)
+  int sum_cols = 1;       // fused sum: columns per lane (1, or 2 for an even row length)
 };
 Tuning tuning_for(int family);
 

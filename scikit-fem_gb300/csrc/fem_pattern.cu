@@ -383,14 +383,16 @@ __global__ void csr_scaled_kernel(const int32_t* __restrict__ inc_ptr, const int
   }
 }
 
-// csr_scaled_kernel for 4 local functions (TetP1) with 2 lanes per CSR row:
+// csr_scaled_kernel for an even number NU of local functions (TetP1 4,
+// TriP2 6, TetP2 10) with two columns per lane: NU / 2 lanes per CSR row,
 // lane h takes columns 2h and 2h+1 of each incidence entry -- one 16-byte
 // load of its two stiffness values, one 4-byte load of their two slots, one
-// coefficient gather for both -- so a warp keeps 16 rows' entries in
-// flight.  The two columns of an entry have distinct slots, and entries
-// are still added in ascending order (__syncwarp between them): the values
-// are bit for bit those of csr_scaled_kernel.
-template <int U>
+// coefficient gather for both -- so a warp keeps 32 / (NU / 2) rows'
+// entries in flight (the lanes beyond them idle).  The columns of an entry
+// have distinct slots, and entries are still added in ascending order
+// (__syncwarp between them): the values are bit for bit those of
+// csr_scaled_kernel.
+template <int NU, int U>
 __global__ void csr_scaled_pair_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                                        const uint16_t* __restrict__ slot, const int32_t* __restrict__ indptr,
                                        const double* __restrict__ stiff, const double* __restrict__ field,
@@ -398,24 +400,27 @@ __global__ void csr_scaled_pair_kernel(const int32_t* __restrict__ inc_ptr, cons
                                        double mscale, int64_t row0, int64_t nrows, int stride,
                                        double* __restrict__ vals) {
   extern __shared__ double acc_smem[];
-  constexpr int RPW = 16;
+  constexpr int LPR = NU / 2;        // lanes per row
+  constexpr int RPW = 32 / LPR;      // rows per warp
+  static_assert(NU % 2 == 0 && LPR <= 32, "two columns per lane need an even row length");
   const int lane = threadIdx.x & 31;
-  const int sub = lane >> 1;
-  const int h = lane & 1;
+  const int sub = lane / LPR;        // RPW for the idle lanes
+  const int h = lane - sub * LPR;
   const int wib = threadIdx.x >> 5;
-  double* acc = acc_smem + ((size_t)wib * RPW + sub) * stride;
+  const bool row_lane = sub < RPW;
+  double* acc = acc_smem + ((size_t)wib * RPW + (row_lane ? sub : 0)) * stride;
   const int64_t rows_per_block = (int64_t)(blockDim.x >> 5) * RPW;
   for (int64_t rb = row0 + (int64_t)blockIdx.x * rows_per_block; rb < nrows;
        rb += (int64_t)gridDim.x * rows_per_block) {
     const int64_t r = rb + (int64_t)wib * RPW + sub;
     int32_t b = 0, len = 0, p0 = 0, nnz = 0;
-    if (r < nrows) {
+    if (row_lane && r < nrows) {
       b = inc_ptr[r];
       len = stiff ? inc_ptr[r + 1] - b : 0;
       p0 = indptr[r];
       nnz = indptr[r + 1] - p0;
     }
-    for (int k = h; k < nnz; k += 2) acc[k] = 0.0;
+    for (int k = h; k < nnz; k += LPR) acc[k] = 0.0;
     int maxlen = len;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
@@ -431,10 +436,10 @@ __global__ void csr_scaled_pair_kernel(const int32_t* __restrict__ inc_ptr, cons
         v[u] = make_double2(0.0, 0.0);
         kv[u] = 1.0;
         if (q < len) {
-          const int64_t at = ((int64_t)b + q) * 4 + 2 * h;
+          const int64_t at = ((int64_t)b + q) * NU + 2 * h;
           s[u] = __ldg(reinterpret_cast<const uint32_t*>(slot + at));
           v[u] = __ldg(reinterpret_cast<const double2*>(stiff + at));
-          if (field) kv[u] = __ldg(field + (int64_t)(__ldg(inc + b + q) >> 2) * fstride);
+          if (field) kv[u] = __ldg(field + (int64_t)((uint32_t)__ldg(inc + b + q) / NU) * fstride);
         }
       }
 #pragma unroll
@@ -445,7 +450,7 @@ __global__ void csr_scaled_pair_kernel(const int32_t* __restrict__ inc_ptr, cons
         __syncwarp();
       }
     }
-    for (int k = h; k < nnz; k += 2) {
+    for (int k = h; k < nnz; k += LPR) {
       double a = dscale * acc[k];
       if (mass1) a = __fma_rn(mscale, __ldg(mass1 + p0 + k), a);
       vals[p0 + k] = a;
@@ -817,14 +822,26 @@ int csr_sum_scaled(const Pattern& P, const double* stiff, const FemCoef& diff,
   };
   const int U = P.sum_unroll;
   int rc;
-  if (nu == 4 && P.sum_lanes == 2) {
-    auto kern = U >= 16 ? csr_scaled_pair_kernel<16> : U >= 8 ? csr_scaled_pair_kernel<8> : csr_scaled_pair_kernel<4>;
-    const size_t smem = (size_t)warps * 16 * stride * sizeof(double);
+  if (P.sum_cols == 2 && (nu == 4 || nu == 6 || nu == 10)) {
+    using Kern = decltype(&csr_scaled_pair_kernel<4, 4>);
+    Kern kern;
+    int rpw;
+    if (nu == 4) {
+      kern = U >= 16 ? csr_scaled_pair_kernel<4, 16> : U >= 8 ? csr_scaled_pair_kernel<4, 8> : csr_scaled_pair_kernel<4, 4>;
+      rpw = 16;
+    } else if (nu == 6) {
+      kern = U >= 16 ? csr_scaled_pair_kernel<6, 16> : U >= 8 ? csr_scaled_pair_kernel<6, 8> : csr_scaled_pair_kernel<6, 4>;
+      rpw = 10;
+    } else {
+      kern = U >= 8 ? csr_scaled_pair_kernel<10, 8> : csr_scaled_pair_kernel<10, 4>;
+      rpw = 6;
+    }
+    const size_t smem = (size_t)warps * rpw * stride * sizeof(double);
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return check_cuda(e, "csr_scaled smem");
     }
-    const int64_t rows_per_block = (int64_t)warps * 16;
+    const int64_t rows_per_block = (int64_t)warps * rpw;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(row1 - row0, rows_per_block),
                                                                 (int64_t)num_sms() * 64));
     kern<<<grid, threads, smem, st>>>(P.inc_ptr, P.inc, P.slot, P.indptr, stiff, field, fstride,

@@ -1,6 +1,7 @@
 """Autotuner of the launch parameters (cells per CTA of the local kernel,
 persistent grid, incidence entries loaded together by the segmented sum,
-and for TetP1 the lanes per CSR row of the fused sum).
+and for the scalar bases with an even number of local functions the
+columns per lane of the fused sum).
 
 Times ``fem_assemble`` on the caller's own basis and form for every
 candidate (CUDA events, after warm-up), keeps the fastest and sets it with
@@ -21,9 +22,9 @@ CANDIDATES = {
     "persistent": (0, 4),
     "sum_unroll": (4, 8, 16),
 }
-# lanes per CSR row of the fused sum: only bases with 4 local functions have
-# the 2-lane variant
-LANES = {"TetP1": (4, 2)}
+# columns per lane of the fused sum: the scalar bases with 4, 6 or 10 local
+# functions also have the two-columns-per-lane kernel
+COLS = {"TetP1": (1, 2), "TriP2": (1, 2), "TetP2": (1, 2)}
 
 
 def _cache_path():
@@ -41,7 +42,7 @@ def _key(basis):
 
 def apply(family_code, cfg):
     N.check(N.lib().fem_set_tuning(family_code, cfg["local_block"], cfg["persistent"],
-                                   cfg["sum_unroll"], cfg.get("sum_lanes", 4)))
+                                   cfg["sum_unroll"], cfg.get("sum_cols", 1)))
 
 
 def tune(form, basis, coefs, reps=3, use_cache=True):
@@ -64,9 +65,9 @@ def tune(form, basis, coefs, reps=3, use_cache=True):
     vals = torch.empty(entry.nnz, dtype=torch.float64, device=basis.device)
     lib = N.lib()
     timings = []
-    lanes = LANES.get(basis.elem.family, (4,)) if not basis.elem.vector else (4,)
-    for lb, pers, un, ln in itertools.product(*CANDIDATES.values(), lanes):
-        cfg = {"local_block": lb, "persistent": pers, "sum_unroll": un, "sum_lanes": ln}
+    cols = COLS.get(basis.elem.family, (1,)) if not basis.elem.vector else (1,)
+    for lb, pers, un, nc in itertools.product(*CANDIDATES.values(), cols):
+        cfg = {"local_block": lb, "persistent": pers, "sum_unroll": un, "sum_cols": nc}
         apply(fam, cfg)
         s = N.stream_ptr()
 

@@ -180,31 +180,36 @@ def test_fused_checks_report_stale_and_varying():
             del coeffs, ch
 
 
+COLS = [("TetP1", F.MeshTet, 3, 15, F.ElementTetP1), ("TriP2", F.MeshTri, 2, 41, F.ElementTriP2),
+        ("TetP2", F.MeshTet, 3, 8, F.ElementTetP2)]
+
+
 @pytest.mark.parametrize("form", ["k_lap_mass", "lap_mass_const"])
-def test_fused_sum_lanes_are_bitwise_equal(form):
-    """The 2-lane fused sum of TetP1 (each lane two columns of an incidence
-    entry) adds every slot's contributions in the same order as the 4-lane
-    one: equal bit for bit for every unroll, on the device path and through
-    the pipelined host path, in a shuffled cell order."""
+@pytest.mark.parametrize("fam,cls,dim,n,elem", COLS, ids=[c[0] for c in COLS])
+def test_fused_sum_columns_per_lane_are_bitwise_equal(fam, cls, dim, n, elem, form):
+    """The fused sum with two columns per lane (TetP1, TriP2, TetP2) adds
+    every slot's contributions in the same order as the one-column kernel:
+    equal bit for bit for every unroll, on the device path and through the
+    pipelined host path, in a shuffled cell order."""
     from skfem_gb300 import autotune
-    m = F.MeshTet.init_tensor(*(np.linspace(0, 1, 15),) * 3)
+    m = cls.init_tensor(*(np.linspace(0, 1, n),) * dim)
     perm = np.random.default_rng(8).permutation(m.t.shape[1])
-    b = F.Basis(F.MeshTet(m.p, np.ascontiguousarray(m.t[:, perm])), F.ElementTetP1())
+    b = F.Basis(cls(m.p, np.ascontiguousarray(m.t[:, perm])), elem())
     f = k_lap_mass if form == "k_lap_mass" else lap_mass_const
     k = np.random.default_rng(9).lognormal(0, 1, b.nelems)
     kw = {"k": torch.from_numpy(k).cuda()} if form == "k_lap_mass" else {}
     kh = {"k": b.zero_w() + k[:, None]} if form == "k_lap_mass" else {}
-    fam = N.FAMILY["TetP1"]
-    base = {"local_block": 128, "persistent": 0, "sum_unroll": 8, "sum_lanes": 4}
+    code = N.FAMILY[fam]
+    base = {"local_block": 128, "persistent": 0, "sum_unroll": 8, "sum_cols": 1}
     try:
-        autotune.apply(fam, base)
+        autotune.apply(code, base)
         ref = f.assemble_torch(b, **kw).values().clone()
         ref_host = f.assemble(b, **kh)
         for unroll in (4, 8, 16):
-            autotune.apply(fam, dict(base, sum_unroll=unroll, sum_lanes=2))
+            autotune.apply(code, dict(base, sum_unroll=unroll, sum_cols=2))
             assert torch.equal(f.assemble_torch(b, **kw).values(), ref)
             Kh = f.assemble(b, **kh)
             np.testing.assert_array_equal(Kh.data, ref_host.data)
         np.testing.assert_array_equal(ref_host.data, ref.cpu().numpy())
     finally:
-        autotune.apply(fam, base)
+        autotune.apply(code, base)
