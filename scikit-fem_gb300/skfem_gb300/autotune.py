@@ -27,6 +27,15 @@ CANDIDATES = {
 COLS = {"TetP1": (1, 2), "TriP2": (1, 2), "TetP2": (1, 2)}
 
 
+def candidates(family, vector=False):
+    """Every configuration the autotuner times for a basis of this family:
+    the product of CANDIDATES, times the columns per lane of the fused sum
+    where the family has the two-columns kernel (scalar bases only)."""
+    cols = (1,) if vector else COLS.get(family, (1,))
+    return [{"local_block": lb, "persistent": pers, "sum_unroll": un, "sum_cols": nc}
+            for lb, pers, un, nc in itertools.product(*CANDIDATES.values(), cols)]
+
+
 def _cache_path():
     root = os.environ.get("SKFEM_GB300_CACHE",
                           os.path.join(os.path.expanduser("~"), ".cache", "skfem_gb300"))
@@ -65,9 +74,7 @@ def tune(form, basis, coefs, reps=3, use_cache=True):
     vals = torch.empty(entry.nnz, dtype=torch.float64, device=basis.device)
     lib = N.lib()
     timings = []
-    cols = COLS.get(basis.elem.family, (1,)) if not basis.elem.vector else (1,)
-    for lb, pers, un, nc in itertools.product(*CANDIDATES.values(), cols):
-        cfg = {"local_block": lb, "persistent": pers, "sum_unroll": un, "sum_cols": nc}
+    for cfg in candidates(basis.elem.family, bool(basis.elem.vector)):
         apply(fam, cfg)
         s = N.stream_ptr()
 

@@ -80,3 +80,17 @@ def test_staged_sum_validates_on_the_host():
     rc = lib.fem_csr_sum_staged(None, None, None, None)
     assert rc == N.FEM_ERR_ARGUMENT
     assert b"null pattern" in lib.fem_last_error()
+
+
+def test_tuning_is_validated_on_the_host():
+    """fem_set_tuning refuses values outside its documented sets (block
+    64/128/256, unroll 4/8/16, columns per lane 1/2) and accepts the rest;
+    no CUDA call is involved."""
+    from skfem_gb300 import _build, _native as N
+    lib = ctypes.CDLL(_build.build())
+    fam = N.FAMILY["TetP1"]
+    for bad in ((fam, 96, 0, 8, 1), (fam, 128, -1, 8, 1), (fam, 128, 0, 5, 1),
+                (fam, 128, 0, 8, 3), (0, 128, 0, 8, 1), (9, 128, 0, 8, 1)):
+        assert lib.fem_set_tuning(*bad) == N.FEM_ERR_ARGUMENT
+    assert lib.fem_set_tuning(fam, 128, 0, 8, 2) == 0
+    assert lib.fem_set_tuning(fam, 128, 0, 8, 1) == 0

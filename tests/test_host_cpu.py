@@ -147,3 +147,21 @@ def test_complement_dofs():
     np.testing.assert_array_equal(b.complement_dofs(D), np.setdiff1d(np.arange(b.N), D))
     np.testing.assert_array_equal(b.complement_dofs(np.array([1]), np.array([2, 7])),
                                   np.setdiff1d(np.arange(b.N), [1, 2, 7]))
+
+
+def test_autotune_candidates_per_family():
+    """The autotuner times every block size, grid and unroll; the scalar
+    bases with an even number of local functions (TetP1, TriP2, TetP2) also
+    try two columns per lane in the fused sum, the others and every vector
+    basis only one."""
+    from skfem_gb300 import autotune
+    base = 3 * 2 * 3
+    for fam in ("TetP1", "TriP2", "TetP2"):
+        c = autotune.candidates(fam)
+        assert len(c) == 2 * base and {x["sum_cols"] for x in c} == {1, 2}
+        assert len(autotune.candidates(fam, vector=True)) == base
+    for fam in ("TriP1", "Hex1"):
+        c = autotune.candidates(fam)
+        assert len(c) == base and {x["sum_cols"] for x in c} == {1}
+    c = autotune.candidates("TetP1")
+    assert len({tuple(sorted(x.items())) for x in c}) == len(c)
