@@ -246,9 +246,15 @@ int fem_pattern_build(const FemMesh* mesh, const FemBasis* basis, const FemBilin
  * fem_assemble, fem_assemble_local and fem_assemble_to_host_pipelined then
  * read it instead of the coordinates whenever the mesh they are given has
  * the same p pointer; after changing the coordinates in place, call this
- * again (or fem_pattern_drop_geometry).  Other families, or no device
- * memory left for the cache: no cache, returns 0 (the kernels then compute
- * the geometry per call).
+ * again (or fem_pattern_drop_geometry).  With the geometry the call also
+ * builds the fused cache: every cell's unit-coefficient stiffness rows in
+ * the sum's incidence order (nelems * nbfun^2 doubles) and the CSR values
+ * of the unit-coefficient mass matrix (nnz doubles), from which
+ * fem_assemble and fem_assemble_to_host_pipelined assemble forms with a
+ * constant mass coefficient in one fused sum.  Other families, or no device
+ * memory left for a cache: that cache is left out, returns 0 (the kernels
+ * then compute the geometry per call, or run the local kernel and the
+ * staging sum).
  * Stream-ordered; not concurrently with assembly calls on the pattern.
  */
 int fem_pattern_cache_geometry(FemPattern* pat, const FemMesh* mesh, const FemBasis* basis,
