@@ -430,11 +430,14 @@ class _PatternEntry:
             self.refresh_geometry(basis, stream)
 
     def refresh_geometry(self, basis, stream=None):
-        """The channel pattern's per-cell geometry cache (scalar simplex
-        bases; CellBasis keeps its mapping the same way), recomputed when
-        the basis's coordinates changed -- in place (the tensor's version
-        counter) or replaced (its pointer).  While the mesh points at other
-        coordinates (the adjoint's X) the kernels compute the geometry."""
+        """The channel pattern's per-cell geometry cache and, with it, the
+        fused cache (unit-coefficient stiffness rows in incidence order and
+        the unit-coefficient mass matrix) of scalar simplex bases -- CellBasis
+        keeps its mapping the same way -- recomputed when the basis's
+        coordinates changed: in place (the tensor's version counter) or
+        replaced (its pointer).  While the mesh points at other coordinates
+        (the adjoint's X) the kernels compute the geometry and run the
+        two-pass assembly."""
         p = basis.p_dev
         if basis.c_mesh.p != p.data_ptr():
             return
@@ -679,11 +682,11 @@ class BilinearForm(Form):
         One native call queues the pipeline: the cells in order of their
         smallest DOF, in UPLOAD_CHUNKS chunks; per chunk the strided host
         coefficients' rows are read from host memory by a kernel on a copy
-        stream, the chunk's local kernel follows, and the rows it completes
-        are summed and copied back behind their sum -- the upload, the
-        FP64-bound local kernel and the copy of the values overlap.  Where
-        kernels cannot read pageable host memory the coefficients are
-        uploaded first."""
+        stream, the chunk's coefficient checks (with the fused cache) or
+        local kernel follow, and the rows it completes are summed and copied
+        back behind their sum -- the upload, the kernels and the copy of the
+        values overlap.  Where kernels cannot read pageable host memory the
+        coefficients are uploaded first."""
         main = torch.cuda.current_stream()
         uploaded = False
         for attempt in range(2):
