@@ -200,8 +200,14 @@ const char* fem_version(void);
  * grid-stride), incidence entries loaded together by the segmented sum
  * (4, 8, 16) and columns per lane of the fused sum (1, or 2 for bases
  * with 4, 6 or 10 local functions: each lane then takes two columns of an
- * incidence entry).  Process-wide; affects later launches, never the
- * values.
+ * incidence entry).  This table is the library's one piece of process-wide
+ * configuration besides the thread-local error message: one entry per
+ * family, written by this call (normally once, at set-up) and read under a
+ * lock when a later call launches its kernels.  It chooses launch shapes
+ * only -- every setting gives the same values bit for bit -- so calls that
+ * race with a retune still return the same results; a caller that needs
+ * fixed launch shapes per pattern sets the table once before its first
+ * assembly.
  */
 int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll, int sum_cols);
 
@@ -306,8 +312,14 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
  * file-scope device array that every GPU loading the library keeps until
  * exit; meshes needing more (nelems * nbfun^2 * 8 bytes: TetP1 up to
  * 524,288 cells) are rejected with FEM_ERR_CAPACITY.  The first call on a
- * device looks up the array's device address (make it before any stream
- * capture).  Calls share the array: calls that overlap on the GPU race.
+ * device loads the module holding the array (CUDA's lazy loading: that is
+ * when the 64 MiB are taken) and looks up its device address for the
+ * runtime's primary context; a caller whose allocator reserves the device's
+ * memory makes one warm-up call at start-up, before that reservation and
+ * before any stream capture.  Calls share the array: calls that overlap on
+ * the GPU race.  Arguments are checked as fem_assemble checks them; status
+ * (may be NULL) receives the same coefficient checks, and with NULL none
+ * runs (a stale pattern then goes unreported).
  */
 int fem_assemble_noalloc(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
                          const FemPattern* pat, double* csr_values, int32_t* status,

@@ -301,6 +301,17 @@ static int validate(const FemMesh* m, const FemBasis* b, bool generic = false) {
   return 0;
 }
 
+namespace fem {
+// The host-side argument checks of the channel entry points (fem_assemble's),
+// for the entry points in other translation units.
+int validate_mesh_basis(const FemMesh* m, const FemBasis* b) { return validate(m, b); }
+// The pattern's per-cell geometry cache when it was built from this mesh's
+// coordinates, else null.
+const double* pattern_geometry(const FemPattern* h, const FemMesh* m) {
+  return (h && m) ? cached_geometry(h, m) : nullptr;
+}
+}  // namespace fem
+
 static int read_status(int32_t* dstatus, cudaStream_t st) {
   int32_t h = 0;
   FEM_TRY_CUDA(cudaMemcpyAsync(&h, dstatus, sizeof(int32_t), cudaMemcpyDeviceToHost, st));

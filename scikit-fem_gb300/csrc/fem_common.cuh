@@ -64,6 +64,28 @@ struct Pattern {
 // ---------------------------------------------------------------- helpers
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// Stream-ordered scratch that is released on every return path of the
+// function that owns it (cudaFreeAsync on the stream it was taken on).
+struct AsyncScratch {
+  cudaStream_t st;
+  void* ptrs[8] = {};
+  int n = 0;
+  explicit AsyncScratch(cudaStream_t s) : st(s) {}
+  AsyncScratch(const AsyncScratch&) = delete;
+  AsyncScratch& operator=(const AsyncScratch&) = delete;
+  template <typename T>
+  cudaError_t alloc(T** p, size_t bytes) {
+    *p = nullptr;
+    if (n >= 8) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMallocAsync((void**)p, bytes, st);
+    if (e == cudaSuccess) ptrs[n++] = (void*)*p;
+    return e;
+  }
+  ~AsyncScratch() {
+    for (int i = n - 1; i >= 0; --i) cudaFreeAsync(ptrs[i], st);
+  }
+};
+
 inline int num_sms() {
   static int n = 0;
   if (n == 0) {

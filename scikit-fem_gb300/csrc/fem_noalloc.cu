@@ -21,20 +21,29 @@
 // kernel writes every entry the sum reads), but two calls whose kernels
 // overlap on the GPU -- on different streams, or from different host
 // threads -- race on it; callers serialise them.
+//
+// Loading: with CUDA's lazy module loading the module that holds the array
+// is loaded on a device by this entry point's first call there (the symbol
+// lookup below), which is also when its 64 MiB are taken.  A caller whose
+// allocator reserves the device's memory makes one warm-up call at
+// start-up, before that reservation and before any stream capture.  The
+// device address is cached per device ordinal, for the runtime's primary
+// context of that device (the context the CUDA runtime and torch use).
 
 #include <mutex>
 
 #include "fem_common.cuh"
 
 namespace fem_fast {
-int local_matrices(const FemMesh&, const FemBasis&, const FemBilinear&, double*, int32_t*,
-                   cudaStream_t);
+int local_matrices_checked(const FemMesh&, const FemBasis&, const FemBilinear&, double*,
+                           const uint8_t*, int32_t*, cudaStream_t, int64_t ebeg, int64_t eend,
+                           const int32_t* cells, int upper, const double* geo);
 }
 namespace fem {
 const Pattern* pattern_of(const FemPattern* h);
 const uint8_t* pattern_coef_bits(const FemPattern* h);
-int coef_check(const FemBilinear& f, int64_t n, const uint8_t* ref, int32_t* status,
-               cudaStream_t st);
+int validate_mesh_basis(const FemMesh* m, const FemBasis* b);
+const double* pattern_geometry(const FemPattern* h, const FemMesh* m);
 }  // namespace fem
 
 namespace {
@@ -72,22 +81,31 @@ int scratch_address(double** out) {
 
 }  // namespace
 
+// The two-pass path of fem_assemble -- the local kernel (on the pattern's
+// per-cell geometry cache when the mesh's coordinates are the cached ones)
+// into the full local-matrix layout, then the fixed-order sum -- with the
+// staging in the static array.  status (device int32, may be NULL): with it
+// the local kernel also runs fem_assemble's coefficient checks and reports
+// FEM_ERR_STALE_PATTERN / FEM_ERR_VARYING there; with NULL no check runs, so
+// a coefficient whose zero structure changed since the pattern was built
+// goes unreported (the values are then those of the old pattern).
 extern "C" int fem_assemble_noalloc(const FemMesh* mesh, const FemBasis* basis,
                                     const FemBilinear* form, const FemPattern* pat,
                                     double* csr_values, int32_t* status, fem_stream_t stream) {
-  if (!mesh || !basis || !form || !pat || !csr_values) {
-    fem::set_error(FEM_ERR_ARGUMENT, "null mesh, basis, form, pattern or output");
-    return FEM_ERR_ARGUMENT;
-  }
-  const int nbs = fem::basis_nb_scalar(basis->family);
-  const int dim = fem::basis_dim(basis->family);
-  if (nbs == 0 || dim != mesh->dim || basis->nbfun != (basis->vector ? nbs * dim : nbs)) {
-    fem::set_error(FEM_ERR_ARGUMENT, "Incompatible Mesh and Element");
+  int rc = fem::validate_mesh_basis(mesh, basis);
+  if (rc) return rc;
+  if (!form || !pat) {
+    fem::set_error(FEM_ERR_ARGUMENT, "null form or pattern");
     return FEM_ERR_ARGUMENT;
   }
   const fem::Pattern* P = fem::pattern_of(pat);
   if (!P->has_matrix || P->nelems != mesh->nelems || P->nbfun_v != basis->nbfun) {
     fem::set_error(FEM_ERR_ARGUMENT, "pattern does not belong to this mesh / basis");
+    return FEM_ERR_ARGUMENT;
+  }
+  // an empty pattern (no cells, or only exact zeros) takes no value buffer
+  if (!csr_values && P->nnz > 0) {
+    fem::set_error(FEM_ERR_ARGUMENT, "null output");
     return FEM_ERR_ARGUMENT;
   }
   const int64_t need = mesh->nelems * (int64_t)basis->nbfun * basis->nbfun * (int64_t)sizeof(double);
@@ -100,15 +118,14 @@ extern "C" int fem_assemble_noalloc(const FemMesh* mesh, const FemBasis* basis,
                    (long long)kNoAllocScratchBytes);
     return FEM_ERR_CAPACITY;
   }
+  if (mesh->nelems == 0) return 0;
   double* scratch = nullptr;
-  int rc = scratch_address(&scratch);
+  rc = scratch_address(&scratch);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
-  if (status && fem::pattern_coef_bits(pat) && mesh->nelems > 0) {
-    rc = fem::coef_check(*form, mesh->nelems, fem::pattern_coef_bits(pat), status, st);
-    if (rc) return rc;
-  }
-  rc = fem_fast::local_matrices(*mesh, *basis, *form, scratch, status, st);
+  rc = fem_fast::local_matrices_checked(*mesh, *basis, *form, scratch,
+                                        status ? fem::pattern_coef_bits(pat) : nullptr, status, st,
+                                        0, -1, nullptr, 0, fem::pattern_geometry(pat, mesh));
   if (rc) return rc;
   return fem::csr_sum(*P, scratch, csr_values, st);
 }

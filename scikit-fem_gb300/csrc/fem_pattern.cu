@@ -533,9 +533,10 @@ __global__ void scan_add_kernel(int32_t* __restrict__ out, int64_t n, const int3
 
 int scan_rec(const int32_t* in, int32_t* out, int64_t n, cudaStream_t st) {
   const int64_t nb = ceil_div(n, kScanBlock);
+  AsyncScratch scratch(st);
   int32_t *sums = nullptr, *offs = nullptr;
-  FEM_TRY_CUDA(cudaMallocAsync(&sums, nb * sizeof(int32_t), st));
-  FEM_TRY_CUDA(cudaMallocAsync(&offs, nb * sizeof(int32_t), st));
+  FEM_TRY_CUDA(scratch.alloc(&sums, nb * sizeof(int32_t)));
+  FEM_TRY_CUDA(scratch.alloc(&offs, nb * sizeof(int32_t)));
   scan_blocks_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(in, out, n, sums);
   FEM_LAUNCH_CHECK("scan_blocks_kernel");
   if (nb > 1) {
@@ -544,9 +545,27 @@ int scan_rec(const int32_t* in, int32_t* out, int64_t n, cudaStream_t st) {
     scan_add_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(out, n, offs);
     FEM_LAUNCH_CHECK("scan_add_kernel");
   }
-  cudaFreeAsync(sums, st);
-  cudaFreeAsync(offs, st);
   return 0;
+}
+
+// 64-bit total of n nonnegative int32 counts (one atomic per block), so that
+// a total beyond int32 is reported instead of wrapping in the scan.
+__global__ void count_total_kernel(const int32_t* __restrict__ in, int64_t n,
+                                   unsigned long long* __restrict__ total) {
+  unsigned long long s = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    s += (unsigned long long)(uint32_t)max(in[i], 0);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ unsigned long long ws[8];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long b = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += ws[w];
+    atomicAdd(total, b);
+  }
 }
 }  // namespace
 
@@ -554,9 +573,29 @@ int exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, int64_t* tota
                        cudaStream_t stream) {
   // out[0..n]: out[k] = sum(in[0..k)); out[n] = total.  `in` must hold n+1
   // entries with in[n] == 0 (callers allocate counts with one spare slot).
+  // A total beyond INT32_MAX (the int32 offsets of the reference's CSR)
+  // returns FEM_ERR_CAPACITY before any offset is written.
   if (n + 1 > INT32_MAX) {
     set_error(FEM_ERR_CAPACITY, "scan of %lld entries exceeds int32", (long long)n);
     return FEM_ERR_CAPACITY;
+  }
+  {
+    AsyncScratch scratch(stream);
+    unsigned long long* dtot = nullptr;
+    FEM_TRY_CUDA(scratch.alloc(&dtot, sizeof(unsigned long long)));
+    FEM_TRY_CUDA(cudaMemsetAsync(dtot, 0, sizeof(unsigned long long), stream));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256),
+                                                                (int64_t)num_sms() * 8));
+    count_total_kernel<<<grid, 256, 0, stream>>>(in, n, dtot);
+    FEM_LAUNCH_CHECK("count_total_kernel");
+    unsigned long long t64 = 0;
+    FEM_TRY_CUDA(cudaMemcpyAsync(&t64, dtot, sizeof(t64), cudaMemcpyDeviceToHost, stream));
+    FEM_TRY_CUDA(cudaStreamSynchronize(stream));
+    if (t64 > (unsigned long long)INT32_MAX) {
+      set_error(FEM_ERR_CAPACITY, "total of %llu entries exceeds the int32 offsets of the CSR",
+                t64);
+      return FEM_ERR_CAPACITY;
+    }
   }
   int rc = scan_rec(in, out, n + 1, stream);
   if (rc) return rc;
@@ -581,12 +620,15 @@ int build_incidence(const int32_t* dofs, int64_t nelems, int nb, int64_t nrows, 
               (long long)P->ninc);
     return FEM_ERR_CAPACITY;
   }
+  // scratch released on every return; the pattern's own arrays are
+  // released by the caller's free_pattern on failure
+  AsyncScratch scratch(st);
   int32_t *cnt = nullptr, *cursor = nullptr, *flags = nullptr;
   FEM_TRY_CUDA(cudaMallocAsync(&P->inc_ptr, (nrows + 1) * sizeof(int32_t), st));
   FEM_TRY_CUDA(cudaMallocAsync(&P->inc, std::max<int64_t>(1, P->ninc) * sizeof(int32_t), st));
-  FEM_TRY_CUDA(cudaMallocAsync(&cnt, (nrows + 1) * sizeof(int32_t), st));
-  FEM_TRY_CUDA(cudaMallocAsync(&cursor, (nrows + 1) * sizeof(int32_t), st));
-  FEM_TRY_CUDA(cudaMallocAsync(&flags, 2 * sizeof(int32_t), st));
+  FEM_TRY_CUDA(scratch.alloc(&cnt, (nrows + 1) * sizeof(int32_t)));
+  FEM_TRY_CUDA(scratch.alloc(&cursor, (nrows + 1) * sizeof(int32_t)));
+  FEM_TRY_CUDA(scratch.alloc(&flags, 2 * sizeof(int32_t)));
   FEM_TRY_CUDA(cudaMemsetAsync(cnt, 0, (nrows + 1) * sizeof(int32_t), st));
   FEM_TRY_CUDA(cudaMemsetAsync(cursor, 0, (nrows + 1) * sizeof(int32_t), st));
   FEM_TRY_CUDA(cudaMemsetAsync(flags, 0, 2 * sizeof(int32_t), st));
@@ -610,9 +652,6 @@ int build_incidence(const int32_t* dofs, int64_t nelems, int nb, int64_t nrows, 
   int32_t h[2] = {0, 0};
   FEM_TRY_CUDA(cudaMemcpyAsync(h, flags, sizeof(h), cudaMemcpyDeviceToHost, st));
   FEM_TRY_CUDA(cudaStreamSynchronize(st));
-  cudaFreeAsync(cnt, st);
-  cudaFreeAsync(cursor, st);
-  cudaFreeAsync(flags, st);
   if (h[0]) {
     set_error(FEM_ERR_ARGUMENT, "element_dofs holds an index outside [0, %lld)", (long long)nrows);
     return FEM_ERR_ARGUMENT;
@@ -646,9 +685,10 @@ int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, 
     FEM_TRY_CUDA(cudaFuncSetAttribute(row_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
   }
+  AsyncScratch scratch(st);
   int32_t *row_nnz = nullptr, *flags = nullptr;
-  FEM_TRY_CUDA(cudaMallocAsync(&row_nnz, (P->nrows + 1) * sizeof(int32_t), st));
-  FEM_TRY_CUDA(cudaMallocAsync(&flags, sizeof(int32_t), st));
+  FEM_TRY_CUDA(scratch.alloc(&row_nnz, (P->nrows + 1) * sizeof(int32_t)));
+  FEM_TRY_CUDA(scratch.alloc(&flags, sizeof(int32_t)));
   FEM_TRY_CUDA(cudaMemsetAsync(flags, 0, sizeof(int32_t), st));
   FEM_TRY_CUDA(cudaMemsetAsync(row_nnz, 0, (P->nrows + 1) * sizeof(int32_t), st));
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(P->nrows, kWarpsPerBlock),
@@ -680,8 +720,6 @@ int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, 
                                                             P->indptr, P->indices, P->slot);
     FEM_LAUNCH_CHECK("row_fill_kernel");
   }
-  cudaFreeAsync(row_nnz, st);
-  cudaFreeAsync(flags, st);
   FEM_TRY_CUDA(cudaStreamSynchronize(st));
   (void)ncols;
   P->has_matrix = true;

@@ -1,8 +1,10 @@
 """In-tree build of libskfem_gb300.so for sm_103a (GB300).
 
-Four translation units compiled in parallel with one -gencode each; the
-local-matrix kernels are compiled twice: with FMA contraction (values) and
-with ``-fmad=false`` (the exact-zero mask of the pattern build).
+The translation units of UNITS compiled in parallel with one -gencode each;
+the local-matrix kernels are compiled twice: with FMA contraction (values)
+and with ``-fmad=false`` (the exact-zero mask of the pattern build).  The
+header texts the run-time compiler embeds (fem_jit_sources.inc) are written
+into the output folder on every build, never committed.
 """
 
 import os
@@ -25,7 +27,6 @@ UNITS = [
     ("fem_local.cu", "fem_local_exact.o", ["-DFEM_EXACT", "-fmad=false"]),
     ("fem_pattern.cu", "fem_pattern.o", []),
     ("fem_vjp.cu", "fem_vjp.o", []),
-    ("fem_batched.cu", "fem_batched.o", []),
     ("fem_abi.cu", "fem_abi.o", []),
     ("fem_noalloc.cu", "fem_noalloc.o", []),
     ("fem_faithful.cu", "fem_faithful.o", ["-fmad=false"]),
@@ -79,7 +80,10 @@ def build(force=False, verbose=False):
     # could change the last bits of numpy-computed quadrature nodes.
     cc = nvcc()
     write_jit_sources()
-    units = [u for u in UNITS if os.path.exists(os.path.join(CSRC, u[0]))]
+    missing = [u[0] for u in UNITS if not os.path.exists(os.path.join(CSRC, u[0]))]
+    if missing:
+        raise RuntimeError("missing CUDA sources: %s" % ", ".join(missing))
+    units = UNITS
 
     def compile_unit(u):
         src, obj, extra = u
