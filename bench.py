@@ -4,19 +4,23 @@ Default workload: TetP1 k*dot(grad u, grad v) + u*v on the unit-cube tensor
 mesh with 101 nodes per axis (6,000,000 tets, 1,030,301 nodes), per-element
 k ~ lognormal(0, 1) (seeded), float64, plain forward assembly to CSR.
 
-One step = one assembly of the whole mesh into the CSR pattern (coefficient
-checks + one fixed-order fused sum over the basis's cached stiffness rows and
-unit mass matrix), inputs resident in HBM.  The working set (stiffness rows
-768 MB, CSR 122 MB) is far larger than L2, so no flush is needed between
-steps.  ``e2e`` times the public API call a user makes --
+One step = one plain assembly of the whole mesh into its CSR pattern, inputs
+resident in HBM: the coefficient checks, then the one-pass P1 assembly --
+each CSR row contracts the form per (cell, local row) from the basis's
+per-cell geometry cache (what CellBasis keeps of its mapping) and sums the
+contributions in a fixed order.  Nothing of an earlier call is reused: the
+form is contracted and summed every step.  The working set (geometry 528 MB,
+incidence and slots 290 MB, CSR 122 MB) is far larger than L2, so no flush
+is needed between steps.  ``e2e`` times the public API call a user makes --
 ``form.assemble(basis, k=<(nelems, nqp) host array>)`` returning a
 scipy.sparse.csr_matrix -- including the host->device copy of k and the
 device->host copy of the CSR.
 
-``--impl reference`` times the CPU oracle (a numpy restatement of
-scikit-fem's assembly, single process, its local loop split over all host
-threads as BilinearForm(nthreads=...) does) on a bounded sample of the same
-workload.
+``--impl reference`` times the CPU oracle (the numpy restatement of
+scikit-fem's assembly, its local loop split over all host threads as
+BilinearForm(nthreads=...) does) on the same 101^3 workload: each step is
+``assemble`` on a prebuilt basis, like the GPU step; one Basis + assemble
+run is reported beside it, as scikit-fem's performance.py times it.
 """
 
 import argparse
@@ -37,22 +41,17 @@ for p in (ROOT, os.path.join(ROOT, "scikit-fem_gb300")):
 METRIC = "elements/s & %HBM roofline: plain vs adjoint/batched assemble, rel err <=1e-12"
 UNIT = "elements/s"
 
-# algorithmic bytes per element of a steady-state TetP1 assembly
-# (element ids 16 B + coefficient 8 B) + coordinates + CSR values, which is
-# the minimum one pass has to move (algorithmic_bytes below)
-# DRAM bytes per cell of one steady-state TetP1 step, from the ncu capture on
-# the 61^3-node cube (1,296,000 cells): the fused sum (cached stiffness rows
-# 128 B, slots 32 B, incidence codes 16 B, per-cell coefficient 8 B, unit
-# mass values read and CSR values written 2 x 20 B, row pointers) and the
-# coefficient checks (k 8 B, zero bits 1 B)
-FUSED_B_PER_CELL = 221.4
+# DRAM bytes per cell of the kernels, from ncu captures of one launch each
+# on the 61^3-node cube (1,296,000 cells) -- the one-pass sum and the
+# coefficient checks of the step; the two-pass kernels (local kernel on the
+# cached geometry, staging sum) and the opt-in coefficient-update sum for
+# comparison.  None until a capture of that kernel exists.
+ONEPASS_B_PER_CELL = None
 CHECK_B_PER_CELL = 9.0
-TRAFFIC_B_PER_CELL = FUSED_B_PER_CELL + CHECK_B_PER_CELL
-TRAFFIC_SOURCE = "ncu dram__bytes_read+write per launch on the 1.3M-cell case, per cell"
-# the two-pass kernels (local kernel on the cached geometry, staging sum),
-# from the ncu capture on the 61^3-node cube
 LOCAL_B_PER_CELL = 233.0
 SUM_B_PER_CELL = 193.9
+FUSED_B_PER_CELL = 218.5
+TRAFFIC_SOURCE = "ncu dram__bytes_read+write of one launch on the 1.3M-cell case, per cell"
 
 
 def max_over_ranks(ms, dist=None, device="cpu"):
@@ -143,7 +142,16 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def build_workload(n_nodes, seed):
+# ------------------------------------------------------------ workloads
+# Seeded synthetic inputs of the benchmark configurations (the tests build
+# the same ones to check them against the oracle at these sizes).
+
+SEED = 20261203
+
+
+def build_workload(n_nodes, seed=SEED):
+    """TetP1 k*Laplace + mass: MeshTet.init_tensor with n_nodes per axis
+    (6 tets per cube), per-cell k ~ lognormal(0, 1)."""
     import skfem_gb300 as F
     m = F.MeshTet.init_tensor(*(np.linspace(0, 1, n_nodes),) * 3)
     rng = np.random.default_rng(seed)
@@ -151,12 +159,78 @@ def build_workload(n_nodes, seed):
     return m, k
 
 
+def tri_square(n_cells=256):
+    """TriP1 Laplace + unit load: the unit square as n x n squares, each cut
+    into two triangles."""
+    import skfem_gb300 as F
+    x = np.linspace(0, 1, n_cells + 1)
+    return F.MeshTri.init_tensor(x, x)
+
+
+def jittered_tet_cube(n_cells, seed=SEED + 3):
+    """Vector TetP2 elasticity mesh: n^3 cubes x 6 tets, interior nodes
+    moved uniformly by up to 0.2 h per axis."""
+    import skfem_gb300 as F
+    m = F.MeshTet.init_tensor(*(np.linspace(0, 1, n_cells + 1),) * 3)
+    p = m.p.copy()
+    inner = np.all((p > 1e-12) & (p < 1 - 1e-12), axis=0)
+    rng = np.random.default_rng(seed)
+    p[:, inner] += rng.uniform(-0.2 / n_cells, 0.2 / n_cells, size=(3, int(inner.sum())))
+    return F.MeshTet(p, m.t)
+
+
+def hex_cube_workload(n_cells, seed=SEED + 4, jitter=0.0):
+    """Hex1 theta*Laplace: n^3 hexahedra (interior nodes jittered by up to
+    jitter * h per axis when jitter > 0: isoparametric cells), theta ~
+    U[0.01, 1] per cell, adjoint vectors w, u ~ N(0, 1)."""
+    import skfem_gb300 as F
+    m = F.MeshHex.init_tensor(*(np.linspace(0, 1, n_cells + 1),) * 3)
+    rng = np.random.default_rng(seed)
+    if jitter > 0:
+        p = m.p.copy()
+        inner = np.all((p > 1e-12) & (p < 1 - 1e-12), axis=0)
+        p[:, inner] += rng.uniform(-jitter / n_cells, jitter / n_cells,
+                                   size=(3, int(inner.sum())))
+        m = F.MeshHex(p, m.t)
+    theta = rng.uniform(0.01, 1.0, m.nelements)
+    w = rng.standard_normal(m.p.shape[1])
+    u = rng.standard_normal(m.p.shape[1])
+    return m, theta, w, u
+
+
+def trip2_batch(n_meshes, seed=SEED + 5):
+    """Batched TriP2 k*Laplace: meshes of log-uniform cell counts in
+    [2k, 200k], each a jittered unit-square grid, k ~ lognormal(0, 0.5)."""
+    import skfem_gb300 as F
+    rng = np.random.default_rng(seed)
+    cells = np.exp(rng.uniform(np.log(2e3), np.log(2e5), n_meshes))
+    meshes, ks = [], []
+    for c in cells:
+        nn = max(1, int(round(np.sqrt(c / 2))))
+        mm = F.MeshTri.init_tensor(np.linspace(0, 1, nn + 1), np.linspace(0, 1, nn + 1))
+        pp = mm.p.copy()
+        inner = np.all((pp > 1e-12) & (pp < 1 - 1e-12), axis=0)
+        pp[:, inner] += rng.uniform(-0.2 / nn, 0.2 / nn, size=(2, int(inner.sum())))
+        meshes.append(F.MeshTri(pp, mm.t))
+        ks.append(rng.lognormal(0.0, 0.5, mm.nelements))
+    return meshes, ks
+
+
+def k_laplace_mass_form():
+    import skfem_gb300 as F
+    from skfem_gb300 import helpers as H
+
+    @F.BilinearForm
+    def form(u, v, w):
+        return w.k * H.dot(H.grad(u), H.grad(v)) + u * v
+    return form
+
+
 def gpu_arm(args):
     import torch
 
     import skfem_gb300 as F
     from skfem_gb300 import _native as N
-    from skfem_gb300 import helpers as H
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -167,12 +241,9 @@ def gpu_arm(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    m, k = build_workload(args.nodes, args.seed + rank)
+    m, k = build_workload(args.nodes, SEED + rank)
     b = F.Basis(m, F.ElementTetP1())
-
-    @F.BilinearForm
-    def form(u, v, w):
-        return w.k * H.dot(H.grad(u), H.grad(v)) + u * v
+    form = k_laplace_mass_form()
 
     kd = torch.from_numpy(k).cuda()
     # first call builds the pattern and the per-cell geometry cache (one-time,
@@ -221,30 +292,30 @@ def gpu_arm(args):
     assert int(status.item()) == 0, "assembly status %d" % int(status.item())
     assert torch.equal(vals, K0.values()), "repeated assembly not bitwise identical"
 
-    # per-kernel split (same stream, CUDA events): the step is the coefficient
-    # checks and the fused sum over the basis's cached stiffness rows and
-    # unit mass matrix; the same call without a status runs the fused sum
-    # alone.  For comparison, the two-pass kernels (the local kernel on the
-    # cached geometry + the staging sum, as fem_assemble_local and
-    # fem_csr_sum_staged run them) and the local kernel computing its
-    # geometry from the coordinates (fem_local_matrices)
+    # per-kernel split (same stream, CUDA events): the step is the
+    # coefficient checks and the one-pass sum; the same call without a
+    # status runs the one-pass sum alone.  For comparison, the two-pass
+    # kernels (the local kernel on the cached geometry + the staging sum, as
+    # fem_assemble_local and fem_csr_sum_staged run them) and the local
+    # kernel computing its geometry from the coordinates
     local_buf = entry.staging
     e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-    t_local, t_sum, t_geom, t_fused = 0.0, 0.0, 0.0, 0.0
+    t_local, t_sum, t_geom, t_one = 0.0, 0.0, 0.0, 0.0
     reps = max(3, args.steps)
+    two_pass = torch.empty_like(vals)
     for _ in range(reps):
         e0.record(stream)
         N.check(lib.fem_assemble(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
                                  entry.pat.handle, N.ptr(entry.staging), N.ptr(vals), None, sp))
         e1.record(stream)
         torch.cuda.synchronize()
-        t_fused += e0.elapsed_time(e1)
+        t_one += e0.elapsed_time(e1)
         e0.record(stream)
         N.check(lib.fem_assemble_local(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
                                        entry.pat.handle, N.ptr(local_buf), N.ptr(status), 0, nel,
                                        sp))
         e1.record(stream)
-        N.check(lib.fem_csr_sum_staged(entry.pat.handle, N.ptr(local_buf), N.ptr(vals), sp))
+        N.check(lib.fem_csr_sum_staged(entry.pat.handle, N.ptr(local_buf), N.ptr(two_pass), sp))
         e2.record(stream)
         torch.cuda.synchronize()
         t_local += e0.elapsed_time(e1)
@@ -258,8 +329,21 @@ def gpu_arm(args):
     t_local /= reps
     t_sum /= reps
     t_geom /= reps
-    t_fused /= reps
-    t_checks = max(0.0, ms - t_fused)
+    t_one /= reps
+    t_checks = max(0.0, ms - t_one)
+    d = (two_pass - vals).abs().max().item() / vals.abs().max().item()
+
+    # the opt-in coefficient-update cache (cached unit-coefficient stiffness
+    # rows and mass matrix; a form re-assembled with new k many times): one
+    # fused sum per call -- reported beside the plain step, not as it
+    form.cache_coefficient_update(b, k=kd)
+    t_cu = _time(step, reps)
+    lib.fem_pattern_drop_coefficient_update(entry.pat.handle)
+    entry.coef_update = False
+    b.__dict__.pop("_coef_update", None)
+    step()
+    torch.cuda.synchronize()
+    assert torch.equal(vals, K0.values())
 
     # e2e: public API with host buffers (k as the reference takes it)
     kw_host = b.zero_w() + k[:, None]
@@ -274,17 +358,27 @@ def gpu_arm(args):
         e2e_times.append(time.perf_counter() - t0)
         del Kh
     Kh = form.assemble(b, k=kw_host)
+    assert np.array_equal(Kh.data, K0.values().cpu().numpy()), "e2e values differ from the step"
     e2e_s = sum(e2e_times) / len(e2e_times)
     h2d = kw_host.nbytes
     d2h = Kh.data.nbytes + Kh.indices.nbytes + Kh.indptr.nbytes
 
     hbm, peak_kind = peaks()
-    B = algorithmic_bytes(nel, m.p.shape[1], nnz)
-    achieved = B / (ms * 1e-3) / 1e9
+    Bytes = algorithmic_bytes(nel, m.p.shape[1], nnz)
+    achieved = Bytes / (ms * 1e-3) / 1e9
     # FP64 work of the TetP1 local kernel computing its geometry, per cell,
     # from its ncu instruction counts: 18 DADD + 21 DMUL + 38 DFMA (2 FLOP each)
     flops_per_el = 115.0
     fp64_achieved = nel * flops_per_el / (t_geom * 1e-3) / 1e9
+
+    def kern(name, t, bpc):
+        out = {"kernel": name, "ms": t, "dram_bytes_per_cell": bpc}
+        if bpc is not None:
+            out["gbs"] = bpc * nel / (t * 1e-3) / 1e9
+            out["frac_hbm"] = out["gbs"] / hbm
+        return out
+
+    traffic = None if ONEPASS_B_PER_CELL is None else (ONEPASS_B_PER_CELL + CHECK_B_PER_CELL) * nel
     res = {
         "metric": METRIC, "value": replica_value(nel, world, ms), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -292,51 +386,55 @@ def gpu_arm(args):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded tensor mesh, lognormal k)",
         "config": {"workload": "TetP1 k*laplace+mass, 101^3-node unit cube tensor mesh, 6 tets/cell",
                    "nelems": nel, "nverts": int(m.p.shape[1]), "nnz": nnz,
-                   "l2": "inputs+staging larger than L2 (no flush)", "parallelism": "replicas",
+                   "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas",
                    "pattern_build_s": pattern_s, "autotuned": tuned,
-                   "basis_caches": "built once with the pattern (in pattern_build_s): per-cell "
-                                   "geometry, unit-coefficient stiffness rows, unit-coefficient "
-                                   "mass matrix -- mesh-only data; every step reads and sums the "
-                                   "per-cell k"},
+                   "step": "plain assembly: coefficient checks + one-pass sum contracting the "
+                           "form per cell row from the per-cell geometry cache (Gram matrix of "
+                           "the barycentric gradients / (6|det|), |det|) -- the mapping data "
+                           "CellBasis keeps; the form is contracted and summed every step"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": TRAFFIC_B_PER_CELL * nel,
-                     "traffic_source": "%s, %.1f B/cell, scaled by cells"
-                                       % (TRAFFIC_SOURCE, TRAFFIC_B_PER_CELL),
-                     "peak_kind": peak_kind, "algorithmic_bytes_per_step": B,
-                     "kernel": "whole assembly step (coefficient checks + fused sum)"},
+                     "traffic": traffic,
+                     "traffic_source": (None if traffic is None else
+                                        "%s: one-pass sum %.1f + checks %.1f B/cell, scaled by "
+                                        "cells" % (TRAFFIC_SOURCE, ONEPASS_B_PER_CELL,
+                                                   CHECK_B_PER_CELL)),
+                     "peak_kind": peak_kind, "algorithmic_bytes_per_step": Bytes,
+                     "kernel": "whole assembly step (coefficient checks + one-pass sum)",
+                     "fp64_floor_ms": nel * 16 / 0.598e12 * 1e3},
         "kernels": {
-            "fused_sum": {"kernel": "csr_scaled_pair_kernel<4,U> or csr_scaled_kernel<4,U,4> (autotuned columns per lane; cached stiffness rows, unit mass)",
-                          "ms": t_fused, "dram_bytes_per_cell": FUSED_B_PER_CELL,
-                          "gbs": FUSED_B_PER_CELL * nel / (t_fused * 1e-3) / 1e9,
-                          "frac_hbm": FUSED_B_PER_CELL * nel / (t_fused * 1e-3) / 1e9 / hbm},
-            "coef_checks": {"kernel": "coef_fields_kernel (step time minus the fused sum)",
-                            "ms": t_checks, "dram_bytes_per_cell": CHECK_B_PER_CELL},
-            "two_pass_local": {"kernel": "simplex_scalar_kernel<3,1,BS,cached geometry>",
-                               "ms": t_local, "dram_bytes_per_cell": LOCAL_B_PER_CELL,
-                               "frac_hbm": LOCAL_B_PER_CELL * nel / (t_local * 1e-3) / 1e9 / hbm},
-            "two_pass_sum": {"kernel": "csr_sum_kernel<4,U,0>", "ms": t_sum,
-                             "dram_bytes_per_cell": SUM_B_PER_CELL,
-                             "frac_hbm": SUM_B_PER_CELL * nel / (t_sum * 1e-3) / 1e9 / hbm},
-            "bytes_source": TRAFFIC_SOURCE},
+            "onepass_sum": kern("csr_geometry_p1_kernel<4,U,false> (one-pass P1 sum on the "
+                                "cached geometry)", t_one, ONEPASS_B_PER_CELL),
+            "coef_checks": kern("coef_fields_kernel (step time minus the one-pass sum)",
+                                t_checks, CHECK_B_PER_CELL),
+            "two_pass_local": kern("simplex_scalar_kernel<3,1,BS,cached geometry>", t_local,
+                                   LOCAL_B_PER_CELL),
+            "two_pass_sum": kern("csr_sum_kernel<4,U,0>", t_sum, SUM_B_PER_CELL),
+            "coefficient_update_sum": kern("csr_scaled_pair_kernel<4,U> (opt-in cache of "
+                                           "unit-coefficient rows and mass matrix; not the "
+                                           "plain step)", t_cu, FUSED_B_PER_CELL),
+            "bytes_source": TRAFFIC_SOURCE,
+            "two_pass_vs_onepass_max_rel": d},
         "fp64": {"kernel": "local matrices computing their geometry (fem_local_matrices; the "
                            "step reads the basis's cached geometry instead)",
                  "ms": t_geom, "gflops": fp64_achieved, "peak_gflops": FP64_PEAK_GFLOPS,
                  "frac": fp64_achieved / FP64_PEAK_GFLOPS},
-        "kernels_ms": {"fused_sum": t_fused, "coef_checks": t_checks,
+        "kernels_ms": {"onepass_sum": t_one, "coef_checks": t_checks,
                        "two_pass_local": t_local, "two_pass_sum": t_sum,
+                       "two_pass_step": t_local + t_sum,
+                       "coefficient_update_step": t_cu,
                        "local_computing_geometry": t_geom},
         "clocks": clk.summary(),
         "e2e": {"value": nel / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s,
                 "s_per_step_median": sorted(e2e_times)[len(e2e_times) // 2],
                 "api": "BilinearForm.assemble(basis, k=(nelems, nqp) host array) -> scipy CSR"},
-        "gpu_launches": 2 * args.steps,   # coefficient checks + fused sum per step
+        "gpu_launches": 2 * args.steps,   # coefficient checks + one-pass sum per step
     }
+    if rank == 0 and not args.no_cpu:
+        res["cpu_baseline"], res["parity"] = cpu_baseline(args)
     if rank == 0 and not args.no_secondary:
         res["secondary"] = secondary_workloads(args)
-    if rank == 0 and not args.no_cpu:
-        res["cpu_baseline"] = cpu_baseline(args)
     if dist:
         dist.destroy_process_group()
     if rank == 0:
@@ -409,11 +507,7 @@ def secondary_workloads(args, only=None):
     if want('tet_p2_vec'):
         # cfg3: vector TetP2 elasticity, 41^3 nodes jittered +-0.2h, lambda=1, mu=0.5
         n = args.vec_n
-        m = F.MeshTet.init_tensor(*(np.linspace(0, 1, n + 1),) * 3)
-        p = m.p.copy()
-        inner = np.all((p > 1e-12) & (p < 1 - 1e-12), axis=0)
-        p[:, inner] += rng.uniform(-0.2 / n, 0.2 / n, size=(3, int(inner.sum())))
-        m = F.MeshTet(p, m.t)
+        m = jittered_tet_cube(n)
         b = F.Basis(m, F.ElementVector(F.ElementTetP2()), intorder=4)
         form = linear_elasticity(1.0, 0.5)
         t0 = time.perf_counter()
@@ -435,51 +529,51 @@ def secondary_workloads(args, only=None):
         torch.cuda.empty_cache()
 
     if want('hex1_vjp'):
-        # cfg4: Hex1 theta*Laplace 64^3 cells: plain assembly vs forward + adjoint
+        # cfg4: Hex1 theta*Laplace 64^3 cells: plain assembly vs forward + adjoint,
+        # on the tensor cube (parallelepiped cells: closed form) and on the same
+        # cube with interior nodes jittered by up to 0.2 h (isoparametric
+        # cells: the 4x4x4-point quadrature and its adjoint)
         from skfem_gb300.autodiff import _vertex_incidence
-        m = F.MeshHex.init_tensor(*(np.linspace(0, 1, args.hex_n + 1),) * 3)
-        b = F.Basis(m, F.ElementHex1())
 
         @F.BilinearForm
         def theta_laplace(u, v, w):
             return w.theta * H.dot(H.grad(u), H.grad(v))
 
-        theta = torch.tensor(rng.uniform(0.01, 1.0, m.nelements), device="cuda")
-        w = torch.tensor(rng.standard_normal(b.N), device="cuda")
-        u = torch.tensor(rng.standard_normal(b.N), device="cuda")
-        step, entry, c_form, vals = _abi_step(F, N, theta_laplace, b, {"theta": theta})
-        vinc = _vertex_incidence(b)
-        dth = torch.empty(m.nelements, dtype=torch.float64, device="cuda")
-        dX = torch.empty_like(b.p_dev)
-        scratch = torch.empty(m.nelements * 24, dtype=torch.float64, device="cuda")
+        for jit, tag in ((0.0, ""), (0.2, "_jittered")):
+            m, theta_h, w_h, u_h = hex_cube_workload(args.hex_n, jitter=jit)
+            b = F.Basis(m, F.ElementHex1())
+            theta = torch.tensor(theta_h, device="cuda")
+            w = torch.tensor(w_h, device="cuda")
+            u = torch.tensor(u_h, device="cuda")
+            step, entry, c_form, vals = _abi_step(F, N, theta_laplace, b, {"theta": theta})
+            vinc = _vertex_incidence(b)
+            dth = torch.empty(m.nelements, dtype=torch.float64, device="cuda")
+            dX = torch.empty_like(b.p_dev)
+            scratch = torch.empty(m.nelements * 24, dtype=torch.float64, device="cuda")
 
-        def vjp():
-            N.check(lib.fem_bilinear_vjp(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
-                                         vinc.handle, N.ptr(w), N.ptr(u), N.ptr(dth), None,
-                                         N.ptr(dX), N.ptr(scratch), N.stream_ptr()))
+            def vjp():
+                N.check(lib.fem_bilinear_vjp(N.byref(b.c_mesh), N.byref(b.c_basis),
+                                             N.byref(c_form), vinc.handle, N.ptr(w), N.ptr(u),
+                                             N.ptr(dth), None, N.ptr(dX), N.ptr(scratch),
+                                             N.stream_ptr()))
 
-        ms_f = _time(step, reps)
-        ms_fv = _time(lambda: (step(), vjp()), reps)
-        out["hex1_theta_laplace_%d_vjp" % args.hex_n] = {
-            "nelems": m.nelements, "nnz": entry.nnz, "ms_forward": ms_f, "ms_forward_plus_vjp": ms_fv,
-            "vjp_over_forward": ms_fv / ms_f, "elements_per_s_forward": m.nelements / (ms_f * 1e-3)}
-        del step, entry, vals, b, scratch
-        torch.cuda.empty_cache()
+            ms_f = _time(step, reps)
+            ms_v = _time(vjp, reps)
+            ms_fv = _time(lambda: (step(), vjp()), reps)
+            out["hex1_theta_laplace_%d%s_vjp" % (args.hex_n, tag)] = {
+                "nelems": m.nelements, "nnz": entry.nnz, "ms_forward": ms_f, "ms_vjp": ms_v,
+                "ms_forward_plus_vjp": ms_fv, "vjp_over_forward": ms_fv / ms_f,
+                "elements_per_s_forward": m.nelements / (ms_f * 1e-3),
+                "cells": "isoparametric (64-point quadrature)" if jit else
+                         "parallelepipeds (closed form)"}
+            del step, entry, vals, b, scratch
+            torch.cuda.empty_cache()
 
     if want('batched'):
         # cfg5: 512 jittered TriP2 squares, cells log-uniform in [2k, 200k], forward + adjoint
         from skfem_gb300.batched import BatchedBasis, GraphedAssembly
-        brng = np.random.default_rng(args.seed + 5)
-        cells = np.exp(brng.uniform(np.log(2e3), np.log(2e5), args.batch))
-        meshes, ks = [], []
-        for c in cells:
-            nn = max(1, int(round(np.sqrt(c / 2))))
-            mm = F.MeshTri.init_tensor(np.linspace(0, 1, nn + 1), np.linspace(0, 1, nn + 1))
-            pp = mm.p.copy()
-            inner = np.all((pp > 1e-12) & (pp < 1 - 1e-12), axis=0)
-            pp[:, inner] += brng.uniform(-0.2 / nn, 0.2 / nn, size=(2, int(inner.sum())))
-            meshes.append(F.MeshTri(pp, mm.t))
-            ks.append(brng.lognormal(0.0, 0.5, mm.nelements))
+        meshes, ks = trip2_batch(args.batch)
+        brng = np.random.default_rng(SEED + 6)
 
         @F.BilinearForm
         def k_laplace(u, v, w):
@@ -576,52 +670,97 @@ def secondary_workloads(args, only=None):
 
 
 def cpu_baseline(args, threads=1):
-    """The oracle (numpy restatement of the reference) on a bounded sample:
-    the same form on a smaller mesh of the same family, timed like the
-    reference's performance.py (Basis construction + assemble)."""
+    """The oracle (numpy restatement of the reference) on a bounded sample
+    of the workload -- the same form on the 61^3-node cube (1,296,000
+    cells) -- timed like scikit-fem's performance.py (Basis construction +
+    assemble) and without the Basis (assemble on a prebuilt basis, what the
+    GPU step times), on `threads` host threads.  The GPU's CSR of the same
+    sample is compared with the oracle's (parity)."""
+    import torch
+
     import oracle as O
+    import skfem_gb300 as F
     n = args.cpu_nodes
     m = O.mesh_tet_tensor(*(np.linspace(0, 1, n),) * 3)
-    k = np.random.default_rng(args.seed).lognormal(0.0, 1.0, m.nelements)
-    times = []
+    k = np.random.default_rng(SEED).lognormal(0.0, 1.0, m.nelements)
+    with_basis, assemble_only = [], []
+    Ko = None
     for _ in range(2):
         t0 = time.perf_counter()
         bo = O.OBasis(m, O.TetP1())
-        O.bilinear_assemble(O.k_laplace_mass, bo, k=bo.zero_w() + k[:, None], nthreads=threads)
-        times.append(time.perf_counter() - t0)
-    t = min(times)
-    return {"value": m.nelements / t, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "TetP1 k*laplace+mass on a %d^3-node cube (%d tets), Basis + assemble, "
-                      "best of 2" % (n, m.nelements)}
+        t1 = time.perf_counter()
+        Ko = O.bilinear_assemble(O.k_laplace_mass, bo, k=bo.zero_w() + k[:, None], nthreads=threads)
+        t2 = time.perf_counter()
+        with_basis.append(t2 - t0)
+        assemble_only.append(t2 - t1)
+    base = {"value": m.nelements / min(assemble_only), "unit": UNIT, "cores": threads,
+            "kind": "port",
+            "sample": "TetP1 k*laplace+mass on a %d^3-node cube (%d tets), assemble on a prebuilt "
+                      "basis, best of 2" % (n, m.nelements),
+            "with_basis": {"value": m.nelements / min(with_basis), "unit": UNIT,
+                           "sample": "the same, Basis construction + assemble (performance.py)"}}
+    # parity: the GPU's CSR of the same sample (host (nelems, nqp) coefficient,
+    # public API) against the oracle's
+    fm = F.MeshTet(m.p, m.t)
+    fb = F.Basis(fm, F.ElementTetP1())
+    Kg = k_laplace_mass_form().assemble(fb, k=fb.zero_w() + k[:, None])
+    same = (np.array_equal(Kg.indptr, Ko.indptr) and np.array_equal(Kg.indices, Ko.indices))
+    rel_fro = rel_max = None
+    if same:
+        dd = Kg.data - Ko.data
+        rel_fro = float(np.linalg.norm(dd) / np.linalg.norm(Ko.data))
+        rel_max = float(np.abs(dd).max() / np.abs(Ko.data).max())
+    parity = {"against": "oracle (numpy restatement of scikit-fem 12.0.1, pinned to reference "
+                         "fixtures)",
+              "case": "TetP1 k*laplace+mass, %d^3-node cube, %d cells, nnz %d"
+                      % (n, m.nelements, Ko.nnz),
+              "indptr_indices_bit_exact": bool(same), "rel_fro": rel_fro, "rel_max": rel_max,
+              "bounds": {"rel_fro": 1e-12, "rel_max": 1e-13},
+              "ok": bool(same and rel_fro <= 1e-12 and rel_max <= 1e-13)}
+    del fb
+    torch.cuda.empty_cache()
+    return base, parity
 
 
 def reference_arm(args):
+    """The CPU oracle with all host threads on the GPU arm's own workload
+    (101^3 nodes, 6M cells): each step assembles on a prebuilt basis, as the
+    GPU step does; one Basis + assemble run is reported beside it."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     import oracle as O
-    n = args.cpu_nodes
+    n = args.nodes
     m = O.mesh_tet_tensor(*(np.linspace(0, 1, n),) * 3)
-    k = np.random.default_rng(args.seed).lognormal(0.0, 1.0, m.nelements)
-    for _ in range(args.warmup):
-        bo = O.OBasis(m, O.TetP1())
-        O.bilinear_assemble(O.k_laplace_mass, bo, k=bo.zero_w() + k[:, None], nthreads=threads)
+    k = np.random.default_rng(SEED).lognormal(0.0, 1.0, m.nelements)
+    t0 = time.perf_counter()
+    bo = O.OBasis(m, O.TetP1())
+    kw = bo.zero_w() + k[:, None]
+    t1 = time.perf_counter()
+    O.bilinear_assemble(O.k_laplace_mass, bo, k=kw, nthreads=threads)
+    with_basis_s = time.perf_counter() - t0
+    basis_s = t1 - t0
+    for _ in range(max(0, args.warmup - 1)):
+        O.bilinear_assemble(O.k_laplace_mass, bo, k=kw, nthreads=threads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        bo = O.OBasis(m, O.TetP1())
-        O.bilinear_assemble(O.k_laplace_mass, bo, k=bo.zero_w() + k[:, None], nthreads=threads)
+        O.bilinear_assemble(O.k_laplace_mass, bo, k=kw, nthreads=threads)
     dt = (time.perf_counter() - t0) / args.steps
     v = m.nelements / dt
     res = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
            "higher_is_better": True, "scaling": "replicas only", "vs_baseline": None,
            "dtype": "f64", "data": "synthetic (seeded tensor mesh, lognormal k)",
-           "config": {"workload": "TetP1 k*laplace+mass, tensor cube mesh (bounded sample of the "
-                                  "101^3-node workload)", "nodes_per_axis": n,
-                      "nelems": m.nelements},
+           "config": {"workload": "TetP1 k*laplace+mass, %d^3-node unit cube tensor mesh, 6 "
+                                  "tets/cell" % n, "nelems": m.nelements,
+                      "step": "assemble on a prebuilt basis (form contraction + COO -> CSR)"},
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                            "sample": "%d^3-node cube, %d tets per step" % (n, m.nelements)},
+                            "sample": "the whole %d^3-node workload (%d tets) per step"
+                                      % (n, m.nelements)},
+           "with_basis": {"value": m.nelements / with_basis_s, "unit": UNIT,
+                          "basis_s": basis_s, "s": with_basis_s,
+                          "note": "one Basis(...) + assemble run, as performance.py times it"},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(res))
 

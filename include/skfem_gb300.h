@@ -252,20 +252,38 @@ int fem_pattern_build(const FemMesh* mesh, const FemBasis* basis, const FemBilin
  * fem_assemble, fem_assemble_local and fem_assemble_to_host_pipelined then
  * read it instead of the coordinates whenever the mesh they are given has
  * the same p pointer; after changing the coordinates in place, call this
- * again (or fem_pattern_drop_geometry).  With the geometry the call also
- * builds the fused cache: every cell's unit-coefficient stiffness rows in
- * the sum's incidence order (nelems * nbfun^2 doubles) and the CSR values
- * of the unit-coefficient mass matrix (nnz doubles), from which
- * fem_assemble and fem_assemble_to_host_pipelined assemble forms with a
- * constant mass coefficient in one fused sum.  Other families, or no device
- * memory left for a cache: that cache is left out, returns 0 (the kernels
- * then compute the geometry per call, or run the local kernel and the
- * staging sum).
+ * again (or fem_pattern_drop_geometry).  For scalar TriP1 / TetP1 bases the
+ * call also records, per row, the binary point of the one-pass assembly's
+ * fixed-point mass sums (from the cells' |det|, 2 bytes per row): with it
+ * fem_assemble and fem_assemble_to_host_pipelined assemble
+ * k_e dot(grad u, grad v) + m u v in one pass over the rows, contracting
+ * the form per cell row from the cached geometry as they sum.  When the
+ * pattern holds a coefficient-update cache (below) the call refreshes it.
+ * Other families, or no device memory left for a cache: that cache is
+ * left out, returns 0 (the kernels then compute the geometry per call, or
+ * run the local kernel and the staging sum).
  * Stream-ordered; not concurrently with assembly calls on the pattern.
  */
 int fem_pattern_cache_geometry(FemPattern* pat, const FemMesh* mesh, const FemBasis* basis,
                                fem_stream_t stream);
 void fem_pattern_drop_geometry(FemPattern* pat);
+
+/*
+ * Opt-in coefficient-update cache of a scalar simplex pattern -- no
+ * counterpart in the reference, which contracts the form on every call.
+ * For callers that re-assemble one form with new per-cell stiffness
+ * coefficients many times (optimisation loops): every cell's
+ * unit-coefficient stiffness rows in the sum's incidence order (nelems *
+ * nbfun^2 doubles) and the CSR values of the unit-coefficient mass matrix
+ * (nnz doubles); fem_assemble then takes forms whose mass coefficient is
+ * one constant as diff * sum_e k_e S_e + mass * M in one fused sum.  Needs
+ * the pattern's geometry cache of this mesh's coordinates; refreshed with
+ * it; fem_pattern_drop_coefficient_update releases it.  No room: returns 0
+ * without the cache.
+ */
+int fem_pattern_cache_coefficient_update(FemPattern* pat, const FemMesh* mesh,
+                                         const FemBasis* basis, fem_stream_t stream);
+void fem_pattern_drop_coefficient_update(FemPattern* pat);
 
 /* Sizes: nnz of the CSR pattern, number of rows (N), and the bytes of the
  * local-matrix staging buffer fem_assemble needs.  The staging holds the
@@ -286,13 +304,18 @@ void fem_pattern_destroy(FemPattern* pat);
 /*
  * Steady-state assembly into an existing pattern: local matrices into
  * `staging` (fem_pattern_info bytes), then a fixed-order, atomic-free
- * segmented sum into csr_values (nnz).  When the pattern holds the fused
- * cache of this mesh's coordinates (fem_pattern_cache_geometry, scalar
- * simplex bases) and the form's mass coefficient is one constant, the
- * coefficient checks and one fused sum diff * sum_e k_e S_e + mass * M
- * replace both (staging untouched); its additions are grouped differently,
- * so the values may differ from the two-pass ones in the last bits (within
- * 1e-14 of max|K|), and are bitwise the same on every call and through
+ * segmented sum into csr_values (nnz).  Scalar TriP1 / TetP1 bases whose
+ * pattern holds the geometry cache of this mesh's coordinates
+ * (fem_pattern_cache_geometry) take one pass instead: the coefficient
+ * checks, then each CSR row sums k_e * G_e[il][j] (FP64, ascending cell
+ * order) and |det_e| (exact fixed point, or m_e |det_e| in FP64 for a
+ * per-cell mass field) over its cells straight from the cached geometry
+ * (staging untouched).  When the pattern holds a coefficient-update cache
+ * (fem_pattern_cache_coefficient_update) and the form's mass coefficient
+ * is one constant, one fused sum diff * sum_e k_e S_e + mass * M runs
+ * instead.  Both group the additions differently from the two-pass path,
+ * so the values may differ from its in the last bits (within 1e-14 of
+ * max|K|), and are bitwise the same on every call and through
  * fem_assemble_to_host_pipelined.  status (device int32, may be NULL)
  * receives FEM_ERR_STALE_PATTERN when the exact-zero structure of the local
  * matrices may have changed: some per-element coefficient became exactly

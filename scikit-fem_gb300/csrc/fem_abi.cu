@@ -140,6 +140,14 @@ struct FemPattern {
   // nbfun) and the CSR values of the unit-coefficient mass matrix (nnz).
   double* stiff = nullptr;
   double* mass1 = nullptr;
+  // The coefficient-update cache above is built only on request
+  // (fem_pattern_cache_coefficient_update), then refreshed with geo.
+  bool fused_wanted = false;
+  // One-pass P1 assembly from geo (scalar TriP1 / TetP1, built with geo):
+  // each row's binary point of the fixed-point mass sums; mbase_ok false
+  // when some cell's |det| lies outside the range it covers.
+  int16_t* mbase = nullptr;
+  bool mbase_ok = false;
 };
 
 namespace {
@@ -159,6 +167,17 @@ struct FusedSum {
   double mscale;
 };
 
+// The one-pass P1 assembly of one call: scalar TriP1 / TetP1 forms
+// k_e dot(grad u, grad v) + m_e u v over the geometry cache, when the
+// pattern holds the cache of this mesh's coordinates.
+bool geometry_sum(const FemPattern* pat, const FemMesh* mesh, const FemBasis* basis,
+                  const FemBilinear* form) {
+  if (basis->vector || !cached_geometry(pat, mesh)) return false;
+  if (basis->family != FEM_TRI_P1 && basis->family != FEM_TET_P1) return false;
+  if (pat->P.nbfun_u != pat->P.nbfun_v) return false;
+  return form->mass.field ? true : (pat->mbase && pat->mbase_ok);
+}
+
 bool fused_sum(const FemPattern* pat, const FemMesh* mesh, const FemBasis* basis,
                const FemBilinear* form, FusedSum* fs) {
   if (!pat->stiff || !pat->mass1 || !cached_geometry(pat, mesh) || basis->vector ||
@@ -177,6 +196,36 @@ void drop_fused(FemPattern* pat) {
   cudaFree(pat->mass1);
   pat->stiff = nullptr;
   pat->mass1 = nullptr;
+}
+
+// The rows' fixed-point binary points of the one-pass P1 assembly, from the
+// geometry cache just queued (scalar TriP1 / TetP1 patterns).  Without room
+// for them the calls run the local kernel and the staging sum.
+int cache_mass_base(FemPattern* pat, const FemMesh* mesh, const FemBasis* basis, cudaStream_t st) {
+  const fem::Pattern& P = pat->P;
+  pat->mbase_ok = false;
+  if (basis->vector || (basis->family != FEM_TRI_P1 && basis->family != FEM_TET_P1) ||
+      !P.has_matrix || P.nbfun_u != P.nbfun_v)
+    return 0;
+  if (!pat->mbase) {
+    cudaError_t e = cudaMalloc(&pat->mbase, std::max<int64_t>(1, P.nrows) * sizeof(int16_t));
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      pat->mbase = nullptr;
+      return 0;
+    }
+    if (e != cudaSuccess) {
+      pat->mbase = nullptr;
+      return fem::check_cuda(e, "cudaMalloc(row mass base)");
+    }
+  }
+  const int ng = (mesh->dim + 1) * (mesh->dim + 2) / 2;
+  int shmax = 0;
+  bool ok = false;
+  int rc = fem::row_mass_base(P, pat->geo + (int64_t)ng * mesh->nelems, pat->mbase, &shmax, &ok, st);
+  if (rc) return rc;
+  pat->mbase_ok = ok;
+  return 0;
 }
 
 // Builds the fused cache from the geometry cache just queued: the local
@@ -490,6 +539,7 @@ void fem_pattern_destroy(FemPattern* pat) {
   cudaFree(pat->coef_bits);
   cudaFree(pat->plan_cells);
   cudaFree(pat->geo);
+  cudaFree(pat->mbase);
   drop_fused(pat);
   delete pat;
 }
@@ -523,10 +573,37 @@ int fem_pattern_cache_geometry(FemPattern* pat, const FemMesh* mesh, const FemBa
   pat->geo_p = nullptr;  // not valid until the kernels below have been queued
   rc = fem_fast::geometry_cache(*mesh, *basis, pat->geo, st);
   if (rc) return rc;
-  rc = cache_fused(pat, mesh, basis, st);
+  rc = cache_mass_base(pat, mesh, basis, st);
   if (rc) return rc;
+  if (pat->fused_wanted) {
+    rc = cache_fused(pat, mesh, basis, st);
+    if (rc) return rc;
+  }
   pat->geo_p = mesh->p;
   return 0;
+}
+
+int fem_pattern_cache_coefficient_update(FemPattern* pat, const FemMesh* mesh,
+                                         const FemBasis* basis, fem_stream_t stream) {
+  int rc = validate(mesh, basis);
+  if (rc) return rc;
+  if (!pat || pat->P.nelems != mesh->nelems || pat->P.nbfun_v != basis->nbfun) {
+    set_error(FEM_ERR_ARGUMENT, "pattern does not belong to this mesh / basis");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (!cached_geometry(pat, mesh)) {
+    set_error(FEM_ERR_ARGUMENT, "the coefficient-update cache needs the pattern's geometry cache "
+              "of this mesh's coordinates (fem_pattern_cache_geometry)");
+    return FEM_ERR_ARGUMENT;
+  }
+  pat->fused_wanted = true;
+  return cache_fused(pat, mesh, basis, (cudaStream_t)stream);
+}
+
+void fem_pattern_drop_coefficient_update(FemPattern* pat) {
+  if (!pat) return;
+  pat->fused_wanted = false;
+  drop_fused(pat);
 }
 
 void fem_pattern_drop_geometry(FemPattern* pat) {
@@ -562,6 +639,16 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
     P.sum_unroll = t.sum_unroll;
     P.sum_cols = t.sum_cols;
     return fem::csr_sum_scaled(P, fs.stiff, fs.diff, fs.mass1, fs.mscale, csr_values, st);
+  }
+  if (geometry_sum(pat, mesh, basis, form)) {
+    // the coefficient checks, then the one-pass P1 assembly over the
+    // cached geometry (the form contracted per cell row as the rows sum)
+    rc = fem_fast::coef_checks(*form, pat->coef_bits, status, st, 0, mesh->nelems, nullptr);
+    if (rc) return rc;
+    fem::Pattern P = pat->P;
+    P.sum_unroll = fem::tuning_for(basis->family).sum_unroll;
+    return fem::csr_sum_geometry_p1(P, mesh->dim, pat->geo, form->diff, form->mass, pat->mbase,
+                                    csr_values, st);
   }
   // the local kernel also compares each element's coefficient zero bits
   // with the pattern's (FEM_ERR_STALE_PATTERN)
@@ -622,12 +709,23 @@ std::vector<int64_t> row_ranges(const std::vector<int32_t>& ip, int64_t nrows, i
 // Sums rows [row0, row1) -- from the staging, or fused from the pattern's
 // cache when fs is given -- and queues their values' copy to the host on cs
 // behind the sum.
+// The one-pass P1 assembly's inputs for sum_rows_to_host.
+struct GeometrySum {
+  int dim;
+  const double* geo;
+  FemCoef diff, mass;
+  const int16_t* mbase;
+};
+
 int sum_rows_to_host(const fem::Pattern& P, const std::vector<int32_t>& ip, const double* staging,
                      double* csr_values, double* host_values, int64_t row0, int64_t row1,
-                     cudaStream_t st, cudaStream_t cs, const FusedSum* fs = nullptr) {
+                     cudaStream_t st, cudaStream_t cs, const FusedSum* fs = nullptr,
+                     const GeometrySum* gs = nullptr) {
   int rc = fs ? fem::csr_sum_scaled(P, fs->stiff, fs->diff, fs->mass1, fs->mscale, csr_values, st,
                                     row0, row1)
-              : fem::csr_sum(P, staging, csr_values, st, row0, row1, nullptr, P.staging_sym);
+           : gs ? fem::csr_sum_geometry_p1(P, gs->dim, gs->geo, gs->diff, gs->mass, gs->mbase,
+                                           csr_values, st, row0, row1)
+                : fem::csr_sum(P, staging, csr_values, st, row0, row1, nullptr, P.staging_sym);
   if (rc) return rc;
   const int64_t a = ip[row0], b = ip[row1];
   if (b > a) {
@@ -927,6 +1025,8 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
   const int32_t* cells = pat->plan_cells;
   FusedSum fs;
   const bool fused = fused_sum(pat, mesh, basis, form, &fs);
+  GeometrySum gs{mesh->dim, pat->geo, form->diff, form->mass, pat->mbase};
+  const bool onepass = !fused && geometry_sum(pat, mesh, basis, form);
   std::vector<cudaEvent_t> evs;
   auto event = [&](cudaEvent_t* ev) -> cudaError_t {
     cudaError_t e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
@@ -974,8 +1074,9 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
       }
     }
     if (cb[c + 1] > cb[c]) {
-      rc = fused ? fem_fast::coef_checks(*form, pat->coef_bits, status, st, cb[c], cb[c + 1], cells)
-                 : fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
+      rc = (fused || onepass)
+               ? fem_fast::coef_checks(*form, pat->coef_bits, status, st, cb[c], cb[c + 1], cells)
+               : fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
                                                     status ? pat->coef_bits : nullptr, status, st,
                                                     cb[c], cb[c + 1], cells,
                                                     pat->P.staging_sym > 0,
@@ -989,7 +1090,7 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
     const int64_t row1 = done[c];
     if (row1 > row) {
       rc = sum_rows_to_host(P, pat->host_indptr, staging, csr_values, host_values, row, row1, st,
-                            cs, fused ? &fs : nullptr);
+                            cs, fused ? &fs : nullptr, onepass ? &gs : nullptr);
       if (rc) {
         release();
         return rc;

@@ -195,6 +195,20 @@ int csr_sum_scaled(const Pattern& P, const double* stiff, const FemCoef& diff,
 // order (ninc x nbfun) for csr_sum_scaled.
 int incidence_rows(const Pattern& P, const double* local, double* out, cudaStream_t st);
 
+// One-pass assembly of a scalar P1 simplex form k_e S_e + m M_e (rows
+// [row0, row1)) from the per-cell geometry cache geo (Gram entries scaled
+// by 1/(d! |det|), then |det|); mbase: the rows' fixed-point binary points
+// of the constant-coefficient mass sums (row_mass_base; unused when the
+// mass coefficient has a field).
+int csr_sum_geometry_p1(const Pattern& P, int dim, const double* geo, const FemCoef& diff,
+                        const FemCoef& mass, const int16_t* mbase, double* vals, cudaStream_t st,
+                        int64_t row0 = 0, int64_t row1 = -1);
+// The rows' binary points for csr_sum_geometry_p1 from the cells' |det|
+// (adet: nelems doubles); *ok false when some |det| is outside the range
+// the fixed point covers (degenerate or non-finite cells).
+int row_mass_base(const Pattern& P, const double* adet, int16_t* mbase, int* shmax, bool* ok,
+                  cudaStream_t st);
+
 int basis_nb_scalar(int family);
 int basis_dim(int family);
 

@@ -459,6 +459,173 @@ __global__ void csr_scaled_pair_kernel(const int32_t* __restrict__ inc_ptr, cons
   }
 }
 
+// ------------------------------------------------ one-pass P1 assembly
+// Assembly of a scalar P1 simplex form  k_e * dot(grad u, grad v) + m * u v
+// in one pass over the CSR rows, from the basis's per-cell geometry cache
+// (geo[g * nelems + e]: the Gram entries of the barycentric gradients scaled
+// by 1/(d! |det|), row-major upper, then |det| -- what CellBasis keeps of
+// its mapping, cell_basis.py:101-105).  Every call contracts the form per
+// cell row as it sums: for CSR row r and each incidence entry (cell e, local
+// row il) in ascending order, local column j adds
+//   stiffness  k_e * G_e[il][j]                  -> acc_k[slot], one DFMA
+//   mass       |det_e| (twice on the diagonal)  -> acc_m[slot]
+// and the entry is  kscale * acc_k + m * c_P1 * acc_m  (c_P1 the P1 mass
+// integral per unit |det| off the diagonal, 1/((d+1)(d+2) d!)).
+//
+// With a constant mass coefficient (MFIELD false) acc_m is an exact int64
+// fixed-point sum of |det_e|: each row has its own binary point
+// (mbase[r], from the largest |det| among the row's cells, with shmax bits
+// of headroom for the row's entries), so the row's mass sums are exact and
+// rounded once when converted back -- order-independent, and FP64-free in
+// the loop (GB300's FP64 pipe runs 1/58 of its FP32 rate; the integer pipes
+// take the mass term).  With a per-cell mass field, acc_m sums m_e |det_e|
+// in FP64 in the same fixed order.
+//
+// Two lanes per row, lane h taking columns 2h and 2h+1 (TriP1: lane 1 only
+// column 2), 16 rows per warp, U entries' loads in flight; entries are
+// added in ascending (cell, local row) order (__syncwarp between them), so
+// every call gives the same bits.  The local entries are the two-pass
+// kernels' up to rounding: k_e G and |det| c are combined per CSR entry
+// instead of per cell (within 1e-14 of max|K|, tested).
+__device__ __forceinline__ long long fixed_of(double x, int base) {
+  const unsigned long long bits = dbits(x);            // x > 0, normal
+  const int ex = (int)(bits >> 52);
+  const unsigned long long man = (bits & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
+  const int sh = ex - base;
+  return sh >= 0 ? (long long)(man << sh) : (long long)(man >> min(-sh, 63));
+}
+
+template <int NU, int U, bool MFIELD>
+__global__ void __launch_bounds__(128) csr_geometry_p1_kernel(
+    const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+    const uint16_t* __restrict__ slot, const int32_t* __restrict__ indptr,
+    const double* __restrict__ geo, int64_t nelems, const double* __restrict__ kfield,
+    int64_t kstride, double kscale, const double* __restrict__ mfield, int64_t mstride,
+    double mscale, double moff, const int16_t* __restrict__ mbase, int64_t row0, int64_t nrows,
+    int stride, double* __restrict__ vals) {
+  constexpr int NG = NU * (NU + 1) / 2;    // Gram entries; geo[NG] is |det|
+  constexpr int RPW = 16;
+  using MAcc = typename std::conditional<MFIELD, double, long long>::type;
+  extern __shared__ double acc_smem[];
+  const int lane = threadIdx.x & 31;
+  const int sub = lane >> 1;
+  const int h = lane & 1;
+  const int wib = threadIdx.x >> 5;
+  double* acck = acc_smem + ((size_t)wib * RPW + sub) * stride;
+  MAcc* accm = reinterpret_cast<MAcc*>(acc_smem + (size_t)(blockDim.x >> 5) * RPW * stride) +
+               ((size_t)wib * RPW + sub) * stride;
+  const int j0 = 2 * h, j1 = 2 * h + 1;
+  const bool has1 = j1 < NU;
+  const double* __restrict__ adet_arr = geo + (int64_t)NG * nelems;
+  const int64_t rows_per_block = (int64_t)(blockDim.x >> 5) * RPW;
+  for (int64_t rb = row0 + (int64_t)blockIdx.x * rows_per_block; rb < nrows;
+       rb += (int64_t)gridDim.x * rows_per_block) {
+    const int64_t r = rb + (int64_t)wib * RPW + sub;
+    int32_t b = 0, len = 0, p0 = 0, nnz = 0, base = 0;
+    if (r < nrows) {
+      b = inc_ptr[r];
+      len = inc_ptr[r + 1] - b;
+      p0 = indptr[r];
+      nnz = indptr[r + 1] - p0;
+      if (!MFIELD) base = mbase[r];
+    }
+    for (int k = h; k < nnz; k += 2) {
+      acck[k] = 0.0;
+      accm[k] = (MAcc)0;
+    }
+    int maxlen = len;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
+    __syncwarp();
+    for (int q0 = 0; q0 < maxlen; q0 += U) {
+      double kv[U], g0[U], g1[U];
+      MAcc mv[U];
+      uint32_t s0[U], s1[U];
+      int il[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int q = q0 + u;
+        s0[u] = 0xFFFFu;
+        s1[u] = 0xFFFFu;
+        kv[u] = 0.0;
+        g0[u] = 0.0;
+        g1[u] = 0.0;
+        mv[u] = (MAcc)0;
+        il[u] = -1;
+        if (q < len) {
+          const uint32_t code = (uint32_t)__ldg(inc + b + q);
+          const uint32_t e = NU == 4 ? (code >> 2) : (__umulhi(code, 0xAAAAAAABu) >> 1);
+          const int l = (int)(code - e * NU);
+          il[u] = l;
+          const uint16_t* sq = slot + ((int64_t)b + q) * NU;
+          s0[u] = __ldg(sq + j0);
+          if (has1) s1[u] = __ldg(sq + j1);
+          kv[u] = kfield ? __ldg(kfield + (int64_t)e * kstride) : 1.0;
+          const int a0 = min(l, j0), c0 = max(l, j0);
+          g0[u] = __ldg(geo + (int64_t)(a0 * (2 * NU + 1 - a0) / 2 + c0 - a0) * nelems + e);
+          if (has1) {
+            const int a1 = min(l, j1), c1 = max(l, j1);
+            g1[u] = __ldg(geo + (int64_t)(a1 * (2 * NU + 1 - a1) / 2 + c1 - a1) * nelems + e);
+          }
+          const double adet = __ldg(adet_arr + e);
+          if constexpr (MFIELD) mv[u] = __ldg(mfield + (int64_t)e * mstride) * adet;
+          else mv[u] = fixed_of(adet, base);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (s0[u] != 0xFFFFu) {
+          acck[s0[u]] = __fma_rn(kv[u], g0[u], acck[s0[u]]);
+          accm[s0[u]] += il[u] == j0 ? mv[u] + mv[u] : mv[u];
+        }
+        if (s1[u] != 0xFFFFu) {
+          acck[s1[u]] = __fma_rn(kv[u], g1[u], acck[s1[u]]);
+          accm[s1[u]] += il[u] == j1 ? mv[u] + mv[u] : mv[u];
+        }
+        __syncwarp();
+      }
+    }
+    double mc;
+    if constexpr (MFIELD) {
+      mc = moff;
+    } else {
+      // 2^(base - 1075): the value of one unit of the row's fixed point
+      const double unit = dfrombits((unsigned long long)(base - 1075 + 1023) << 52);
+      mc = (mscale * moff) * unit;
+    }
+    for (int k = h; k < nnz; k += 2) {
+      const double m = MFIELD ? (double)accm[k] : __ll2double_rn((long long)accm[k]);
+      vals[p0 + k] = __fma_rn(mc, m, kscale * acck[k]);
+    }
+    __syncwarp();
+  }
+}
+
+// mbase[r] = (largest exponent field of |det_e| over the cells of row r)
+// - shmax, the binary point of row r's fixed-point mass sums; *minexp the
+// smallest exponent field of any |det| (0: a degenerate cell), *maxexp the
+// largest (2047: inf / nan) -- the host then leaves the fixed-point path.
+__global__ void row_mass_base_kernel(const int32_t* __restrict__ inc_ptr,
+                                     const int32_t* __restrict__ inc, int64_t nrows, int nu,
+                                     const double* __restrict__ adet, int shmax,
+                                     int16_t* __restrict__ mbase, int32_t* __restrict__ ext) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int32_t b = inc_ptr[r], n = inc_ptr[r + 1] - b;
+  int emax = 0, emin = 2047;
+  for (int q = 0; q < n; ++q) {
+    const uint32_t e = (uint32_t)inc[b + q] / (uint32_t)nu;
+    const int ex = (int)((dbits(adet[e]) >> 52) & 0x7FF);
+    emax = max(emax, ex);
+    emin = min(emin, ex);
+  }
+  mbase[r] = (int16_t)(n > 0 ? emax - shmax : 1075);
+  if (n > 0) {
+    atomicMin(ext, emin);
+    atomicMax(ext + 1, emax);
+  }
+}
+
 // out[q * nu + j] = local[inc[q] * nu + j]: element-major local rows
 // gathered into incidence order.
 __global__ void incidence_rows_kernel(const int32_t* __restrict__ inc, int64_t ninc, int nu,
@@ -913,6 +1080,92 @@ void free_pattern(Pattern* P) {
   cudaFree(P->indices);
   cudaFree(P->slot);
   delete P;
+}
+
+
+int row_mass_base(const Pattern& P, const double* adet, int16_t* mbase, int* shmax_out,
+                  bool* ok, cudaStream_t st) {
+  // headroom: a row adds at most max_row_inc entries of at most 2 * 2^(53 + shmax)
+  int lg = 0;
+  while ((1 << lg) < std::max(1, P.max_row_inc)) ++lg;
+  const int shmax = 8 - lg;
+  *shmax_out = shmax;
+  *ok = false;
+  if (P.nrows == 0) {
+    *ok = true;
+    return 0;
+  }
+  AsyncScratch scratch(st);
+  int32_t* ext = nullptr;
+  FEM_TRY_CUDA(scratch.alloc(&ext, 2 * sizeof(int32_t)));
+  const int32_t init[2] = {2047, 0};
+  FEM_TRY_CUDA(cudaMemcpyAsync(ext, init, sizeof(init), cudaMemcpyHostToDevice, st));
+  row_mass_base_kernel<<<(unsigned)ceil_div(P.nrows, 256), 256, 0, st>>>(
+      P.inc_ptr, P.inc, P.nrows, P.nbfun_v, adet, shmax, mbase, ext);
+  FEM_LAUNCH_CHECK("row_mass_base_kernel");
+  int32_t h[2] = {0, 0};
+  FEM_TRY_CUDA(cudaMemcpyAsync(h, ext, sizeof(h), cudaMemcpyDeviceToHost, st));
+  FEM_TRY_CUDA(cudaStreamSynchronize(st));
+  // the unit 2^(base - 1075) must be a normal double: base = exponent - shmax
+  // in [53 + ..., 2046]; degenerate (0) or non-finite (2047) cells excluded
+  *ok = shmax >= 0 && h[0] >= 64 + shmax && h[1] <= 2000;
+  return 0;
+}
+
+int csr_sum_geometry_p1(const Pattern& P, int dim, const double* geo, const FemCoef& diff,
+                        const FemCoef& mass, const int16_t* mbase, double* vals, cudaStream_t st,
+                        int64_t row0, int64_t row1) {
+  const int nu = dim + 1;
+  if (!P.has_matrix || P.nbfun_u != nu || P.nbfun_v != nu || (dim != 2 && dim != 3)) {
+    set_error(FEM_ERR_ARGUMENT, "the one-pass P1 sum needs a square P1 simplex pattern");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (!mass.field && !mbase) {
+    set_error(FEM_ERR_ARGUMENT, "the one-pass P1 sum needs the rows' mass binary points");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (row1 < 0 || row1 > P.nrows) row1 = P.nrows;
+  if (row0 < 0) row0 = 0;
+  if (row1 <= row0 || P.nnz == 0) return 0;
+  if (P.nelems * (int64_t)nu >= ((int64_t)1 << 32)) {
+    set_error(FEM_ERR_CAPACITY, "%lld incidence codes exceed 2^32", (long long)(P.nelems * nu));
+    return FEM_ERR_CAPACITY;
+  }
+  // off-diagonal P1 mass per unit |det|: 1/((d+1)(d+2) d!) -- 1/120 (tet), 1/24 (tri)
+  const double moff = dim == 3 ? 0.05 * (1.0 / 6.0) : (1.0 / 12.0) * 0.5;
+  const int stride = std::max(1, P.max_row_nnz);
+  const int threads = 128;
+  const int warps = threads / 32;
+  const int rpw = 16;
+  const size_t smem = (size_t)warps * rpw * stride * (sizeof(double) + 8);
+  const int64_t rows_per_block = (int64_t)warps * rpw;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(row1 - row0, rows_per_block),
+                                                              (int64_t)num_sms() * 64));
+  const double* kf = diff.field;
+  const int64_t ks = diff.stride > 1 ? diff.stride : 1;
+  const double* mf = mass.field;
+  const int64_t ms = mass.stride > 1 ? mass.stride : 1;
+  const int U = P.sum_unroll >= 8 ? 8 : 4;
+  auto launch = [&](auto kern) -> int {
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return check_cuda(e, "csr_geometry_p1 smem");
+    }
+    kern<<<grid, threads, smem, st>>>(P.inc_ptr, P.inc, P.slot, P.indptr, geo, P.nelems, kf, ks,
+                                      diff.scale, mf, ms, mass.scale, moff, mbase, row0, row1,
+                                      stride, vals);
+    return 0;
+  };
+  int rc;
+#define FEM_GEO_PICK(NU)                                                                      \
+  if (mf) rc = U == 8 ? launch(csr_geometry_p1_kernel<NU, 8, true>) : launch(csr_geometry_p1_kernel<NU, 4, true>); \
+  else rc = U == 8 ? launch(csr_geometry_p1_kernel<NU, 8, false>) : launch(csr_geometry_p1_kernel<NU, 4, false>);
+  if (nu == 4) { FEM_GEO_PICK(4) }
+  else { FEM_GEO_PICK(3) }
+#undef FEM_GEO_PICK
+  if (rc) return rc;
+  FEM_LAUNCH_CHECK("csr_geometry_p1_kernel");
+  return 0;
 }
 
 }  // namespace fem

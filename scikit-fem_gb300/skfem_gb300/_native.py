@@ -139,6 +139,8 @@ _SIGS = {
     "fem_host_memory_access": (ctypes.c_int, [_P]),
     "fem_pattern_cache_geometry": (ctypes.c_int, [_P, _P, _P, _P]),
     "fem_pattern_drop_geometry": (None, [_P]),
+    "fem_pattern_cache_coefficient_update": (ctypes.c_int, [_P, _P, _P, _P]),
+    "fem_pattern_drop_coefficient_update": (None, [_P]),
     "fem_assemble_to_host_pipelined": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _P,
                                                       ctypes.c_int32, ctypes.c_int32, _P, _P,
                                                       _P]),

@@ -93,7 +93,8 @@ class GraphedAssembly:
                      for k, v in coefs.items()}
         # first assembly builds (and caches) the pattern eagerly
         K = form.assemble_torch(basis, **self.coef)
-        self.entry = next(e for key, e in basis._patterns.items() if key[0] == "bilinear")
+        self.key, self.entry = next((key, e) for key, e in basis._patterns.items()
+                                    if key[0] == "bilinear")
         self.indptr, self.indices = K.crow_indices(), K.col_indices()
         self.values = torch.empty(self.entry.nnz, dtype=torch.float64, device=dev)
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
@@ -123,7 +124,7 @@ class GraphedAssembly:
         lib = N.lib()
         b = self.basis
         s = N.stream_ptr()
-        self.entry.refresh_geometry(b, s)
+        self.entry.ensure_caches(b, self.key, s)
         N.check(lib.fem_assemble(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(self.c_form),
                                  self.entry.pat.handle, N.ptr(self.entry.staging),
                                  N.ptr(self.values), N.ptr(self.status), s))

@@ -430,14 +430,13 @@ class _PatternEntry:
             self.refresh_geometry(basis, stream)
 
     def refresh_geometry(self, basis, stream=None):
-        """The channel pattern's per-cell geometry cache and, with it, the
-        fused cache (unit-coefficient stiffness rows in incidence order and
-        the unit-coefficient mass matrix) of scalar simplex bases -- CellBasis
-        keeps its mapping the same way -- recomputed when the basis's
-        coordinates changed: in place (the tensor's version counter) or
-        replaced (its pointer).  While the mesh points at other coordinates
-        (the adjoint's X) the kernels compute the geometry and run the
-        two-pass assembly."""
+        """The channel pattern's per-cell geometry cache of scalar simplex
+        bases -- CellBasis keeps its mapping the same way -- recomputed when
+        the basis's coordinates changed: in place (the tensor's version
+        counter) or replaced (its pointer); an opted-in coefficient-update
+        cache is refreshed with it.  While the mesh points at other
+        coordinates (the adjoint's X) the kernels compute the geometry and
+        run the two-pass assembly."""
         p = basis.p_dev
         if basis.c_mesh.p != p.data_ptr():
             return
@@ -448,6 +447,18 @@ class _PatternEntry:
             self.pat.handle, N.byref(basis.c_mesh), N.byref(basis.c_basis),
             stream if stream is not None else N.stream_ptr()))
         self.geo_key = key
+
+    def ensure_caches(self, basis, key, stream):
+        """The geometry cache, and the coefficient-update cache when the
+        basis asked for one on this form structure (kept across pattern
+        rebuilds)."""
+        self.refresh_geometry(basis, stream)
+        if key in basis.__dict__.get("_coef_update", ()) and not getattr(self, "coef_update", False):
+            if self.geo_key is None:
+                return
+            N.check(N.lib().fem_pattern_cache_coefficient_update(
+                self.pat.handle, N.byref(basis.c_mesh), N.byref(basis.c_basis), stream))
+            self.coef_update = True
 
 
 _SIDE = {}
@@ -537,7 +548,7 @@ class BilinearForm(Form):
             entry = _PatternEntry(ubasis, c_form, stream, prog)
             del keep
             ubasis._patterns[key] = entry
-        entry.refresh_geometry(ubasis, stream)
+        entry.ensure_caches(ubasis, key, stream)
         vals = torch.empty(max(entry.nnz, 1), dtype=torch.float64, device=ubasis.device)[:entry.nnz]
         entry.status.zero_()
         N.check(N.lib().fem_assemble(N.byref(ubasis.c_mesh), N.byref(ubasis.c_basis),
@@ -702,7 +713,7 @@ class BilinearForm(Form):
                 entry = _PatternEntry(ubasis, c_form, stream, prog)
                 del keep
                 ubasis._patterns[key] = entry
-            entry.refresh_geometry(ubasis, stream)
+            entry.ensure_caches(ubasis, key, stream)
             data = torch.empty(entry.nnz, dtype=torch.float64, pin_memory=True)
             indices = torch.empty(entry.nnz, dtype=torch.int32, pin_memory=True)
             indptr = torch.empty(entry.nrows + 1, dtype=torch.int32, pin_memory=True)
@@ -786,6 +797,24 @@ class BilinearForm(Form):
         N.check(N.lib().fem_local_matrices(N.byref(ubasis.c_mesh), N.byref(ubasis.c_basis),
                                            N.byref(c_form), N.ptr(out), N.stream_ptr()))
         return out
+
+    def cache_coefficient_update(self, ubasis, **kwargs):
+        """Opt into the coefficient-update cache of this form on ``ubasis``
+        (no counterpart in the reference): the cells' unit-coefficient
+        stiffness rows in the sum's order and the unit-coefficient mass
+        matrix are kept, and later assemblies with new per-cell stiffness
+        coefficients (and one constant mass coefficient) run as one fused
+        sum over them.  For loops that re-assemble one form many times; it
+        costs nelems * Nbfun^2 + nnz doubles of device memory.  Scalar
+        simplex bases only; elsewhere a no-op."""
+        coeffs = _Coefficients(ubasis, kwargs)
+        ch = self._trace(ubasis, coeffs, "bilinear")
+        if ch is None or ubasis.elem.vector:
+            return self
+        key = ("bilinear", _structure_key(ch))
+        ubasis.__dict__.setdefault("_coef_update", set()).add(key)
+        entry, _vals, _key = self._fast_once(ubasis, coeffs, ch)
+        return self
 
     def pattern(self, ubasis, **kwargs):
         """(indptr, indices) device tensors of the cached CSR pattern."""

@@ -98,22 +98,38 @@ FUSED = [(F.MeshTri, 2, 33, F.ElementTriP1), (F.MeshTri, 2, 17, F.ElementTriP2),
          (F.MeshTet, 3, 11, F.ElementTetP1), (F.MeshTet, 3, 7, F.ElementTetP2)]
 
 
-@pytest.mark.parametrize("form", ["k_lap_mass", "lap_mass_const", "mass_only"])
+@F.BilinearForm
+def k_lap_cmass(u, v, w):
+    return w.k * H.dot(H.grad(u), H.grad(v)) + w.c * u * v
+
+
+@pytest.mark.parametrize("path", ["default", "coefficient_update"])
+@pytest.mark.parametrize("form", ["k_lap_mass", "lap_mass_const", "mass_only", "k_lap_cmass"])
 @pytest.mark.parametrize("cls,dim,n,elem", FUSED, ids=[c[3].__name__ for c in FUSED])
-def test_fused_sum_equals_staging_sum(cls, dim, n, elem, form):
-    """Scalar simplex forms with a constant mass coefficient assemble in one
-    fused sum over the basis's cached stiffness rows and unit mass matrix
-    (K = diff * sum_e k_e S_e + mass * M): equal to the local kernel plus
-    staging sum within 1e-14 of max|K| (the additions are grouped
-    differently), with the same CSR structure, and bitwise on reruns."""
+def test_one_pass_sums_equal_staging_sum(cls, dim, n, elem, form, path):
+    """The one-pass assemblies of scalar simplex forms -- TriP1 / TetP1 by
+    default (each CSR row contracting k_e G_e from the geometry cache and
+    summing |det_e| in exact fixed point, or m_e |det_e| in FP64 for a mass
+    field), and the opt-in coefficient-update cache (K = diff * sum_e k_e S_e
+    + mass * M over cached unit-coefficient rows, constant mass only) -- are
+    equal to the local kernel plus staging sum within 1e-14 of max|K| (the
+    additions are grouped differently), with the same CSR structure, and
+    bitwise on reruns."""
     m = cls.init_tensor(*(np.linspace(0, 1, n),) * dim)
     p = m.p.copy()
     inner = np.all((p > 1e-12) & (p < 1 - 1e-12), axis=0)
     p[:, inner] += np.random.default_rng(5).uniform(-0.2 / n, 0.2 / n, (dim, int(inner.sum())))
     b = F.Basis(cls(p, m.t), elem())
-    f = {"k_lap_mass": k_lap_mass, "lap_mass_const": lap_mass_const, "mass_only": mass_only}[form]
-    kw = {"k": torch.from_numpy(np.random.default_rng(6).lognormal(0, 1, b.nelems)).cuda()} \
-        if form == "k_lap_mass" else {}
+    f = {"k_lap_mass": k_lap_mass, "lap_mass_const": lap_mass_const, "mass_only": mass_only,
+         "k_lap_cmass": k_lap_cmass}[form]
+    rng = np.random.default_rng(6)
+    kw = {}
+    if form in ("k_lap_mass", "k_lap_cmass"):
+        kw["k"] = torch.from_numpy(rng.lognormal(0, 1, b.nelems)).cuda()
+    if form == "k_lap_cmass":
+        kw["c"] = torch.from_numpy(rng.uniform(0.5, 2.0, b.nelems)).cuda()
+    if path == "coefficient_update":
+        f.cache_coefficient_update(b, **kw)
     Kf = f.assemble_torch(b, **kw)
     Kf2 = f.assemble_torch(b, **kw)
     assert torch.equal(Kf.values(), Kf2.values())
@@ -122,6 +138,7 @@ def test_fused_sum_equals_staging_sum(cls, dim, n, elem, form):
     lib = N.lib()
     lib.fem_pattern_drop_geometry(entry.pat.handle)
     entry.geo_key = None
+    entry.coef_update = False
     ref = torch.full_like(Kf.values(), np.nan)
     N.check(lib.fem_assemble(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
                              entry.pat.handle, N.ptr(entry.staging), N.ptr(ref), None,
@@ -160,8 +177,12 @@ def test_fused_checks_report_stale_and_varying():
     vals = torch.empty(entry.nnz, dtype=torch.float64, device="cuda")
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
     seen = []
-    for cached in (True, False):
-        if not cached:
+    for cached in ("coefficient_update", "geometry", None):
+        if cached == "coefficient_update":
+            k_lap_mass.cache_coefficient_update(b, k=torch.from_numpy(k).cuda())
+        elif cached == "geometry":
+            lib.fem_pattern_drop_coefficient_update(entry.pat.handle)
+        else:
             lib.fem_pattern_drop_geometry(entry.pat.handle)
             entry.geo_key = None
         for kd, want in cases:
@@ -187,10 +208,11 @@ COLS = [("TetP1", F.MeshTet, 3, 15, F.ElementTetP1), ("TriP2", F.MeshTri, 2, 41,
 @pytest.mark.parametrize("form", ["k_lap_mass", "lap_mass_const"])
 @pytest.mark.parametrize("fam,cls,dim,n,elem", COLS, ids=[c[0] for c in COLS])
 def test_fused_sum_columns_per_lane_are_bitwise_equal(fam, cls, dim, n, elem, form):
-    """The fused sum with two columns per lane (TetP1, TriP2, TetP2) adds
-    every slot's contributions in the same order as the one-column kernel:
-    equal bit for bit for every unroll, on the device path and through the
-    pipelined host path, in a shuffled cell order."""
+    """The coefficient-update cache's fused sum with two columns per lane
+    (TetP1, TriP2, TetP2) adds every slot's contributions in the same order
+    as the one-column kernel: equal bit for bit for every unroll, on the
+    device path and through the pipelined host path, in a shuffled cell
+    order."""
     from skfem_gb300 import autotune
     m = cls.init_tensor(*(np.linspace(0, 1, n),) * dim)
     perm = np.random.default_rng(8).permutation(m.t.shape[1])
@@ -199,6 +221,7 @@ def test_fused_sum_columns_per_lane_are_bitwise_equal(fam, cls, dim, n, elem, fo
     k = np.random.default_rng(9).lognormal(0, 1, b.nelems)
     kw = {"k": torch.from_numpy(k).cuda()} if form == "k_lap_mass" else {}
     kh = {"k": b.zero_w() + k[:, None]} if form == "k_lap_mass" else {}
+    f.cache_coefficient_update(b, **kw)
     code = N.FAMILY[fam]
     base = {"local_block": 128, "persistent": 0, "sum_unroll": 8, "sum_cols": 1}
     try:
