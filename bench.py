@@ -373,7 +373,7 @@ def gpu_arm(args):
 
     def kern(name, t, bpc):
         out = {"kernel": name, "ms": t, "dram_bytes_per_cell": bpc}
-        if bpc is not None:
+        if bpc is not None and t > 0:
             out["gbs"] = bpc * nel / (t * 1e-3) / 1e9
             out["frac_hbm"] = out["gbs"] / hbm
         return out

@@ -630,8 +630,69 @@ def doflocs_case():
     save("doflocs", **out)
 
 
+def _digest(a):
+    import hashlib
+    return np.frombuffer(hashlib.sha256(np.ascontiguousarray(a).tobytes()).digest(),
+                         dtype=np.uint8).copy()
+
+
+def config_cases():
+    """The benchmark configurations at the sizes the GPU tests assemble them
+    (bench.py's own seeded workloads), run through scikit-fem: per case the
+    nnz, SHA-256 digests of indptr and indices (int32) and the Frobenius norm
+    and sum of the values.  The matrices are too large to store; the digests
+    pin the reference's exact CSR pattern, which the GPU reproduces by
+    replaying numpy's arithmetic of this platform (noise-level local entries
+    that come out exactly 0.0 are dropped by eliminate_zeros)."""
+    root = os.path.dirname(os.path.dirname(OUT))
+    for q in (root, os.path.join(root, "scikit-fem_gb300")):
+        if q not in sys.path:
+            sys.path.insert(0, q)
+    import bench as B
+
+    out = {}
+
+    def record(name, K, **extra):
+        K = K.tocsr()
+        out[name + "__nnz"] = np.array(K.nnz)
+        out[name + "__indptr"] = _digest(K.indptr.astype(np.int32))
+        out[name + "__indices"] = _digest(K.indices.astype(np.int32))
+        out[name + "__fro"] = np.array(np.linalg.norm(K.data))
+        out[name + "__sum"] = np.array(K.data.sum())
+        for k, v in extra.items():
+            out[name + "__" + k] = v
+        print(name, K.nnz)
+
+    # TriP1 Laplace + unit load, 256 x 256 squares
+    m = MeshTri.init_tensor(*(np.linspace(0, 1, 257),) * 2)
+    ib = Basis(m, ElementTriP1())
+    record("tri_p1_256", laplace.assemble(ib), b=unit_load.assemble(ib))
+    # TetP1 k*Laplace + mass, the 61^3-node sample of the 101^3 workload
+    _, k = B.build_workload(61)
+    m = MeshTet.init_tensor(*(np.linspace(0, 1, 61),) * 3)
+    ib = Basis(m, ElementTetP1())
+    record("tet_p1_61", k_laplace_mass.assemble(ib, k=ib.zero_w() + k[:, None]))
+    # Hex1 theta*Laplace, 64^3 cells
+    _, theta, _, _ = B.hex_cube_workload(64)
+    m = MeshHex.init_tensor(*(np.linspace(0, 1, 65),) * 3)
+    ib = Basis(m, ElementHex1())
+    record("hex1_64", theta_laplace.assemble(ib, theta=ib.zero_w() + theta[:, None]))
+    # vector TetP2 elasticity, jittered 16^3 cells, intorder 4
+    fm = B.jittered_tet_cube(16)
+    ib = Basis(MeshTet(fm.p, fm.t), ElementVector(ElementTetP2()), intorder=4)
+    record("vec_tet_p2_16", linear_elasticity(1.0, 0.5).assemble(ib))
+    # four meshes of the batched TriP2 workload
+    meshes, ks = B.trip2_batch(4)
+    for i, (fmm, kk) in enumerate(zip(meshes, ks)):
+        ib = Basis(MeshTri(fmm.p, fmm.t), ElementTriP2())
+        record("trip2_batch_%d" % i, k_laplace.assemble(ib, k=ib.zero_w() + kk[:, None]))
+    np.savez_compressed(os.path.join(OUT, "config_patterns.npz"), **out)
+
+
 if __name__ == "__main__":
-    if sys.argv[1:] == ["--quadrature"]:
+    if sys.argv[1:] == ["--configs"]:
+        config_cases()
+    elif sys.argv[1:] == ["--quadrature"]:
         quadrature_rules()
     elif sys.argv[1:] == ["--doflocs"]:
         doflocs_case()
