@@ -539,7 +539,8 @@ def secondary_workloads(args, only=None):
         def theta_laplace(u, v, w):
             return w.theta * H.dot(H.grad(u), H.grad(v))
 
-        for jit, tag in ((0.0, ""), (0.2, "_jittered")):
+        for jit in args.hex_jitter:
+            tag = "_jittered" if jit > 0 else ""
             m, theta_h, w_h, u_h = hex_cube_workload(args.hex_n, jitter=jit)
             b = F.Basis(m, F.ElementHex1())
             theta = torch.tensor(theta_h, device="cuda")
@@ -777,6 +778,9 @@ def main():
     ap.add_argument("--batch", type=int, default=512, help="meshes of the batched workload")
     ap.add_argument("--vec-n", type=int, default=40, help="cells per axis, vector TetP2 workload")
     ap.add_argument("--hex-n", type=int, default=64, help="cells per axis, Hex1 adjoint workload")
+    ap.add_argument("--hex-jitter", type=float, nargs="+", default=[0.0, 0.2],
+                    help="Hex1 workloads: interior-node jitter (fraction of h) of each case; "
+                         "0 = the tensor cube (parallelepiped cells)")
     ap.add_argument("--generic-n", type=int, default=60,
                     help="cells per axis, generic-kernel TetP1 workload")
     ap.add_argument("--only", default=None,

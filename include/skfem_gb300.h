@@ -212,6 +212,16 @@ const char* fem_version(void);
 int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll, int sum_cols);
 
 /*
+ * The one-pass TriP1 / TetP1 sum's variant, in the same table: 0 two lanes
+ * per CSR row adding (cell, local row) contributions into shared-memory
+ * slots; 1 (the default) one lane per CSR entry on or above the diagonal
+ * walking that entry's contribution list in registers and writing the
+ * entry and its transpose.  Both add every entry's contributions in the
+ * same order: the values are the same bit for bit.
+ */
+int fem_set_onepass(int family, int variant);
+
+/*
  * Local (element) matrices: local[(e * nbfun + i) * nbfun + j] = K_e[i][j],
  * i = test function (row), j = trial function (column), the same entry as
  * the reference's data[j, i, e] (bilinear_form.py:90-98).
@@ -498,6 +508,21 @@ int fem_program_local_matrices_mixed(const FemMesh* mesh, const FemBasis* vbasis
 int fem_pattern_build_local_mixed(const FemMesh* mesh, const FemBasis* vbasis,
                                   const FemBasis* ubasis, const double* local, FemPattern** out,
                                   fem_stream_t stream);
+
+/*
+ * CSR pattern of a general COO matrix (replaces COOData._assemble_scipy_csr,
+ * coo_data.py:27-36, for COOData built or combined by the caller): n
+ * entries (rows[k], cols[k], data[k]) of an nrows x ncols matrix; entries
+ * whose value is exactly +-0.0 create no CSR entry (eliminate_zeros), the
+ * others are summed per (row, column) by fem_csr_sum(pat, data, values)
+ * in ascending entry order.  Rows outside [0, nrows) or columns outside
+ * [0, ncols) are refused (FEM_ERR_ARGUMENT); a row gathering more than
+ * 8,192 entries returns FEM_ERR_CAPACITY.  The pattern is released with
+ * fem_pattern_destroy.
+ */
+int fem_coo_pattern_build(const int32_t* rows, const int32_t* cols, const double* data,
+                          int64_t n, int64_t nrows, int64_t ncols, FemPattern** out,
+                          fem_stream_t stream);
 int fem_program_local_vectors(const FemMesh* mesh, const FemBasis* basis,
                               const FemProgram* program, double* local, int32_t* status,
                               fem_stream_t stream);

@@ -148,6 +148,10 @@ struct FemPattern {
   // when some cell's |det| lies outside the range it covers.
   int16_t* mbase = nullptr;
   bool mbase_ok = false;
+  // The one-pass P1 sum's upper-gather lists (pattern-only; built with the
+  // first geometry cache of a scalar TriP1 / TetP1 pattern).
+  fem::UpperLists upper;
+  bool upper_ok = false, upper_tried = false;
 };
 
 namespace {
@@ -225,6 +229,18 @@ int cache_mass_base(FemPattern* pat, const FemMesh* mesh, const FemBasis* basis,
   int rc = fem::row_mass_base(P, pat->geo + (int64_t)ng * mesh->nelems, pat->mbase, &shmax, &ok, st);
   if (rc) return rc;
   pat->mbase_ok = ok;
+  if (!pat->upper_tried) {
+    // the upper-gather form of the one-pass sum: an optimisation, left out
+    // (with its error cleared) when the pattern is not symmetric or there
+    // is no room for its lists
+    pat->upper_tried = true;
+    rc = fem::build_upper_lists(P, &pat->upper, st);
+    pat->upper_ok = rc == 0;
+    if (rc) {
+      cudaGetLastError();
+      fem::set_error(FEM_OK, "");
+    }
+  }
   return 0;
 }
 
@@ -406,6 +422,16 @@ const char* fem_last_error(void) { return fem::g_err.c_str(); }
 
 const char* fem_version(void) { return "skfem_gb300 0.1 (sm_103a)"; }
 
+int fem_set_onepass(int family, int variant) {
+  if (family < 1 || family > 5 || variant < 0 || variant > 1) {
+    set_error(FEM_ERR_ARGUMENT, "family %d / one-pass variant %d out of range", family, variant);
+    return FEM_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> lock(fem::g_tuning_mu);
+  fem::g_tuning[family].onepass = variant;
+  return 0;
+}
+
 int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll, int sum_cols) {
   if (family < 1 || family > 5 || (local_block != 64 && local_block != 128 && local_block != 256) ||
       persistent < 0 || (sum_unroll != 4 && sum_unroll != 8 && sum_unroll != 16) ||
@@ -540,6 +566,7 @@ void fem_pattern_destroy(FemPattern* pat) {
   cudaFree(pat->plan_cells);
   cudaFree(pat->geo);
   cudaFree(pat->mbase);
+  fem::free_upper_lists(&pat->upper);
   drop_fused(pat);
   delete pat;
 }
@@ -646,7 +673,11 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
     rc = fem_fast::coef_checks(*form, pat->coef_bits, status, st, 0, mesh->nelems, nullptr);
     if (rc) return rc;
     fem::Pattern P = pat->P;
-    P.sum_unroll = fem::tuning_for(basis->family).sum_unroll;
+    const fem::Tuning t = fem::tuning_for(basis->family);
+    P.sum_unroll = t.sum_unroll;
+    if (t.onepass == 1 && pat->upper_ok)
+      return fem::csr_sum_upper_p1(P, pat->upper, mesh->dim, pat->geo, form->diff, form->mass,
+                                   pat->mbase, csr_values, st);
     return fem::csr_sum_geometry_p1(P, mesh->dim, pat->geo, form->diff, form->mass, pat->mbase,
                                     csr_values, st);
   }
@@ -715,6 +746,7 @@ struct GeometrySum {
   const double* geo;
   FemCoef diff, mass;
   const int16_t* mbase;
+  const fem::UpperLists* upper;   // null: the row kernel
 };
 
 int sum_rows_to_host(const fem::Pattern& P, const std::vector<int32_t>& ip, const double* staging,
@@ -723,8 +755,11 @@ int sum_rows_to_host(const fem::Pattern& P, const std::vector<int32_t>& ip, cons
                      const GeometrySum* gs = nullptr) {
   int rc = fs ? fem::csr_sum_scaled(P, fs->stiff, fs->diff, fs->mass1, fs->mscale, csr_values, st,
                                     row0, row1)
-           : gs ? fem::csr_sum_geometry_p1(P, gs->dim, gs->geo, gs->diff, gs->mass, gs->mbase,
-                                           csr_values, st, row0, row1)
+           : gs ? (gs->upper ? fem::csr_sum_upper_p1(P, *gs->upper, gs->dim, gs->geo, gs->diff,
+                                                      gs->mass, gs->mbase, csr_values, st, row0,
+                                                      row1)
+                             : fem::csr_sum_geometry_p1(P, gs->dim, gs->geo, gs->diff, gs->mass,
+                                                        gs->mbase, csr_values, st, row0, row1))
                 : fem::csr_sum(P, staging, csr_values, st, row0, row1, nullptr, P.staging_sym);
   if (rc) return rc;
   const int64_t a = ip[row0], b = ip[row1];
@@ -1025,7 +1060,8 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
   const int32_t* cells = pat->plan_cells;
   FusedSum fs;
   const bool fused = fused_sum(pat, mesh, basis, form, &fs);
-  GeometrySum gs{mesh->dim, pat->geo, form->diff, form->mass, pat->mbase};
+  GeometrySum gs{mesh->dim, pat->geo, form->diff, form->mass, pat->mbase,
+                 (tune.onepass == 1 && pat->upper_ok) ? &pat->upper : nullptr};
   const bool onepass = !fused && geometry_sum(pat, mesh, basis, form);
   std::vector<cudaEvent_t> evs;
   auto event = [&](cudaEvent_t* ev) -> cudaError_t {
@@ -1211,6 +1247,55 @@ int fem_pattern_build_local_mixed(const FemMesh* mesh, const FemBasis* vbasis,
   rc = fem::build_incidence(vbasis->element_dofs, mesh->nelems, vbasis->nbfun, vbasis->ndofs,
                             &H->P, st);
   if (!rc) rc = fem::build_csr(ubasis->element_dofs, ubasis->nbfun, ubasis->ndofs, local, &H->P, st);
+  if (!rc) rc = host_row_pointer(H, st);
+  if (rc) {
+    fem::free_pattern(new fem::Pattern(H->P));
+    delete H;
+    return rc;
+  }
+  *out = H;
+  return 0;
+}
+
+namespace {
+__global__ void index_range_kernel(const int32_t* __restrict__ idx, int64_t n, int64_t hi,
+                                   int32_t* __restrict__ bad) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    if (idx[i] < 0 || idx[i] >= hi) atomicOr(bad, 1);
+}
+}  // namespace
+
+int fem_coo_pattern_build(const int32_t* rows, const int32_t* cols, const double* data,
+                          int64_t n, int64_t nrows, int64_t ncols, FemPattern** out,
+                          fem_stream_t stream) {
+  if (!out || n < 0 || nrows < 0 || ncols < 0 || (n > 0 && (!rows || !cols || !data))) {
+    set_error(FEM_ERR_ARGUMENT, "null COO arrays or output handle, or a negative size");
+    return FEM_ERR_ARGUMENT;
+  }
+  *out = nullptr;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n > 0) {
+    fem::AsyncScratch scratch(st);
+    int32_t* bad = nullptr;
+    FEM_TRY_CUDA(scratch.alloc(&bad, sizeof(int32_t)));
+    FEM_TRY_CUDA(cudaMemsetAsync(bad, 0, sizeof(int32_t), st));
+    const unsigned grid = (unsigned)std::min<int64_t>(fem::ceil_div(n, 256), fem::num_sms() * 8);
+    index_range_kernel<<<grid, 256, 0, st>>>(cols, n, ncols, bad);
+    FEM_LAUNCH_CHECK("index_range_kernel");
+    int32_t h = 0;
+    FEM_TRY_CUDA(cudaMemcpyAsync(&h, bad, sizeof(h), cudaMemcpyDeviceToHost, st));
+    FEM_TRY_CUDA(cudaStreamSynchronize(st));
+    if (h) {
+      set_error(FEM_ERR_ARGUMENT, "a COO column index lies outside [0, %lld)", (long long)ncols);
+      return FEM_ERR_ARGUMENT;
+    }
+  }
+  FemPattern* H = new FemPattern();
+  // each COO entry is a 1 x 1 "cell": its row the test DOF, its column the
+  // trial DOF, its value the local entry (exact zeros create no CSR entry)
+  int rc = fem::build_incidence(rows, n, 1, nrows, &H->P, st);
+  if (!rc) rc = fem::build_csr(cols, 1, ncols, data, &H->P, st);
   if (!rc) rc = host_row_pointer(H, st);
   if (rc) {
     fem::free_pattern(new fem::Pattern(H->P));

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <algorithm>
 #include <string>
+#include <vector>
 
 #include "../../include/skfem_gb300.h"
 
@@ -172,6 +173,7 @@ struct Tuning {
   int persistent = 0;     // >0: grid capped at persistent * SMs (grid-stride)
   int sum_unroll = 8;     // incidence entries loaded together in the sum
   int sum_cols = 1;       // fused sum: columns per lane (1, or 2 for an even row length)
+  int onepass = 1;        // one-pass P1 sum: 0 two lanes per row, 1 a lane per upper entry
 };
 Tuning tuning_for(int family);
 
@@ -208,6 +210,27 @@ int csr_sum_geometry_p1(const Pattern& P, int dim, const double* geo, const FemC
 // the fixed point covers (degenerate or non-finite cells).
 int row_mass_base(const Pattern& P, const double* adet, int16_t* mbase, int* shmax, bool* ok,
                   cudaStream_t st);
+
+// The one-pass P1 sum in its upper-gather form (csr_upper_p1_kernel): per
+// CSR entry on or above the diagonal, the (cell, local pair) contributions
+// in the sum's order, sliced 32 entries at a time.  Pattern-only data.
+struct UpperLists {
+  int64_t nd = 0, nupper = 0, nslices = 0, ncodes = 0;
+  int32_t* dpos = nullptr;      // nrows + 1: row -> first diagonal entry
+  int32_t* opos = nullptr;      // nrows + 1: row -> first off-diagonal entry (after nd)
+  int32_t* pos = nullptr;       // nupper: CSR index of (i, j)
+  int32_t* tpos = nullptr;      // nupper: CSR index of (j, i); -1 on the diagonal
+  int32_t* row = nullptr;       // nupper: i
+  int32_t* slice_len = nullptr;   // nslices
+  int32_t* slice_base = nullptr;  // nslices: first code row (32 codes) of the slice
+  uint32_t* codes = nullptr;    // ncodes: e * 16 + li * 4 + lj, 0xFFFFFFFF padding
+  std::vector<int32_t> dpos_h, opos_h;
+};
+int build_upper_lists(const Pattern& P, UpperLists* U, cudaStream_t st);
+void free_upper_lists(UpperLists* U);
+int csr_sum_upper_p1(const Pattern& P, const UpperLists& U, int dim, const double* geo,
+                     const FemCoef& diff, const FemCoef& mass, const int16_t* mbase, double* vals,
+                     cudaStream_t st, int64_t row0 = 0, int64_t row1 = -1);
 
 int basis_nb_scalar(int family);
 int basis_dim(int family);

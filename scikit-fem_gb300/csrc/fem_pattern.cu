@@ -495,6 +495,11 @@ __device__ __forceinline__ long long fixed_of(double x, int base) {
   return sh >= 0 ? (long long)(man << sh) : (long long)(man >> min(-sh, 63));
 }
 
+// Packed symmetric index of Gram entry (a, b) (row-major upper triangle).
+__host__ __device__ constexpr int gram_index(int nu, int a, int b) {
+  return a <= b ? a * (2 * nu + 1 - a) / 2 + b - a : b * (2 * nu + 1 - b) / 2 + a - b;
+}
+
 template <int NU, int U, bool MFIELD>
 __global__ void __launch_bounds__(128) csr_geometry_p1_kernel(
     const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
@@ -516,6 +521,13 @@ __global__ void __launch_bounds__(128) csr_geometry_p1_kernel(
                ((size_t)wib * RPW + sub) * stride;
   const int j0 = 2 * h, j1 = 2 * h + 1;
   const bool has1 = j1 < NU;
+  // this lane's Gram arrays for local rows l = 0 .. NU-1, 4 bits each
+  uint32_t tab0 = 0, tab1 = 0;
+#pragma unroll
+  for (int l = 0; l < NU; ++l) {
+    tab0 |= (uint32_t)gram_index(NU, l, j0) << (4 * l);
+    if (has1) tab1 |= (uint32_t)gram_index(NU, l, j1) << (4 * l);
+  }
   const double* __restrict__ adet_arr = geo + (int64_t)NG * nelems;
   const int64_t rows_per_block = (int64_t)(blockDim.x >> 5) * RPW;
   for (int64_t rb = row0 + (int64_t)blockIdx.x * rows_per_block; rb < nrows;
@@ -537,36 +549,45 @@ __global__ void __launch_bounds__(128) csr_geometry_p1_kernel(
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
     __syncwarp();
+    // the incidence codes of the next U entries are loaded one batch ahead,
+    // so that each batch waits for one round of gathers, not two
+    uint32_t cnext[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) cnext[u] = u < len ? (uint32_t)__ldg(inc + b + u) : 0u;
     for (int q0 = 0; q0 < maxlen; q0 += U) {
+      uint32_t code[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        code[u] = cnext[u];
+        const int qn = q0 + U + u;
+        cnext[u] = qn < len ? (uint32_t)__ldg(inc + b + qn) : 0u;
+      }
       double kv[U], g0[U], g1[U];
       MAcc mv[U];
-      uint32_t s0[U], s1[U];
+      uint32_t sp[U];
       int il[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int q = q0 + u;
-        s0[u] = 0xFFFFu;
-        s1[u] = 0xFFFFu;
+        sp[u] = 0xFFFFFFFFu;
         kv[u] = 0.0;
         g0[u] = 0.0;
         g1[u] = 0.0;
         mv[u] = (MAcc)0;
         il[u] = -1;
         if (q < len) {
-          const uint32_t code = (uint32_t)__ldg(inc + b + q);
-          const uint32_t e = NU == 4 ? (code >> 2) : (__umulhi(code, 0xAAAAAAABu) >> 1);
-          const int l = (int)(code - e * NU);
+          const uint32_t e = NU == 4 ? (code[u] >> 2) : (__umulhi(code[u], 0xAAAAAAABu) >> 1);
+          const int l = (int)(code[u] - e * NU);
           il[u] = l;
           const uint16_t* sq = slot + ((int64_t)b + q) * NU;
-          s0[u] = __ldg(sq + j0);
-          if (has1) s1[u] = __ldg(sq + j1);
-          kv[u] = kfield ? __ldg(kfield + (int64_t)e * kstride) : 1.0;
-          const int a0 = min(l, j0), c0 = max(l, j0);
-          g0[u] = __ldg(geo + (int64_t)(a0 * (2 * NU + 1 - a0) / 2 + c0 - a0) * nelems + e);
-          if (has1) {
-            const int a1 = min(l, j1), c1 = max(l, j1);
-            g1[u] = __ldg(geo + (int64_t)(a1 * (2 * NU + 1 - a1) / 2 + c1 - a1) * nelems + e);
+          if constexpr (NU % 2 == 0) {
+            sp[u] = __ldg(reinterpret_cast<const uint32_t*>(sq + j0));
+          } else {
+            sp[u] = (uint32_t)__ldg(sq + j0) | (has1 ? (uint32_t)__ldg(sq + j1) << 16 : 0xFFFF0000u);
           }
+          kv[u] = kfield ? __ldg(kfield + (int64_t)e * kstride) : 1.0;
+          g0[u] = __ldg(geo + (int64_t)((tab0 >> (4 * l)) & 15u) * nelems + e);
+          if (has1) g1[u] = __ldg(geo + (int64_t)((tab1 >> (4 * l)) & 15u) * nelems + e);
           const double adet = __ldg(adet_arr + e);
           if constexpr (MFIELD) mv[u] = __ldg(mfield + (int64_t)e * mstride) * adet;
           else mv[u] = fixed_of(adet, base);
@@ -574,13 +595,14 @@ __global__ void __launch_bounds__(128) csr_geometry_p1_kernel(
       }
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        if (s0[u] != 0xFFFFu) {
-          acck[s0[u]] = __fma_rn(kv[u], g0[u], acck[s0[u]]);
-          accm[s0[u]] += il[u] == j0 ? mv[u] + mv[u] : mv[u];
+        const uint32_t s0 = sp[u] & 0xFFFFu, s1 = sp[u] >> 16;
+        if (s0 != 0xFFFFu) {
+          acck[s0] = __fma_rn(kv[u], g0[u], acck[s0]);
+          accm[s0] += il[u] == j0 ? mv[u] + mv[u] : mv[u];
         }
-        if (s1[u] != 0xFFFFu) {
-          acck[s1[u]] = __fma_rn(kv[u], g1[u], acck[s1[u]]);
-          accm[s1[u]] += il[u] == j1 ? mv[u] + mv[u] : mv[u];
+        if (s1 != 0xFFFFu) {
+          acck[s1] = __fma_rn(kv[u], g1[u], acck[s1]);
+          accm[s1] += il[u] == j1 ? mv[u] + mv[u] : mv[u];
         }
         __syncwarp();
       }
@@ -598,6 +620,235 @@ __global__ void __launch_bounds__(128) csr_geometry_p1_kernel(
       vals[p0 + k] = __fma_rn(mc, m, kscale * acck[k]);
     }
     __syncwarp();
+  }
+}
+
+// ------------------------------------------ one-pass P1, upper gather form
+// The same assembly as csr_geometry_p1_kernel with one lane per CSR entry
+// on or above the diagonal (an "upper entry" (i, j), j >= i) instead of
+// two lanes per row: the lane walks the entry's contribution list -- every
+// (cell e, local pair (li, lj)) with dof(li) = i, dof(lj) = j whose local
+// entry is not an exact zero, in ascending (e, li) order, the order in
+// which the row kernel adds them into the slot -- accumulating
+//   acc_k = fma(k_e, G_e[li][lj], acc_k)      (FP64, in registers)
+//   acc_m += |det_e| (twice on the diagonal)  (exact fixed point / FP64)
+// and writes the entry to (i, j) and, off the diagonal, to (j, i): the
+// symmetric forms' local matrices are symmetric bit for bit
+// (G_e[li][lj] is one cached number), so the two positions receive the
+// same additions in the same order.  Each cell's 10 (TetP1) or 6 (TriP1)
+// Gram entries are read and multiplied once, and there is no shared-memory
+// accumulation or warp barrier: every lane's sum lives in its registers.
+// The values equal csr_geometry_p1_kernel's bit for bit.
+//
+// Lists are stored sliced: 32 consecutive upper entries form a slice of
+// len = the longest list among them; code p of the slice's lane l sits at
+// codes[(base + p) * 32 + l] (coalesced), padded with 0xFFFFFFFF.  A code
+// is e * 16 + li * 4 + lj.  Upper entries are numbered diagonal entries
+// first (by row), then the others by (row, column), so list lengths within
+// a slice are alike (a vertex's cells vs an edge's cells).
+template <int NU, int U, bool MFIELD>
+__global__ void __launch_bounds__(128) csr_upper_p1_kernel(
+    int64_t ua, int64_t ub, const int32_t* __restrict__ slice_len,
+    const int32_t* __restrict__ slice_base, const uint32_t* __restrict__ codes,
+    const int32_t* __restrict__ pos, const int32_t* __restrict__ tpos,
+    const int32_t* __restrict__ urow, const double* __restrict__ geo, int64_t nelems,
+    const double* __restrict__ kfield, int64_t kstride, double kscale,
+    const double* __restrict__ mfield, int64_t mstride, double mscale, double moff,
+    const int16_t* __restrict__ mbase, double* __restrict__ vals) {
+  constexpr int NG = NU * (NU + 1) / 2;
+  using MAcc = typename std::conditional<MFIELD, double, long long>::type;
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t s0 = ua >> 5, s1 = (ub + 31) >> 5;
+  const double* __restrict__ adet_arr = geo + (int64_t)NG * nelems;
+  for (int64_t sl = s0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); sl < s1;
+       sl += warps) {
+    const int64_t u = sl * 32 + lane;
+    const bool live = u >= ua && u < ub;
+    const int len = slice_len[sl];
+    const int64_t base = slice_base[sl];
+    int mb = 0;
+    if (!MFIELD && live) mb = mbase[urow[u]];
+    const uint32_t* __restrict__ cp = codes + base * 32 + lane;
+    double acck = 0.0;
+    MAcc accm = (MAcc)0;
+    uint32_t cn[U];
+#pragma unroll
+    for (int v = 0; v < U; ++v) cn[v] = v < len ? __ldg(cp + (int64_t)v * 32) : 0xFFFFFFFFu;
+    for (int p0 = 0; p0 < len; p0 += U) {
+      uint32_t c[U];
+#pragma unroll
+      for (int v = 0; v < U; ++v) {
+        c[v] = cn[v];
+        const int pn = p0 + U + v;
+        cn[v] = pn < len ? __ldg(cp + (int64_t)pn * 32) : 0xFFFFFFFFu;
+      }
+      double kv[U], g[U];
+      MAcc mv[U];
+#pragma unroll
+      for (int v = 0; v < U; ++v) {
+        kv[v] = 0.0;
+        g[v] = 0.0;
+        mv[v] = (MAcc)0;
+        if (live && c[v] != 0xFFFFFFFFu) {
+          const uint32_t e = c[v] >> 4;
+          const int li = (int)((c[v] >> 2) & 3u), lj = (int)(c[v] & 3u);
+          kv[v] = kfield ? __ldg(kfield + (int64_t)e * kstride) : 1.0;
+          g[v] = __ldg(geo + (int64_t)gram_index(NU, li, lj) * nelems + e);
+          const double adet = __ldg(adet_arr + e);
+          MAcc m;
+          if constexpr (MFIELD) m = __ldg(mfield + (int64_t)e * mstride) * adet;
+          else m = fixed_of(adet, mb);
+          mv[v] = li == lj ? m + m : m;
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < U; ++v) {
+        acck = __fma_rn(kv[v], g[v], acck);
+        accm += mv[v];
+      }
+    }
+    if (live) {
+      double mc;
+      if constexpr (MFIELD) {
+        mc = moff;
+      } else {
+        const double unit = dfrombits((unsigned long long)(mb - 1075 + 1023) << 52);
+        mc = (mscale * moff) * unit;
+      }
+      const double m = MFIELD ? (double)accm : __ll2double_rn((long long)accm);
+      const double val = __fma_rn(mc, m, kscale * acck);
+      vals[pos[u]] = val;
+      const int32_t t = tpos[u];
+      if (t >= 0) vals[t] = val;
+    }
+  }
+}
+
+// Upper-entry numbering of a square pattern, one thread per row: the
+// offset of the diagonal (or of the first column above it) in row i, and
+// whether the diagonal is present; then the number of upper entries.
+__global__ void upper_count_kernel(const int32_t* __restrict__ indptr,
+                                   const int32_t* __restrict__ indices, int64_t nrows,
+                                   int32_t* __restrict__ ndiag, int32_t* __restrict__ noff) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrows) return;
+  const int32_t p0 = indptr[i], p1 = indptr[i + 1];
+  int lo = p0, hi = p1;                     // first column >= i
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (indices[mid] < i) lo = mid + 1;
+    else hi = mid;
+  }
+  const bool d = lo < p1 && indices[lo] == i;
+  ndiag[i] = d ? 1 : 0;
+  noff[i] = p1 - lo - (d ? 1 : 0);
+}
+
+// Per row i: pos / tpos / row of its upper entries, and the length of each
+// entry's contribution list (cnt, indexed by upper entry).
+__global__ void upper_fill_kernel(const int32_t* __restrict__ indptr,
+                                  const int32_t* __restrict__ indices,
+                                  const int32_t* __restrict__ inc_ptr,
+                                  const int32_t* __restrict__ inc,
+                                  const uint16_t* __restrict__ slot, int nu, int64_t nrows,
+                                  const int32_t* __restrict__ dpos, const int32_t* __restrict__ opos,
+                                  int64_t nd, int32_t* __restrict__ pos, int32_t* __restrict__ tpos,
+                                  int32_t* __restrict__ urow, int32_t* __restrict__ cnt,
+                                  int32_t* __restrict__ asym) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrows) return;
+  const int32_t p0 = indptr[i], p1 = indptr[i + 1];
+  int lo = p0, hi = p1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (indices[mid] < i) lo = mid + 1;
+    else hi = mid;
+  }
+  const bool d = lo < p1 && indices[lo] == i;
+  const int sd = lo - p0;                   // offset of the diagonal / first upper column
+  const int so = sd + (d ? 1 : 0);          // offset of the first column above the diagonal
+  if (d) {
+    const int64_t u = dpos[i];
+    pos[u] = lo;
+    tpos[u] = -1;
+    urow[u] = (int32_t)i;
+    cnt[u] = 0;
+  }
+  for (int s = so; s < p1 - p0; ++s) {
+    const int64_t u = nd + opos[i] + (s - so);
+    const int32_t j = indices[p0 + s];
+    pos[u] = p0 + s;
+    // (j, i) in row j: i < j is among its columns (the pattern is symmetric)
+    int a = indptr[j], z = indptr[j + 1];
+    while (a < z) {
+      const int mid = (a + z) >> 1;
+      if (indices[mid] < i) a = mid + 1;
+      else z = mid;
+    }
+    const bool found = a < indptr[j + 1] && indices[a] == i;
+    tpos[u] = found ? a : -1;
+    if (!found) atomicOr(asym, 1);      // not a symmetric pattern: no upper form
+    urow[u] = (int32_t)i;
+    cnt[u] = 0;
+  }
+  const int32_t b = inc_ptr[i], len = inc_ptr[i + 1] - b;
+  for (int q = 0; q < len; ++q)
+    for (int j = 0; j < nu; ++j) {
+      const uint16_t sv = slot[((int64_t)b + q) * nu + j];
+      if (sv == 0xFFFF || (int)sv < sd) continue;
+      const int64_t u = ((int)sv == sd && d) ? (int64_t)dpos[i] : nd + opos[i] + ((int)sv - so);
+      cnt[u] += 1;
+    }
+}
+
+// slice_len[sl] = longest list among the slice's 32 entries
+__global__ void upper_slice_len_kernel(const int32_t* __restrict__ cnt, int64_t nupper,
+                                       int64_t nslices, int32_t* __restrict__ slice_len) {
+  const int64_t sl = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (sl >= nslices) return;
+  const int64_t u = sl * 32 + lane;
+  int v = u < nupper ? cnt[u] : 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if (lane == 0) slice_len[sl] = v;
+}
+
+// Codes of every list, in ascending (cell, local row) order: one thread per
+// row walks the row's incidence (ascending) and appends to its entries.
+__global__ void upper_codes_kernel(const int32_t* __restrict__ indptr,
+                                   const int32_t* __restrict__ indices,
+                                   const int32_t* __restrict__ inc_ptr,
+                                   const int32_t* __restrict__ inc,
+                                   const uint16_t* __restrict__ slot, int nu, int64_t nrows,
+                                   const int32_t* __restrict__ dpos,
+                                   const int32_t* __restrict__ opos, int64_t nd,
+                                   const int32_t* __restrict__ slice_base,
+                                   int32_t* __restrict__ cursor, uint32_t* __restrict__ codes) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrows) return;
+  const int32_t p0 = indptr[i], p1 = indptr[i + 1];
+  int lo = p0, hi = p1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (indices[mid] < i) lo = mid + 1;
+    else hi = mid;
+  }
+  const bool d = lo < p1 && indices[lo] == i;
+  const int sd = lo - p0, so = sd + (d ? 1 : 0);
+  const int32_t b = inc_ptr[i], len = inc_ptr[i + 1] - b;
+  for (int q = 0; q < len; ++q) {
+    const uint32_t code = (uint32_t)inc[b + q];
+    const uint32_t e = code / (uint32_t)nu;
+    const uint32_t li = code - e * (uint32_t)nu;
+    for (int j = 0; j < nu; ++j) {
+      const uint16_t sv = slot[((int64_t)b + q) * nu + j];
+      if (sv == 0xFFFF || (int)sv < sd) continue;
+      const int64_t u = ((int)sv == sd && d) ? (int64_t)dpos[i] : nd + opos[i] + ((int)sv - so);
+      const int c = cursor[u]++;
+      codes[((int64_t)slice_base[u >> 5] + c) * 32 + (u & 31)] = (e << 4) | (li << 2) | (uint32_t)j;
+    }
   }
 }
 
@@ -1165,6 +1416,171 @@ int csr_sum_geometry_p1(const Pattern& P, int dim, const double* geo, const FemC
 #undef FEM_GEO_PICK
   if (rc) return rc;
   FEM_LAUNCH_CHECK("csr_geometry_p1_kernel");
+  return 0;
+}
+
+
+int build_upper_lists(const Pattern& P, UpperLists* U, cudaStream_t st) {
+  *U = UpperLists();
+  const int nu = P.nbfun_u;
+  if (!P.has_matrix || P.nbfun_v != nu || nu > 4) {
+    set_error(FEM_ERR_ARGUMENT, "upper lists need a square pattern of at most 4 local functions");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (P.nelems >= ((int64_t)1 << 28)) {
+    set_error(FEM_ERR_CAPACITY, "%lld cells exceed the upper lists' 28-bit cell codes",
+              (long long)P.nelems);
+    return FEM_ERR_CAPACITY;
+  }
+  const int64_t n = P.nrows;
+  AsyncScratch scratch(st);
+  int32_t *nd = nullptr, *no = nullptr, *cnt = nullptr;
+  FEM_TRY_CUDA(scratch.alloc(&nd, (n + 1) * sizeof(int32_t)));
+  FEM_TRY_CUDA(scratch.alloc(&no, (n + 1) * sizeof(int32_t)));
+  FEM_TRY_CUDA(cudaMemsetAsync(nd, 0, (n + 1) * sizeof(int32_t), st));
+  FEM_TRY_CUDA(cudaMemsetAsync(no, 0, (n + 1) * sizeof(int32_t), st));
+  if (n > 0) {
+    upper_count_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(P.indptr, P.indices, n, nd, no);
+    FEM_LAUNCH_CHECK("upper_count_kernel");
+  }
+  auto fail = [&](int rc) {
+    free_upper_lists(U);
+    return rc;
+  };
+  int64_t tot_d = 0, tot_o = 0;
+  FEM_TRY_CUDA(cudaMalloc(&U->dpos, (n + 1) * sizeof(int32_t)));
+  FEM_TRY_CUDA(cudaMalloc(&U->opos, (n + 1) * sizeof(int32_t)));
+  int rc = exclusive_scan_i32(nd, U->dpos, n, &tot_d, st);
+  if (!rc) rc = exclusive_scan_i32(no, U->opos, n, &tot_o, st);
+  if (rc) return fail(rc);
+  U->nd = tot_d;
+  U->nupper = tot_d + tot_o;
+  U->nslices = ceil_div(U->nupper, 32);
+  const int64_t nup1 = std::max<int64_t>(1, U->nupper);
+  cudaError_t e = cudaMalloc(&U->pos, nup1 * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&U->tpos, nup1 * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&U->row, nup1 * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&U->slice_len, (U->nslices + 1) * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&U->slice_base, (U->nslices + 1) * sizeof(int32_t));
+  if (e != cudaSuccess) return fail(check_cuda(e, "cudaMalloc(upper lists)"));
+  int32_t* asym = nullptr;
+  e = scratch.alloc(&cnt, nup1 * sizeof(int32_t));
+  if (e == cudaSuccess) e = scratch.alloc(&asym, sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMemsetAsync(asym, 0, sizeof(int32_t), st);
+  if (e != cudaSuccess) return fail(check_cuda(e, "cudaMallocAsync(upper list lengths)"));
+  if (n > 0) {
+    upper_fill_kernel<<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(
+        P.indptr, P.indices, P.inc_ptr, P.inc, P.slot, nu, n, U->dpos, U->opos, U->nd, U->pos,
+        U->tpos, U->row, cnt, asym);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(check_cuda(e, "upper_fill_kernel"));
+    int32_t h = 0;
+    e = cudaMemcpyAsync(&h, asym, sizeof(h), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(check_cuda(e, "upper_fill_kernel"));
+    if (h) {
+      set_error(FEM_ERR_UNSUPPORTED, "the CSR pattern is not symmetric: no upper lists");
+      return fail(FEM_ERR_UNSUPPORTED);
+    }
+  }
+  FEM_TRY_CUDA(cudaMemsetAsync(U->slice_len, 0, (U->nslices + 1) * sizeof(int32_t), st));
+  if (U->nslices > 0) {
+    upper_slice_len_kernel<<<(unsigned)ceil_div(U->nslices * 32, 256), 256, 0, st>>>(
+        cnt, U->nupper, U->nslices, U->slice_len);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(check_cuda(e, "upper_slice_len_kernel"));
+  }
+  int64_t rows32 = 0;
+  rc = exclusive_scan_i32(U->slice_len, U->slice_base, U->nslices, &rows32, st);
+  if (rc) return fail(rc);
+  if (rows32 * 32 >= INT32_MAX) {
+    set_error(FEM_ERR_CAPACITY, "upper lists of %lld codes exceed int32 offsets",
+              (long long)(rows32 * 32));
+    return fail(FEM_ERR_CAPACITY);
+  }
+  U->ncodes = rows32 * 32;
+  e = cudaMalloc(&U->codes, std::max<int64_t>(1, U->ncodes) * sizeof(uint32_t));
+  if (e != cudaSuccess) return fail(check_cuda(e, "cudaMalloc(upper codes)"));
+  FEM_TRY_CUDA(cudaMemsetAsync(U->codes, 0xFF, std::max<int64_t>(1, U->ncodes) * sizeof(uint32_t), st));
+  FEM_TRY_CUDA(cudaMemsetAsync(cnt, 0, nup1 * sizeof(int32_t), st));
+  if (n > 0) {
+    upper_codes_kernel<<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(
+        P.indptr, P.indices, P.inc_ptr, P.inc, P.slot, nu, n, U->dpos, U->opos, U->nd,
+        U->slice_base, cnt, U->codes);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(check_cuda(e, "upper_codes_kernel"));
+  }
+  // host copies of the row -> upper-entry offsets (row ranges of the
+  // pipelined host path)
+  U->dpos_h.resize(n + 1);
+  U->opos_h.resize(n + 1);
+  e = cudaMemcpyAsync(U->dpos_h.data(), U->dpos, (n + 1) * sizeof(int32_t),
+                      cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(U->opos_h.data(), U->opos, (n + 1) * sizeof(int32_t),
+                        cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail(check_cuda(e, "upper lists"));
+  return 0;
+}
+
+void free_upper_lists(UpperLists* U) {
+  if (!U) return;
+  cudaFree(U->dpos);
+  cudaFree(U->opos);
+  cudaFree(U->pos);
+  cudaFree(U->tpos);
+  cudaFree(U->row);
+  cudaFree(U->slice_len);
+  cudaFree(U->slice_base);
+  cudaFree(U->codes);
+  *U = UpperLists();
+}
+
+int csr_sum_upper_p1(const Pattern& P, const UpperLists& U, int dim, const double* geo,
+                     const FemCoef& diff, const FemCoef& mass, const int16_t* mbase, double* vals,
+                     cudaStream_t st, int64_t row0, int64_t row1) {
+  const int nu = dim + 1;
+  if (!U.codes || P.nbfun_u != nu || (dim != 2 && dim != 3)) {
+    set_error(FEM_ERR_ARGUMENT, "the upper-gather P1 sum needs the pattern's upper lists");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (!mass.field && !mbase) {
+    set_error(FEM_ERR_ARGUMENT, "the one-pass P1 sum needs the rows' mass binary points");
+    return FEM_ERR_ARGUMENT;
+  }
+  if (row1 < 0 || row1 > P.nrows) row1 = P.nrows;
+  if (row0 < 0) row0 = 0;
+  if (row1 <= row0 || U.nupper == 0) return 0;
+  const double moff = dim == 3 ? 0.05 * (1.0 / 6.0) : (1.0 / 12.0) * 0.5;
+  const double* kf = diff.field;
+  const int64_t ks = diff.stride > 1 ? diff.stride : 1;
+  const double* mf = mass.field;
+  const int64_t ms = mass.stride > 1 ? mass.stride : 1;
+  const int Un = P.sum_unroll >= 8 ? 8 : 4;
+  // upper entries of rows [row0, row1): a diagonal range and an off-diagonal one
+  const int64_t ranges[2][2] = {{U.dpos_h[row0], U.dpos_h[row1]},
+                                {U.nd + U.opos_h[row0], U.nd + U.opos_h[row1]}};
+  const int threads = 128;
+  for (int k = 0; k < 2; ++k) {
+    const int64_t ua = ranges[k][0], ub = ranges[k][1];
+    if (ub <= ua) continue;
+    const int64_t nsl = ((ub + 31) >> 5) - (ua >> 5);
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nsl, threads / 32),
+                                                                (int64_t)num_sms() * 32));
+    auto launch = [&](auto kern) {
+      kern<<<grid, threads, 0, st>>>(ua, ub, U.slice_len, U.slice_base, U.codes, U.pos, U.tpos,
+                                     U.row, geo, P.nelems, kf, ks, diff.scale, mf, ms, mass.scale,
+                                     moff, mbase, vals);
+    };
+#define FEM_UP_PICK(NU)                                                                     \
+    if (mf) { if (Un == 8) launch(csr_upper_p1_kernel<NU, 8, true>); else launch(csr_upper_p1_kernel<NU, 4, true>); } \
+    else { if (Un == 8) launch(csr_upper_p1_kernel<NU, 8, false>); else launch(csr_upper_p1_kernel<NU, 4, false>); }
+    if (nu == 4) { FEM_UP_PICK(4) }
+    else { FEM_UP_PICK(3) }
+#undef FEM_UP_PICK
+    FEM_LAUNCH_CHECK("csr_upper_p1_kernel");
+  }
   return 0;
 }
 

@@ -202,7 +202,9 @@ __global__ void simplex_bilinear_vjp_kernel(FemMesh m, FemBasis b, FemBilinear f
   const double kd = coef_at(f.diff, e), km = coef_at(f.mass, e);
   if (dcd) dcd[e] = f.diff.scale * V * S;
   if (dcm) dcm[e] = f.mass.scale * V * mu;
-  // P = (Q + Q^T) G
+  // P = (Q + Q^T) G -- the vertex gradients, only when dX was asked for
+  // (scratch null: the coefficient gradients alone)
+  if (!scratch) return;
 #pragma unroll
   for (int n = 0; n < NV; ++n) {
     double grad[D];
@@ -244,6 +246,7 @@ __global__ void simplex_linear_vjp_kernel(FemMesh m, FemBasis b, FemLinear f,
 #undef W
   const double fe = coef_at(f.load, e);
   if (dl) dl[e] = f.load.scale * V * lw;
+  if (!scratch) return;
 #pragma unroll
   for (int n = 0; n < NV; ++n)
 #pragma unroll
@@ -611,6 +614,7 @@ __device__ __noinline__ void hex_vjp_general(const FemMesh m, const FemBasis b, 
   }
   if (dcd) dcd[e] = cd.scale * Ed;
   if (MODE == 0 && dcm) dcm[e] = cm.scale * Em;
+  if (!scratch) return;   // no dX asked for: the coefficient gradients alone
 #pragma unroll
   for (int n = 0; n < 8; ++n)
 #pragma unroll
@@ -661,6 +665,7 @@ __global__ void hex_vjp_kernel(FemMesh m, FemBasis b, FemCoef cd, FemCoef cm,
   hex_vjp_affine<MODE>(x, wl, ul, kd, km, Ed, Em, gx, status);
   if (dcd) dcd[e] = cd.scale * Ed;
   if (MODE == 0 && dcm) dcm[e] = cm.scale * Em;
+  if (!scratch) return;   // no dX asked for: the coefficient gradients alone
 #pragma unroll
   for (int n = 0; n < 8; ++n)
 #pragma unroll

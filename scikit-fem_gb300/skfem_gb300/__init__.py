@@ -12,6 +12,7 @@ from .quadrature import get_quadrature  # noqa: F401
 from .dofs import Dofs  # noqa: F401
 from .basis import Basis, CellBasis, FacetBasis  # noqa: F401
 from .form import Form, BilinearForm, LinearForm, Functional, asm, ElementField  # noqa: F401
+from .coo import COOData  # noqa: F401
 from .field import DiscreteField  # noqa: F401
 from . import helpers, models  # noqa: F401
 

@@ -148,7 +148,11 @@ _SIGS = {
     "fem_enforce": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _P, ctypes.c_int64,
                                    ctypes.c_double, _P, _P, _P, _P]),
     "fem_set_tuning": (ctypes.c_int, [ctypes.c_int] * 5),
+    "fem_set_onepass": (ctypes.c_int, [ctypes.c_int] * 2),
     "fem_assemble_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
+    "fem_coo_pattern_build": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64,
+                                             ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p),
+                                             _P]),
 }
 
 

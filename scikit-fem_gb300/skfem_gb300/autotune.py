@@ -25,15 +25,20 @@ CANDIDATES = {
 # columns per lane of the fused sum: the scalar bases with 4, 6 or 10 local
 # functions also have the two-columns-per-lane kernel
 COLS = {"TetP1": (1, 2), "TriP2": (1, 2), "TetP2": (1, 2)}
+# the one-pass P1 sum's two forms (two lanes per row / a lane per upper entry)
+ONEPASS = {"TriP1": (0, 1), "TetP1": (0, 1)}
 
 
 def candidates(family, vector=False):
     """Every configuration the autotuner times for a basis of this family:
     the product of CANDIDATES, times the columns per lane of the fused sum
-    where the family has the two-columns kernel (scalar bases only)."""
+    where the family has the two-columns kernel, times the one-pass sum's
+    forms for the P1 simplex families (scalar bases only)."""
     cols = (1,) if vector else COLS.get(family, (1,))
-    return [{"local_block": lb, "persistent": pers, "sum_unroll": un, "sum_cols": nc}
-            for lb, pers, un, nc in itertools.product(*CANDIDATES.values(), cols)]
+    onep = (1,) if vector else ONEPASS.get(family, (1,))
+    return [{"local_block": lb, "persistent": pers, "sum_unroll": un, "sum_cols": nc,
+             "onepass": op}
+            for lb, pers, un, nc, op in itertools.product(*CANDIDATES.values(), cols, onep)]
 
 
 def _cache_path():
@@ -52,6 +57,7 @@ def _key(basis):
 def apply(family_code, cfg):
     N.check(N.lib().fem_set_tuning(family_code, cfg["local_block"], cfg["persistent"],
                                    cfg["sum_unroll"], cfg.get("sum_cols", 1)))
+    N.check(N.lib().fem_set_onepass(family_code, cfg.get("onepass", 1)))
 
 
 def tune(form, basis, coefs, reps=3, use_cache=True):

@@ -35,6 +35,33 @@ from .tracer import (FieldSpec, bilinear_channels, linear_channels, trace_biline
 __all__ = ["Form", "BilinearForm", "LinearForm", "Functional", "asm", "ElementField"]
 
 
+def _zeros_like(x):
+    """A zero argument of the same kind as a form argument x (the traced
+    stand-ins of the GPU path, or a DiscreteField), for Form.block: the
+    reference passes ``arg.zeros()``."""
+    from .tracer import Sym, SymField, TapeNode
+    if isinstance(x, DiscreteField):
+        return x.zeros()
+    if isinstance(x, SymField):
+        z = SymField(np.vectorize(lambda c: _zeros_like(c), otypes=[object])(np.asarray(x)))
+        if getattr(x, "grad", None) is not None:
+            z.grad = np.vectorize(lambda c: _zeros_like(c), otypes=[object])(x.grad)
+        return z
+    if isinstance(x, Sym):
+        z = Sym()
+        if getattr(x, "grad", None) is not None:
+            z.grad = np.array([Sym() for _ in x.grad], dtype=object)
+        return z
+    if isinstance(x, TapeNode):
+        z = x.tape.const(0.0)
+        if getattr(x, "grad", None) is not None:
+            z.grad = np.array([x.tape.const(0.0) for _ in x.grad], dtype=object)
+        return z
+    if isinstance(x, np.ndarray):
+        return np.zeros_like(x)
+    return 0.0 * x
+
+
 class ElementField:
     """An explicit per-element coefficient (one value per cell), accepted
     wherever the reference takes a (nelems, nqp) array that is constant in
@@ -239,6 +266,30 @@ class Form:
     @property
     def __name__(self):
         return getattr(self.form, "__name__", "form")
+
+    def block(self, *args):
+        """form.py:53-60: the block of a form written on product spaces --
+        block(i, j) of form(u0, u1, ..., v0, v1, ..., w) is the form of
+        (u, v, w) that passes u as u_i, v as v_j and zero fields in the
+        other slots."""
+        import inspect
+        orig = self.form
+        nargs = len(inspect.signature(orig).parameters)
+
+        def blk(*arg):
+            per = (nargs - 1) // (len(arg) - 1)
+            return orig(*[arg[k] if args[k] == j else _zeros_like(arg[k])
+                          for k in range(len(arg) - 1) for j in range(per)], arg[-1])
+        blk.__name__ = getattr(orig, "__name__", "form")
+        return type(self)(form=blk, dtype=self.dtype, nthreads=self.nthreads, **self.params)
+
+    def elemental(self, *args, **kwargs):
+        """form.py:82-85: the unassembled element values as a COOData."""
+        return self._coo(*args, **kwargs)
+
+    def coo_data(self, *args, **kwargs):
+        """form.py:87-89 (the older name of elemental)."""
+        return self._coo(*args, **kwargs)
 
     # tracing is cached per (element kind, field names, numbers)
     def _key(self, basis, coeffs, kind):
@@ -783,6 +834,44 @@ class BilinearForm(Form):
         return torch.sparse_csr_tensor(entry.indptr, entry.indices, vals,
                                        size=(ubasis.N, ubasis.N))
 
+    def _coo(self, ubasis, vbasis=None, idx=None, **kwargs):
+        """bilinear_form.py:58-128's COO triplet: data[j, i, e] (trial j,
+        test i, cell e) flattened in C order, rows = the test basis's DOFs,
+        cols = the trial basis's, from the device local matrices."""
+        from .coo import COOData
+        if idx is not None:
+            kwargs["idx"] = idx
+        if vbasis is None or vbasis is ubasis:
+            vbasis = ubasis
+            local = self.elemental_torch(ubasis, **kwargs)               # (ne, Nv, Nu)
+        else:
+            local = self._mixed_local(ubasis, vbasis, kwargs)
+        dev = local.device
+        ne, nv, nu = local.shape
+        data = local.permute(2, 1, 0).reshape(-1)
+        edv = torch.as_tensor(np.ascontiguousarray(vbasis.element_dofs), device=dev)
+        edu = torch.as_tensor(np.ascontiguousarray(ubasis.element_dofs), device=dev)
+        rows = edv[None, :, :].expand(nu, nv, ne).reshape(-1)
+        cols = edu[:, None, :].expand(nu, nv, ne).reshape(-1)
+        return COOData(np.stack([rows.cpu().numpy(), cols.cpu().numpy()]).astype(np.int32),
+                       data.cpu().numpy(), (vbasis.N, ubasis.N), (vbasis.Nbfun, ubasis.Nbfun))
+
+    def _mixed_local(self, ubasis, vbasis, kwargs):
+        """Local matrices (ne, Nv, Nu) of a trial / test basis pair (generic
+        kernels, as _mixed_assemble computes them)."""
+        self._check_pair(ubasis, vbasis)
+        coeffs = _Coefficients(ubasis, kwargs)
+        g, _ = self._generic(vbasis, coeffs, "bilinear", ubasis)
+        prog = g.struct(vbasis, coeffs, "bilinear", ubasis)
+        nl = vbasis.nelems * vbasis.Nbfun * ubasis.Nbfun
+        local = torch.empty(max(1, nl), dtype=torch.float64, device=vbasis.device)
+        status = torch.zeros(1, dtype=torch.int32, device=vbasis.device)
+        N.check(N.lib().fem_program_local_matrices_mixed(
+            N.byref(vbasis.c_mesh), N.byref(vbasis.c_basis), N.byref(ubasis.c_basis),
+            N.byref(prog), N.ptr(local), N.ptr(status), N.stream_ptr()))
+        _raise_status(int(status.item()))
+        return local[:nl].view(vbasis.nelems, vbasis.Nbfun, ubasis.Nbfun)
+
     def elemental_torch(self, ubasis, **kwargs):
         """Local matrices (nelems, Nbfun, Nbfun), row = test function."""
         coeffs = _Coefficients(ubasis, kwargs)
@@ -880,6 +969,34 @@ class LinearForm(Form):
         b, _ = self._device_assemble(basis, vbasis, **kwargs)
         return b
 
+    def elemental_torch(self, basis, **kwargs):
+        """Local load vectors (nelems, Nbfun) on the device."""
+        coeffs = _Coefficients(basis, kwargs)
+        ch = self._trace(basis, coeffs, "linear")
+        nb = basis.Nbfun
+        if ch is None:
+            local, status = self._local_generic(basis, coeffs)
+            _raise_status(int(status.item()))
+            return local[:basis.nelems * nb].view(basis.nelems, nb)
+        c_form = N.FemLinear(coeffs.coef(ch["load"], basis.nelems, basis.device))
+        out = torch.empty((basis.nelems, nb), dtype=torch.float64, device=basis.device)
+        N.check(N.lib().fem_local_vectors(N.byref(basis.c_mesh), N.byref(basis.c_basis),
+                                          N.byref(c_form), N.ptr(out), N.stream_ptr()))
+        return out
+
+    def _coo(self, basis, vbasis=None, idx=None, **kwargs):
+        """linear_form.py:18-46's COO pair: data[i, e] flattened, rows =
+        the basis's DOFs."""
+        from .coo import COOData
+        if vbasis is not None:
+            raise ValueError("LinearForm takes one basis")
+        if idx is not None:
+            kwargs["idx"] = idx
+        local = self.elemental_torch(basis, **kwargs)                   # (ne, Nb)
+        data = local.t().reshape(-1)
+        rows = np.ascontiguousarray(basis.element_dofs, dtype=np.int32).reshape(-1)
+        return COOData(rows[None, :], data.cpu().numpy(), (basis.N,), (basis.Nbfun,))
+
 
 class Functional(Form):
     """functional.py:10-61: a form of ``w`` alone, integrated per cell
@@ -916,29 +1033,36 @@ class Functional(Form):
         """The functional's value (functional.py:36-61) as a numpy float64."""
         return np.float64(self.assemble_torch(ubasis, vbasis, **kwargs).item())
 
+    def _coo(self, ubasis, vbasis=None, idx=None, **kwargs):
+        """functional.py:36-61's COO form: no indices, one datum (the
+        functional's value), a 0-tensor."""
+        from .coo import COOData
+        if idx is not None:
+            kwargs["idx"] = idx
+        return COOData(np.array([]), np.array([self.assemble(ubasis, vbasis, **kwargs)]), (), ())
 
-def asm(form, *args, to=None, **kwargs):
+
+def _sum_blocks(blocks):
+    out = sum(blocks)
+    assert not isinstance(out, int)
+    return out.todefault()
+
+
+def asm(form, *args, to=_sum_blocks, **kwargs):
     """skfem/assembly/__init__.py:69-97: assemble ``form`` on its bases; an
     argument that is a list of bases assembles every combination (the
-    product over the lists) and sums the results -- e.g. one form over
-    several element subsets or facet sets."""
+    product over the lists), each block told its position as ``w.idx``,
+    and ``to`` reduces the blocks' COOData (default: their sum, as
+    COOData.__add__ concatenates them, assembled on the GPU).  A single
+    combination with the default reducer goes straight to ``assemble``."""
+    from itertools import product
     if not isinstance(form, Form):
         import inspect
         nargs = len(inspect.signature(form).parameters)
         form = {3: BilinearForm, 2: LinearForm, 1: Functional}[nargs](form)
-    if to is not None:
-        raise NotImplementedError("asm(to=...) is not supported; the results are summed")
     lists = [a if isinstance(a, list) else [a] for a in args]
-    if all(len(a) == 1 for a in lists):
+    if to is _sum_blocks and all(len(a) == 1 for a in lists) and not any(
+            isinstance(a, list) for a in args):
         return form.assemble(*[a[0] for a in lists], **kwargs)
-    from itertools import product
-    parts = [form.assemble(*combo, **kwargs) for combo in product(*lists)]
-    if sp.issparse(parts[0]):
-        # concatenated COO then CSR, as COOData.__add__ + todefault: an entry
-        # is kept when any part has it, even if the sum cancels to zero
-        coo = [P.tocoo() for P in parts]
-        K = sp.coo_matrix((np.concatenate([P.data for P in coo]),
-                           (np.concatenate([P.row for P in coo]),
-                            np.concatenate([P.col for P in coo]))), shape=parts[0].shape)
-        return K.tocsr()
-    return sum(parts[1:], parts[0])
+    return to(map(lambda a: form.coo_data(*a[1], idx=a[0], **kwargs),
+                  zip(product(*(range(len(x)) for x in lists)), product(*lists))))

@@ -689,8 +689,67 @@ def config_cases():
     np.savez_compressed(os.path.join(OUT, "config_patterns.npz"), **out)
 
 
+def coo_cases():
+    """COOData / Form.elemental / Form.block / asm(to=...) results of
+    scikit-fem (coo_data.py, form.py:53-89, assembly/__init__.py:69-97)."""
+    from skfem import FacetBasis, asm
+    from skfem.helpers import dot as hdot
+    out = {}
+    m = MeshTri.init_tensor(np.linspace(0, 1, 5), np.linspace(0, 1, 4))
+    ib = Basis(m, ElementTriP1())
+    A = laplace.elemental(ib)
+    out["lap_indices"], out["lap_data"] = A.indices, A.data
+    out["lap_shape"], out["lap_local_shape"] = np.array(A.shape), np.array(A.local_shape)
+    out["lap_tolocal"] = A.tolocal()
+    K = A.tocsr()
+    out["lap_indptr"], out["lap_csr_indices"], out["lap_csr_data"] = K.indptr, K.indices, K.data
+    b = unit_load.elemental(ib)
+    out["load_indices"], out["load_data"], out["load_array"] = b.indices, b.data, b.toarray()
+    # mass matrices inverted cell by cell, then assembled
+    out["mass_inverse"] = mass.coo_data(ib).inverse().tocsr().toarray()
+    # trial P2 / test P1 pair
+    pb = Basis(m, ElementTriP2())
+    ib2 = Basis(m, ElementTriP1(), intorder=4)     # the trial basis's quadrature
+
+    @BilinearForm
+    def mixed(u, v, w):
+        return u.grad[0] * v + 0.5 * u * v.grad[1]
+    C = mixed.elemental(pb, ib2)
+    out["mixed_indices"], out["mixed_data"] = C.indices, C.data
+    out["mixed_shape"], out["mixed_local_shape"] = np.array(C.shape), np.array(C.local_shape)
+    # asm over lists of bases (element subsets), summed; and a custom reducer
+    b1 = Basis(m, ElementTriP1(), elements=lambda x: x[0] < 0.5)
+    b2 = Basis(m, ElementTriP1(), elements=lambda x: x[0] >= 0.5)
+    S = asm(laplace, [b1, b2])
+    out["asm_sum_indptr"], out["asm_sum_indices"], out["asm_sum_data"] = S.indptr, S.indices, S.data
+    parts = asm(laplace, [b1, b2], to=list)
+    out["asm_to_list_0"] = parts[0].todefault().toarray()
+    out["asm_to_list_1"] = parts[1].todefault().toarray()
+    out["asm_load_sum"] = asm(unit_load, [b1, b2])
+
+    @BilinearForm
+    def with_idx(u, v, w):
+        return (1.0 + w.idx[0]) * u * v
+    out["asm_idx"] = asm(with_idx, [b1, b2]).toarray()
+    # blocks of a form written on a product space
+    @BilinearForm
+    def prod(u1, u2, v1, v2, w):
+        return hdot(grad(u1), grad(v1)) + 2.0 * u2 * v2 + u1 * v2
+    for i in (0, 1):
+        for j in (0, 1):
+            out["block_%d%d" % (i, j)] = asm(prod.block(i, j), ib).toarray()
+    # facet matrices summed per cell
+    fb = FacetBasis(m, ElementTriP1())
+    F_ = mass.elemental(fb)
+    out["facet_tolocal"] = F_.tolocal(fb)
+    np.savez_compressed(os.path.join(OUT, "coo_api.npz"), **out)
+    print("coo_api", {k: v.shape for k, v in out.items()})
+
+
 if __name__ == "__main__":
-    if sys.argv[1:] == ["--configs"]:
+    if sys.argv[1:] == ["--coo"]:
+        coo_cases()
+    elif sys.argv[1:] == ["--configs"]:
         config_cases()
     elif sys.argv[1:] == ["--quadrature"]:
         quadrature_rules()

@@ -236,3 +236,62 @@ def test_fused_sum_columns_per_lane_are_bitwise_equal(fam, cls, dim, n, elem, fo
         np.testing.assert_array_equal(ref_host.data, ref.cpu().numpy())
     finally:
         autotune.apply(code, base)
+
+
+P1 = [("TriP1", F.MeshTri, 2, 41, F.ElementTriP1), ("TetP1", F.MeshTet, 3, 13, F.ElementTetP1)]
+
+
+@pytest.mark.parametrize("form", ["k_lap_mass", "lap_mass_const", "k_lap_cmass"])
+@pytest.mark.parametrize("fam,cls,dim,n,elem", P1, ids=[c[0] for c in P1])
+def test_one_pass_forms_agree(fam, cls, dim, n, elem, form):
+    """The one-pass P1 sum's two forms -- two lanes per row adding into
+    shared-memory slots, and a lane per upper entry walking its list in
+    registers and writing the entry and its transpose -- add every entry's
+    contributions in the same order: on a jittered mesh (cells around a
+    vertex within a factor 8 in |det|, so the fixed-point mass sums are
+    exact in both) they agree bit for bit, on the device path and through
+    the pipelined host path, for every unroll; on a strongly graded mesh
+    within 1e-15 of max|K|."""
+    from skfem_gb300 import autotune
+    code = N.FAMILY[fam]
+    f = {"k_lap_mass": k_lap_mass, "lap_mass_const": lap_mass_const,
+         "k_lap_cmass": k_lap_cmass}[form]
+    base = {"local_block": 128, "persistent": 0, "sum_unroll": 8, "sum_cols": 1, "onepass": 0}
+    for graded in (False, True):
+        m = cls.init_tensor(*(np.linspace(0, 1, n),) * dim)
+        p = m.p.copy()
+        if graded:
+            p = p ** 4                     # cell sizes over four orders of magnitude
+        else:
+            inner = np.all((p > 1e-12) & (p < 1 - 1e-12), axis=0)
+            p[:, inner] += np.random.default_rng(3).uniform(-0.2 / n, 0.2 / n,
+                                                            (dim, int(inner.sum())))
+        perm = np.random.default_rng(8).permutation(m.t.shape[1])
+        b = F.Basis(cls(p, np.ascontiguousarray(m.t[:, perm])), elem())
+        rng = np.random.default_rng(10)
+        k = rng.lognormal(0, 1, b.nelems)
+        c = rng.uniform(0.5, 2.0, b.nelems)
+        kw, kh = {}, {}
+        if form != "lap_mass_const":
+            kw["k"] = torch.from_numpy(k).cuda()
+            kh["k"] = b.zero_w() + k[:, None]
+        if form == "k_lap_cmass":
+            kw["c"] = torch.from_numpy(c).cuda()
+            kh["c"] = b.zero_w() + c[:, None]
+        try:
+            autotune.apply(code, base)
+            ref = f.assemble_torch(b, **kw).values().clone()
+            ref_host = f.assemble(b, **kh).data
+            for unroll in (4, 8):
+                autotune.apply(code, dict(base, sum_unroll=unroll, onepass=1))
+                got = f.assemble_torch(b, **kw).values()
+                got_host = f.assemble(b, **kh).data
+                if graded:
+                    scale = ref.abs().max().item()
+                    assert (got - ref).abs().max().item() <= 1e-15 * scale
+                    assert np.abs(got_host - ref_host).max() <= 1e-15 * scale
+                else:
+                    assert torch.equal(got, ref)
+                    np.testing.assert_array_equal(got_host, ref_host)
+        finally:
+            autotune.apply(code, dict(base, onepass=1))

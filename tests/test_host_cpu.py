@@ -152,16 +152,41 @@ def test_complement_dofs():
 def test_autotune_candidates_per_family():
     """The autotuner times every block size, grid and unroll; the scalar
     bases with an even number of local functions (TetP1, TriP2, TetP2) also
-    try two columns per lane in the fused sum, the others and every vector
-    basis only one."""
+    try two columns per lane in the fused sum, the P1 simplex families both
+    forms of the one-pass sum, the others and every vector basis one of
+    each."""
     from skfem_gb300 import autotune
     base = 3 * 2 * 3
-    for fam in ("TetP1", "TriP2", "TetP2"):
+    for fam in ("TriP2", "TetP2"):
         c = autotune.candidates(fam)
         assert len(c) == 2 * base and {x["sum_cols"] for x in c} == {1, 2}
+        assert {x["onepass"] for x in c} == {1}
         assert len(autotune.candidates(fam, vector=True)) == base
-    for fam in ("TriP1", "Hex1"):
-        c = autotune.candidates(fam)
-        assert len(c) == base and {x["sum_cols"] for x in c} == {1}
+    c = autotune.candidates("TetP1")
+    assert len(c) == 4 * base and {x["sum_cols"] for x in c} == {1, 2}
+    assert {x["onepass"] for x in c} == {0, 1}
+    assert len(autotune.candidates("TetP1", vector=True)) == base
+    c = autotune.candidates("TriP1")
+    assert len(c) == 2 * base and {x["onepass"] for x in c} == {0, 1}
+    c = autotune.candidates("Hex1")
+    assert len(c) == base and {x["sum_cols"] for x in c} == {1}
     c = autotune.candidates("TetP1")
     assert len({tuple(sorted(x.items())) for x in c}) == len(c)
+
+
+def test_coodata_host_side_matches_reference_layout():
+    """COOData's host-side operations on the reference's own arrays
+    (coo_api.npz): tolocal / fromlocal reshape exactly as coo_data.py does,
+    __add__ concatenates and widens the shape, sum() starts from 0."""
+    from skfem_gb300.coo import COOData
+    from _util import golden
+    g = golden("coo_api")
+    A = COOData(g["lap_indices"], g["lap_data"], tuple(g["lap_shape"]),
+                tuple(g["lap_local_shape"]))
+    np.testing.assert_array_equal(A.tolocal(), g["lap_tolocal"])
+    np.testing.assert_array_equal(A.fromlocal(A.tolocal()).data, A.data)
+    B = sum([A, A])
+    assert B.indices.shape == (2, 2 * A.indices.shape[1]) and B.local_shape is None
+    assert B.shape == A.shape
+    idx, data, shape = A.astuple()
+    assert idx is A.indices and data is A.data and shape == A.shape
