@@ -1558,9 +1558,11 @@ int csr_sum_upper_p1(const Pattern& P, const UpperLists& U, int dim, const doubl
   const double* mf = mass.field;
   const int64_t ms = mass.stride > 1 ? mass.stride : 1;
   const int Un = P.sum_unroll >= 8 ? 8 : 4;
-  // upper entries of rows [row0, row1): a diagonal range and an off-diagonal one
-  const int64_t ranges[2][2] = {{U.dpos_h[row0], U.dpos_h[row1]},
-                                {U.nd + U.opos_h[row0], U.nd + U.opos_h[row1]}};
+  // upper entries of rows [row0, row1): a diagonal range and an off-diagonal
+  // one (all rows: the two are adjacent, one launch)
+  const bool all = row0 == 0 && row1 == P.nrows;
+  const int64_t ranges[2][2] = {{all ? 0 : U.dpos_h[row0], all ? U.nupper : U.dpos_h[row1]},
+                                {all ? 0 : U.nd + U.opos_h[row0], all ? 0 : U.nd + U.opos_h[row1]}};
   const int threads = 128;
   for (int k = 0; k < 2; ++k) {
     const int64_t ua = ranges[k][0], ub = ranges[k][1];

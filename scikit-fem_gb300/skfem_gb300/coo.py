@@ -97,8 +97,8 @@ class COOData:
         local = np.moveaxis(self.data.reshape(tuple(self.local_shape) + (-1,), order="C"), -1, 0)
         if basis is not None:
             dev = _device()
-            out = torch.zeros((basis.mesh.nfacets,) + local.shape[1:], dtype=torch.float64,
-                              device=dev)
+            nfacets = int(np.asarray(basis.mesh.facets).shape[1])
+            out = torch.zeros((nfacets,) + local.shape[1:], dtype=torch.float64, device=dev)
             out[torch.as_tensor(np.asarray(basis.find), device=dev).long()] = \
                 torch.as_tensor(np.ascontiguousarray(local), device=dev)
             t2f = torch.as_tensor(np.asarray(basis.mesh.t2f), device=dev).long()
