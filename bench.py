@@ -587,21 +587,42 @@ def secondary_workloads(args, only=None):
         ub = torch.tensor(brng.standard_normal(bb.N), device="cuda")
         from skfem_gb300 import autotune
         best, _ = autotune.tune(k_laplace, bb, {"k": kk}, reps=2, use_cache=False)
+        # one persistent work-queue launch per step (forward + coefficient adjoint)
         ga = GraphedAssembly(k_laplace, bb, {"k": kk}, w=wb, u=ub).capture()
         torch.cuda.synchronize()
         setup_s = time.perf_counter() - t0
         ms_graph = _time(ga.replay, 5)
         ga.check()
-        # per-mesh plain launches of the same kernels (patterns prebuilt, eager)
+        # the same union with the separate kernels (local, staging sum, adjoint)
+        gs = GraphedAssembly(k_laplace, bb, {"k": kk}, w=wb, u=ub, persistent=False).capture()
+        ms_union = _time(gs.replay, 5)
+        gs.check()
+        # per-mesh plain launches of the same work (fem_assemble + the adjoint
+        # kernel per mesh, patterns and geometry prebuilt): eager, and all of
+        # them captured into one CUDA graph (no host launch cost, only the
+        # kernels and the gaps between them)
         per = []
         for mm, kv in zip(meshes, ks):
             bm = F.Basis(mm, F.ElementTriP2())
             kt = torch.tensor(kv, device="cuda")
             g1 = GraphedAssembly(k_laplace, bm, {"k": kt},
                                  w=torch.zeros(bm.N, dtype=torch.float64, device="cuda"),
-                                 u=torch.zeros(bm.N, dtype=torch.float64, device="cuda"))
+                                 u=torch.zeros(bm.N, dtype=torch.float64, device="cuda"),
+                                 persistent=False)
             per.append(g1)
         ms_loop = _time(lambda: [g.run_eager() for g in per], 3, warm=1)
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for g in per:
+                g.run_eager()
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        loop_graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(loop_graph):
+            for g in per:
+                g.run_eager()
+        ms_loop_graph = _time(loop_graph.replay, 3, warm=1)
         # per-mesh calls through the public API (assemble + autograd adjoint), as a
         # user without the batched path would write them
         from skfem_gb300.autodiff import assemble_vjp
@@ -614,8 +635,7 @@ def secondary_workloads(args, only=None):
         def api_loop():
             for bm, kt, wv, uv in api:
                 kr = kt.clone().requires_grad_(True)
-                X = bm.p_dev.clone().requires_grad_(True)
-                J = assemble_vjp(k_laplace, bm, wv, uv, X=X, k=kr)
+                J = assemble_vjp(k_laplace, bm, wv, uv, k=kr)
                 J.backward()
         api_loop()
         torch.cuda.synchronize()
@@ -626,12 +646,17 @@ def secondary_workloads(args, only=None):
         ncell = int(bb.nelems)
         out["batched_512_trip2_forward_vjp"] = {
             "meshes": len(meshes), "nelems": ncell, "nnz": int(ga.entry.nnz), "setup_s": setup_s,
-            "autotuned": best, "ms_graph_replay": ms_graph, "ms_per_mesh_launches": ms_loop,
+            "step": "CSR values + d(w^T K u)/dk per cell (the coefficient adjoint)",
+            "autotuned": best, "ms_graph_replay": ms_graph, "work_units": ga.nunits,
+            "ms_union_separate_kernels": ms_union,
+            "ms_per_mesh_launches": ms_loop, "ms_per_mesh_launches_one_graph": ms_loop_graph,
             "elements_per_s_batched": ncell / (ms_graph * 1e-3),
             "elements_per_s_per_mesh": ncell / (ms_loop * 1e-3),
             "speedup_vs_per_mesh_launches": ms_loop / ms_graph,
+            "speedup_vs_per_mesh_launches_one_graph": ms_loop_graph / ms_graph,
             "ms_per_mesh_api_calls": ms_api, "speedup_vs_per_mesh_api": ms_api / ms_graph,
-            "launches_per_step": ga.launches_per_step()}
+            "launches_per_step": ga.launches_per_step(),
+            "launches_per_step_per_mesh": sum(g.launches_per_step() for g in per)}
 
     if want("generic"):
         # generic per-point kernels: a Newton-step matrix with an

@@ -60,8 +60,10 @@ enum FemStatus {
   FEM_ERR_CAPACITY = 6,      /* a CSR row exceeds the per-row working-set limit */
   FEM_ERR_VARYING = 7,       /* a strided coefficient is not constant over a cell's
                                 points (status word only): use the generic kernels */
-  FEM_ERR_NEWTON = 8         /* the inverse isoparametric map did not converge
+  FEM_ERR_NEWTON = 8,        /* the inverse isoparametric map did not converge
                                 (status word only, fem_facet_geometry) */
+  FEM_ERR_TIMEOUT = 9        /* a bounded wait inside a persistent kernel ran out; that
+                                launch's results are not valid (status word only) */
 };
 
 /* Element families (the reference classes they stand for). */
@@ -186,6 +188,7 @@ int fem_program_source(const FemInstr* ins, int32_t ninstr, int32_t out, int32_t
 
 /* Opaque one-time structure: row incidence, CSR pattern, local-to-slot map. */
 typedef struct FemPattern FemPattern;
+typedef struct FemBatchPlan FemBatchPlan;
 
 /* Last error message of the calling thread ("" if none). */
 const char* fem_last_error(void);
@@ -609,6 +612,44 @@ int fem_facet_interpolate(const FemMesh* mesh, const FemBasis* basis, const FemF
 /* Vertex incidence of the mesh (rows = vertices), used by the adjoint's
  * fixed-order gather of per-element coordinate gradients. */
 int fem_vertex_incidence_build(const FemMesh* mesh, FemPattern** out, fem_stream_t stream);
+
+/*
+ * Batched assembly in one persistent launch -- no counterpart in the
+ * reference, which assembles one mesh per BilinearForm.assemble call
+ * (bilinear_form.py:130-148).  The meshes form one block-diagonal union
+ * (FemMesh / FemBasis of the union, each mesh's cells, vertices and DOFs
+ * offset, its own numbering kept inside its block).
+ *
+ * fem_batch_plan_build: the device work queue of the union, from the
+ * meshes' cell offsets and row (DOF) offsets (nmeshes + 1 each, host
+ * arrays): per mesh, units of 128 cells and units of rows_per_unit rows,
+ * every mesh's cell units queued before its row units.  Released with
+ * fem_batch_plan_destroy; fem_batch_plan_info gives the number of units
+ * and of int32 counters a launch needs.
+ *
+ * fem_batched_assemble_vjp: one launch (after a memset of `counters`,
+ * 1 + nmeshes int32) whose blocks take units in queue order from an atomic
+ * ticket: a cell unit writes its cells' local matrices (k_e S_e + m_e M_e
+ * from the pattern's geometry cache, required) into the staging and, when
+ * w and u are given, dJ/dk_e = w_e^T S_e u_e and dJ/dm_e = w_e^T M_e u_e of
+ * J = w^T K u (the scales of the form's channels applied) into
+ * dcoef_diff / dcoef_mass (either may be NULL); a row unit waits (bounded)
+ * until its mesh's cell units are done, then sums its rows in the fixed
+ * order of fem_assemble's staging sum -- the CSR values equal fem_assemble's
+ * two-pass values bit for bit.  Scalar simplex bases (TriP1/P2, TetP1/P2)
+ * and forms k dot(grad u, grad v) + m u v.  status (device int32)
+ * receives the coefficient checks' bits and FEM_ERR_TIMEOUT if a wait ran
+ * out.  Capturable in a CUDA graph (memset + kernel).
+ */
+int fem_batch_plan_build(const int64_t* cell_offsets, const int64_t* row_offsets,
+                         int32_t nmeshes, int32_t rows_per_unit, FemBatchPlan** out);
+void fem_batch_plan_destroy(FemBatchPlan* plan);
+int fem_batch_plan_info(const FemBatchPlan* plan, int64_t* nunits, int64_t* ncounters);
+int fem_batched_assemble_vjp(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* form,
+                             const FemPattern* pat, const FemBatchPlan* plan, double* staging,
+                             double* csr_values, const double* w, const double* u,
+                             double* dcoef_diff, double* dcoef_mass, int32_t* counters,
+                             int32_t* status, fem_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -27,6 +27,7 @@ UNITS = [
     ("fem_local.cu", "fem_local_exact.o", ["-DFEM_EXACT", "-fmad=false"]),
     ("fem_pattern.cu", "fem_pattern.o", []),
     ("fem_vjp.cu", "fem_vjp.o", []),
+    ("fem_batched.cu", "fem_batched.o", []),
     ("fem_abi.cu", "fem_abi.o", []),
     ("fem_noalloc.cu", "fem_noalloc.o", []),
     ("fem_faithful.cu", "fem_faithful.o", ["-fmad=false"]),

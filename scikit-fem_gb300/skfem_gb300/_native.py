@@ -21,6 +21,7 @@ FEM_ERR_STALE_PATTERN = 5
 FEM_ERR_CAPACITY = 6
 FEM_ERR_VARYING = 7
 FEM_ERR_NEWTON = 8
+FEM_ERR_TIMEOUT = 9
 
 FAMILY = {"TriP1": 1, "TriP2": 2, "TetP1": 3, "TetP2": 4, "Hex1": 5}
 
@@ -150,6 +151,11 @@ _SIGS = {
     "fem_set_tuning": (ctypes.c_int, [ctypes.c_int] * 5),
     "fem_set_onepass": (ctypes.c_int, [ctypes.c_int] * 2),
     "fem_assemble_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
+    "fem_batch_plan_build": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_int32,
+                                            ctypes.POINTER(ctypes.c_void_p)]),
+    "fem_batch_plan_destroy": (None, [_P]),
+    "fem_batch_plan_info": (ctypes.c_int, [_P, _I64P, _I64P]),
+    "fem_batched_assemble_vjp": (ctypes.c_int, [_P] * 14),
     "fem_coo_pattern_build": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64,
                                              ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p),
                                              _P]),

@@ -4,10 +4,17 @@ The reference assembles one mesh per call (a Python loop over meshes is the
 batched baseline).  Here meshes of one element family become a single
 block-diagonal system: vertices, cells and DOFs are offset per mesh while
 each mesh keeps the reference's own numbering (so block m of the result is,
-bit for bit, mesh m's scipy CSR).  One pattern build covers all meshes; every
-later step is one local-matrix launch and one segmented-sum launch over all
-cells (grid-stride, sized by the autotuner), optionally followed by the
-adjoint, captured once in a CUDA graph and replayed.
+bit for bit, mesh m's scipy CSR).  One pattern build covers all meshes.
+
+Every later step of a scalar simplex basis (TriP1/P2, TetP1/P2) is ONE
+persistent launch (fem_batched_assemble_vjp) whose blocks take work units
+from a device queue -- per mesh, units of 128 cells (local matrices from the
+geometry cache and, with the adjoint, the cells' coefficient gradients from
+the same matrices) queued before units of rows (the fixed-order segmented
+sum, waiting on the mesh's cell units) -- captured once in a CUDA graph
+(a counter reset and the kernel) and replayed.  Other bases, and the
+coordinate gradient (with_dX), run the separate local / sum / adjoint
+kernels over the union.
 """
 
 import ctypes
@@ -23,6 +30,22 @@ from .form import _Coefficients
 from .mesh import as_mesh
 
 __all__ = ["BatchedBasis", "GraphedAssembly"]
+
+
+class _Plan:
+    """Owns a FemBatchPlan handle."""
+
+    def __init__(self, handle):
+        self.handle = handle
+
+    def __del__(self):
+        h, self.handle = getattr(self, "handle", None), None
+        if h and N._lib is not None:
+            try:
+                torch.cuda.synchronize()
+            except Exception:
+                pass
+            N._lib.fem_batch_plan_destroy(h)
 
 
 class _UnionDofs:
@@ -80,13 +103,21 @@ class BatchedBasis(CellBasis):
         return [x[self.elem_offsets[k]:self.elem_offsets[k + 1]] for k in range(self.nmeshes)]
 
 
+ROWS_PER_UNIT = 256
+
+
 class GraphedAssembly:
     """Forward assembly (+ optional adjoint) of one form over a basis,
     captured in a CUDA graph.  Static device buffers: ``coef[name]``
     (per-element fields), ``w``, ``u`` (adjoint vectors); outputs ``values``
-    (CSR values in the cached pattern), ``dcoef[name]`` and ``dX``."""
+    (CSR values in the cached pattern), ``dcoef[name]`` (d(w^T K u) / d
+    coefficient field) and, with ``with_dX``, ``dX`` (/ d node coordinates).
+    ``persistent`` (default: wherever supported) runs forward + coefficient
+    adjoint as one persistent work-queue launch; False runs the separate
+    kernels."""
 
-    def __init__(self, form, basis, coefs, w=None, u=None, adjoint=True):
+    def __init__(self, form, basis, coefs, w=None, u=None, adjoint=True, with_dX=False,
+                 persistent=None):
         self.form, self.basis = form, basis
         dev = basis.device
         self.coef = {k: torch.as_tensor(v, dtype=torch.float64, device=dev).clone()
@@ -114,28 +145,77 @@ class GraphedAssembly:
                 self.dcoef[chf["diff"]] = self.dcd
             if "mass" in chf:
                 self.dcoef.setdefault(chf["mass"], self.dcm)
-            self.dX = torch.empty_like(basis.p_dev)
-            self.scratch = torch.empty(ne * basis.mesh.t.shape[0] * basis.mesh.p.shape[0],
-                                       dtype=torch.float64, device=dev)
-            self.vinc = _vertex_incidence(basis)
+            self.with_dX = with_dX
+            if with_dX:
+                self.dX = torch.empty_like(basis.p_dev)
+                self.scratch = torch.empty(ne * basis.mesh.t.shape[0] * basis.mesh.p.shape[0],
+                                           dtype=torch.float64, device=dev)
+                self.vinc = _vertex_incidence(basis)
+            else:
+                self.dX = self.scratch = self.vinc = None
+        else:
+            self.with_dX = False
+        supported = (not basis.elem.vector and basis.elem.family in
+                     ("TriP1", "TriP2", "TetP1", "TetP2"))
+        if persistent is None:
+            persistent = supported and not self.with_dX
+        if persistent and (not supported or self.with_dX):
+            raise NotImplementedError("the persistent batched launch takes scalar simplex "
+                                      "bases and the coefficient adjoint only")
+        self.plan = None
+        if persistent:
+            self._build_plan()
         self.graph = None
+
+    def _build_plan(self):
+        b = self.basis
+        if isinstance(b, BatchedBasis):
+            cells = np.ascontiguousarray(b.elem_offsets, dtype=np.int64)
+            rows = np.ascontiguousarray(b.dof_offsets, dtype=np.int64)
+        else:
+            cells = np.array([0, b.nelems], dtype=np.int64)
+            rows = np.array([0, b.N], dtype=np.int64)
+        h = ctypes.c_void_p()
+        N.check(N.lib().fem_batch_plan_build(cells.ctypes.data, rows.ctypes.data, len(cells) - 1,
+                                             ROWS_PER_UNIT, ctypes.byref(h)))
+        self.plan = _Plan(h.value)
+        nu, nc = ctypes.c_int64(), ctypes.c_int64()
+        N.check(N.lib().fem_batch_plan_info(self.plan.handle, ctypes.byref(nu), ctypes.byref(nc)))
+        self.nunits = nu.value
+        self.counters = torch.zeros(nc.value, dtype=torch.int32, device=b.device)
 
     def _launch(self):
         lib = N.lib()
         b = self.basis
         s = N.stream_ptr()
         self.entry.ensure_caches(b, self.key, s)
+        if self.plan is not None:
+            adj = self.adjoint
+            N.check(lib.fem_batched_assemble_vjp(
+                N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(self.c_form),
+                self.entry.pat.handle, self.plan.handle, N.ptr(self.entry.staging),
+                N.ptr(self.values), N.ptr(self.w) if adj else None,
+                N.ptr(self.u) if adj else None, N.ptr(self.dcd) if adj else None,
+                N.ptr(self.dcm) if adj else None, N.ptr(self.counters), N.ptr(self.status), s))
+            return
         N.check(lib.fem_assemble(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(self.c_form),
                                  self.entry.pat.handle, N.ptr(self.entry.staging),
                                  N.ptr(self.values), N.ptr(self.status), s))
         if self.adjoint:
             N.check(lib.fem_bilinear_vjp(N.byref(b.c_mesh), N.byref(b.c_basis),
-                                         N.byref(self.c_form), self.vinc.handle, N.ptr(self.w),
+                                         N.byref(self.c_form),
+                                         self.vinc.handle if self.vinc else None, N.ptr(self.w),
                                          N.ptr(self.u), N.ptr(self.dcd), N.ptr(self.dcm),
                                          N.ptr(self.dX), N.ptr(self.scratch), s))
 
     def launches_per_step(self):
-        return 2 + (2 if self.adjoint else 0)
+        """Kernel launches one step issues (the persistent path: one kernel
+        after a counter reset)."""
+        if self.plan is not None:
+            return 1
+        fwd = 2
+        adj = (1 + (1 if self.with_dX else 0)) if self.adjoint else 0
+        return fwd + adj
 
     def run_eager(self):
         self._launch()
@@ -161,6 +241,9 @@ class GraphedAssembly:
 
     def check(self):
         st = int(self.status.item())
+        if st & (1 << N.FEM_ERR_TIMEOUT):
+            raise N.FemError("a wait of the persistent batched launch ran out: its results are "
+                             "not valid")
         if st:
             raise N.FemError("batched assembly status %d" % st)
 

@@ -837,13 +837,19 @@ class BilinearForm(Form):
     def _coo(self, ubasis, vbasis=None, idx=None, **kwargs):
         """bilinear_form.py:58-128's COO triplet: data[j, i, e] (trial j,
         test i, cell e) flattened in C order, rows = the test basis's DOFs,
-        cols = the trial basis's, from the device local matrices."""
+        cols = the trial basis's.  The local values come from the generic
+        kernels, which evaluate the form with the reference's own sequence
+        of operations: the data are the reference's bit for bit, so the
+        exact zeros that COOData.tocsr drops (eliminate_zeros) are its."""
         from .coo import COOData
         if idx is not None:
             kwargs["idx"] = idx
         if vbasis is None or vbasis is ubasis:
             vbasis = ubasis
-            local = self.elemental_torch(ubasis, **kwargs)               # (ne, Nv, Nu)
+            nb = ubasis.Nbfun
+            flat, status, _ = self._local_generic(ubasis, _Coefficients(ubasis, kwargs))
+            _raise_status(int(status.item()))
+            local = flat[:ubasis.nelems * nb * nb].view(ubasis.nelems, nb, nb)   # (ne, Nv, Nu)
         else:
             local = self._mixed_local(ubasis, vbasis, kwargs)
         dev = local.device
@@ -986,13 +992,17 @@ class LinearForm(Form):
 
     def _coo(self, basis, vbasis=None, idx=None, **kwargs):
         """linear_form.py:18-46's COO pair: data[i, e] flattened, rows =
-        the basis's DOFs."""
+        the basis's DOFs (local values from the generic kernels: the
+        reference's bit for bit)."""
         from .coo import COOData
         if vbasis is not None:
             raise ValueError("LinearForm takes one basis")
         if idx is not None:
             kwargs["idx"] = idx
-        local = self.elemental_torch(basis, **kwargs)                   # (ne, Nb)
+        nb = basis.Nbfun
+        flat, status = self._local_generic(basis, _Coefficients(basis, kwargs))
+        _raise_status(int(status.item()))
+        local = flat[:basis.nelems * nb].view(basis.nelems, nb)         # (ne, Nb)
         data = local.t().reshape(-1)
         rows = np.ascontiguousarray(basis.element_dofs, dtype=np.int32).reshape(-1)
         return COOData(rows[None, :], data.cpu().numpy(), (basis.N,), (basis.Nbfun,))
