@@ -635,8 +635,11 @@ int fem_vertex_incidence_build(const FemMesh* mesh, FemPattern** out, fem_stream
  * J = w^T K u (the scales of the form's channels applied) into
  * dcoef_diff / dcoef_mass (either may be NULL); a row unit waits (bounded)
  * until its mesh's cell units are done, then sums its rows in the fixed
- * order of fem_assemble's staging sum -- the CSR values equal fem_assemble's
- * two-pass values bit for bit.  Scalar simplex bases (TriP1/P2, TetP1/P2)
+ * order of fem_assemble's staging sum -- the CSR values equal the split
+ * entry points' (fem_assemble_local + fem_csr_sum_staged) bit for bit for
+ * TriP1, TriP2 and TetP1, within a few ulps for TetP2 (whose longer tensor
+ * sums the compiler may contract differently).  Scalar simplex bases
+ * (TriP1/P2, TetP1/P2)
  * and forms k dot(grad u, grad v) + m u v.  status (device int32)
  * receives the coefficient checks' bits and FEM_ERR_TIMEOUT if a wait ran
  * out.  Capturable in a CUDA graph (memset + kernel).

@@ -117,8 +117,11 @@ __global__ void __launch_bounds__(kBlock) batched_forward_vjp_kernel(
     const int64_t a = ubeg[k], z = uend[k];
     if ((km & 1) == 0) {
       // ---------------------------------------------------- cell unit
+      // each thread writes its cell's matrix straight into the staging (the
+      // rows of one cell contiguous; the L2 merges the lanes' partial
+      // sectors), so the block needs no shared memory for the cell units
       const int64_t e = a + threadIdx.x;
-      double* row = smem + threadIdx.x * (L + 1);
+      double* row = staging + e * L;
       if (e < z) {
         const int rb = ref_bits ? (int)__ldg(ref_bits + e) : -1;
         double gram[D + 1][D + 1];
@@ -167,14 +170,6 @@ __global__ void __launch_bounds__(kBlock) batched_forward_vjp_kernel(
           if (dcm) dcm[e] = f.mass.scale * adet * jm;
         }
         flags |= cell_status(f, e, rb);
-      }
-      __syncthreads();
-      // coalesced stores of the unit's rows, cell after cell
-      const int64_t n = (z - a) * L;
-      double* dst = staging + a * L;
-      for (int64_t g = threadIdx.x; g < n; g += blockDim.x) {
-        const int el = (int)(g / L);
-        dst[g] = smem[el * (L + 1) + (int)(g - (int64_t)el * L)];
       }
       __syncthreads();
       if (threadIdx.x == 0) {
@@ -388,9 +383,8 @@ int fem_batched_assemble_vjp(const FemMesh* mesh, const FemBasis* basis, const F
   const int tU = fem::tuning_for(basis->family).sum_unroll >= 8 ? 8 : 4;
   auto launch = [&](auto kern, int L, int G) -> int {
     const int rpw = 32 / G;
-    const size_t sm_cells = (size_t)fem_batched::kBlock * (L + 1) * sizeof(double);
-    const size_t sm_rows = (size_t)(fem_batched::kBlock / 32) * rpw * sa.stride * sizeof(double);
-    const size_t smem = std::max(sm_cells, sm_rows);
+    (void)L;
+    const size_t smem = (size_t)(fem_batched::kBlock / 32) * rpw * sa.stride * sizeof(double);
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem);

@@ -103,7 +103,7 @@ class BatchedBasis(CellBasis):
         return [x[self.elem_offsets[k]:self.elem_offsets[k + 1]] for k in range(self.nmeshes)]
 
 
-ROWS_PER_UNIT = 256
+ROWS_PER_UNIT = 1024
 
 
 class GraphedAssembly:
