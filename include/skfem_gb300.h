@@ -219,8 +219,13 @@ int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll, 
  * per CSR row adding (cell, local row) contributions into shared-memory
  * slots; 1 (the default) one lane per CSR entry on or above the diagonal
  * walking that entry's contribution list in registers and writing the
- * entry and its transpose.  Both add every entry's contributions in the
- * same order: the values are the same bit for bit.
+ * entry and its transpose; 2 variant 1 with each warp's next list codes
+ * brought into shared memory by the TMA bulk-copy engine (double-buffered
+ * on mbarriers; used when the call passes a status word, which receives
+ * FEM_ERR_TIMEOUT if a bounded wait runs out).  All add every entry's
+ * contributions in the same order: the values are the same bit for bit
+ * (up to the fixed-point mass sums' truncation on meshes whose cells around
+ * a vertex differ in size by more than a factor 8, a few ulps).
  */
 int fem_set_onepass(int family, int variant);
 

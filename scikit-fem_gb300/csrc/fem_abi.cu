@@ -423,7 +423,7 @@ const char* fem_last_error(void) { return fem::g_err.c_str(); }
 const char* fem_version(void) { return "skfem_gb300 0.1 (sm_103a)"; }
 
 int fem_set_onepass(int family, int variant) {
-  if (family < 1 || family > 5 || variant < 0 || variant > 1) {
+  if (family < 1 || family > 5 || variant < 0 || variant > 2) {
     set_error(FEM_ERR_ARGUMENT, "family %d / one-pass variant %d out of range", family, variant);
     return FEM_ERR_ARGUMENT;
   }
@@ -675,9 +675,9 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
     fem::Pattern P = pat->P;
     const fem::Tuning t = fem::tuning_for(basis->family);
     P.sum_unroll = t.sum_unroll;
-    if (t.onepass == 1 && pat->upper_ok)
+    if (t.onepass >= 1 && pat->upper_ok)
       return fem::csr_sum_upper_p1(P, pat->upper, mesh->dim, pat->geo, form->diff, form->mass,
-                                   pat->mbase, csr_values, st);
+                                   pat->mbase, csr_values, st, 0, -1, status, t.onepass == 2);
     return fem::csr_sum_geometry_p1(P, mesh->dim, pat->geo, form->diff, form->mass, pat->mbase,
                                     csr_values, st);
   }
@@ -747,6 +747,8 @@ struct GeometrySum {
   FemCoef diff, mass;
   const int16_t* mbase;
   const fem::UpperLists* upper;   // null: the row kernel
+  int32_t* status;                 // the staged upper form's wait errors
+  bool tma;                        // stage the upper lists' codes with TMA
 };
 
 int sum_rows_to_host(const fem::Pattern& P, const std::vector<int32_t>& ip, const double* staging,
@@ -757,7 +759,7 @@ int sum_rows_to_host(const fem::Pattern& P, const std::vector<int32_t>& ip, cons
                                     row0, row1)
            : gs ? (gs->upper ? fem::csr_sum_upper_p1(P, *gs->upper, gs->dim, gs->geo, gs->diff,
                                                       gs->mass, gs->mbase, csr_values, st, row0,
-                                                      row1)
+                                                      row1, gs->status, gs->tma)
                              : fem::csr_sum_geometry_p1(P, gs->dim, gs->geo, gs->diff, gs->mass,
                                                         gs->mbase, csr_values, st, row0, row1))
                 : fem::csr_sum(P, staging, csr_values, st, row0, row1, nullptr, P.staging_sym);
@@ -1061,7 +1063,8 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
   FusedSum fs;
   const bool fused = fused_sum(pat, mesh, basis, form, &fs);
   GeometrySum gs{mesh->dim, pat->geo, form->diff, form->mass, pat->mbase,
-                 (tune.onepass == 1 && pat->upper_ok) ? &pat->upper : nullptr};
+                 (tune.onepass >= 1 && pat->upper_ok) ? &pat->upper : nullptr, status,
+                 tune.onepass == 2};
   const bool onepass = !fused && geometry_sum(pat, mesh, basis, form);
   std::vector<cudaEvent_t> evs;
   auto event = [&](cudaEvent_t* ev) -> cudaError_t {

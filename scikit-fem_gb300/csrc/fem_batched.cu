@@ -153,21 +153,28 @@ __global__ void __launch_bounds__(kBlock) batched_forward_vjp_kernel(
             wl[i] = w[dof];
             ul[i] = u[dof];
           }
-          double js = 0.0, jm = 0.0;
+          if (dcd) {
+            double js = 0.0;
 #pragma unroll
-          for (int i = 0; i < NB; ++i) {
-            double ks = 0.0, ms = 0.0;
+            for (int i = 0; i < NB; ++i) {
+              double ks = 0.0;
 #pragma unroll
-            for (int j = 0; j < NB; ++j) {
-              const double sij = i <= j ? kst[i][j] : kst[j][i];
-              ks = __fma_rn(sij, ul[j], ks);
-              ms = __fma_rn(mm[i][j], ul[j], ms);
+              for (int j = 0; j < NB; ++j) ks = __fma_rn(i <= j ? kst[i][j] : kst[j][i], ul[j], ks);
+              js = __fma_rn(wl[i], ks, js);
             }
-            js = __fma_rn(wl[i], ks, js);
-            jm = __fma_rn(wl[i], ms, jm);
+            dcd[e] = f.diff.scale * js;
           }
-          if (dcd) dcd[e] = f.diff.scale * js;
-          if (dcm) dcm[e] = f.mass.scale * adet * jm;
+          if (dcm) {
+            double jm = 0.0;
+#pragma unroll
+            for (int i = 0; i < NB; ++i) {
+              double ms = 0.0;
+#pragma unroll
+              for (int j = 0; j < NB; ++j) ms = __fma_rn(mm[i][j], ul[j], ms);
+              jm = __fma_rn(wl[i], ms, jm);
+            }
+            dcm[e] = f.mass.scale * adet * jm;
+          }
         }
         flags |= cell_status(f, e, rb);
       }

@@ -173,7 +173,8 @@ struct Tuning {
   int persistent = 0;     // >0: grid capped at persistent * SMs (grid-stride)
   int sum_unroll = 8;     // incidence entries loaded together in the sum
   int sum_cols = 1;       // fused sum: columns per lane (1, or 2 for an even row length)
-  int onepass = 1;        // one-pass P1 sum: 0 two lanes per row, 1 a lane per upper entry
+  int onepass = 1;        // one-pass P1 sum: 0 two lanes per row, 1 a lane per upper entry,
+                          // 2 the same with its codes staged in shared memory by TMA
 };
 Tuning tuning_for(int family);
 
@@ -216,6 +217,7 @@ int row_mass_base(const Pattern& P, const double* adet, int16_t* mbase, int* shm
 // in the sum's order, sliced 32 entries at a time.  Pattern-only data.
 struct UpperLists {
   int64_t nd = 0, nupper = 0, nslices = 0, ncodes = 0;
+  int32_t max_len = 0;          // the longest slice (codes per lane)
   int32_t* dpos = nullptr;      // nrows + 1: row -> first diagonal entry
   int32_t* opos = nullptr;      // nrows + 1: row -> first off-diagonal entry (after nd)
   int32_t* pos = nullptr;       // nupper: CSR index of (i, j)
@@ -228,9 +230,12 @@ struct UpperLists {
 };
 int build_upper_lists(const Pattern& P, UpperLists* U, cudaStream_t st);
 void free_upper_lists(UpperLists* U);
+// tma: stage each warp's slice codes in shared memory with bulk copies
+// (needs status for its bounded waits' error bit)
 int csr_sum_upper_p1(const Pattern& P, const UpperLists& U, int dim, const double* geo,
                      const FemCoef& diff, const FemCoef& mass, const int16_t* mbase, double* vals,
-                     cudaStream_t st, int64_t row0 = 0, int64_t row1 = -1);
+                     cudaStream_t st, int64_t row0 = 0, int64_t row1 = -1,
+                     int32_t* status = nullptr, bool tma = false);
 
 int basis_nb_scalar(int family);
 int basis_dim(int family);

@@ -646,6 +646,115 @@ __global__ void __launch_bounds__(128) csr_geometry_p1_kernel(
 // is e * 16 + li * 4 + lj.  Upper entries are numbered diagonal entries
 // first (by row), then the others by (row, column), so list lengths within
 // a slice are alike (a vertex's cells vs an edge's cells).
+// TMA (bulk-copy engine) helpers for the staged form below.
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// One bulk copy of `bytes` (a multiple of 16, both ends 16-byte aligned)
+// from global memory into this CTA's shared memory, completing on `bar`.
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t bytes,
+                                            uint64_t* bar) {
+  unsigned long long state;
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+               : "=l"(state) : "r"(smem_addr(bar)), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+  (void)state;
+}
+// Bounded wait for the phase `parity` of `bar`; false when it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit) {
+  for (long long it = 0; it < limit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
+        "selp.u32 %0, 1, 0, p; }"
+        : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// One slice of upper entries: lane `lane` walks codes cp[p * 32], p < len.
+template <int NU, int U, bool MFIELD, bool SMEM>
+__device__ __forceinline__ void upper_slice(
+    const uint32_t* __restrict__ cp, int len, int64_t u, bool live,
+    const int32_t* __restrict__ pos, const int32_t* __restrict__ tpos,
+    const int32_t* __restrict__ urow, const double* __restrict__ geo, int64_t nelems,
+    const double* __restrict__ kfield, int64_t kstride, double kscale,
+    const double* __restrict__ mfield, int64_t mstride, double mscale, double moff,
+    const int16_t* __restrict__ mbase, double* __restrict__ vals) {
+  constexpr int NG = NU * (NU + 1) / 2;
+  using MAcc = typename std::conditional<MFIELD, double, long long>::type;
+  const double* __restrict__ adet_arr = geo + (int64_t)NG * nelems;
+  auto code_at = [&](int p) -> uint32_t {
+    if constexpr (SMEM) return cp[p * 32];
+    else return __ldg(cp + (int64_t)p * 32);
+  };
+  int mb = 0;
+  if (!MFIELD && live) mb = mbase[urow[u]];
+  double acck = 0.0;
+  MAcc accm = (MAcc)0;
+  uint32_t cn[U];
+#pragma unroll
+  for (int v = 0; v < U; ++v) cn[v] = v < len ? code_at(v) : 0xFFFFFFFFu;
+  for (int p0 = 0; p0 < len; p0 += U) {
+    uint32_t c[U];
+#pragma unroll
+    for (int v = 0; v < U; ++v) {
+      c[v] = cn[v];
+      const int pn = p0 + U + v;
+      cn[v] = pn < len ? code_at(pn) : 0xFFFFFFFFu;
+    }
+    double kv[U], g[U];
+    MAcc mv[U];
+#pragma unroll
+    for (int v = 0; v < U; ++v) {
+      kv[v] = 0.0;
+      g[v] = 0.0;
+      mv[v] = (MAcc)0;
+      if (live && c[v] != 0xFFFFFFFFu) {
+        const uint32_t e = c[v] >> 4;
+        const int li = (int)((c[v] >> 2) & 3u), lj = (int)(c[v] & 3u);
+        kv[v] = kfield ? __ldg(kfield + (int64_t)e * kstride) : 1.0;
+        g[v] = __ldg(geo + (int64_t)gram_index(NU, li, lj) * nelems + e);
+        const double adet = __ldg(adet_arr + e);
+        MAcc m;
+        if constexpr (MFIELD) m = __ldg(mfield + (int64_t)e * mstride) * adet;
+        else m = fixed_of(adet, mb);
+        mv[v] = li == lj ? m + m : m;
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < U; ++v) {
+      acck = __fma_rn(kv[v], g[v], acck);
+      accm += mv[v];
+    }
+  }
+  if (live) {
+    double mc;
+    if constexpr (MFIELD) {
+      mc = moff;
+    } else {
+      const double unit = dfrombits((unsigned long long)(mb - 1075 + 1023) << 52);
+      mc = (mscale * moff) * unit;
+    }
+    const double m = MFIELD ? (double)accm : __ll2double_rn((long long)accm);
+    const double val = __fma_rn(mc, m, kscale * acck);
+    vals[pos[u]] = val;
+    const int32_t t = tpos[u];
+    if (t >= 0) vals[t] = val;
+  }
+}
+
 template <int NU, int U, bool MFIELD>
 __global__ void __launch_bounds__(128) csr_upper_p1_kernel(
     int64_t ua, int64_t ub, const int32_t* __restrict__ slice_len,
@@ -655,73 +764,87 @@ __global__ void __launch_bounds__(128) csr_upper_p1_kernel(
     const double* __restrict__ kfield, int64_t kstride, double kscale,
     const double* __restrict__ mfield, int64_t mstride, double mscale, double moff,
     const int16_t* __restrict__ mbase, double* __restrict__ vals) {
-  constexpr int NG = NU * (NU + 1) / 2;
-  using MAcc = typename std::conditional<MFIELD, double, long long>::type;
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   const int64_t s0 = ua >> 5, s1 = (ub + 31) >> 5;
-  const double* __restrict__ adet_arr = geo + (int64_t)NG * nelems;
   for (int64_t sl = s0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); sl < s1;
        sl += warps) {
     const int64_t u = sl * 32 + lane;
-    const bool live = u >= ua && u < ub;
+    upper_slice<NU, U, MFIELD, false>(codes + (int64_t)slice_base[sl] * 32 + lane, slice_len[sl],
+                                      u, u >= ua && u < ub, pos, tpos, urow, geo, nelems, kfield,
+                                      kstride, kscale, mfield, mstride, mscale, moff, mbase, vals);
+  }
+}
+
+// The same sum with each warp's slice codes staged in shared memory by the
+// TMA bulk-copy engine: lane 0 of the warp issues one cp.async.bulk of the
+// next slice's codes (len x 128 bytes, contiguous) while the warp works on
+// the current one, double-buffered on two mbarriers, so the lanes read their
+// codes from shared memory and only the geometry gathers go to L2 / HBM.
+// cap: the longest slice (codes per lane) the buffers hold.  Every wait is
+// bounded; past the limit the warp sets FEM_ERR_TIMEOUT in *status and
+// stops, after a second bounded wait for its copies in flight.
+template <int NU, int U, bool MFIELD>
+__global__ void __launch_bounds__(128) csr_upper_p1_tma_kernel(
+    int64_t ua, int64_t ub, const int32_t* __restrict__ slice_len,
+    const int32_t* __restrict__ slice_base, const uint32_t* __restrict__ codes, int cap,
+    const int32_t* __restrict__ pos, const int32_t* __restrict__ tpos,
+    const int32_t* __restrict__ urow, const double* __restrict__ geo, int64_t nelems,
+    const double* __restrict__ kfield, int64_t kstride, double kscale,
+    const double* __restrict__ mfield, int64_t mstride, double mscale, double moff,
+    const int16_t* __restrict__ mbase, double* __restrict__ vals, int32_t* __restrict__ status) {
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  constexpr long long kWaitLimit = 1ll << 24;
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  uint32_t* const buf0 = reinterpret_cast<uint32_t*>(tma_smem) + (size_t)wib * 2 * cap * 32;
+  uint32_t* const buf1 = buf0 + (size_t)cap * 32;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tma_smem + (size_t)nw * 2 * cap * 32 * 4) + wib * 2;
+  if (lane == 0) {
+    mbar_init(bar);
+    mbar_init(bar + 1);
+    mbar_init_fence();
+  }
+  __syncwarp();
+  const int64_t warps = (int64_t)gridDim.x * nw;
+  const int64_t s0 = ua >> 5, s1 = (ub + 31) >> 5;
+  int64_t sl = s0 + (int64_t)blockIdx.x * nw + wib;
+  uint32_t ph0 = 0u, ph1 = 0u;    // the phase each buffer's barrier waits for next
+  auto issue = [&](int64_t s, int k) {
+    if (s < s1 && lane == 0) {
+      const int len = slice_len[s];
+      if (len > 0)
+        tma_load_1d(k ? buf1 : buf0, codes + (int64_t)slice_base[s] * 32, (uint32_t)len * 128u,
+                    bar + k);
+    }
+  };
+  issue(sl, 0);
+  int k = 0;
+  while (sl < s1) {
+    const int64_t next = sl + warps;
+    issue(next, k ^ 1);          // that buffer was released by the __syncwarp below
     const int len = slice_len[sl];
-    const int64_t base = slice_base[sl];
-    int mb = 0;
-    if (!MFIELD && live) mb = mbase[urow[u]];
-    const uint32_t* __restrict__ cp = codes + base * 32 + lane;
-    double acck = 0.0;
-    MAcc accm = (MAcc)0;
-    uint32_t cn[U];
-#pragma unroll
-    for (int v = 0; v < U; ++v) cn[v] = v < len ? __ldg(cp + (int64_t)v * 32) : 0xFFFFFFFFu;
-    for (int p0 = 0; p0 < len; p0 += U) {
-      uint32_t c[U];
-#pragma unroll
-      for (int v = 0; v < U; ++v) {
-        c[v] = cn[v];
-        const int pn = p0 + U + v;
-        cn[v] = pn < len ? __ldg(cp + (int64_t)pn * 32) : 0xFFFFFFFFu;
+    if (len > 0) {
+      const uint32_t ph = k ? ph1 : ph0;
+      if (!mbar_wait(bar + k, ph, kWaitLimit)) {
+        if (lane == 0 && status) atomicOr(status, 1 << FEM_ERR_TIMEOUT);
+        // the copies still in flight must land before the block exits
+        mbar_wait(bar + k, ph, kWaitLimit);
+        if (next < s1 && slice_len[next] > 0)
+          mbar_wait(bar + (k ^ 1), k ? ph0 : ph1, kWaitLimit);
+        return;
       }
-      double kv[U], g[U];
-      MAcc mv[U];
-#pragma unroll
-      for (int v = 0; v < U; ++v) {
-        kv[v] = 0.0;
-        g[v] = 0.0;
-        mv[v] = (MAcc)0;
-        if (live && c[v] != 0xFFFFFFFFu) {
-          const uint32_t e = c[v] >> 4;
-          const int li = (int)((c[v] >> 2) & 3u), lj = (int)(c[v] & 3u);
-          kv[v] = kfield ? __ldg(kfield + (int64_t)e * kstride) : 1.0;
-          g[v] = __ldg(geo + (int64_t)gram_index(NU, li, lj) * nelems + e);
-          const double adet = __ldg(adet_arr + e);
-          MAcc m;
-          if constexpr (MFIELD) m = __ldg(mfield + (int64_t)e * mstride) * adet;
-          else m = fixed_of(adet, mb);
-          mv[v] = li == lj ? m + m : m;
-        }
-      }
-#pragma unroll
-      for (int v = 0; v < U; ++v) {
-        acck = __fma_rn(kv[v], g[v], acck);
-        accm += mv[v];
-      }
+      if (k) ph1 ^= 1u;
+      else ph0 ^= 1u;
     }
-    if (live) {
-      double mc;
-      if constexpr (MFIELD) {
-        mc = moff;
-      } else {
-        const double unit = dfrombits((unsigned long long)(mb - 1075 + 1023) << 52);
-        mc = (mscale * moff) * unit;
-      }
-      const double m = MFIELD ? (double)accm : __ll2double_rn((long long)accm);
-      const double val = __fma_rn(mc, m, kscale * acck);
-      vals[pos[u]] = val;
-      const int32_t t = tpos[u];
-      if (t >= 0) vals[t] = val;
-    }
+    const int64_t u = sl * 32 + lane;
+    upper_slice<NU, U, MFIELD, true>((k ? buf1 : buf0) + lane, len, u, u >= ua && u < ub, pos,
+                                     tpos, urow, geo, nelems, kfield, kstride, kscale, mfield,
+                                     mstride, mscale, moff, mbase, vals);
+    __syncwarp();
+    sl = next;
+    k ^= 1;
   }
 }
 
@@ -1499,6 +1622,15 @@ int build_upper_lists(const Pattern& P, UpperLists* U, cudaStream_t st) {
     return fail(FEM_ERR_CAPACITY);
   }
   U->ncodes = rows32 * 32;
+  {
+    std::vector<int32_t> lens(U->nslices);
+    e = cudaMemcpyAsync(lens.data(), U->slice_len, U->nslices * sizeof(int32_t),
+                        cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(check_cuda(e, "upper slice lengths"));
+    U->max_len = 0;
+    for (int32_t v : lens) U->max_len = std::max(U->max_len, v);
+  }
   e = cudaMalloc(&U->codes, std::max<int64_t>(1, U->ncodes) * sizeof(uint32_t));
   if (e != cudaSuccess) return fail(check_cuda(e, "cudaMalloc(upper codes)"));
   FEM_TRY_CUDA(cudaMemsetAsync(U->codes, 0xFF, std::max<int64_t>(1, U->ncodes) * sizeof(uint32_t), st));
@@ -1539,7 +1671,7 @@ void free_upper_lists(UpperLists* U) {
 
 int csr_sum_upper_p1(const Pattern& P, const UpperLists& U, int dim, const double* geo,
                      const FemCoef& diff, const FemCoef& mass, const int16_t* mbase, double* vals,
-                     cudaStream_t st, int64_t row0, int64_t row1) {
+                     cudaStream_t st, int64_t row0, int64_t row1, int32_t* status, bool tma) {
   const int nu = dim + 1;
   if (!U.codes || P.nbfun_u != nu || (dim != 2 && dim != 3)) {
     set_error(FEM_ERR_ARGUMENT, "the upper-gather P1 sum needs the pattern's upper lists");
@@ -1570,17 +1702,37 @@ int csr_sum_upper_p1(const Pattern& P, const UpperLists& U, int dim, const doubl
     const int64_t nsl = ((ub + 31) >> 5) - (ua >> 5);
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nsl, threads / 32),
                                                                 (int64_t)num_sms() * 32));
+    // the staged form: two buffers of the longest slice per warp + 2 mbarriers
+    const size_t tma_smem = (size_t)(threads / 32) * (2 * (size_t)U.max_len * 128 + 16);
+    const bool staged = tma && status && U.max_len > 0 && tma_smem <= 96 * 1024;
     auto launch = [&](auto kern) {
       kern<<<grid, threads, 0, st>>>(ua, ub, U.slice_len, U.slice_base, U.codes, U.pos, U.tpos,
                                      U.row, geo, P.nelems, kf, ks, diff.scale, mf, ms, mass.scale,
                                      moff, mbase, vals);
     };
+    auto launch_tma = [&](auto kern) -> int {
+      if (tma_smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)tma_smem);
+        if (e != cudaSuccess) return check_cuda(e, "csr_upper_p1_tma smem");
+      }
+      kern<<<grid, threads, tma_smem, st>>>(ua, ub, U.slice_len, U.slice_base, U.codes,
+                                            U.max_len, U.pos, U.tpos, U.row, geo, P.nelems, kf, ks,
+                                            diff.scale, mf, ms, mass.scale, moff, mbase, vals,
+                                            status);
+      return 0;
+    };
+    int rc = 0;
 #define FEM_UP_PICK(NU)                                                                     \
-    if (mf) { if (Un == 8) launch(csr_upper_p1_kernel<NU, 8, true>); else launch(csr_upper_p1_kernel<NU, 4, true>); } \
+    if (staged) { \
+      if (mf) rc = Un == 8 ? launch_tma(csr_upper_p1_tma_kernel<NU, 8, true>) : launch_tma(csr_upper_p1_tma_kernel<NU, 4, true>); \
+      else rc = Un == 8 ? launch_tma(csr_upper_p1_tma_kernel<NU, 8, false>) : launch_tma(csr_upper_p1_tma_kernel<NU, 4, false>); \
+    } else if (mf) { if (Un == 8) launch(csr_upper_p1_kernel<NU, 8, true>); else launch(csr_upper_p1_kernel<NU, 4, true>); } \
     else { if (Un == 8) launch(csr_upper_p1_kernel<NU, 8, false>); else launch(csr_upper_p1_kernel<NU, 4, false>); }
     if (nu == 4) { FEM_UP_PICK(4) }
     else { FEM_UP_PICK(3) }
 #undef FEM_UP_PICK
+    if (rc) return rc;
     FEM_LAUNCH_CHECK("csr_upper_p1_kernel");
   }
   return 0;

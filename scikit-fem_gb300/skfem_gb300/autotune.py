@@ -25,8 +25,9 @@ CANDIDATES = {
 # columns per lane of the fused sum: the scalar bases with 4, 6 or 10 local
 # functions also have the two-columns-per-lane kernel
 COLS = {"TetP1": (1, 2), "TriP2": (1, 2), "TetP2": (1, 2)}
-# the one-pass P1 sum's two forms (two lanes per row / a lane per upper entry)
-ONEPASS = {"TriP1": (0, 1), "TetP1": (0, 1)}
+# the one-pass P1 sum's forms (two lanes per row / a lane per upper entry /
+# the same with TMA-staged list codes)
+ONEPASS = {"TriP1": (0, 1, 2), "TetP1": (0, 1, 2)}
 
 
 def candidates(family, vector=False):

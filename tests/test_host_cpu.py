@@ -163,11 +163,11 @@ def test_autotune_candidates_per_family():
         assert {x["onepass"] for x in c} == {1}
         assert len(autotune.candidates(fam, vector=True)) == base
     c = autotune.candidates("TetP1")
-    assert len(c) == 4 * base and {x["sum_cols"] for x in c} == {1, 2}
-    assert {x["onepass"] for x in c} == {0, 1}
+    assert len(c) == 6 * base and {x["sum_cols"] for x in c} == {1, 2}
+    assert {x["onepass"] for x in c} == {0, 1, 2}
     assert len(autotune.candidates("TetP1", vector=True)) == base
     c = autotune.candidates("TriP1")
-    assert len(c) == 2 * base and {x["onepass"] for x in c} == {0, 1}
+    assert len(c) == 3 * base and {x["onepass"] for x in c} == {0, 1, 2}
     c = autotune.candidates("Hex1")
     assert len(c) == base and {x["sum_cols"] for x in c} == {1}
     c = autotune.candidates("TetP1")
