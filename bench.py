@@ -258,7 +258,16 @@ def gpu_arm(args):
     nel = m.nelements
     # launch parameters by the autotuner on this workload (setup, untimed)
     from skfem_gb300 import autotune
-    tuned, _ = autotune.tune(form, b, {"k": kd}, reps=3, use_cache=False)
+    tuned, timings = autotune.tune(form, b, {"k": kd}, reps=3, use_cache=False)
+    # the fastest configuration of each form of the one-pass sum (0 two lanes
+    # per row, 1 a lane per upper entry, 2 the same with TMA-staged codes)
+    variant_ms = {}
+    for t_ms, cfg in timings:
+        v = str(cfg.get("onepass", 1))
+        variant_ms[v] = min(variant_ms.get(v, float("inf")), t_ms)
+    if args.onepass is not None:
+        tuned = dict(tuned, onepass=args.onepass)
+        autotune.apply(N.FAMILY["TetP1"], tuned)
 
     # a bare C-ABI step: inputs in HBM, results in HBM
     coeffs, ch, c_form = form._setup(b, None, {"k": kd})
@@ -299,6 +308,9 @@ def gpu_arm(args):
     # fem_assemble_local and fem_csr_sum_staged run them) and the local
     # kernel computing its geometry from the coordinates
     local_buf = entry.staging
+    # the two-pass kernels at their own default launch shape (the tuned one
+    # is chosen for the one-pass sum and does not apply to them)
+    autotune.apply(N.FAMILY["TetP1"], dict(tuned, local_block=128, persistent=0))
     e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
     t_local, t_sum, t_geom, t_one = 0.0, 0.0, 0.0, 0.0
     reps = max(3, args.steps)
@@ -326,6 +338,7 @@ def gpu_arm(args):
         e1.record(stream)
         torch.cuda.synchronize()
         t_geom += e0.elapsed_time(e1)
+    autotune.apply(N.FAMILY["TetP1"], tuned)
     t_local /= reps
     t_sum /= reps
     t_geom /= reps
@@ -414,7 +427,8 @@ def gpu_arm(args):
                                            "unit-coefficient rows and mass matrix; not the "
                                            "plain step)", t_cu, FUSED_B_PER_CELL),
             "bytes_source": TRAFFIC_SOURCE,
-            "two_pass_vs_onepass_max_rel": d},
+            "two_pass_vs_onepass_max_rel": d,
+            "onepass_variants_best_ms": variant_ms},
         "fp64": {"kernel": "local matrices computing their geometry (fem_local_matrices; the "
                            "step reads the basis's cached geometry instead)",
                  "ms": t_geom, "gflops": fp64_achieved, "peak_gflops": FP64_PEAK_GFLOPS,
@@ -811,6 +825,8 @@ def main():
     ap.add_argument("--only", default=None,
                     choices=["tri_p1", "tet_p2_vec", "hex1_vjp", "batched", "generic"],
                     help="run one secondary workload alone and print its record")
+    ap.add_argument("--onepass", type=int, default=None, choices=[0, 1, 2],
+                    help="fix the one-pass sum's form after autotuning (default: the fastest)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the TriP1 / vector TetP2 / Hex1 adjoint / batched workloads")

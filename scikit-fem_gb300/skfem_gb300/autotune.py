@@ -79,6 +79,9 @@ def tune(form, basis, coefs, reps=3, use_cache=True):
     entry = next(e for k, e in basis._patterns.items() if k[0] == "bilinear")
     _, _, c_form = form._setup(basis, None, coefs)
     vals = torch.empty(entry.nnz, dtype=torch.float64, device=basis.device)
+    # a status word, as assemblies pass one (the TMA-staged one-pass form
+    # runs only with it)
+    status = torch.zeros(1, dtype=torch.int32, device=basis.device)
     lib = N.lib()
     timings = []
     for cfg in candidates(basis.elem.family, bool(basis.elem.vector)):
@@ -88,7 +91,7 @@ def tune(form, basis, coefs, reps=3, use_cache=True):
         def step():
             N.check(lib.fem_assemble(N.byref(basis.c_mesh), N.byref(basis.c_basis),
                                      N.byref(c_form), entry.pat.handle, N.ptr(entry.staging),
-                                     N.ptr(vals), None, s))
+                                     N.ptr(vals), N.ptr(status), s))
         step()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
