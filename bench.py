@@ -45,8 +45,17 @@ UNIT = "elements/s"
 # on the 61^3-node cube (1,296,000 cells) -- the one-pass sum and the
 # coefficient checks of the step; the two-pass kernels (local kernel on the
 # cached geometry, staging sum) and the opt-in coefficient-update sum for
-# comparison.  None until a capture of that kernel exists.
-ONEPASS_B_PER_CELL = None
+# comparison.  The one-pass sum's figure is per form (fem_set_onepass
+# variant: 0 row form, 1 upper-gather form, 2 upper form with TMA-staged codes);
+# the upper-gather form's is from one launch at the full 101^3 size (6M cells:
+# 1.18 GB read + 168.8 MB written), where fewer geometry gathers hit L2 than
+# at 1.3M cells (185.9 B/cell there).
+ONEPASS_B_PER_CELL = {0: 159.7, 1: 224.8, 2: 185.6}
+ONEPASS_B_SOURCE = {0: "one launch at 1.3M cells", 1: "one launch at 6M cells (this workload)",
+                    2: "one launch at 1.3M cells"}
+ONEPASS_KERNEL = {0: "csr_geometry_p1_kernel<4,U,0> (one-pass P1 sum, row form)",
+                  1: "csr_upper_p1_kernel<4,U,0> (one-pass P1 sum, upper-gather form)",
+                  2: "csr_upper_p1_tma_kernel<4,U,0> (one-pass P1 sum, TMA-staged codes)"}
 CHECK_B_PER_CELL = 9.0
 LOCAL_B_PER_CELL = 233.0
 SUM_B_PER_CELL = 193.9
@@ -391,7 +400,9 @@ def gpu_arm(args):
             out["frac_hbm"] = out["gbs"] / hbm
         return out
 
-    traffic = None if ONEPASS_B_PER_CELL is None else (ONEPASS_B_PER_CELL + CHECK_B_PER_CELL) * nel
+    one_form = int(tuned.get("onepass", 1))
+    one_bpc = ONEPASS_B_PER_CELL.get(one_form)
+    traffic = None if one_bpc is None else (one_bpc + CHECK_B_PER_CELL) * nel
     res = {
         "metric": METRIC, "value": replica_value(nel, world, ms), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -409,15 +420,14 @@ def gpu_arm(args):
                      "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic,
                      "traffic_source": (None if traffic is None else
-                                        "%s: one-pass sum %.1f + checks %.1f B/cell, scaled by "
-                                        "cells" % (TRAFFIC_SOURCE, ONEPASS_B_PER_CELL,
-                                                   CHECK_B_PER_CELL)),
+                                        "ncu dram__bytes_read+write, %s: one-pass sum %.1f + "
+                                        "checks %.1f B/cell" % (ONEPASS_B_SOURCE[one_form],
+                                                                one_bpc, CHECK_B_PER_CELL)),
                      "peak_kind": peak_kind, "algorithmic_bytes_per_step": Bytes,
                      "kernel": "whole assembly step (coefficient checks + one-pass sum)",
                      "fp64_floor_ms": nel * 16 / 0.598e12 * 1e3},
         "kernels": {
-            "onepass_sum": kern("csr_geometry_p1_kernel<4,U,false> (one-pass P1 sum on the "
-                                "cached geometry)", t_one, ONEPASS_B_PER_CELL),
+            "onepass_sum": kern(ONEPASS_KERNEL[one_form], t_one, one_bpc),
             "coef_checks": kern("coef_fields_kernel (step time minus the one-pass sum)",
                                 t_checks, CHECK_B_PER_CELL),
             "two_pass_local": kern("simplex_scalar_kernel<3,1,BS,cached geometry>", t_local,

@@ -392,6 +392,11 @@ int fem_batched_assemble_vjp(const FemMesh* mesh, const FemBasis* basis, const F
     const int rpw = 32 / G;
     (void)L;
     const size_t smem = (size_t)(fem_batched::kBlock / 32) * rpw * sa.stride * sizeof(double);
+    if (smem > 227 * 1024) {
+      fem::set_error(FEM_ERR_CAPACITY, "a CSR row of %d entries needs more shared memory for "
+                     "the batched kernel's row accumulators than a block has", sa.stride);
+      return FEM_ERR_CAPACITY;
+    }
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem);

@@ -30,6 +30,26 @@ namespace fem {
 namespace {
 
 constexpr int kWarpsPerBlock = 4;
+constexpr size_t kMaxBlockSmem = 227 * 1024;
+// candidate columns a warp gathers and sorts for one CSR row (a power of two;
+// 2 x 16384 words = 128 KB of shared memory, one warp per block at that size)
+constexpr int kMaxRowCandidates = 16384;
+
+// Warps per block of a kernel whose warps each hold bytes_per_warp of shared
+// memory (candidate columns, row accumulators): kWarpsPerBlock, or fewer when
+// that does not fit the 227 KB a block may use; 0 when one warp does not fit.
+static int smem_block_warps(size_t bytes_per_warp) {
+  for (int w = kWarpsPerBlock; w >= 1; --w)
+    if ((size_t)w * bytes_per_warp <= kMaxBlockSmem) return w;
+  return 0;
+}
+
+static int row_smem_error(int row_nnz) {
+  set_error(FEM_ERR_CAPACITY,
+            "a CSR row of %d entries needs more shared memory for its accumulators than a "
+            "block has (227 KB)", row_nnz);
+  return FEM_ERR_CAPACITY;
+}
 
 __global__ void count_rows_kernel(const int32_t* __restrict__ dofs, int64_t nelems, int nb,
                                   int64_t nrows, int32_t* __restrict__ cnt,
@@ -148,10 +168,10 @@ __global__ void row_nnz_kernel(const int32_t* __restrict__ inc_ptr, const int32_
                                int32_t* __restrict__ row_nnz, int32_t* __restrict__ maxnnz) {
   extern __shared__ int32_t ismem[];
   const int w = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
   int32_t* cand = ismem + (size_t)w * 2 * cap;
   int32_t* srt = cand + cap;
-  for (int64_t r = (int64_t)blockIdx.x * kWarpsPerBlock + w; r < nrows;
-       r += (int64_t)gridDim.x * kWarpsPerBlock) {
+  for (int64_t r = (int64_t)blockIdx.x * nw + w; r < nrows; r += (int64_t)gridDim.x * nw) {
     const int cnt = row_columns(r, inc_ptr, inc, udofs, local, nelems, nv, nu, cap, cand, srt);
     if ((threadIdx.x & 31) == 0) {
       row_nnz[r] = cnt;
@@ -169,10 +189,10 @@ __global__ void row_fill_kernel(const int32_t* __restrict__ inc_ptr, const int32
   extern __shared__ int32_t ismem[];
   const int w = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
   int32_t* cand = ismem + (size_t)w * 2 * cap;
   int32_t* srt = cand + cap;
-  for (int64_t r = (int64_t)blockIdx.x * kWarpsPerBlock + w; r < nrows;
-       r += (int64_t)gridDim.x * kWarpsPerBlock) {
+  for (int64_t r = (int64_t)blockIdx.x * nw + w; r < nrows; r += (int64_t)gridDim.x * nw) {
     row_columns(r, inc_ptr, inc, udofs, local, nelems, nv, nu, cap, cand, srt);
     const int32_t b = inc_ptr[r], len = inc_ptr[r + 1] - b;
     const int n = len * nu;
@@ -1213,13 +1233,15 @@ int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, 
   int cap = 1;
   while (cap < P->max_row_inc * nu) cap <<= 1;
   cap = std::max(cap, 32);
-  if (cap > 8192) {
+  if (cap > kMaxRowCandidates) {
     set_error(FEM_ERR_CAPACITY,
-              "a row gathers %d candidate columns (limit 8192): the mesh has a DOF shared by "
-              "%d cells", P->max_row_inc * nu, P->max_row_inc);
+              "a row gathers %d candidate columns (limit %d): the mesh has a DOF shared by "
+              "%d cells", P->max_row_inc * nu, kMaxRowCandidates, P->max_row_inc);
     return FEM_ERR_CAPACITY;
   }
-  const size_t smem = (size_t)kWarpsPerBlock * 2 * cap * sizeof(int32_t);
+  // a warp sorts its row's candidates in shared memory (2 x cap words)
+  const int rwarps = smem_block_warps((size_t)2 * cap * sizeof(int32_t));
+  const size_t smem = (size_t)rwarps * 2 * cap * sizeof(int32_t);
   if (smem > 48 * 1024) {
     FEM_TRY_CUDA(cudaFuncSetAttribute(row_nnz_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
@@ -1232,10 +1254,10 @@ int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, 
   FEM_TRY_CUDA(scratch.alloc(&flags, sizeof(int32_t)));
   FEM_TRY_CUDA(cudaMemsetAsync(flags, 0, sizeof(int32_t), st));
   FEM_TRY_CUDA(cudaMemsetAsync(row_nnz, 0, (P->nrows + 1) * sizeof(int32_t), st));
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(P->nrows, kWarpsPerBlock),
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(P->nrows, rwarps),
                                                               (int64_t)num_sms() * 16));
   if (P->nrows > 0) {
-    row_nnz_kernel<<<grid, 32 * kWarpsPerBlock, smem, st>>>(P->inc_ptr, P->inc, udofs, local,
+    row_nnz_kernel<<<grid, 32 * rwarps, smem, st>>>(P->inc_ptr, P->inc, udofs, local,
                                                            P->nrows, P->nelems, nv, nu, cap,
                                                            row_nnz, flags);
     FEM_LAUNCH_CHECK("row_nnz_kernel");
@@ -1256,7 +1278,7 @@ int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, 
   FEM_TRY_CUDA(cudaMallocAsync(&P->indices, std::max<int64_t>(1, nnz) * sizeof(int32_t), st));
   FEM_TRY_CUDA(cudaMallocAsync(&P->slot, std::max<int64_t>(1, P->ninc * nu) * sizeof(uint16_t), st));
   if (P->nrows > 0) {
-    row_fill_kernel<<<grid, 32 * kWarpsPerBlock, smem, st>>>(P->inc_ptr, P->inc, udofs, local,
+    row_fill_kernel<<<grid, 32 * rwarps, smem, st>>>(P->inc_ptr, P->inc, udofs, local,
                                                             P->nrows, P->nelems, nv, nu, cap,
                                                             P->indptr, P->indices, P->slot);
     FEM_LAUNCH_CHECK("row_fill_kernel");
@@ -1278,12 +1300,14 @@ int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st
   if (row1 <= row0 || (P.nnz == 0 && !check_status)) return 0;
   const int nu = P.nbfun_u;
   const int stride = std::max(1, P.max_row_nnz);
-  const int threads = 128;
-  const int warps = threads / 32;
   int rc = 0;
   auto launch = [&](auto kern, int G) -> int {
     const int rpw = 32 / G;
-    const size_t smem = (size_t)warps * rpw * stride * (sizeof(double) + (check_status ? 1 : 0));
+    const size_t per_warp = (size_t)rpw * stride * (sizeof(double) + (check_status ? 1 : 0));
+    const int warps = smem_block_warps(per_warp);
+    if (!warps) return row_smem_error(stride);
+    const int threads = 32 * warps;
+    const size_t smem = warps * per_warp;
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return check_cuda(e, "csr_sum smem");
@@ -1322,7 +1346,11 @@ int csr_sum(const Pattern& P, const double* local, double* vals, cudaStream_t st
     const unsigned long long magic = ~0ull / (unsigned long long)nu + 1ull;
     auto launch_sym = [&](auto kern, int G) -> int {
       const int rpw = 32 / G;
-      const size_t smem = (size_t)warps * rpw * stride * sizeof(double);
+      const size_t per_warp = (size_t)rpw * stride * sizeof(double);
+      const int warps = smem_block_warps(per_warp);
+      if (!warps) return row_smem_error(stride);
+      const int threads = 32 * warps;
+      const size_t smem = warps * per_warp;
       if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return check_cuda(e, "csr_sum smem");
@@ -1382,11 +1410,13 @@ int csr_sum_scaled(const Pattern& P, const double* stiff, const FemCoef& diff,
   const double* field = diff.field;
   const int64_t fstride = diff.stride > 1 ? diff.stride : 1;
   const int stride = std::max(1, P.max_row_nnz);
-  const int threads = 128;
-  const int warps = threads / 32;
   auto launch = [&](auto kern, int G) -> int {
     const int rpw = 32 / G;
-    const size_t smem = (size_t)warps * rpw * stride * sizeof(double);
+    const size_t per_warp = (size_t)rpw * stride * sizeof(double);
+    const int warps = smem_block_warps(per_warp);
+    if (!warps) return row_smem_error(stride);
+    const int threads = 32 * warps;
+    const size_t smem = warps * per_warp;
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return check_cuda(e, "csr_scaled smem");
@@ -1415,7 +1445,11 @@ int csr_sum_scaled(const Pattern& P, const double* stiff, const FemCoef& diff,
       kern = U >= 8 ? csr_scaled_pair_kernel<10, 8> : csr_scaled_pair_kernel<10, 4>;
       rpw = 6;
     }
-    const size_t smem = (size_t)warps * rpw * stride * sizeof(double);
+    const size_t per_warp = (size_t)rpw * stride * sizeof(double);
+    const int warps = smem_block_warps(per_warp);
+    if (!warps) return row_smem_error(stride);
+    const int threads = 32 * warps;
+    const size_t smem = warps * per_warp;
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return check_cuda(e, "csr_scaled smem");
@@ -1508,10 +1542,12 @@ int csr_sum_geometry_p1(const Pattern& P, int dim, const double* geo, const FemC
   // off-diagonal P1 mass per unit |det|: 1/((d+1)(d+2) d!) -- 1/120 (tet), 1/24 (tri)
   const double moff = dim == 3 ? 0.05 * (1.0 / 6.0) : (1.0 / 12.0) * 0.5;
   const int stride = std::max(1, P.max_row_nnz);
-  const int threads = 128;
-  const int warps = threads / 32;
   const int rpw = 16;
-  const size_t smem = (size_t)warps * rpw * stride * (sizeof(double) + 8);
+  const size_t per_warp = (size_t)rpw * stride * (sizeof(double) + 8);
+  const int warps = smem_block_warps(per_warp);
+  if (!warps) return row_smem_error(stride);
+  const int threads = 32 * warps;
+  const size_t smem = warps * per_warp;
   const int64_t rows_per_block = (int64_t)warps * rpw;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(row1 - row0, rows_per_block),
                                                               (int64_t)num_sms() * 64));
