@@ -60,6 +60,10 @@ CHECK_B_PER_CELL = 9.0
 LOCAL_B_PER_CELL = 233.0
 SUM_B_PER_CELL = 193.9
 FUSED_B_PER_CELL = 218.5
+# FP64 operations per cell of the one-pass vector TetP2 elasticity: the pair
+# blocks (geometry ~70, E ~250) and the node blocks' reference-tensor terms
+# (1,194 FMAs for the 55 blocks on and above the block diagonal)
+VEC_TETP2_FP64_PER_CELL = 70 + 250 + 1194
 TRAFFIC_SOURCE = "ncu dram__bytes_read+write of one launch on the 1.3M-cell case, per cell"
 
 
@@ -538,17 +542,35 @@ def secondary_workloads(args, only=None):
         step, entry, c_form, vals = _abi_step(F, N, form, b, {})
         torch.cuda.synchronize()
         build_s = time.perf_counter() - t0
-        ms = _time(step, 3)
+        ms = _time(step, 5)
+        first = vals.clone()
+        step()
+        torch.cuda.synchronize()
+        same = bool(torch.equal(first, vals))
         lib = N.lib()
-        # the local kernel as the assembly runs it (the pattern's staging layout)
-        ms_local = _time(lambda: N.check(lib.fem_assemble_local(
-            N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form), entry.pat.handle,
-            N.ptr(entry.staging), None, 0, b.nelems, N.stream_ptr())), 3)
+        # the two-pass path for comparison: local matrices into the staging
+        # (block-upper layout), then the fixed-order segmented sum
+        fam = N.FAMILY["TetP2"]
+        lib.fem_set_onepass(fam, 0)
+        try:
+            ms_two = _time(step, 3)
+            dev = float(((vals - first).abs().max() / first.abs().max()).item())
+            ms_local = _time(lambda: N.check(lib.fem_assemble_local(
+                N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form), entry.pat.handle,
+                N.ptr(entry.staging), None, 0, b.nelems, N.stream_ptr())), 3)
+        finally:
+            lib.fem_set_onepass(fam, 1)
         B = m.nelements * (10 * 4) + m.p.size * 8 + entry.nnz * 8
         out["tet_p2_vec_elasticity_%d" % (n + 1)] = {
-            "nelems": m.nelements, "ndofs": b.N, "nnz": entry.nnz, "ms": ms, "ms_local": ms_local,
+            "nelems": m.nelements, "ndofs": b.N, "nnz": entry.nnz, "ms": ms,
+            "step": "one-pass vector sum: the cells' pair blocks, then one lane per node block "
+                    "contracting the reference tensor while it sums (no local matrices stored)",
+            "repeat_bitwise_equal": same,
+            "ms_two_pass": ms_two, "ms_two_pass_local": ms_local,
+            "two_pass_vs_onepass_max_rel": dev,
             "pattern_build_s": build_s, "elements_per_s": m.nelements / (ms * 1e-3),
-            "hbm_frac": B / (ms * 1e-3) / 1e9 / hbm, "algorithmic_bytes": B}
+            "hbm_frac": B / (ms * 1e-3) / 1e9 / hbm, "algorithmic_bytes": B,
+            "fp64_floor_ms": m.nelements * VEC_TETP2_FP64_PER_CELL / 0.598e12 * 1e3}
         del step, entry, vals, b
         torch.cuda.empty_cache()
 

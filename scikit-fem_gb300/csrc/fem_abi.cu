@@ -27,6 +27,10 @@ int coef_checks(const FemBilinear& f, const uint8_t* ref_bits, int32_t* status, 
                 int64_t ebeg, int64_t eend, const int32_t* cells);
 int local_vectors(const FemMesh&, const FemBasis&, const FemLinear&, double*, int32_t*,
                   cudaStream_t);
+// the vector channel forms' per-cell pair blocks (fem::vec_pair_stride doubles per
+// cell) of the cells [ebeg, eend) (of the list cells, when given)
+int vector_pair_blocks(const FemMesh&, const FemBasis&, const FemBilinear&, double*, cudaStream_t,
+                       int64_t ebeg = 0, int64_t eend = -1, const int32_t* cells = nullptr);
 }  // namespace fem_fast
 namespace fem_exact {
 int local_matrices(const FemMesh&, const FemBasis&, const FemBilinear&, double*, int32_t*,
@@ -34,12 +38,7 @@ int local_matrices(const FemMesh&, const FemBasis&, const FemBilinear&, double*,
 }  // namespace fem_exact
 
 namespace fem {
-int build_incidence(const int32_t* dofs, int64_t nelems, int nb, int64_t nrows, Pattern* P,
-                    cudaStream_t st);
-int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, Pattern* P,
-              cudaStream_t st);
 int vector_sum(const Pattern& P, const double* local, double* b, cudaStream_t st);
-void free_pattern(Pattern* P);
 int program_eval(int mode, const FemMesh& m, const FemBasis& b, const FemFacets* fc,
                  const FemProgram& prog, double* out, int32_t* status, cudaStream_t st,
                  const FemBasis* bu);
@@ -152,6 +151,10 @@ struct FemPattern {
   // first geometry cache of a scalar TriP1 / TetP1 pattern).
   fem::UpperLists upper;
   bool upper_ok = false, upper_tried = false;
+  // The one-pass vector sum's node-block lists (simplex ElementVector bases;
+  // pattern-only, built with the first fem_pattern_cache_geometry call).
+  fem::VecUpper vec;
+  bool vec_ok = false, vec_tried = false;
 };
 
 namespace {
@@ -180,6 +183,15 @@ bool geometry_sum(const FemPattern* pat, const FemMesh* mesh, const FemBasis* ba
   if (basis->family != FEM_TRI_P1 && basis->family != FEM_TET_P1) return false;
   if (pat->P.nbfun_u != pat->P.nbfun_v) return false;
   return form->mass.field ? true : (pat->mbase && pat->mbase_ok);
+}
+
+// The one-pass vector sum applies: simplex ElementVector bases whose
+// pattern holds its lists, unless the family's tuning selects the two-pass
+// path (fem_set_onepass variant 0).
+bool vector_onepass(const FemPattern* pat, const FemMesh* mesh, const FemBasis* basis) {
+  if (!basis->vector || !pat->vec_ok || pat->vec.dim != mesh->dim) return false;
+  if (pat->P.nbfun_u != pat->P.nbfun_v || pat->P.nbfun_v != basis->nbfun) return false;
+  return fem::tuning_for(basis->family).onepass >= 1;
 }
 
 bool fused_sum(const FemPattern* pat, const FemMesh* mesh, const FemBasis* basis,
@@ -567,6 +579,7 @@ void fem_pattern_destroy(FemPattern* pat) {
   cudaFree(pat->geo);
   cudaFree(pat->mbase);
   fem::free_upper_lists(&pat->upper);
+  fem::free_vec_upper(&pat->vec);
   drop_fused(pat);
   delete pat;
 }
@@ -579,9 +592,26 @@ int fem_pattern_cache_geometry(FemPattern* pat, const FemMesh* mesh, const FemBa
     set_error(FEM_ERR_ARGUMENT, "pattern does not belong to this mesh / basis");
     return FEM_ERR_ARGUMENT;
   }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (basis->vector && !pat->vec_tried) {
+    // the one-pass vector sum's lists (pattern-only): an optimisation, left
+    // out (with its error cleared) when the pattern does not allow it or
+    // there is no room for them
+    pat->vec_tried = true;
+    pat->vec_ok = false;
+    const int fam = basis->family;
+    if ((fam == FEM_TRI_P1 || fam == FEM_TRI_P2 || fam == FEM_TET_P1 || fam == FEM_TET_P2) &&
+        fem::basis_dim(fam) == mesh->dim) {
+      rc = fem::build_vec_upper(pat->P, basis->element_dofs, fam, mesh->dim, &pat->vec, st);
+      pat->vec_ok = rc == 0;
+      if (rc) {
+        cudaGetLastError();
+        fem::set_error(FEM_OK, "");
+      }
+    }
+  }
   const int ng = fem_fast::geometry_count(*mesh, *basis);
   if (ng == 0) return 0;  // families without a cache compute their geometry per call
-  cudaStream_t st = (cudaStream_t)stream;
   if (!pat->geo) {
     cudaError_t e = cudaMalloc(&pat->geo, std::max<int64_t>(1, mesh->nelems) * ng * sizeof(double));
     if (e == cudaErrorMemoryAllocation) {
@@ -681,6 +711,16 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
     return fem::csr_sum_geometry_p1(P, mesh->dim, pat->geo, form->diff, form->mass, pat->mbase,
                                     csr_values, st);
   }
+  if (vector_onepass(pat, mesh, basis)) {
+    // the coefficient checks, the cells' pair blocks (in the staging), then
+    // the one-pass vector sum contracting and summing the node blocks
+    rc = fem_fast::coef_checks(*form, pat->coef_bits, status, st, 0, mesh->nelems, nullptr);
+    if (rc) return rc;
+    rc = fem_fast::vector_pair_blocks(*mesh, *basis, *form, staging, st);
+    if (rc) return rc;
+    const bool mass = form->mass.field || form->mass.scale != 0.0;
+    return fem::vec_upper_sum(pat->vec, staging, mass, csr_values, st);
+  }
   // the local kernel also compares each element's coefficient zero bits
   // with the pattern's (FEM_ERR_STALE_PATTERN)
   rc = fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
@@ -751,11 +791,19 @@ struct GeometrySum {
   bool tma;                        // stage the upper lists' codes with TMA
 };
 
+// The one-pass vector sum's inputs for sum_rows_to_host (its pair blocks
+// are in the staging).
+struct VecSum {
+  const fem::VecUpper* vec;
+  bool mass;
+};
+
 int sum_rows_to_host(const fem::Pattern& P, const std::vector<int32_t>& ip, const double* staging,
                      double* csr_values, double* host_values, int64_t row0, int64_t row1,
                      cudaStream_t st, cudaStream_t cs, const FusedSum* fs = nullptr,
-                     const GeometrySum* gs = nullptr) {
-  int rc = fs ? fem::csr_sum_scaled(P, fs->stiff, fs->diff, fs->mass1, fs->mscale, csr_values, st,
+                     const GeometrySum* gs = nullptr, const VecSum* vs = nullptr) {
+  int rc = vs ? fem::vec_upper_sum(*vs->vec, staging, vs->mass, csr_values, st, row0, row1)
+           : fs ? fem::csr_sum_scaled(P, fs->stiff, fs->diff, fs->mass1, fs->mscale, csr_values, st,
                                     row0, row1)
            : gs ? (gs->upper ? fem::csr_sum_upper_p1(P, *gs->upper, gs->dim, gs->geo, gs->diff,
                                                       gs->mass, gs->mbase, csr_values, st, row0,
@@ -1066,6 +1114,8 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
                  (tune.onepass >= 1 && pat->upper_ok) ? &pat->upper : nullptr, status,
                  tune.onepass == 2};
   const bool onepass = !fused && geometry_sum(pat, mesh, basis, form);
+  const bool vec1 = !fused && !onepass && vector_onepass(pat, mesh, basis);
+  const VecSum vs{&pat->vec, form->mass.field || form->mass.scale != 0.0};
   std::vector<cudaEvent_t> evs;
   auto event = [&](cudaEvent_t* ev) -> cudaError_t {
     cudaError_t e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
@@ -1113,13 +1163,16 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
       }
     }
     if (cb[c + 1] > cb[c]) {
-      rc = (fused || onepass)
+      rc = (fused || onepass || vec1)
                ? fem_fast::coef_checks(*form, pat->coef_bits, status, st, cb[c], cb[c + 1], cells)
                : fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
                                                     status ? pat->coef_bits : nullptr, status, st,
                                                     cb[c], cb[c + 1], cells,
                                                     pat->P.staging_sym > 0,
                                                     cached_geometry(pat, mesh));
+      if (!rc && vec1)
+        rc = fem_fast::vector_pair_blocks(*mesh, *basis, *form, staging, st, cb[c], cb[c + 1],
+                                          cells);
       if (rc) {
         release();
         return rc;
@@ -1129,7 +1182,8 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
     const int64_t row1 = done[c];
     if (row1 > row) {
       rc = sum_rows_to_host(P, pat->host_indptr, staging, csr_values, host_values, row, row1, st,
-                            cs, fused ? &fs : nullptr, onepass ? &gs : nullptr);
+                            cs, fused ? &fs : nullptr, onepass ? &gs : nullptr,
+                            vec1 ? &vs : nullptr);
       if (rc) {
         release();
         return rc;

@@ -225,10 +225,13 @@ struct UpperLists {
   int32_t* row = nullptr;       // nupper: i
   int32_t* slice_len = nullptr;   // nslices
   int32_t* slice_base = nullptr;  // nslices: first code row (32 codes) of the slice
-  uint32_t* codes = nullptr;    // ncodes: e * 16 + li * 4 + lj, 0xFFFFFFFF padding
+  // ncodes, 0xFFFFFFFF padding: e * 16 + li * 4 + lj (at most 4 local
+  // functions, narrow codes), or e * 128 + li * nu + lj (wide codes, nu <= 11)
+  uint32_t* codes = nullptr;
   std::vector<int32_t> dpos_h, opos_h;
 };
-int build_upper_lists(const Pattern& P, UpperLists* U, cudaStream_t st);
+// wide: codes e * 128 + li * nu + lj whatever nu (always for nu > 4)
+int build_upper_lists(const Pattern& P, UpperLists* U, cudaStream_t st, bool wide = false);
 void free_upper_lists(UpperLists* U);
 // tma: stage each warp's slice codes in shared memory with bulk copies
 // (needs status for its bounded waits' error bit)
@@ -239,5 +242,41 @@ int csr_sum_upper_p1(const Pattern& P, const UpperLists& U, int dim, const doubl
 
 int basis_nb_scalar(int family);
 int basis_dim(int family);
+
+int build_incidence(const int32_t* dofs, int64_t nelems, int nb, int64_t nrows, Pattern* P,
+                    cudaStream_t st);
+// local == nullptr: every (row, column) pair of a cell is an entry
+int build_csr(const int32_t* udofs, int nu, int64_t ncols, const double* local, Pattern* P,
+              cudaStream_t st);
+void free_pattern(Pattern* P);
+
+// One-pass sum of the vector channel forms on simplex ElementVector bases
+// (fem_vecsum.cu): per node block (I, J), I <= J, its contribution list (the
+// node-level pattern's upper lists, codes e * 128 + i * ns + j) and the
+// vector CSR positions and presence mask of its entries.
+struct VecUpper {
+  int dim = 0, ns = 0;
+  int64_t nelems = 0;
+  UpperLists U;                 // pos / tpos / row released after the build
+  int32_t* vpos = nullptr;      // dim * nupper: rows D*I + a, first entry of the block
+  int32_t* vposT = nullptr;     // dim * nupper: rows D*J + b (transposed block; -1 if I == J)
+  uint16_t* vmask = nullptr;    // nupper: bit a*D + b, entry (D*I + a, D*J + b) present
+  void* terms = nullptr;        // reference-tensor terms per local node pair
+  int32_t* count = nullptr;
+  double* mm = nullptr;         // mass table per local node pair
+};
+int build_vec_upper(const Pattern& P, const int32_t* udofs, int family, int dim, VecUpper* V,
+                    cudaStream_t st);
+void free_vec_upper(VecUpper* V);
+// doubles per cell of the pair blocks the sum reads (vector_pair_blocks)
+inline int64_t vec_pair_stride(int dim) {
+  const int np = (dim + 1) * (dim + 2) / 2;
+  return (int64_t)np * dim * dim + 1;
+}
+// DOF rows [row0, row1) (multiples of dim; row1 < 0: to the last row): the
+// node blocks of their node rows, which also complete the rows' entries
+// left of the diagonal (written by earlier node rows' blocks)
+int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, cudaStream_t st,
+                  int64_t row0 = 0, int64_t row1 = -1);
 
 }  // namespace fem

@@ -455,6 +455,59 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
   fem::publish_status(status, flags);
 }
 
+// Per-cell pair blocks of the vector channel forms, the inputs of the
+// one-pass vector sum (fem_vecsum.cu): for the vertex pairs p <= q in
+// row-major upper order k, out[e * R + k * D * D + a * D + b] = E_pq[a][b]
+// (simplex_vector_kernel's expression), and out[e * R + NP * D * D] the
+// mass scale m_e |det| / d!.  R = NP * D * D + 1, NP = (D + 1)(D + 2) / 2.
+// Cells: positions [ebeg, eend) of the list `cells` (null: the cells
+// themselves), each written at its own cell's row.
+template <int D, int BS>
+__global__ void __launch_bounds__(BS) vector_pair_blocks_kernel(FemMesh m, FemBilinear f,
+                                                                double* __restrict__ out,
+                                                                const int32_t* __restrict__ cells,
+                                                                int64_t ebeg, int64_t eend) {
+  constexpr int NV = D + 1;
+  constexpr int NP = NV * (NV + 1) / 2;
+  constexpr int R = NP * D * D + 1;
+  constexpr double FACT = D == 3 ? 6.0 : 2.0;
+  extern __shared__ double smem[];
+  int64_t* cid = cells ? reinterpret_cast<int64_t*>(smem + (size_t)BS * (R + 1)) : nullptr;
+  const int64_t e0 = ebeg + (int64_t)blockIdx.x * BS;
+  const int64_t pos = e0 + threadIdx.x;
+  if (pos < eend) {
+    const int64_t e = cell_at(cells, pos);
+    if (cid) cid[threadIdx.x] = e;
+    Simplex<D> s;
+    simplex_geometry<D>(m, e, s);
+    simplex_c0<D>(s);
+    const double adet = fem::abs_bits(s.det);
+    const double s0 = 1.0 / (FACT * adet);
+    const double lam = coef_at(f.lam, e) * s0;
+    const double lap = coef_at(f.lap, e) * s0;
+    const double tr = coef_at(f.tr, e) * s0;
+    double* row = smem + threadIdx.x * (R + 1);
+    int k = 0;
+#pragma unroll
+    for (int p = 0; p < NV; ++p)
+#pragma unroll
+      for (int q = p; q < NV; ++q) {
+        const double g = lap * dotc<D>(s.c[p], s.c[q]);
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+          for (int b = 0; b < D; ++b) {
+            double v = lam * (s.c[p][a] * s.c[q][b]) + tr * (s.c[p][b] * s.c[q][a]);
+            if (a == b) v = v + g;
+            row[k * D * D + a * D + b] = v;
+          }
+        ++k;
+      }
+    row[NP * D * D] = coef_at(f.mass, e) * (adet / FACT);
+  }
+  flush_rows<R, BS>(smem, out, e0, eend, cid);
+}
+
 // ----------------------------------------------------------- hexahedron Q1
 // Reference node k sits at corner c_hex_corner[k] (refdom.py:173-180);
 // phi_k = prod_ax f(c, x_ax) with f(1,t) = t, f(0,t) = 1 - t.
@@ -901,6 +954,33 @@ int coef_checks(const FemBilinear& f, const uint8_t* ref_bits, int32_t* status, 
   const int64_t grid = fem::ceil_div(eend - ebeg, 256);
   coef_fields_kernel<<<(unsigned)grid, 256, 0, st>>>(c, ref_bits, status, cells, ebeg, eend);
   FEM_LAUNCH_CHECK("coef_fields_kernel");
+  return 0;
+}
+
+int vector_pair_blocks(const FemMesh& m, const FemBasis& b, const FemBilinear& f, double* out,
+                       cudaStream_t st, int64_t ebeg, int64_t eend, const int32_t* cells) {
+  if (eend < 0) eend = m.nelems;
+  if (eend <= ebeg) return 0;
+  constexpr int BS = 64;
+  const unsigned grid = (unsigned)fem::ceil_div(eend - ebeg, BS);
+  const size_t cid = cells ? kCidBytes<BS> : 0;
+  if (m.dim == 3) {
+    const size_t sm = (size_t)BS * (10 * 9 + 2) * sizeof(double) + cid;
+    if (sm > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(vector_pair_blocks_kernel<3, BS>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return fem::check_cuda(e, "vector_pair_blocks smem");
+    }
+    vector_pair_blocks_kernel<3, BS><<<grid, BS, sm, st>>>(m, f, out, cells, ebeg, eend);
+  } else if (m.dim == 2) {
+    const size_t sm = (size_t)BS * (6 * 4 + 2) * sizeof(double) + cid;
+    vector_pair_blocks_kernel<2, BS><<<grid, BS, sm, st>>>(m, f, out, cells, ebeg, eend);
+  } else {
+    fem::set_error(FEM_ERR_UNSUPPORTED, "vector pair blocks of a %d-D mesh", m.dim);
+    return FEM_ERR_UNSUPPORTED;
+  }
+  (void)b;
+  FEM_LAUNCH_CHECK("vector_pair_blocks_kernel");
   return 0;
 }
 

@@ -140,8 +140,8 @@ __device__ int row_columns(int64_t r, const int32_t* __restrict__ inc_ptr,
       const int32_t code = inc[b + q];
       const int64_t e = code / nv;
       const int64_t i = code - e * nv;
-      const double v = local[(e * nv + i) * nu + j];
-      if (v != 0.0) c = udofs[(int64_t)j * nelems + e];
+      // without local matrices every (row, column) pair is an entry
+      if (!local || local[(e * nv + i) * nu + j] != 0.0) c = udofs[(int64_t)j * nelems + e];
     }
     if (k < n) cand[k] = c;
     srt[k] = c;
@@ -968,7 +968,8 @@ __global__ void upper_codes_kernel(const int32_t* __restrict__ indptr,
                                    const int32_t* __restrict__ dpos,
                                    const int32_t* __restrict__ opos, int64_t nd,
                                    const int32_t* __restrict__ slice_base,
-                                   int32_t* __restrict__ cursor, uint32_t* __restrict__ codes) {
+                                   int32_t* __restrict__ cursor, uint32_t* __restrict__ codes,
+                                   bool wide) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nrows) return;
   const int32_t p0 = indptr[i], p1 = indptr[i + 1];
@@ -990,7 +991,8 @@ __global__ void upper_codes_kernel(const int32_t* __restrict__ indptr,
       if (sv == 0xFFFF || (int)sv < sd) continue;
       const int64_t u = ((int)sv == sd && d) ? (int64_t)dpos[i] : nd + opos[i] + ((int)sv - so);
       const int c = cursor[u]++;
-      codes[((int64_t)slice_base[u >> 5] + c) * 32 + (u & 31)] = (e << 4) | (li << 2) | (uint32_t)j;
+      codes[((int64_t)slice_base[u >> 5] + c) * 32 + (u & 31)] =
+          wide ? (e << 7) | (li * (uint32_t)nu + (uint32_t)j) : (e << 4) | (li << 2) | (uint32_t)j;
     }
   }
 }
@@ -1579,16 +1581,18 @@ int csr_sum_geometry_p1(const Pattern& P, int dim, const double* geo, const FemC
 }
 
 
-int build_upper_lists(const Pattern& P, UpperLists* U, cudaStream_t st) {
+int build_upper_lists(const Pattern& P, UpperLists* U, cudaStream_t st, bool wide) {
   *U = UpperLists();
   const int nu = P.nbfun_u;
-  if (!P.has_matrix || P.nbfun_v != nu || nu > 4) {
-    set_error(FEM_ERR_ARGUMENT, "upper lists need a square pattern of at most 4 local functions");
+  wide = wide || nu > 4;
+  if (!P.has_matrix || P.nbfun_v != nu || nu > 11) {
+    set_error(FEM_ERR_ARGUMENT, "upper lists need a square pattern of at most 11 local functions");
     return FEM_ERR_ARGUMENT;
   }
-  if (P.nelems >= ((int64_t)1 << 28)) {
-    set_error(FEM_ERR_CAPACITY, "%lld cells exceed the upper lists' 28-bit cell codes",
-              (long long)P.nelems);
+  const int cell_bits = wide ? 25 : 28;
+  if (P.nelems >= ((int64_t)1 << cell_bits)) {
+    set_error(FEM_ERR_CAPACITY, "%lld cells exceed the upper lists' %d-bit cell codes",
+              (long long)P.nelems, cell_bits);
     return FEM_ERR_CAPACITY;
   }
   const int64_t n = P.nrows;
@@ -1674,7 +1678,7 @@ int build_upper_lists(const Pattern& P, UpperLists* U, cudaStream_t st) {
   if (n > 0) {
     upper_codes_kernel<<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(
         P.indptr, P.indices, P.inc_ptr, P.inc, P.slot, nu, n, U->dpos, U->opos, U->nd,
-        U->slice_base, cnt, U->codes);
+        U->slice_base, cnt, U->codes, wide);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(check_cuda(e, "upper_codes_kernel"));
   }

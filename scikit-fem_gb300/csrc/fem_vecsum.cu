@@ -1,0 +1,420 @@
+// One-pass assembly of the vector channel forms on simplex ElementVector
+// bases (vector TriP1/P2, TetP1/P2: linear elasticity and its relatives).
+//
+// The reference builds each cell's (D*NS)^2 local matrix, then sums the COO
+// triplets (bilinear_form.py:130-148, coo_data.py:27-36).  Here the local
+// matrices are never stored: their D x D node blocks are contracted while
+// the CSR entries are summed.
+//
+//   K_e[(i a)(j b)] = sum_{p,q} BB[i][j][p][q] E_pq[a][b]      (D x D block (i, j))
+//
+// with BB the element's exact reference tensor (fem_tables.cuh, at most 2 x 2
+// vertex pairs per node pair) and E_pq the cell's pair blocks, computed per
+// call from the coordinates and coefficients (vector_pair_blocks_kernel).
+//
+// Work unit: one node block (I, J), I <= J, of the CSR (DOF D*node + a, the
+// reference's interleaved numbering).  A lane owns a block, walks its
+// contribution list -- the cells holding both nodes, ascending, each with
+// its local pair (i, j) -- and accumulates the D*D entries in registers in
+// that fixed order, then writes them to (I, J) and, transposed, to (J, I).
+// Entries that the reference's eliminate_zeros left out of the pattern are
+// skipped through the block's presence mask.  Lists are sliced 32 blocks at a
+// time (code p of lane l at codes[(base + p) * 32 + l]), as the scalar
+// one-pass sum's; they come from the upper lists of the node-level pattern.
+
+#include "fem_common.cuh"
+#include "fem_tables.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace fem {
+
+namespace {
+
+constexpr int kMaxTerms = 4;
+
+struct VecTerm {
+  int32_t k;    // pair index of (min(p,q), max(p,q)) in row-major upper order
+  int32_t tr;   // 1: the term reads E_qp transposed (p > q)
+  double c;
+};
+
+int pair_index(int nv, int p, int q) { return p * nv - p * (p - 1) / 2 + (q - p); }
+
+// terms[(i * ns + j) * kMaxTerms + t], count[i * ns + j]: the BB[i][j]
+// terms of the element's reference tensor; mm[i * ns + j] its mass table.
+int fill_terms(int family, int dim, std::vector<VecTerm>* terms, std::vector<int32_t>* count,
+               std::vector<double>* mm) {
+  const int ns = basis_nb_scalar(family);
+  const int nv = dim + 1;
+  terms->assign((size_t)ns * ns * kMaxTerms, VecTerm{0, 0, 0.0});
+  count->assign((size_t)ns * ns, 0);
+  mm->assign((size_t)ns * ns, 0.0);
+  bool over = false;
+  auto add = [&](int i, int j, int p, int q, double c) {
+    int& n = (*count)[i * ns + j];
+    if (n >= kMaxTerms) {
+      over = true;
+      return;
+    }
+    const bool tr = p > q;
+    (*terms)[(size_t)(i * ns + j) * kMaxTerms + n] =
+        VecTerm{pair_index(nv, tr ? q : p, tr ? p : q), tr ? 1 : 0, c};
+    ++n;
+  };
+  for (int i = 0; i < ns; ++i)
+    for (int j = 0; j < ns; ++j) {
+#define VT(p, q, c) add(i, j, (p), (q), (c));
+      if (family == FEM_TET_P2) {
+        switch (i) {
+          case 0: TET2BB_ROW0(j, VT) break;
+          case 1: TET2BB_ROW1(j, VT) break;
+          case 2: TET2BB_ROW2(j, VT) break;
+          case 3: TET2BB_ROW3(j, VT) break;
+          case 4: TET2BB_ROW4(j, VT) break;
+          case 5: TET2BB_ROW5(j, VT) break;
+          case 6: TET2BB_ROW6(j, VT) break;
+          case 7: TET2BB_ROW7(j, VT) break;
+          case 8: TET2BB_ROW8(j, VT) break;
+          case 9: TET2BB_ROW9(j, VT) break;
+          default: break;
+        }
+      } else if (family == FEM_TRI_P2) {
+        switch (i) {
+          case 0: TRI2BB_ROW0(j, VT) break;
+          case 1: TRI2BB_ROW1(j, VT) break;
+          case 2: TRI2BB_ROW2(j, VT) break;
+          case 3: TRI2BB_ROW3(j, VT) break;
+          case 4: TRI2BB_ROW4(j, VT) break;
+          case 5: TRI2BB_ROW5(j, VT) break;
+          default: break;
+        }
+      } else {
+        // P1: grad phi_i = grad lambda_i, BB[i][j][p][q] = delta_ip delta_jq
+        add(i, j, i, j, 1.0);
+      }
+#undef VT
+    }
+  if (over) {
+    set_error(FEM_ERR_UNSUPPORTED, "more than %d reference-tensor terms per node pair", kMaxTerms);
+    return FEM_ERR_UNSUPPORTED;
+  }
+  // the mass tables live in constant memory: read them back to the host
+  const void* sym = family == FEM_TET_P2 ? (const void*)&c_tet2_mm
+                    : family == FEM_TRI_P2 ? (const void*)&c_tri2_mm
+                    : family == FEM_TET_P1 ? (const void*)&c_tet1_mm
+                                           : (const void*)&c_tri1_mm;
+  FEM_TRY_CUDA(cudaMemcpyFromSymbol(mm->data(), sym, (size_t)ns * ns * sizeof(double)));
+  return 0;
+}
+
+// node[i][e] = element_dofs[D i][e] / D; *bad set when a cell's DOFs are not
+// D consecutive numbers D*node + a per scalar node (the interleaved layout)
+__global__ void node_dofs_kernel(const int32_t* __restrict__ udofs, int64_t nelems, int ns,
+                                 int dim, int32_t* __restrict__ node, int32_t* __restrict__ bad) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nelems * ns) return;
+  const int i = (int)(idx / nelems);
+  const int64_t e = idx - (int64_t)i * nelems;
+  const int32_t d0 = udofs[(int64_t)(dim * i) * nelems + e];
+  bool ok = d0 >= 0 && d0 % dim == 0;
+  for (int a = 1; a < dim; ++a) ok = ok && udofs[(int64_t)(dim * i + a) * nelems + e] == d0 + a;
+  if (!ok) atomicOr(bad, 1);
+  node[idx] = d0 / dim;
+}
+
+// first position of row r of the vector CSR with a column >= col
+__device__ __forceinline__ int32_t row_lower_bound(const int32_t* __restrict__ indptr,
+                                                   const int32_t* __restrict__ indices, int64_t r,
+                                                   int32_t col) {
+  int32_t lo = indptr[r], hi = indptr[r + 1];
+  while (lo < hi) {
+    const int32_t mid = (lo + hi) >> 1;
+    if (indices[mid] < col) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Per node block u = (I, J): the vector CSR position of each row's first
+// entry in the block (vpos[a][u], rows D*I + a) and of the transposed
+// block's (vposT[b][u], rows D*J + b; I < J), and the entries present
+// (bit a*D + b).  *asym when the transposed block's entries differ.
+__global__ void vec_block_pos_kernel(const int32_t* __restrict__ urow,
+                                     const int32_t* __restrict__ upos,
+                                     const int32_t* __restrict__ nindices, int64_t nupper,
+                                     int64_t nd, int dim, const int32_t* __restrict__ indptr,
+                                     const int32_t* __restrict__ indices,
+                                     int32_t* __restrict__ vpos, int32_t* __restrict__ vposT,
+                                     uint16_t* __restrict__ vmask, int32_t* __restrict__ asym) {
+  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nupper) return;
+  const int64_t I = urow[u];
+  const int64_t J = nindices[upos[u]];
+  unsigned mask = 0, maskT = 0;
+  for (int a = 0; a < dim; ++a) {
+    const int64_t r = dim * I + a;
+    int32_t p = row_lower_bound(indptr, indices, r, (int32_t)(dim * J));
+    vpos[a * nupper + u] = p;
+    const int32_t end = indptr[r + 1];
+    for (int b = 0; b < dim; ++b)
+      if (p < end && indices[p] == (int32_t)(dim * J + b)) {
+        mask |= 1u << (a * dim + b);
+        ++p;
+      }
+  }
+  if (u >= nd) {
+    for (int b = 0; b < dim; ++b) {
+      const int64_t r = dim * J + b;
+      int32_t p = row_lower_bound(indptr, indices, r, (int32_t)(dim * I));
+      vposT[b * nupper + u] = p;
+      const int32_t end = indptr[r + 1];
+      for (int a = 0; a < dim; ++a)
+        if (p < end && indices[p] == (int32_t)(dim * I + a)) {
+          maskT |= 1u << (a * dim + b);
+          ++p;
+        }
+    }
+    if (maskT != mask) atomicOr(asym, 1);
+  } else {
+    for (int b = 0; b < dim; ++b) vposT[b * nupper + u] = -1;
+  }
+  vmask[u] = (uint16_t)mask;
+}
+
+// The sum.  MASS: add m_e |det| / d! * MM[i][j] on the block diagonals.
+template <int D, bool MASS>
+__global__ void __launch_bounds__(128) vec_upper_kernel(
+    int64_t ua, int64_t ub, int64_t nupper, int64_t nd, int64_t nelems, int ns,
+    const int32_t* __restrict__ slice_len,
+    const int32_t* __restrict__ slice_base, const uint32_t* __restrict__ codes,
+    const int32_t* __restrict__ vpos, const int32_t* __restrict__ vposT,
+    const uint16_t* __restrict__ vmask, const VecTerm* __restrict__ terms_g,
+    const int32_t* __restrict__ count_g, const double* __restrict__ mm_g,
+    const double* __restrict__ E, double* __restrict__ vals) {
+  constexpr int DD = D * D;
+  constexpr int NP = (D + 1) * (D + 2) / 2;
+  constexpr int R = NP * DD + 1;
+  __shared__ VecTerm terms[100 * kMaxTerms];
+  __shared__ int32_t count[100];
+  __shared__ double mm[100];
+  const int npairs = ns * ns;
+  for (int k = threadIdx.x; k < npairs * kMaxTerms; k += blockDim.x) terms[k] = terms_g[k];
+  for (int k = threadIdx.x; k < npairs; k += blockDim.x) {
+    count[k] = count_g[k];
+    mm[k] = mm_g[k];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t s1 = (ub + 31) >> 5;
+  for (int64_t sl = (ua >> 5) + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+       sl < s1; sl += warps) {
+    const int64_t u = sl * 32 + lane;
+    if (u < ua || u >= ub) continue;            // a block of the neighbouring range
+    const int len = slice_len[sl];
+    const uint32_t* cp = codes + (int64_t)slice_base[sl] * 32 + lane;
+    double acc[DD];
+#pragma unroll
+    for (int q = 0; q < DD; ++q) acc[q] = 0.0;
+    uint32_t next = len > 0 ? __ldg(cp) : 0xFFFFFFFFu;
+    for (int p = 0; p < len; ++p) {
+      const uint32_t code = next;
+      if (p + 1 < len) next = __ldg(cp + (int64_t)(p + 1) * 32);   // one code ahead
+      if (code == 0xFFFFFFFFu) continue;                            // this lane's list ended
+      const int64_t e = code >> 7;
+      const int ij = (int)(code & 127u);
+      if (e >= nelems || ij >= npairs) continue;   // never for the lists this file builds
+      const double* Eb = E + e * R;
+      const int nt = count[ij];
+      for (int t = 0; t < nt; ++t) {
+        const VecTerm tm = terms[ij * kMaxTerms + t];
+        const double* Ep = Eb + tm.k * DD;
+        double v[DD];
+#pragma unroll
+        for (int q = 0; q < DD; ++q) v[q] = __ldg(Ep + q);
+        if (tm.tr) {
+#pragma unroll
+          for (int a = 0; a < D; ++a)
+#pragma unroll
+            for (int b = a + 1; b < D; ++b) {
+              const double x = v[a * D + b];
+              v[a * D + b] = v[b * D + a];
+              v[b * D + a] = x;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < DD; ++q) acc[q] = __fma_rn(tm.c, v[q], acc[q]);
+      }
+      if (MASS) {
+        const double sm = __ldg(Eb + NP * DD);
+        const double mv = mm[ij];
+#pragma unroll
+        for (int a = 0; a < D; ++a) acc[a * D + a] = __fma_rn(sm, mv, acc[a * D + a]);
+      }
+    }
+    {
+      const unsigned mk = vmask[u];
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        int32_t pos = vpos[a * nupper + u];
+#pragma unroll
+        for (int b = 0; b < D; ++b)
+          if ((mk >> (a * D + b)) & 1u) vals[pos++] = acc[a * D + b];
+      }
+      if (u >= nd) {
+#pragma unroll
+        for (int b = 0; b < D; ++b) {
+          int32_t pos = vposT[b * nupper + u];
+#pragma unroll
+          for (int a = 0; a < D; ++a)
+            if ((mk >> (a * D + b)) & 1u) vals[pos++] = acc[a * D + b];
+        }
+      }
+    }
+  }
+}
+
+}  // namespace
+
+void free_vec_upper(VecUpper* V) {
+  if (!V) return;
+  free_upper_lists(&V->U);
+  cudaFree(V->vpos);
+  cudaFree(V->vposT);
+  cudaFree(V->vmask);
+  cudaFree(V->terms);
+  cudaFree(V->count);
+  cudaFree(V->mm);
+  *V = VecUpper();
+}
+
+int build_vec_upper(const Pattern& P, const int32_t* udofs, int family, int dim, VecUpper* V,
+                    cudaStream_t st) {
+  *V = VecUpper();
+  const int ns = basis_nb_scalar(family);
+  if ((dim != 2 && dim != 3) || ns <= 0 || ns > 10 || basis_dim(family) != dim ||
+      P.nbfun_u != dim * ns || P.nbfun_v != dim * ns || !P.has_matrix || P.nrows % dim) {
+    set_error(FEM_ERR_UNSUPPORTED, "one-pass vector sum: not a vector simplex pattern");
+    return FEM_ERR_UNSUPPORTED;
+  }
+  V->dim = dim;
+  V->ns = ns;
+  V->nelems = P.nelems;
+  const int64_t nelems = P.nelems, nnodes = P.nrows / dim;
+  std::vector<VecTerm> terms;
+  std::vector<int32_t> count;
+  std::vector<double> mm;
+  int rc = fill_terms(family, dim, &terms, &count, &mm);
+  if (rc) return rc;
+  auto fail = [&](int code) {
+    free_vec_upper(V);
+    return code;
+  };
+  // node-level pattern: every pair of nodes sharing a cell
+  Pattern N;
+  AsyncScratch scratch(st);
+  int32_t *node = nullptr, *flag = nullptr;
+  FEM_TRY_CUDA(scratch.alloc(&node, std::max<int64_t>(1, nelems * ns) * sizeof(int32_t)));
+  FEM_TRY_CUDA(scratch.alloc(&flag, sizeof(int32_t)));
+  FEM_TRY_CUDA(cudaMemsetAsync(flag, 0, sizeof(int32_t), st));
+  if (nelems > 0) {
+    node_dofs_kernel<<<(unsigned)ceil_div(nelems * ns, 256), 256, 0, st>>>(udofs, nelems, ns, dim,
+                                                                           node, flag);
+    FEM_LAUNCH_CHECK("node_dofs_kernel");
+  }
+  int32_t h = 0;
+  FEM_TRY_CUDA(cudaMemcpyAsync(&h, flag, sizeof(h), cudaMemcpyDeviceToHost, st));
+  FEM_TRY_CUDA(cudaStreamSynchronize(st));
+  if (h) {
+    set_error(FEM_ERR_UNSUPPORTED, "one-pass vector sum: DOFs are not interleaved by node");
+    return FEM_ERR_UNSUPPORTED;
+  }
+  rc = build_incidence(node, nelems, ns, nnodes, &N, st);
+  if (!rc) rc = build_csr(node, ns, nnodes, nullptr, &N, st);
+  if (!rc) rc = build_upper_lists(N, &V->U, st, /*wide=*/true);
+  if (rc) {
+    free_pattern(new Pattern(N));   // releases N's device arrays
+    return fail(rc);
+  }
+  const int64_t nu = V->U.nupper;
+  cudaError_t e = cudaMalloc(&V->vpos, std::max<int64_t>(1, nu * dim) * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&V->vposT, std::max<int64_t>(1, nu * dim) * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&V->vmask, std::max<int64_t>(1, nu) * sizeof(uint16_t));
+  if (e == cudaSuccess) e = cudaMalloc(&V->terms, terms.size() * sizeof(VecTerm));
+  if (e == cudaSuccess) e = cudaMalloc(&V->count, count.size() * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&V->mm, mm.size() * sizeof(double));
+  if (e != cudaSuccess) {
+    free_pattern(new Pattern(N));   // releases N's device arrays
+    return fail(check_cuda(e, "cudaMalloc(vector one-pass lists)"));
+  }
+  e = cudaMemcpyAsync(V->terms, terms.data(), terms.size() * sizeof(VecTerm),
+                      cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(V->count, count.data(), count.size() * sizeof(int32_t),
+                        cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(V->mm, mm.data(), mm.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(flag, 0, sizeof(int32_t), st);
+  if (e == cudaSuccess && nu > 0) {
+    vec_block_pos_kernel<<<(unsigned)ceil_div(nu, 256), 256, 0, st>>>(
+        V->U.row, V->U.pos, N.indices, nu, V->U.nd, dim, P.indptr, P.indices, V->vpos, V->vposT,
+        V->vmask, flag);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, flag, sizeof(h), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  free_pattern(new Pattern(N));   // releases N's device arrays
+  if (e != cudaSuccess) return fail(check_cuda(e, "vec_block_pos_kernel"));
+  if (h) {
+    set_error(FEM_ERR_UNSUPPORTED, "one-pass vector sum: the CSR pattern is not block-symmetric");
+    return fail(FEM_ERR_UNSUPPORTED);
+  }
+  // the node-level CSR positions, rows and transposes are build-time only
+  cudaFree(V->U.pos);
+  cudaFree(V->U.tpos);
+  cudaFree(V->U.row);
+  V->U.pos = V->U.tpos = V->U.row = nullptr;
+  return 0;
+}
+
+int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, cudaStream_t st,
+                  int64_t row0, int64_t row1) {
+  if (V.U.nupper == 0) return 0;
+  const int64_t nnodes = (int64_t)V.U.dpos_h.size() - 1;
+  // node rows [n0, n1) of DOF rows [row0, row1) (multiples of dim)
+  int64_t n0 = row0 < 0 ? 0 : row0 / V.dim;
+  int64_t n1 = (row1 < 0 || row1 / V.dim > nnodes) ? nnodes : row1 / V.dim;
+  if (n1 <= n0) return 0;
+  const bool all = n0 == 0 && n1 == nnodes;
+  // the node rows' diagonal blocks and their blocks above the diagonal
+  // (every node row: the two ranges are adjacent, one launch)
+  const int64_t ranges[2][2] = {
+      {all ? 0 : V.U.dpos_h[n0], all ? V.U.nupper : V.U.dpos_h[n1]},
+      {all ? 0 : V.U.nd + V.U.opos_h[n0], all ? 0 : V.U.nd + V.U.opos_h[n1]}};
+  const int threads = 128;
+  for (int k = 0; k < 2; ++k) {
+    const int64_t ua = ranges[k][0], ub = ranges[k][1];
+    if (ub <= ua) continue;
+    const int64_t nsl = ((ub + 31) >> 5) - (ua >> 5);
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nsl, threads / 32),
+                                                                (int64_t)num_sms() * 32));
+    auto launch = [&](auto kern) {
+      kern<<<grid, threads, 0, st>>>(ua, ub, V.U.nupper, V.U.nd, V.nelems, V.ns, V.U.slice_len,
+                                     V.U.slice_base, V.U.codes, V.vpos, V.vposT, V.vmask,
+                                     static_cast<const VecTerm*>(V.terms), V.count, V.mm, E, vals);
+    };
+    if (V.dim == 3) {
+      if (mass) launch(vec_upper_kernel<3, true>);
+      else launch(vec_upper_kernel<3, false>);
+    } else {
+      if (mass) launch(vec_upper_kernel<2, true>);
+      else launch(vec_upper_kernel<2, false>);
+    }
+    FEM_LAUNCH_CHECK("vec_upper_kernel");
+  }
+  return 0;
+}
+
+}  // namespace fem

@@ -28,6 +28,7 @@ UNITS = [
     ("fem_pattern.cu", "fem_pattern.o", []),
     ("fem_vjp.cu", "fem_vjp.o", []),
     ("fem_batched.cu", "fem_batched.o", []),
+    ("fem_vecsum.cu", "fem_vecsum.o", []),
     ("fem_abi.cu", "fem_abi.o", []),
     ("fem_noalloc.cu", "fem_noalloc.o", []),
     ("fem_faithful.cu", "fem_faithful.o", ["-fmad=false"]),

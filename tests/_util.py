@@ -47,3 +47,32 @@ def csr_diff(indptr, indices, data, gindptr, gindices, gdata, shape):
     rel_fro = sp.linalg.norm(D) / max(sp.linalg.norm(B), 1e-300)
     rel_max = (abs(D).max() if D.nnz else 0.0) / kmax
     return same, onlyA.nnz, onlyB.nnz, noise / kmax, rel_fro, rel_max
+
+
+def double_cone_arrays(n):
+    """(p, t) of a double cone: a ring of n vertices around the origin, an
+    apex above (z = 1) and below (z = -1.1); every tet (origin, ring_i,
+    ring_i+1, apex) holds the origin, which 2n cells share."""
+    ang = 2 * np.pi * np.arange(n) / n
+    ring = np.vstack((np.cos(ang), np.sin(ang), np.zeros(n)))
+    p = np.hstack((np.zeros((3, 1)), ring, [[0.0], [0.0], [1.0]], [[0.0], [0.0], [-1.1]]))
+    top, bot = n + 1, n + 2
+    t = []
+    for i in range(n):
+        a, b = 1 + i, 1 + (i + 1) % n
+        t.append((0, a, b, top))
+        t.append((0, a, b, bot))
+    return p, np.array(t, dtype=np.int64).T
+
+
+def fan_arrays(n):
+    """(p, t) of n triangles around the origin."""
+    ang = 2 * np.pi * np.arange(n) / n
+    p = np.hstack((np.zeros((2, 1)), np.vstack((np.cos(ang), np.sin(ang)))))
+    t = np.array([(0, 1 + i, 1 + (i + 1) % n) for i in range(n)], dtype=np.int64).T
+    return p, t
+
+
+def fan_coefficient(n):
+    """The per-cell k of the fan case (seeded)."""
+    return np.random.default_rng(3).lognormal(0.0, 1.0, n)

@@ -689,6 +689,40 @@ def config_cases():
     np.savez_compressed(os.path.join(OUT, "config_patterns.npz"), **out)
 
 
+def capacity_cases():
+    """Rows of high-valence DOFs at the pattern build's candidate limit:
+    vector TetP2 elasticity on the double cone of 273 ring vertices (546
+    cells share the origin) and TriP2 k*Laplace on a fan of 1,500 triangles,
+    run through scikit-fem -- nnz, digests of indptr / indices, Frobenius
+    norm and sum, as config_cases records them."""
+    sys.path.insert(0, os.path.dirname(OUT))
+    from _util import double_cone_arrays, fan_arrays, fan_coefficient
+
+    out = {}
+
+    def record(name, K):
+        # the whole pattern too: on these symmetric meshes the oracle's
+        # exact zeros differ from the reference's in a few noise entries
+        K = K.tocsr()
+        out[name + "__nnz"] = np.array(K.nnz)
+        out[name + "__indptr"] = _digest(K.indptr.astype(np.int32))
+        out[name + "__indices"] = _digest(K.indices.astype(np.int32))
+        out[name + "__fro"] = np.array(np.linalg.norm(K.data))
+        out[name + "__sum"] = np.array(K.data.sum())
+        out[name + "__pattern_indptr"] = K.indptr.astype(np.int32)
+        out[name + "__pattern_indices"] = K.indices.astype(np.int32)
+        print(name, K.nnz)
+
+    p, t = double_cone_arrays(273)
+    ib = Basis(MeshTet(p, t), ElementVector(ElementTetP2()))
+    record("cone_273_vec_tet_p2", linear_elasticity(1.0, 0.5).assemble(ib))
+    p, t = fan_arrays(1500)
+    ib = Basis(MeshTri(p, t), ElementTriP2())
+    k = fan_coefficient(t.shape[1])
+    record("fan_1500_tri_p2", k_laplace.assemble(ib, k=ib.zero_w() + k[:, None]))
+    np.savez_compressed(os.path.join(OUT, "capacity_patterns.npz"), **out)
+
+
 def coo_cases():
     """COOData / Form.elemental / Form.block / asm(to=...) results of
     scikit-fem (coo_data.py, form.py:53-89, assembly/__init__.py:69-97)."""
@@ -751,6 +785,8 @@ if __name__ == "__main__":
         coo_cases()
     elif sys.argv[1:] == ["--configs"]:
         config_cases()
+    elif sys.argv[1:] == ["--capacity"]:
+        capacity_cases()
     elif sys.argv[1:] == ["--quadrature"]:
         quadrature_rules()
     elif sys.argv[1:] == ["--doflocs"]:
