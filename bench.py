@@ -551,8 +551,13 @@ def secondary_workloads(args, only=None):
         # the two-pass path for comparison: local matrices into the staging
         # (block-upper layout), then the fixed-order segmented sum
         fam = N.FAMILY["TetP2"]
-        lib.fem_set_onepass(fam, 0)
         try:
+            # the one-pass sum's cooperative form (the D*D lanes of a node block
+            # together), bitwise the same values
+            lib.fem_set_onepass(fam, 2)
+            ms_coop = _time(step, 5)
+            coop_same = bool(torch.equal(first, vals))
+            lib.fem_set_onepass(fam, 0)
             ms_two = _time(step, 3)
             dev = float(((vals - first).abs().max() / first.abs().max()).item())
             ms_local = _time(lambda: N.check(lib.fem_assemble_local(
@@ -566,6 +571,7 @@ def secondary_workloads(args, only=None):
             "step": "one-pass vector sum: the cells' pair blocks, then one lane per node block "
                     "contracting the reference tensor while it sums (no local matrices stored)",
             "repeat_bitwise_equal": same,
+            "ms_onepass_coop": ms_coop, "coop_bitwise_equal": coop_same,
             "ms_two_pass": ms_two, "ms_two_pass_local": ms_local,
             "two_pass_vs_onepass_max_rel": dev,
             "pattern_build_s": build_s, "elements_per_s": m.nelements / (ms * 1e-3),

@@ -226,6 +226,14 @@ int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll, 
  * contributions in the same order: the values are the same bit for bit
  * (up to the fixed-point mass sums' truncation on meshes whose cells around
  * a vertex differ in size by more than a factor 8, a few ulps).
+ * For ElementVector bases of the same families (vector channel forms):
+ * 0 the two-pass path (local matrices into the staging, then the
+ * segmented sum); 1 (the default) the one-pass vector sum, one lane per
+ * D x D node block of the CSR accumulating its cells' reference-tensor
+ * terms from their pair blocks (computed into the staging first); 2 the
+ * same with the D*D lanes of a block cooperating on its entries.  Variants
+ * 1 and 2 are bitwise equal; the two-pass path agrees within 1e-14 of
+ * max|K|.
  */
 int fem_set_onepass(int family, int variant);
 

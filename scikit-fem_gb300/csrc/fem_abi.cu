@@ -719,7 +719,8 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
     rc = fem_fast::vector_pair_blocks(*mesh, *basis, *form, staging, st);
     if (rc) return rc;
     const bool mass = form->mass.field || form->mass.scale != 0.0;
-    return fem::vec_upper_sum(pat->vec, staging, mass, csr_values, st);
+    return fem::vec_upper_sum(pat->vec, staging, mass, csr_values, st, 0, -1,
+                              fem::tuning_for(basis->family).onepass == 2);
   }
   // the local kernel also compares each element's coefficient zero bits
   // with the pattern's (FEM_ERR_STALE_PATTERN)
@@ -796,13 +797,15 @@ struct GeometrySum {
 struct VecSum {
   const fem::VecUpper* vec;
   bool mass;
+  bool coop;   // the cooperative form (fem_set_onepass variant 2)
 };
 
 int sum_rows_to_host(const fem::Pattern& P, const std::vector<int32_t>& ip, const double* staging,
                      double* csr_values, double* host_values, int64_t row0, int64_t row1,
                      cudaStream_t st, cudaStream_t cs, const FusedSum* fs = nullptr,
                      const GeometrySum* gs = nullptr, const VecSum* vs = nullptr) {
-  int rc = vs ? fem::vec_upper_sum(*vs->vec, staging, vs->mass, csr_values, st, row0, row1)
+  int rc = vs ? fem::vec_upper_sum(*vs->vec, staging, vs->mass, csr_values, st, row0, row1,
+                                   vs->coop)
            : fs ? fem::csr_sum_scaled(P, fs->stiff, fs->diff, fs->mass1, fs->mscale, csr_values, st,
                                     row0, row1)
            : gs ? (gs->upper ? fem::csr_sum_upper_p1(P, *gs->upper, gs->dim, gs->geo, gs->diff,
@@ -1115,7 +1118,7 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
                  tune.onepass == 2};
   const bool onepass = !fused && geometry_sum(pat, mesh, basis, form);
   const bool vec1 = !fused && !onepass && vector_onepass(pat, mesh, basis);
-  const VecSum vs{&pat->vec, form->mass.field || form->mass.scale != 0.0};
+  const VecSum vs{&pat->vec, form->mass.field || form->mass.scale != 0.0, tune.onepass == 2};
   std::vector<cudaEvent_t> evs;
   auto event = [&](cudaEvent_t* ev) -> cudaError_t {
     cudaError_t e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
@@ -1179,7 +1182,12 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
       }
     }
     // rows below the smallest DOF of the next chunk's first cell are final
-    const int64_t row1 = done[c];
+    // (the one-pass vector sum: down to a window of its node blocks)
+    int64_t row1 = done[c];
+    if (vec1 && row1 < P.nrows) {
+      const int64_t w = fem::vec_window_rows(pat->vec);
+      row1 = row1 / w * w;
+    }
     if (row1 > row) {
       rc = sum_rows_to_host(P, pat->host_indptr, staging, csr_values, host_values, row, row1, st,
                             cs, fused ? &fs : nullptr, onepass ? &gs : nullptr,

@@ -69,7 +69,7 @@ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 // function that owns it (cudaFreeAsync on the stream it was taken on).
 struct AsyncScratch {
   cudaStream_t st;
-  void* ptrs[8] = {};
+  void* ptrs[16] = {};
   int n = 0;
   explicit AsyncScratch(cudaStream_t s) : st(s) {}
   AsyncScratch(const AsyncScratch&) = delete;
@@ -77,7 +77,7 @@ struct AsyncScratch {
   template <typename T>
   cudaError_t alloc(T** p, size_t bytes) {
     *p = nullptr;
-    if (n >= 8) return cudaErrorInvalidValue;
+    if (n >= 16) return cudaErrorInvalidValue;
     cudaError_t e = cudaMallocAsync((void**)p, bytes, st);
     if (e == cudaSuccess) ptrs[n++] = (void*)*p;
     return e;
@@ -276,7 +276,11 @@ inline int64_t vec_pair_stride(int dim) {
 // DOF rows [row0, row1) (multiples of dim; row1 < 0: to the last row): the
 // node blocks of their node rows, which also complete the rows' entries
 // left of the diagonal (written by earlier node rows' blocks)
+// DOF rows per window of the node blocks' work-sorted layout: row ranges of
+// vec_upper_sum start and end on multiples of it (or end at the last row)
+int64_t vec_window_rows(const VecUpper& V);
+// coop: the D*D lanes of a node block cooperate (vec_upper_coop_kernel)
 int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, cudaStream_t st,
-                  int64_t row0 = 0, int64_t row1 = -1);
+                  int64_t row0 = 0, int64_t row1 = -1, bool coop = false);
 
 }  // namespace fem

@@ -458,8 +458,11 @@ __global__ void __launch_bounds__(64) simplex_vector_kernel(FemMesh m, FemBiline
 // Per-cell pair blocks of the vector channel forms, the inputs of the
 // one-pass vector sum (fem_vecsum.cu): for the vertex pairs p <= q in
 // row-major upper order k, out[e * R + k * D * D + a * D + b] = E_pq[a][b]
-// (simplex_vector_kernel's expression), and out[e * R + NP * D * D] the
-// mass scale m_e |det| / d!.  R = NP * D * D + 1, NP = (D + 1)(D + 2) / 2.
+// = lam c_p[a] c_q[b] + tr c_p[b] c_q[a] + lap (c_p . c_q) delta_ab (the
+// coefficients times 1/(d! |det|)), evaluated as fma(lam c_p[a], c_q[b],
+// (tr c_p[b]) c_q[a]) -- 2 FP64 operations per entry, 1 on the symmetric
+// blocks p = q -- and out[e * R + NP * D * D] the mass scale m_e |det| / d!.
+// R = NP * D * D + 1, NP = (D + 1)(D + 2) / 2.
 // Cells: positions [ebeg, eend) of the list `cells` (null: the cells
 // themselves), each written at its own cell's row.
 template <int D, int BS>
@@ -487,20 +490,44 @@ __global__ void __launch_bounds__(BS) vector_pair_blocks_kernel(FemMesh m, FemBi
     const double lap = coef_at(f.lap, e) * s0;
     const double tr = coef_at(f.tr, e) * s0;
     double* row = smem + threadIdx.x * (R + 1);
+    double L[NV][D], T[NV][D];
+#pragma unroll
+    for (int p = 0; p < NV; ++p)
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        L[p][a] = lam * s.c[p][a];
+        T[p][a] = tr * s.c[p][a];
+      }
+    const double lt = lam + tr;
     int k = 0;
 #pragma unroll
     for (int p = 0; p < NV; ++p)
 #pragma unroll
       for (int q = p; q < NV; ++q) {
         const double g = lap * dotc<D>(s.c[p], s.c[q]);
+        if (p == q) {
+          // symmetric: (lam + tr) c_p[a] c_p[b] + g delta_ab
 #pragma unroll
-        for (int a = 0; a < D; ++a)
+          for (int a = 0; a < D; ++a) {
+            const double la = lt * s.c[p][a];
 #pragma unroll
-          for (int b = 0; b < D; ++b) {
-            double v = lam * (s.c[p][a] * s.c[q][b]) + tr * (s.c[p][b] * s.c[q][a]);
-            if (a == b) v = v + g;
-            row[k * D * D + a * D + b] = v;
+            for (int b = a; b < D; ++b) {
+              double v = la * s.c[p][b];
+              if (a == b) v = v + g;
+              row[k * D * D + a * D + b] = v;
+              row[k * D * D + b * D + a] = v;
+            }
           }
+        } else {
+#pragma unroll
+          for (int a = 0; a < D; ++a)
+#pragma unroll
+            for (int b = 0; b < D; ++b) {
+              double v = __fma_rn(L[p][a], s.c[q][b], T[p][b] * s.c[q][a]);
+              if (a == b) v = v + g;
+              row[k * D * D + a * D + b] = v;
+            }
+        }
         ++k;
       }
     row[NP * D * D] = coef_at(f.mass, e) * (adet / FACT);

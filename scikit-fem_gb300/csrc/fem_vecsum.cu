@@ -25,6 +25,8 @@
 #include "fem_common.cuh"
 #include "fem_tables.cuh"
 
+#include <cub/device/device_radix_sort.cuh>
+
 #include <algorithm>
 #include <vector>
 
@@ -137,21 +139,92 @@ __device__ __forceinline__ int32_t row_lower_bound(const int32_t* __restrict__ i
   return lo;
 }
 
+// Node rows per window of the work-sorted layout: the blocks of a window's
+// node rows keep their slots' range, sorted inside it.  One row: lanes of a
+// slice stay on neighbouring rows, whose blocks share cells (their pair
+// blocks hit L1) and whose values are written side by side; wider windows
+// measured slower (cfg3, 384k cells: 1.71 ms at 1 row, 1.74 at 8, 1.86 at
+// 64, 1.90 at 512, 1.80 unsorted).
+constexpr int64_t kWindowRows = 1;
+
+// Per node block u (natural order): its list length and the sort key of
+// the work-sorted layout -- (segment << 32) | ~(length x terms), segments
+// the windows' diagonal ranges, then their off-diagonal ranges.
+__global__ void block_work_kernel(const int32_t* __restrict__ slice_len,
+                                  const int32_t* __restrict__ slice_base,
+                                  const uint32_t* __restrict__ codes,
+                                  const int32_t* __restrict__ urow, int64_t nupper, int64_t nd,
+                                  int64_t nwin, const int32_t* __restrict__ count, int npairs,
+                                  int32_t* __restrict__ len, unsigned long long* __restrict__ key,
+                                  int32_t* __restrict__ ident) {
+  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nupper) return;
+  const int64_t sl = u >> 5;
+  const uint32_t* cp = codes + (int64_t)slice_base[sl] * 32 + (u & 31);
+  const int sl_len = slice_len[sl];
+  int n = 0;
+  while (n < sl_len && cp[(int64_t)n * 32] != 0xFFFFFFFFu) ++n;
+  int nt = 1;
+  if (n > 0) {
+    const int ij = (int)(cp[0] & 127u);
+    nt = ij < npairs ? max(1, count[ij]) : 1;
+  }
+  len[u] = n;
+  const int64_t w = urow[u] / kWindowRows;
+  const unsigned long long seg = (unsigned long long)(u < nd ? w : nwin + w);
+  const unsigned long long work = (unsigned long long)n * (unsigned long long)nt;
+  key[u] = (seg << 32) | (0xFFFFFFFFull - (work > 0xFFFFFFFFull ? 0xFFFFFFFFull : work));
+  ident[u] = (int32_t)u;
+}
+
+// Longest list of each slice of 32 slots of the sorted layout.
+__global__ void sorted_slice_len_kernel(const int32_t* __restrict__ perm,
+                                        const int32_t* __restrict__ len, int64_t nupper,
+                                        int64_t nslices, int32_t* __restrict__ slice_len) {
+  const int64_t sl = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (sl >= nslices) return;
+  const int64_t s = sl * 32 + lane;
+  int v = s < nupper ? len[perm[s]] : 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if (lane == 0) slice_len[sl] = v;
+}
+
+// Every slot's list copied from its block's natural position.
+__global__ void sorted_codes_kernel(const int32_t* __restrict__ perm,
+                                    const int32_t* __restrict__ len,
+                                    const int32_t* __restrict__ old_base,
+                                    const uint32_t* __restrict__ old_codes,
+                                    const int32_t* __restrict__ new_base, int64_t nupper,
+                                    uint32_t* __restrict__ new_codes) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nupper) return;
+  const int64_t u = perm[s];
+  const uint32_t* src = old_codes + (int64_t)old_base[u >> 5] * 32 + (u & 31);
+  uint32_t* dst = new_codes + (int64_t)new_base[s >> 5] * 32 + (s & 31);
+  const int n = len[u];
+  for (int p = 0; p < n; ++p) dst[(int64_t)p * 32] = src[(int64_t)p * 32];
+}
+
 // Per node block u = (I, J): the vector CSR position of each row's first
 // entry in the block (vpos[a][u], rows D*I + a) and of the transposed
 // block's (vposT[b][u], rows D*J + b; I < J), and the entries present
 // (bit a*D + b).  *asym when the transposed block's entries differ.
-__global__ void vec_block_pos_kernel(const int32_t* __restrict__ urow,
+__global__ void vec_block_pos_kernel(const int32_t* __restrict__ perm,
+                                     const int32_t* __restrict__ urow,
                                      const int32_t* __restrict__ upos,
                                      const int32_t* __restrict__ nindices, int64_t nupper,
                                      int64_t nd, int dim, const int32_t* __restrict__ indptr,
                                      const int32_t* __restrict__ indices,
                                      int32_t* __restrict__ vpos, int32_t* __restrict__ vposT,
                                      uint16_t* __restrict__ vmask, int32_t* __restrict__ asym) {
+  // u: the slot (the sorted layout's position); b0: its block's natural index
   const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= nupper) return;
-  const int64_t I = urow[u];
-  const int64_t J = nindices[upos[u]];
+  const int64_t b0 = perm[u];
+  const int64_t I = urow[b0];
+  const int64_t J = nindices[upos[b0]];
   unsigned mask = 0, maskT = 0;
   for (int a = 0; a < dim; ++a) {
     const int64_t r = dim * I + a;
@@ -212,49 +285,72 @@ __global__ void __launch_bounds__(128) vec_upper_kernel(
   for (int64_t sl = (ua >> 5) + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
        sl < s1; sl += warps) {
     const int64_t u = sl * 32 + lane;
-    if (u < ua || u >= ub) continue;            // a block of the neighbouring range
-    const int len = slice_len[sl];
+    // a lane whose block belongs to the neighbouring range takes part in
+    // the warp's votes with an empty list and writes nothing
+    const bool inr = u >= ua && u < ub;
+    const int len = inr ? slice_len[sl] : 0;
     const uint32_t* cp = codes + (int64_t)slice_base[sl] * 32 + lane;
     double acc[DD];
 #pragma unroll
     for (int q = 0; q < DD; ++q) acc[q] = 0.0;
-    uint32_t next = len > 0 ? __ldg(cp) : 0xFFFFFFFFu;
-    for (int p = 0; p < len; ++p) {
-      const uint32_t code = next;
-      if (p + 1 < len) next = __ldg(cp + (int64_t)(p + 1) * 32);   // one code ahead
-      if (code == 0xFFFFFFFFu) continue;                            // this lane's list ended
-      const int64_t e = code >> 7;
-      const int ij = (int)(code & 127u);
-      if (e >= nelems || ij >= npairs) continue;   // never for the lists this file builds
-      const double* Eb = E + e * R;
-      const int nt = count[ij];
-      for (int t = 0; t < nt; ++t) {
-        const VecTerm tm = terms[ij * kMaxTerms + t];
-        const double* Ep = Eb + tm.k * DD;
-        double v[DD];
+    // One loop over (contribution, term) steps: a lane moves to its next
+    // contribution as soon as it has done the current one's terms, so the
+    // warp runs max over its lanes of (list length x terms) steps, not
+    // (longest list) x (most terms).  Per contribution: its terms, then its
+    // mass, in that order.
+    uint32_t cur = len > 0 ? __ldg(cp) : 0xFFFFFFFFu;
+    uint32_t nxt = len > 1 ? __ldg(cp + 32) : 0xFFFFFFFFu;
+    int p = 0, t = 0, nt = 0, ij = 0;
+    bool valid = false;
+    const double* Eb = E;
+    auto decode = [&]() {
+      const int64_t e = cur >> 7;
+      ij = (int)(cur & 127u);
+      valid = e < nelems && ij < npairs;   // never false for the lists this file builds
+      nt = valid ? count[ij] : 0;
+      Eb = E + (valid ? e : 0) * R;
+    };
+    bool live = cur != 0xFFFFFFFFu;        // this lane's list is not done
+    if (live) decode();
+    while (__any_sync(0xffffffffu, live)) {
+      if (live) {
+        if (t < nt) {
+          const VecTerm tm = terms[ij * kMaxTerms + t];
+          const double* Ep = Eb + tm.k * DD;
+          double v[DD];
 #pragma unroll
-        for (int q = 0; q < DD; ++q) v[q] = __ldg(Ep + q);
-        if (tm.tr) {
+          for (int q = 0; q < DD; ++q) v[q] = __ldg(Ep + q);
+          if (tm.tr) {
 #pragma unroll
-          for (int a = 0; a < D; ++a)
+            for (int a = 0; a < D; ++a)
 #pragma unroll
-            for (int b = a + 1; b < D; ++b) {
-              const double x = v[a * D + b];
-              v[a * D + b] = v[b * D + a];
-              v[b * D + a] = x;
-            }
+              for (int b = a + 1; b < D; ++b) {
+                const double x = v[a * D + b];
+                v[a * D + b] = v[b * D + a];
+                v[b * D + a] = x;
+              }
+          }
+#pragma unroll
+          for (int q = 0; q < DD; ++q) acc[q] = __fma_rn(tm.c, v[q], acc[q]);
+          ++t;
         }
+        if (t >= nt) {
+          if (MASS && valid) {
+            const double sm = __ldg(Eb + NP * DD);
+            const double mv = mm[ij];
 #pragma unroll
-        for (int q = 0; q < DD; ++q) acc[q] = __fma_rn(tm.c, v[q], acc[q]);
-      }
-      if (MASS) {
-        const double sm = __ldg(Eb + NP * DD);
-        const double mv = mm[ij];
-#pragma unroll
-        for (int a = 0; a < D; ++a) acc[a * D + a] = __fma_rn(sm, mv, acc[a * D + a]);
+            for (int a = 0; a < D; ++a) acc[a * D + a] = __fma_rn(sm, mv, acc[a * D + a]);
+          }
+          t = 0;
+          ++p;
+          cur = nxt;
+          nxt = p + 1 < len ? __ldg(cp + (int64_t)(p + 1) * 32) : 0xFFFFFFFFu;   // one code ahead
+          live = cur != 0xFFFFFFFFu;
+          if (live) decode();
+        }
       }
     }
-    {
+    if (inr) {
       const unsigned mk = vmask[u];
 #pragma unroll
       for (int a = 0; a < D; ++a) {
@@ -271,6 +367,77 @@ __global__ void __launch_bounds__(128) vec_upper_kernel(
           for (int a = 0; a < D; ++a)
             if ((mk >> (a * D + b)) & 1u) vals[pos++] = acc[a * D + b];
         }
+      }
+    }
+  }
+}
+
+// The same sum with the D*D lanes of a node block's entries cooperating:
+// 32 / (D*D) blocks per warp, lane (a, b) of a block accumulates entry
+// (a, b) over the block's cells -- one coalesced load of the cell's pair
+// block per term for the block, where the lane-per-block form issues D*D
+// scattered loads per lane.  Same terms in the same order per entry: the
+// values are bitwise those of vec_upper_kernel.
+template <int D, bool MASS>
+__global__ void __launch_bounds__(128) vec_upper_coop_kernel(
+    int64_t ua, int64_t ub, int64_t nupper, int64_t nd, int64_t nelems, int ns,
+    const int32_t* __restrict__ slice_len, const int32_t* __restrict__ slice_base,
+    const uint32_t* __restrict__ codes, const int32_t* __restrict__ vpos,
+    const int32_t* __restrict__ vposT, const uint16_t* __restrict__ vmask,
+    const VecTerm* __restrict__ terms_g, const int32_t* __restrict__ count_g,
+    const double* __restrict__ mm_g, const double* __restrict__ E, double* __restrict__ vals) {
+  constexpr int DD = D * D;
+  constexpr int BPW = 32 / DD;   // node blocks per warp
+  constexpr int NP = (D + 1) * (D + 2) / 2;
+  constexpr int R = NP * DD + 1;
+  __shared__ VecTerm terms[100 * kMaxTerms];
+  __shared__ int32_t count[100];
+  __shared__ double mm[100];
+  const int npairs = ns * ns;
+  for (int k = threadIdx.x; k < npairs * kMaxTerms; k += blockDim.x) terms[k] = terms_g[k];
+  for (int k = threadIdx.x; k < npairs; k += blockDim.x) {
+    count[k] = count_g[k];
+    mm[k] = mm_g[k];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int sub = lane / DD;            // block of the warp
+  const int q = lane - sub * DD;        // entry of the block
+  const int a = q / D, b = q - a * D;
+  const int qt = b * D + a;             // the entry's position in a transposed pair block
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  for (int64_t u0 = ua + gw * BPW; u0 < ub; u0 += nwarps * BPW) {
+    const int64_t u = u0 + sub;
+    if (sub >= BPW || u >= ub) continue;
+    const int len = slice_len[u >> 5];
+    const uint32_t* cp = codes + (int64_t)slice_base[u >> 5] * 32 + (u & 31);
+    double acc = 0.0;
+    uint32_t next = len > 0 ? __ldg(cp) : 0xFFFFFFFFu;
+    for (int p = 0; p < len; ++p) {
+      const uint32_t code = next;
+      if (code == 0xFFFFFFFFu) break;                               // the block's list ended
+      if (p + 1 < len) next = __ldg(cp + (int64_t)(p + 1) * 32);    // one code ahead
+      const int64_t e = code >> 7;
+      const int ij = (int)(code & 127u);
+      if (e >= nelems || ij >= npairs) continue;   // never for the lists this file builds
+      const double* Eb = E + e * R;
+      const int nt = count[ij];
+      for (int t = 0; t < nt; ++t) {
+        const VecTerm tm = terms[ij * kMaxTerms + t];
+        acc = __fma_rn(tm.c, __ldg(Eb + tm.k * DD + (tm.tr ? qt : q)), acc);
+      }
+      if (MASS && a == b) acc = __fma_rn(__ldg(Eb + NP * DD), mm[ij], acc);
+    }
+    const unsigned mk = vmask[u];
+    if ((mk >> q) & 1u) {
+      const unsigned row = (mk >> (a * D)) & ((1u << D) - 1u);
+      vals[vpos[a * nupper + u] + __popc(row & ((1u << b) - 1u))] = acc;
+      if (u >= nd) {
+        unsigned col = 0;
+#pragma unroll
+        for (int a2 = 0; a2 < D; ++a2) col |= ((mk >> (a2 * D + b)) & 1u) << a2;
+        vals[vposT[b * nupper + u] + __popc(col & ((1u << a) - 1u))] = acc;
       }
     }
   }
@@ -356,11 +523,86 @@ int build_vec_upper(const Pattern& P, const int32_t* udofs, int family, int dim,
                         cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(V->mm, mm.data(), mm.size() * sizeof(double), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(flag, 0, sizeof(int32_t), st);
+  if (e != cudaSuccess) {
+    free_pattern(new Pattern(N));   // releases N's device arrays
+    return fail(check_cuda(e, "vector one-pass tables"));
+  }
+  // The work-sorted layout: inside each window of node rows (its diagonal
+  // blocks, then its blocks above the diagonal) the blocks are ordered by
+  // descending list length x terms, so that a slice's 32 lanes carry about
+  // the same FP64 work (the lanes of a warp share the FP64 pipe's issue).
+  // perm[slot] = the block's natural index; a window's slots stay its range.
+  int32_t* perm = nullptr;
+  if (nu > 0) {
+    const int64_t nwin = ceil_div(nnodes, kWindowRows);
+    int32_t *len = nullptr, *ident = nullptr;
+    unsigned long long *key = nullptr, *key2 = nullptr;
+    e = scratch.alloc(&len, nu * sizeof(int32_t));
+    if (e == cudaSuccess) e = scratch.alloc(&ident, nu * sizeof(int32_t));
+    if (e == cudaSuccess) e = scratch.alloc(&perm, nu * sizeof(int32_t));
+    if (e == cudaSuccess) e = scratch.alloc(&key, nu * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = scratch.alloc(&key2, nu * sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+      block_work_kernel<<<(unsigned)ceil_div(nu, 256), 256, 0, st>>>(
+          V->U.slice_len, V->U.slice_base, V->U.codes, V->U.row, nu, V->U.nd, nwin, V->count,
+          ns * ns, len, key, ident);
+      e = cudaGetLastError();
+    }
+    size_t tmp_bytes = 0;
+    void* tmp = nullptr;
+    if (e == cudaSuccess)
+      e = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, key, key2, ident, perm, nu, 0, 64,
+                                          st);
+    if (e == cudaSuccess) e = scratch.alloc(&tmp, std::max<size_t>(1, tmp_bytes));
+    if (e == cudaSuccess)
+      e = cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, key, key2, ident, perm, nu, 0, 64, st);
+    // slices of the sorted slots, and their codes
+    int32_t *nlen = nullptr, *nbase = nullptr;
+    uint32_t* ncodes = nullptr;
+    const int64_t nsl = V->U.nslices;
+    if (e == cudaSuccess) e = cudaMalloc(&nlen, (nsl + 1) * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&nbase, (nsl + 1) * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMemsetAsync(nlen, 0, (nsl + 1) * sizeof(int32_t), st);
+    if (e == cudaSuccess) {
+      sorted_slice_len_kernel<<<(unsigned)ceil_div(nsl * 32, 256), 256, 0, st>>>(perm, len, nu,
+                                                                                 nsl, nlen);
+      e = cudaGetLastError();
+    }
+    int64_t rows32 = 0;
+    if (e == cudaSuccess) {
+      rc = exclusive_scan_i32(nlen, nbase, nsl, &rows32, st);
+      if (rc) e = cudaErrorUnknown;
+    }
+    if (e == cudaSuccess && rows32 * 32 >= INT32_MAX) e = cudaErrorInvalidValue;
+    if (e == cudaSuccess) e = cudaMalloc(&ncodes, std::max<int64_t>(1, rows32 * 32) * sizeof(uint32_t));
+    if (e == cudaSuccess)
+      e = cudaMemsetAsync(ncodes, 0xFF, std::max<int64_t>(1, rows32 * 32) * sizeof(uint32_t), st);
+    if (e == cudaSuccess) {
+      sorted_codes_kernel<<<(unsigned)ceil_div(nu, 256), 256, 0, st>>>(
+          perm, len, V->U.slice_base, V->U.codes, nbase, nu, ncodes);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      cudaFree(nlen);
+      cudaFree(nbase);
+      cudaFree(ncodes);
+      free_pattern(new Pattern(N));   // releases N's device arrays
+      return fail(rc ? rc : check_cuda(e, "work-sorted node blocks"));
+    }
+    cudaFree(V->U.slice_len);
+    cudaFree(V->U.slice_base);
+    cudaFree(V->U.codes);
+    V->U.slice_len = nlen;
+    V->U.slice_base = nbase;
+    V->U.codes = ncodes;
+    V->U.ncodes = rows32 * 32;
+  }
+  e = cudaMemsetAsync(flag, 0, sizeof(int32_t), st);
   if (e == cudaSuccess && nu > 0) {
     vec_block_pos_kernel<<<(unsigned)ceil_div(nu, 256), 256, 0, st>>>(
-        V->U.row, V->U.pos, N.indices, nu, V->U.nd, dim, P.indptr, P.indices, V->vpos, V->vposT,
-        V->vmask, flag);
+        perm, V->U.row, V->U.pos, N.indices, nu, V->U.nd, dim, P.indptr, P.indices, V->vpos,
+        V->vposT, V->vmask, flag);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(&h, flag, sizeof(h), cudaMemcpyDeviceToHost, st);
@@ -379,14 +621,22 @@ int build_vec_upper(const Pattern& P, const int32_t* udofs, int family, int dim,
   return 0;
 }
 
+int64_t vec_window_rows(const VecUpper& V) { return kWindowRows * V.dim; }
+
 int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, cudaStream_t st,
-                  int64_t row0, int64_t row1) {
+                  int64_t row0, int64_t row1, bool coop) {
   if (V.U.nupper == 0) return 0;
   const int64_t nnodes = (int64_t)V.U.dpos_h.size() - 1;
-  // node rows [n0, n1) of DOF rows [row0, row1) (multiples of dim)
+  // node rows [n0, n1) of DOF rows [row0, row1) (multiples of dim; window
+  // boundaries of the work-sorted layout, or the last row)
   int64_t n0 = row0 < 0 ? 0 : row0 / V.dim;
   int64_t n1 = (row1 < 0 || row1 / V.dim > nnodes) ? nnodes : row1 / V.dim;
   if (n1 <= n0) return 0;
+  if ((n0 % kWindowRows) || ((n1 % kWindowRows) && n1 != nnodes)) {
+    set_error(FEM_ERR_ARGUMENT, "vector one-pass rows [%lld, %lld) off the %lld-row windows",
+              (long long)row0, (long long)row1, (long long)(kWindowRows * V.dim));
+    return FEM_ERR_ARGUMENT;
+  }
   const bool all = n0 == 0 && n1 == nnodes;
   // the node rows' diagonal blocks and their blocks above the diagonal
   // (every node row: the two ranges are adjacent, one launch)
@@ -398,14 +648,24 @@ int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, c
     const int64_t ua = ranges[k][0], ub = ranges[k][1];
     if (ub <= ua) continue;
     const int64_t nsl = ((ub + 31) >> 5) - (ua >> 5);
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nsl, threads / 32),
+    // lane per block: a warp per slice of 32 blocks; cooperative: 32 / D^2 blocks per warp
+    const int64_t nwarp = coop ? ceil_div(ub - ua, 32 / (V.dim * V.dim)) : nsl;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nwarp, threads / 32),
                                                                 (int64_t)num_sms() * 32));
     auto launch = [&](auto kern) {
       kern<<<grid, threads, 0, st>>>(ua, ub, V.U.nupper, V.U.nd, V.nelems, V.ns, V.U.slice_len,
                                      V.U.slice_base, V.U.codes, V.vpos, V.vposT, V.vmask,
                                      static_cast<const VecTerm*>(V.terms), V.count, V.mm, E, vals);
     };
-    if (V.dim == 3) {
+    if (coop) {
+      if (V.dim == 3) {
+        if (mass) launch(vec_upper_coop_kernel<3, true>);
+        else launch(vec_upper_coop_kernel<3, false>);
+      } else {
+        if (mass) launch(vec_upper_coop_kernel<2, true>);
+        else launch(vec_upper_coop_kernel<2, false>);
+      }
+    } else if (V.dim == 3) {
       if (mass) launch(vec_upper_kernel<3, true>);
       else launch(vec_upper_kernel<3, false>);
     } else {

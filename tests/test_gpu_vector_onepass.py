@@ -59,8 +59,12 @@ def _both_paths(form, b, fam, **kw):
     one = form.assemble(b, **kw)
     again = form.assemble(b, **kw)
     np.testing.assert_array_equal(one.data, again.data)
-    lib.fem_set_onepass(N.FAMILY[fam], 0)
     try:
+        # the cooperative form of the one-pass sum: the same values bit for bit
+        lib.fem_set_onepass(N.FAMILY[fam], 2)
+        coop = form.assemble(b, **kw)
+        np.testing.assert_array_equal(one.data, coop.data)
+        lib.fem_set_onepass(N.FAMILY[fam], 0)
         two = form.assemble(b, **kw)
     finally:
         lib.fem_set_onepass(N.FAMILY[fam], 1)
