@@ -351,6 +351,28 @@ def gpu_arm(args):
         e1.record(stream)
         torch.cuda.synchronize()
         t_geom += e0.elapsed_time(e1)
+    # the local kernel with each tile's geometry staged by a 2-D TMA tensor
+    # copy (fem_set_local_tma), against its coalesced loads above
+    N.check(lib.fem_assemble_local(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
+                                   entry.pat.handle, N.ptr(local_buf), N.ptr(status), 0, nel, sp))
+    torch.cuda.synchronize()
+    local_ref = local_buf.clone()
+    t_local_tma = 0.0
+    lib.fem_set_local_tma(N.FAMILY["TetP1"], 1)
+    try:
+        for _ in range(reps + 1):
+            e0.record(stream)
+            N.check(lib.fem_assemble_local(N.byref(b.c_mesh), N.byref(b.c_basis),
+                                           N.byref(c_form), entry.pat.handle, N.ptr(local_buf),
+                                           N.ptr(status), 0, nel, sp))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t_local_tma += e0.elapsed_time(e1) if _ else 0.0   # the first is a warm-up
+    finally:
+        lib.fem_set_local_tma(N.FAMILY["TetP1"], 0)
+    assert int(status.item()) == 0, "TMA-staged local kernel status %d" % int(status.item())
+    local_tma_same = bool(torch.equal(local_buf, local_ref))
+    t_local_tma /= reps
     autotune.apply(N.FAMILY["TetP1"], tuned)
     t_local /= reps
     t_sum /= reps
@@ -437,6 +459,10 @@ def gpu_arm(args):
             "two_pass_local": kern("simplex_scalar_kernel<3,1,BS,cached geometry>", t_local,
                                    LOCAL_B_PER_CELL),
             "two_pass_sum": kern("csr_sum_kernel<4,U,0>", t_sum, SUM_B_PER_CELL),
+            "two_pass_local_tma": dict(kern("simplex_scalar_kernel<3,1,128,cached,TMA> (each tile's "
+                                            "geometry by one cp.async.bulk.tensor.2d copy)",
+                                            t_local_tma, LOCAL_B_PER_CELL),
+                                       bitwise_equal=local_tma_same),
             "coefficient_update_sum": kern("csr_scaled_pair_kernel<4,U> (opt-in cache of "
                                            "unit-coefficient rows and mass matrix; not the "
                                            "plain step)", t_cu, FUSED_B_PER_CELL),
@@ -448,7 +474,8 @@ def gpu_arm(args):
                  "ms": t_geom, "gflops": fp64_achieved, "peak_gflops": FP64_PEAK_GFLOPS,
                  "frac": fp64_achieved / FP64_PEAK_GFLOPS},
         "kernels_ms": {"onepass_sum": t_one, "coef_checks": t_checks,
-                       "two_pass_local": t_local, "two_pass_sum": t_sum,
+                       "two_pass_local": t_local, "two_pass_local_tma": t_local_tma,
+                       "two_pass_sum": t_sum,
                        "two_pass_step": t_local + t_sum,
                        "coefficient_update_step": t_cu,
                        "local_computing_geometry": t_geom},

@@ -238,6 +238,18 @@ int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll, 
 int fem_set_onepass(int family, int variant);
 
 /*
+ * The local-matrix kernel of the scalar simplex families on the pattern's
+ * geometry cache (the two-pass path), in the same table: on = 1 brings each
+ * tile's geometry -- a (cache entries) x (cells per block) box of the SoA
+ * cache -- into shared memory with one 2-D TMA tensor copy
+ * (cp.async.bulk.tensor) instead of per-thread coalesced loads.  Used when
+ * the call passes a status word (FEM_ERR_TIMEOUT if its bounded wait runs
+ * out), without a cell list, on a mesh with an even number of cells (the
+ * tensor map's row stride); otherwise the loads.  Same values bit for bit.
+ */
+int fem_set_local_tma(int family, int on);
+
+/*
  * Local (element) matrices: local[(e * nbfun + i) * nbfun + j] = K_e[i][j],
  * i = test function (row), j = trial function (column), the same entry as
  * the reference's data[j, i, e] (bilinear_form.py:90-98).

@@ -444,6 +444,16 @@ int fem_set_onepass(int family, int variant) {
   return 0;
 }
 
+int fem_set_local_tma(int family, int on) {
+  if (family < 1 || family > 5 || (on != 0 && on != 1)) {
+    set_error(FEM_ERR_ARGUMENT, "family %d / local TMA flag %d out of range", family, on);
+    return FEM_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> lock(fem::g_tuning_mu);
+  fem::g_tuning[family].local_tma = on;
+  return 0;
+}
+
 int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll, int sum_cols) {
   if (family < 1 || family > 5 || (local_block != 64 && local_block != 128 && local_block != 256) ||
       persistent < 0 || (sum_unroll != 4 && sum_unroll != 8 && sum_unroll != 16) ||

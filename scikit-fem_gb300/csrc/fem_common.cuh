@@ -175,6 +175,8 @@ struct Tuning {
   int sum_cols = 1;       // fused sum: columns per lane (1, or 2 for an even row length)
   int onepass = 1;        // one-pass P1 sum: 0 two lanes per row, 1 a lane per upper entry,
                           // 2 the same with its codes staged in shared memory by TMA
+  int local_tma = 0;      // local kernel on the geometry cache: 1 each tile's geometry
+                          // staged by a 2-D TMA tensor copy (fem_set_local_tma)
 };
 Tuning tuning_for(int family);
 
@@ -225,8 +227,9 @@ struct UpperLists {
   int32_t* row = nullptr;       // nupper: i
   int32_t* slice_len = nullptr;   // nslices
   int32_t* slice_base = nullptr;  // nslices: first code row (32 codes) of the slice
-  // ncodes, 0xFFFFFFFF padding: e * 16 + li * 4 + lj (at most 4 local
-  // functions, narrow codes), or e * 128 + li * nu + lj (wide codes, nu <= 11)
+  // ncodes, 0xFFFFFFFF padding: e * 16 + k, k the Gram entry of the local
+  // pair (li, lj) (at most 4 local functions, narrow codes), or
+  // e * 128 + li * nu + lj (wide codes, nu <= 11)
   uint32_t* codes = nullptr;
   std::vector<int32_t> dpos_h, opos_h;
 };

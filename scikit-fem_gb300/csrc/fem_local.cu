@@ -24,6 +24,8 @@
 // separately rounded arithmetic -- as numpy evaluates them -- come out as
 // exact zeros; that build feeds the eliminate_zeros mask of the pattern.
 
+#include <cuda.h>   // CUtensorMap (the TMA-staged local kernel)
+#include <cstring>
 #include <type_traits>
 
 #include "fem_common.cuh"
@@ -251,10 +253,28 @@ __global__ void simplex_geometry_cache_kernel(FemMesh m, double* __restrict__ ge
   geo[(int64_t)k * m.nelems + e] = adet;
 }
 
+// Bounded mbarrier wait (the TMA-staged kernel): false when it gave up.
+__device__ __forceinline__ bool tile_wait(uint32_t bar, uint32_t parity, long long limit) {
+  for (long long it = 0; it < limit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
+        "selp.u32 %0, 1, 0, p; }"
+        : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 // CACHED: the geometry comes from geo (simplex_geometry_cache_kernel on the
 // same coordinates) instead of the mesh -- coefficient changes then cost
 // the ~14 FP64 operations per cell of the form alone.
-template <int D, int ORDER, int BS, bool CACHED>
+// TMA (with CACHED, no cell list): each tile's geometry -- the (NG+1) x BS
+// box of the SoA cache at column e0 -- comes into shared memory by one
+// cp.async.bulk.tensor.2d copy (tensor map tmap) instead of per-thread
+// loads; the wait is bounded (FEM_ERR_TIMEOUT in *status, after a second
+// bounded wait for the copy in flight).
+template <int D, int ORDER, int BS, bool CACHED, bool TMA = false>
 __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBilinear f,
                                                                 FemCoef kdiff,
                                                                 double* __restrict__ out,
@@ -262,16 +282,58 @@ __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBiline
                                                                 int32_t* __restrict__ status,
                                                                 const int32_t* __restrict__ cells,
                                                                 const double* __restrict__ geo,
-                                                                int64_t ebeg, int64_t eend) {
+                                                                int64_t ebeg, int64_t eend,
+                                                                const __grid_constant__ CUtensorMap tmap) {
   constexpr int NB = SimplexTraits<D, ORDER>::NB;
   constexpr int L = NB * NB;
+  constexpr int NGEO = kGeoCount<D>;
   constexpr double INV_FACT = 1.0 / SimplexTraits<D, ORDER>::FACT;
   extern __shared__ double smem[];
   int64_t* cid = cells ? reinterpret_cast<int64_t*>(smem + (size_t)BS * (L + 1)) : nullptr;
+  // TMA: the geometry tile after the row buffer (128-byte aligned), then the mbarrier
+  constexpr size_t kTileOff = (((size_t)BS * (L + 1) * sizeof(double)) + 127) / 128 * 128;
+  double* sgeo = reinterpret_cast<double*>(reinterpret_cast<char*>(smem) + kTileOff);
+  uint64_t* sbar = reinterpret_cast<uint64_t*>(sgeo + (size_t)NGEO * BS);
+  uint32_t phase = 0;
+  if constexpr (TMA) {
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"((uint32_t)__cvta_generic_to_shared(sbar)) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+  }
   int32_t flags = 0;
   // grid-stride over element tiles of BS cells (persistent when the grid is
   // smaller than the number of tiles)
   for (int64_t e0 = ebeg + (int64_t)blockIdx.x * BS; e0 < eend; e0 += (int64_t)gridDim.x * BS) {
+  if constexpr (TMA) {
+    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(sbar);
+    if (threadIdx.x == 0) {
+      // the previous tile's reads (generic proxy) before the copy's writes (async proxy)
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      unsigned long long state;
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+                   : "=l"(state) : "r"(bar), "r"((uint32_t)(NGEO * BS * sizeof(double))) : "memory");
+      asm volatile(
+          "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+          "[%0], [%1, {%2, %3}], [%4];"
+          :: "r"((uint32_t)__cvta_generic_to_shared(sgeo)), "l"(&tmap), "r"((int32_t)e0), "r"(0),
+             "r"(bar) : "memory");
+      (void)state;
+    }
+    // every thread waits (bounded); the outcome is made block-uniform
+    if (!__syncthreads_and(tile_wait(bar, phase, 1ll << 22) ? 1 : 0)) {
+      // gave up: report, let this tile's copy land (bounded), stop
+      if (threadIdx.x == 0) {
+        fem::publish_status(status, 1 << FEM_ERR_TIMEOUT);
+        tile_wait(bar, phase, 1ll << 22);
+      }
+      __syncthreads();
+      return;
+    }
+    phase ^= 1u;
+  }
   const int64_t pos = e0 + threadIdx.x;
   if (pos < eend) {
     const int64_t e = cell_at(cells, pos);
@@ -283,7 +345,15 @@ __global__ void __launch_bounds__(BS) simplex_scalar_kernel(FemMesh m, FemBiline
     // (the 1/d! of the mass goes into the table constants, folded at
     // compile time)
     double gram[D + 1][D + 1], adet, sd;
-    if constexpr (CACHED) {
+    if constexpr (CACHED && TMA) {
+      int k = 0;
+#pragma unroll
+      for (int a = 0; a <= D; ++a)
+#pragma unroll
+        for (int b = a; b <= D; ++b) gram[a][b] = sgeo[(k++) * BS + threadIdx.x];
+      adet = sgeo[k * BS + threadIdx.x];
+      sd = coef_at(f.diff, e);
+    } else if constexpr (CACHED) {
       int k = 0;
 #pragma unroll
       for (int a = 0; a <= D; ++a)
@@ -815,27 +885,70 @@ static int set_smem(K kernel, size_t bytes) {
   return 0;
 }
 
+// The 2-D tensor map of the SoA geometry cache (ng rows of nelems doubles)
+// with a box of ng x bs: encoded through the driver's cuTensorMapEncodeTiled
+// (looked up once through the runtime).  False when it cannot be made
+// (the row stride must be a multiple of 16 bytes: nelems even).
+static bool geometry_tensor_map(const double* geo, int64_t nelems, int ng, int bs,
+                                CUtensorMap* map) {
+  using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                              const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                              const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                              CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static Encode encode = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    looked = true;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &fn, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      encode = reinterpret_cast<Encode>(fn);
+    cudaGetLastError();
+  }
+  if (!encode || nelems <= 0 || (nelems * 8) % 16 != 0 || ((uintptr_t)geo % 16) != 0) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)nelems, (cuuint64_t)ng};
+  const cuuint64_t strides[1] = {(cuuint64_t)nelems * sizeof(double)};
+  const cuuint32_t box[2] = {(cuuint32_t)bs, (cuuint32_t)ng};
+  const cuuint32_t estr[2] = {1, 1};
+  return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double*>(geo), dims, strides,
+                box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
+
 template <int D, int O, int BS>
 static int launch_scalar(const FemMesh& m, const FemBilinear& f, double* out,
                          const uint8_t* ref_bits, int32_t* status, int persistent,
                          cudaStream_t st, int64_t ebeg, int64_t eend, const int32_t* cells,
-                         const double* geo) {
+                         const double* geo, bool tma) {
   constexpr int NB = SimplexTraits<D, O>::NB;
   const size_t sm = (size_t)BS * (NB * NB + 1) * sizeof(double) + (cells ? kCidBytes<BS> : 0);
   int64_t grid = fem::ceil_div(eend - ebeg, BS);
   if (persistent > 0) grid = std::min<int64_t>(grid, (int64_t)persistent * fem::num_sms());
   FemCoef kdiff = f.diff;
   kdiff.scale = f.diff.scale * (1.0 / SimplexTraits<D, O>::FACT);
-  if (geo) {
+  CUtensorMap tmap;
+  std::memset(&tmap, 0, sizeof(tmap));
+  if (geo && tma && status && !cells && ebeg % 2 == 0 &&
+      geometry_tensor_map(geo, m.nelems, kGeoCount<D>, BS, &tmap)) {
+    // the TMA-staged form: the row buffer, the geometry tile (128-byte aligned), the mbarrier
+    const size_t tile_off = ((size_t)BS * (NB * NB + 1) * sizeof(double) + 127) / 128 * 128;
+    const size_t smt = tile_off + (size_t)kGeoCount<D> * BS * sizeof(double) + 16;
+    int rc = set_smem(simplex_scalar_kernel<D, O, BS, true, true>, smt);
+    if (rc) return rc;
+    simplex_scalar_kernel<D, O, BS, true, true><<<(unsigned)grid, BS, smt, st>>>(
+        m, f, kdiff, out, ref_bits, status, cells, geo, ebeg, eend, tmap);
+  } else if (geo) {
     int rc = set_smem(simplex_scalar_kernel<D, O, BS, true>, sm);
     if (rc) return rc;
     simplex_scalar_kernel<D, O, BS, true><<<(unsigned)grid, BS, sm, st>>>(
-        m, f, kdiff, out, ref_bits, status, cells, geo, ebeg, eend);
+        m, f, kdiff, out, ref_bits, status, cells, geo, ebeg, eend, tmap);
   } else {
     int rc = set_smem(simplex_scalar_kernel<D, O, BS, false>, sm);
     if (rc) return rc;
     simplex_scalar_kernel<D, O, BS, false><<<(unsigned)grid, BS, sm, st>>>(
-        m, f, kdiff, out, ref_bits, status, cells, nullptr, ebeg, eend);
+        m, f, kdiff, out, ref_bits, status, cells, nullptr, ebeg, eend, tmap);
   }
   return 0;
 }
@@ -847,10 +960,11 @@ static int launch_scalar_tuned(const FemMesh& m, const FemBilinear& f, double* o
                                const double* geo) {
   const fem::Tuning t = fem::tuning_for(D == 2 ? (O == 1 ? FEM_TRI_P1 : FEM_TRI_P2)
                                                : (O == 1 ? FEM_TET_P1 : FEM_TET_P2));
+  const bool tma = t.local_tma != 0;
   switch (t.local_block) {
-    case 64: return launch_scalar<D, O, 64>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend, cells, geo);
-    case 256: return launch_scalar<D, O, 256>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend, cells, geo);
-    default: return launch_scalar<D, O, 128>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend, cells, geo);
+    case 64: return launch_scalar<D, O, 64>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend, cells, geo, tma);
+    case 256: return launch_scalar<D, O, 256>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend, cells, geo, tma);
+    default: return launch_scalar<D, O, 128>(m, f, out, ref_bits, status, t.persistent, st, ebeg, eend, cells, geo, tma);
   }
 }
 

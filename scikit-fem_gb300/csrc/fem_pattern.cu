@@ -520,6 +520,16 @@ __host__ __device__ constexpr int gram_index(int nu, int a, int b) {
   return a <= b ? a * (2 * nu + 1 - a) / 2 + b - a : b * (2 * nu + 1 - b) / 2 + a - b;
 }
 
+// Bit k set when Gram entry k is a diagonal one (gram_index(nu, a, a)).
+template <int NU>
+constexpr uint32_t gram_diag_mask() {
+  uint32_t m = 0;
+  for (int a = 0; a < NU; ++a) m |= 1u << gram_index(NU, a, a);
+  return m;
+}
+template <int NU>
+constexpr uint32_t kGramDiag = gram_diag_mask<NU>();
+
 template <int NU, int U, bool MFIELD>
 __global__ void __launch_bounds__(128) csr_geometry_p1_kernel(
     const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
@@ -663,7 +673,8 @@ __global__ void __launch_bounds__(128) csr_geometry_p1_kernel(
 // Lists are stored sliced: 32 consecutive upper entries form a slice of
 // len = the longest list among them; code p of the slice's lane l sits at
 // codes[(base + p) * 32 + l] (coalesced), padded with 0xFFFFFFFF.  A code
-// is e * 16 + li * 4 + lj.  Upper entries are numbered diagonal entries
+// is e * 16 + k, k the Gram entry gram_index(li, lj) of the cell's local
+// pair (diagonal ones flagged by kGramDiag).  Upper entries are numbered diagonal entries
 // first (by row), then the others by (row, column), so list lengths within
 // a slice are alike (a vertex's cells vs an edge's cells).
 // TMA (bulk-copy engine) helpers for the staged form below.
@@ -743,14 +754,15 @@ __device__ __forceinline__ void upper_slice(
       mv[v] = (MAcc)0;
       if (live && c[v] != 0xFFFFFFFFu) {
         const uint32_t e = c[v] >> 4;
-        const int li = (int)((c[v] >> 2) & 3u), lj = (int)(c[v] & 3u);
+        const int gk = (int)(c[v] & 15u);        // the pair's Gram entry
+        const bool diag = (kGramDiag<NU> >> gk) & 1u;
         kv[v] = kfield ? __ldg(kfield + (int64_t)e * kstride) : 1.0;
-        g[v] = __ldg(geo + (int64_t)gram_index(NU, li, lj) * nelems + e);
+        g[v] = __ldg(geo + (int64_t)gk * nelems + e);
         const double adet = __ldg(adet_arr + e);
         MAcc m;
         if constexpr (MFIELD) m = __ldg(mfield + (int64_t)e * mstride) * adet;
         else m = fixed_of(adet, mb);
-        mv[v] = li == lj ? m + m : m;
+        mv[v] = diag ? m + m : m;
       }
     }
 #pragma unroll
@@ -992,7 +1004,8 @@ __global__ void upper_codes_kernel(const int32_t* __restrict__ indptr,
       const int64_t u = ((int)sv == sd && d) ? (int64_t)dpos[i] : nd + opos[i] + ((int)sv - so);
       const int c = cursor[u]++;
       codes[((int64_t)slice_base[u >> 5] + c) * 32 + (u & 31)] =
-          wide ? (e << 7) | (li * (uint32_t)nu + (uint32_t)j) : (e << 4) | (li << 2) | (uint32_t)j;
+          wide ? (e << 7) | (li * (uint32_t)nu + (uint32_t)j)
+               : (e << 4) | (uint32_t)gram_index(nu, (int)li, j);
     }
   }
 }

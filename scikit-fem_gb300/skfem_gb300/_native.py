@@ -150,6 +150,7 @@ _SIGS = {
                                    ctypes.c_double, _P, _P, _P, _P]),
     "fem_set_tuning": (ctypes.c_int, [ctypes.c_int] * 5),
     "fem_set_onepass": (ctypes.c_int, [ctypes.c_int] * 2),
+    "fem_set_local_tma": (ctypes.c_int, [ctypes.c_int] * 2),
     "fem_assemble_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "fem_batch_plan_build": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_int32,
                                             ctypes.POINTER(ctypes.c_void_p)]),

@@ -295,3 +295,44 @@ def test_one_pass_forms_agree(fam, cls, dim, n, elem, form):
                     np.testing.assert_array_equal(got_host, ref_host)
         finally:
             autotune.apply(code, dict(base, onepass=1))
+
+
+@pytest.mark.parametrize("fam,cls,dim,n,elem", [
+    ("TriP1", F.MeshTri, 2, 40, F.ElementTriP1), ("TriP2", F.MeshTri, 2, 30, F.ElementTriP2),
+    ("TetP1", F.MeshTet, 3, 12, F.ElementTetP1), ("TetP2", F.MeshTet, 3, 8, F.ElementTetP2)])
+def test_local_kernel_tma_staged_geometry_is_bitwise_the_same(fam, cls, dim, n, elem):
+    """fem_set_local_tma: the local kernel on the geometry cache with each
+    tile's geometry brought in by one 2-D TMA tensor copy writes the same
+    local matrices, bit for bit, as with per-thread loads; the status word
+    stays clean (no bounded wait ran out)."""
+    m = cls.init_tensor(*(np.linspace(0, 1, n),) * dim)
+    p = m.p.copy()
+    inner = np.all((p > 1e-12) & (p < 1 - 1e-12), axis=0)
+    p[:, inner] += np.random.default_rng(4).uniform(-0.2 / n, 0.2 / n, (dim, int(inner.sum())))
+    b = F.Basis(cls(p, m.t), elem())
+    assert b.nelems % 2 == 0                  # the tensor map's row stride
+    k = torch.from_numpy(np.random.default_rng(6).lognormal(0, 1, b.nelems)).cuda()
+    c = torch.from_numpy(np.random.default_rng(7).uniform(0.5, 2.0, b.nelems)).cuda()
+    K = k_lap_cmass.assemble_torch(b, k=k, c=c)
+    entry = next(e for key, e in b._patterns.items() if key[0] == "bilinear")
+    c_form = k_lap_cmass._setup(b, None, {"k": k, "c": c})[2]
+    lib = N.lib()
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+    def local():
+        out = torch.full_like(entry.staging, np.nan)
+        N.check(lib.fem_assemble_local(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
+                                       entry.pat.handle, N.ptr(out), N.ptr(status), 0, b.nelems,
+                                       N.stream_ptr()))
+        torch.cuda.synchronize()
+        return out
+    ref = local()
+    try:
+        lib.fem_set_local_tma(N.FAMILY[fam], 1)
+        got = local()
+    finally:
+        lib.fem_set_local_tma(N.FAMILY[fam], 0)
+    assert int(status.item()) == 0
+    nloc = b.nelems * b.Nbfun * b.Nbfun
+    assert torch.equal(got[:nloc], ref[:nloc])
+    assert K.values().numel() > 0
