@@ -246,7 +246,7 @@ int cache_mass_base(FemPattern* pat, const FemMesh* mesh, const FemBasis* basis,
     // (with its error cleared) when the pattern is not symmetric or there
     // is no room for its lists
     pat->upper_tried = true;
-    rc = fem::build_upper_lists(P, &pat->upper, st);
+    rc = fem::build_upper_lists(P, &pat->upper, st, false, fem::kUpperBlockRows);
     pat->upper_ok = rc == 0;
     if (rc) {
       cudaGetLastError();
@@ -1198,6 +1198,8 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
       const int64_t w = fem::vec_window_rows(pat->vec);
       row1 = row1 / w * w;
     }
+    if (onepass && gs.upper && gs.upper->block_rows > 0 && row1 < P.nrows)
+      row1 = row1 / gs.upper->block_rows * gs.upper->block_rows;
     if (row1 > row) {
       rc = sum_rows_to_host(P, pat->host_indptr, staging, csr_values, host_values, row, row1, st,
                             cs, fused ? &fs : nullptr, onepass ? &gs : nullptr,

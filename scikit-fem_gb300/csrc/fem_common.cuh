@@ -219,6 +219,9 @@ int row_mass_base(const Pattern& P, const double* adet, int16_t* mbase, int* shm
 // in the sum's order, sliced 32 entries at a time.  Pattern-only data.
 struct UpperLists {
   int64_t nd = 0, nupper = 0, nslices = 0, ncodes = 0;
+  // 0: diagonal entries first, then the others; > 0: rows in blocks of
+  // block_rows, each block's diagonal entries then its others (upper_slot)
+  int64_t block_rows = 0;
   int32_t max_len = 0;          // the longest slice (codes per lane)
   int32_t* dpos = nullptr;      // nrows + 1: row -> first diagonal entry
   int32_t* opos = nullptr;      // nrows + 1: row -> first off-diagonal entry (after nd)
@@ -233,8 +236,12 @@ struct UpperLists {
   uint32_t* codes = nullptr;
   std::vector<int32_t> dpos_h, opos_h;
 };
-// wide: codes e * 128 + li * nu + lj whatever nu (always for nu > 4)
-int build_upper_lists(const Pattern& P, UpperLists* U, cudaStream_t st, bool wide = false);
+// wide: codes e * 128 + li * nu + lj whatever nu (always for nu > 4);
+// block_rows: the row-block layout (UpperLists::block_rows)
+int build_upper_lists(const Pattern& P, UpperLists* U, cudaStream_t st, bool wide = false,
+                      int64_t block_rows = 0);
+// Rows per block of the one-pass P1 sum's upper lists
+constexpr int64_t kUpperBlockRows = 4096;
 void free_upper_lists(UpperLists* U);
 // tma: stage each warp's slice codes in shared memory with bulk copies
 // (needs status for its bounded waits' error bit)

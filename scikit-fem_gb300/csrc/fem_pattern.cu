@@ -883,6 +883,24 @@ __global__ void __launch_bounds__(128) csr_upper_p1_tma_kernel(
 // Upper-entry numbering of a square pattern, one thread per row: the
 // offset of the diagonal (or of the first column above it) in row i, and
 // whether the diagonal is present; then the number of upper entries.
+// Slot of row i's upper entries: its diagonal (k < 0) or its k-th entry
+// above the diagonal.  block_rows == 0: every diagonal entry first (by row),
+// then the others by (row, column).  block_rows > 0: the rows in blocks of
+// block_rows, each block's diagonal entries, then its other entries -- the
+// entries of neighbouring rows, diagonal or not, are summed at about the
+// same time, so each cell's geometry is read about once.
+__device__ __forceinline__ int64_t upper_slot(const int32_t* __restrict__ dpos,
+                                              const int32_t* __restrict__ opos, int64_t nd,
+                                              int64_t nrows, int64_t block_rows, int64_t i,
+                                              int k) {
+  if (block_rows <= 0) return k < 0 ? (int64_t)dpos[i] : nd + opos[i] + k;
+  const int64_t b0 = i / block_rows * block_rows;
+  const int64_t b1 = b0 + block_rows < nrows ? b0 + block_rows : nrows;
+  const int64_t start = (int64_t)dpos[b0] + opos[b0];
+  if (k < 0) return start + (dpos[i] - dpos[b0]);
+  return start + (dpos[b1] - dpos[b0]) + (opos[i] - opos[b0]) + k;
+}
+
 __global__ void upper_count_kernel(const int32_t* __restrict__ indptr,
                                    const int32_t* __restrict__ indices, int64_t nrows,
                                    int32_t* __restrict__ ndiag, int32_t* __restrict__ noff) {
@@ -908,7 +926,8 @@ __global__ void upper_fill_kernel(const int32_t* __restrict__ indptr,
                                   const int32_t* __restrict__ inc,
                                   const uint16_t* __restrict__ slot, int nu, int64_t nrows,
                                   const int32_t* __restrict__ dpos, const int32_t* __restrict__ opos,
-                                  int64_t nd, int32_t* __restrict__ pos, int32_t* __restrict__ tpos,
+                                  int64_t nd, int64_t block_rows, int32_t* __restrict__ pos,
+                                  int32_t* __restrict__ tpos,
                                   int32_t* __restrict__ urow, int32_t* __restrict__ cnt,
                                   int32_t* __restrict__ asym) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -924,14 +943,14 @@ __global__ void upper_fill_kernel(const int32_t* __restrict__ indptr,
   const int sd = lo - p0;                   // offset of the diagonal / first upper column
   const int so = sd + (d ? 1 : 0);          // offset of the first column above the diagonal
   if (d) {
-    const int64_t u = dpos[i];
+    const int64_t u = upper_slot(dpos, opos, nd, nrows, block_rows, i, -1);
     pos[u] = lo;
     tpos[u] = -1;
     urow[u] = (int32_t)i;
     cnt[u] = 0;
   }
   for (int s = so; s < p1 - p0; ++s) {
-    const int64_t u = nd + opos[i] + (s - so);
+    const int64_t u = upper_slot(dpos, opos, nd, nrows, block_rows, i, s - so);
     const int32_t j = indices[p0 + s];
     pos[u] = p0 + s;
     // (j, i) in row j: i < j is among its columns (the pattern is symmetric)
@@ -952,7 +971,8 @@ __global__ void upper_fill_kernel(const int32_t* __restrict__ indptr,
     for (int j = 0; j < nu; ++j) {
       const uint16_t sv = slot[((int64_t)b + q) * nu + j];
       if (sv == 0xFFFF || (int)sv < sd) continue;
-      const int64_t u = ((int)sv == sd && d) ? (int64_t)dpos[i] : nd + opos[i] + ((int)sv - so);
+      const int64_t u = upper_slot(dpos, opos, nd, nrows, block_rows, i,
+                                   ((int)sv == sd && d) ? -1 : (int)sv - so);
       cnt[u] += 1;
     }
 }
@@ -979,6 +999,7 @@ __global__ void upper_codes_kernel(const int32_t* __restrict__ indptr,
                                    const uint16_t* __restrict__ slot, int nu, int64_t nrows,
                                    const int32_t* __restrict__ dpos,
                                    const int32_t* __restrict__ opos, int64_t nd,
+                                   int64_t block_rows,
                                    const int32_t* __restrict__ slice_base,
                                    int32_t* __restrict__ cursor, uint32_t* __restrict__ codes,
                                    bool wide) {
@@ -1001,7 +1022,8 @@ __global__ void upper_codes_kernel(const int32_t* __restrict__ indptr,
     for (int j = 0; j < nu; ++j) {
       const uint16_t sv = slot[((int64_t)b + q) * nu + j];
       if (sv == 0xFFFF || (int)sv < sd) continue;
-      const int64_t u = ((int)sv == sd && d) ? (int64_t)dpos[i] : nd + opos[i] + ((int)sv - so);
+      const int64_t u = upper_slot(dpos, opos, nd, nrows, block_rows, i,
+                                   ((int)sv == sd && d) ? -1 : (int)sv - so);
       const int c = cursor[u]++;
       codes[((int64_t)slice_base[u >> 5] + c) * 32 + (u & 31)] =
           wide ? (e << 7) | (li * (uint32_t)nu + (uint32_t)j)
@@ -1594,8 +1616,10 @@ int csr_sum_geometry_p1(const Pattern& P, int dim, const double* geo, const FemC
 }
 
 
-int build_upper_lists(const Pattern& P, UpperLists* U, cudaStream_t st, bool wide) {
+int build_upper_lists(const Pattern& P, UpperLists* U, cudaStream_t st, bool wide,
+                      int64_t block_rows) {
   *U = UpperLists();
+  U->block_rows = block_rows > 0 ? block_rows : 0;
   const int nu = P.nbfun_u;
   wide = wide || nu > 4;
   if (!P.has_matrix || P.nbfun_v != nu || nu > 11) {
@@ -1646,8 +1670,8 @@ int build_upper_lists(const Pattern& P, UpperLists* U, cudaStream_t st, bool wid
   if (e != cudaSuccess) return fail(check_cuda(e, "cudaMallocAsync(upper list lengths)"));
   if (n > 0) {
     upper_fill_kernel<<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(
-        P.indptr, P.indices, P.inc_ptr, P.inc, P.slot, nu, n, U->dpos, U->opos, U->nd, U->pos,
-        U->tpos, U->row, cnt, asym);
+        P.indptr, P.indices, P.inc_ptr, P.inc, P.slot, nu, n, U->dpos, U->opos, U->nd,
+        U->block_rows, U->pos, U->tpos, U->row, cnt, asym);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(check_cuda(e, "upper_fill_kernel"));
     int32_t h = 0;
@@ -1691,7 +1715,7 @@ int build_upper_lists(const Pattern& P, UpperLists* U, cudaStream_t st, bool wid
   if (n > 0) {
     upper_codes_kernel<<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(
         P.indptr, P.indices, P.inc_ptr, P.inc, P.slot, nu, n, U->dpos, U->opos, U->nd,
-        U->slice_base, cnt, U->codes, wide);
+        U->block_rows, U->slice_base, cnt, U->codes, wide);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(check_cuda(e, "upper_codes_kernel"));
   }
@@ -1744,10 +1768,21 @@ int csr_sum_upper_p1(const Pattern& P, const UpperLists& U, int dim, const doubl
   const int64_t ms = mass.stride > 1 ? mass.stride : 1;
   const int Un = P.sum_unroll >= 8 ? 8 : 4;
   // upper entries of rows [row0, row1): a diagonal range and an off-diagonal
-  // one (all rows: the two are adjacent, one launch)
+  // one (all rows: the two are adjacent, one launch); in the row-block
+  // layout one range, the rows' blocks
   const bool all = row0 == 0 && row1 == P.nrows;
-  const int64_t ranges[2][2] = {{all ? 0 : U.dpos_h[row0], all ? U.nupper : U.dpos_h[row1]},
-                                {all ? 0 : U.nd + U.opos_h[row0], all ? 0 : U.nd + U.opos_h[row1]}};
+  int64_t ranges[2][2] = {{all ? 0 : U.dpos_h[row0], all ? U.nupper : U.dpos_h[row1]},
+                          {all ? 0 : U.nd + U.opos_h[row0], all ? 0 : U.nd + U.opos_h[row1]}};
+  if (U.block_rows > 0 && !all) {
+    if (row0 % U.block_rows || (row1 % U.block_rows && row1 != P.nrows)) {
+      set_error(FEM_ERR_ARGUMENT, "upper-list rows [%lld, %lld) off the %lld-row blocks",
+                (long long)row0, (long long)row1, (long long)U.block_rows);
+      return FEM_ERR_ARGUMENT;
+    }
+    ranges[0][0] = (int64_t)U.dpos_h[row0] + U.opos_h[row0];
+    ranges[0][1] = (int64_t)U.dpos_h[row1] + U.opos_h[row1];
+    ranges[1][0] = ranges[1][1] = 0;
+  }
   const int threads = 128;
   for (int k = 0; k < 2; ++k) {
     const int64_t ua = ranges[k][0], ub = ranges[k][1];
