@@ -35,6 +35,8 @@ namespace fem {
 namespace {
 
 constexpr int kMaxTerms = 4;
+// vmask bit of a node block off the diagonal (its transpose is written too)
+constexpr unsigned kOffDiagBit = 1u << 15;
 
 struct VecTerm {
   int32_t k;    // pair index of (min(p,q), max(p,q)) in row-major upper order
@@ -139,22 +141,28 @@ __device__ __forceinline__ int32_t row_lower_bound(const int32_t* __restrict__ i
   return lo;
 }
 
-// Node rows per window of the work-sorted layout: the blocks of a window's
-// node rows keep their slots' range, sorted inside it.  One row: lanes of a
-// slice stay on neighbouring rows, whose blocks share cells (their pair
-// blocks hit L1) and whose values are written side by side; wider windows
-// measured slower (cfg3, 384k cells: 1.71 ms at 1 row, 1.74 at 8, 1.86 at
-// 64, 1.90 at 512, 1.80 unsorted).
-constexpr int64_t kWindowRows = 1;
+// The node blocks' layout: node rows in blocks of kBlockRows (the upper
+// lists' row-block layout: each block's diagonal node blocks, then its
+// others, so a cell's pair blocks are read in one sweep), and inside each
+// block the diagonal node blocks, then each row's others, sorted by
+// descending list length x terms -- the lanes of a slice carry about the
+// same FP64 work and stay on neighbouring rows, whose node blocks share cells
+// (their pair blocks hit L1) and whose values are written side by side.
+// Sorting across rows evens the work further but loses that locality
+// (measured at 384k cells: 1.71 ms per step sorting within each row, 1.74 /
+// 1.86 / 1.90 ms across 8 / 64 / 512 rows, 1.80 ms unsorted).
+constexpr int64_t kBlockRows = 512;
 
 // Per node block u (natural order): its list length and the sort key of
-// the work-sorted layout -- (segment << 32) | ~(length x terms), segments
-// the windows' diagonal ranges, then their off-diagonal ranges.
+// the work-sorted layout -- (segment << 32) | ~(length x terms); segment
+// (b, 0) for row block b's diagonal node blocks, (b, 1 + r) for row r's
+// others (r counted in the block): the natural order's ranges.
 __global__ void block_work_kernel(const int32_t* __restrict__ slice_len,
                                   const int32_t* __restrict__ slice_base,
                                   const uint32_t* __restrict__ codes,
-                                  const int32_t* __restrict__ urow, int64_t nupper, int64_t nd,
-                                  int64_t nwin, const int32_t* __restrict__ count, int npairs,
+                                  const int32_t* __restrict__ urow,
+                                  const int32_t* __restrict__ utpos, int64_t nupper,
+                                  const int32_t* __restrict__ count, int npairs,
                                   int32_t* __restrict__ len, unsigned long long* __restrict__ key,
                                   int32_t* __restrict__ ident) {
   const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -170,8 +178,11 @@ __global__ void block_work_kernel(const int32_t* __restrict__ slice_len,
     nt = ij < npairs ? max(1, count[ij]) : 1;
   }
   len[u] = n;
-  const int64_t w = urow[u] / kWindowRows;
-  const unsigned long long seg = (unsigned long long)(u < nd ? w : nwin + w);
+  const int64_t row = urow[u];
+  const int64_t b = row / kBlockRows;
+  const bool diag = utpos[u] < 0;
+  const unsigned long long seg =
+      (unsigned long long)(b * (kBlockRows + 1) + (diag ? 0 : 1 + (row - b * kBlockRows)));
   const unsigned long long work = (unsigned long long)n * (unsigned long long)nt;
   key[u] = (seg << 32) | (0xFFFFFFFFull - (work > 0xFFFFFFFFull ? 0xFFFFFFFFull : work));
   ident[u] = (int32_t)u;
@@ -225,6 +236,7 @@ __global__ void vec_block_pos_kernel(const int32_t* __restrict__ perm,
   const int64_t b0 = perm[u];
   const int64_t I = urow[b0];
   const int64_t J = nindices[upos[b0]];
+  const bool off = I != J;
   unsigned mask = 0, maskT = 0;
   for (int a = 0; a < dim; ++a) {
     const int64_t r = dim * I + a;
@@ -237,7 +249,7 @@ __global__ void vec_block_pos_kernel(const int32_t* __restrict__ perm,
         ++p;
       }
   }
-  if (u >= nd) {
+  if (off) {
     for (int b = 0; b < dim; ++b) {
       const int64_t r = dim * J + b;
       int32_t p = row_lower_bound(indptr, indices, r, (int32_t)(dim * I));
@@ -253,7 +265,7 @@ __global__ void vec_block_pos_kernel(const int32_t* __restrict__ perm,
   } else {
     for (int b = 0; b < dim; ++b) vposT[b * nupper + u] = -1;
   }
-  vmask[u] = (uint16_t)mask;
+  vmask[u] = (uint16_t)(mask | (off ? kOffDiagBit : 0u));
 }
 
 // The sum.  MASS: add m_e |det| / d! * MM[i][j] on the block diagonals.
@@ -359,7 +371,7 @@ __global__ void __launch_bounds__(128) vec_upper_kernel(
         for (int b = 0; b < D; ++b)
           if ((mk >> (a * D + b)) & 1u) vals[pos++] = acc[a * D + b];
       }
-      if (u >= nd) {
+      if (mk & kOffDiagBit) {
 #pragma unroll
         for (int b = 0; b < D; ++b) {
           int32_t pos = vposT[b * nupper + u];
@@ -433,7 +445,7 @@ __global__ void __launch_bounds__(128) vec_upper_coop_kernel(
     if ((mk >> q) & 1u) {
       const unsigned row = (mk >> (a * D)) & ((1u << D) - 1u);
       vals[vpos[a * nupper + u] + __popc(row & ((1u << b) - 1u))] = acc;
-      if (u >= nd) {
+      if (mk & kOffDiagBit) {
         unsigned col = 0;
 #pragma unroll
         for (int a2 = 0; a2 < D; ++a2) col |= ((mk >> (a2 * D + b)) & 1u) << a2;
@@ -500,7 +512,7 @@ int build_vec_upper(const Pattern& P, const int32_t* udofs, int family, int dim,
   }
   rc = build_incidence(node, nelems, ns, nnodes, &N, st);
   if (!rc) rc = build_csr(node, ns, nnodes, nullptr, &N, st);
-  if (!rc) rc = build_upper_lists(N, &V->U, st, /*wide=*/true);
+  if (!rc) rc = build_upper_lists(N, &V->U, st, /*wide=*/true, kBlockRows);
   if (rc) {
     free_pattern(new Pattern(N));   // releases N's device arrays
     return fail(rc);
@@ -534,7 +546,6 @@ int build_vec_upper(const Pattern& P, const int32_t* udofs, int family, int dim,
   // perm[slot] = the block's natural index; a window's slots stay its range.
   int32_t* perm = nullptr;
   if (nu > 0) {
-    const int64_t nwin = ceil_div(nnodes, kWindowRows);
     int32_t *len = nullptr, *ident = nullptr;
     unsigned long long *key = nullptr, *key2 = nullptr;
     e = scratch.alloc(&len, nu * sizeof(int32_t));
@@ -544,7 +555,7 @@ int build_vec_upper(const Pattern& P, const int32_t* udofs, int family, int dim,
     if (e == cudaSuccess) e = scratch.alloc(&key2, nu * sizeof(unsigned long long));
     if (e == cudaSuccess) {
       block_work_kernel<<<(unsigned)ceil_div(nu, 256), 256, 0, st>>>(
-          V->U.slice_len, V->U.slice_base, V->U.codes, V->U.row, nu, V->U.nd, nwin, V->count,
+          V->U.slice_len, V->U.slice_base, V->U.codes, V->U.row, V->U.tpos, nu, V->count,
           ns * ns, len, key, ident);
       e = cudaGetLastError();
     }
@@ -621,7 +632,7 @@ int build_vec_upper(const Pattern& P, const int32_t* udofs, int family, int dim,
   return 0;
 }
 
-int64_t vec_window_rows(const VecUpper& V) { return kWindowRows * V.dim; }
+int64_t vec_window_rows(const VecUpper& V) { return kBlockRows * V.dim; }
 
 int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, cudaStream_t st,
                   int64_t row0, int64_t row1, bool coop) {
@@ -632,17 +643,15 @@ int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, c
   int64_t n0 = row0 < 0 ? 0 : row0 / V.dim;
   int64_t n1 = (row1 < 0 || row1 / V.dim > nnodes) ? nnodes : row1 / V.dim;
   if (n1 <= n0) return 0;
-  if ((n0 % kWindowRows) || ((n1 % kWindowRows) && n1 != nnodes)) {
-    set_error(FEM_ERR_ARGUMENT, "vector one-pass rows [%lld, %lld) off the %lld-row windows",
-              (long long)row0, (long long)row1, (long long)(kWindowRows * V.dim));
+  if ((n0 % kBlockRows) || ((n1 % kBlockRows) && n1 != nnodes)) {
+    set_error(FEM_ERR_ARGUMENT, "vector one-pass rows [%lld, %lld) off the %lld-row blocks",
+              (long long)row0, (long long)row1, (long long)(kBlockRows * V.dim));
     return FEM_ERR_ARGUMENT;
   }
-  const bool all = n0 == 0 && n1 == nnodes;
-  // the node rows' diagonal blocks and their blocks above the diagonal
-  // (every node row: the two ranges are adjacent, one launch)
+  // the node rows' blocks: one range of the row-block layout
   const int64_t ranges[2][2] = {
-      {all ? 0 : V.U.dpos_h[n0], all ? V.U.nupper : V.U.dpos_h[n1]},
-      {all ? 0 : V.U.nd + V.U.opos_h[n0], all ? 0 : V.U.nd + V.U.opos_h[n1]}};
+      {(int64_t)V.U.dpos_h[n0] + V.U.opos_h[n0], (int64_t)V.U.dpos_h[n1] + V.U.opos_h[n1]},
+      {0, 0}};
   const int threads = 128;
   for (int k = 0; k < 2; ++k) {
     const int64_t ua = ranges[k][0], ub = ranges[k][1];
