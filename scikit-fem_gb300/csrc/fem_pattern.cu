@@ -776,11 +776,21 @@ __device__ __forceinline__ void upper_slice(
     if constexpr (MFIELD) {
       mc = moff;
     } else {
-      const double unit = dfrombits((unsigned long long)(mb - 1075 + 1023) << 52);
-      mc = (mscale * moff) * unit;
+      // mcoef * 2^(mb - 1075) (mcoef = mscale * moff): a power-of-two scaling,
+      // done on the exponent field (integer pipes) while the result stays
+      // normal -- the same value as the FP64 product
+      const double mcoef = mscale * moff;
+      const unsigned long long cb = dbits(mcoef);
+      const int sh = mb - 1075;
+      const int ex = (int)((cb >> 52) & 0x7ffu) + sh;
+      if (ex >= 1 && ex <= 2046 && ((cb >> 52) & 0x7ffu) != 0u)
+        mc = dfrombits(cb + ((unsigned long long)(long long)sh << 52));
+      else
+        mc = mcoef * dfrombits((unsigned long long)(sh + 1023) << 52);
     }
     const double m = MFIELD ? (double)accm : __ll2double_rn((long long)accm);
-    const double val = __fma_rn(mc, m, kscale * acck);
+    if (kscale != 1.0) acck = kscale * acck;
+    const double val = __fma_rn(mc, m, acck);
     vals[pos[u]] = val;
     const int32_t t = tpos[u];
     if (t >= 0) vals[t] = val;
