@@ -700,17 +700,45 @@ __global__ void __launch_bounds__(kBlock) hex_scalar_kernel(FemMesh m, FemBiline
   int64_t* cid = cells ? reinterpret_cast<int64_t*>(smem + (size_t)kBlock * (L + 1)) : nullptr;
   const int64_t e0 = ebeg + (int64_t)blockIdx.x * kBlock;
   int32_t flags = 0;
-  if (e0 + threadIdx.x < eend) {
-    const int64_t e = cell_at(cells, e0 + threadIdx.x);
+  const bool live = e0 + threadIdx.x < eend;
+  int64_t e = 0;
+  Hex h;
+  double J[3][3];
+  bool affine = true;
+  if (live) {
+    e = cell_at(cells, e0 + threadIdx.x);
+    hex_load(m, e, h);
+    affine = hex_affine(h, J);
+  }
+  // the reference element's values and gradients at the 64 points and the
+  // points' weights, once per block that holds a general cell (every cell
+  // reads them: broadcasts)
+  double* tab = smem + (size_t)kBlock * (L + 1) + kBlock;   // after the rows and the cell ids
+  double* sphi = tab;                 // [64][8]
+  double* sdphi = tab + 64 * 8;       // [64][8][3]
+  double* sw = tab + 64 * 32;         // [64]
+  if (__syncthreads_or(affine ? 0 : 1)) {
+    for (int q = threadIdx.x; q < 64; q += blockDim.x) {
+      const int qx = q & 3, qy = (q >> 2) & 3, qz = q >> 4;
+      double phi[8], dphi[8][3];
+      hex_shape(c_gl4_x[qx], c_gl4_x[qy], c_gl4_x[qz], phi, dphi);
+#pragma unroll
+      for (int n = 0; n < 8; ++n) {
+        sphi[q * 8 + n] = phi[n];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) sdphi[(q * 8 + n) * 3 + k] = dphi[n][k];
+      }
+      sw[q] = c_gl4_w[qx] * c_gl4_w[qy] * c_gl4_w[qz];
+    }
+    __syncthreads();
+  }
+  if (live) {
     if (cid) cid[threadIdx.x] = e;
     const int rb = ref_byte(ref_bits, e);
-    Hex h;
-    hex_load(m, e, h);
     const double kd = coef_at(f.diff, e);
     const double km = coef_at(f.mass, e);
     double* row = smem + threadIdx.x * (L + 1);
-    double J[3][3];
-    if (hex_affine(h, J)) {
+    if (affine) {
       double ad[3][3];
       const double det = adj3(J, ad);
       if (fem::zero_bits(det)) flags |= 1 << FEM_ERR_ZERO_JACOBIAN;
@@ -733,15 +761,12 @@ __global__ void __launch_bounds__(kBlock) hex_scalar_kernel(FemMesh m, FemBiline
     } else {
 #pragma unroll
       for (int k = 0; k < 64; ++k) row[k] = 0.0;
+      const bool mass = !fem::zero_bits(km);
 #pragma unroll 1
-      for (int qz = 0; qz < 4; ++qz)
-#pragma unroll 1
-        for (int qy = 0; qy < 4; ++qy)
-#pragma unroll 1
-          for (int qx = 0; qx < 4; ++qx) {
-            double phi[8], dphi[8][3];
-            hex_shape(c_gl4_x[qx], c_gl4_x[qy], c_gl4_x[qz], phi, dphi);
-            const double w = c_gl4_w[qx] * c_gl4_w[qy] * c_gl4_w[qz];
+      for (int q = 0; q < 64; ++q) {
+            const double* phi = sphi + q * 8;
+            const double (*dphi)[3] = reinterpret_cast<const double (*)[3]>(sdphi + q * 24);
+            const double w = sw[q];
             double Jq[3][3];
 #pragma unroll
             for (int a = 0; a < 3; ++a)
@@ -767,15 +792,25 @@ __global__ void __launch_bounds__(kBlock) hex_scalar_kernel(FemMesh m, FemBiline
 #pragma unroll
               for (int k = 0; k < 3; ++k)
                 hv[i][k] = M[k][0] * dphi[i][0] + M[k][1] * dphi[i][1] + M[k][2] * dphi[i][2];
+            if (mass) {
 #pragma unroll
-            for (int i = 0; i < 8; ++i)
+              for (int i = 0; i < 8; ++i)
 #pragma unroll
-              for (int j = i; j < 8; ++j) {
-                const double v = hv[i][0] * dphi[j][0] + hv[i][1] * dphi[j][1] +
-                                 hv[i][2] * dphi[j][2] + sm * (phi[i] * phi[j]);
-                row[i * 8 + j] += v;
-              }
-          }
+                for (int j = i; j < 8; ++j) {
+                  const double v = hv[i][0] * dphi[j][0] + hv[i][1] * dphi[j][1] +
+                                   hv[i][2] * dphi[j][2] + sm * (phi[i] * phi[j]);
+                  row[i * 8 + j] += v;
+                }
+            } else {
+              // no mass term (a zero mass coefficient): the stiffness alone
+#pragma unroll
+              for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = i; j < 8; ++j)
+                  row[i * 8 + j] += hv[i][0] * dphi[j][0] + hv[i][1] * dphi[j][1] +
+                                    hv[i][2] * dphi[j][2];
+            }
+      }
 #pragma unroll
       for (int i = 0; i < 8; ++i)
 #pragma unroll
@@ -985,7 +1020,8 @@ int local_matrices_checked(const FemMesh& m, const FemBasis& b, const FemBilinea
       case FEM_TET_P1: rc = launch_scalar_tuned<3, 1>(m, f, out, ref_bits, status, st, ebeg, eend, cells, geo); break;
       case FEM_TET_P2: rc = launch_scalar_tuned<3, 2>(m, f, out, ref_bits, status, st, ebeg, eend, cells, geo); break;
       case FEM_HEX_1: {
-        const size_t sm = (size_t)kBlock * 65 * sizeof(double) + (cells ? kCidBytes<kBlock> : 0);
+        // the rows, room for the cell ids, the 64 points' tables
+        const size_t sm = ((size_t)kBlock * 65 + kBlock + 64 * 33) * sizeof(double);
         if ((rc = set_smem(hex_scalar_kernel, sm))) return rc;
         hex_scalar_kernel<<<(unsigned)grid, kBlock, sm, st>>>(m, f, out, ref_bits, status, cells,
                                                               ebeg, eend);

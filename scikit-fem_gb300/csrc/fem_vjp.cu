@@ -510,12 +510,14 @@ __device__ __forceinline__ void hex_vjp_affine(const double x[8][3], const doubl
 
 // Non-parallelepiped cells: the 4x4x4 isoparametric rule (kept out of line
 // so that its registers do not load the common parallelepiped path).
+// tab: the reference element's values [64][8], gradients [64][8][3] and the
+// points' weights [64] (shared memory, filled once per block).
 template <int MODE>
 __device__ __noinline__ void hex_vjp_general(const FemMesh m, const FemBasis b, const FemCoef cd,
                                              const FemCoef cm, const double* __restrict__ w,
                                              const double* __restrict__ u, double* dcd,
                                              double* dcm, double* scratch, int32_t* status,
-                                             int64_t e) {
+                                             int64_t e, const double* tab) {
   const int nq = 4;
   double x[8][3], wl[8], ul[8];
 #pragma unroll
@@ -534,13 +536,12 @@ __device__ __noinline__ void hex_vjp_general(const FemMesh m, const FemBasis b, 
   for (int n = 0; n < 8; ++n)
 #pragma unroll
     for (int k = 0; k < 3; ++k) gx[n][k] = 0.0;
+  // the mass channel's terms only when it is present or its gradient is asked for
+  const bool mass = MODE == 0 && (dcm != nullptr || !fem::zero_bits(km));
   for (int q = 0; q < nq * nq * nq; ++q) {
-    const int qx = q % nq, qy = (q / nq) % nq, qz = q / (nq * nq);
-    const double* xs = c_gl4_x;
-    const double* ws = c_gl4_w;
-    double phi[8], dphi[8][3];
-    hex_shape(xs[qx], xs[qy], xs[qz], phi, dphi);
-    const double wq = ws[qx] * ws[qy] * ws[qz];
+    const double* phi = tab + q * 8;
+    const double (*dphi)[3] = reinterpret_cast<const double (*)[3]>(tab + 64 * 8 + q * 24);
+    const double wq = tab[64 * 32 + q];
     double J[3][3];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
@@ -566,8 +567,8 @@ __device__ __noinline__ void hex_vjp_general(const FemMesh m, const FemBasis b, 
     double ar[3] = {0, 0, 0}, br[3] = {0, 0, 0}, wv = 0.0, uv = 0.0;
 #pragma unroll
     for (int n = 0; n < 8; ++n) {
-      wv += wl[n] * phi[n];
-      uv += ul[n] * phi[n];
+      if (mass || MODE == 1) wv += wl[n] * phi[n];
+      if (mass) uv += ul[n] * phi[n];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         ar[k] += wl[n] * dphi[n][k];
@@ -591,8 +592,13 @@ __device__ __noinline__ void hex_vjp_general(const FemMesh m, const FemBasis b, 
       const double s = ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2];
       const double cdf = wq * adet;
       Ed += cdf * s;
-      Em += cdf * wv * uv;
-      const double c0 = cdf * (kd * s + km * wv * uv);
+      double c0;
+      if (mass) {
+        Em += cdf * wv * uv;
+        c0 = cdf * (kd * s + km * wv * uv);
+      } else {
+        c0 = cdf * (kd * s);
+      }
 #pragma unroll
       for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -628,29 +634,50 @@ __global__ void hex_vjp_kernel(FemMesh m, FemBasis b, FemCoef cd, FemCoef cm,
                                double* __restrict__ dcd, double* __restrict__ dcm,
                                double* __restrict__ scratch, int32_t* __restrict__ status) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= m.nelems) return;
+  const bool live = e < m.nelems;
   double x[8][3], wl[8], ul[8];
-#pragma unroll
-  for (int n = 0; n < 8; ++n) {
-    const int64_t v = m.t[n * m.nelems + e];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) x[n][k] = m.p[k * m.nverts + v];
-    const int64_t dof = b.element_dofs[n * m.nelems + e];
-    wl[n] = w[dof];
-    ul[n] = MODE == 0 ? u[dof] : 0.0;
-  }
-  // parallelepiped test (as the forward kernel)
   bool affine = true;
+  if (live) {
 #pragma unroll
-  for (int n = 0; n < 8; ++n)
+    for (int n = 0; n < 8; ++n) {
+      const int64_t v = m.t[n * m.nelems + e];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      double v = x[7][k];
-      if (hex_corner(n, 0)) v = v + (x[4][k] - x[7][k]);
-      if (hex_corner(n, 1)) v = v + (x[5][k] - x[7][k]);
-      if (hex_corner(n, 2)) v = v + (x[6][k] - x[7][k]);
-      affine = affine && (v == x[n][k]);
+      for (int k = 0; k < 3; ++k) x[n][k] = m.p[k * m.nverts + v];
+      const int64_t dof = b.element_dofs[n * m.nelems + e];
+      wl[n] = w[dof];
+      ul[n] = MODE == 0 ? u[dof] : 0.0;
     }
+    // parallelepiped test (as the forward kernel)
+#pragma unroll
+    for (int n = 0; n < 8; ++n)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        double v = x[7][k];
+        if (hex_corner(n, 0)) v = v + (x[4][k] - x[7][k]);
+        if (hex_corner(n, 1)) v = v + (x[5][k] - x[7][k]);
+        if (hex_corner(n, 2)) v = v + (x[6][k] - x[7][k]);
+        affine = affine && (v == x[n][k]);
+      }
+  }
+  // the reference element at the 64 points, once per block that holds a
+  // general cell (their 4x4x4 rule)
+  __shared__ double tab[64 * 33];
+  if (__syncthreads_or(affine ? 0 : 1)) {
+    for (int q = threadIdx.x; q < 64; q += blockDim.x) {
+      const int qx = q & 3, qy = (q >> 2) & 3, qz = q >> 4;
+      double phi[8], dphi[8][3];
+      hex_shape(c_gl4_x[qx], c_gl4_x[qy], c_gl4_x[qz], phi, dphi);
+#pragma unroll
+      for (int n = 0; n < 8; ++n) {
+        tab[q * 8 + n] = phi[n];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) tab[64 * 8 + (q * 8 + n) * 3 + k] = dphi[n][k];
+      }
+      tab[64 * 32 + q] = c_gl4_w[qx] * c_gl4_w[qy] * c_gl4_w[qz];
+    }
+    __syncthreads();
+  }
+  if (!live) return;
   const double kd = coef_at(cd, e), km = MODE == 0 ? coef_at(cm, e) : 0.0;
   double Ed = 0.0, Em = 0.0;
   double gx[8][3];
@@ -659,7 +686,7 @@ __global__ void hex_vjp_kernel(FemMesh m, FemBasis b, FemCoef cd, FemCoef cm,
 #pragma unroll
     for (int k = 0; k < 3; ++k) gx[n][k] = 0.0;
   if (!affine) {
-    hex_vjp_general<MODE>(m, b, cd, cm, w, u, dcd, dcm, scratch, status, e);
+    hex_vjp_general<MODE>(m, b, cd, cm, w, u, dcd, dcm, scratch, status, e, tab);
     return;
   }
   hex_vjp_affine<MODE>(x, wl, ul, kd, km, Ed, Em, gx, status);
