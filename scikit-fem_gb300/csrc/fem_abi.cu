@@ -709,15 +709,28 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
   }
   if (geometry_sum(pat, mesh, basis, form)) {
     // the coefficient checks, then the one-pass P1 assembly over the
-    // cached geometry (the form contracted per cell row as the rows sum)
-    rc = fem_fast::coef_checks(*form, pat->coef_bits, status, st, 0, mesh->nelems, nullptr);
-    if (rc) return rc;
+    // cached geometry (the form contracted per cell row as the rows sum);
+    // the plain upper form checks the coefficients itself where it can
     fem::Pattern P = pat->P;
     const fem::Tuning t = fem::tuning_for(basis->family);
     P.sum_unroll = t.sum_unroll;
-    if (t.onepass >= 1 && pat->upper_ok)
+    const bool upper = t.onepass >= 1 && pat->upper_ok;
+    const bool folded = upper && status && pat->coef_bits &&
+                        fem::upper_p1_checks(form->diff, form->mass, t.onepass == 2);
+    if (!folded) {
+      rc = fem_fast::coef_checks(*form, pat->coef_bits, status, st, 0, mesh->nelems, nullptr);
+      if (rc) return rc;
+    }
+    if (upper) {
+      // the zero bits of the channels without a field (as coef_fields_kernel)
+      int const_bits = form->diff.scale == 0.0 ? 1 : 0;
+      const FemCoef* rest[4] = {&form->mass, &form->lam, &form->lap, &form->tr};
+      for (int k = 0; k < 4; ++k)
+        if (!rest[k]->field && rest[k]->scale == 0.0) const_bits |= 1 << (k + 1);
       return fem::csr_sum_upper_p1(P, pat->upper, mesh->dim, pat->geo, form->diff, form->mass,
-                                   pat->mbase, csr_values, st, 0, -1, status, t.onepass == 2);
+                                   pat->mbase, csr_values, st, 0, -1, status, t.onepass == 2,
+                                   folded ? pat->coef_bits : nullptr, const_bits);
+    }
     return fem::csr_sum_geometry_p1(P, mesh->dim, pat->geo, form->diff, form->mass, pat->mbase,
                                     csr_values, st);
   }

@@ -245,10 +245,19 @@ constexpr int64_t kUpperBlockRows = 4096;
 void free_upper_lists(UpperLists* U);
 // tma: stage each warp's slice codes in shared memory with bulk copies
 // (needs status for its bounded waits' error bit)
+// ref_bits / const_bits: the coefficient checks folded into the plain form
+// (a per-cell stiffness field of stride 1 and a nonzero constant mass; the
+// cells' zero bits against the pattern's, FEM_ERR_STALE_PATTERN in *status)
 int csr_sum_upper_p1(const Pattern& P, const UpperLists& U, int dim, const double* geo,
                      const FemCoef& diff, const FemCoef& mass, const int16_t* mbase, double* vals,
                      cudaStream_t st, int64_t row0 = 0, int64_t row1 = -1,
-                     int32_t* status = nullptr, bool tma = false);
+                     int32_t* status = nullptr, bool tma = false,
+                     const uint8_t* ref_bits = nullptr, int const_bits = 0);
+// True when csr_sum_upper_p1 checks the coefficients itself for this form
+// (the plain form, not TMA-staged)
+inline bool upper_p1_checks(const FemCoef& diff, const FemCoef& mass, bool tma) {
+  return !tma && diff.field && diff.stride <= 1 && !mass.field && mass.scale != 0.0;
+}
 
 int basis_nb_scalar(int family);
 int basis_dim(int family);

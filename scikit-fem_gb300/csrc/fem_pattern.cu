@@ -515,6 +515,9 @@ __device__ __forceinline__ long long fixed_of(double x, int base) {
   return sh >= 0 ? (long long)(man << sh) : (long long)(man >> min(-sh, 63));
 }
 
+// x == 0.0 of either sign, on the integer pipes.
+__device__ __forceinline__ bool fem_zero(double x) { return (dbits(x) << 1) == 0ull; }
+
 // Packed symmetric index of Gram entry (a, b) (row-major upper triangle).
 __host__ __device__ constexpr int gram_index(int nu, int a, int b) {
   return a <= b ? a * (2 * nu + 1 - a) / 2 + b - a : b * (2 * nu + 1 - b) / 2 + a - b;
@@ -715,14 +718,21 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long l
 }
 
 // One slice of upper entries: lane `lane` walks codes cp[p * 32], p < len.
-template <int NU, int U, bool MFIELD, bool SMEM>
+// CHECK (a per-cell stiffness field of stride 1, a nonzero constant mass):
+// the coefficient checks ride along -- at each cell's contribution of Gram
+// entry 0 (its local diagonal (0, 0), which the mass keeps in every list)
+// the cell's zero bits, const_bits | (k_e == 0), are compared with the
+// pattern's ref_bits[e]; a difference sets FEM_ERR_STALE_PATTERN in *stale.
+template <int NU, int U, bool MFIELD, bool SMEM, bool CHECK = false>
 __device__ __forceinline__ void upper_slice(
     const uint32_t* __restrict__ cp, int len, int64_t u, bool live,
     const int32_t* __restrict__ pos, const int32_t* __restrict__ tpos,
     const int32_t* __restrict__ urow, const double* __restrict__ geo, int64_t nelems,
     const double* __restrict__ kfield, int64_t kstride, double kscale,
     const double* __restrict__ mfield, int64_t mstride, double mscale, double moff,
-    const int16_t* __restrict__ mbase, double* __restrict__ vals) {
+    const int16_t* __restrict__ mbase, double* __restrict__ vals,
+    const uint8_t* __restrict__ ref_bits = nullptr, int const_bits = 0,
+    int32_t* stale = nullptr) {
   constexpr int NG = NU * (NU + 1) / 2;
   using MAcc = typename std::conditional<MFIELD, double, long long>::type;
   const double* __restrict__ adet_arr = geo + (int64_t)NG * nelems;
@@ -758,6 +768,12 @@ __device__ __forceinline__ void upper_slice(
         const bool diag = (kGramDiag<NU> >> gk) & 1u;
         kv[v] = kfield ? __ldg(kfield + (int64_t)e * kstride) : 1.0;
         g[v] = __ldg(geo + (int64_t)gk * nelems + e);
+        if constexpr (CHECK) {
+          if (gk == 0) {
+            const int bits = const_bits | (fem_zero(kv[v]) ? 1 : 0);
+            if (bits != (int)__ldg(ref_bits + e)) *stale = 1 << FEM_ERR_STALE_PATTERN;
+          }
+        }
         const double adet = __ldg(adet_arr + e);
         MAcc m;
         if constexpr (MFIELD) m = __ldg(mfield + (int64_t)e * mstride) * adet;
@@ -797,7 +813,7 @@ __device__ __forceinline__ void upper_slice(
   }
 }
 
-template <int NU, int U, bool MFIELD>
+template <int NU, int U, bool MFIELD, bool CHECK = false>
 __global__ void __launch_bounds__(128) csr_upper_p1_kernel(
     int64_t ua, int64_t ub, const int32_t* __restrict__ slice_len,
     const int32_t* __restrict__ slice_base, const uint32_t* __restrict__ codes,
@@ -805,17 +821,22 @@ __global__ void __launch_bounds__(128) csr_upper_p1_kernel(
     const int32_t* __restrict__ urow, const double* __restrict__ geo, int64_t nelems,
     const double* __restrict__ kfield, int64_t kstride, double kscale,
     const double* __restrict__ mfield, int64_t mstride, double mscale, double moff,
-    const int16_t* __restrict__ mbase, double* __restrict__ vals) {
+    const int16_t* __restrict__ mbase, double* __restrict__ vals,
+    const uint8_t* __restrict__ ref_bits = nullptr, int const_bits = 0,
+    int32_t* __restrict__ status = nullptr) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   const int64_t s0 = ua >> 5, s1 = (ub + 31) >> 5;
+  int32_t stale = 0;
   for (int64_t sl = s0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); sl < s1;
        sl += warps) {
     const int64_t u = sl * 32 + lane;
-    upper_slice<NU, U, MFIELD, false>(codes + (int64_t)slice_base[sl] * 32 + lane, slice_len[sl],
-                                      u, u >= ua && u < ub, pos, tpos, urow, geo, nelems, kfield,
-                                      kstride, kscale, mfield, mstride, mscale, moff, mbase, vals);
+    upper_slice<NU, U, MFIELD, false, CHECK>(
+        codes + (int64_t)slice_base[sl] * 32 + lane, slice_len[sl], u, u >= ua && u < ub, pos,
+        tpos, urow, geo, nelems, kfield, kstride, kscale, mfield, mstride, mscale, moff, mbase,
+        vals, ref_bits, const_bits, &stale);
   }
+  if constexpr (CHECK) fem::publish_status(status, stale);
 }
 
 // The same sum with each warp's slice codes staged in shared memory by the
@@ -1758,7 +1779,8 @@ void free_upper_lists(UpperLists* U) {
 
 int csr_sum_upper_p1(const Pattern& P, const UpperLists& U, int dim, const double* geo,
                      const FemCoef& diff, const FemCoef& mass, const int16_t* mbase, double* vals,
-                     cudaStream_t st, int64_t row0, int64_t row1, int32_t* status, bool tma) {
+                     cudaStream_t st, int64_t row0, int64_t row1, int32_t* status, bool tma,
+                     const uint8_t* ref_bits, int const_bits) {
   const int nu = dim + 1;
   if (!U.codes || P.nbfun_u != nu || (dim != 2 && dim != 3)) {
     set_error(FEM_ERR_ARGUMENT, "the upper-gather P1 sum needs the pattern's upper lists");
@@ -1806,8 +1828,9 @@ int csr_sum_upper_p1(const Pattern& P, const UpperLists& U, int dim, const doubl
     auto launch = [&](auto kern) {
       kern<<<grid, threads, 0, st>>>(ua, ub, U.slice_len, U.slice_base, U.codes, U.pos, U.tpos,
                                      U.row, geo, P.nelems, kf, ks, diff.scale, mf, ms, mass.scale,
-                                     moff, mbase, vals);
+                                     moff, mbase, vals, ref_bits, const_bits, status);
     };
+    const bool check = ref_bits && status && kf && ks == 1 && !mf && mass.scale != 0.0;
     auto launch_tma = [&](auto kern) -> int {
       if (tma_smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1826,6 +1849,7 @@ int csr_sum_upper_p1(const Pattern& P, const UpperLists& U, int dim, const doubl
       if (mf) rc = Un == 8 ? launch_tma(csr_upper_p1_tma_kernel<NU, 8, true>) : launch_tma(csr_upper_p1_tma_kernel<NU, 4, true>); \
       else rc = Un == 8 ? launch_tma(csr_upper_p1_tma_kernel<NU, 8, false>) : launch_tma(csr_upper_p1_tma_kernel<NU, 4, false>); \
     } else if (mf) { if (Un == 8) launch(csr_upper_p1_kernel<NU, 8, true>); else launch(csr_upper_p1_kernel<NU, 4, true>); } \
+    else if (check) { if (Un == 8) launch(csr_upper_p1_kernel<NU, 8, false, true>); else launch(csr_upper_p1_kernel<NU, 4, false, true>); } \
     else { if (Un == 8) launch(csr_upper_p1_kernel<NU, 8, false>); else launch(csr_upper_p1_kernel<NU, 4, false>); }
     if (nu == 4) { FEM_UP_PICK(4) }
     else { FEM_UP_PICK(3) }
