@@ -64,6 +64,11 @@ FUSED_B_PER_CELL = 218.5
 # blocks (geometry ~70, E ~250) and the node blocks' reference-tensor terms
 # (1,194 FMAs for the 55 blocks on and above the block diagonal)
 VEC_TETP2_FP64_PER_CELL = 70 + 250 + 1194
+# FP64 operations per cell of the one-pass scalar TetP2 k*Laplace + mass: the
+# pair values (10 products of k and the cached Gram entries, 2 for the mass
+# scale) and the CSR entries' reference-tensor terms (136 FMAs for the 55
+# node pairs on and above the diagonal, symmetric terms merged) and mass (55)
+SCALAR_TETP2_FP64_PER_CELL = 12 + 136 + 55
 TRAFFIC_SOURCE = "ncu dram__bytes_read+write of one launch on the 1.3M-cell case, per cell"
 
 
@@ -538,8 +543,9 @@ def _abi_step(F, N, form, b, coefs):
 
 def secondary_workloads(args, only=None):
     """The other workloads of the assembly path, each timed on the device.
-    ``only`` restricts the run to one of tri_p1 / tet_p2_vec / hex1_vjp /
-    batched / generic (sizes from --vec-n, --hex-n, --batch, --generic-n)."""
+    ``only`` restricts the run to one of tri_p1 / tet_p2 / tet_p2_vec /
+    hex1_vjp / batched / generic (sizes from --p2-n, --vec-n, --hex-n, --batch,
+    --generic-n)."""
     want = (lambda name: only is None or only == name)
     import torch
 
@@ -614,6 +620,58 @@ def secondary_workloads(args, only=None):
             "pattern_build_s": build_s, "elements_per_s": m.nelements / (ms * 1e-3),
             "hbm_frac": B / (ms * 1e-3) / 1e9 / hbm, "algorithmic_bytes": B,
             "fp64_floor_ms": m.nelements * VEC_TETP2_FP64_PER_CELL / 0.598e12 * 1e3}
+        del step, entry, vals, b
+        torch.cuda.empty_cache()
+
+    if want('tet_p2'):
+        # plain scalar TetP2 k*Laplace + mass (the TetP1 workload's form and
+        # lognormal k at second order) on the 61^3-node cube, 1,296,000 cells
+        m, k = build_workload(args.p2_n)
+        b = F.Basis(m, F.ElementTetP2())
+        kd = torch.tensor(k, device="cuda")
+
+        @F.BilinearForm
+        def k_laplace_mass(u, v, w):
+            return w.k * H.dot(H.grad(u), H.grad(v)) + u * v
+
+        t0 = time.perf_counter()
+        step, entry, c_form, vals = _abi_step(F, N, k_laplace_mass, b, {"k": kd})
+        torch.cuda.synchronize()
+        build_s = time.perf_counter() - t0
+        ms = _time(step, 5)
+        first = vals.clone()
+        step()
+        torch.cuda.synchronize()
+        same = bool(torch.equal(first, vals))
+        fam = N.FAMILY["TetP2"]
+        try:
+            # the sum's flattened form (one FMA per step), bitwise the same values
+            lib.fem_set_onepass(fam, 2)
+            ms_flat = _time(step, 5)
+            flat_same = bool(torch.equal(first, vals))
+            # the two-pass path: local matrices into the staging, then the
+            # fixed-order segmented sum
+            lib.fem_set_onepass(fam, 0)
+            ms_two = _time(step, 3)
+            dev = float(((vals - first).abs().max() / first.abs().max()).item())
+            ms_local = _time(lambda: N.check(lib.fem_assemble_local(
+                N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form), entry.pat.handle,
+                N.ptr(entry.staging), None, 0, b.nelems, N.stream_ptr())), 3)
+        finally:
+            lib.fem_set_onepass(fam, 1)
+        B = m.nelements * (10 * 4 + 8) + m.p.size * 8 + entry.nnz * 8
+        out["tet_p2_k_laplace_mass_%d" % args.p2_n] = {
+            "nelems": m.nelements, "ndofs": b.N, "nnz": entry.nnz, "ms": ms,
+            "step": "one-pass node-block sum: per cell the 10 scaled Gram entries times k and "
+                    "the mass scale, then one lane per CSR entry on and above the diagonal "
+                    "contracting the reference tensor while it sums (no local matrices stored)",
+            "repeat_bitwise_equal": same,
+            "ms_onepass_flat": ms_flat, "flat_bitwise_equal": flat_same,
+            "ms_two_pass": ms_two, "ms_two_pass_local": ms_local,
+            "two_pass_vs_onepass_max_rel": dev,
+            "pattern_build_s": build_s, "elements_per_s": m.nelements / (ms * 1e-3),
+            "hbm_frac": B / (ms * 1e-3) / 1e9 / hbm, "algorithmic_bytes": B,
+            "fp64_floor_ms": m.nelements * SCALAR_TETP2_FP64_PER_CELL / 0.598e12 * 1e3}
         del step, entry, vals, b
         torch.cuda.empty_cache()
 
@@ -891,6 +949,8 @@ def main():
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--batch", type=int, default=512, help="meshes of the batched workload")
     ap.add_argument("--vec-n", type=int, default=40, help="cells per axis, vector TetP2 workload")
+    ap.add_argument("--p2-n", type=int, default=61,
+                    help="nodes per axis, scalar TetP2 workload")
     ap.add_argument("--hex-n", type=int, default=64, help="cells per axis, Hex1 adjoint workload")
     ap.add_argument("--hex-jitter", type=float, nargs="+", default=[0.0, 0.2],
                     help="Hex1 workloads: interior-node jitter (fraction of h) of each case; "
@@ -898,7 +958,8 @@ def main():
     ap.add_argument("--generic-n", type=int, default=60,
                     help="cells per axis, generic-kernel TetP1 workload")
     ap.add_argument("--only", default=None,
-                    choices=["tri_p1", "tet_p2_vec", "hex1_vjp", "batched", "generic"],
+                    choices=["tri_p1", "tet_p2", "tet_p2_vec", "hex1_vjp", "batched",
+                             "generic"],
                     help="run one secondary workload alone and print its record")
     ap.add_argument("--onepass", type=int, default=None, choices=[0, 1, 2],
                     help="fix the one-pass sum's form after autotuning (default: the fastest)")

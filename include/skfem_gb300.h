@@ -234,6 +234,13 @@ int fem_set_tuning(int family, int local_block, int persistent, int sum_unroll, 
  * same with the D*D lanes of a block cooperating on its entries.  Variants
  * 1 and 2 are bitwise equal; the two-pass path agrees within 1e-14 of
  * max|K|.
+ * For scalar TriP2 / TetP2 bases (k dot(grad u, grad v) + m u v): 0 the
+ * two-pass path; 1 (the default) the same one-pass sum with 1 x 1 blocks,
+ * one lane per CSR entry on or above the diagonal (per cell the scaled
+ * Gram entries times k, and the mass scale, computed into the staging
+ * first); 2 the same with one FMA per step of the lane's loop.  Variants
+ * 1 and 2 are bitwise equal; the two-pass path agrees within 1e-14 of
+ * max|K|.
  */
 int fem_set_onepass(int family, int variant);
 

@@ -31,6 +31,11 @@ int local_vectors(const FemMesh&, const FemBasis&, const FemLinear&, double*, in
 // cell) of the cells [ebeg, eend) (of the list cells, when given)
 int vector_pair_blocks(const FemMesh&, const FemBasis&, const FemBilinear&, double*, cudaStream_t,
                        int64_t ebeg = 0, int64_t eend = -1, const int32_t* cells = nullptr);
+// the same for scalar TriP2 / TetP2 bases (geo: the pattern's geometry cache
+// of this mesh, or null)
+int scalar_pair_values(const FemMesh&, const FemBasis&, const FemBilinear&, const double* geo,
+                       double*, cudaStream_t, int64_t ebeg = 0, int64_t eend = -1,
+                       const int32_t* cells = nullptr);
 }  // namespace fem_fast
 namespace fem_exact {
 int local_matrices(const FemMesh&, const FemBasis&, const FemBilinear&, double*, int32_t*,
@@ -151,8 +156,9 @@ struct FemPattern {
   // first geometry cache of a scalar TriP1 / TetP1 pattern).
   fem::UpperLists upper;
   bool upper_ok = false, upper_tried = false;
-  // The one-pass vector sum's node-block lists (simplex ElementVector bases;
-  // pattern-only, built with the first fem_pattern_cache_geometry call).
+  // The one-pass node-block sum's lists (simplex ElementVector bases, scalar
+  // TriP2 / TetP2 bases; pattern-only, built with the first
+  // fem_pattern_cache_geometry call).
   fem::VecUpper vec;
   bool vec_ok = false, vec_tried = false;
 };
@@ -185,13 +191,25 @@ bool geometry_sum(const FemPattern* pat, const FemMesh* mesh, const FemBasis* ba
   return form->mass.field ? true : (pat->mbase && pat->mbase_ok);
 }
 
-// The one-pass vector sum applies: simplex ElementVector bases whose
-// pattern holds its lists, unless the family's tuning selects the two-pass
-// path (fem_set_onepass variant 0).
+// The one-pass node-block sum applies: simplex ElementVector bases and
+// scalar TriP2 / TetP2 bases whose pattern holds its lists, unless the
+// family's tuning selects the two-pass path (fem_set_onepass variant 0).
 bool vector_onepass(const FemPattern* pat, const FemMesh* mesh, const FemBasis* basis) {
-  if (!basis->vector || !pat->vec_ok || pat->vec.dim != mesh->dim) return false;
+  if (!pat->vec_ok || pat->vec.sdim != mesh->dim) return false;
+  if (pat->vec.dim != (basis->vector ? mesh->dim : 1)) return false;
   if (pat->P.nbfun_u != pat->P.nbfun_v || pat->P.nbfun_v != basis->nbfun) return false;
   return fem::tuning_for(basis->family).onepass >= 1;
+}
+
+// The per-cell pair values the one-pass node-block sum reads, cells
+// [ebeg, eend) (of the list cells, when given), into the staging.
+int node_pair_values(const FemPattern* pat, const FemMesh* mesh, const FemBasis* basis,
+                     const FemBilinear* form, double* staging, cudaStream_t st, int64_t ebeg = 0,
+                     int64_t eend = -1, const int32_t* cells = nullptr) {
+  if (basis->vector)
+    return fem_fast::vector_pair_blocks(*mesh, *basis, *form, staging, st, ebeg, eend, cells);
+  return fem_fast::scalar_pair_values(*mesh, *basis, *form, cached_geometry(pat, mesh), staging,
+                                      st, ebeg, eend, cells);
 }
 
 bool fused_sum(const FemPattern* pat, const FemMesh* mesh, const FemBasis* basis,
@@ -603,16 +621,20 @@ int fem_pattern_cache_geometry(FemPattern* pat, const FemMesh* mesh, const FemBa
     return FEM_ERR_ARGUMENT;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  if (basis->vector && !pat->vec_tried) {
-    // the one-pass vector sum's lists (pattern-only): an optimisation, left
-    // out (with its error cleared) when the pattern does not allow it or
-    // there is no room for them
+  const int fam = basis->family;
+  const bool node_blocks =
+      basis->vector ? (fam == FEM_TRI_P1 || fam == FEM_TRI_P2 || fam == FEM_TET_P1 ||
+                       fam == FEM_TET_P2)
+                    : (fam == FEM_TRI_P2 || fam == FEM_TET_P2);
+  if (node_blocks && !pat->vec_tried) {
+    // the one-pass node-block sum's lists (pattern-only): an optimisation,
+    // left out (with its error cleared) when the pattern does not allow it
+    // or there is no room for them
     pat->vec_tried = true;
     pat->vec_ok = false;
-    const int fam = basis->family;
-    if ((fam == FEM_TRI_P1 || fam == FEM_TRI_P2 || fam == FEM_TET_P1 || fam == FEM_TET_P2) &&
-        fem::basis_dim(fam) == mesh->dim) {
-      rc = fem::build_vec_upper(pat->P, basis->element_dofs, fam, mesh->dim, &pat->vec, st);
+    if (fem::basis_dim(fam) == mesh->dim) {
+      rc = fem::build_vec_upper(pat->P, basis->element_dofs, fam, basis->vector ? mesh->dim : 1,
+                                &pat->vec, st);
       pat->vec_ok = rc == 0;
       if (rc) {
         cudaGetLastError();
@@ -739,7 +761,7 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
     // the one-pass vector sum contracting and summing the node blocks
     rc = fem_fast::coef_checks(*form, pat->coef_bits, status, st, 0, mesh->nelems, nullptr);
     if (rc) return rc;
-    rc = fem_fast::vector_pair_blocks(*mesh, *basis, *form, staging, st);
+    rc = node_pair_values(pat, mesh, basis, form, staging, st);
     if (rc) return rc;
     const bool mass = form->mass.field || form->mass.scale != 0.0;
     return fem::vec_upper_sum(pat->vec, staging, mass, csr_values, st, 0, -1,
@@ -1197,8 +1219,7 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
                                                     pat->P.staging_sym > 0,
                                                     cached_geometry(pat, mesh));
       if (!rc && vec1)
-        rc = fem_fast::vector_pair_blocks(*mesh, *basis, *form, staging, st, cb[c], cb[c + 1],
-                                          cells);
+        rc = node_pair_values(pat, mesh, basis, form, staging, st, cb[c], cb[c + 1], cells);
       if (rc) {
         release();
         return rc;

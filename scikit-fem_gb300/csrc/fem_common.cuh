@@ -274,7 +274,9 @@ void free_pattern(Pattern* P);
 // node-level pattern's upper lists, codes e * 128 + i * ns + j) and the
 // vector CSR positions and presence mask of its entries.
 struct VecUpper {
-  int dim = 0, ns = 0;
+  int dim = 0, ns = 0;          // dim: the block size (the mesh dimension; 1 for scalar bases)
+  int sdim = 0;                 // the mesh dimension
+  int64_t block_rows = 0;       // node rows per block of the lists' row-block layout
   int64_t nelems = 0;
   UpperLists U;                 // pos / tpos / row released after the build
   int32_t* vpos = nullptr;      // dim * nupper: rows D*I + a, first entry of the block
@@ -284,12 +286,15 @@ struct VecUpper {
   int32_t* count = nullptr;
   double* mm = nullptr;         // mass table per local node pair
 };
+// dim: the block size -- the family's dimension (ElementVector bases) or 1
+// (scalar TriP2 / TetP2 bases)
 int build_vec_upper(const Pattern& P, const int32_t* udofs, int family, int dim, VecUpper* V,
                     cudaStream_t st);
 void free_vec_upper(VecUpper* V);
-// doubles per cell of the pair blocks the sum reads (vector_pair_blocks)
-inline int64_t vec_pair_stride(int dim) {
-  const int np = (dim + 1) * (dim + 2) / 2;
+// doubles per cell of the pair blocks the sum reads (vector_pair_blocks,
+// scalar_pair_values): sdim the mesh dimension, dim the block size
+inline int64_t vec_pair_stride(int sdim, int dim) {
+  const int np = (sdim + 1) * (sdim + 2) / 2;
   return (int64_t)np * dim * dim + 1;
 }
 // DOF rows [row0, row1) (multiples of dim; row1 < 0: to the last row): the

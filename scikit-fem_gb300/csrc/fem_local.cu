@@ -605,6 +605,50 @@ __global__ void __launch_bounds__(BS) vector_pair_blocks_kernel(FemMesh m, FemBi
   flush_rows<R, BS>(smem, out, e0, eend, cid);
 }
 
+// ------------------------------------- simplex, scalar P2 (one-pass sum)
+// The scalar forms k_e dot(grad u, grad v) + m_e u v on TriP2 / TetP2 as the
+// one-pass node-block sum reads them: per cell the NP numbers
+//   E_pq = k_e |det| / d! grad(lambda_p) . grad(lambda_q)   (p <= q)
+// and m_e |det| / d!.  The Gram entries come from the geometry cache when
+// geo is given, else from the coordinates with the cache kernel's rounding
+// (the scaled Gram entries, then the coefficient), so both give the same bits.
+template <int D, int BS>
+__global__ void __launch_bounds__(BS) scalar_pair_kernel(FemMesh m, FemBilinear f,
+                                                         const double* __restrict__ geo,
+                                                         double* __restrict__ out,
+                                                         const int32_t* __restrict__ cells,
+                                                         int64_t ebeg, int64_t eend) {
+  constexpr int NP = kGramCount<D>;
+  constexpr int R = NP + 1;
+  extern __shared__ double smem[];
+  int64_t* cid = cells ? reinterpret_cast<int64_t*>(smem + (size_t)BS * (R + 1)) : nullptr;
+  const int64_t e0 = ebeg + (int64_t)blockIdx.x * BS;
+  const int64_t pos = e0 + threadIdx.x;
+  if (pos < eend) {
+    const int64_t e = cell_at(cells, pos);
+    if (cid) cid[threadIdx.x] = e;
+    double* row = smem + threadIdx.x * (R + 1);
+    const double sd = coef_at(f.diff, e);
+    double adet;
+    if (geo) {
+#pragma unroll
+      for (int k = 0; k < NP; ++k) row[k] = sd * __ldg(geo + (int64_t)k * m.nelems + e);
+      adet = __ldg(geo + (int64_t)NP * m.nelems + e);
+    } else {
+      double gram[D + 1][D + 1], rinv;
+      simplex_gram<D>(m, e, gram, adet, rinv);
+      const double s = rinv * kInvFact<D>;
+      int k = 0;
+#pragma unroll
+      for (int a = 0; a <= D; ++a)
+#pragma unroll
+        for (int b = a; b <= D; ++b) row[k++] = sd * (gram[a][b] * s);
+    }
+    row[NP] = coef_at(f.mass, e) * (adet * kInvFact<D>);
+  }
+  flush_rows<R, BS>(smem, out, e0, eend, cid);
+}
+
 // ----------------------------------------------------------- hexahedron Q1
 // Reference node k sits at corner c_hex_corner[k] (refdom.py:173-180);
 // phi_k = prod_ax f(c, x_ax) with f(1,t) = t, f(0,t) = 1 - t.
@@ -1158,6 +1202,30 @@ int vector_pair_blocks(const FemMesh& m, const FemBasis& b, const FemBilinear& f
   }
   (void)b;
   FEM_LAUNCH_CHECK("vector_pair_blocks_kernel");
+  return 0;
+}
+
+int scalar_pair_values(const FemMesh& m, const FemBasis& b, const FemBilinear& f,
+                       const double* geo, double* out, cudaStream_t st, int64_t ebeg,
+                       int64_t eend, const int32_t* cells) {
+  if (eend < 0) eend = m.nelems;
+  if (eend <= ebeg) return 0;
+  if (b.vector || (b.family != FEM_TRI_P2 && b.family != FEM_TET_P2) ||
+      fem::basis_dim(b.family) != m.dim) {
+    fem::set_error(FEM_ERR_UNSUPPORTED, "scalar pair values: not a scalar TriP2 / TetP2 basis");
+    return FEM_ERR_UNSUPPORTED;
+  }
+  constexpr int BS = 128;
+  const unsigned grid = (unsigned)fem::ceil_div(eend - ebeg, BS);
+  const size_t cid = cells ? kCidBytes<BS> : 0;
+  if (m.dim == 3) {
+    const size_t sm = (size_t)BS * (kGramCount<3> + 2) * sizeof(double) + cid;
+    scalar_pair_kernel<3, BS><<<grid, BS, sm, st>>>(m, f, geo, out, cells, ebeg, eend);
+  } else {
+    const size_t sm = (size_t)BS * (kGramCount<2> + 2) * sizeof(double) + cid;
+    scalar_pair_kernel<2, BS><<<grid, BS, sm, st>>>(m, f, geo, out, cells, ebeg, eend);
+  }
+  FEM_LAUNCH_CHECK("scalar_pair_kernel");
   return 0;
 }
 

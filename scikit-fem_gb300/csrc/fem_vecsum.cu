@@ -12,6 +12,10 @@
 // vertex pairs per node pair) and E_pq the cell's pair blocks, computed per
 // call from the coordinates and coefficients (vector_pair_blocks_kernel).
 //
+// Scalar TriP2 / TetP2 bases take the same path with D = 1: E_pq is then the
+// number k_e |det| / d! grad(lambda_p) . grad(lambda_q) (scalar_pair_values)
+// and a node block is one CSR entry.
+//
 // Work unit: one node block (I, J), I <= J, of the CSR (DOF D*node + a, the
 // reference's interleaved numbering).  A lane owns a block, walks its
 // contribution list -- the cells holding both nodes, ascending, each with
@@ -48,8 +52,11 @@ int pair_index(int nv, int p, int q) { return p * nv - p * (p - 1) / 2 + (q - p)
 
 // terms[(i * ns + j) * kMaxTerms + t], count[i * ns + j]: the BB[i][j]
 // terms of the element's reference tensor; mm[i * ns + j] its mass table.
-int fill_terms(int family, int dim, std::vector<VecTerm>* terms, std::vector<int32_t>* count,
-               std::vector<double>* mm) {
+// scalar: the pair values are numbers (E_qp = E_pq), so the terms of BB[i][j]
+// on (p, q) and (q, p) are one term with the coefficients' sum (exact for
+// the tables' coefficients, which are equal there).
+int fill_terms(int family, int dim, bool scalar, std::vector<VecTerm>* terms,
+               std::vector<int32_t>* count, std::vector<double>* mm) {
   const int ns = basis_nb_scalar(family);
   const int nv = dim + 1;
   terms->assign((size_t)ns * ns * kMaxTerms, VecTerm{0, 0, 0.0});
@@ -58,6 +65,16 @@ int fill_terms(int family, int dim, std::vector<VecTerm>* terms, std::vector<int
   bool over = false;
   auto add = [&](int i, int j, int p, int q, double c) {
     int& n = (*count)[i * ns + j];
+    if (scalar) {
+      const int k = pair_index(nv, std::min(p, q), std::max(p, q));
+      for (int t = 0; t < n; ++t) {
+        VecTerm& tm = (*terms)[(size_t)(i * ns + j) * kMaxTerms + t];
+        if (tm.k == k) {
+          tm.c += c;
+          return;
+        }
+      }
+    }
     if (n >= kMaxTerms) {
       over = true;
       return;
@@ -157,13 +174,21 @@ constexpr int64_t kBlockRows = 512;
 // the work-sorted layout -- (segment << 32) | ~(length x terms); segment
 // (b, 0) for row block b's diagonal node blocks, (b, 1 + r) for row r's
 // others (r counted in the block): the natural order's ranges.
+// by_terms (scalar bases, 1 x 1 blocks): segment (b, 1) for all of row
+// block b's others, and the key's low word ordered by the terms per
+// contribution (fewest first), then by descending length: the terms per
+// contribution are fixed by the two nodes' kinds (vertex / edge), so the
+// lanes of a slice add the same number of terms per step (measured at 1.3M
+// TetP2 cells: 0.91 ms per step against 1.13 ms sorted by length x terms
+// within each row; sorting within windows of 8 / 32 / 128 rows 1.02 / 0.95 /
+// 0.96 ms; blocks of 2,048 / 8,192 rows 0.95 / 0.95 ms).
 __global__ void block_work_kernel(const int32_t* __restrict__ slice_len,
                                   const int32_t* __restrict__ slice_base,
                                   const uint32_t* __restrict__ codes,
                                   const int32_t* __restrict__ urow,
                                   const int32_t* __restrict__ utpos, int64_t nupper,
                                   const int32_t* __restrict__ count, int npairs,
-                                  int32_t* __restrict__ len, unsigned long long* __restrict__ key,
+                                  int64_t block_rows, bool by_terms, int32_t* __restrict__ len, unsigned long long* __restrict__ key,
                                   int32_t* __restrict__ ident) {
   const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= nupper) return;
@@ -179,13 +204,20 @@ __global__ void block_work_kernel(const int32_t* __restrict__ slice_len,
   }
   len[u] = n;
   const int64_t row = urow[u];
-  const int64_t b = row / kBlockRows;
+  const int64_t b = row / block_rows;
   const bool diag = utpos[u] < 0;
+  ident[u] = (int32_t)u;
+  if (by_terms) {
+    const unsigned long long seg = (unsigned long long)(b * 2 + (diag ? 0 : 1));
+    const unsigned long long lo = ((unsigned long long)min(nt, 15) << 28) |
+                                  (0x0FFFFFFFull - (unsigned long long)min(n, 0x0FFFFFFF));
+    key[u] = (seg << 32) | lo;
+    return;
+  }
   const unsigned long long seg =
-      (unsigned long long)(b * (kBlockRows + 1) + (diag ? 0 : 1 + (row - b * kBlockRows)));
+      (unsigned long long)(b * (block_rows + 1) + (diag ? 0 : 1 + (row - b * block_rows)));
   const unsigned long long work = (unsigned long long)n * (unsigned long long)nt;
   key[u] = (seg << 32) | (0xFFFFFFFFull - (work > 0xFFFFFFFFull ? 0xFFFFFFFFull : work));
-  ident[u] = (int32_t)u;
 }
 
 // Longest list of each slice of 32 slots of the sorted layout.
@@ -269,7 +301,14 @@ __global__ void vec_block_pos_kernel(const int32_t* __restrict__ perm,
 }
 
 // The sum.  MASS: add m_e |det| / d! * MM[i][j] on the block diagonals.
-template <int D, bool MASS>
+// S: the spatial dimension (S + 1 vertices, the pair blocks' count); D: the
+// block size (S for vector bases, 1 for scalar ones).  D = 1: per step a
+// contribution's terms (predicated up to kMaxTerms) and its mass; FLAT: one
+// FMA per step -- a term, or the mass after a contribution's terms -- with
+// the next step's operand loaded before this one's FMA (the same FMAs in the
+// same order, bitwise the same values; as fast once the lanes of a slice
+// carry the same terms per contribution, at 37 against 32 registers).
+template <int S, int D, bool MASS, bool FLAT = false>
 __global__ void __launch_bounds__(128) vec_upper_kernel(
     int64_t ua, int64_t ub, int64_t nupper, int64_t nd, int64_t nelems, int ns,
     const int32_t* __restrict__ slice_len,
@@ -279,7 +318,7 @@ __global__ void __launch_bounds__(128) vec_upper_kernel(
     const int32_t* __restrict__ count_g, const double* __restrict__ mm_g,
     const double* __restrict__ E, double* __restrict__ vals) {
   constexpr int DD = D * D;
-  constexpr int NP = (D + 1) * (D + 2) / 2;
+  constexpr int NP = (S + 1) * (S + 2) / 2;
   constexpr int R = NP * DD + 1;
   __shared__ VecTerm terms[100 * kMaxTerms];
   __shared__ int32_t count[100];
@@ -324,8 +363,72 @@ __global__ void __launch_bounds__(128) vec_upper_kernel(
     };
     bool live = cur != 0xFFFFFFFFu;        // this lane's list is not done
     if (live) decode();
-    while (__any_sync(0xffffffffu, live)) {
-      if (live) {
+    if constexpr (D == 1 && FLAT) {
+      // One FMA per step, software-pipelined: the next step's operand is
+      // loaded before this step's FMA, so that a lane has two gathers in
+      // flight.  Steps: each contribution's terms, then its mass.
+      auto advance = [&]() {
+        t = 0;
+        ++p;
+        cur = nxt;
+        nxt = p + 1 < len ? __ldg(cp + (int64_t)(p + 1) * 32) : 0xFFFFFFFFu;
+        live = cur != 0xFFFFFFFFu;
+        if (live) decode();
+      };
+      // the lane's next step (false: its list is done); a null operand
+      // address is a step without an FMA (a contribution without terms or
+      // mass, or a code out of range)
+      auto fetch = [&](double& c, const double*& a) -> bool {
+        if (!live) return false;
+        a = nullptr;
+        if (valid && t < nt) {
+          const VecTerm tm = terms[ij * kMaxTerms + t];
+          c = tm.c;
+          a = Eb + tm.k;
+          if (++t >= nt && !MASS) advance();
+          return true;
+        }
+        if (MASS && valid) {
+          c = mm[ij];
+          a = Eb + NP;
+        }
+        advance();
+        return true;
+      };
+      double ca = 0.0, va = 0.0;
+      const double* aa = nullptr;
+      bool ha = fetch(ca, aa);
+      if (ha && aa) va = __ldg(aa);
+      while (__any_sync(0xffffffffu, ha)) {
+        double cb = 0.0, vb = 0.0;
+        const double* ab = nullptr;
+        const bool hb = fetch(cb, ab);
+        if (hb && ab) vb = __ldg(ab);
+        if (ha && aa) acc[0] = __fma_rn(ca, va, acc[0]);
+        ca = cb;
+        va = vb;
+        aa = ab;
+        ha = hb;
+      }
+    }
+    while (!(D == 1 && FLAT) && __any_sync(0xffffffffu, live)) {
+      if (D == 1 && live) {
+        // one number per term: a contribution's terms (at most kMaxTerms,
+        // predicated) and its mass in one step -- the per-step overhead
+        // would otherwise outweigh the single FMA of a term
+#pragma unroll
+        for (int u = 0; u < kMaxTerms; ++u)
+          if (u < nt) {
+            const VecTerm tm = terms[ij * kMaxTerms + u];
+            acc[0] = __fma_rn(tm.c, __ldg(Eb + tm.k), acc[0]);
+          }
+        if (MASS && valid) acc[0] = __fma_rn(__ldg(Eb + NP), mm[ij], acc[0]);
+        ++p;
+        cur = nxt;
+        nxt = p + 1 < len ? __ldg(cp + (int64_t)(p + 1) * 32) : 0xFFFFFFFFu;
+        live = cur != 0xFFFFFFFFu;
+        if (live) decode();
+      } else if (live) {
         if (t < nt) {
           const VecTerm tm = terms[ij * kMaxTerms + t];
           const double* Ep = Eb + tm.k * DD;
@@ -473,19 +576,21 @@ int build_vec_upper(const Pattern& P, const int32_t* udofs, int family, int dim,
                     cudaStream_t st) {
   *V = VecUpper();
   const int ns = basis_nb_scalar(family);
-  if ((dim != 2 && dim != 3) || ns <= 0 || ns > 10 || basis_dim(family) != dim ||
+  const int sdim = basis_dim(family);
+  if ((sdim != 2 && sdim != 3) || (dim != 1 && dim != sdim) || ns <= 0 || ns > 10 ||
       P.nbfun_u != dim * ns || P.nbfun_v != dim * ns || !P.has_matrix || P.nrows % dim) {
-    set_error(FEM_ERR_UNSUPPORTED, "one-pass vector sum: not a vector simplex pattern");
+    set_error(FEM_ERR_UNSUPPORTED, "one-pass node-block sum: not a simplex pattern");
     return FEM_ERR_UNSUPPORTED;
   }
   V->dim = dim;
+  V->sdim = sdim;
   V->ns = ns;
   V->nelems = P.nelems;
   const int64_t nelems = P.nelems, nnodes = P.nrows / dim;
   std::vector<VecTerm> terms;
   std::vector<int32_t> count;
   std::vector<double> mm;
-  int rc = fill_terms(family, dim, &terms, &count, &mm);
+  int rc = fill_terms(family, sdim, dim == 1, &terms, &count, &mm);
   if (rc) return rc;
   auto fail = [&](int code) {
     free_vec_upper(V);
@@ -507,12 +612,13 @@ int build_vec_upper(const Pattern& P, const int32_t* udofs, int family, int dim,
   FEM_TRY_CUDA(cudaMemcpyAsync(&h, flag, sizeof(h), cudaMemcpyDeviceToHost, st));
   FEM_TRY_CUDA(cudaStreamSynchronize(st));
   if (h) {
-    set_error(FEM_ERR_UNSUPPORTED, "one-pass vector sum: DOFs are not interleaved by node");
+    set_error(FEM_ERR_UNSUPPORTED, "one-pass node-block sum: DOFs are not interleaved by node");
     return FEM_ERR_UNSUPPORTED;
   }
   rc = build_incidence(node, nelems, ns, nnodes, &N, st);
   if (!rc) rc = build_csr(node, ns, nnodes, nullptr, &N, st);
-  if (!rc) rc = build_upper_lists(N, &V->U, st, /*wide=*/true, kBlockRows);
+  V->block_rows = kBlockRows;
+  if (!rc) rc = build_upper_lists(N, &V->U, st, /*wide=*/true, V->block_rows);
   if (rc) {
     free_pattern(new Pattern(N));   // releases N's device arrays
     return fail(rc);
@@ -556,7 +662,7 @@ int build_vec_upper(const Pattern& P, const int32_t* udofs, int family, int dim,
     if (e == cudaSuccess) {
       block_work_kernel<<<(unsigned)ceil_div(nu, 256), 256, 0, st>>>(
           V->U.slice_len, V->U.slice_base, V->U.codes, V->U.row, V->U.tpos, nu, V->count,
-          ns * ns, len, key, ident);
+          ns * ns, V->block_rows, dim == 1, len, key, ident);
       e = cudaGetLastError();
     }
     size_t tmp_bytes = 0;
@@ -621,7 +727,7 @@ int build_vec_upper(const Pattern& P, const int32_t* udofs, int family, int dim,
   free_pattern(new Pattern(N));   // releases N's device arrays
   if (e != cudaSuccess) return fail(check_cuda(e, "vec_block_pos_kernel"));
   if (h) {
-    set_error(FEM_ERR_UNSUPPORTED, "one-pass vector sum: the CSR pattern is not block-symmetric");
+    set_error(FEM_ERR_UNSUPPORTED, "one-pass node-block sum: the CSR pattern is not block-symmetric");
     return fail(FEM_ERR_UNSUPPORTED);
   }
   // the node-level CSR positions, rows and transposes are build-time only
@@ -632,7 +738,7 @@ int build_vec_upper(const Pattern& P, const int32_t* udofs, int family, int dim,
   return 0;
 }
 
-int64_t vec_window_rows(const VecUpper& V) { return kBlockRows * V.dim; }
+int64_t vec_window_rows(const VecUpper& V) { return V.block_rows * V.dim; }
 
 int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, cudaStream_t st,
                   int64_t row0, int64_t row1, bool coop) {
@@ -643,9 +749,9 @@ int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, c
   int64_t n0 = row0 < 0 ? 0 : row0 / V.dim;
   int64_t n1 = (row1 < 0 || row1 / V.dim > nnodes) ? nnodes : row1 / V.dim;
   if (n1 <= n0) return 0;
-  if ((n0 % kBlockRows) || ((n1 % kBlockRows) && n1 != nnodes)) {
+  if ((n0 % V.block_rows) || ((n1 % V.block_rows) && n1 != nnodes)) {
     set_error(FEM_ERR_ARGUMENT, "vector one-pass rows [%lld, %lld) off the %lld-row blocks",
-              (long long)row0, (long long)row1, (long long)(kBlockRows * V.dim));
+              (long long)row0, (long long)row1, (long long)(V.block_rows * V.dim));
     return FEM_ERR_ARGUMENT;
   }
   // the node rows' blocks: one range of the row-block layout
@@ -658,7 +764,7 @@ int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, c
     if (ub <= ua) continue;
     const int64_t nsl = ((ub + 31) >> 5) - (ua >> 5);
     // lane per block: a warp per slice of 32 blocks; cooperative: 32 / D^2 blocks per warp
-    const int64_t nwarp = coop ? ceil_div(ub - ua, 32 / (V.dim * V.dim)) : nsl;
+    const int64_t nwarp = (coop && V.dim > 1) ? ceil_div(ub - ua, 32 / (V.dim * V.dim)) : nsl;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nwarp, threads / 32),
                                                                 (int64_t)num_sms() * 32));
     auto launch = [&](auto kern) {
@@ -666,7 +772,27 @@ int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, c
                                      V.U.slice_base, V.U.codes, V.vpos, V.vposT, V.vmask,
                                      static_cast<const VecTerm*>(V.terms), V.count, V.mm, E, vals);
     };
-    if (coop) {
+    if (V.dim == 1) {
+      // scalar bases: one entry per node block
+      // (coop: the flattened form, one FMA per step)
+      if (V.sdim == 3) {
+        if (coop) {
+          if (mass) launch(vec_upper_kernel<3, 1, true, true>);
+          else launch(vec_upper_kernel<3, 1, false, true>);
+        } else {
+          if (mass) launch(vec_upper_kernel<3, 1, true>);
+          else launch(vec_upper_kernel<3, 1, false>);
+        }
+      } else {
+        if (coop) {
+          if (mass) launch(vec_upper_kernel<2, 1, true, true>);
+          else launch(vec_upper_kernel<2, 1, false, true>);
+        } else {
+          if (mass) launch(vec_upper_kernel<2, 1, true>);
+          else launch(vec_upper_kernel<2, 1, false>);
+        }
+      }
+    } else if (coop) {
       if (V.dim == 3) {
         if (mass) launch(vec_upper_coop_kernel<3, true>);
         else launch(vec_upper_coop_kernel<3, false>);
@@ -675,11 +801,11 @@ int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, c
         else launch(vec_upper_coop_kernel<2, false>);
       }
     } else if (V.dim == 3) {
-      if (mass) launch(vec_upper_kernel<3, true>);
-      else launch(vec_upper_kernel<3, false>);
+      if (mass) launch(vec_upper_kernel<3, 3, true>);
+      else launch(vec_upper_kernel<3, 3, false>);
     } else {
-      if (mass) launch(vec_upper_kernel<2, true>);
-      else launch(vec_upper_kernel<2, false>);
+      if (mass) launch(vec_upper_kernel<2, 2, true>);
+      else launch(vec_upper_kernel<2, 2, false>);
     }
     FEM_LAUNCH_CHECK("vec_upper_kernel");
   }

@@ -53,14 +53,21 @@ def test_split_entry_points_equal_fem_assemble(name, shuffle):
     coeffs, ch, c_form = form._setup(b, None, kw)
     lib = N.lib()
     s = N.stream_ptr()
-    # without the geometry cache (and the fused sum it enables) fem_assemble
-    # runs the local kernel and the staging sum, as the split entry points do
+    # without the geometry cache (and the fused sum it enables), and with the
+    # family's one-pass sums off, fem_assemble runs the local kernel and the
+    # staging sum, as the split entry points do
     lib.fem_pattern_drop_geometry(entry.pat.handle)
     entry.geo_key = None
     ref = torch.full_like(K.values(), np.nan)
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
-    N.check(lib.fem_assemble(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
-                             entry.pat.handle, N.ptr(entry.staging), N.ptr(ref), N.ptr(status), s))
+    fam = N.FAMILY[name.split("-")[0]]
+    try:
+        lib.fem_set_onepass(fam, 0)
+        N.check(lib.fem_assemble(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
+                                 entry.pat.handle, N.ptr(entry.staging), N.ptr(ref),
+                                 N.ptr(status), s))
+    finally:
+        lib.fem_set_onepass(fam, 1)
     vals = torch.full_like(ref, np.nan)
     # whole mesh
     N.check(lib.fem_assemble_local(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
