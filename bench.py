@@ -525,6 +525,16 @@ def _time(fn, reps, warm=2):
     return e0.elapsed_time(e1) / reps
 
 
+def _cpu_oracle(assemble, cells, sample):
+    """The oracle (the numpy restatement of the reference) on a bounded
+    sample of a workload, on all host threads: cells per second of one run."""
+    t0 = time.perf_counter()
+    assemble()
+    s = time.perf_counter() - t0
+    return {"cells_per_s": cells / s, "s": s, "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": sample}
+
+
 def _abi_step(F, N, form, b, coefs):
     """Bare C-ABI assembly step (inputs and outputs in HBM)."""
     import torch
@@ -559,6 +569,11 @@ def secondary_workloads(args, only=None):
     hbm, _ = peaks()
     out = {}
     rng = np.random.default_rng(args.seed)
+    # the oracle on a bounded sample of each workload, all host threads
+    cpu = not getattr(args, "no_cpu", False)
+    nthr = os.cpu_count() or 1
+    if cpu:
+        import oracle as O
     reps = 10
     lib = N.lib()
 
@@ -574,6 +589,15 @@ def secondary_workloads(args, only=None):
             "nelems": m.nelements, "nnz": entry.nnz, "ms_matrix": ms_k, "ms_load": ms_b,
             "elements_per_s": m.nelements / ((ms_k + ms_b) * 1e-3),
             "hbm_frac_matrix": B / (ms_k * 1e-3) / 1e9 / hbm}
+        if cpu:
+            om = O.mesh_tri_tensor(np.linspace(0, 1, 257), np.linspace(0, 1, 257))
+            ob = O.OBasis(om, O.TriP1())
+            c = _cpu_oracle(lambda: (O.bilinear_assemble(O.laplace, ob, nthreads=nthr),
+                                     O.linear_assemble(O.unit_load, ob)),
+                            om.nelements, "the whole workload (matrix + load), prebuilt basis")
+            out["tri_p1_laplace_256"]["cpu_oracle"] = c
+            out["tri_p1_laplace_256"]["speedup_vs_cpu_oracle"] = (
+                out["tri_p1_laplace_256"]["elements_per_s"] / c["cells_per_s"])
 
     if want('tet_p2_vec'):
         # cfg3: vector TetP2 elasticity, 41^3 nodes jittered +-0.2h, lambda=1, mu=0.5
@@ -620,6 +644,17 @@ def secondary_workloads(args, only=None):
             "pattern_build_s": build_s, "elements_per_s": m.nelements / (ms * 1e-3),
             "hbm_frac": B / (ms * 1e-3) / 1e9 / hbm, "algorithmic_bytes": B,
             "fp64_floor_ms": m.nelements * VEC_TETP2_FP64_PER_CELL / 0.598e12 * 1e3}
+        if cpu:
+            sm = jittered_tet_cube(16)
+            ob = O.OBasis(O.OMesh(np.asarray(sm.p), np.asarray(sm.t), "tet"),
+                          O.Vector(O.TetP2()), intorder=4)
+            c = _cpu_oracle(lambda: O.bilinear_assemble(O.linear_elasticity(1.0, 0.5), ob,
+                                                        nthreads=nthr),
+                            sm.nelements, "16^3 cubes jittered the same way (%d tets), prebuilt "
+                                          "basis" % sm.nelements)
+            key = "tet_p2_vec_elasticity_%d" % (n + 1)
+            out[key]["cpu_oracle"] = c
+            out[key]["speedup_vs_cpu_oracle"] = out[key]["elements_per_s"] / c["cells_per_s"]
         del step, entry, vals, b
         torch.cuda.empty_cache()
 
@@ -672,6 +707,18 @@ def secondary_workloads(args, only=None):
             "pattern_build_s": build_s, "elements_per_s": m.nelements / (ms * 1e-3),
             "hbm_frac": B / (ms * 1e-3) / 1e9 / hbm, "algorithmic_bytes": B,
             "fp64_floor_ms": m.nelements * SCALAR_TETP2_FP64_PER_CELL / 0.598e12 * 1e3}
+        if cpu:
+            om = O.mesh_tet_tensor(*(np.linspace(0, 1, 41),) * 3)
+            kc = np.random.default_rng(SEED).lognormal(0.0, 1.0, om.nelements)
+            ob = O.OBasis(om, O.TetP2())
+            c = _cpu_oracle(lambda: O.bilinear_assemble(O.k_laplace_mass, ob,
+                                                        k=ob.zero_w() + kc[:, None],
+                                                        nthreads=nthr),
+                            om.nelements, "the 41^3-node cube (%d tets), prebuilt basis"
+                                          % om.nelements)
+            key = "tet_p2_k_laplace_mass_%d" % args.p2_n
+            out[key]["cpu_oracle"] = c
+            out[key]["speedup_vs_cpu_oracle"] = out[key]["elements_per_s"] / c["cells_per_s"]
         del step, entry, vals, b
         torch.cuda.empty_cache()
 
@@ -714,6 +761,18 @@ def secondary_workloads(args, only=None):
                 "elements_per_s_forward": m.nelements / (ms_f * 1e-3),
                 "cells": "isoparametric (64-point quadrature)" if jit else
                          "parallelepipeds (closed form)"}
+            if cpu:
+                sm, th_s, _, _ = hex_cube_workload(args.hex_n, jitter=jit)
+                ob = O.OBasis(O.OMesh(np.asarray(sm.p), np.asarray(sm.t), "hex"), O.Hex1())
+                c = _cpu_oracle(lambda: O.bilinear_assemble(O.theta_laplace, ob,
+                                                            theta=ob.zero_w() + th_s[:, None],
+                                                            nthreads=nthr),
+                                sm.nelements, "the whole workload, forward assembly, "
+                                              "prebuilt basis")
+                key = "hex1_theta_laplace_%d%s_vjp" % (args.hex_n, tag)
+                out[key]["cpu_oracle"] = c
+                out[key]["speedup_vs_cpu_oracle"] = (out[key]["elements_per_s_forward"] /
+                                                     c["cells_per_s"])
             del step, entry, vals, b, scratch
             torch.cuda.empty_cache()
 
@@ -804,6 +863,24 @@ def secondary_workloads(args, only=None):
             "ms_per_mesh_api_calls": ms_api, "speedup_vs_per_mesh_api": ms_api / ms_graph,
             "launches_per_step": ga.launches_per_step(),
             "launches_per_step_per_mesh": sum(g.launches_per_step() for g in per)}
+        if cpu:
+            # the reference's way for many meshes: a Python loop of per-mesh
+            # assemblies (forward), on every 16th mesh (their sizes spread as
+            # the batch's)
+            sample, cells = [], 0
+            for mm, kv in list(zip(meshes, ks))[::16]:
+                ob = O.OBasis(O.OMesh(np.asarray(mm.p), np.asarray(mm.t), "tri"), O.TriP2())
+                sample.append((ob, kv))
+                cells += mm.nelements
+            c = _cpu_oracle(lambda: [O.bilinear_assemble(O.k_laplace, ob,
+                                                         k=ob.zero_w() + kv[:, None],
+                                                         nthreads=nthr) for ob, kv in sample],
+                            cells, "every 16th mesh (%d meshes, %d cells), a loop of forward "
+                                   "assemblies on prebuilt bases" % (len(sample), cells))
+            key = "batched_512_trip2_forward_vjp"
+            out[key]["cpu_oracle"] = c
+            out[key]["speedup_vs_cpu_oracle"] = (out[key]["elements_per_s_batched"] /
+                                                 c["cells_per_s"])
 
     if want("generic"):
         # generic per-point kernels: a Newton-step matrix with an

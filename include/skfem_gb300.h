@@ -675,6 +675,16 @@ int fem_vertex_incidence_build(const FemMesh* mesh, FemPattern** out, fem_stream
  * and forms k dot(grad u, grad v) + m u v.  status (device int32)
  * receives the coefficient checks' bits and FEM_ERR_TIMEOUT if a wait ran
  * out.  Capturable in a CUDA graph (memset + kernel).
+ * Scalar TriP2 / TetP2 patterns holding the one-pass node-block lists
+ * (fem_pattern_cache_geometry builds them), unless fem_set_onepass selects
+ * the two-pass path for the family: the launch runs the batched form of
+ * fem_assemble's one-pass sum instead -- cell units write each cell's pair
+ * values (and the same dJ/dk_e, dJ/dm_e), row-block units (the lists' slots
+ * of one block of rows) wait (bounded) for the cell units of every mesh
+ * their rows belong to and sum one CSR entry per lane; the CSR values then
+ * equal fem_assemble's bit for bit.  Its queue is built from the pattern's
+ * lists on the first such call (not during a stream capture: run the call
+ * once before capturing it); fem_batch_plan_info then reports its units.
  */
 int fem_batch_plan_build(const int64_t* cell_offsets, const int64_t* row_offsets,
                          int32_t nmeshes, int32_t rows_per_unit, FemBatchPlan** out);

@@ -28,14 +28,17 @@ int coef_checks(const FemBilinear& f, const uint8_t* ref_bits, int32_t* status, 
 int local_vectors(const FemMesh&, const FemBasis&, const FemLinear&, double*, int32_t*,
                   cudaStream_t);
 // the vector channel forms' per-cell pair blocks (fem::vec_pair_stride doubles per
-// cell) of the cells [ebeg, eend) (of the list cells, when given)
+// cell) of the cells [ebeg, eend) (of the list cells, when given); with a
+// status word also the coefficient checks (ref_bits: the pattern's zero bits)
 int vector_pair_blocks(const FemMesh&, const FemBasis&, const FemBilinear&, double*, cudaStream_t,
-                       int64_t ebeg = 0, int64_t eend = -1, const int32_t* cells = nullptr);
+                       int64_t ebeg = 0, int64_t eend = -1, const int32_t* cells = nullptr,
+                       const uint8_t* ref_bits = nullptr, int32_t* status = nullptr);
 // the same for scalar TriP2 / TetP2 bases (geo: the pattern's geometry cache
 // of this mesh, or null)
 int scalar_pair_values(const FemMesh&, const FemBasis&, const FemBilinear&, const double* geo,
                        double*, cudaStream_t, int64_t ebeg = 0, int64_t eend = -1,
-                       const int32_t* cells = nullptr);
+                       const int32_t* cells = nullptr, const uint8_t* ref_bits = nullptr,
+                       int32_t* status = nullptr);
 }  // namespace fem_fast
 namespace fem_exact {
 int local_matrices(const FemMesh&, const FemBasis&, const FemBilinear&, double*, int32_t*,
@@ -202,14 +205,18 @@ bool vector_onepass(const FemPattern* pat, const FemMesh* mesh, const FemBasis* 
 }
 
 // The per-cell pair values the one-pass node-block sum reads, cells
-// [ebeg, eend) (of the list cells, when given), into the staging.
+// [ebeg, eend) (of the list cells, when given), into the staging; with a
+// status word the same kernel runs the coefficient checks (as the two-pass
+// local kernel does).
 int node_pair_values(const FemPattern* pat, const FemMesh* mesh, const FemBasis* basis,
-                     const FemBilinear* form, double* staging, cudaStream_t st, int64_t ebeg = 0,
-                     int64_t eend = -1, const int32_t* cells = nullptr) {
+                     const FemBilinear* form, double* staging, int32_t* status, cudaStream_t st,
+                     int64_t ebeg = 0, int64_t eend = -1, const int32_t* cells = nullptr) {
+  const uint8_t* ref = status ? pat->coef_bits : nullptr;
   if (basis->vector)
-    return fem_fast::vector_pair_blocks(*mesh, *basis, *form, staging, st, ebeg, eend, cells);
+    return fem_fast::vector_pair_blocks(*mesh, *basis, *form, staging, st, ebeg, eend, cells,
+                                        ref, status);
   return fem_fast::scalar_pair_values(*mesh, *basis, *form, cached_geometry(pat, mesh), staging,
-                                      st, ebeg, eend, cells);
+                                      st, ebeg, eend, cells, ref, status);
 }
 
 bool fused_sum(const FemPattern* pat, const FemMesh* mesh, const FemBasis* basis,
@@ -333,6 +340,10 @@ using fem::set_error;
 namespace fem {
 const Pattern* pattern_of(const FemPattern* h) { return h ? &h->P : nullptr; }
 const uint8_t* pattern_coef_bits(const FemPattern* h) { return h ? h->coef_bits : nullptr; }
+// the pattern's one-pass node-block lists (null: none built)
+const VecUpper* pattern_node_lists(const FemPattern* h) {
+  return (h && h->vec_ok) ? &h->vec : nullptr;
+}
 int coef_check(const FemBilinear& f, int64_t n, const uint8_t* ref, int32_t* status,
                cudaStream_t st) {
   coef_zero_bits_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(f, n, ref, nullptr, status);
@@ -757,11 +768,9 @@ int fem_assemble(const FemMesh* mesh, const FemBasis* basis, const FemBilinear* 
                                     csr_values, st);
   }
   if (vector_onepass(pat, mesh, basis)) {
-    // the coefficient checks, the cells' pair blocks (in the staging), then
-    // the one-pass vector sum contracting and summing the node blocks
-    rc = fem_fast::coef_checks(*form, pat->coef_bits, status, st, 0, mesh->nelems, nullptr);
-    if (rc) return rc;
-    rc = node_pair_values(pat, mesh, basis, form, staging, st);
+    // the cells' pair values (in the staging) with the coefficient checks,
+    // then the one-pass sum contracting and summing the node blocks
+    rc = node_pair_values(pat, mesh, basis, form, staging, status, st);
     if (rc) return rc;
     const bool mass = form->mass.field || form->mass.scale != 0.0;
     return fem::vec_upper_sum(pat->vec, staging, mass, csr_values, st, 0, -1,
@@ -1211,15 +1220,15 @@ int fem_assemble_to_host_pipelined(const FemMesh* mesh, const FemBasis* basis,
       }
     }
     if (cb[c + 1] > cb[c]) {
-      rc = (fused || onepass || vec1)
+      rc = vec1 ? node_pair_values(pat, mesh, basis, form, staging, status, st, cb[c],
+                                   cb[c + 1], cells)
+           : (fused || onepass)
                ? fem_fast::coef_checks(*form, pat->coef_bits, status, st, cb[c], cb[c + 1], cells)
                : fem_fast::local_matrices_checked(*mesh, *basis, *form, staging,
                                                     status ? pat->coef_bits : nullptr, status, st,
                                                     cb[c], cb[c + 1], cells,
                                                     pat->P.staging_sym > 0,
                                                     cached_geometry(pat, mesh));
-      if (!rc && vec1)
-        rc = node_pair_values(pat, mesh, basis, form, staging, st, cb[c], cb[c + 1], cells);
       if (rc) {
         release();
         return rc;

@@ -26,8 +26,10 @@
 // sets FEM_ERR_TIMEOUT in the status word and skips the unit.
 
 #include "fem_common.cuh"
+#include "fem_nodesum.cuh"
 #include "fem_tables.cuh"
 
+#include <algorithm>
 #include <vector>
 
 struct FemBatchPlan {
@@ -38,6 +40,18 @@ struct FemBatchPlan {
   int64_t* unit_end = nullptr;    // nunits
   int32_t* unit_kind_mesh = nullptr;  // nunits: kind (bit 0) | mesh << 1
   int32_t* cell_units = nullptr;  // nmeshes: cell units of each mesh
+  std::vector<int64_t> cell_off, row_off;   // the meshes' offsets (host)
+  // The one-pass queue (scalar TriP2 / TetP2 patterns with node-block
+  // lists), built on first use for the lists it was built from: cell units
+  // as above, then row-block units (kind 1, mesh = the block's last mesh,
+  // [begin, end) = the block's slots of the lists) waiting on the meshes
+  // [op_mesh_lo, mesh] of the block's rows.
+  const void* op_lists = nullptr;
+  int64_t op_nunits = 0;
+  int64_t* op_begin = nullptr;
+  int64_t* op_end = nullptr;
+  int32_t* op_kind_mesh = nullptr;
+  int32_t* op_mesh_lo = nullptr;
 };
 
 namespace fem_batched {
@@ -250,14 +264,267 @@ __global__ void __launch_bounds__(kBlock) batched_forward_vjp_kernel(
   fem::publish_status(status, flags);
 }
 
+// The one-pass form for scalar TriP2 / TetP2 (ORDER 2) patterns with
+// node-block lists -- the batched form of the one-pass node-block sum:
+//   cell unit: each thread one cell -- its pair values E[e] (the scaled Gram
+//     entries times k_e, then m_e |det| / d!; scalar_pair_kernel's rounding)
+//     into the staging, and dJ/dk_e = w_e^T S_e u_e, dJ/dm_e = w_e^T M_e u_e
+//     from the cached geometry, as the two-pass form computes them;
+//   row-block unit (the lists' slots of one block of rows): after a bounded
+//     acquire-wait on the cell units of every mesh the block's rows belong
+//     to, the block's slices, one lane per CSR entry (scalar_entry_sum: the
+//     reference-tensor terms and mass of its cells in ascending order).
+// The same values bit for bit as fem_assemble's one-pass sum.
+struct NodeArgs {
+  const int32_t* slice_len;
+  const int32_t* slice_base;
+  const uint32_t* codes;
+  const int32_t* vpos;
+  const int32_t* vposT;
+  const uint16_t* vmask;
+  const fem::VecTerm* terms;
+  const int32_t* count;
+  const double* mm;
+  int npairs;
+};
+
+template <int D, bool MASS>
+__global__ void __launch_bounds__(kBlock) batched_onepass_vjp_kernel(
+    FemMesh m, FemBasis b, FemBilinear f, const double* __restrict__ geo, NodeArgs na,
+    const int32_t* __restrict__ kind_mesh, const int32_t* __restrict__ mesh_lo,
+    const int64_t* __restrict__ ubeg, const int64_t* __restrict__ uend, int64_t nunits,
+    const int32_t* __restrict__ cell_units, int32_t* __restrict__ counters,
+    const uint8_t* __restrict__ ref_bits, double* __restrict__ staging,
+    double* __restrict__ vals, const double* __restrict__ w, const double* __restrict__ u,
+    double* __restrict__ dcd, double* __restrict__ dcm, int32_t* __restrict__ status) {
+  constexpr int NB = Traits<D, 2>::NB;
+  constexpr double INV_FACT = 1.0 / Traits<D, 2>::FACT;
+  constexpr int NG = (D + 1) * (D + 2) / 2;
+  constexpr int R = NG + 1;
+  __shared__ fem::VecTerm terms[fem::kMaxNodePairs * fem::kMaxTerms];
+  __shared__ int32_t count[fem::kMaxNodePairs];
+  __shared__ double mmt[fem::kMaxNodePairs];
+  __shared__ long long s_unit;
+  __shared__ int s_skip;
+  for (int k = threadIdx.x; k < na.npairs * fem::kMaxTerms; k += blockDim.x)
+    terms[k] = na.terms[k];
+  for (int k = threadIdx.x; k < na.npairs; k += blockDim.x) {
+    count[k] = na.count[k];
+    mmt[k] = na.mm[k];
+  }
+  __syncthreads();
+  int32_t* ticket = counters;
+  int32_t* done = counters + 1;
+  int32_t flags = 0;
+  for (;;) {
+    if (threadIdx.x == 0) s_unit = atomicAdd(ticket, 1);
+    __syncthreads();
+    const long long k = s_unit;
+    __syncthreads();
+    if (k >= nunits) break;
+    const int km = kind_mesh[k];
+    const int mesh = km >> 1;
+    const int64_t a = ubeg[k], z = uend[k];
+    if ((km & 1) == 0) {
+      // ---------------------------------------------------- cell unit
+      const int64_t e = a + threadIdx.x;
+      if (e < z) {
+        const int rb = ref_bits ? (int)__ldg(ref_bits + e) : -1;
+        double gram[D + 1][D + 1];
+        int q = 0;
+#pragma unroll
+        for (int i = 0; i <= D; ++i)
+#pragma unroll
+          for (int j = i; j <= D; ++j) gram[i][j] = __ldg(geo + (int64_t)(q++) * m.nelems + e);
+        const double adet = __ldg(geo + (int64_t)NG * m.nelems + e);
+        const double sd = coef_at(f.diff, e);
+        double* row = staging + e * R;
+        q = 0;
+#pragma unroll
+        for (int i = 0; i <= D; ++i)
+#pragma unroll
+          for (int j = i; j <= D; ++j) {
+            row[q] = sd * gram[i][j];
+            ++q;
+          }
+        row[NG] = coef_at(f.mass, e) * (adet * INV_FACT);
+        if (w && u && (dcd || dcm)) {
+          double kst[NB][NB];
+          double mm[NB][NB];
+#define G_(i, j) ((i) <= (j) ? gram[i][j] : gram[j][i])
+#define KS(i, j, v) { kst[i][j] = (v); }
+#define KM(i, j, v) { constexpr double _m = (v) * INV_FACT; mm[i][j] = _m; mm[j][i] = _m; }
+          if constexpr (D == 2) { TRI2_STIFF(G_, KS); TRI2_MASS(KM); }
+          if constexpr (D == 3) { TET2_STIFF(G_, KS); TET2_MASS(KM); }
+#undef G_
+#undef KS
+#undef KM
+          double wl[NB], ul[NB];
+#pragma unroll
+          for (int i = 0; i < NB; ++i) {
+            const int64_t dof = b.element_dofs[(int64_t)i * m.nelems + e];
+            wl[i] = w[dof];
+            ul[i] = u[dof];
+          }
+          if (dcd) {
+            double js = 0.0;
+#pragma unroll
+            for (int i = 0; i < NB; ++i) {
+              double ks = 0.0;
+#pragma unroll
+              for (int j = 0; j < NB; ++j) ks = __fma_rn(i <= j ? kst[i][j] : kst[j][i], ul[j], ks);
+              js = __fma_rn(wl[i], ks, js);
+            }
+            dcd[e] = f.diff.scale * js;
+          }
+          if (dcm) {
+            double jm = 0.0;
+#pragma unroll
+            for (int i = 0; i < NB; ++i) {
+              double ms = 0.0;
+#pragma unroll
+              for (int j = 0; j < NB; ++j) ms = __fma_rn(mm[i][j], ul[j], ms);
+              jm = __fma_rn(wl[i], ms, jm);
+            }
+            dcm[e] = f.mass.scale * adet * jm;
+          }
+        }
+        flags |= cell_status(f, e, rb);
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(done + mesh, 1);
+      }
+    } else {
+      // ------------------------------------------------ row-block unit
+      if (threadIdx.x == 0) {
+        int skip = 0;
+        for (int mm = mesh_lo[k]; mm <= mesh && !skip; ++mm) {
+          const int need = cell_units[mm];
+          long long it = 0;
+          while (load_acquire(done + mm) < need && it < kSpinLimit) {
+            __nanosleep(128);
+            ++it;
+          }
+          skip = load_acquire(done + mm) < need;
+        }
+        s_skip = skip;
+        if (skip) atomicOr(status, 1 << FEM_ERR_TIMEOUT);
+        __threadfence();
+      }
+      __syncthreads();
+      if (!s_skip) {
+        const int lane = threadIdx.x & 31;
+        const int64_t s1 = (z + 31) >> 5;
+        for (int64_t sl = (a >> 5) + (threadIdx.x >> 5); sl < s1; sl += kBlock / 32) {
+          const int64_t slot = sl * 32 + lane;
+          const bool inr = slot >= a && slot < z;
+          const int len = inr ? __ldg(na.slice_len + sl) : 0;
+          const uint32_t* cp = na.codes + (int64_t)__ldg(na.slice_base + sl) * 32 + lane;
+          fem::scalar_entry_sum<D, MASS, true>(inr, slot, len, cp, m.nelems, na.npairs, terms,
+                                               count, mmt, na.vpos, na.vposT, na.vmask, staging,
+                                               vals);
+        }
+      }
+      __syncthreads();
+    }
+  }
+  fem::publish_status(status, flags);
+}
+
 }  // namespace fem_batched
 
 namespace fem {
+const VecUpper* pattern_node_lists(const FemPattern* h);
 const Pattern* pattern_of(const FemPattern* h);
 const uint8_t* pattern_coef_bits(const FemPattern* h);
 int validate_mesh_basis(const FemMesh* m, const FemBasis* b);
 const double* pattern_geometry(const FemPattern* h, const FemMesh* m);
 }  // namespace fem
+
+namespace {
+
+// The one-pass queue of a plan for node-block lists V (one node per row):
+// per mesh its cell units, then the row blocks whose rows all belong to
+// earlier meshes -- every row-block unit's cells are queued before it.
+int build_onepass_queue(FemBatchPlan* P, const fem::VecUpper& V) {
+  if (P->op_lists == &V) return 0;
+  cudaFree(P->op_begin);
+  cudaFree(P->op_end);
+  cudaFree(P->op_kind_mesh);
+  cudaFree(P->op_mesh_lo);
+  P->op_begin = P->op_end = nullptr;
+  P->op_kind_mesh = P->op_mesh_lo = nullptr;
+  P->op_lists = nullptr;
+  P->op_nunits = 0;
+  const int M = P->nmeshes;
+  const int64_t nrows = (int64_t)V.U.dpos_h.size() - 1;
+  if (M <= 0 || P->row_off[M] != nrows || V.block_rows <= 0) {
+    fem::set_error(FEM_ERR_ARGUMENT, "batch plan rows do not match the pattern's lists");
+    return FEM_ERR_ARGUMENT;
+  }
+  const int cpu = fem_batched::kBlock;
+  auto mesh_of = [&](int64_t r) {
+    return (int)(std::upper_bound(P->row_off.begin(), P->row_off.end(), r) -
+                 P->row_off.begin()) - 1;
+  };
+  std::vector<int32_t> km, lo;
+  std::vector<int64_t> ub, ue;
+  const int64_t nb = (nrows + V.block_rows - 1) / V.block_rows;
+  int64_t next = 0;   // the next row block to queue
+  auto blocks_upto = [&](int last_mesh) {
+    for (; next < nb; ++next) {
+      const int64_t n0 = next * V.block_rows, n1 = std::min(nrows, n0 + V.block_rows);
+      const int mh = mesh_of(n1 - 1);
+      if (mh > last_mesh) break;
+      const int64_t a = (int64_t)V.U.dpos_h[n0] + V.U.opos_h[n0];
+      const int64_t z = (int64_t)V.U.dpos_h[n1] + V.U.opos_h[n1];
+      if (z <= a) continue;
+      km.push_back((mh << 1) | 1);
+      lo.push_back(mesh_of(n0));
+      ub.push_back(a);
+      ue.push_back(z);
+    }
+  };
+  for (int m = 0; m < M; ++m) {
+    for (int64_t a = P->cell_off[m]; a < P->cell_off[m + 1]; a += cpu) {
+      km.push_back(m << 1);
+      lo.push_back(m);
+      ub.push_back(a);
+      ue.push_back(std::min<int64_t>(a + cpu, P->cell_off[m + 1]));
+    }
+    blocks_upto(m - 1);
+  }
+  blocks_upto(M - 1);
+  const size_t n = std::max<size_t>(1, km.size());
+  cudaError_t e = cudaMalloc(&P->op_kind_mesh, n * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&P->op_mesh_lo, n * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&P->op_begin, n * sizeof(int64_t));
+  if (e == cudaSuccess) e = cudaMalloc(&P->op_end, n * sizeof(int64_t));
+  if (e == cudaSuccess && !km.empty())
+    e = cudaMemcpy(P->op_kind_mesh, km.data(), km.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !km.empty())
+    e = cudaMemcpy(P->op_mesh_lo, lo.data(), lo.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !km.empty())
+    e = cudaMemcpy(P->op_begin, ub.data(), ub.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !km.empty())
+    e = cudaMemcpy(P->op_end, ue.data(), ue.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(P->op_begin);
+    cudaFree(P->op_end);
+    cudaFree(P->op_kind_mesh);
+    cudaFree(P->op_mesh_lo);
+    P->op_begin = P->op_end = nullptr;
+    P->op_kind_mesh = P->op_mesh_lo = nullptr;
+    return fem::check_cuda(e, "batch one-pass queue");
+  }
+  P->op_nunits = (int64_t)km.size();
+  P->op_lists = &V;
+  return 0;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -302,6 +569,8 @@ int fem_batch_plan_build(const int64_t* cell_offsets, const int64_t* row_offsets
   FemBatchPlan* P = new FemBatchPlan();
   P->nmeshes = nmeshes;
   P->nunits = (int64_t)km.size();
+  P->cell_off.assign(cell_offsets, cell_offsets + nmeshes + 1);
+  P->row_off.assign(row_offsets, row_offsets + nmeshes + 1);
   P->cells_per_unit = cpu;
   P->rows_per_unit = rows_per_unit;
   const size_t nu1 = std::max<size_t>(1, km.size());
@@ -335,6 +604,10 @@ void fem_batch_plan_destroy(FemBatchPlan* P) {
   cudaFree(P->unit_begin);
   cudaFree(P->unit_end);
   cudaFree(P->cell_units);
+  cudaFree(P->op_begin);
+  cudaFree(P->op_end);
+  cudaFree(P->op_kind_mesh);
+  cudaFree(P->op_mesh_lo);
   delete P;
 }
 
@@ -343,7 +616,7 @@ int fem_batch_plan_info(const FemBatchPlan* P, int64_t* nunits, int64_t* ncounte
     fem::set_error(FEM_ERR_ARGUMENT, "null plan");
     return FEM_ERR_ARGUMENT;
   }
-  if (nunits) *nunits = P->nunits;
+  if (nunits) *nunits = P->op_lists ? P->op_nunits : P->nunits;
   if (ncounters) *ncounters = 1 + (int64_t)P->nmeshes;
   return 0;
 }
@@ -384,9 +657,49 @@ int fem_batched_assemble_vjp(const FemMesh* mesh, const FemBasis* basis, const F
   cudaStream_t st = (cudaStream_t)stream;
   FEM_TRY_CUDA(cudaMemsetAsync(counters, 0, (1 + (size_t)plan->nmeshes) * sizeof(int32_t), st));
   if (plan->nunits == 0) return 0;
+  const uint8_t* ref = fem::pattern_coef_bits(pat);
+  // scalar TriP2 / TetP2 with the pattern's node-block lists: the one-pass
+  // form, unless the family's tuning selects the two-pass path
+  const fem::VecUpper* V = fem::pattern_node_lists(pat);
+  if (V && V->dim == 1 && V->sdim == mesh->dim &&
+      (basis->family == FEM_TRI_P2 || basis->family == FEM_TET_P2) &&
+      fem::tuning_for(basis->family).onepass >= 1) {
+    if (mesh->nelems * (int64_t)(V->sdim == 3 ? 11 : 7) >
+        mesh->nelems * (int64_t)P.nbfun_u * P.nbfun_v) {
+      fem::set_error(FEM_ERR_CAPACITY, "staging too small for the pair values");
+      return FEM_ERR_CAPACITY;
+    }
+    rc = build_onepass_queue(const_cast<FemBatchPlan*>(plan), *V);
+    if (rc) return rc;
+    fem_batched::NodeArgs na{V->U.slice_len, V->U.slice_base, V->U.codes, V->vpos, V->vposT,
+                             V->vmask, static_cast<const fem::VecTerm*>(V->terms), V->count,
+                             V->mm, V->ns * V->ns};
+    const bool mass = form->mass.field || form->mass.scale != 0.0;
+    auto launch1 = [&](auto kern) -> int {
+      int per_sm = 0;
+      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern,
+                                                                    fem_batched::kBlock, 0);
+      if (e != cudaSuccess) return fem::check_cuda(e, "batched kernel occupancy");
+      const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(
+          (int64_t)std::max(1, per_sm) * fem::num_sms(), plan->op_nunits));
+      kern<<<(unsigned)grid, fem_batched::kBlock, 0, st>>>(
+          *mesh, *basis, *form, geo, na, plan->op_kind_mesh, plan->op_mesh_lo, plan->op_begin,
+          plan->op_end, plan->op_nunits, plan->cell_units, counters, ref, staging, csr_values,
+          w, u, dcoef_diff, dcoef_mass, status);
+      return 0;
+    };
+    if (mesh->dim == 3)
+      rc = mass ? launch1(fem_batched::batched_onepass_vjp_kernel<3, true>)
+                : launch1(fem_batched::batched_onepass_vjp_kernel<3, false>);
+    else
+      rc = mass ? launch1(fem_batched::batched_onepass_vjp_kernel<2, true>)
+                : launch1(fem_batched::batched_onepass_vjp_kernel<2, false>);
+    if (rc) return rc;
+    FEM_LAUNCH_CHECK("batched_onepass_vjp_kernel");
+    return 0;
+  }
   fem_batched::SumArgs sa{P.inc_ptr, P.inc, P.slot, P.indptr, P.nbfun_u,
                           std::max(1, P.max_row_nnz)};
-  const uint8_t* ref = fem::pattern_coef_bits(pat);
   const int tU = fem::tuning_for(basis->family).sum_unroll >= 8 ? 8 : 4;
   auto launch = [&](auto kern, int L, int G) -> int {
     const int rpw = 32 / G;

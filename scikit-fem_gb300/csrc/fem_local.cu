@@ -539,7 +539,9 @@ template <int D, int BS>
 __global__ void __launch_bounds__(BS) vector_pair_blocks_kernel(FemMesh m, FemBilinear f,
                                                                 double* __restrict__ out,
                                                                 const int32_t* __restrict__ cells,
-                                                                int64_t ebeg, int64_t eend) {
+                                                                int64_t ebeg, int64_t eend,
+                                                                const uint8_t* __restrict__ ref_bits,
+                                                                int32_t* __restrict__ status) {
   constexpr int NV = D + 1;
   constexpr int NP = NV * (NV + 1) / 2;
   constexpr int R = NP * D * D + 1;
@@ -548,9 +550,11 @@ __global__ void __launch_bounds__(BS) vector_pair_blocks_kernel(FemMesh m, FemBi
   int64_t* cid = cells ? reinterpret_cast<int64_t*>(smem + (size_t)BS * (R + 1)) : nullptr;
   const int64_t e0 = ebeg + (int64_t)blockIdx.x * BS;
   const int64_t pos = e0 + threadIdx.x;
+  int32_t flags = 0;
   if (pos < eend) {
     const int64_t e = cell_at(cells, pos);
     if (cid) cid[threadIdx.x] = e;
+    const int rb = ref_byte(ref_bits, e);
     Simplex<D> s;
     simplex_geometry<D>(m, e, s);
     simplex_c0<D>(s);
@@ -601,8 +605,10 @@ __global__ void __launch_bounds__(BS) vector_pair_blocks_kernel(FemMesh m, FemBi
         ++k;
       }
     row[NP * D * D] = coef_at(f.mass, e) * (adet / FACT);
+    if (status) flags = coef_status(f, e, rb);
   }
   flush_rows<R, BS>(smem, out, e0, eend, cid);
+  fem::publish_status(status, flags);
 }
 
 // ------------------------------------- simplex, scalar P2 (one-pass sum)
@@ -617,16 +623,20 @@ __global__ void __launch_bounds__(BS) scalar_pair_kernel(FemMesh m, FemBilinear 
                                                          const double* __restrict__ geo,
                                                          double* __restrict__ out,
                                                          const int32_t* __restrict__ cells,
-                                                         int64_t ebeg, int64_t eend) {
+                                                         int64_t ebeg, int64_t eend,
+                                                         const uint8_t* __restrict__ ref_bits,
+                                                         int32_t* __restrict__ status) {
   constexpr int NP = kGramCount<D>;
   constexpr int R = NP + 1;
   extern __shared__ double smem[];
   int64_t* cid = cells ? reinterpret_cast<int64_t*>(smem + (size_t)BS * (R + 1)) : nullptr;
   const int64_t e0 = ebeg + (int64_t)blockIdx.x * BS;
   const int64_t pos = e0 + threadIdx.x;
+  int32_t flags = 0;
   if (pos < eend) {
     const int64_t e = cell_at(cells, pos);
     if (cid) cid[threadIdx.x] = e;
+    const int rb = ref_byte(ref_bits, e);
     double* row = smem + threadIdx.x * (R + 1);
     const double sd = coef_at(f.diff, e);
     double adet;
@@ -645,8 +655,10 @@ __global__ void __launch_bounds__(BS) scalar_pair_kernel(FemMesh m, FemBilinear 
         for (int b = a; b <= D; ++b) row[k++] = sd * (gram[a][b] * s);
     }
     row[NP] = coef_at(f.mass, e) * (adet * kInvFact<D>);
+    if (status) flags = coef_status(f, e, rb);
   }
   flush_rows<R, BS>(smem, out, e0, eend, cid);
+  fem::publish_status(status, flags);
 }
 
 // ----------------------------------------------------------- hexahedron Q1
@@ -1179,7 +1191,8 @@ int coef_checks(const FemBilinear& f, const uint8_t* ref_bits, int32_t* status, 
 }
 
 int vector_pair_blocks(const FemMesh& m, const FemBasis& b, const FemBilinear& f, double* out,
-                       cudaStream_t st, int64_t ebeg, int64_t eend, const int32_t* cells) {
+                       cudaStream_t st, int64_t ebeg, int64_t eend, const int32_t* cells,
+                       const uint8_t* ref_bits, int32_t* status) {
   if (eend < 0) eend = m.nelems;
   if (eend <= ebeg) return 0;
   constexpr int BS = 64;
@@ -1192,10 +1205,12 @@ int vector_pair_blocks(const FemMesh& m, const FemBasis& b, const FemBilinear& f
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
       if (e != cudaSuccess) return fem::check_cuda(e, "vector_pair_blocks smem");
     }
-    vector_pair_blocks_kernel<3, BS><<<grid, BS, sm, st>>>(m, f, out, cells, ebeg, eend);
+    vector_pair_blocks_kernel<3, BS><<<grid, BS, sm, st>>>(m, f, out, cells, ebeg, eend,
+                                                           ref_bits, status);
   } else if (m.dim == 2) {
     const size_t sm = (size_t)BS * (6 * 4 + 2) * sizeof(double) + cid;
-    vector_pair_blocks_kernel<2, BS><<<grid, BS, sm, st>>>(m, f, out, cells, ebeg, eend);
+    vector_pair_blocks_kernel<2, BS><<<grid, BS, sm, st>>>(m, f, out, cells, ebeg, eend,
+                                                           ref_bits, status);
   } else {
     fem::set_error(FEM_ERR_UNSUPPORTED, "vector pair blocks of a %d-D mesh", m.dim);
     return FEM_ERR_UNSUPPORTED;
@@ -1207,7 +1222,8 @@ int vector_pair_blocks(const FemMesh& m, const FemBasis& b, const FemBilinear& f
 
 int scalar_pair_values(const FemMesh& m, const FemBasis& b, const FemBilinear& f,
                        const double* geo, double* out, cudaStream_t st, int64_t ebeg,
-                       int64_t eend, const int32_t* cells) {
+                       int64_t eend, const int32_t* cells, const uint8_t* ref_bits,
+                       int32_t* status) {
   if (eend < 0) eend = m.nelems;
   if (eend <= ebeg) return 0;
   if (b.vector || (b.family != FEM_TRI_P2 && b.family != FEM_TET_P2) ||
@@ -1220,10 +1236,12 @@ int scalar_pair_values(const FemMesh& m, const FemBasis& b, const FemBilinear& f
   const size_t cid = cells ? kCidBytes<BS> : 0;
   if (m.dim == 3) {
     const size_t sm = (size_t)BS * (kGramCount<3> + 2) * sizeof(double) + cid;
-    scalar_pair_kernel<3, BS><<<grid, BS, sm, st>>>(m, f, geo, out, cells, ebeg, eend);
+    scalar_pair_kernel<3, BS><<<grid, BS, sm, st>>>(m, f, geo, out, cells, ebeg, eend,
+                                                    ref_bits, status);
   } else {
     const size_t sm = (size_t)BS * (kGramCount<2> + 2) * sizeof(double) + cid;
-    scalar_pair_kernel<2, BS><<<grid, BS, sm, st>>>(m, f, geo, out, cells, ebeg, eend);
+    scalar_pair_kernel<2, BS><<<grid, BS, sm, st>>>(m, f, geo, out, cells, ebeg, eend,
+                                                    ref_bits, status);
   }
   FEM_LAUNCH_CHECK("scalar_pair_kernel");
   return 0;

@@ -27,6 +27,7 @@
 // one-pass sum's; they come from the upper lists of the node-level pattern.
 
 #include "fem_common.cuh"
+#include "fem_nodesum.cuh"
 #include "fem_tables.cuh"
 
 #include <cub/device/device_radix_sort.cuh>
@@ -37,16 +38,6 @@
 namespace fem {
 
 namespace {
-
-constexpr int kMaxTerms = 4;
-// vmask bit of a node block off the diagonal (its transpose is written too)
-constexpr unsigned kOffDiagBit = 1u << 15;
-
-struct VecTerm {
-  int32_t k;    // pair index of (min(p,q), max(p,q)) in row-major upper order
-  int32_t tr;   // 1: the term reads E_qp transposed (p > q)
-  double c;
-};
 
 int pair_index(int nv, int p, int q) { return p * nv - p * (p - 1) / 2 + (q - p); }
 
@@ -320,9 +311,9 @@ __global__ void __launch_bounds__(128) vec_upper_kernel(
   constexpr int DD = D * D;
   constexpr int NP = (S + 1) * (S + 2) / 2;
   constexpr int R = NP * DD + 1;
-  __shared__ VecTerm terms[100 * kMaxTerms];
-  __shared__ int32_t count[100];
-  __shared__ double mm[100];
+  __shared__ VecTerm terms[kMaxNodePairs * kMaxTerms];
+  __shared__ int32_t count[kMaxNodePairs];
+  __shared__ double mm[kMaxNodePairs];
   const int npairs = ns * ns;
   for (int k = threadIdx.x; k < npairs * kMaxTerms; k += blockDim.x) terms[k] = terms_g[k];
   for (int k = threadIdx.x; k < npairs; k += blockDim.x) {
@@ -341,6 +332,11 @@ __global__ void __launch_bounds__(128) vec_upper_kernel(
     const bool inr = u >= ua && u < ub;
     const int len = inr ? slice_len[sl] : 0;
     const uint32_t* cp = codes + (int64_t)slice_base[sl] * 32 + lane;
+    if constexpr (D == 1 && !FLAT) {
+      scalar_entry_sum<S, MASS, false>(inr, u, len, cp, nelems, npairs, terms, count, mm, vpos,
+                                       vposT, vmask, E, vals);
+      continue;
+    }
     double acc[DD];
 #pragma unroll
     for (int q = 0; q < DD; ++q) acc[q] = 0.0;
@@ -412,23 +408,7 @@ __global__ void __launch_bounds__(128) vec_upper_kernel(
       }
     }
     while (!(D == 1 && FLAT) && __any_sync(0xffffffffu, live)) {
-      if (D == 1 && live) {
-        // one number per term: a contribution's terms (at most kMaxTerms,
-        // predicated) and its mass in one step -- the per-step overhead
-        // would otherwise outweigh the single FMA of a term
-#pragma unroll
-        for (int u = 0; u < kMaxTerms; ++u)
-          if (u < nt) {
-            const VecTerm tm = terms[ij * kMaxTerms + u];
-            acc[0] = __fma_rn(tm.c, __ldg(Eb + tm.k), acc[0]);
-          }
-        if (MASS && valid) acc[0] = __fma_rn(__ldg(Eb + NP), mm[ij], acc[0]);
-        ++p;
-        cur = nxt;
-        nxt = p + 1 < len ? __ldg(cp + (int64_t)(p + 1) * 32) : 0xFFFFFFFFu;
-        live = cur != 0xFFFFFFFFu;
-        if (live) decode();
-      } else if (live) {
+      if (live) {
         if (t < nt) {
           const VecTerm tm = terms[ij * kMaxTerms + t];
           const double* Ep = Eb + tm.k * DD;
@@ -505,9 +485,9 @@ __global__ void __launch_bounds__(128) vec_upper_coop_kernel(
   constexpr int BPW = 32 / DD;   // node blocks per warp
   constexpr int NP = (D + 1) * (D + 2) / 2;
   constexpr int R = NP * DD + 1;
-  __shared__ VecTerm terms[100 * kMaxTerms];
-  __shared__ int32_t count[100];
-  __shared__ double mm[100];
+  __shared__ VecTerm terms[kMaxNodePairs * kMaxTerms];
+  __shared__ int32_t count[kMaxNodePairs];
+  __shared__ double mm[kMaxNodePairs];
   const int npairs = ns * ns;
   for (int k = threadIdx.x; k < npairs * kMaxTerms; k += blockDim.x) terms[k] = terms_g[k];
   for (int k = threadIdx.x; k < npairs; k += blockDim.x) {

@@ -26,7 +26,9 @@ CANDIDATES = {
 # functions also have the two-columns-per-lane kernel
 COLS = {"TetP1": (1, 2), "TriP2": (1, 2), "TetP2": (1, 2)}
 # the one-pass P1 sum's forms (two lanes per row / a lane per upper entry /
-# the same with TMA-staged list codes)
+# the same with TMA-staged list codes), which give the same bits; the scalar
+# P2 families keep the one-pass node-block sum (its two-pass alternative adds
+# in another grouping: a tuning never changes the values)
 ONEPASS = {"TriP1": (0, 1, 2), "TetP1": (0, 1, 2)}
 
 

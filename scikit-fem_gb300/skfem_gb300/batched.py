@@ -181,8 +181,17 @@ class GraphedAssembly:
         self.plan = _Plan(h.value)
         nu, nc = ctypes.c_int64(), ctypes.c_int64()
         N.check(N.lib().fem_batch_plan_info(self.plan.handle, ctypes.byref(nu), ctypes.byref(nc)))
-        self.nunits = nu.value
         self.counters = torch.zeros(nc.value, dtype=torch.int32, device=b.device)
+
+    @property
+    def nunits(self):
+        """Work units of the queue the persistent launch runs (the one-pass
+        queue of scalar P2 bases once it has run), or None without a plan."""
+        if self.plan is None:
+            return None
+        nu, nc = ctypes.c_int64(), ctypes.c_int64()
+        N.check(N.lib().fem_batch_plan_info(self.plan.handle, ctypes.byref(nu), ctypes.byref(nc)))
+        return nu.value
 
     def _launch(self):
         lib = N.lib()

@@ -95,10 +95,13 @@ def k_laplace_c_mass(u, v, w):
                                       (F.ElementTetP1, 3), (F.ElementTetP2, 3)])
 def test_persistent_launch_equals_separate_kernels(elem, dim):
     """One persistent work-queue launch (cell units, then row units waiting
-    on their mesh's cells) gives the split entry points' CSR values (bit for
-    bit but TetP2) and the separate adjoint kernel's gradients within 1e-13; graph replay equals the
-    eager launch bit for bit; meshes of very uneven size, and repeated
-    replays with new coefficients, keep the status word clear."""
+    on their mesh's cells) gives the CSR values of fem_assemble's path for the
+    family -- TriP1 / TetP1: the split entry points' (bit for bit), TriP2 /
+    TetP2: the one-pass node-block sum's (bit for bit; its row-block units
+    wait on every mesh their rows belong to) -- and the separate adjoint
+    kernel's gradients within 1e-13; graph replay equals the eager launch bit
+    for bit; meshes of very uneven size, and repeated replays with new
+    coefficients, keep the status word clear."""
     rng = np.random.default_rng(12)
     if dim == 2:
         meshes, _ = make_batch([1, 17, 3, 40, 2, 9], seed=7)
@@ -123,7 +126,7 @@ def test_persistent_launch_equals_separate_kernels(elem, dim):
     torch.cuda.synchronize()
     per.check()
     sep.check()
-    ref = _two_pass(per)
+    ref = _reference(per, elem)
     _same(per.values, ref, elem)
     for name in ("k", "c"):
         scale = sep.dcoef[name].abs().max()
@@ -141,17 +144,67 @@ def test_persistent_launch_equals_separate_kernels(elem, dim):
     per.replay()
     torch.cuda.synchronize()
     per.check()
-    _same(per.values, _two_pass(per), elem)
+    _same(per.values, _reference(per, elem), elem)
+
+
+@pytest.mark.parametrize("elem,dim", [(F.ElementTriP2, 2), (F.ElementTetP2, 3)])
+def test_persistent_two_pass_form_for_p2(elem, dim):
+    """With the family's one-pass sums off (fem_set_onepass 0) the
+    persistent launch runs its two-pass form for P2 too: local matrices in
+    the cell units, the staging sum in the row units -- the split entry
+    points' values (bit for bit for TriP2, within 1e-14 of max|K| for TetP2,
+    whose longer tensor sums the compiler may contract differently)."""
+    from skfem_gb300 import _native as N
+    rng = np.random.default_rng(21)
+    if dim == 2:
+        meshes, _ = make_batch([5, 12, 3], seed=8)
+    else:
+        meshes = [F.MeshTet.init_tensor(*(np.linspace(0, 1, n + 1),) * 3) for n in (3, 2, 4)]
+    bb = BatchedBasis(meshes, elem())
+    k = torch.tensor(rng.lognormal(0, 0.5, bb.nelems), device="cuda")
+    c = torch.tensor(rng.uniform(0.5, 2.0, bb.nelems), device="cuda")
+    w = torch.tensor(rng.standard_normal(bb.N), device="cuda")
+    u = torch.tensor(rng.standard_normal(bb.N), device="cuda")
+    fam = N.FAMILY["TriP2" if dim == 2 else "TetP2"]
+    lib = N.lib()
+    try:
+        lib.fem_set_onepass(fam, 0)
+        per = GraphedAssembly(k_laplace_c_mass, bb, {"k": k, "c": c}, w=w, u=u)
+        per.run_eager()
+        torch.cuda.synchronize()
+        per.check()
+        ref = _two_pass(per)
+    finally:
+        lib.fem_set_onepass(fam, 1)
+    if elem is F.ElementTetP2:
+        assert (per.values - ref).abs().max() <= 1e-14 * ref.abs().max()
+    else:
+        assert torch.equal(per.values, ref)
 
 
 def _same(a, b, elem):
-    """Bitwise for TriP1 / TriP2 / TetP1; TetP2's longer tensor sums may be
-    contracted differently by the compiler in the two kernels: within 1e-14
-    of max|K|."""
-    if elem is F.ElementTetP2:
-        assert (a - b).abs().max() <= 1e-14 * b.abs().max()
-    else:
-        assert torch.equal(a, b)
+    """Bitwise (the one-pass forms of TriP2 / TetP2 add the same terms in
+    the same order in both kernels)."""
+    assert torch.equal(a, b)
+
+
+def _reference(ga, elem):
+    if elem in (F.ElementTriP2, F.ElementTetP2):
+        return _one_pass(ga)
+    return _two_pass(ga)
+
+
+def _one_pass(ga):
+    """The CSR values of fem_assemble (the one-pass node-block sum for
+    scalar P2 bases)."""
+    from skfem_gb300 import _native as N
+    b, e = ga.basis, ga.entry
+    out = torch.full_like(ga.values, float("nan"))
+    staging = torch.empty_like(e.staging)
+    N.check(N.lib().fem_assemble(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(ga.c_form),
+                                 e.pat.handle, N.ptr(staging), N.ptr(out), None, N.stream_ptr()))
+    torch.cuda.synchronize()
+    return out
 
 
 def _two_pass(ga):

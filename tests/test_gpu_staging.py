@@ -157,14 +157,18 @@ def test_one_pass_sums_equal_staging_sum(cls, dim, n, elem, form, path):
     del coeffs, ch
 
 
-def test_fused_checks_report_stale_and_varying():
-    """The coefficient checks of the fused path: a coefficient that became
-    exactly zero on some cells sets FEM_ERR_STALE_PATTERN, a per-point
-    coefficient that varies inside a cell sets FEM_ERR_VARYING, and a
-    constant per-point row (with +0.0 / -0.0 taken as equal) sets neither --
-    the same bits as the local kernel's checks without the cache."""
-    m = F.MeshTet.init_tensor(*(np.linspace(0, 1, 9),) * 3)
-    b = F.Basis(m, F.ElementTetP1())
+@pytest.mark.parametrize("elem,n", [(F.ElementTetP1, 9), (F.ElementTetP2, 5)],
+                         ids=["TetP1", "TetP2"])
+def test_fused_checks_report_stale_and_varying(elem, n):
+    """The coefficient checks of the fused path and of the one-pass sums
+    (TetP1: folded into the sum; TetP2: in the pair-value kernel): a
+    coefficient that became exactly zero on some cells sets
+    FEM_ERR_STALE_PATTERN, a per-point coefficient that varies inside a cell
+    sets FEM_ERR_VARYING, and a constant per-point row (with +0.0 / -0.0
+    taken as equal) sets neither -- the same bits as the local kernel's
+    checks without the cache."""
+    m = F.MeshTet.init_tensor(*(np.linspace(0, 1, n),) * 3)
+    b = F.Basis(m, elem())
     rng = np.random.default_rng(7)
     k = rng.lognormal(0, 1, b.nelems)
     k_lap_mass.assemble_torch(b, k=torch.from_numpy(k).cuda())

@@ -120,3 +120,38 @@ def test_vector_onepass_device_and_host_coefficients_agree():
                                     mu=torch.tensor(mu, device="cuda"),
                                     rho=torch.tensor(rho, device="cuda"))
     np.testing.assert_array_equal(T.values().cpu().numpy(), Kh.data)
+
+
+def test_vector_onepass_coefficient_checks():
+    # the pair-block kernel runs the coefficient checks: a density that
+    # became exactly zero on some cells sets FEM_ERR_STALE_PATTERN, a
+    # per-point density varying inside a cell FEM_ERR_VARYING
+    m = _mesh("tet", 4, 10)
+    b = F.Basis(m, F.ElementVector(F.ElementTetP2()))
+    rng = np.random.default_rng(11)
+    lam, mu, rho = (rng.lognormal(0.0, 0.5, m.nelements) for _ in range(3))
+    dev = {k: torch.tensor(v, device="cuda") for k, v in (("lam", lam), ("mu", mu), ("rho", rho))}
+    elastic_mass.assemble_torch(b, **dev)
+    entry = next(e for key, e in b._patterns.items() if key[0] == "bilinear")
+    nq = b.zero_w().shape[1]
+    rho_zero = rho.copy()
+    rho_zero[[2, 50, 300]] = 0.0
+    rho_vary = np.repeat(rho[:, None], nq, axis=1)
+    rho_vary[7, 1] *= 1.5
+    lib = N.lib()
+    vals = torch.empty(entry.nnz, dtype=torch.float64, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    for rd, want in ((torch.tensor(rho_zero, device="cuda"), 1 << N.FEM_ERR_STALE_PATTERN),
+                     (torch.tensor(rho_vary, device="cuda"), 1 << N.FEM_ERR_VARYING),
+                     (dev["rho"], 0)):
+        r1 = rd[:, 0].contiguous() if rd.dim() > 1 else rd
+        coeffs, ch, c_form = elastic_mass._setup(b, None, {**dev, "rho": r1})
+        if rd.dim() > 1:
+            c_form.mass = N.FemCoef(c_form.mass.scale, rd.data_ptr(), rd.shape[1])
+        status.zero_()
+        N.check(lib.fem_assemble(N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form),
+                                 entry.pat.handle, N.ptr(entry.staging), N.ptr(vals),
+                                 N.ptr(status), N.stream_ptr()))
+        torch.cuda.synchronize()
+        assert int(status.item()) == want
+        del coeffs, ch

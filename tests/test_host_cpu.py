@@ -152,9 +152,9 @@ def test_complement_dofs():
 def test_autotune_candidates_per_family():
     """The autotuner times every block size, grid and unroll; the scalar
     bases with an even number of local functions (TetP1, TriP2, TetP2) also
-    try two columns per lane in the fused sum, the P1 simplex families both
-    forms of the one-pass sum, the others and every vector basis one of
-    each."""
+    try two columns per lane in the fused sum, the P1 simplex families the
+    three forms of the one-pass sum (bitwise equal), the others and every
+    vector basis one of each."""
     from skfem_gb300 import autotune
     base = 3 * 2 * 3
     for fam in ("TriP2", "TetP2"):
