@@ -94,3 +94,15 @@ def test_tuning_is_validated_on_the_host():
         assert lib.fem_set_tuning(*bad) == N.FEM_ERR_ARGUMENT
     assert lib.fem_set_tuning(fam, 128, 0, 8, 2) == 0
     assert lib.fem_set_tuning(fam, 128, 0, 8, 1) == 0
+
+
+def test_onepass_variant_is_validated_on_the_host():
+    """fem_set_onepass takes variants 0-2 for families 1-5 and refuses the
+    rest; no CUDA call."""
+    from skfem_gb300 import _build, _native as N
+    lib = ctypes.CDLL(_build.build())
+    fam = N.FAMILY["TetP1"]
+    for bad in ((fam, -1), (fam, 3), (0, 1), (6, 1)):
+        assert lib.fem_set_onepass(*bad) == N.FEM_ERR_ARGUMENT
+    for v in (0, 2, 1):
+        assert lib.fem_set_onepass(fam, v) == 0
