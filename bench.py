@@ -554,8 +554,8 @@ def _abi_step(F, N, form, b, coefs):
 def secondary_workloads(args, only=None):
     """The other workloads of the assembly path, each timed on the device.
     ``only`` restricts the run to one of tri_p1 / tet_p2 / tet_p2_vec /
-    hex1_vjp / batched / generic (sizes from --p2-n, --vec-n, --hex-n, --batch,
-    --generic-n)."""
+    hex1_vjp / batched / generic / condense (sizes from --p2-n, --vec-n,
+    --hex-n, --batch, --generic-n, --nodes)."""
     want = (lambda name: only is None or only == name)
     import torch
 
@@ -882,6 +882,81 @@ def secondary_workloads(args, only=None):
             out[key]["speedup_vs_cpu_oracle"] = (out[key]["elements_per_s_batched"] /
                                                  c["cells_per_s"])
 
+    if want("condense"):
+        # Dirichlet condensation on the device (skfem.utils.condense,
+        # utils.py:462-600): A_II = A[I][:, I] and b_I = b[I] - A[I][:, D] x[D]
+        # of the TetP1 k*Laplace+mass system on the --nodes cube, D its
+        # boundary nodes; beside it the reference's own scipy slicing of the
+        # same system on the host (one run)
+        import scipy.sparse as sp
+        from skfem_gb300.utils import condense
+        n = args.nodes
+        m = F.MeshTet.init_tensor(*(np.linspace(0, 1, n),) * 3)
+        bs = F.Basis(m, F.ElementTetP1())
+        kd = torch.from_numpy(rng.lognormal(0.0, 1.0, m.nelements)).cuda()
+        form = k_laplace_mass_form()
+        K = form.assemble_torch(bs, k=kd)
+        bv = unit_load.assemble_torch(bs)
+        D = bs.get_dofs().flatten()
+        I = np.setdiff1d(np.arange(bs.N), D)
+        xv = torch.from_numpy(rng.standard_normal(bs.N)).cuda()
+        ms_call = _time(lambda: condense(K, bv, x=xv, D=D), 3, warm=1)
+        # the two C-ABI calls alone (map of kept DOFs prebuilt; the pattern
+        # call reads back the condensed nnz, one synchronisation)
+        mp = np.full(bs.N, -1, dtype=np.int32)
+        mp[I] = np.arange(len(I), dtype=np.int32)
+        mp_d = torch.from_numpy(mp).cuda()
+        crow = K.crow_indices().to(torch.int32).contiguous()
+        col = K.col_indices().to(torch.int32).contiguous()
+        val = K.values().contiguous()
+        oi = torch.empty(len(I) + 1, dtype=torch.int32, device="cuda")
+        nnz_c = N.ctypes.c_int64()
+        N.check(lib.fem_condense_pattern(N.ptr(crow), N.ptr(col), bs.N, N.ptr(mp_d), len(I),
+                                         N.ptr(oi), N.ctypes.byref(nnz_c), N.stream_ptr()))
+        oj = torch.empty(max(nnz_c.value, 1), dtype=torch.int32, device="cuda")
+        ov = torch.empty(max(nnz_c.value, 1), dtype=torch.float64, device="cuda")
+        ob = torch.empty(len(I), dtype=torch.float64, device="cuda")
+
+        def pattern():
+            N.check(lib.fem_condense_pattern(N.ptr(crow), N.ptr(col), bs.N, N.ptr(mp_d),
+                                             len(I), N.ptr(oi), N.ctypes.byref(nnz_c),
+                                             N.stream_ptr()))
+
+        def values():
+            N.check(lib.fem_condense_values(N.ptr(crow), N.ptr(col), N.ptr(val), bs.N,
+                                            N.ptr(mp_d), N.ptr(bv), N.ptr(xv), N.ptr(oi),
+                                            N.ptr(oj), N.ptr(ov), N.ptr(ob), N.stream_ptr()))
+        ms_pat = _time(pattern, reps)
+        ms_val = _time(values, reps)
+        # the same on the host with the reference's slicing, checked against
+        # the device result
+        Kh = sp.csr_matrix((val.cpu().numpy(), col.cpu().numpy(), crow.cpu().numpy()),
+                           shape=(bs.N, bs.N))
+        bh, xh = bv.cpu().numpy(), xv.cpu().numpy()
+        t0 = time.perf_counter()
+        KII = Kh[I][:, I]
+        bI = bh[I] - Kh[I][:, D] @ xh[D]
+        s_host = time.perf_counter() - t0
+        KII.sort_indices()
+        AII, bII = condense(K, bv, x=xv, D=D, expand=False)
+        same = (np.array_equal(AII.crow_indices().cpu().numpy(), KII.indptr)
+                and np.array_equal(AII.col_indices().cpu().numpy(), KII.indices)
+                and np.array_equal(AII.values().cpu().numpy(), KII.data))
+        b_rel = float(np.abs(bII.cpu().numpy() - bI).max() / np.abs(bI).max())
+        # bytes: the CSR read (indptr, indices, values) and the condensed CSR
+        # and load vector written
+        Bc = (bs.N + 1) * 4 + K.values().numel() * 12 + bs.N * 16 + \
+            (len(I) + 1) * 4 + nnz_c.value * 12 + len(I) * 8
+        out["condense_tet_p1_%d" % n] = {
+            "nrows": int(bs.N), "nnz": int(K.values().numel()), "kept": int(len(I)),
+            "nnz_condensed": int(nnz_c.value), "ms_call": ms_call, "ms_pattern": ms_pat,
+            "ms_values": ms_val, "gbs_values": Bc / (ms_val * 1e-3) / 1e9,
+            "hbm_frac_values": Bc / (ms_val * 1e-3) / 1e9 / hbm,
+            "s_host_scipy": s_host, "matches_scipy_bitwise": bool(same),
+            "rhs_max_rel_diff": b_rel,
+            "step": "condense(K, b, x, D=boundary) on the device CSR; host: the reference's "
+                    "A[I][:, I] and b[I] - A[I][:, D] @ x[D] with scipy, one run"}
+
     if want("generic"):
         # generic per-point kernels: a Newton-step matrix with an
         # interpolated DOF vector (exact reference arithmetic, -fmad=false),
@@ -1036,7 +1111,7 @@ def main():
                     help="cells per axis, generic-kernel TetP1 workload")
     ap.add_argument("--only", default=None,
                     choices=["tri_p1", "tet_p2", "tet_p2_vec", "hex1_vjp", "batched",
-                             "generic"],
+                             "generic", "condense"],
                     help="run one secondary workload alone and print its record")
     ap.add_argument("--onepass", type=int, default=None, choices=[0, 1, 2],
                     help="fix the one-pass sum's form after autotuning (default: the fastest)")

@@ -25,6 +25,14 @@ def _dofs(S, n, device):
     return np.unique(S.astype(np.int64))
 
 
+def _complement(n, S):
+    """The sorted DOFs of range(n) not in S: np.setdiff1d(np.arange(n), S)
+    (utils.py:_init_bc) by a mask, O(n) instead of a sort of both arrays."""
+    keep = np.ones(n, dtype=bool)
+    keep[S] = False
+    return np.nonzero(keep)[0]
+
+
 def condense(A, b=None, x=None, I=None, D=None, expand=True):
     """Eliminate DOFs: returns (A_II, b_I[, x, I]) with
     A_II = A[I][:, I] and b_I = b[I] - A[I][:, D] x[D] (utils.py:578-598).
@@ -43,7 +51,7 @@ def condense(A, b=None, x=None, I=None, D=None, expand=True):
     if In is not None and Dn is not None:
         raise Exception("Give only I or only D!")
     if In is None:
-        In = np.setdiff1d(np.arange(n), Dn)
+        In = _complement(n, Dn)
     mp = np.full(n, -1, dtype=np.int32)
     mp[In] = np.arange(len(In), dtype=np.int32)
     mp_d = torch.from_numpy(mp).to(dev)
@@ -95,7 +103,7 @@ def _bc_sets(n, I, D):
     if In is not None and Dn is not None:
         raise Exception("Give only I or only D!")
     if Dn is None:
-        Dn = np.setdiff1d(np.arange(n), In)
+        Dn = _complement(n, In)
     return Dn
 
 

@@ -190,3 +190,19 @@ def test_coodata_host_side_matches_reference_layout():
     assert B.shape == A.shape
     idx, data, shape = A.astuple()
     assert idx is A.indices and data is A.data and shape == A.shape
+
+
+def test_condense_complement_matches_setdiff1d():
+    """The kept DOFs of condense / enforce (the complement of the given set)
+    equal np.setdiff1d(np.arange(n), D), as the reference computes them
+    (utils.py _init_bc), on empty, partial and full sets."""
+    from skfem_gb300.utils import _complement, _dofs
+    rng = np.random.default_rng(1)
+    for n in (0, 1, 5, 100, 10007):
+        for k in sorted({0, 1, 3, n // 2, n}):
+            if k > n:
+                continue
+            D = _dofs(rng.choice(n, k, replace=False) if n else np.array([], dtype=np.int64),
+                      n, None)
+            got, ref = _complement(n, D), np.setdiff1d(np.arange(n), D)
+            assert np.array_equal(got, ref) and got.dtype == ref.dtype
