@@ -288,8 +288,12 @@ struct NodeArgs {
   int npairs;
 };
 
+// Triangles: at most 64 registers (60, no spills) for eight resident blocks
+// per SM -- the kernel waits on its gathers (about 23 long-scoreboard
+// stalls per issue), so more warps per SM pay (9.73 -> 9.28 ms on 512
+// TriP2 meshes); tetrahedra keep their registers (a bound spills).
 template <int D, bool MASS>
-__global__ void __launch_bounds__(kBlock) batched_onepass_vjp_kernel(
+__global__ void __launch_bounds__(kBlock, D == 2 ? 8 : 1) batched_onepass_vjp_kernel(
     FemMesh m, FemBasis b, FemBilinear f, const double* __restrict__ geo, NodeArgs na,
     const int32_t* __restrict__ kind_mesh, const int32_t* __restrict__ mesh_lo,
     const int64_t* __restrict__ ubeg, const int64_t* __restrict__ uend, int64_t nunits,
