@@ -673,17 +673,22 @@ def secondary_workloads(args, only=None):
         step, entry, c_form, vals = _abi_step(F, N, k_laplace_mass, b, {"k": kd})
         torch.cuda.synchronize()
         build_s = time.perf_counter() - t0
-        ms = _time(step, 5)
-        first = vals.clone()
-        step()
-        torch.cuda.synchronize()
-        same = bool(torch.equal(first, vals))
         fam = N.FAMILY["TetP2"]
+        from skfem_gb300 import autotune
         try:
-            # the sum's flattened form (one FMA per step), bitwise the same values
-            lib.fem_set_onepass(fam, 2)
-            ms_flat = _time(step, 5)
-            flat_same = bool(torch.equal(first, vals))
+            # launch shape and the one-pass sum's form (per contribution / one
+            # FMA per step: the same bits) by the autotuner
+            tuned, _ = autotune.tune(k_laplace_mass, b, {"k": kd}, reps=3, use_cache=False)
+            ms = _time(step, 5)
+            first = vals.clone()
+            step()
+            torch.cuda.synchronize()
+            same = bool(torch.equal(first, vals))
+            form_ms = {}
+            for v in (1, 2):
+                lib.fem_set_onepass(fam, v)
+                form_ms[v] = _time(step, 5)
+                same = same and bool(torch.equal(first, vals))
             # the two-pass path: local matrices into the staging, then the
             # fixed-order segmented sum
             lib.fem_set_onepass(fam, 0)
@@ -693,15 +698,18 @@ def secondary_workloads(args, only=None):
                 N.byref(b.c_mesh), N.byref(b.c_basis), N.byref(c_form), entry.pat.handle,
                 N.ptr(entry.staging), None, 0, b.nelems, N.stream_ptr())), 3)
         finally:
-            lib.fem_set_onepass(fam, 1)
+            # the library's default tuning for the later workloads of the family
+            autotune.apply(fam, {"local_block": 128, "persistent": 0, "sum_unroll": 8,
+                                 "sum_cols": 1, "onepass": 1})
         B = m.nelements * (10 * 4 + 8) + m.p.size * 8 + entry.nnz * 8
         out["tet_p2_k_laplace_mass_%d" % args.p2_n] = {
             "nelems": m.nelements, "ndofs": b.N, "nnz": entry.nnz, "ms": ms,
             "step": "one-pass node-block sum: per cell the 10 scaled Gram entries times k and "
                     "the mass scale, then one lane per CSR entry on and above the diagonal "
                     "contracting the reference tensor while it sums (no local matrices stored)",
-            "repeat_bitwise_equal": same,
-            "ms_onepass_flat": ms_flat, "flat_bitwise_equal": flat_same,
+            "autotuned": tuned,
+            "forms_and_repeats_bitwise_equal": same,
+            "ms_onepass_per_contribution": form_ms[1], "ms_onepass_flat": form_ms[2],
             "ms_two_pass": ms_two, "ms_two_pass_local": ms_local,
             "two_pass_vs_onepass_max_rel": dev,
             "pattern_build_s": build_s, "elements_per_s": m.nelements / (ms * 1e-3),

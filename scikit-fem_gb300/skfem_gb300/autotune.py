@@ -26,17 +26,19 @@ CANDIDATES = {
 # functions also have the two-columns-per-lane kernel
 COLS = {"TetP1": (1, 2), "TriP2": (1, 2), "TetP2": (1, 2)}
 # the one-pass P1 sum's forms (two lanes per row / a lane per upper entry /
-# the same with TMA-staged list codes), which give the same bits; the scalar
-# P2 families keep the one-pass node-block sum (its two-pass alternative adds
-# in another grouping: a tuning never changes the values)
-ONEPASS = {"TriP1": (0, 1, 2), "TetP1": (0, 1, 2)}
+# the same with TMA-staged list codes), which give the same bits; for the
+# scalar P2 families the one-pass node-block sum's two forms (per
+# contribution / one FMA per step), also bitwise equal -- their two-pass
+# alternative adds in another grouping and is never tried: a tuning never
+# changes the values
+ONEPASS = {"TriP1": (0, 1, 2), "TetP1": (0, 1, 2), "TriP2": (1, 2), "TetP2": (1, 2)}
 
 
 def candidates(family, vector=False):
     """Every configuration the autotuner times for a basis of this family:
     the product of CANDIDATES, times the columns per lane of the fused sum
     where the family has the two-columns kernel, times the one-pass sum's
-    forms for the P1 simplex families (scalar bases only)."""
+    forms for the simplex families (scalar bases only)."""
     cols = (1,) if vector else COLS.get(family, (1,))
     onep = (1,) if vector else ONEPASS.get(family, (1,))
     return [{"local_block": lb, "persistent": pers, "sum_unroll": un, "sum_cols": nc,

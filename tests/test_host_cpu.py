@@ -153,15 +153,17 @@ def test_autotune_candidates_per_family():
     """The autotuner times every block size, grid and unroll; the scalar
     bases with an even number of local functions (TetP1, TriP2, TetP2) also
     try two columns per lane in the fused sum, the P1 simplex families the
-    three forms of the one-pass sum (bitwise equal), the others and every
-    vector basis one of each."""
+    three forms of the one-pass sum and the scalar P2 families the two
+    forms of the one-pass node-block sum (bitwise equal), the others and
+    every vector basis one of each."""
     from skfem_gb300 import autotune
     base = 3 * 2 * 3
     for fam in ("TriP2", "TetP2"):
         c = autotune.candidates(fam)
-        assert len(c) == 2 * base and {x["sum_cols"] for x in c} == {1, 2}
-        assert {x["onepass"] for x in c} == {1}
-        assert len(autotune.candidates(fam, vector=True)) == base
+        assert len(c) == 4 * base and {x["sum_cols"] for x in c} == {1, 2}
+        assert {x["onepass"] for x in c} == {1, 2}
+        v = autotune.candidates(fam, vector=True)
+        assert len(v) == base and {x["onepass"] for x in v} == {1}
     c = autotune.candidates("TetP1")
     assert len(c) == 6 * base and {x["sum_cols"] for x in c} == {1, 2}
     assert {x["onepass"] for x in c} == {0, 1, 2}
