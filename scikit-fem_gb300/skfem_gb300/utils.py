@@ -33,30 +33,63 @@ def _complement(n, S):
     return np.nonzero(keep)[0]
 
 
+def _device_dofs(S, n, device):
+    """A DOF set (index array, list, bool mask or tensor) as a sorted,
+    duplicate-free int64 tensor on the device; indices outside [0, n) raise
+    IndexError here, before any device indexing uses them."""
+    if S is None:
+        return None
+    if not isinstance(S, torch.Tensor):
+        S = torch.from_numpy(np.ascontiguousarray(np.asarray(S)))
+    S = S.to(device)
+    if S.dtype == torch.bool:
+        if S.numel() != n:
+            raise IndexError("boolean DOF mask of length %d for %d DOFs" % (S.numel(), n))
+        return torch.nonzero(S).squeeze(1)
+    S = torch.unique(S.to(torch.int64))          # sorted
+    if S.numel() and (int(S[0]) < 0 or int(S[-1]) >= n):
+        raise IndexError("DOF index out of range for %d DOFs" % n)
+    return S
+
+
+def _kept_map(n, I, D, device):
+    """(In, map): the kept DOFs In (sorted, device int64) and the int32 map
+    DOF -> its index in In (-1 for eliminated DOFs), built on the device."""
+    Dn, In = _device_dofs(D, n, device), _device_dofs(I, n, device)
+    if In is None and Dn is None:
+        raise Exception("Either I or D must be given!")
+    if In is not None and Dn is not None:
+        raise Exception("Give only I or only D!")
+    if In is None:
+        keep = torch.ones(n, dtype=torch.bool, device=device)
+        keep[Dn] = False
+        In = torch.nonzero(keep).squeeze(1)
+    mp = torch.full((n,), -1, dtype=torch.int32, device=device)
+    mp[In] = torch.arange(In.numel(), dtype=torch.int32, device=device)
+    return In, mp
+
+
 def condense(A, b=None, x=None, I=None, D=None, expand=True):
     """Eliminate DOFs: returns (A_II, b_I[, x, I]) with
     A_II = A[I][:, I] and b_I = b[I] - A[I][:, D] x[D] (utils.py:578-598).
 
     ``A`` is a torch sparse CSR tensor on the GPU (``assemble_torch``);
     ``b`` and ``x`` are torch vectors (``b`` may also be a sparse mass matrix
-    for generalized eigenproblems: then ``B[I][:, I]`` is returned).
+    for generalized eigenproblems: then ``B[I][:, I]`` is returned); with
+    ``x`` given and no ``b``, ``b`` is zero (utils.py:319-322).  ``I`` / ``D``
+    are index arrays, boolean masks, tensors or DofsViews; the sets are
+    formed on the device, and an index outside the matrix raises IndexError.
     """
     if not (isinstance(A, torch.Tensor) and A.layout == torch.sparse_csr):
         raise TypeError("condense on the GPU takes the torch CSR of assemble_torch")
     n = A.shape[0]
     dev = A.device
-    Dn, In = _dofs(D, n, dev), _dofs(I, n, dev)
-    if In is None and Dn is None:
-        raise Exception("Either I or D must be given!")
-    if In is not None and Dn is not None:
-        raise Exception("Give only I or only D!")
-    if In is None:
-        In = _complement(n, Dn)
-    mp = np.full(n, -1, dtype=np.int32)
-    mp[In] = np.arange(len(In), dtype=np.int32)
-    mp_d = torch.from_numpy(mp).to(dev)
+    In, mp_d = _kept_map(n, I, D, dev)
+    nk = In.numel()
     if x is None:
         x = torch.zeros(n, dtype=torch.float64, device=dev)
+    elif b is None:
+        b = torch.zeros(n, dtype=torch.float64, device=dev)
     x = torch.as_tensor(x, dtype=torch.float64, device=dev).contiguous()
 
     def sub(M, rhs=None):
@@ -64,22 +97,22 @@ def condense(A, b=None, x=None, I=None, D=None, expand=True):
         col = M.col_indices().to(torch.int32).contiguous()
         val = M.values().contiguous()
         lib = N.lib()
-        out_ptr = torch.empty(len(In) + 1, dtype=torch.int32, device=dev)
+        out_ptr = torch.empty(nk + 1, dtype=torch.int32, device=dev)
         nnz = N.ctypes.c_int64()
         s = N.stream_ptr()
-        N.check(lib.fem_condense_pattern(N.ptr(crow), N.ptr(col), n, N.ptr(mp_d), len(In),
+        N.check(lib.fem_condense_pattern(N.ptr(crow), N.ptr(col), n, N.ptr(mp_d), nk,
                                          N.ptr(out_ptr), N.ctypes.byref(nnz), s))
         out_ind = torch.empty(max(nnz.value, 1), dtype=torch.int32, device=dev)[:nnz.value]
         out_val = torch.empty(max(nnz.value, 1), dtype=torch.float64, device=dev)[:nnz.value]
-        out_b = torch.empty(len(In), dtype=torch.float64, device=dev) if rhs is not False else None
+        out_b = torch.empty(nk, dtype=torch.float64, device=dev) if rhs is not False else None
         bb = rhs if isinstance(rhs, torch.Tensor) else None
         N.check(lib.fem_condense_values(N.ptr(crow), N.ptr(col), N.ptr(val), n, N.ptr(mp_d),
                                         N.ptr(bb), N.ptr(x), N.ptr(out_ptr), N.ptr(out_ind),
                                         N.ptr(out_val), N.ptr(out_b), s))
-        Mc = torch.sparse_csr_tensor(out_ptr, out_ind, out_val, size=(len(In), len(In)))
+        Mc = torch.sparse_csr_tensor(out_ptr, out_ind, out_val, size=(nk, nk))
         return Mc, out_b
 
-    I_t = torch.from_numpy(In).to(dev)
+    I_t = In
     if b is None:
         AII, _ = sub(A, rhs=False)
         ret = (AII,)

@@ -336,6 +336,27 @@ def test_condense_on_device_matches_reference_semantics():
     np.testing.assert_array_equal(I.cpu().numpy(), Iref)
     # only A: the reference returns the matrix alone when b is None and expand=False
     assert isinstance(condense(A, D=D, expand=False), torch.Tensor)
+    # the same sets given as I, as a boolean mask, as a device tensor, with
+    # duplicates: the same condensed system
+    mask = np.zeros(b.N, dtype=bool)
+    mask[D] = True
+    for kw in ({"I": Iref}, {"D": mask}, {"D": torch.as_tensor(D, device="cuda")},
+               {"D": np.concatenate([D, D[:5]])}):
+        A2, b2, _, I2 = condense(A, rhs, x=x, **kw)
+        np.testing.assert_array_equal(A2.values().cpu().numpy(), Aref.data)
+        np.testing.assert_array_equal(b2.cpu().numpy(), bI.cpu().numpy())
+        np.testing.assert_array_equal(I2.cpu().numpy(), Iref)
+    # x without b: b is zero, as the reference's _init_bc makes it
+    A3, b3 = condense(A, x=x, D=D, expand=False)
+    b3ref = -(Ks[Iref][:, D] @ x.cpu().numpy()[D])
+    np.testing.assert_allclose(b3.cpu().numpy(), b3ref, rtol=1e-13,
+                               atol=1e-13 * np.abs(b3ref).max())
+    # indices outside the matrix are refused on the host side
+    for bad in (np.array([0, b.N]), np.array([-1, 3])):
+        with pytest.raises(IndexError):
+            condense(A, rhs, D=bad)
+    with pytest.raises(Exception, match="Give only I or only D"):
+        condense(A, rhs, I=Iref, D=D)
 
 
 def test_host_coefficients_checked_in_kernel():

@@ -45,7 +45,7 @@ def test_host_pipeline_equals_device_path(kind, shuffle):
     Kd = k_lap_mass.assemble_torch(b, k=torch.from_numpy(k).cuda())
     old = FM.UPLOAD_CHUNKS
     try:
-        for chunks in (1, 3, 8):
+        for chunks in (1, 3, 8, 16):
             FM.UPLOAD_CHUNKS = chunks
             Kh = k_lap_mass.assemble(b, k=b.zero_w() + k[:, None])
             np.testing.assert_array_equal(Kh.indptr, Kd.crow_indices().cpu().numpy())
