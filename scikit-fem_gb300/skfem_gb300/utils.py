@@ -14,25 +14,6 @@ from . import _native as N
 __all__ = ["condense", "enforce"]
 
 
-def _dofs(S, n, device):
-    if S is None:
-        return None
-    if isinstance(S, torch.Tensor):
-        S = S.detach().cpu().numpy()
-    S = np.asarray(S)
-    if S.dtype == bool:
-        S = np.nonzero(S)[0]
-    return np.unique(S.astype(np.int64))
-
-
-def _complement(n, S):
-    """The sorted DOFs of range(n) not in S: np.setdiff1d(np.arange(n), S)
-    (utils.py:_init_bc) by a mask, O(n) instead of a sort of both arrays."""
-    keep = np.ones(n, dtype=bool)
-    keep[S] = False
-    return np.nonzero(keep)[0]
-
-
 def _device_dofs(S, n, device):
     """A DOF set (index array, list, bool mask or tensor) as a sorted,
     duplicate-free int64 tensor on the device; indices outside [0, n) raise
@@ -129,14 +110,17 @@ def condense(A, b=None, x=None, I=None, D=None, expand=True):
     return ret if len(ret) > 1 else ret[0]
 
 
-def _bc_sets(n, I, D):
-    Dn, In = _dofs(D, n, None), _dofs(I, n, None)
+def _bc_sets(n, I, D, device):
+    """The constrained DOFs (sorted, device int64) of enforce's I / D."""
+    Dn, In = _device_dofs(D, n, device), _device_dofs(I, n, device)
     if In is None and Dn is None:
         raise Exception("Either I or D must be given!")
     if In is not None and Dn is not None:
         raise Exception("Give only I or only D!")
     if Dn is None:
-        Dn = _complement(n, In)
+        rest = torch.ones(n, dtype=torch.bool, device=device)
+        rest[In] = False
+        Dn = torch.nonzero(rest).squeeze(1)
     return Dn
 
 
@@ -167,8 +151,8 @@ def enforce(A, b=None, x=None, I=None, D=None, diag=1., overwrite=False):
         raise TypeError("enforce on the GPU takes the torch CSR of assemble_torch")
     n = A.shape[0]
     dev = A.device
-    Dn = _bc_sets(n, I, D)
-    rows = torch.from_numpy(Dn.astype(np.int32)).to(dev)
+    Dn = _bc_sets(n, I, D, dev)
+    rows = Dn.to(torch.int32)
     if x is not None:
         x = torch.as_tensor(x, dtype=torch.float64, device=dev).contiguous()
         if b is None:
@@ -178,9 +162,9 @@ def enforce(A, b=None, x=None, I=None, D=None, diag=1., overwrite=False):
     if b is not None and not sparse_b:
         bt = torch.as_tensor(b, dtype=torch.float64, device=dev)
         bout = bt if (overwrite and bt.is_contiguous()) else bt.clone().contiguous()
-    Aout = _rows_to_identity(A, rows, len(Dn), diag, bout, x, overwrite)
+    Aout = _rows_to_identity(A, rows, rows.numel(), diag, bout, x, overwrite)
     if b is None:
         return Aout
     if sparse_b:
-        return Aout, _rows_to_identity(b, rows, len(Dn), 0.0, None, None, overwrite)
+        return Aout, _rows_to_identity(b, rows, rows.numel(), 0.0, None, None, overwrite)
     return Aout, bout

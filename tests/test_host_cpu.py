@@ -194,17 +194,29 @@ def test_coodata_host_side_matches_reference_layout():
     assert idx is A.indices and data is A.data and shape == A.shape
 
 
-def test_condense_complement_matches_setdiff1d():
-    """The kept DOFs of condense / enforce (the complement of the given set)
-    equal np.setdiff1d(np.arange(n), D), as the reference computes them
-    (utils.py _init_bc), on empty, partial and full sets."""
-    from skfem_gb300.utils import _complement, _dofs
+def test_condense_dof_sets_match_setdiff1d():
+    """The kept DOFs and their map that condense forms on the device (here
+    with CPU tensors) equal the reference's np.setdiff1d(np.arange(n), D)
+    (utils.py _init_bc), for empty, partial and full sets given as D, as I,
+    as boolean masks and with duplicates; indices outside [0, n) raise."""
+    import torch
+    from skfem_gb300.utils import _bc_sets, _kept_map
     rng = np.random.default_rng(1)
-    for n in (0, 1, 5, 100, 10007):
+    for n in (1, 5, 100, 10007):
         for k in sorted({0, 1, 3, n // 2, n}):
             if k > n:
                 continue
-            D = _dofs(rng.choice(n, k, replace=False) if n else np.array([], dtype=np.int64),
-                      n, None)
-            got, ref = _complement(n, D), np.setdiff1d(np.arange(n), D)
-            assert np.array_equal(got, ref) and got.dtype == ref.dtype
+            D = rng.choice(n, k, replace=False)
+            ref = np.setdiff1d(np.arange(n), D)
+            mask = np.zeros(n, dtype=bool)
+            mask[D] = True
+            for kw in ({"D": D}, {"D": np.concatenate([D, D[:2]])}, {"D": mask}, {"I": ref}):
+                In, mp = _kept_map(n, kw.get("I"), kw.get("D"), "cpu")
+                assert np.array_equal(In.numpy(), ref)
+                want = np.full(n, -1)
+                want[ref] = np.arange(len(ref))
+                assert np.array_equal(mp.numpy(), want) and mp.dtype == torch.int32
+            assert np.array_equal(_bc_sets(n, ref, None, "cpu").numpy(), np.unique(D))
+    for bad in ([0, 5], [-1]):
+        with pytest.raises(IndexError):
+            _kept_map(5, None, np.array(bad), "cpu")
