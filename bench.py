@@ -49,7 +49,7 @@ UNIT = "elements/s"
 # variant: 0 row form, 1 upper-gather form, 2 upper form with TMA-staged codes);
 # the upper-gather form's is from one launch at the full 101^3 size (6M cells,
 # upper entries in blocks of 4,096 rows: 1.06 GB read + 147.7 MB written).
-ONEPASS_B_PER_CELL = {0: 159.7, 1: 201.3, 2: 185.6}
+ONEPASS_B_PER_CELL = {0: 159.7, 1: 185.6, 2: 185.6}
 ONEPASS_B_SOURCE = {0: "one launch at 1.3M cells", 1: "one launch at 6M cells (this workload)",
                     2: "one launch at 1.3M cells"}
 ONEPASS_KERNEL = {0: "csr_geometry_p1_kernel<4,U,0> (one-pass P1 sum, row form)",

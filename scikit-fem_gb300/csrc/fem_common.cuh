@@ -87,6 +87,27 @@ struct AsyncScratch {
   }
 };
 
+inline int num_sms();
+// Blocks of a grid-stride kernel: enough for work_blocks, at most one wave
+// of resident blocks (kern's occupancy at this block size and dynamic
+// shared memory), so that every block runs from the start and no partial
+// last wave idles the SMs.  Used by the one-pass P1 sums, whose slices
+// carry about equal work (6M TetP1 cells: 0.338 ms in one wave against
+// 0.369 ms in 3.5 waves of a 32-blocks-per-SM grid); the node-block sums,
+// whose slices differ in work, keep an oversubscribed grid that the block
+// scheduler balances (one wave measured slower there).
+template <typename K>
+inline int resident_grid(K kern, int threads, size_t smem, int64_t work_blocks) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) !=
+          cudaSuccess ||
+      per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  return (int)std::max<int64_t>(1, std::min<int64_t>(work_blocks, (int64_t)per_sm * num_sms()));
+}
+
 inline int num_sms() {
   static int n = 0;
   if (n == 0) {

@@ -1617,8 +1617,6 @@ int csr_sum_geometry_p1(const Pattern& P, int dim, const double* geo, const FemC
   const int threads = 32 * warps;
   const size_t smem = warps * per_warp;
   const int64_t rows_per_block = (int64_t)warps * rpw;
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(row1 - row0, rows_per_block),
-                                                              (int64_t)num_sms() * 64));
   const double* kf = diff.field;
   const int64_t ks = diff.stride > 1 ? diff.stride : 1;
   const double* mf = mass.field;
@@ -1629,6 +1627,7 @@ int csr_sum_geometry_p1(const Pattern& P, int dim, const double* geo, const FemC
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return check_cuda(e, "csr_geometry_p1 smem");
     }
+    const int grid = resident_grid(kern, threads, smem, ceil_div(row1 - row0, rows_per_block));
     kern<<<grid, threads, smem, st>>>(P.inc_ptr, P.inc, P.slot, P.indptr, geo, P.nelems, kf, ks,
                                       diff.scale, mf, ms, mass.scale, moff, mbase, row0, row1,
                                       stride, vals);
@@ -1820,12 +1819,12 @@ int csr_sum_upper_p1(const Pattern& P, const UpperLists& U, int dim, const doubl
     const int64_t ua = ranges[k][0], ub = ranges[k][1];
     if (ub <= ua) continue;
     const int64_t nsl = ((ub + 31) >> 5) - (ua >> 5);
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nsl, threads / 32),
-                                                                (int64_t)num_sms() * 32));
+    const int64_t work = ceil_div(nsl, threads / 32);
     // the staged form: two buffers of the longest slice per warp + 2 mbarriers
     const size_t tma_smem = (size_t)(threads / 32) * (2 * (size_t)U.max_len * 128 + 16);
     const bool staged = tma && status && U.max_len > 0 && tma_smem <= 96 * 1024;
     auto launch = [&](auto kern) {
+      const int grid = resident_grid(kern, threads, 0, work);
       kern<<<grid, threads, 0, st>>>(ua, ub, U.slice_len, U.slice_base, U.codes, U.pos, U.tpos,
                                      U.row, geo, P.nelems, kf, ks, diff.scale, mf, ms, mass.scale,
                                      moff, mbase, vals, ref_bits, const_bits, status);
@@ -1837,6 +1836,7 @@ int csr_sum_upper_p1(const Pattern& P, const UpperLists& U, int dim, const doubl
                                              (int)tma_smem);
         if (e != cudaSuccess) return check_cuda(e, "csr_upper_p1_tma smem");
       }
+      const int grid = resident_grid(kern, threads, tma_smem, work);
       kern<<<grid, threads, tma_smem, st>>>(ua, ub, U.slice_len, U.slice_base, U.codes,
                                             U.max_len, U.pos, U.tpos, U.row, geo, P.nelems, kf, ks,
                                             diff.scale, mf, ms, mass.scale, moff, mbase, vals,
