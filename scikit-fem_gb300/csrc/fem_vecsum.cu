@@ -299,7 +299,12 @@ __global__ void vec_block_pos_kernel(const int32_t* __restrict__ perm,
 // the next step's operand loaded before this one's FMA (the same FMAs in the
 // same order, bitwise the same values; as fast once the lanes of a slice
 // carry the same terms per contribution, at 37 against 32 registers).
-template <int S, int D, bool MASS, bool FLAT = false>
+// DYN: one wave of resident blocks whose warps take their slices in order
+// from a ticket (*ticket, zero at launch) instead of a fixed grid stride:
+// the slices in flight stay a narrow band of node rows (their cells' pair
+// values shared in L2), and a warp with a long slice does not hold up the
+// others.  Each slice's sums are the same whichever warp runs it.
+template <int S, int D, bool MASS, bool FLAT = false, bool DYN = false>
 __global__ void __launch_bounds__(128) vec_upper_kernel(
     int64_t ua, int64_t ub, int64_t nupper, int64_t nd, int64_t nelems, int ns,
     const int32_t* __restrict__ slice_len,
@@ -307,7 +312,8 @@ __global__ void __launch_bounds__(128) vec_upper_kernel(
     const int32_t* __restrict__ vpos, const int32_t* __restrict__ vposT,
     const uint16_t* __restrict__ vmask, const VecTerm* __restrict__ terms_g,
     const int32_t* __restrict__ count_g, const double* __restrict__ mm_g,
-    const double* __restrict__ E, double* __restrict__ vals) {
+    const double* __restrict__ E, double* __restrict__ vals,
+    int32_t* __restrict__ ticket = nullptr) {
   constexpr int DD = D * D;
   constexpr int NP = (S + 1) * (S + 2) / 2;
   constexpr int R = NP * DD + 1;
@@ -324,8 +330,19 @@ __global__ void __launch_bounds__(128) vec_upper_kernel(
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   const int64_t s1 = (ub + 31) >> 5;
-  for (int64_t sl = (ua >> 5) + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-       sl < s1; sl += warps) {
+  // the warp's next slice (warp-uniform)
+  auto next_slice = [&](int64_t cur) -> int64_t {
+    if constexpr (DYN) {
+      int t = 0;
+      if (lane == 0) t = atomicAdd(ticket, 1);
+      return (ua >> 5) + __shfl_sync(0xffffffffu, t, 0);
+    } else {
+      return cur + warps;
+    }
+  };
+  const int64_t first =
+      DYN ? next_slice(0) : (ua >> 5) + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  for (int64_t sl = first; sl < s1; sl = next_slice(sl)) {
     const int64_t u = sl * 32 + lane;
     // a lane whose block belongs to the neighbouring range takes part in
     // the warp's votes with an empty list and writes nothing
@@ -745,19 +762,44 @@ int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, c
     const int64_t nsl = ((ub + 31) >> 5) - (ua >> 5);
     // lane per block: a warp per slice of 32 blocks; cooperative: 32 / D^2 blocks per warp
     const int64_t nwarp = (coop && V.dim > 1) ? ceil_div(ub - ua, 32 / (V.dim * V.dim)) : nsl;
-    // (a grid of 32 blocks per SM, not one resident wave: the slices' work
-    // is uneven, and the block scheduler's dynamic order evens it out --
-    // one wave measured 1.68 against 1.62 ms on vector TetP2 elasticity)
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nwarp, threads / 32),
-                                                                (int64_t)num_sms() * 32));
-    auto launch = [&](auto kern) {
+    // (scalar bases and the cooperative form: a grid of 32 blocks per SM,
+    // the block scheduler evening out the slices' uneven work; vector bases,
+    // lane per block: one resident wave taking slices from a ticket --
+    // vector TetP2 elasticity on 384k cells 1.43 against 1.62 ms)
+    const int64_t work = ceil_div(nwarp, threads / 32);
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(work, (int64_t)num_sms() * 32));
+    auto launch_coop = [&](auto kern) {
       kern<<<grid, threads, 0, st>>>(ua, ub, V.U.nupper, V.U.nd, V.nelems, V.ns, V.U.slice_len,
                                      V.U.slice_base, V.U.codes, V.vpos, V.vposT, V.vmask,
                                      static_cast<const VecTerm*>(V.terms), V.count, V.mm, E, vals);
     };
+    auto launch = [&](auto kern) {
+      kern<<<grid, threads, 0, st>>>(ua, ub, V.U.nupper, V.U.nd, V.nelems, V.ns, V.U.slice_len,
+                                     V.U.slice_base, V.U.codes, V.vpos, V.vposT, V.vmask,
+                                     static_cast<const VecTerm*>(V.terms), V.count, V.mm, E, vals,
+                                     nullptr);
+    };
+    auto launch_dyn = [&](auto kern) -> int {
+      int32_t* ticket = nullptr;
+      FEM_TRY_CUDA(cudaMallocAsync(&ticket, sizeof(int32_t), st));
+      cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(int32_t), st);
+      if (e == cudaSuccess) {
+        const int g = resident_grid(kern, threads, 0, work);
+        kern<<<g, threads, 0, st>>>(ua, ub, V.U.nupper, V.U.nd, V.nelems, V.ns, V.U.slice_len,
+                                    V.U.slice_base, V.U.codes, V.vpos, V.vposT, V.vmask,
+                                    static_cast<const VecTerm*>(V.terms), V.count, V.mm, E, vals,
+                                    ticket);
+        e = cudaGetLastError();
+      }
+      cudaFreeAsync(ticket, st);
+      return e == cudaSuccess ? 0 : check_cuda(e, "vec_upper_kernel");
+    };
+    int rc = 0;
     if (V.dim == 1) {
       // scalar bases: one entry per node block
       // (coop: the flattened form, one FMA per step)
+      // (the fixed grid: a scalar entry's slice is too little work per
+      // ticket -- 7.8M slices of 512 TriP2 meshes serialised on one counter)
       if (V.sdim == 3) {
         if (coop) {
           if (mass) launch(vec_upper_kernel<3, 1, true, true>);
@@ -777,19 +819,20 @@ int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, c
       }
     } else if (coop) {
       if (V.dim == 3) {
-        if (mass) launch(vec_upper_coop_kernel<3, true>);
-        else launch(vec_upper_coop_kernel<3, false>);
+        if (mass) launch_coop(vec_upper_coop_kernel<3, true>);
+        else launch_coop(vec_upper_coop_kernel<3, false>);
       } else {
-        if (mass) launch(vec_upper_coop_kernel<2, true>);
-        else launch(vec_upper_coop_kernel<2, false>);
+        if (mass) launch_coop(vec_upper_coop_kernel<2, true>);
+        else launch_coop(vec_upper_coop_kernel<2, false>);
       }
     } else if (V.dim == 3) {
-      if (mass) launch(vec_upper_kernel<3, 3, true>);
-      else launch(vec_upper_kernel<3, 3, false>);
+      if (mass) rc = launch_dyn(vec_upper_kernel<3, 3, true, false, true>);
+      else rc = launch_dyn(vec_upper_kernel<3, 3, false, false, true>);
     } else {
-      if (mass) launch(vec_upper_kernel<2, 2, true>);
-      else launch(vec_upper_kernel<2, 2, false>);
+      if (mass) rc = launch_dyn(vec_upper_kernel<2, 2, true, false, true>);
+      else rc = launch_dyn(vec_upper_kernel<2, 2, false, false, true>);
     }
+    if (rc) return rc;
     FEM_LAUNCH_CHECK("vec_upper_kernel");
   }
   return 0;
