@@ -781,7 +781,12 @@ int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, c
     };
     auto launch_dyn = [&](auto kern) -> int {
       int32_t* ticket = nullptr;
-      FEM_TRY_CUDA(cudaMallocAsync(&ticket, sizeof(int32_t), st));
+      if (cudaMallocAsync(&ticket, sizeof(int32_t), st) != cudaSuccess) {
+        // no room for the ticket: the fixed grid (the same values)
+        cudaGetLastError();
+        launch(kern);
+        return 0;
+      }
       cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(int32_t), st);
       if (e == cudaSuccess) {
         const int g = resident_grid(kern, threads, 0, work);
