@@ -330,18 +330,19 @@ __global__ void __launch_bounds__(128) vec_upper_kernel(
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   const int64_t s1 = (ub + 31) >> 5;
-  // the warp's next slice (warp-uniform)
+  // the warp's next slice (warp-uniform); without a ticket the fixed
+  // grid stride
+  const bool dyn = DYN && ticket != nullptr;
   auto next_slice = [&](int64_t cur) -> int64_t {
-    if constexpr (DYN) {
+    if (dyn) {
       int t = 0;
       if (lane == 0) t = atomicAdd(ticket, 1);
       return (ua >> 5) + __shfl_sync(0xffffffffu, t, 0);
-    } else {
-      return cur + warps;
     }
+    return cur + warps;
   };
   const int64_t first =
-      DYN ? next_slice(0) : (ua >> 5) + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+      dyn ? next_slice(0) : (ua >> 5) + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   for (int64_t sl = first; sl < s1; sl = next_slice(sl)) {
     const int64_t u = sl * 32 + lane;
     // a lane whose block belongs to the neighbouring range takes part in
@@ -782,10 +783,12 @@ int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, c
     auto launch_dyn = [&](auto kern) -> int {
       int32_t* ticket = nullptr;
       if (cudaMallocAsync(&ticket, sizeof(int32_t), st) != cudaSuccess) {
-        // no room for the ticket: the fixed grid (the same values)
+        // no room for the ticket: the kernel on the fixed grid stride (a
+        // null ticket; the same values)
         cudaGetLastError();
         launch(kern);
-        return 0;
+        const cudaError_t le = cudaGetLastError();
+        return le == cudaSuccess ? 0 : check_cuda(le, "vec_upper_kernel");
       }
       cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(int32_t), st);
       if (e == cudaSuccess) {
