@@ -1,6 +1,8 @@
 // extern "C" entry points of libskfem_gb300 (declared in include/skfem_gb300.h).
 
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 
 #include "fem_common.cuh"
@@ -69,6 +71,29 @@ void set_error(int code, const char* fmt, ...) {
   vsnprintf(buf, sizeof(buf), fmt, ap);
   va_end(ap);
   g_err = std::string("[") + std::to_string(code) + "] " + buf;
+}
+
+int resident_blocks_per_sm(const void* kern, int threads, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::tuple<const void*, int, size_t, int>, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const auto key = std::make_tuple(kern, threads, smem, dev);
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) !=
+          cudaSuccess ||
+      per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  cache[key] = per_sm;
+  return per_sm;
 }
 
 int check_cuda(cudaError_t err, const char* what) {

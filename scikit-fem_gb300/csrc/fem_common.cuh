@@ -96,15 +96,12 @@ inline int num_sms();
 // 0.369 ms in 3.5 waves of a 32-blocks-per-SM grid); the node-block sums,
 // whose slices differ in work, keep an oversubscribed grid that the block
 // scheduler balances (one wave measured slower there).
+// The occupancy is looked up once per (kernel, block size, shared memory,
+// device) and cached.
+int resident_blocks_per_sm(const void* kern, int threads, size_t smem);
 template <typename K>
 inline int resident_grid(K kern, int threads, size_t smem, int64_t work_blocks) {
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) !=
-          cudaSuccess ||
-      per_sm < 1) {
-    cudaGetLastError();
-    per_sm = 1;
-  }
+  const int per_sm = resident_blocks_per_sm(reinterpret_cast<const void*>(kern), threads, smem);
   return (int)std::max<int64_t>(1, std::min<int64_t>(work_blocks, (int64_t)per_sm * num_sms()));
 }
 
@@ -324,7 +321,10 @@ inline int64_t vec_pair_stride(int sdim, int dim) {
 // DOF rows per window of the node blocks' work-sorted layout: row ranges of
 // vec_upper_sum start and end on multiples of it (or end at the last row)
 int64_t vec_window_rows(const VecUpper& V);
-// coop: the D*D lanes of a node block cooperate (vec_upper_coop_kernel)
+// coop: the D*D lanes of a node block cooperate (vec_upper_coop_kernel).
+// E: the caller's staging (nelems x nbfun^2 doubles) holding the pair values
+// in its first nelems x vec_pair_stride doubles; the 4 bytes after them are
+// written (the slices' ticket).
 int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, cudaStream_t st,
                   int64_t row0 = 0, int64_t row1 = -1, bool coop = false);
 

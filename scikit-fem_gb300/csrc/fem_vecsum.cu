@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(128) vec_upper_kernel(
     const uint16_t* __restrict__ vmask, const VecTerm* __restrict__ terms_g,
     const int32_t* __restrict__ count_g, const double* __restrict__ mm_g,
     const double* __restrict__ E, double* __restrict__ vals,
-    int32_t* __restrict__ ticket = nullptr) {
+    int32_t* __restrict__ ticket = nullptr, int chunk = 1) {
   constexpr int DD = D * D;
   constexpr int NP = (S + 1) * (S + 2) / 2;
   constexpr int R = NP * DD + 1;
@@ -332,17 +332,22 @@ __global__ void __launch_bounds__(128) vec_upper_kernel(
   const int64_t s1 = (ub + 31) >> 5;
   // the warp's next slice (warp-uniform); without a ticket the fixed
   // grid stride
+  // grid stride.  A ticket hands out `chunk` consecutive slices.
   const bool dyn = DYN && ticket != nullptr;
+  int64_t chunk_end = 0;
   auto next_slice = [&](int64_t cur) -> int64_t {
     if (dyn) {
+      if (cur + 1 < chunk_end) return cur + 1;
       int t = 0;
       if (lane == 0) t = atomicAdd(ticket, 1);
-      return (ua >> 5) + __shfl_sync(0xffffffffu, t, 0);
+      const int64_t b = (ua >> 5) + (int64_t)__shfl_sync(0xffffffffu, t, 0) * chunk;
+      chunk_end = b + chunk;
+      return b;
     }
     return cur + warps;
   };
   const int64_t first =
-      dyn ? next_slice(0) : (ua >> 5) + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+      dyn ? next_slice(-1) : (ua >> 5) + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   for (int64_t sl = first; sl < s1; sl = next_slice(sl)) {
     const int64_t u = sl * 32 + lane;
     // a lane whose block belongs to the neighbouring range takes part in
@@ -738,6 +743,12 @@ int build_vec_upper(const Pattern& P, const int32_t* udofs, int family, int dim,
 
 int64_t vec_window_rows(const VecUpper& V) { return V.block_rows * V.dim; }
 
+// Slices per ticket of the scalar (1 x 1 block) sums, and the resident
+// waves of work from which the node-block sums take their slices from a
+// ticket.
+constexpr int kScalarChunk = 4;
+constexpr int kTicketWaves = 8;
+
 int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, cudaStream_t st,
                   int64_t row0, int64_t row1, bool coop) {
   if (V.U.nupper == 0) return 0;
@@ -763,10 +774,11 @@ int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, c
     const int64_t nsl = ((ub + 31) >> 5) - (ua >> 5);
     // lane per block: a warp per slice of 32 blocks; cooperative: 32 / D^2 blocks per warp
     const int64_t nwarp = (coop && V.dim > 1) ? ceil_div(ub - ua, 32 / (V.dim * V.dim)) : nsl;
-    // (scalar bases and the cooperative form: a grid of 32 blocks per SM,
-    // the block scheduler evening out the slices' uneven work; vector bases,
-    // lane per block: one resident wave taking slices from a ticket --
-    // vector TetP2 elasticity on 384k cells 1.43 against 1.62 ms)
+    // (lane per block and the scalar forms: one resident wave taking slices
+    // from a ticket -- vector TetP2 elasticity on 384k cells 1.43 against
+    // 1.62 ms, scalar TetP2 on 1.3M cells 0.83 against 0.91 ms; the vector
+    // cooperative form: a grid of 32 blocks per SM, the block scheduler
+    // evening out the slices' uneven work)
     const int64_t work = ceil_div(nwarp, threads / 32);
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(work, (int64_t)num_sms() * 32));
     auto launch_coop = [&](auto kern) {
@@ -778,51 +790,58 @@ int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, c
       kern<<<grid, threads, 0, st>>>(ua, ub, V.U.nupper, V.U.nd, V.nelems, V.ns, V.U.slice_len,
                                      V.U.slice_base, V.U.codes, V.vpos, V.vposT, V.vmask,
                                      static_cast<const VecTerm*>(V.terms), V.count, V.mm, E, vals,
-                                     nullptr);
+                                     nullptr, 1);
     };
-    auto launch_dyn = [&](auto kern) -> int {
-      int32_t* ticket = nullptr;
-      if (cudaMallocAsync(&ticket, sizeof(int32_t), st) != cudaSuccess) {
-        // no room for the ticket: the kernel on the fixed grid stride (a
-        // null ticket; the same values)
-        cudaGetLastError();
+    // the slices' ticket: the word after the pair values in the caller's
+    // staging (nelems x nbfun^2 doubles, always longer than the pair values'
+    // nelems x vec_pair_stride), so concurrent calls with their own staging
+    // never share it and nothing is allocated
+    int32_t* ticket =
+        reinterpret_cast<int32_t*>(const_cast<double*>(E) + V.nelems * vec_pair_stride(V.sdim, V.dim));
+    // (the ticket pays where the slices' cells do not fit L2 at once; work
+    // of at most kTicketWaves resident waves -- a mesh of up to about 200k
+    // TriP2 cells -- keeps the oversubscribed grid, which the block
+    // scheduler balances: 512 per-mesh TriP2 launches 21.0 ms that way,
+    // 23.4 ms with the ticket from one wave up)
+    auto launch_dyn = [&](auto kern, int chunk) -> int {
+      const int g = resident_grid(kern, threads, 0, work);
+      if (work <= (int64_t)g * kTicketWaves) {
         launch(kern);
         const cudaError_t le = cudaGetLastError();
         return le == cudaSuccess ? 0 : check_cuda(le, "vec_upper_kernel");
       }
       cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(int32_t), st);
       if (e == cudaSuccess) {
-        const int g = resident_grid(kern, threads, 0, work);
         kern<<<g, threads, 0, st>>>(ua, ub, V.U.nupper, V.U.nd, V.nelems, V.ns, V.U.slice_len,
                                     V.U.slice_base, V.U.codes, V.vpos, V.vposT, V.vmask,
                                     static_cast<const VecTerm*>(V.terms), V.count, V.mm, E, vals,
-                                    ticket);
+                                    ticket, chunk);
         e = cudaGetLastError();
       }
-      cudaFreeAsync(ticket, st);
       return e == cudaSuccess ? 0 : check_cuda(e, "vec_upper_kernel");
     };
     int rc = 0;
     if (V.dim == 1) {
       // scalar bases: one entry per node block
       // (coop: the flattened form, one FMA per step)
-      // (the fixed grid: a scalar entry's slice is too little work per
-      // ticket -- 7.8M slices of 512 TriP2 meshes serialised on one counter)
+      // (four slices per ticket: a scalar entry's slice is little work, and
+      // one ticket per slice serialised the ~8M slices of 512 TriP2 meshes
+      // on the counter)
       if (V.sdim == 3) {
         if (coop) {
-          if (mass) launch(vec_upper_kernel<3, 1, true, true>);
-          else launch(vec_upper_kernel<3, 1, false, true>);
+          if (mass) rc = launch_dyn(vec_upper_kernel<3, 1, true, true, true>, kScalarChunk);
+          else rc = launch_dyn(vec_upper_kernel<3, 1, false, true, true>, kScalarChunk);
         } else {
-          if (mass) launch(vec_upper_kernel<3, 1, true>);
-          else launch(vec_upper_kernel<3, 1, false>);
+          if (mass) rc = launch_dyn(vec_upper_kernel<3, 1, true, false, true>, kScalarChunk);
+          else rc = launch_dyn(vec_upper_kernel<3, 1, false, false, true>, kScalarChunk);
         }
       } else {
         if (coop) {
-          if (mass) launch(vec_upper_kernel<2, 1, true, true>);
-          else launch(vec_upper_kernel<2, 1, false, true>);
+          if (mass) rc = launch_dyn(vec_upper_kernel<2, 1, true, true, true>, kScalarChunk);
+          else rc = launch_dyn(vec_upper_kernel<2, 1, false, true, true>, kScalarChunk);
         } else {
-          if (mass) launch(vec_upper_kernel<2, 1, true>);
-          else launch(vec_upper_kernel<2, 1, false>);
+          if (mass) rc = launch_dyn(vec_upper_kernel<2, 1, true, false, true>, kScalarChunk);
+          else rc = launch_dyn(vec_upper_kernel<2, 1, false, false, true>, kScalarChunk);
         }
       }
     } else if (coop) {
@@ -834,11 +853,11 @@ int vec_upper_sum(const VecUpper& V, const double* E, bool mass, double* vals, c
         else launch_coop(vec_upper_coop_kernel<2, false>);
       }
     } else if (V.dim == 3) {
-      if (mass) rc = launch_dyn(vec_upper_kernel<3, 3, true, false, true>);
-      else rc = launch_dyn(vec_upper_kernel<3, 3, false, false, true>);
+      if (mass) rc = launch_dyn(vec_upper_kernel<3, 3, true, false, true>, 1);
+      else rc = launch_dyn(vec_upper_kernel<3, 3, false, false, true>, 1);
     } else {
-      if (mass) rc = launch_dyn(vec_upper_kernel<2, 2, true, false, true>);
-      else rc = launch_dyn(vec_upper_kernel<2, 2, false, false, true>);
+      if (mass) rc = launch_dyn(vec_upper_kernel<2, 2, true, false, true>, 1);
+      else rc = launch_dyn(vec_upper_kernel<2, 2, false, false, true>, 1);
     }
     if (rc) return rc;
     FEM_LAUNCH_CHECK("vec_upper_kernel");
